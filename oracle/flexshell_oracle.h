@@ -1,0 +1,101 @@
+/*
+ * CPU oracle for the shell element-assembly hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * (FinEtoolsFlexStructures.jl 3.6.4) element loops and of the FinEtools
+ * assembler semantics.  It is the checker for the CUDA library and the timed
+ * CPU baseline; the product never links it.
+ *
+ * It follows the reference's own dense formulation (explicit 18x18 / 24x24
+ * transformation matrices and Q^T E Q congruences) so that it is an
+ * independent check of the structure-aware GPU kernels.
+ *
+ * Conventions (Julia's): xyz is nnodes x 3 column-major; dofnums nnodes x 6
+ * column-major, 1-based; conn is nelem x nen row-per-element, 1-based.
+ * Element matrices are column-major.
+ */
+#ifndef FLEXSHELL_ORACLE_H
+#define FLEXSHELL_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_T3FF = 0, ORC_T3FFCOMP = 1, ORC_Q4RS = 2, ORC_Q4RSCOMP = 3 };
+enum { ORC_KEEP_ZEROS = 0, ORC_DROP_ZEROS = 1, ORC_DIAG = 2 };
+
+/* Per-element constitutive data for the layered variants and the
+ * homogeneous material.  Group g owns A,B,D (3x3), H (2x2), csmat (3x3),
+ * thickness, mass and rotary-inertia densities, all column-major. */
+typedef struct {
+    int etype;
+    /* homogeneous material */
+    double Dps[9];
+    double Dt[4];
+    double rho;
+    /* per-element thickness (homogeneous) */
+    const double *thickness;     /* nelem */
+    /* layup groups (composite) */
+    int ngroups;
+    const int32_t *group;        /* nelem, 0-based group of each element */
+    const double *gA, *gB, *gD;  /* ngroups x 9 */
+    const double *gH;            /* ngroups x 4 */
+    const double *gcsmat;        /* ngroups x 9 */
+    const double *gthick;        /* ngroups */
+    const double *gmass;         /* ngroups: mass density per unit area */
+    const double *gmoi;          /* ngroups: rotary inertia density */
+    /* formulation knobs */
+    double stab_c;               /* stab_fun(t,h) = t^2/(t^2 + stab_c h^2) */
+    double drill_scale;
+    int tsf;                     /* T3: 0 = average B, 1 = average K */
+} orc_params;
+
+int orc_normals(int etype, int64_t nnodes, const double *xyz, int64_t nelem,
+                const int64_t *conn, const int64_t *order, double threshold_deg,
+                const orc_params *p, double *normals, uint8_t *valid);
+
+int orc_element_stiffness(const orc_params *p, int64_t e, const double *X,
+                          const double *nrm, const uint8_t *nvalid, double *Ke);
+
+int orc_element_mass(const orc_params *p, int64_t e, const double *X, double *tm,
+                     double *rm);
+
+/* Element loop + assembly.  `order` (may be NULL) is the sequence in which
+ * elements are assembled (layup-group order).  The result is kept in a
+ * handle and copied out with orc_result_copy (CSC == CSR arrays for a
+ * symmetric matrix; 1-based). */
+typedef struct orc_result orc_result;
+int orc_assemble(int what /*0 K, 1 M*/, int mode, int64_t nnodes, const double *xyz,
+                 int64_t nelem, const int64_t *conn, const int64_t *order,
+                 const int64_t *dofnums, int64_t n, const double *normals,
+                 const uint8_t *valid, const orc_params *p, int nthreads,
+                 orc_result **out);
+int64_t orc_result_nnz(const orc_result *r);
+int64_t orc_result_n(const orc_result *r);
+void orc_result_copy(const orc_result *r, int64_t *colptr, int64_t *rowval, double *nzval);
+void orc_result_free(orc_result *r);
+
+/* Dense element matrices for all elements (column-major ndof x ndof each). */
+int orc_all_element_stiffness(int64_t nnodes, const double *xyz, int64_t nelem,
+                              const int64_t *conn, const double *normals,
+                              const uint8_t *valid, const orc_params *p, int nthreads,
+                              double *Ke_all);
+
+/* Central-difference loop of the reference explicit examples (mass
+ * proportional damping, CSR stiffness, zero external force). */
+int orc_cd_steps(int64_t n, const int64_t *rowptr, const int64_t *colidx,
+                 const double *vals, const double *invMC, const double *C, double dt,
+                 int64_t nsteps, double *U, double *V, double *A, int nthreads);
+
+/* Laminate stiffness of a layup (CompositeLayupModule). */
+int orc_laminate(int nplies, const double *ply_Dps, const double *ply_Dts,
+                 const double *ply_t, const double *ply_angle_deg, const double *ply_rho,
+                 double offset, int shear_model /*0 VS, 1 constant*/, double tcf,
+                 double *A, double *B, double *D, double *H, double *mass_density,
+                 double *moi_density);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,120 @@
+"""Problem builders shared by the oracle pins and the GPU parity tests.
+
+Each builder restates the set-up of a reference test (mesh, material,
+boundary conditions) using the FinEtools-equivalent helpers of
+``flexshell.mesh``.
+"""
+import numpy as np
+
+from flexshell import mesh, materials
+
+PHI40 = 40 / 360 * 2 * np.pi
+
+
+def fv12(orientation="a", n=8):
+    """NAFEMS FV12 free plate, test/test_shell_dynamics.jl:27-66."""
+    E, nu, rho, t, L = 200e9, 0.3, 8000.0, 0.05, 10.0
+    xy, conn = mesh.T3block(L, L, n, n, orientation)
+    xy[:, 0] -= L / 2
+    xy[:, 1] -= L / 2
+    xyz = mesh.xyz3(xy)
+    mat = materials.MatDeforElastIso(E, nu, rho)
+    Dps, Dt = materials.shell_material_stiffness(mat)
+    dof, nfree = mesh.numberdofs(np.zeros((xyz.shape[0], 6), bool))
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=t,
+                material=dict(Dps=Dps, Dt=Dt, rho=rho), stab_c=0.2)
+
+
+# test/test_shell_dynamics.jl:113-128
+FV12_REF = [0.0, 0.0, 2.604869127850317e-7, 4.698288861559094e-6, 6.749716652051837e-6,
+            9.829373450823236e-6, 1.572130183778014, 2.2424585076387427, 2.8079394352847316,
+            3.883763676656034, 4.039123204140305, 6.787320617260535, 6.920636670319986,
+            7.127888889722697]
+
+# test/test_shell_statics.jl:97-104 and test/test_q4rs_shell_statics.jl:95-101
+SLO_N = [4, 8, 10, 12, 16, 24]
+SLO_T3_REF = [66.54771615057949, 85.54615143134853, 89.85075281481419, 92.50616661644985,
+              95.40469210310079, 97.65376880486126]
+SLO_Q4_REF = [97.88098976068304, 98.766679964194, 99.1305903792941, 99.33597700449404,
+              99.52904556664862, 99.63694998474682]
+
+
+def scordelis_lo(quads, n):
+    """Scordelis-Lo roof, test/test_shell_statics.jl:14-90 (T3) and
+    test/test_q4rs_shell_statics.jl:14-88 (Q4)."""
+    E, nu, t, R, L = 4.32e8, 0.0, 0.25, 25.0, 50.0
+    tol = R / n / 1000
+    if quads:
+        xy, conn = mesh.Q4block(PHI40, L / 2, n, n)
+    else:
+        xy, conn = mesh.T3block(PHI40, L / 2, n, n)
+    a, y = xy[:, 0].copy(), xy[:, 1].copy()
+    xyz = np.stack([R * np.sin(a), y, R * (np.cos(a) - 1)], 1)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    inf = np.inf
+    l1 = mesh.selectnode(xyz, [-inf, inf, 0, 0, -inf, inf], tol) - 1
+    for i in [1, 3, 5]:
+        fixed[l1, i - 1] = True
+    l1 = mesh.selectnode(xyz, [-inf, inf, L / 2, L / 2, -inf, inf], tol) - 1
+    for i in [2, 4, 6]:
+        fixed[l1, i - 1] = True
+    l1 = mesh.selectnode(xyz, [0, 0, -inf, inf, -inf, inf], tol) - 1
+    for i in [1, 5, 6]:
+        fixed[l1, i - 1] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, nu))
+    nl = mesh.selectnode(xyz, [np.sin(PHI40) * 25] * 2 + [L / 2, L / 2, -inf, inf], tol)[0] - 1
+    F = surface_load(xyz, conn, dof, -90.0)
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=t,
+                material=dict(Dps=Dps, Dt=Dt, rho=0.0), stab_c=0.2, F=F, probe=nl)
+
+
+def surface_load(xyz, conn, dof, qz):
+    """Consistent nodal loads of a uniform z traction (FinEtools distribloads
+    with TriRule(3) on triangles / GaussRule(2,2) on quads)."""
+    F = np.zeros(int(dof.max()))
+    g = 0.577350269189626
+    for e in range(conn.shape[0]):
+        X = xyz[conn[e] - 1]
+        if conn.shape[1] == 3:
+            A = 0.5 * np.linalg.norm(np.cross(X[1] - X[0], X[2] - X[0]))
+            for a in range(3):
+                F[dof[conn[e, a] - 1, 2] - 1] += qz * A / 3
+        else:
+            for xi, eta in [(-g, -g), (-g, g), (g, -g), (g, g)]:
+                N = 0.25 * np.array([(1 - xi) * (1 - eta), (1 + xi) * (1 - eta),
+                                     (1 + xi) * (1 + eta), (1 - xi) * (1 + eta)])
+                dN = 0.25 * np.array([[-(1 - eta), -(1 - xi)], [(1 - eta), -(1 + xi)],
+                                      [(1 + eta), (1 + xi)], [-(1 + eta), (1 - xi)]])
+                J = X.T @ dN
+                Jac = np.linalg.norm(np.cross(J[:, 0], J[:, 1]))
+                for a in range(4):
+                    F[dof[conn[e, a] - 1, 2] - 1] += qz * N[a] * Jac
+    return F
+
+
+def solve_probe(K, prob):
+    """K_ff u = F_f (solve_blocked! with zero prescribed values); returns the
+    probe's transverse deflection as percent of -0.3024."""
+    import scipy.sparse.linalg as spl
+    nf = prob["nfree"]
+    Kff = K[:nf, :nf].tocsc()
+    u = spl.spsolve(Kff, prob["F"][:nf])
+    d = prob["dofnums"][prob["probe"], 2]
+    return (u[d - 1] if d <= nf else 0.0) / -0.3024 * 100
+
+
+def jittered_plate(n, quads, side=1.0, jitter=0.2, seed=0, wavy=0.0, clamp_x0=True):
+    """Seeded synthetic plate: n x n quads (or 2 n^2 triangles) on
+    [0,side]^2, interior nodes jittered U(+-jitter*h), z = wavy*sin(pi x)
+    sin(pi y); edge x = 0 clamped."""
+    zf = None
+    if wavy:
+        zf = lambda x, y: wavy * np.sin(np.pi * x / side) * np.sin(np.pi * y / side)
+    xyz, connq = mesh.jittered_plate_q(n, side, jitter, seed, zf)
+    conn = connq if quads else mesh.quads_to_triangles(connq)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    if clamp_x0:
+        fixed[np.abs(xyz[:, 0]) < 1e-12 * side, :] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    return xyz, conn, dof, nfree

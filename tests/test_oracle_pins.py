@@ -1,0 +1,84 @@
+"""Pins of the CPU oracle against the reference's own known answers.
+
+The reference (Julia) cannot run here, so the oracle is trusted only because
+it reproduces the numbers the reference's test-suite asserts.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+from oracle import oracle as O
+import problems as PB
+
+
+def _problem(etype, d, **kw):
+    P = O.Problem(etype, d["xyz"], d["conn"], d["dofnums"], thickness=d["thickness"],
+                  material=d["material"], stab_c=d["stab_c"], **kw)
+    P.compute_normals()
+    return P
+
+
+@pytest.mark.parametrize("orientation", ["a", "b"])
+def test_fv12_frequencies(orientation):
+    # test/test_shell_dynamics.jl:130-133: rtol 1e-6 on the frequencies
+    d = PB.fv12(orientation)
+    P = _problem(O.T3FF, d)
+    K = P.assemble_scipy("K", O.DROP_ZEROS).toarray()
+    M = P.assemble_scipy("M", O.DROP_ZEROS).toarray()
+    w = sl.eigh(K, M, eigvals_only=True)
+    fs = np.sqrt(np.abs(w[:14])) / (2 * np.pi)
+    ref = np.array(PB.FV12_REF)
+    np.testing.assert_allclose(fs[6:], ref[6:], rtol=1e-6)
+    # the six rigid-body frequencies are numerical zeros in both codes
+    assert np.all(fs[:6] < 1e-3)
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_scordelis_lo_t3ff(k):
+    n = PB.SLO_N[k]
+    d = PB.scordelis_lo(False, n)
+    P = _problem(O.T3FF, d)
+    v = PB.solve_probe(P.assemble_scipy("K", O.DROP_ZEROS), d)
+    assert abs(v - PB.SLO_T3_REF[k]) <= 1e-4 * abs(PB.SLO_T3_REF[k])
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_scordelis_lo_q4rs(k):
+    n = PB.SLO_N[k]
+    d = PB.scordelis_lo(True, n)
+    P = _problem(O.Q4RS, d)
+    v = PB.solve_probe(P.assemble_scipy("K", O.DROP_ZEROS), d)
+    assert abs(v - PB.SLO_Q4_REF[k]) <= 1e-4 * abs(PB.SLO_Q4_REF[k])
+
+
+def test_keep_and_drop_zero_patterns_agree_in_value():
+    d = PB.scordelis_lo(False, 4)
+    P = _problem(O.T3FF, d)
+    Kk = P.assemble_scipy("K", O.KEEP_ZEROS)
+    Kd = P.assemble_scipy("K", O.DROP_ZEROS)
+    assert Kk.nnz >= Kd.nnz
+    diff = abs(Kk - Kd).max()
+    assert diff <= 1e-12 * abs(Kk).max()
+
+
+def test_free_element_rigid_translations_and_symmetry():
+    # A free element: rigid translations carry no strain energy (K r = 0)
+    # and the element matrix is symmetric (complete_lt!).
+    d = PB.fv12()
+    for etype, nen in ((O.T3FF, 3), (O.Q4RS, 4)):
+        if nen == 3:
+            xyz = np.array([[0, 0, 0], [1.0, 0.1, 0.05], [0.2, 0.9, -0.03]])
+        else:
+            xy = np.array([[0, 0], [1.0, 0.1], [1.1, 0.95], [-0.1, 1.0]])
+            # planar (tilted) quad: a warped quad is not exactly rigid-body free
+            xyz = np.column_stack([xy, 0.1 * xy[:, 0] + 0.05 * xy[:, 1]])
+        conn = np.arange(1, nen + 1)[None, :]
+        P = O.Problem(etype, xyz, conn, thickness=0.01, material=d["material"])
+        P.compute_normals()
+        Ke = P.element_stiffness()[0]
+        scale = np.abs(Ke).max()
+        assert np.allclose(Ke, Ke.T, rtol=0, atol=1e-12 * scale)
+        for c in range(3):
+            r = np.zeros(6 * nen)
+            r[c::6] = 1.0
+            assert np.abs(Ke @ r).max() <= 1e-9 * scale
