@@ -1,0 +1,371 @@
+"""Benchmark of the shell element-assembly hot path on one GB300.
+
+Workload (the reference's configuration 2, synthetic): a 1024 x 1024 quad
+plate on [0,1]^2, interior nodes jittered U(+-0.2 h) (PCG64 seed 0),
+z = 0.01 sin(pi x) sin(pi y), thickness 0.005, steel (E 200 GPa, nu 0.3,
+rho 7850).  T3FF uses the 2,097,152 triangles of the split quads, Q4RS the
+1,048,576 quads; 1,050,625 nodes x 6 dofs, all dofs in the matrix.
+
+A step is one stiffness assembly: element matrices + deterministic CSR value
+gather, on device-resident inputs with the sparsity pattern built (it depends
+only on the mesh and is built once per mesh; its time is reported apart).
+`value` is mixed-precision T3FF elements assembled per second; the FP64 path
+and Q4RS are reported beside it.  `e2e` is the same assembly through the C
+ABI from pinned host buffers: geometry and dof numbering uploaded, pattern
+rebuilt, assembled, CSC arrays (colptr, rowval, nzval) copied back.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "finetoolsflexstructures.jl_gb300")
+for _p in (PKG, ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np
+
+METRIC = "shell elements assembled/s, mixed vs FP64 on one GB300 at <=1e-6 rel err; CPU ref"
+E, NU, RHO, THICK = 200e9, 0.3, 7850.0, 0.005
+
+
+def plate(n, quads, seed=0):
+    from flexshell import mesh
+    xyz, connq = mesh.jittered_plate_q(n, 1.0, 0.2, seed,
+                                       lambda x, y: 0.01 * np.sin(np.pi * x) * np.sin(np.pi * y))
+    conn = connq if quads else mesh.quads_to_triangles(connq)
+    dof, nfree = mesh.numberdofs(np.zeros((xyz.shape[0], 6), bool))
+    return np.asfortranarray(xyz), np.ascontiguousarray(conn), np.asfortranarray(dof)
+
+
+def params(quads):
+    from flexshell import _abi, materials
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, NU, RHO))
+    return _abi.make_params(Dps, Dt, RHO, THICK, quads=quads)
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during a timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if len(f) > 2 + k and f[2 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(steps=None, budget_s=10.0, n=96):
+    """The oracle (C restatement of the reference loops, OpenMP over elements)
+    on a bounded sample: an n x n quad plate split in triangles."""
+    from oracle import oracle as O
+    from flexshell import materials
+    xyz, conn, dof = plate(n, False, seed=1)
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, NU, RHO))
+    P = O.Problem(O.T3FF, xyz, conn, dof, thickness=THICK, material=dict(Dps=Dps, Dt=Dt, rho=RHO))
+    P.compute_normals()
+    cores = os.cpu_count() or 1
+    P.assemble("K", O.KEEP_ZEROS, nthreads=cores)  # warm
+    t0 = time.perf_counter()
+    reps = 0
+    times = []
+    while True:
+        t1 = time.perf_counter()
+        P.assemble("K", O.KEEP_ZEROS, nthreads=cores)
+        times.append(time.perf_counter() - t1)
+        reps += 1
+        if steps is not None and reps >= steps:
+            break
+        if steps is None and time.perf_counter() - t0 > budget_s:
+            break
+    el = conn.shape[0]
+    return {"value": el * reps / sum(times), "unit": "elements/s", "cores": cores, "kind": "port",
+            "sample": "T3FF stiffness, %dx%d quad plate split in %d triangles, element loop + COO->CSC "
+                      "assembly, %d repetitions" % (n, n, el, reps)}, times
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build()
+    w = max(args.warmup, 0)
+    cpu_baseline(steps=max(w, 1), n=64)
+    cb, times = cpu_baseline(steps=args.steps, n=96)
+    ms = 1e3 * float(np.mean(times))
+    line = {"metric": METRIC, "value": cb["value"], "unit": "elements/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "T3FF stiffness assembly, jittered wavy plate (bounded CPU sample of the "
+                                   "1024x1024 configuration)", "sample": cb["sample"]},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "elements/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+class Assembler:
+    """One library context with one mesh resident."""
+
+    def __init__(self, xyz, conn, dof, quads, device=0):
+        from flexshell import _abi
+        from flexshell._lib import Context, ptr
+        self.ptr = ptr
+        self.ctx = Context(device)
+        self.quads = quads
+        self.nelem = conn.shape[0]
+        self.n = dof.shape[0] * 6
+        et = _abi.FS_Q4RS if quads else _abi.FS_T3FF
+        self.ctx.call("fs_mesh_set", et, xyz.shape[0], ptr(xyz), conn.shape[0], ptr(conn), None, ptr(dof))
+        self.ctx.call("fs_params_set", params(quads), None)
+        self.ctx.call("fs_normals_compute")
+
+    def stiffness(self, precision):
+        nnz = ctypes.c_int64()
+        self.ctx.call("fs_stiffness", precision, 0, self.n, ctypes.byref(nnz))
+        return nnz.value
+
+    def timings(self):
+        t = np.zeros(4)
+        self.ctx.call("fs_timings", self.ptr(t), 4)
+        return t
+
+    def values(self, nnz):
+        v = np.empty(nnz)
+        self.ctx.call("fs_matrix_copy", None, None, self.ptr(v))
+        return v
+
+
+def time_steps(asm, precision, steps, warmup, torch, stream):
+    for _ in range(warmup):
+        asm.stiffness(precision)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phases = np.zeros(4)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        nnz = asm.stiffness(precision)
+        phases += asm.timings()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / steps, phases / steps, nnz
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--n", type=int, default=1024, help="quads per side")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    from flexshell import _abi
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+
+    res = {}
+    # --- T3FF (headline) -----------------------------------------------------
+    xyz, conn, dof = plate(args.n, False)
+    asm = Assembler(xyz, conn, dof, False, device=local)
+    stream = torch.cuda.ExternalStream(asm.ctx.stream())
+    asm.stiffness(_abi.FS_MIXED)  # builds the pattern
+    t_sym = asm.timings()[2]
+    if world > 1:
+        dist.barrier()
+    clocks = Clocks(local)
+    with clocks:
+        ms_mixed, ph_mixed, nnz = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
+    if world > 1:
+        t = torch.tensor([ms_mixed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_mixed = float(t.item())
+    v_mixed = asm.values(nnz)
+    ms_fp64, ph_fp64, _ = time_steps(asm, _abi.FS_FP64, args.steps, args.warmup, torch, stream)
+    v_fp64 = asm.values(nnz)
+    err_t3 = float(np.abs(v_mixed - v_fp64).max() / np.abs(v_fp64).max())
+    fro_t3 = float(np.linalg.norm(v_mixed - v_fp64) / np.linalg.norm(v_fp64))
+    del v_mixed, v_fp64
+    res["t3"] = dict(ms_mixed=ms_mixed, ms_fp64=ms_fp64, ph_mixed=ph_mixed, ph_fp64=ph_fp64, nnz=nnz,
+                     err=err_t3, fro=fro_t3, t_sym=t_sym, nelem=conn.shape[0])
+
+    # --- e2e through the C ABI from pinned host buffers (T3FF, mixed) ------------
+    nn = xyz.shape[0]
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    h_xyz = pin((3 * nn,), torch.float64)
+    h_xyz[:] = xyz.flatten(order="F")
+    h_dof = pin((6 * nn,), torch.int64)
+    h_dof[:] = dof.flatten(order="F")
+    h_colptr = pin((asm.n + 1,), torch.int64)
+    h_rowval = pin((nnz,), torch.int64)
+    h_nzval = pin((nnz,), torch.float64)
+    P = asm.ptr
+
+    def e2e_step():
+        asm.ctx.call("fs_geometry_set", P(h_xyz))
+        asm.ctx.call("fs_dofs_set", P(h_dof))
+        k = ctypes.c_int64()
+        asm.ctx.call("fs_stiffness", _abi.FS_MIXED, 0, asm.n, ctypes.byref(k))
+        asm.ctx.call("fs_matrix_copy", P(h_colptr), P(h_rowval), P(h_nzval))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    ms_e2e = 1e3 * (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    h2d = (3 * nn) * 8 + (6 * nn) * 8
+    d2h = (asm.n + 1) * 8 + nnz * 8 + nnz * 8
+    del h_colptr, h_rowval, h_nzval
+    asm.ctx.close()
+    del asm
+
+    # --- Q4RS -------------------------------------------------------------------
+    xyz, conn, dof = plate(args.n, True)
+    asm = Assembler(xyz, conn, dof, True, device=local)
+    stream = torch.cuda.ExternalStream(asm.ctx.stream())
+    asm.stiffness(_abi.FS_MIXED)
+    t_sym_q4 = asm.timings()[2]
+    ms_q_mixed, ph_q_mixed, nnz_q = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
+    vq_m = asm.values(nnz_q)
+    ms_q_fp64, ph_q_fp64, _ = time_steps(asm, _abi.FS_FP64, args.steps, args.warmup, torch, stream)
+    vq_d = asm.values(nnz_q)
+    err_q4 = float(np.abs(vq_m - vq_d).max() / np.abs(vq_d).max())
+    del vq_m, vq_d
+    asm.ctx.close()
+    del asm
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
+    t3 = res["t3"]
+    ne3, ne4 = t3["nelem"], conn.shape[0]
+    value = world * ne3 / (ms_mixed * 1e-3)
+    # roofline of the dominant kernel of the headline path
+    hbm, peak_kind = read_peaks()
+    el_ms, ga_ms = t3["ph_mixed"][0], t3["ph_mixed"][1]
+    nodes = (args.n + 1) ** 2
+    # algorithmic bytes per launch (per element / per stored value)
+    el_bytes = ne3 * (3 * 4 + 3 * 24 + 3 * 24 + 3 + 8 + 324 * 4)
+    ga_bytes = ne3 * 324 * 4 + nnz * 8 + ne3 * 3 * 8 + nodes * (6 * 4 + 8 + 4 + 8)
+    if el_ms >= ga_ms:
+        dom, ms_dom, alg = "k_t3_elements<float>", el_ms, el_bytes
+    else:
+        dom, ms_dom, alg = "k_gather<float>", ga_ms, ga_bytes
+    achieved = alg / (ms_dom * 1e-3) / 1e9
+    cb = None
+    if not args.no_cpu:
+        cb, _ = cpu_baseline()
+    line = {
+        "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-element/f64-assembly", "data": "synthetic",
+        "config": {"workload": "T3FF stiffness assembly, mixed precision, 1024x1024 jittered wavy plate "
+                               "(2,097,152 triangles, 1,050,625 nodes, 6,303,750 dofs)",
+                   "elements": ne3, "nnz": nnz, "precision": "FS_MIXED", "assembler": "SysmatAssemblerSparse",
+                   "pattern": "built once per mesh (symbolic %.2f ms), not in the timed step" % t3["t_sym"],
+                   "l2": "inputs larger than L2 (element matrices %.2f GB, values %.2f GB)" % (
+                       ne3 * 324 * 4 / 1e9, nnz * 8 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": world * ne3 / (ms_e2e * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
+                "path": "C ABI from pinned host: fs_geometry_set + fs_dofs_set + fs_stiffness (pattern "
+                        "rebuilt) + fs_matrix_copy"},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms_dom},
+        "clocks": clocks.summary(),
+        "cpu_baseline": cb,
+        "results": {
+            "t3ff": {"elements": ne3, "nnz": nnz, "mixed_elements_per_s": ne3 / (ms_mixed * 1e-3),
+                     "fp64_elements_per_s": ne3 / (ms_fp64 * 1e-3),
+                     "mixed_over_fp64": ms_fp64 / ms_mixed, "nnz_per_s_mixed": nnz / (ms_mixed * 1e-3),
+                     "rel_err_K_mixed_vs_fp64_max": t3["err"], "rel_err_K_mixed_vs_fp64_fro": t3["fro"],
+                     "ms_elements_mixed": t3["ph_mixed"][0], "ms_gather_mixed": t3["ph_mixed"][1],
+                     "ms_elements_fp64": t3["ph_fp64"][0], "ms_gather_fp64": t3["ph_fp64"][1],
+                     "ms_symbolic": t3["t_sym"], "e2e_ms": ms_e2e},
+            "q4rs": {"elements": ne4, "nnz": nnz_q, "mixed_elements_per_s": ne4 / (ms_q_mixed * 1e-3),
+                     "fp64_elements_per_s": ne4 / (ms_q_fp64 * 1e-3), "mixed_over_fp64": ms_q_fp64 / ms_q_mixed,
+                     "rel_err_K_mixed_vs_fp64_max": err_q4, "ms_elements_mixed": ph_q_mixed[0],
+                     "ms_gather_mixed": ph_q_mixed[1], "ms_elements_fp64": ph_q_fp64[0],
+                     "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4},
+        },
+    }
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

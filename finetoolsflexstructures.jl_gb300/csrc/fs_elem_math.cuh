@@ -1,0 +1,680 @@
+// Per-element math of the shell hot path, shared by the CUDA kernels (and,
+// for checking, by a host build of the same header).
+//
+// Formulation.  The reference (FinEtoolsFlexStructures.jl 3.6.4) builds the
+// element matrix in the element frame and then applies two dense 18x18 /
+// 24x24 congruences (src/FEMMShellT3FFModule.jl:708-730,
+// src/FEMMShellQ4RSModule.jl:925-936).  Here the same matrix is written as a
+// Gram product K = Bh^T Bh, where every row of Bh is one strain component
+// already expressed on the GLOBAL dofs:
+//
+//   * the element-frame strain-displacement rows (membrane, bending,
+//     transverse shear) are combined with the Cholesky factor of the
+//     material matrix (D = L L^T) and the quadrature weight, and
+//   * the nodal-to-element transformation (triads, drilling coupling
+//     1/2 (v,x - u,y) of src/FEMMShellT3FFModule.jl:421-463) and the
+//     global-to-nodal rotation are folded into each row analytically,
+//   * the drilling penalty kavg * (n . theta)^2 becomes one extra row per
+//     node with a valid normal.
+//
+// Mathematically this is identical to the reference; numerically it differs
+// by rounding only.  Geometry (element frame, nodal triads, the drilling
+// factor) is always computed in double; the strain rows and the Gram product
+// use the template precision R (double for the FP64 path, float for the
+// mixed path).
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#ifndef FS_HD
+#if defined(__CUDACC__)
+#define FS_HD __host__ __device__ __forceinline__
+#else
+#define FS_HD inline
+#endif
+#endif
+
+namespace fs {
+
+// ---------------------------------------------------------------------------
+// small vector helpers
+// ---------------------------------------------------------------------------
+template <class T> FS_HD T dot3(const T a[3], const T b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+template <class T> FS_HD void cross3(const T a[3], const T b[3], T c[3])
+{
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+FS_HD double rsqrt_d(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return rsqrt(x);
+#else
+    return 1.0 / sqrt(x);
+#endif
+}
+
+// Element frame from two tangents (reference _e_g!, src/FEMMShellT3FFModule.jl:283-305):
+// e1 = a/|a|, e3 = (e1 x b)/|e1 x b|, e2 = e3 x e1.  e[k][c] = component c of e_k.
+FS_HD void make_frame(const double a[3], const double b[3], double e[3][3])
+{
+    double s = rsqrt_d(dot3(a, a));
+    for (int c = 0; c < 3; c++) e[0][c] = a[c] * s;
+    cross3(e[0], b, e[2]);
+    s = rsqrt_d(dot3(e[2], e[2]));
+    for (int c = 0; c < 3; c++) e[2][c] *= s;
+    cross3(e[2], e[0], e[1]);
+}
+
+// Nodal triad (reference _NodalTriadsE, src/FEMMShellT3FFModule.jl:355-388):
+// the rotation by the vector a = e3_e x n_e (angle |a|, FinEtools rotmat3!),
+// in Rodrigues form R = I + s(x) [a]x + c(x) [a]x^2 with x = |a|^2,
+// s = sin(phi)/phi, c = (1 - cos(phi))/phi^2.  Both are evaluated from
+// their Taylor series in x (9 terms: truncation below 1e-17 for x <= 1).
+FS_HD void sinc_cosc(double x, double &s, double &c)
+{
+    if (x <= 1.0) {
+        // s = sum (-x)^k/(2k+1)!,  c = sum (-x)^k/(2k+2)!
+        s = 1.0 / 355687428096000.0;              // 1/17!
+        s = 1.0 / 1307674368000.0 - x * s;        // 1/15!
+        s = 1.0 / 6227020800.0 - x * s;           // 1/13!
+        s = 1.0 / 39916800.0 - x * s;             // 1/11!
+        s = 1.0 / 362880.0 - x * s;               // 1/9!
+        s = 1.0 / 5040.0 - x * s;                 // 1/7!
+        s = 1.0 / 120.0 - x * s;                  // 1/5!
+        s = 1.0 / 6.0 - x * s;                    // 1/3!
+        s = 1.0 - x * s;
+        c = 1.0 / 6402373705728000.0;             // 1/18!
+        c = 1.0 / 20922789888000.0 - x * c;       // 1/16!
+        c = 1.0 / 87178291200.0 - x * c;          // 1/14!
+        c = 1.0 / 479001600.0 - x * c;            // 1/12!
+        c = 1.0 / 3628800.0 - x * c;              // 1/10!
+        c = 1.0 / 40320.0 - x * c;                // 1/8!
+        c = 1.0 / 720.0 - x * c;                  // 1/6!
+        c = 1.0 / 24.0 - x * c;                   // 1/4!
+        c = 0.5 - x * c;                          // 1/2!
+    } else {
+        double phi = sqrt(x);
+        s = sin(phi) / phi;
+        c = (1.0 - cos(phi)) / x;
+    }
+}
+
+// R[r][k]: row r, column k of the triad A_E of one node.
+FS_HD void nodal_triad(const double e[3][3], const double n[3], bool valid, double R[3][3])
+{
+    double a0 = 0.0, a1 = 0.0;
+    if (valid) {
+        double ne0 = dot3(e[0], n), ne1 = dot3(e[1], n);
+        a0 = -ne1;
+        a1 = ne0;
+    }
+    double x = a0 * a0 + a1 * a1;
+    if (!(x > 1.0e-24)) {
+        R[0][0] = 1; R[0][1] = 0; R[0][2] = 0;
+        R[1][0] = 0; R[1][1] = 1; R[1][2] = 0;
+        R[2][0] = 0; R[2][1] = 0; R[2][2] = 1;
+        return;
+    }
+    double s, c;
+    sinc_cosc(x, s, c);
+    R[0][0] = 1.0 - c * a1 * a1; R[0][1] = c * a0 * a1;       R[0][2] = s * a1;
+    R[1][0] = c * a0 * a1;       R[1][1] = 1.0 - c * a0 * a0; R[1][2] = -s * a0;
+    R[2][0] = -s * a1;           R[2][1] = s * a0;            R[2][2] = 1.0 - c * x;
+}
+
+// ---------------------------------------------------------------------------
+// Mapping of element-frame strain rows to global dofs
+// ---------------------------------------------------------------------------
+// Element-frame dofs per node: u, v, w, thx, thy (the element drilling
+// rotation row of T_ae is zero and carries no stiffness).
+template <class R, int NN> struct GlobalMap {
+    R e[3][3];      // element basis (global components)
+    R t[NN][3][3];  // nodal triad vectors in global components: t[i][k] = E A_i[:,k]
+    R A01[NN][2][3];// rows 0,1 of A_i
+    R R2[NN][2][2]; // rotation block of T_ae
+    R m[NN][2];     // drilling coupling multipliers A_i[r][2]/A_i[2][2]
+    R g[NN][2];     // basis function gradients on the element basis
+};
+
+// Build the map from the double-precision frame and triads.
+template <class R, int NN>
+FS_HD void build_map(const double e[3][3], const double A[NN][3][3], const R g[NN][2],
+                     GlobalMap<R, NN> &M)
+{
+    for (int k = 0; k < 3; k++)
+        for (int c = 0; c < 3; c++) M.e[k][c] = (R)e[k][c];
+    for (int i = 0; i < NN; i++) {
+        for (int k = 0; k < 3; k++)
+            for (int c = 0; c < 3; c++)
+                M.t[i][k][c] = (R)(A[i][0][k] * e[0][c] + A[i][1][k] * e[1][c] + A[i][2][k] * e[2][c]);
+        double inv33 = 1.0 / A[i][2][2];
+        for (int r = 0; r < 2; r++) {
+            for (int k = 0; k < 3; k++) M.A01[i][r][k] = (R)A[i][r][k];
+            M.m[i][r] = (R)(A[i][r][2] * inv33);
+            for (int cl = 0; cl < 2; cl++) M.R2[i][r][cl] = (R)(A[i][r][cl] - inv33 * A[i][r][2] * A[i][cl][2]);
+        }
+        M.g[i][0] = g[i][0];
+        M.g[i][1] = g[i][1];
+    }
+}
+
+// Expand one element-frame row c[NN][5] (u,v,w,thx,thy per node) into a row
+// on the global dofs out[6*NN] (3 translations, 3 rotations per node).
+template <class R, int NN>
+FS_HD void expand_row(const GlobalMap<R, NN> &M, const R c[NN][5], R *out)
+{
+    R P0[3] = {0, 0, 0}, P1[3] = {0, 0, 0};
+    for (int i = 0; i < NN; i++) {
+        R mu = c[i][3] * M.m[i][0] + c[i][4] * M.m[i][1];
+        for (int k = 0; k < 3; k++) {
+            P0[k] += mu * M.A01[i][0][k];
+            P1[k] += mu * M.A01[i][1][k];
+        }
+    }
+    for (int j = 0; j < NN; j++) {
+        R h[3];
+        for (int k = 0; k < 3; k++) h[k] = (R)0.5 * (M.g[j][0] * P1[k] - M.g[j][1] * P0[k]);
+        R r0 = c[j][3] * M.R2[j][0][0] + c[j][4] * M.R2[j][1][0];
+        R r1 = c[j][3] * M.R2[j][0][1] + c[j][4] * M.R2[j][1][1];
+        for (int q = 0; q < 3; q++) {
+            out[6 * j + q] = c[j][0] * M.e[0][q] + c[j][1] * M.e[1][q] + c[j][2] * M.e[2][q] +
+                             h[0] * M.t[j][0][q] + h[1] * M.t[j][1][q] + h[2] * M.t[j][2][q];
+            out[6 * j + 3 + q] = r0 * M.t[j][0][q] + r1 * M.t[j][1][q];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Material factors
+// ---------------------------------------------------------------------------
+// Per-call constant material data (host precomputed).
+struct MatConst {
+    double Lps[6];    // Cholesky factor of Dps, lower, packed (L00,L10,L11,L20,L21,L22)
+    double Lt[3];     // Cholesky factor of (5/6) Dt, lower packed (L00,L10,L11)
+    double stab_c;    // stab_fun(t,h) = t^2/(t^2 + stab_c h^2)
+    double drill_scale;
+    double rho;
+};
+
+// Layup group (host precomputed from the laminate A,B,D,H): Cholesky factor
+// of the 6x6 [A B; B D] (lower packed, 21) and of H (lower packed, 3).
+struct GroupConst {
+    double L6[21];
+    double LH[3];
+    double csmat[9];  // column-major layup csys (first column = layup reference direction)
+    double thickness;
+    double mass;      // mass density per unit area (laminate_inertia!)
+    double moi;       // rotary inertia density
+    double pad;
+};
+
+FS_HD int lp(int r, int c) { return r * (r + 1) / 2 + c; }  // packed lower index, r >= c
+
+// rows_out[r] = scale * sum_{c>=r} L[c][r] rows_in[c]   (L^T applied to stacked rows)
+template <class R, int NN, int NR>
+FS_HD void mix_rows(const double *Lpk, double scale, const R in[NR][NN][5], R out[NR][NN][5])
+{
+    for (int r = 0; r < NR; r++) {
+        R f[NR];
+        for (int c = 0; c < NR; c++) f[c] = (c >= r) ? (R)(scale * Lpk[lp(c, r)]) : (R)0;
+        for (int i = 0; i < NN; i++)
+            for (int q = 0; q < 5; q++) {
+                R s = 0;
+                for (int c = r; c < NR; c++) s += f[c] * in[c][i][q];
+                out[r][i][q] = s;
+            }
+    }
+}
+
+// Layup-to-element angle (reference Layup2ElementAngle, src/TransformerModule.jl:92-105)
+FS_HD void layup_angle(const double e[3][3], const double cs[9], double &m, double &n)
+{
+    // M = E^T csmat, 2x2 leading block, columns normalised
+    double a11 = e[0][0] * cs[0] + e[0][1] * cs[1] + e[0][2] * cs[2];
+    double a21 = e[1][0] * cs[0] + e[1][1] * cs[1] + e[1][2] * cs[2];
+    double a12 = e[0][0] * cs[3] + e[0][1] * cs[4] + e[0][2] * cs[5];
+    double a22 = e[1][0] * cs[3] + e[1][1] * cs[4] + e[1][2] * cs[5];
+    double n1 = sqrt(a11 * a11 + a21 * a21), n2 = sqrt(a12 * a12 + a22 * a22);
+    a11 /= n1; a21 /= n1; a12 /= n2; a22 /= n2;
+    m = (a11 + a22) / 2.0;
+    double nn = (a12 - a21) / 2.0;
+    double q = 1.0 - m * m;
+    n = (nn >= 0.0 ? 1.0 : -1.0) * sqrt(q > 0.0 ? q : 0.0);
+}
+
+// Rotate the membrane and bending element-frame rows by Tbar and the shear
+// rows by Tts (plane_stress_Tbar_matrix!, src/CompositeLayupModule.jl:364-378;
+// transverse_shear_T_matrix!, :463-471): strain' = T strain.
+template <class R, int NN>
+FS_HD void rotate3(double m, double n, R rows[3][NN][5])
+{
+    double T[3][3] = {{m * m, n * n, -(m * n)}, {n * n, m * m, (m * n)}, {2 * (m * n), -2 * (m * n), m * m - n * n}};
+    for (int i = 0; i < NN; i++)
+        for (int q = 0; q < 5; q++) {
+            R a = rows[0][i][q], b = rows[1][i][q], c = rows[2][i][q];
+            rows[0][i][q] = (R)T[0][0] * a + (R)T[0][1] * b + (R)T[0][2] * c;
+            rows[1][i][q] = (R)T[1][0] * a + (R)T[1][1] * b + (R)T[1][2] * c;
+            rows[2][i][q] = (R)T[2][0] * a + (R)T[2][1] * b + (R)T[2][2] * c;
+        }
+}
+template <class R, int NN>
+FS_HD void rotate2(double m, double n, R rows[2][NN][5])
+{
+    for (int i = 0; i < NN; i++)
+        for (int q = 0; q < 5; q++) {
+            R a = rows[0][i][q], b = rows[1][i][q];
+            rows[0][i][q] = (R)m * a - (R)n * b;
+            rows[1][i][q] = (R)n * a + (R)m * b;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Element inputs
+// ---------------------------------------------------------------------------
+template <int NN> struct ElemIn {
+    double X[NN][3];     // node coordinates
+    double nrm[NN][3];   // nodal normals
+    bool valid[NN];      // normal valid flags
+    double t;            // thickness
+    int group;           // layup group (composite)
+};
+
+// ---------------------------------------------------------------------------
+// T3FF: rows of one element
+// ---------------------------------------------------------------------------
+// Number of Gram rows: membrane+bending 6, shear 2 (average B) or 6
+// (average K), drilling 3.
+template <bool AVGK> struct T3Rows { static const int NS = AVGK ? 6 : 2; static const int N = 6 + NS + 3; };
+
+// T3 element-frame shear rows for the node ordering (s,p,q)
+// (reference _add_Bsmat_o!, src/FEMMShellT3FFModule.jl:486-526).
+template <class R>
+FS_HD void t3_bs_ordering(const R x[3], const R y[3], R Ae, int s, int p, int q, R Bs[2][3][5], R w)
+{
+    R a = x[p] - x[s], b = y[p] - y[s], c = x[q] - x[s], d = y[q] - y[s];
+    R mm = w / (2 * Ae);
+    Bs[0][s][2] += mm * (b - d);  Bs[1][s][2] += mm * (c - a);
+    Bs[0][s][4] += mm * Ae;       Bs[1][s][3] += -mm * Ae;
+    Bs[0][p][2] += mm * d;        Bs[1][p][2] += -mm * c;
+    Bs[0][p][3] += -mm * b * d / 2; Bs[1][p][3] += mm * b * c / 2;
+    Bs[0][p][4] += mm * a * d / 2;  Bs[1][p][4] += -mm * a * c / 2;
+    Bs[0][q][2] += -mm * b;       Bs[1][q][2] += mm * a;
+    Bs[0][q][3] += mm * b * d / 2;  Bs[1][q][3] += -mm * a * d / 2;
+    Bs[0][q][4] += -mm * b * c / 2; Bs[1][q][4] += mm * a * c / 2;
+}
+
+// Computes the Gram rows (global dofs, 18 wide) of one T3FF / T3FFComp
+// element.  Returns 0 on success.  `rows` is written with row stride `rs`.
+template <class R, bool COMP, bool AVGK>
+FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc, R *rows, int rs)
+{
+    // --- frame and element coordinates (double) ---
+    double J0[3], J1[3], e[3][3];
+    for (int c = 0; c < 3; c++) {
+        J0[c] = in.X[1][c] - in.X[0][c];
+        J1[c] = in.X[2][c] - in.X[0][c];
+    }
+    make_frame(J0, J1, e);
+    double a = dot3(J0, e[0]), b = dot3(J0, e[1]);
+    double cc = dot3(J1, e[0]), d = dot3(J1, e[1]);
+    double Jd = a * d - b * cc;
+    double Ae = Jd / 2;
+    double iJ = 1.0 / Jd;
+    R g[3][2];
+    g[0][0] = (R)((b - d) * iJ); g[1][0] = (R)(d * iJ); g[2][0] = (R)(-b * iJ);
+    g[0][1] = (R)((cc - a) * iJ); g[1][1] = (R)(-cc * iJ); g[2][1] = (R)(a * iJ);
+    double t = COMP ? gc->thickness : in.t;
+    // --- triads (double) ---
+    double A[3][3][3];
+    for (int i = 0; i < 3; i++) nodal_triad(e, in.nrm[i], in.valid[i], A[i]);
+    GlobalMap<R, 3> M;
+    build_map<R, 3>(e, A, g, M);
+
+    // --- element-frame rows ---
+    R mb[6][3][5];
+    for (int r = 0; r < 6; r++)
+        for (int i = 0; i < 3; i++)
+            for (int q = 0; q < 5; q++) mb[r][i][q] = 0;
+    for (int i = 0; i < 3; i++) {
+        mb[0][i][0] = g[i][0];
+        mb[1][i][1] = g[i][1];
+        mb[2][i][0] = g[i][1]; mb[2][i][1] = g[i][0];
+        mb[3][i][4] = g[i][0];
+        mb[4][i][3] = -g[i][1];
+        mb[5][i][3] = -g[i][0]; mb[5][i][4] = g[i][1];
+    }
+    const int NS = T3Rows<AVGK>::NS;
+    R sh[NS][3][5];
+    for (int r = 0; r < NS; r++)
+        for (int i = 0; i < 3; i++)
+            for (int q = 0; q < 5; q++) sh[r][i][q] = 0;
+    R x[3] = {0, (R)a, (R)cc}, y[3] = {0, (R)b, (R)d};
+    R AeR = (R)Ae;
+    if (AVGK) {
+        t3_bs_ordering<R>(x, y, AeR, 0, 1, 2, (R(*)[3][5])sh[0], (R)1);
+        t3_bs_ordering<R>(x, y, AeR, 1, 2, 0, (R(*)[3][5])sh[2], (R)1);
+        t3_bs_ordering<R>(x, y, AeR, 2, 0, 1, (R(*)[3][5])sh[4], (R)1);
+    } else {
+        t3_bs_ordering<R>(x, y, AeR, 0, 1, 2, (R(*)[3][5])sh[0], (R)(1.0 / 3));
+        t3_bs_ordering<R>(x, y, AeR, 1, 2, 0, (R(*)[3][5])sh[0], (R)(1.0 / 3));
+        t3_bs_ordering<R>(x, y, AeR, 2, 0, 1, (R(*)[3][5])sh[0], (R)(1.0 / 3));
+    }
+    // --- material mixing ---
+    double h2 = 2 * Ae;  // h = sqrt(2 Ae)
+    double stab = t * t / (t * t + mc.stab_c * h2);
+    R mixed[6 + NS][3][5];
+    if (!COMP) {
+        R inm[3][3][5], inb[3][3][5];
+        for (int r = 0; r < 3; r++)
+            for (int i = 0; i < 3; i++)
+                for (int q = 0; q < 5; q++) { inm[r][i][q] = mb[r][i][q]; inb[r][i][q] = mb[3 + r][i][q]; }
+        mix_rows<R, 3, 3>(mc.Lps, sqrt(t * Ae), inm, (R(*)[3][5])mixed[0]);
+        mix_rows<R, 3, 3>(mc.Lps, sqrt(t * t * t / 12 * Ae), inb, (R(*)[3][5])mixed[3]);
+        double ws = t * stab * Ae * (AVGK ? 1.0 / 3 : 1.0);
+        for (int o = 0; o < NS / 2; o++)
+            mix_rows<R, 3, 2>(mc.Lt, sqrt(ws), (R(*)[3][5])sh[2 * o], (R(*)[3][5])mixed[6 + 2 * o]);
+    } else {
+        double lm, ln;
+        layup_angle(e, gc->csmat, lm, ln);
+        rotate3<R, 3>(lm, ln, (R(*)[3][5])mb[0]);
+        rotate3<R, 3>(lm, ln, (R(*)[3][5])mb[3]);
+        mix_rows<R, 3, 6>(gc->L6, sqrt(Ae), mb, (R(*)[3][5])mixed[0]);
+        double ws = stab * Ae * (AVGK ? 1.0 / 3 : 1.0);
+        for (int o = 0; o < NS / 2; o++) {
+            rotate2<R, 3>(lm, ln, (R(*)[3][5])sh[2 * o]);
+            mix_rows<R, 3, 2>(gc->LH, sqrt(ws), (R(*)[3][5])sh[2 * o], (R(*)[3][5])mixed[6 + 2 * o]);
+        }
+    }
+    // --- drilling factor (double): mean of the nodal-basis bending
+    //     diagonals, src/FEMMShellT3FFModule.jl:713-727 ---
+    double ksum = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int cl = 0; cl < 2; cl++) {
+            double s2 = 0.0;
+            for (int r = 0; r < 6 + NS; r++) {
+                double v = (double)mixed[r][i][3] * (double)M.R2[i][0][cl] +
+                           (double)mixed[r][i][4] * (double)M.R2[i][1][cl];
+                s2 += v * v;
+            }
+            ksum += s2;
+        }
+    double kavg = ksum / 6.0 * mc.drill_scale;
+    // --- global rows ---
+    for (int r = 0; r < 6 + NS; r++) expand_row<R, 3>(M, (const R(*)[5])mixed[r], rows + r * rs);
+    double sk = kavg > 0.0 ? sqrt(kavg) : 0.0;
+    for (int i = 0; i < 3; i++) {
+        R *o = rows + (6 + NS + i) * rs;
+        for (int q = 0; q < 18; q++) o[q] = 0;
+        if (in.valid[i])
+            for (int c = 0; c < 3; c++) o[6 * i + 3 + c] = (R)(sk * (double)M.t[i][2][c]);
+    }
+    return (kavg < 0.0) ? 2 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Q4RS: rows of one quadrature point
+// ---------------------------------------------------------------------------
+static const double Q4_GP = 0.577350269189626;  // FinEtools GaussRule(2,2) abscissa
+
+FS_HD void q4_point(int j, double &xi, double &eta)
+{
+    xi = (j < 2 ? -Q4_GP : Q4_GP);
+    eta = ((j & 1) ? Q4_GP : -Q4_GP);
+}
+
+FS_HD void q4_dbasis(double xi, double eta, double gp[4][2])
+{
+    gp[0][0] = -0.25 * (1 - eta); gp[0][1] = -0.25 * (1 - xi);
+    gp[1][0] = 0.25 * (1 - eta);  gp[1][1] = -0.25 * (1 + xi);
+    gp[2][0] = 0.25 * (1 + eta);  gp[2][1] = 0.25 * (1 + xi);
+    gp[3][0] = -0.25 * (1 + eta); gp[3][1] = 0.25 * (1 - xi);
+}
+
+// MITC transverse shear rows in the element frame
+// (reference _Bsmat, src/FEMMShellQ4RSModule.jl:702-751), regrouped: each
+// entry is p*LA*fa(node) + q*LB*fb(node) with (p,q) = (sa,sb) for gxz and
+// (-ca,-cb) for gyz.
+template <class R>
+FS_HD void q4_bs(const R X[4], const R Y[4], R r, R s, R Bs[2][4][5])
+{
+    R J11 = (X[0] * (s - 1) - X[1] * (s - 1) + X[2] * (s + 1) - X[3] * (s + 1)) / 4;
+    R J21 = (Y[0] * (s - 1) - Y[1] * (s - 1) + Y[2] * (s + 1) - Y[3] * (s + 1)) / 4;
+    R J12 = (X[0] * (r - 1) - X[1] * (r + 1) + X[2] * (r + 1) - X[3] * (r - 1)) / 4;
+    R J22 = (Y[0] * (r - 1) - Y[1] * (r + 1) + Y[2] * (r + 1) - Y[3] * (r - 1)) / 4;
+    R A = sqrt(J11 * J11 + J21 * J21), B = sqrt(J12 * J12 + J22 * J22);
+    R ca = J11 / A, sa = J21 / A, cb = J12 / B, sb = J22 / B;
+    R detJ = J11 * J22 - J12 * J21;
+    R Ax = X[0] - X[1] - X[2] + X[3], Ay = Y[0] - Y[1] - Y[2] + Y[3];
+    R Bx = X[0] - X[1] + X[2] - X[3], By = Y[0] - Y[1] + Y[2] - Y[3];
+    R Cx = X[0] + X[1] - X[2] - X[3], Cy = Y[0] + Y[1] - Y[2] - Y[3];
+    R LA = sqrt((Ax + Bx * s) * (Ax + Bx * s) + (Ay + By * s) * (Ay + By * s));
+    R LB = sqrt((Bx * r + Cx) * (Bx * r + Cx) + (By * r + Cy) * (By * r + Cy));
+    R rp = r + 1, rm = r - 1, sp = s + 1, sm = s - 1;
+    R d16 = 1 / (16 * detJ), d32 = 1 / (32 * detJ);
+    // node-wise factors of the LA (tying along r) and LB (along s) terms
+    R fw_a[4] = {rp, -rm, rm, -rp}, fw_b[4] = {-sp, sp, -sm, sm};
+    R fx_a[4] = {-(Y[0] - Y[3]) * rp, (Y[1] - Y[2]) * rm, (Y[1] - Y[2]) * rm, -(Y[0] - Y[3]) * rp};
+    R fx_b[4] = {(Y[0] - Y[1]) * sp, (Y[0] - Y[1]) * sp, (Y[2] - Y[3]) * sm, (Y[2] - Y[3]) * sm};
+    R fy_a[4] = {(X[0] - X[3]) * rp, -(X[1] - X[2]) * rm, -(X[1] - X[2]) * rm, (X[0] - X[3]) * rp};
+    R fy_b[4] = {-(X[0] - X[1]) * sp, -(X[0] - X[1]) * sp, -(X[2] - X[3]) * sm, -(X[2] - X[3]) * sm};
+    for (int row = 0; row < 2; row++) {
+        R pa = (row == 0 ? sa : -ca) * LA, qb = (row == 0 ? sb : -cb) * LB;
+        for (int k = 0; k < 4; k++) {
+            Bs[row][k][0] = 0;
+            Bs[row][k][1] = 0;
+            Bs[row][k][2] = (pa * fw_a[k] + qb * fw_b[k]) * d16;
+            Bs[row][k][3] = (pa * fx_a[k] + qb * fx_b[k]) * d32;
+            Bs[row][k][4] = (pa * fy_a[k] + qb * fy_b[k]) * d32;
+        }
+    }
+}
+
+// Q4 element-level constants shared by the four quadrature points.
+struct Q4Elem {
+    double Xr[4][3];   // node coordinates relative to the centroid
+    double h2;         // squared diameter (max distance from node 1)
+};
+
+FS_HD void q4_prepare(const ElemIn<4> &in, Q4Elem &qe)
+{
+    double cen[3] = {0, 0, 0};
+    for (int a = 0; a < 4; a++)
+        for (int c = 0; c < 3; c++) cen[c] += in.X[a][c];
+    for (int c = 0; c < 3; c++) cen[c] /= 4;
+    double mx = 0.0;
+    for (int a = 0; a < 4; a++) {
+        for (int c = 0; c < 3; c++) qe.Xr[a][c] = in.X[a][c] - cen[c];
+        if (a > 0) {
+            double dx = in.X[a][0] - in.X[0][0], dy = in.X[a][1] - in.X[0][1], dz = in.X[a][2] - in.X[0][2];
+            double dd = dx * dx + dy * dy + dz * dz;
+            mx = dd > mx ? dd : mx;
+        }
+    }
+    qe.h2 = mx;
+}
+
+// Rows of quadrature point j (8 rows: membrane+bending 6, shear 2) on the
+// global dofs (24 wide), plus this point's contribution to the drilling
+// traces tr(P K_rr P) of each node (src/FEMMShellQ4RSModule.jl:807-838).
+// Returns nonzero on a singular metric (src/FEMMShellQ4RSModule.jl:308-311).
+template <class R, bool COMP>
+FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatConst &mc,
+                        const GroupConst *gc, R *rows, int rs, double trace[4])
+{
+    double xi, eta, gp[4][2];
+    q4_point(j, xi, eta);
+    q4_dbasis(xi, eta, gp);
+    double J0[3], J1[3];
+    for (int c = 0; c < 3; c++) {
+        J0[c] = qe.Xr[0][c] * gp[0][0] + qe.Xr[1][c] * gp[1][0] + qe.Xr[2][c] * gp[2][0] + qe.Xr[3][c] * gp[3][0];
+        J1[c] = qe.Xr[0][c] * gp[0][1] + qe.Xr[1][c] * gp[1][1] + qe.Xr[2][c] * gp[2][1] + qe.Xr[3][c] * gp[3][1];
+    }
+    double nJ[3];
+    cross3(J0, J1, nJ);
+    double Jac = sqrt(dot3(nJ, nJ));
+    double e[3][3];
+    make_frame(J0, J1, e);
+    // element coordinates (centroid relative) and basis gradients
+    R X[4], Y[4];
+    for (int a = 0; a < 4; a++) {
+        X[a] = (R)dot3(qe.Xr[a], e[0]);
+        Y[a] = (R)dot3(qe.Xr[a], e[1]);
+    }
+    R J0r[3] = {(R)J0[0], (R)J0[1], (R)J0[2]}, J1r[3] = {(R)J1[0], (R)J1[1], (R)J1[2]};
+    R G11 = dot3(J0r, J0r), G12 = dot3(J0r, J1r), G22 = dot3(J1r, J1r);
+    R detG = G11 * G22 - G12 * G12;
+    if (detG == (R)0) return 4;
+    R i11 = G22 / detG, i12 = -G12 / detG, i22 = G11 / detG;
+    R e0[3] = {(R)e[0][0], (R)e[0][1], (R)e[0][2]}, e1[3] = {(R)e[1][0], (R)e[1][1], (R)e[1][2]};
+    R g[4][2];
+    // g_a = J invG gradNparams_a, projected on e1, e2
+    R pj0[2] = {dot3(e0, J0r), dot3(e1, J0r)}, pj1[2] = {dot3(e0, J1r), dot3(e1, J1r)};
+    for (int a = 0; a < 4; a++) {
+        R t1 = i11 * (R)gp[a][0] + i12 * (R)gp[a][1];
+        R t2 = i12 * (R)gp[a][0] + i22 * (R)gp[a][1];
+        g[a][0] = pj0[0] * t1 + pj1[0] * t2;
+        g[a][1] = pj0[1] * t1 + pj1[1] * t2;
+    }
+    double A[4][3][3];
+    for (int i = 0; i < 4; i++) nodal_triad(e, in.nrm[i], in.valid[i], A[i]);
+    GlobalMap<R, 4> M;
+    build_map<R, 4>(e, A, g, M);
+    R mb[6][4][5];
+    for (int r = 0; r < 6; r++)
+        for (int i = 0; i < 4; i++)
+            for (int q = 0; q < 5; q++) mb[r][i][q] = 0;
+    for (int i = 0; i < 4; i++) {
+        mb[0][i][0] = g[i][0];
+        mb[1][i][1] = g[i][1];
+        mb[2][i][0] = g[i][1]; mb[2][i][1] = g[i][0];
+        mb[3][i][4] = g[i][0];
+        mb[4][i][3] = -g[i][1];
+        mb[5][i][3] = -g[i][0]; mb[5][i][4] = g[i][1];
+    }
+    R sh[2][4][5];
+    q4_bs<R>(X, Y, (R)xi, (R)eta, sh);
+    double t = COMP ? gc->thickness : in.t;
+    double stab = t * t / (t * t + mc.stab_c * qe.h2);
+    R mixed[8][4][5];
+    if (!COMP) {
+        R inm[3][4][5], inb[3][4][5];
+        for (int r = 0; r < 3; r++)
+            for (int i = 0; i < 4; i++)
+                for (int q = 0; q < 5; q++) { inm[r][i][q] = mb[r][i][q]; inb[r][i][q] = mb[3 + r][i][q]; }
+        mix_rows<R, 4, 3>(mc.Lps, sqrt(t * Jac), inm, (R(*)[4][5])mixed[0]);
+        mix_rows<R, 4, 3>(mc.Lps, sqrt(t * t * t / 12.0 * Jac), inb, (R(*)[4][5])mixed[3]);
+        mix_rows<R, 4, 2>(mc.Lt, sqrt(t * stab * Jac), sh, (R(*)[4][5])mixed[6]);
+    } else {
+        double lm, ln;
+        layup_angle(e, gc->csmat, lm, ln);
+        rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[0]);
+        rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[3]);
+        mix_rows<R, 4, 6>(gc->L6, sqrt(Jac), mb, (R(*)[4][5])mixed[0]);
+        rotate2<R, 4>(lm, ln, sh);
+        mix_rows<R, 4, 2>(gc->LH, sqrt(stab * Jac), sh, (R(*)[4][5])mixed[6]);
+    }
+    for (int r = 0; r < 8; r++) expand_row<R, 4>(M, (const R(*)[5])mixed[r], rows + r * rs);
+    // drilling traces: sum over rows of |b|^2 - (b.n)^2 on the rotation block
+    for (int k = 0; k < 4; k++) {
+        const double *nv = in.nrm[k];
+        double nn = sqrt(dot3(nv, nv));
+        double u[3] = {0, 0, 0};
+        if (nn > 0.0) { u[0] = nv[0] / nn; u[1] = nv[1] / nn; u[2] = nv[2] / nn; }
+        double tr = 0.0;
+        for (int r = 0; r < 8; r++) {
+            const R *o = rows + r * rs + 6 * k + 3;
+            double b0 = o[0], b1 = o[1], b2 = o[2];
+            double bn = b0 * u[0] + b1 * u[1] + b2 * u[2];
+            tr += b0 * b0 + b1 * b1 + b2 * b2 - bn * bn;
+        }
+        trace[k] = tr;
+    }
+    return 0;
+}
+
+// Drilling rows of a Q4 element from the summed traces
+// (src/FEMMShellQ4RSModule.jl:807-859): kavg = scale * mean over nodes with
+// a valid nonzero normal of max(0, tr/2); row k = sqrt(kavg) n_k on the
+// rotations of node k.
+template <class R>
+FS_HD void q4_drill_rows(const ElemIn<4> &in, const double trace[4], double scale, R *rows, int rs)
+{
+    double sum = 0.0;
+    int cnt = 0;
+    bool use[4];
+    for (int k = 0; k < 4; k++) {
+        const double *nv = in.nrm[k];
+        use[k] = in.valid[k] && (sqrt(dot3(nv, nv)) != 0.0);
+        if (use[k]) {
+            double v = trace[k] / 2.0;
+            sum += v > 0.0 ? v : 0.0;
+            cnt++;
+        }
+    }
+    double kavg = (cnt ? sum / cnt : 0.0) * scale;
+    double sk = kavg > 0.0 ? sqrt(kavg) : 0.0;
+    for (int k = 0; k < 4; k++) {
+        R *o = rows + k * rs;
+        for (int q = 0; q < 24; q++) o[q] = 0;
+        if (use[k] && kavg != 0.0)
+            for (int c = 0; c < 3; c++) o[6 * k + 3 + c] = (R)(sk * in.nrm[k][c]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Lumped mass (src/FEMMShellT3FFModule.jl:770-787, src/FEMMShellQ4RSModule.jl:981-997
+// and the layered variants)
+// ---------------------------------------------------------------------------
+template <int NN>
+FS_HD void lumped_mass(const ElemIn<NN> &in, double rho, bool comp, const GroupConst *gc, double &tm, double &rm)
+{
+    double t = comp ? gc->thickness : in.t;
+    if (NN == 3) {
+        double J0[3], J1[3], e[3][3];
+        for (int c = 0; c < 3; c++) {
+            J0[c] = in.X[1][c] - in.X[0][c];
+            J1[c] = in.X[2][c] - in.X[0][c];
+        }
+        make_frame(J0, J1, e);
+        double a = dot3(J0, e[0]), b = dot3(J0, e[1]), c = dot3(J1, e[0]), d = dot3(J1, e[1]);
+        double Ae = (a * d - b * c) / 2;
+        if (comp) {
+            tm = gc->mass * (Ae / 3);
+            rm = gc->moi * (Ae / 3);
+        } else {
+            tm = rho * (t * Ae) / 3;
+            rm = rho * (t * t * t / 12 * Ae) / 3;
+        }
+    } else {
+        double ts = 0.0, rs = 0.0;
+        for (int j = 0; j < 4; j++) {
+            double xi, eta, gp[4][2];
+            q4_point(j, xi, eta);
+            q4_dbasis(xi, eta, gp);
+            double J0[3] = {0, 0, 0}, J1[3] = {0, 0, 0};
+            for (int a = 0; a < 4; a++)
+                for (int c = 0; c < 3; c++) {
+                    J0[c] += in.X[a][c] * gp[a][0];
+                    J1[c] += in.X[a][c] * gp[a][1];
+                }
+            double nJ[3];
+            cross3(J0, J1, nJ);
+            double Jac = sqrt(dot3(nJ, nJ));
+            if (comp) {
+                ts += gc->mass * Jac;
+                rs += gc->moi * Jac;
+            } else {
+                ts += rho * t * Jac;
+                rs += rho * t * t * t / 12 * Jac;
+            }
+        }
+        tm = ts / 4;
+        rm = rs / 4;
+    }
+}
+
+}  // namespace fs

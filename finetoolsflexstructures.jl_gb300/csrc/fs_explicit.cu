@@ -1,0 +1,203 @@
+// Explicit central-difference time stepping
+// (examples/shells/dynamics/homogeneous/explicit/plate_expl_examples.jl:61-94,
+// _cd_loop!, with mass-proportional damping C and zero external force):
+//
+//   U += dt V + dt^2/2 A;  E = K U;  F = -(E + C (V + dt/2 A));
+//   V += dt/2 A;  A = invMC F;  V += dt/2 A
+//
+// Two kernels per step: the displacement update, then a row-parallel CSR
+// product fused with the force, acceleration and velocity updates of the
+// row.  The displacement and velocity sums carry Kahan compensation terms so
+// that a long run in double does not drift.  Stiffness values are read as
+// double (FS_FP64) or float (FS_MIXED).  The step loop is captured once into
+// a CUDA graph and replayed.
+#include <algorithm>
+
+#include "fs_internal.cuh"
+
+namespace fs {
+
+static const int CD_TPB = 256;
+static const int CD_LANES = 8;  // lanes per CSR row
+static const int CD_GRAPH_STEPS = 64;
+
+__global__ void k_cd_disp(int64_t n, double dt, double dt2_2, double *U, double *cU, const double *V,
+                          const double *A)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double y = (dt * V[i] + dt2_2 * A[i]) - cU[i];
+    double u = U[i];
+    double t = u + y;
+    cU[i] = (t - u) - y;
+    U[i] = t;
+}
+
+__device__ __forceinline__ void kahan_add(double &s, double &c, double incr)
+{
+    double y = incr - c;
+    double t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+template <class VT>
+__global__ void __launch_bounds__(CD_TPB) k_cd_rows(int64_t n, const int64_t *rowptr, const int32_t *colidx,
+                                                  const VT *vals, const double *U, double *V, double *cV,
+                                                  double *A, const double *C, const double *invMC, double dt_2)
+{
+    int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / CD_LANES;
+    const int sub = threadIdx.x & (CD_LANES - 1);
+    const unsigned mask = 0xffffffffu;
+    double s = 0.0;
+    if (row < n) {
+        for (int64_t k = rowptr[row] + sub; k < rowptr[row + 1]; k += CD_LANES)
+            s += (double)vals[k] * U[colidx[k]];
+    }
+#pragma unroll
+    for (int o = CD_LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(mask, s, o);
+    if (row < n && sub == 0) {
+        double a = A[row], v = V[row], cv = cV[row];
+        double f = -(s + C[row] * (v + dt_2 * a));
+        kahan_add(v, cv, dt_2 * a);
+        a = invMC[row] * f;
+        kahan_add(v, cv, dt_2 * a);
+        A[row] = a;
+        V[row] = v;
+        cV[row] = cv;
+    }
+}
+
+static int enqueue_steps(fs_ctx *c, int64_t nsteps)
+{
+    auto &x = c->ex;
+    int64_t n = x.n;
+    double dt = x.dt;
+    unsigned g1 = (unsigned)((n + CD_TPB - 1) / CD_TPB);
+    unsigned g2 = (unsigned)((n * CD_LANES + CD_TPB - 1) / CD_TPB);
+    for (int64_t s = 0; s < nsteps; s++) {
+        k_cd_disp<<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A);
+        if (x.precision == FS_FP64)
+            k_cd_rows<double><<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, c->vals, x.U, x.V,
+                                                            x.cV, x.A, x.C, x.invMC, dt / 2);
+        else
+            k_cd_rows<float><<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, x.vals32, x.U, x.V,
+                                                           x.cV, x.A, x.C, x.invMC, dt / 2);
+    }
+    return cuda_check(c, cudaGetLastError(), "explicit step launch");
+}
+
+int explicit_launch_steps(fs_ctx *c, int64_t nsteps)
+{
+    auto &x = c->ex;
+    if (nsteps <= 0) return FS_OK;
+    if (!x.exec) {
+        FS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int st = enqueue_steps(c, CD_GRAPH_STEPS);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (st != FS_OK) return st;
+        FS_CUDA(c, e);
+        x.graph = g;
+        FS_CUDA(c, cudaGraphInstantiate(&x.exec, g, 0));
+        x.graph_steps = CD_GRAPH_STEPS;
+    }
+    int64_t full = nsteps / x.graph_steps, rest = nsteps % x.graph_steps;
+    for (int64_t k = 0; k < full; k++) FS_CUDA(c, cudaGraphLaunch(x.exec, c->stream));
+    FS_TRY(enqueue_steps(c, rest));
+    return FS_OK;
+}
+
+__global__ void k_to_float(int64_t n, const double *src, float *dst)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
+}
+
+}  // namespace fs
+
+using namespace fs;
+
+extern "C" {
+
+int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const double *C, double dt)
+{
+    if (!c || !invMC || !C) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    if (!c->mat_rowptr) return set_err(c, FS_ERR_STATE, "no stiffness assembled");
+    if (precision != FS_FP64 && precision != FS_MIXED) return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
+    if (!(dt > 0.0)) return set_err(c, FS_ERR_BAD_INPUT, "time step must be positive");
+    auto &x = c->ex;
+    if (x.exec) cudaGraphExecDestroy(x.exec);
+    if (x.graph) cudaGraphDestroy(x.graph);
+    x.exec = nullptr;
+    x.graph = nullptr;
+    int64_t n = c->mat_n;
+    x.n = n;
+    x.dt = dt;
+    x.precision = precision;
+    FS_TRY(dalloc(c, &x.U, (size_t)n)); FS_TRY(dalloc(c, &x.V, (size_t)n)); FS_TRY(dalloc(c, &x.A, (size_t)n));
+    FS_TRY(dalloc(c, &x.cU, (size_t)n)); FS_TRY(dalloc(c, &x.cV, (size_t)n));
+    FS_TRY(dalloc(c, &x.invMC, (size_t)n)); FS_TRY(dalloc(c, &x.C, (size_t)n));
+    size_t bn = sizeof(double) * (size_t)std::max<int64_t>(n, 1);
+    FS_CUDA(c, cudaMemsetAsync(x.U, 0, bn, c->stream));
+    FS_CUDA(c, cudaMemsetAsync(x.V, 0, bn, c->stream));
+    FS_CUDA(c, cudaMemsetAsync(x.A, 0, bn, c->stream));
+    FS_CUDA(c, cudaMemsetAsync(x.cU, 0, bn, c->stream));
+    FS_CUDA(c, cudaMemsetAsync(x.cV, 0, bn, c->stream));
+    FS_CUDA(c, cudaMemcpyAsync(x.invMC, invMC, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    FS_CUDA(c, cudaMemcpyAsync(x.C, C, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    if (precision == FS_MIXED) {
+        FS_TRY(dalloc(c, &x.vals32, (size_t)c->mat_nnz));
+        if (c->mat_nnz)
+            k_to_float<<<(unsigned)((c->mat_nnz + 255) / 256), 256, 0, c->stream>>>(c->mat_nnz, c->vals, x.vals32);
+        FS_CUDA(c, cudaGetLastError());
+    }
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    x.ready = true;
+    return FS_OK;
+}
+
+int fs_explicit_set_state(fs_ctx *c, const double *U, const double *V, const double *A)
+{
+    if (!c) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    auto &x = c->ex;
+    if (!x.ready) return set_err(c, FS_ERR_STATE, "call fs_explicit_setup first");
+    size_t bn = sizeof(double) * (size_t)x.n;
+    if (U) FS_CUDA(c, cudaMemcpyAsync(x.U, U, bn, cudaMemcpyHostToDevice, c->stream));
+    if (V) FS_CUDA(c, cudaMemcpyAsync(x.V, V, bn, cudaMemcpyHostToDevice, c->stream));
+    if (A) FS_CUDA(c, cudaMemcpyAsync(x.A, A, bn, cudaMemcpyHostToDevice, c->stream));
+    if (bn) {
+        FS_CUDA(c, cudaMemsetAsync(x.cU, 0, bn, c->stream));
+        FS_CUDA(c, cudaMemsetAsync(x.cV, 0, bn, c->stream));
+    }
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FS_OK;
+}
+
+int fs_explicit_run(fs_ctx *c, int64_t nsteps)
+{
+    if (!c || nsteps < 0) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    if (!c->ex.ready) return set_err(c, FS_ERR_STATE, "call fs_explicit_setup first");
+    FS_TRY(explicit_launch_steps(c, nsteps));
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FS_OK;
+}
+
+int fs_explicit_get_state(fs_ctx *c, double *U, double *V, double *A)
+{
+    if (!c) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    auto &x = c->ex;
+    if (!x.ready) return set_err(c, FS_ERR_STATE, "call fs_explicit_setup first");
+    size_t bn = sizeof(double) * (size_t)x.n;
+    if (U) FS_CUDA(c, cudaMemcpyAsync(U, x.U, bn, cudaMemcpyDeviceToHost, c->stream));
+    if (V) FS_CUDA(c, cudaMemcpyAsync(V, x.V, bn, cudaMemcpyDeviceToHost, c->stream));
+    if (A) FS_CUDA(c, cudaMemcpyAsync(A, x.A, bn, cudaMemcpyDeviceToHost, c->stream));
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,182 @@
+// Internal declarations of the flexshell CUDA library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/flexshell.h"
+#include "fs_elem_math.cuh"
+
+namespace fs {
+
+// Device arrays owned by a context.  Sizes are in elements.
+template <class T> struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+};
+
+// Status bits written by kernels (never trapping; the host turns them into codes).
+enum : int {
+    DEV_OK = 0,
+    DEV_BAD_CONN = 1,
+    DEV_BAD_DOF = 2,
+    DEV_SINGULAR = 4,
+    DEV_VALENCE = 8,     // too many elements at one node
+    DEV_NEIGHBORS = 16,  // too many neighbour nodes
+    DEV_BAD_ORDER = 32,
+    DEV_NEG_DRILL = 64,
+};
+
+static const int MAX_PAIRS_PER_NODE = 64;   // elements meeting at one node
+static const int MAX_NBRS = 255;            // neighbour nodes of one node (slots are 8-bit)
+static const int GATHER_LMAX = 120;         // row length held in shared memory by the gather
+
+struct MeshDev {
+    int etype = -1, nen = 0;
+    int64_t nnodes = 0, nelem = 0;
+    double *xyz = nullptr;       // 3 x nnodes (SoA, Julia column-major)
+    int32_t *conn = nullptr;     // nelem x nen, by assembly rank, 0-based
+    int32_t *elem_of_rank = nullptr;  // rank -> mesh element
+    int32_t *dof = nullptr;      // 6 x nnodes (SoA), 1-based as given
+    double *thick = nullptr;     // per rank
+    int32_t *group = nullptr;    // per rank
+    GroupConst *groups = nullptr;
+    int ngroups = 0;
+    double *normals = nullptr;   // 3 x nnodes
+    uint8_t *valid = nullptr;
+    // node -> (element rank, local node) adjacency, ascending rank
+    int64_t npairs = 0;
+    int64_t *pp = nullptr;       // nnodes + 1
+    int32_t *pair_e = nullptr;   // rank << 2 | local node
+    int32_t *elem_pair = nullptr;  // per rank x nen: pair index
+};
+
+struct PatternDev {
+    int64_t n = -1;              // matrix size the pattern is built for
+    int64_t nnz = 0;
+    int64_t *nbr_off = nullptr;  // nnodes + 1
+    int32_t *nbr = nullptr;      // neighbour nodes, sorted
+    uint32_t *pair_slots = nullptr;  // per pair: 8-bit slot of each element node
+    int16_t *colpos = nullptr;   // per node: 6 x nnbr positions in the row (or -1)
+    int32_t *rowlen = nullptr;   // per node: row length L
+    int64_t *rowptr = nullptr;   // n + 1
+    int32_t *colidx = nullptr;   // nnz, 0-based
+    int64_t *diag_rowptr = nullptr;  // diagonal pattern (n + 1)
+    int32_t *diag_colidx = nullptr;  // n
+};
+
+}  // namespace fs
+
+struct fs_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int *d_status = nullptr;     // kernel status bits
+    fs::MeshDev mesh;
+    fs_shell_params params{};
+    fs::MatConst mc{};
+    bool params_set = false;
+    bool normals_ready = false;
+    bool dofs_ready = false;
+    fs::PatternDev pat;
+    // element matrices (block layout), element masses
+    void *ke = nullptr;
+    size_t ke_bytes = 0;
+    double *tmrm = nullptr;
+    // current matrix
+    int64_t mat_n = 0, mat_nnz = 0;
+    const int64_t *mat_rowptr = nullptr;
+    const int32_t *mat_colidx = nullptr;
+    double *vals = nullptr;
+    size_t vals_cap = 0;
+    // compacted pattern (assembler dropping zeros)
+    int64_t *cmp_rowptr = nullptr;
+    int32_t *cmp_colidx = nullptr;
+    double *cmp_vals = nullptr;
+    size_t cmp_cap = 0;
+    // phase timing events: element start/end, gather end, compaction end
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double t_symbolic_ms = 0.0;
+    double t_compact_ms = 0.0;
+    bool timed = false;
+    // scratch
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    // staging for host copies
+    int64_t *stage64 = nullptr;
+    size_t stage_cap = 0;
+    // host copies re-applied when the mesh changes
+    std::vector<double> h_thickness;
+    std::vector<fs_layup_group> h_groups;
+    std::vector<int32_t> h_egroup;
+    // explicit dynamics
+    struct Explicit {
+        int precision = 0;
+        int64_t n = 0;
+        double dt = 0;
+        double *U = nullptr, *V = nullptr, *A = nullptr, *F = nullptr;
+        double *cU = nullptr, *cV = nullptr;  // Kahan compensations
+        double *invMC = nullptr, *C = nullptr;
+        float *vals32 = nullptr;
+        bool ready = false;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        int64_t graph_steps = 0;
+    } ex;
+};
+
+namespace fs {
+
+// launchers (defined in the .cu files)
+int launch_prepare_mesh(fs_ctx *c, const int64_t *d_conn_raw, const int64_t *d_order_raw,
+                        const int64_t *d_dof_raw);
+int launch_prepare_dofs(fs_ctx *c, const int64_t *d_dof_raw);
+int build_adjacency(fs_ctx *c);
+int build_pattern(fs_ctx *c, int64_t n);
+int launch_normals(fs_ctx *c);
+int launch_elements(fs_ctx *c, int precision);
+int launch_gather(fs_ctx *c, int precision, double *vals);
+int launch_masses(fs_ctx *c);
+int assemble_mass(fs_ctx *c, int assembler, int64_t n);
+int compact_zeros(fs_ctx *c, int64_t n, const int64_t *rowptr, const int32_t *colidx,
+                  const double *vals, int64_t nnz);
+int exclusive_scan_i64(fs_ctx *c, const int64_t *in, int64_t *out, int64_t n, int64_t *total);
+int ensure_scratch(fs_ctx *c, size_t bytes);
+int read_status(fs_ctx *c, int *bits);
+
+int explicit_launch_steps(fs_ctx *c, int64_t nsteps);
+
+// helpers
+int set_err(fs_ctx *c, int code, const std::string &msg);
+int cuda_check(fs_ctx *c, cudaError_t e, const char *what);
+template <class T> int dalloc(fs_ctx *c, T **p, size_t n)
+{
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return set_err(c, FS_ERR_OOM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+    }
+    return FS_OK;
+}
+template <class T> void dfree(T **p)
+{
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+}
+
+}  // namespace fs
+
+#define FS_TRY(x)                 \
+    do {                          \
+        int _s = (x);             \
+        if (_s != FS_OK) return _s; \
+    } while (0)
+#define FS_CUDA(c, call) FS_TRY(fs::cuda_check((c), (call), #call))

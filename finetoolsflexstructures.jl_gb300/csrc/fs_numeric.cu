@@ -1,0 +1,516 @@
+// Numeric phase: nodal normals, element matrices, the deterministic CSR
+// value gather and the lumped mass.
+//
+// Element matrices.  One thread owns one T3 element (or one quadrature point
+// of a Q4 element, four lanes per element).  It writes the element's Gram
+// rows (csrc/fs_elem_math.cuh) into its own slice of shared memory and then
+// forms K = Bh^T Bh as 6x6 node blocks, writing each upper block and its
+// transpose.  Element matrices are stored by assembly rank as nen x nen
+// blocks of 6x6 (row-major inside a block), so the six rows a node owns in
+// an element are one contiguous slab of nen*36 values.
+//
+// Gather.  One warp owns one node, i.e. the six CSR rows of its dofs.  It
+// walks the node's (element, local node) pairs in ascending assembly rank
+// and adds each slab into a double accumulator, so every CSR value is the
+// left-to-right sum of its element contributions in assembly order, as
+// Julia's sparse(I, J, V) combines duplicates.  No atomics: the result is
+// bitwise reproducible.
+#include "fs_internal.cuh"
+
+namespace fs {
+
+static unsigned nblk2(int64_t n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
+
+template <int NN>
+__device__ __forceinline__ void load_elem(const MeshDev &m, int64_t r, ElemIn<NN> &in)
+{
+    for (int a = 0; a < NN; a++) {
+        int node = m.conn[r * NN + a];
+        for (int c = 0; c < 3; c++) {
+            in.X[a][c] = m.xyz[(int64_t)c * m.nnodes + node];
+            in.nrm[a][c] = m.normals[(int64_t)c * m.nnodes + node];
+        }
+        in.valid[a] = m.valid[node] != 0;
+    }
+    in.t = m.thick ? m.thick[r] : 0.0;
+    in.group = m.group ? m.group[r] : 0;
+}
+
+// ---------------------------------------------------------------------------
+// element kernels
+// ---------------------------------------------------------------------------
+template <class R, int NN>
+__device__ __forceinline__ void write_blocks(const R *rows, int nrows, R *out)
+{
+    const int ND = 6 * NN;
+    for (int a = 0; a < NN; a++)
+        for (int b = a; b < NN; b++) {
+            R acc[6][6];
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+#pragma unroll
+                for (int j = 0; j < 6; j++) acc[i][j] = 0;
+            for (int rho = 0; rho < nrows; rho++) {
+                const R *rr = rows + rho * ND;
+                R ra[6], rb[6];
+#pragma unroll
+                for (int i = 0; i < 6; i++) {
+                    ra[i] = rr[6 * a + i];
+                    rb[i] = rr[6 * b + i];
+                }
+#pragma unroll
+                for (int i = 0; i < 6; i++)
+#pragma unroll
+                    for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
+            }
+            R *oab = out + (a * NN + b) * 36;
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+#pragma unroll
+                for (int j = 0; j < 6; j++) oab[i * 6 + j] = acc[i][j];
+            if (a != b) {
+                R *oba = out + (b * NN + a) * 36;
+#pragma unroll
+                for (int j = 0; j < 6; j++)
+#pragma unroll
+                    for (int i = 0; i < 6; i++) oba[j * 6 + i] = acc[i][j];
+            }
+        }
+}
+
+template <class R, bool COMP, bool AVGK, int EPB>
+__global__ void __launch_bounds__(EPB) k_t3_elements(const MeshDev m, const MatConst mc, R *ke, int *status)
+{
+    constexpr int NR = T3Rows<AVGK>::N;
+    constexpr int ND = 18;
+    constexpr int STRIDE = NR * ND + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *rows = reinterpret_cast<R *>(smem_raw) + threadIdx.x * STRIDE;
+    int64_t r = (int64_t)blockIdx.x * EPB + threadIdx.x;
+    if (r >= m.nelem) return;
+    ElemIn<3> in;
+    load_elem<3>(m, r, in);
+    const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
+    int st = t3_rows<R, COMP, AVGK>(in, mc, gc, rows, ND);
+    if (st) atomicOr(status, DEV_NEG_DRILL);
+    write_blocks<R, 3>(rows, NR, ke + r * (ND * ND));
+}
+
+template <class R, bool COMP, int EPB>
+__global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const MatConst mc, R *ke, int *status)
+{
+    constexpr int NR = 36, ND = 24, STRIDE = NR * ND + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int el = threadIdx.x >> 2, qp = threadIdx.x & 3;
+    R *rows = reinterpret_cast<R *>(smem_raw) + el * STRIDE;
+    int64_t r = (int64_t)blockIdx.x * EPB + el;
+    const bool active = r < m.nelem;
+    ElemIn<4> in;
+    double tr[4] = {0, 0, 0, 0};
+    if (active) {
+        load_elem<4>(m, r, in);
+        const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
+        Q4Elem qe;
+        q4_prepare(in, qe);
+        int st = q4_point_rows<R, COMP>(in, qe, qp, mc, gc, rows + qp * 8 * ND, ND, tr);
+        if (st) {
+            atomicOr(status, DEV_SINGULAR);
+            for (int k = 0; k < 4; k++) tr[k] = 0.0;
+        }
+    }
+    // sum the drilling traces of the four quadrature points (lanes 4el..4el+3)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], 1);
+        tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], 2);
+    }
+    if (active && qp == 0) q4_drill_rows<R>(in, tr, mc.drill_scale, rows + 32 * ND, ND);
+    __syncwarp();
+    if (!active) return;
+    R *out = ke + r * (ND * ND);
+    // ten upper node blocks shared by the four lanes of the element
+    for (int bi = qp; bi < 10; bi += 4) {
+        int a = bi < 4 ? 0 : (bi < 7 ? 1 : (bi < 9 ? 2 : 3));
+        int b = a + (bi - (a == 0 ? 0 : (a == 1 ? 4 : (a == 2 ? 7 : 9))));
+        R acc[6][6];
+#pragma unroll
+        for (int i = 0; i < 6; i++)
+#pragma unroll
+            for (int j = 0; j < 6; j++) acc[i][j] = 0;
+        for (int rho = 0; rho < NR; rho++) {
+            const R *rr = rows + rho * ND;
+            R ra[6], rb[6];
+#pragma unroll
+            for (int i = 0; i < 6; i++) {
+                ra[i] = rr[6 * a + i];
+                rb[i] = rr[6 * b + i];
+            }
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+#pragma unroll
+                for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
+        }
+        R *oab = out + (a * 4 + b) * 36;
+#pragma unroll
+        for (int i = 0; i < 6; i++)
+#pragma unroll
+            for (int j = 0; j < 6; j++) oab[i * 6 + j] = acc[i][j];
+        if (a != b) {
+            R *oba = out + (b * 4 + a) * 36;
+#pragma unroll
+            for (int j = 0; j < 6; j++)
+#pragma unroll
+                for (int i = 0; i < 6; i++) oba[j * 6 + i] = acc[i][j];
+        }
+    }
+}
+
+template <class R, bool COMP, bool AVGK>
+static int run_t3(fs_ctx *c, R *ke)
+{
+    constexpr int EPB = (sizeof(R) == 8 && AVGK) ? 64 : 128;
+    constexpr int NR = T3Rows<AVGK>::N;
+    size_t smem = sizeof(R) * (size_t)EPB * (NR * 18 + 1);
+    auto kern = k_t3_elements<R, COMP, AVGK, EPB>;
+    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<nblk2(c->mesh.nelem, EPB), EPB, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+template <class R, bool COMP>
+static int run_q4(fs_ctx *c, R *ke)
+{
+    constexpr int EPB = 32;
+    size_t smem = sizeof(R) * (size_t)EPB * (36 * 24 + 1);
+    auto kern = k_q4_elements<R, COMP, EPB>;
+    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<nblk2(c->mesh.nelem, EPB), EPB * 4, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+int launch_elements(fs_ctx *c, int precision)
+{
+    MeshDev &m = c->mesh;
+    size_t nd = 6 * m.nen;
+    size_t bytes = (size_t)m.nelem * nd * nd * (precision == FS_FP64 ? 8 : 4);
+    if (bytes > c->ke_bytes) {
+        if (c->ke) cudaFree(c->ke);
+        c->ke = nullptr;
+        c->ke_bytes = 0;
+        cudaError_t e = cudaMalloc(&c->ke, bytes ? bytes : 16);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(c, FS_ERR_OOM, "device allocation of element matrices failed");
+        }
+        c->ke_bytes = bytes;
+    }
+    if (m.nelem == 0) return FS_OK;
+    bool comp = (m.etype == FS_T3FFCOMP || m.etype == FS_Q4RSCOMP);
+    bool avgk = c->params.transv_shear_formulation == 1;
+    if (m.nen == 3) {
+        if (precision == FS_FP64) {
+            double *k = (double *)c->ke;
+            if (comp) return avgk ? run_t3<double, true, true>(c, k) : run_t3<double, true, false>(c, k);
+            return avgk ? run_t3<double, false, true>(c, k) : run_t3<double, false, false>(c, k);
+        }
+        float *k = (float *)c->ke;
+        if (comp) return avgk ? run_t3<float, true, true>(c, k) : run_t3<float, true, false>(c, k);
+        return avgk ? run_t3<float, false, true>(c, k) : run_t3<float, false, false>(c, k);
+    }
+    if (precision == FS_FP64) {
+        double *k = (double *)c->ke;
+        return comp ? run_q4<double, true>(c, k) : run_q4<double, false>(c, k);
+    }
+    float *k = (float *)c->ke;
+    return comp ? run_q4<float, true>(c, k) : run_q4<float, false>(c, k);
+}
+
+// ---------------------------------------------------------------------------
+// gather into CSR values
+// ---------------------------------------------------------------------------
+static const int GATHER_WARPS = 8;
+
+template <class R>
+__global__ void __launch_bounds__(GATHER_WARPS * 32)
+    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
+{
+    __shared__ double acc_all[GATHER_WARPS][6 * GATHER_LMAX];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t r = (int64_t)blockIdx.x * GATHER_WARPS + w;
+    if (r >= m.nnodes) return;
+    const int nen = m.nen, nd = 6 * nen, slab = nen * 36;
+    int32_t d[6];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        d[k] = m.dof[(int64_t)k * m.nnodes + r];
+        any |= (d[k] <= n);
+    }
+    if (!any) return;
+    const int L = P.rowlen[r];
+    const int64_t off6 = P.nbr_off[r] * 6;
+    const int64_t pb = m.pp[r], pe = m.pp[r + 1];
+    if (L <= GATHER_LMAX) {
+        double *acc = acc_all[w];
+        for (int i = lane; i < 6 * GATHER_LMAX; i += 32) acc[i] = 0.0;
+        __syncwarp();
+        for (int64_t p = pb; p < pe; p++) {
+            int32_t pe_ = m.pair_e[p];
+            int64_t rank = pe_ >> 2;
+            int a = pe_ & 3;
+            uint32_t slots = P.pair_slots[p];
+            const R *src = ke + rank * (int64_t)(nd * nd) + a * slab;
+            for (int idx = lane; idx < slab; idx += 32) {
+                int b = idx / 36, rem = idx - 36 * b, krow = rem / 6, kc = rem - 6 * krow;
+                int s = (slots >> (8 * b)) & 0xff;
+                int cp = P.colpos[off6 + s * 6 + kc];
+                if (cp >= 0 && d[krow] <= n) acc[krow * GATHER_LMAX + cp] += (double)src[idx];
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            if (d[k] > n) continue;
+            double *o = vals + P.rowptr[d[k] - 1];
+            for (int j = lane; j < L; j += 32) o[j] = acc[k * GATHER_LMAX + j];
+        }
+    } else {
+        // long rows: accumulate in place in the rows this warp owns
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            if (d[k] > n) continue;
+            double *o = vals + P.rowptr[d[k] - 1];
+            for (int j = lane; j < L; j += 32) o[j] = 0.0;
+        }
+        __syncwarp();
+        for (int64_t p = pb; p < pe; p++) {
+            int32_t pe_ = m.pair_e[p];
+            int64_t rank = pe_ >> 2;
+            int a = pe_ & 3;
+            uint32_t slots = P.pair_slots[p];
+            const R *src = ke + rank * (int64_t)(nd * nd) + a * slab;
+            for (int idx = lane; idx < slab; idx += 32) {
+                int b = idx / 36, rem = idx - 36 * b, krow = rem / 6, kc = rem - 6 * krow;
+                int s = (slots >> (8 * b)) & 0xff;
+                int cp = P.colpos[off6 + s * 6 + kc];
+                if (cp >= 0 && d[krow] <= n) {
+                    double *o = vals + P.rowptr[d[krow] - 1] + cp;
+                    *o += (double)src[idx];
+                }
+            }
+            __threadfence_block();
+            __syncwarp();
+        }
+    }
+}
+
+int launch_gather(fs_ctx *c, int precision, double *vals)
+{
+    MeshDev &m = c->mesh;
+    if (m.nnodes == 0) return FS_OK;
+    unsigned g = nblk2(m.nnodes, GATHER_WARPS);
+    if (precision == FS_FP64)
+        k_gather<double><<<g, GATHER_WARPS * 32, 0, c->stream>>>(m, c->pat, c->pat.n, (const double *)c->ke, vals);
+    else
+        k_gather<float><<<g, GATHER_WARPS * 32, 0, c->stream>>>(m, c->pat, c->pat.n, (const float *)c->ke, vals);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// nodal normals (associategeometry!)
+// ---------------------------------------------------------------------------
+template <int NN>
+__device__ void elem_node_normal(const MeshDev &m, int64_t rank, int a, bool comp, double nn[3])
+{
+    double X[NN][3];
+    for (int q = 0; q < NN; q++) {
+        int node = m.conn[rank * NN + q];
+        for (int c = 0; c < 3; c++) X[q][c] = m.xyz[(int64_t)c * m.nnodes + node];
+    }
+    double J0[3], J1[3], jac = 1.0;
+    if (NN == 3) {
+        for (int c = 0; c < 3; c++) {
+            J0[c] = X[1][c] - X[0][c];
+            J1[c] = X[2][c] - X[0][c];
+        }
+    } else {
+        const double xs[4] = {-1, 1, 1, -1}, ys[4] = {-1, -1, 1, 1};
+        double gp[4][2];
+        q4_dbasis(xs[a], ys[a], gp);
+        for (int c = 0; c < 3; c++) {
+            J0[c] = 0;
+            J1[c] = 0;
+            for (int q = 0; q < NN; q++) {
+                J0[c] += X[q][c] * gp[q][0];
+                J1[c] += X[q][c] * gp[q][1];
+            }
+        }
+        double cr[3];
+        cross3(J0, J1, cr);
+        jac = sqrt(dot3(cr, cr));
+    }
+    if (comp) {
+        const double *cs = m.groups[m.group[rank]].csmat;
+        for (int c = 0; c < 3; c++) nn[c] = jac * cs[6 + c];
+    } else {
+        double e[3][3];
+        make_frame(J0, J1, e);
+        for (int c = 0; c < 3; c++) nn[c] = jac * e[2][c];
+    }
+}
+
+template <int NN>
+__global__ void k_normals(const MeshDev m, bool comp, double cos_thr, double *normals, uint8_t *valid)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m.nnodes) return;
+    double s[3] = {0, 0, 0};
+    for (int64_t p = m.pp[r]; p < m.pp[r + 1]; p++) {
+        int32_t v = m.pair_e[p];
+        double nn[3];
+        elem_node_normal<NN>(m, v >> 2, v & 3, comp, nn);
+        for (int c = 0; c < 3; c++) s[c] += nn[c];
+    }
+    double len = sqrt(dot3(s, s));
+    if (len > 0.0)
+        for (int c = 0; c < 3; c++) s[c] /= len;
+    bool ok = true;
+    for (int64_t p = m.pp[r]; p < m.pp[r + 1]; p++) {
+        int32_t v = m.pair_e[p];
+        double nn[3];
+        elem_node_normal<NN>(m, v >> 2, v & 3, comp, nn);
+        if (NN == 4) {  // the validity test uses the unit normal at the node
+            double l = sqrt(dot3(nn, nn));
+            if (l > 0.0)
+                for (int c = 0; c < 3; c++) nn[c] /= l;
+        }
+        if (dot3(s, nn) < cos_thr) ok = false;
+    }
+    for (int c = 0; c < 3; c++) normals[(int64_t)c * m.nnodes + r] = s[c];
+    valid[r] = ok ? 1 : 0;
+}
+
+int launch_normals(fs_ctx *c)
+{
+    MeshDev &m = c->mesh;
+    if (m.nnodes == 0) return FS_OK;
+    double th = c->params.threshold_angle;
+    double sn = sin(th / 180.0 * M_PI);
+    double ntol = 1 - sqrt(1 - sn * sn);
+    double cos_thr = 1 - ntol;
+    bool comp = (m.etype == FS_T3FFCOMP || m.etype == FS_Q4RSCOMP);
+    if (m.nen == 3)
+        k_normals<3><<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, comp, cos_thr, m.normals, m.valid);
+    else
+        k_normals<4><<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, comp, cos_thr, m.normals, m.valid);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// lumped mass
+// ---------------------------------------------------------------------------
+template <int NN>
+__global__ void k_masses(const MeshDev m, double rho, bool comp, double *tmrm)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m.nelem) return;
+    ElemIn<NN> in;
+    for (int a = 0; a < NN; a++) {
+        int node = m.conn[r * NN + a];
+        for (int c = 0; c < 3; c++) in.X[a][c] = m.xyz[(int64_t)c * m.nnodes + node];
+    }
+    in.t = m.thick ? m.thick[r] : 0.0;
+    const GroupConst *gc = comp ? &m.groups[m.group[r]] : nullptr;
+    double tm, rm;
+    lumped_mass<NN>(in, rho, comp, gc, tm, rm);
+    tmrm[2 * r] = tm;
+    tmrm[2 * r + 1] = rm;
+}
+
+int launch_masses(fs_ctx *c)
+{
+    MeshDev &m = c->mesh;
+    FS_TRY(dalloc(c, &c->tmrm, (size_t)(2 * m.nelem)));
+    if (m.nelem == 0) return FS_OK;
+    bool comp = (m.etype == FS_T3FFCOMP || m.etype == FS_Q4RSCOMP);
+    if (m.nen == 3)
+        k_masses<3><<<nblk2(m.nelem, 128), 128, 0, c->stream>>>(m, c->params.rho, comp, c->tmrm);
+    else
+        k_masses<4><<<nblk2(m.nelem, 128), 128, 0, c->stream>>>(m, c->params.rho, comp, c->tmrm);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+// Diagonal mass values: node sums in assembly order.  `diag_pos` selects the
+// destination: the diagonal pattern (value index d-1) or the position of the
+// diagonal entry inside the full pattern.
+__global__ void k_mass_assemble(const MeshDev m, const PatternDev P, int64_t n, const double *tmrm,
+                                bool full_pattern, double *vals)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m.nnodes) return;
+    double tsum = 0.0, rsum = 0.0;
+    for (int64_t p = m.pp[r]; p < m.pp[r + 1]; p++) {
+        int64_t rank = m.pair_e[p] >> 2;
+        tsum += tmrm[2 * rank];
+        rsum += tmrm[2 * rank + 1];
+    }
+    int self = -1;
+    if (full_pattern) {
+        int64_t off = P.nbr_off[r];
+        int nn = (int)(P.nbr_off[r + 1] - off);
+        int lo = 0, hi = nn - 1;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (P.nbr[off + mid] < r) lo = mid + 1; else hi = mid;
+        }
+        self = lo;
+    }
+    for (int k = 0; k < 6; k++) {
+        int32_t d = m.dof[(int64_t)k * m.nnodes + r];
+        if (d > n) continue;
+        double v = k < 3 ? tsum : rsum;
+        if (full_pattern) {
+            int cp = P.colpos[P.nbr_off[r] * 6 + self * 6 + k];
+            vals[P.rowptr[d - 1] + cp] = v;
+        } else {
+            vals[d - 1] = v;
+        }
+    }
+}
+
+int assemble_mass(fs_ctx *c, int assembler, int64_t n)
+{
+    MeshDev &m = c->mesh;
+    PatternDev &P = c->pat;
+    bool full = (assembler == FS_ASM_SPARSE);
+    int64_t nnz = full ? P.nnz : n;
+    if ((size_t)nnz > c->vals_cap || !c->vals) {
+        FS_TRY(dalloc(c, &c->vals, (size_t)nnz));
+        c->vals_cap = (size_t)nnz;
+    }
+    FS_CUDA(c, cudaMemsetAsync(c->vals, 0, sizeof(double) * std::max<int64_t>(nnz, 1), c->stream));
+    if (m.nnodes)
+        k_mass_assemble<<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, P, n, c->tmrm, full, c->vals);
+    FS_CUDA(c, cudaGetLastError());
+    c->mat_n = n;
+    if (full) {
+        c->mat_rowptr = P.rowptr;
+        c->mat_colidx = P.colidx;
+        c->mat_nnz = P.nnz;
+    } else {
+        c->mat_rowptr = P.diag_rowptr;
+        c->mat_colidx = P.diag_colidx;
+        c->mat_nnz = n;
+        if (assembler == FS_ASM_SPARSE_SYMM)
+            return compact_zeros(c, n, P.diag_rowptr, P.diag_colidx, c->vals, n);
+    }
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FS_OK;
+}
+
+}  // namespace fs

@@ -1,0 +1,518 @@
+// Symbolic phase: mesh preparation, node-to-element adjacency and the CSR
+// sparsity pattern of the assembled matrix.
+//
+// The pattern depends only on the connectivity, the dof numbering and the
+// matrix size, so it is built once per mesh and reused by every numeric
+// assembly.  Its semantics are those of Julia's sparse(I, J, V) over the
+// element dof pairs (FinEtools SysmatAssemblerSparse, src/AssemblyModule.jl):
+// row d holds every column that shares an element with it, sorted.  Rows are
+// produced per node: all six dofs of a node share one sorted column list.
+#include <algorithm>
+
+#include "fs_internal.cuh"
+
+namespace fs {
+
+static const int SCAN_TPB = 256;
+static const int SCAN_ITEMS = 4;
+static const int SCAN_CHUNK = SCAN_TPB * SCAN_ITEMS;
+
+// ---------------------------------------------------------------------------
+// exclusive scan of int64 (out has n + 1 entries, out[n] = total)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t warp_incl_scan(int64_t v)
+{
+    const unsigned lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (unsigned)o) v += u;
+    }
+    return v;
+}
+
+// block-wide exclusive scan of one value per thread; returns the block total
+__device__ int64_t block_excl_scan(int64_t v, int64_t &excl)
+{
+    __shared__ int64_t wsum[SCAN_TPB / 32];
+    int64_t inc = warp_incl_scan(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int64_t s = lane < SCAN_TPB / 32 ? wsum[lane] : 0;
+        s = warp_incl_scan(s);
+        if (lane < SCAN_TPB / 32) wsum[lane] = s;
+    }
+    __syncthreads();
+    int64_t before = w ? wsum[w - 1] : 0;
+    int64_t total = wsum[SCAN_TPB / 32 - 1];
+    excl = before + inc - v;
+    __syncthreads();
+    return total;
+}
+
+__global__ void k_chunk_sums(const int64_t *in, int64_t n, int64_t *sums)
+{
+    int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK;
+    int64_t s = 0;
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        int64_t k = base + (int64_t)i * SCAN_TPB + threadIdx.x;
+        if (k < n) s += in[k];
+    }
+    int64_t ex;
+    int64_t tot = block_excl_scan(s, ex);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+// single block: exclusive scan of the chunk sums in place, total at [nchunks]
+__global__ void k_scan_sums(int64_t *sums, int64_t nchunks)
+{
+    int64_t carry = 0;
+    for (int64_t base = 0; base < nchunks; base += SCAN_TPB) {
+        int64_t k = base + threadIdx.x;
+        int64_t v = k < nchunks ? sums[k] : 0;
+        int64_t ex;
+        int64_t tot = block_excl_scan(v, ex);
+        if (k < nchunks) sums[k] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) sums[nchunks] = carry;
+}
+
+__global__ void k_chunk_scan(const int64_t *in, int64_t n, const int64_t *sums, int64_t *out)
+{
+    int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int64_t v[SCAN_ITEMS];
+    int64_t s = 0;
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        int64_t k = base + i;
+        v[i] = k < n ? in[k] : 0;
+        s += v[i];
+    }
+    int64_t ex;
+    block_excl_scan(s, ex);
+    int64_t run = sums[blockIdx.x] + ex;
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+        int64_t k = base + i;
+        if (k < n) out[k] = run;
+        run += v[i];
+    }
+}
+
+__global__ void k_set_total(int64_t *out, int64_t n, const int64_t *sums, int64_t nchunks)
+{
+    out[n] = sums[nchunks];
+}
+
+int exclusive_scan_i64(fs_ctx *c, const int64_t *in, int64_t *out, int64_t n, int64_t *total)
+{
+    int64_t nchunks = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    if (nchunks == 0) nchunks = 1;
+    FS_TRY(ensure_scratch(c, sizeof(int64_t) * (nchunks + 1)));
+    int64_t *sums = (int64_t *)c->scratch;
+    k_chunk_sums<<<(unsigned)nchunks, SCAN_TPB, 0, c->stream>>>(in, n, sums);
+    k_scan_sums<<<1, SCAN_TPB, 0, c->stream>>>(sums, nchunks);
+    k_chunk_scan<<<(unsigned)nchunks, SCAN_TPB, 0, c->stream>>>(in, n, sums, out);
+    k_set_total<<<1, 1, 0, c->stream>>>(out, n, sums, nchunks);
+    FS_CUDA(c, cudaGetLastError());
+    if (total) {
+        FS_CUDA(c, cudaMemcpyAsync(total, out + n, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+        FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// mesh preparation
+// ---------------------------------------------------------------------------
+__global__ void k_prepare_conn(int64_t nelem, int nen, int64_t nnodes, const int64_t *conn_raw,
+                               const int64_t *order, int32_t *conn, int32_t *elem_of_rank,
+                               int32_t *seen, int *status)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nelem) return;
+    int64_t e = order ? order[r] - 1 : r;
+    if (e < 0 || e >= nelem) {
+        atomicOr(status, DEV_BAD_ORDER);
+        e = 0;
+    } else if (order && atomicAdd(&seen[e], 1) != 0) {
+        atomicOr(status, DEV_BAD_ORDER);
+    }
+    elem_of_rank[r] = (int32_t)e;
+    for (int a = 0; a < nen; a++) {
+        int64_t node = conn_raw[e * nen + a] - 1;
+        if (node < 0 || node >= nnodes) {
+            atomicOr(status, DEV_BAD_CONN);
+            node = 0;
+        }
+        conn[r * nen + a] = (int32_t)node;
+    }
+}
+
+__global__ void k_prepare_dof(int64_t m, const int64_t *dof_raw, int32_t *dof, int *status)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    int64_t v = dof_raw[i];
+    if (v < 1 || v > 0x7fffffffLL) {
+        atomicOr(status, DEV_BAD_DOF);
+        v = 0x7fffffff;
+    }
+    dof[i] = (int32_t)v;
+}
+
+static unsigned nblk(int64_t n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
+
+int launch_prepare_mesh(fs_ctx *c, const int64_t *d_conn_raw, const int64_t *d_order_raw,
+                        const int64_t *d_dof_raw)
+{
+    MeshDev &m = c->mesh;
+    int32_t *seen = nullptr;
+    if (d_order_raw) {
+        FS_TRY(dalloc(c, &seen, (size_t)m.nelem));
+        FS_CUDA(c, cudaMemsetAsync(seen, 0, sizeof(int32_t) * m.nelem, c->stream));
+    }
+    if (m.nelem > 0)
+        k_prepare_conn<<<nblk(m.nelem, 256), 256, 0, c->stream>>>(m.nelem, m.nen, m.nnodes, d_conn_raw,
+                                                                  d_order_raw, m.conn, m.elem_of_rank, seen,
+                                                                  c->d_status);
+    if (d_dof_raw && m.nnodes)
+        k_prepare_dof<<<nblk(6 * m.nnodes, 256), 256, 0, c->stream>>>(6 * m.nnodes, d_dof_raw, m.dof,
+                                                                      c->d_status);
+    FS_CUDA(c, cudaGetLastError());
+    int bits = 0;
+    FS_TRY(read_status(c, &bits));
+    if (seen) cudaFree(seen);
+    if (bits & DEV_BAD_CONN) return set_err(c, FS_ERR_BAD_INPUT, "connectivity refers to a node outside 1..nnodes");
+    if (bits & DEV_BAD_ORDER) return set_err(c, FS_ERR_BAD_INPUT, "assembly order is not a permutation of 1..nelem");
+    if (bits & DEV_BAD_DOF) return set_err(c, FS_ERR_BAD_INPUT, "dof numbers must be in 1..2^31-1");
+    return FS_OK;
+}
+
+int launch_prepare_dofs(fs_ctx *c, const int64_t *d_dof_raw)
+{
+    MeshDev &m = c->mesh;
+    if (m.nnodes)
+        k_prepare_dof<<<nblk(6 * m.nnodes, 256), 256, 0, c->stream>>>(6 * m.nnodes, d_dof_raw, m.dof, c->d_status);
+    FS_CUDA(c, cudaGetLastError());
+    int bits = 0;
+    FS_TRY(read_status(c, &bits));
+    if (bits & DEV_BAD_DOF) return set_err(c, FS_ERR_BAD_INPUT, "dof numbers must be in 1..2^31-1");
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// node -> element adjacency (ascending assembly rank)
+// ---------------------------------------------------------------------------
+__global__ void k_count_pairs(int64_t nelem, int nen, const int32_t *conn, int64_t *cnt)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nelem * nen) return;
+    atomicAdd((unsigned long long *)&cnt[conn[i]], 1ull);
+}
+
+__global__ void k_fill_pairs(int64_t nelem, int nen, const int32_t *conn, const int64_t *pp,
+                             int64_t *fill, int32_t *pair_e)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nelem * nen) return;
+    int node = conn[i];
+    int64_t r = i / nen;
+    int a = (int)(i - r * nen);
+    int64_t s = (int64_t)atomicAdd((unsigned long long *)&fill[node], 1ull);
+    pair_e[pp[node] + s] = (int32_t)((r << 2) | a);
+}
+
+__global__ void k_sort_pairs(int64_t nnodes, const int64_t *pp, int32_t *pair_e, int *status)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nnodes) return;
+    int64_t b = pp[r], e = pp[r + 1];
+    if (e - b > MAX_PAIRS_PER_NODE) atomicOr(status, DEV_VALENCE);
+    for (int64_t i = b + 1; i < e; i++) {
+        int32_t v = pair_e[i];
+        int64_t j = i - 1;
+        while (j >= b && pair_e[j] > v) {
+            pair_e[j + 1] = pair_e[j];
+            j--;
+        }
+        pair_e[j + 1] = v;
+    }
+}
+
+__global__ void k_elem_pair(int64_t npairs, int nen, const int32_t *pair_e, int32_t *elem_pair)
+{
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    int32_t v = pair_e[p];
+    elem_pair[(int64_t)(v >> 2) * nen + (v & 3)] = (int32_t)p;
+}
+
+int build_adjacency(fs_ctx *c)
+{
+    MeshDev &m = c->mesh;
+    int64_t nn = m.nnodes, ne = m.nelem;
+    m.npairs = ne * m.nen;
+    FS_TRY(dalloc(c, &m.pp, (size_t)nn + 1));
+    FS_TRY(dalloc(c, &m.pair_e, (size_t)m.npairs));
+    FS_TRY(dalloc(c, &m.elem_pair, (size_t)m.npairs));
+    int64_t *cnt = nullptr;
+    FS_TRY(dalloc(c, &cnt, (size_t)nn));
+    FS_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * nn, c->stream));
+    if (m.npairs) k_count_pairs<<<nblk(m.npairs, 256), 256, 0, c->stream>>>(ne, m.nen, m.conn, cnt);
+    FS_TRY(exclusive_scan_i64(c, cnt, m.pp, nn, nullptr));
+    FS_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * nn, c->stream));
+    if (m.npairs) k_fill_pairs<<<nblk(m.npairs, 256), 256, 0, c->stream>>>(ne, m.nen, m.conn, m.pp, cnt, m.pair_e);
+    if (nn) k_sort_pairs<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, m.pp, m.pair_e, c->d_status);
+    if (m.npairs) k_elem_pair<<<nblk(m.npairs, 256), 256, 0, c->stream>>>(m.npairs, m.nen, m.pair_e, m.elem_pair);
+    FS_CUDA(c, cudaGetLastError());
+    int bits = 0;
+    FS_TRY(read_status(c, &bits));
+    cudaFree(cnt);
+    if (bits & DEV_VALENCE)
+        return set_err(c, FS_ERR_UNSUPPORTED, "more than 64 elements meet at one node");
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// neighbour lists and per-node column layout
+// ---------------------------------------------------------------------------
+// Sorted unique neighbour nodes of node r, in a thread-local buffer.
+__device__ int node_neighbors(int64_t r, int nen, const int64_t *pp, const int32_t *pair_e,
+                              const int32_t *conn, int32_t *buf)
+{
+    int64_t b = pp[r], e = pp[r + 1];
+    if (e - b > MAX_PAIRS_PER_NODE) e = b + MAX_PAIRS_PER_NODE;
+    int n = 0;
+    for (int64_t p = b; p < e; p++) {
+        int64_t rank = pair_e[p] >> 2;
+        for (int k = 0; k < nen; k++) {
+            int32_t v = conn[rank * nen + k];
+            // insertion into sorted unique buffer
+            int j = n - 1;
+            bool dup = false;
+            while (j >= 0 && buf[j] >= v) {
+                if (buf[j] == v) { dup = true; break; }
+                j--;
+            }
+            if (dup) continue;
+            for (int q = n; q > j + 1; q--) buf[q] = buf[q - 1];
+            buf[j + 1] = v;
+            n++;
+        }
+    }
+    return n;
+}
+
+__global__ void k_count_nbrs(int64_t nnodes, int nen, const int64_t *pp, const int32_t *pair_e,
+                             const int32_t *conn, int64_t *cnt, int *status)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nnodes) return;
+    int32_t buf[MAX_PAIRS_PER_NODE * 4];
+    int n = node_neighbors(r, nen, pp, pair_e, conn, buf);
+    if (n > MAX_NBRS) atomicOr(status, DEV_NEIGHBORS);
+    cnt[r] = n;
+}
+
+__global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_t *pp,
+                            const int32_t *pair_e, const int32_t *conn, const int32_t *dof,
+                            const int64_t *nbr_off, int32_t *nbr, uint32_t *pair_slots,
+                            int16_t *colpos, int32_t *rowlen)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nnodes) return;
+    int32_t buf[MAX_PAIRS_PER_NODE * 4];
+    int n = node_neighbors(r, nen, pp, pair_e, conn, buf);
+    if (n > MAX_NBRS) n = MAX_NBRS;
+    int64_t off = nbr_off[r];
+    for (int s = 0; s < n; s++) nbr[off + s] = buf[s];
+    // slots of each element node in this node's neighbour list
+    for (int64_t p = pp[r]; p < pp[r + 1]; p++) {
+        int64_t rank = pair_e[p] >> 2;
+        uint32_t packed = 0;
+        for (int k = 0; k < nen; k++) {
+            int32_t v = conn[rank * nen + k];
+            int lo = 0, hi = n - 1;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (buf[mid] < v) lo = mid + 1; else hi = mid;
+            }
+            packed |= (uint32_t)(lo & 0xff) << (8 * k);
+        }
+        pair_slots[p] = packed;
+    }
+    // column positions: rank of each valid column dof among the node's columns
+    int L = 0;
+    for (int s = 0; s < n; s++)
+        for (int k = 0; k < 6; k++) L += (dof[(int64_t)k * nnodes + buf[s]] <= n_mat);
+    for (int s = 0; s < n; s++)
+        for (int k = 0; k < 6; k++) {
+            int32_t v = dof[(int64_t)k * nnodes + buf[s]];
+            int16_t pos = -1;
+            if (v <= n_mat) {
+                int cntless = 0;
+                for (int s2 = 0; s2 < n; s2++)
+                    for (int k2 = 0; k2 < 6; k2++) {
+                        int32_t w = dof[(int64_t)k2 * nnodes + buf[s2]];
+                        cntless += (w <= n_mat) & (w < v);
+                    }
+                pos = (int16_t)cntless;
+            }
+            colpos[off * 6 + s * 6 + k] = pos;
+        }
+    rowlen[r] = L;
+}
+
+__global__ void k_row_lengths(int64_t nnodes, int64_t n_mat, const int32_t *dof, const int32_t *rowlen,
+                              int64_t *rl, int32_t *owner_cnt, int *status)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nnodes) return;
+    int64_t r = i % nnodes;
+    int32_t d = dof[i];
+    if (d <= n_mat) {
+        if (atomicAdd(&owner_cnt[d - 1], 1) != 0) atomicOr(status, DEV_BAD_DOF);
+        rl[d - 1] = rowlen[r];
+    }
+}
+
+__global__ void k_fill_colidx(int64_t nnodes, int64_t n_mat, const int32_t *dof, const int64_t *nbr_off,
+                              const int32_t *nbr, const int16_t *colpos, const int64_t *rowptr,
+                              int32_t *colidx)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nnodes) return;
+    int64_t off = nbr_off[r];
+    int n = (int)(nbr_off[r + 1] - off);
+    for (int kr = 0; kr < 6; kr++) {
+        int32_t d = dof[(int64_t)kr * nnodes + r];
+        if (d > n_mat) continue;
+        int64_t base = rowptr[d - 1];
+        for (int s = 0; s < n; s++)
+            for (int k = 0; k < 6; k++) {
+                int16_t pos = colpos[off * 6 + s * 6 + k];
+                if (pos >= 0) colidx[base + pos] = dof[(int64_t)k * nnodes + nbr[off + s]] - 1;
+            }
+    }
+}
+
+__global__ void k_diag_pattern(int64_t n, int64_t *rowptr, int32_t *colidx)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= n) rowptr[i] = i;
+    if (i < n) colidx[i] = (int32_t)i;
+}
+
+int build_pattern(fs_ctx *c, int64_t n)
+{
+    MeshDev &m = c->mesh;
+    PatternDev &P = c->pat;
+    if (P.n == n && P.rowptr) return FS_OK;
+    int64_t nn = m.nnodes;
+    if (n > 0x7fffffffLL) return set_err(c, FS_ERR_UNSUPPORTED, "matrix size above 2^31-1");
+    int64_t *cnt = nullptr;
+    FS_TRY(dalloc(c, &cnt, (size_t)std::max<int64_t>(nn, n)));
+    if (nn) k_count_nbrs<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, m.nen, m.pp, m.pair_e, m.conn, cnt, c->d_status);
+    FS_TRY(dalloc(c, &P.nbr_off, (size_t)nn + 1));
+    int64_t nbr_total = 0;
+    FS_TRY(exclusive_scan_i64(c, cnt, P.nbr_off, nn, &nbr_total));
+    int bits = 0;
+    FS_TRY(read_status(c, &bits));
+    if (bits & DEV_NEIGHBORS) {
+        cudaFree(cnt);
+        return set_err(c, FS_ERR_UNSUPPORTED, "more than 255 neighbour nodes at one node");
+    }
+    FS_TRY(dalloc(c, &P.nbr, (size_t)nbr_total));
+    FS_TRY(dalloc(c, &P.pair_slots, (size_t)m.npairs));
+    FS_TRY(dalloc(c, &P.colpos, (size_t)nbr_total * 6));
+    FS_TRY(dalloc(c, &P.rowlen, (size_t)nn));
+    if (nn)
+        k_fill_nbrs<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, m.nen, n, m.pp, m.pair_e, m.conn, m.dof, P.nbr_off,
+                                                         P.nbr, P.pair_slots, P.colpos, P.rowlen);
+    // row lengths by dof
+    int32_t *owner = nullptr;
+    FS_TRY(dalloc(c, &owner, (size_t)n));
+    FS_CUDA(c, cudaMemsetAsync(owner, 0, sizeof(int32_t) * std::max<int64_t>(n, 1), c->stream));
+    FS_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * std::max<int64_t>(n, 1), c->stream));
+    if (nn) k_row_lengths<<<nblk(6 * nn, 256), 256, 0, c->stream>>>(nn, n, m.dof, P.rowlen, cnt, owner, c->d_status);
+    FS_TRY(dalloc(c, &P.rowptr, (size_t)n + 1));
+    int64_t nnz = 0;
+    FS_TRY(exclusive_scan_i64(c, cnt, P.rowptr, n, &nnz));
+    FS_TRY(read_status(c, &bits));
+    cudaFree(owner);
+    cudaFree(cnt);
+    if (bits & DEV_BAD_DOF) return set_err(c, FS_ERR_BAD_INPUT, "two dofs share one dof number");
+    FS_TRY(dalloc(c, &P.colidx, (size_t)nnz));
+    if (nn) k_fill_colidx<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.colpos, P.rowptr, P.colidx);
+    FS_TRY(dalloc(c, &P.diag_rowptr, (size_t)n + 1));
+    FS_TRY(dalloc(c, &P.diag_colidx, (size_t)n));
+    k_diag_pattern<<<nblk(n + 1, 256), 256, 0, c->stream>>>(n, P.diag_rowptr, P.diag_colidx);
+    FS_CUDA(c, cudaGetLastError());
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    P.n = n;
+    P.nnz = nnz;
+    return FS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dropping exact zeros (FinEtools SysmatAssemblerSparseSymm: S + S^T keeps
+// only nonzero results)
+// ---------------------------------------------------------------------------
+__global__ void k_count_nonzero(int64_t n, const int64_t *rowptr, const double *vals, int64_t *cnt)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t s = 0;
+    for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++) s += (vals[k] != 0.0);
+    cnt[i] = s;
+}
+
+__global__ void k_compact(int64_t n, const int64_t *rowptr, const int32_t *colidx, const double *vals,
+                          const int64_t *nrowptr, int32_t *ncol, double *nval)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t w = nrowptr[i];
+    for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+        if (vals[k] != 0.0) {
+            ncol[w] = colidx[k];
+            nval[w] = vals[k];
+            w++;
+        }
+}
+
+int compact_zeros(fs_ctx *c, int64_t n, const int64_t *rowptr, const int32_t *colidx, const double *vals,
+                  int64_t nnz)
+{
+    int64_t *cnt = nullptr;
+    FS_TRY(dalloc(c, &cnt, (size_t)n));
+    if (n) k_count_nonzero<<<nblk(n, 256), 256, 0, c->stream>>>(n, rowptr, vals, cnt);
+    FS_TRY(dalloc(c, &c->cmp_rowptr, (size_t)n + 1));
+    int64_t nnz2 = 0;
+    FS_TRY(exclusive_scan_i64(c, cnt, c->cmp_rowptr, n, &nnz2));
+    cudaFree(cnt);
+    if (nnz2 == nnz) {
+        // nothing to drop: keep the arrays as they are
+        c->mat_rowptr = rowptr;
+        c->mat_colidx = colidx;
+        c->mat_nnz = nnz;
+        return FS_OK;
+    }
+    if ((size_t)nnz2 > c->cmp_cap || !c->cmp_colidx) {
+        FS_TRY(dalloc(c, &c->cmp_colidx, (size_t)nnz2));
+        FS_TRY(dalloc(c, &c->cmp_vals, (size_t)nnz2));
+        c->cmp_cap = (size_t)nnz2;
+    }
+    if (n) k_compact<<<nblk(n, 256), 256, 0, c->stream>>>(n, rowptr, colidx, vals, c->cmp_rowptr, c->cmp_colidx, c->cmp_vals);
+    FS_CUDA(c, cudaGetLastError());
+    FS_CUDA(c, cudaMemcpyAsync(c->vals, c->cmp_vals, sizeof(double) * nnz2, cudaMemcpyDeviceToDevice, c->stream));
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->mat_rowptr = c->cmp_rowptr;
+    c->mat_colidx = c->cmp_colidx;
+    c->mat_nnz = nnz2;
+    return FS_OK;
+}
+
+}  // namespace fs

@@ -1,0 +1,125 @@
+"""ctypes binding of libflexshell.so (the C ABI of include/flexshell.h).
+
+The library is the only compute path: if it cannot be loaded, or no CUDA
+device is present, every call raises; nothing falls back to the CPU.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libflexshell.so")
+
+_c_dbl_p = ctypes.POINTER(ctypes.c_double)
+_c_i64_p = ctypes.POINTER(ctypes.c_int64)
+
+_lib = None
+
+
+class FlexShellError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("flexshell error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load libflexshell.so (building it first if it is missing or stale)."""
+    global _lib
+    if _lib is None:
+        from . import build as _build
+        _build.build()
+        L = ctypes.CDLL(LIB_PATH)
+        vp = ctypes.c_void_p
+        L.fs_ctx_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+        L.fs_ctx_destroy.argtypes = [vp]
+        L.fs_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+        L.fs_stream.argtypes = [vp, ctypes.POINTER(vp)]
+        L.fs_mesh_set.argtypes = [vp, ctypes.c_int, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, vp]
+        L.fs_params_set.argtypes = [vp, ctypes.POINTER(_abi.fs_shell_params), vp]
+        L.fs_layups_set.argtypes = [vp, ctypes.c_int32, vp, vp]
+        L.fs_normals_compute.argtypes = [vp]
+        L.fs_normals_set.argtypes = [vp, vp, vp]
+        L.fs_normals_get.argtypes = [vp, vp, vp]
+        L.fs_stiffness.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64, _c_i64_p]
+        L.fs_mass.argtypes = [vp, ctypes.c_int, ctypes.c_int64, _c_i64_p]
+        L.fs_matrix_copy.argtypes = [vp, vp, vp, vp]
+        L.fs_matrix_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                                       _c_i64_p, _c_i64_p]
+        L.fs_element_matrices.argtypes = [vp, ctypes.c_int, vp]
+        L.fs_timings.argtypes = [vp, vp, ctypes.c_int]
+        L.fs_geometry_set.argtypes = [vp, vp]
+        L.fs_dofs_set.argtypes = [vp, vp]
+        L.fs_element_masses.argtypes = [vp, vp]
+        L.fs_explicit_setup.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_double]
+        L.fs_explicit_set_state.argtypes = [vp, vp, vp, vp]
+        L.fs_explicit_run.argtypes = [vp, ctypes.c_int64]
+        L.fs_explicit_get_state.argtypes = [vp, vp, vp, vp]
+        L.fs_laminate.argtypes = [ctypes.c_int32, vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_int32,
+                                  ctypes.c_double, ctypes.POINTER(_abi.fs_layup_group)]
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    """Address of a numpy array (or None)."""
+    if a is None:
+        return None
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One library context (device memory, stream) on one GPU."""
+
+    def __init__(self, device=0):
+        self._h = ctypes.c_void_p()
+        st = lib().fs_ctx_create(device, ctypes.byref(self._h))
+        if st != 0:
+            raise FlexShellError(st, "cannot create a context on CUDA device %d" % device)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, st):
+        if st != 0:
+            buf = ctypes.create_string_buffer(512)
+            lib().fs_last_error(self._h, buf, 512)
+            raise FlexShellError(st, buf.value.decode(errors="replace"))
+
+    def call(self, name, *args):
+        self.check(getattr(lib(), name)(self._h, *args))
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        self.check(lib().fs_stream(self._h, ctypes.byref(s)))
+        return s.value
+
+    def close(self):
+        if self._h and self._h.value:
+            lib().fs_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def laminate(plies, offset=0.0, shear_model=0, tcf=0.0):
+    """Layup reduction with the library (fs_laminate): returns an fs_layup_group."""
+    k = len(plies)
+    Dps = np.ascontiguousarray(np.concatenate([np.asarray(p["Dps"], float).flatten(order="F") for p in plies]))
+    Dts = np.ascontiguousarray(np.concatenate([np.asarray(p["Dts"], float).flatten(order="F") for p in plies]))
+    t = np.ascontiguousarray([p["thickness"] for p in plies], dtype=np.float64)
+    ang = np.ascontiguousarray([p["angle"] for p in plies], dtype=np.float64)
+    rho = np.ascontiguousarray([p.get("rho", 0.0) for p in plies], dtype=np.float64)
+    g = _abi.fs_layup_group()
+    st = lib().fs_laminate(k, ptr(Dps), ptr(Dts), ptr(t), ptr(ang), ptr(rho), offset, shear_model, tcf,
+                           ctypes.byref(g))
+    if st != 0:
+        raise FlexShellError(st, "invalid layup")
+    return g

@@ -1,0 +1,309 @@
+"""Host mirror of the reference FEMM interface for the shell hot path.
+
+The classes keep the reference names and call pattern
+(FinEtoolsFlexStructures.jl 3.6.4):
+
+    femm = FEMMShellT3FF.make(fes, thickness, material, stab_fun)   # src/FEMMShellT3FFModule.jl:241-268
+    femm.associategeometry(geom0)                                    # :570-616
+    K = femm.stiffness(assembler, geom0, u1, Rfield1, dchi)          # :635-736
+    M = femm.mass(assembler, geom0, dchi)                            # :757-811
+
+and the same for FEMMShellQ4RS (src/FEMMShellQ4RSModule.jl),
+FEMMShellT3FFComp and FEMMShellQ4RSComp (layup groups).  Matrices are
+returned as scipy.sparse CSC (SparseMatrixCSC) or CSR
+(SysmatAssemblerSparseCSRSymm) matrices.  All computation runs in
+libflexshell.so on the GPU; `u1` and `Rfield1` are accepted and ignored as in
+the reference shells.
+"""
+import numpy as np
+
+from . import _abi, mesh as _mesh
+from ._lib import Context, FlexShellError, ptr
+
+FS_FP64, FS_MIXED = _abi.FS_FP64, _abi.FS_MIXED
+
+
+# ---------------------------------------------------------------------------
+# fields and assemblers (FinEtools)
+# ---------------------------------------------------------------------------
+class NodalField:
+    """FinEtools NodalField: values (nents x ndofn), fixed flags, dof numbers."""
+
+    def __init__(self, values):
+        self.values = np.array(values, dtype=np.float64, order="F")
+        if self.values.ndim == 1:
+            self.values = self.values[:, None]
+        self.is_fixed = np.zeros(self.values.shape, dtype=bool)
+        self.dofnums = np.zeros(self.values.shape, dtype=np.int64, order="F")
+        self.nfreedofs = 0
+
+    def setebc(self, nodes, comp):
+        """Fix component `comp` (1-based) of the 1-based `nodes`."""
+        self.is_fixed[np.asarray(nodes, dtype=np.int64) - 1, comp - 1] = True
+
+    def numberdofs(self):
+        d, nf = _mesh.numberdofs(self.is_fixed)
+        self.dofnums = np.asfortranarray(d)
+        self.nfreedofs = nf
+        return self
+
+    def nalldofs(self):
+        return int(self.values.size)
+
+
+class _Assembler:
+    mode = _abi.FS_ASM_SPARSE
+    csr = False
+    nrows = None  # None: nalldofs(dchi)
+
+
+class SysmatAssemblerSparseSymm(_Assembler):
+    mode = _abi.FS_ASM_SPARSE_SYMM
+
+
+class SysmatAssemblerSparse(_Assembler):
+    mode = _abi.FS_ASM_SPARSE
+
+
+class SysmatAssemblerSparseCSRSymm(_Assembler):
+    """src/AssemblyModule.jl:20-53: SysmatAssemblerSparse result converted to CSR."""
+    mode = _abi.FS_ASM_SPARSE
+    csr = True
+
+
+class SysmatAssemblerSparseDiag(_Assembler):
+    mode = _abi.FS_ASM_DIAG
+
+
+class SysmatAssemblerFFBlock(_Assembler):
+    """Free-free block: dofs above nfreedofs are left out."""
+
+    def __init__(self, a=None, nfree=None, ncfree=None):
+        if nfree is None and isinstance(a, (int, np.integer)):
+            a, nfree = None, int(a)
+        inner = a if a is not None else SysmatAssemblerSparse()
+        self.mode = inner.mode
+        self.csr = inner.csr
+        self.nrows = int(nfree)
+
+
+# ---------------------------------------------------------------------------
+# stab_fun family
+# ---------------------------------------------------------------------------
+def stab_coefficient(stab_fun, default):
+    """The coefficient c of stab_fun(t, h) = t^2/(t^2 + c h^2).  Closures
+    outside this family are rejected (ArgumentError in the Julia shim)."""
+    if stab_fun is None:
+        return default
+    if isinstance(stab_fun, (int, float)):
+        return float(stab_fun)
+    f1 = float(stab_fun(1.0, 1.0))
+    c = 1.0 / f1 - 1.0
+    for t, h in ((0.3, 2.0), (0.01, 0.05)):
+        want = t * t / (t * t + c * h * h)
+        got = float(stab_fun(t, h))
+        if abs(got - want) > 1e-12 * max(abs(want), 1e-300):
+            raise ValueError("stab_fun is not of the form t^2/(t^2 + c h^2)")
+    return c
+
+
+# ---------------------------------------------------------------------------
+# FEMMs
+# ---------------------------------------------------------------------------
+class _FEMMShell:
+    etype = None
+    nen = None
+    default_stab = None
+
+    def __init__(self, conn, thickness, material=None, stab_fun=None, device=0, layup_groups=None):
+        self.conn = np.ascontiguousarray(conn, dtype=np.int64)
+        if self.conn.ndim != 2 or self.conn.shape[1] != self.nen:
+            raise ValueError("connectivity must be nelem x %d" % self.nen)
+        self.material = material
+        self.thickness = thickness
+        self.stab_c = stab_coefficient(stab_fun, self.default_stab)
+        self.transv_shear_formulation = 0
+        self.drilling_stiffness_scale = 1.0
+        self.threshold_angle = 30.0
+        self.layup_groups = layup_groups
+        self.ctx = Context(device)
+        self._geom = None
+        self._dof_key = None
+        self._associatedgeometry = False
+        self._normals = None
+        self._normal_valid = None
+
+    # -- parameters -------------------------------------------------------
+    def _params(self):
+        from .materials import shell_material_stiffness
+        if self.material is not None:
+            Dps, Dt = shell_material_stiffness(self.material)
+            rho = self.material.massdensity()
+        else:
+            Dps, Dt, rho = np.eye(3), np.eye(2), 0.0
+        th = self.thickness
+        scalar_t = float(th) if np.isscalar(th) else 0.0
+        p = _abi.make_params(Dps, Dt, rho, scalar_t, stab_c=self.stab_c,
+                             drilling_stiffness_scale=self.drilling_stiffness_scale,
+                             threshold_angle=self.threshold_angle,
+                             transv_shear_formulation=self.transv_shear_formulation)
+        tharr = None if np.isscalar(th) or th is None else np.ascontiguousarray(th, dtype=np.float64)
+        return p, tharr
+
+    def _order(self):
+        if not self.layup_groups:
+            return None
+        return np.ascontiguousarray(np.concatenate([np.asarray(g[1], dtype=np.int64)
+                                                    for g in self.layup_groups]))
+
+    def _upload_mesh(self, geom0):
+        xyz = np.asfortranarray(geom0.values, dtype=np.float64)
+        order = self._order()
+        self.ctx.call("fs_mesh_set", self.etype, xyz.shape[0], ptr(xyz), self.conn.shape[0],
+                      ptr(self.conn), ptr(order), None)
+        p, tharr = self._params()
+        self.ctx.call("fs_params_set", p, ptr(tharr))
+        if self.layup_groups:
+            groups = [g[0] for g in self.layup_groups]
+            eg = np.zeros(self.conn.shape[0], dtype=np.int32)
+            for k, g in enumerate(self.layup_groups):
+                eg[np.asarray(g[1], dtype=np.int64) - 1] = k
+            arr = (_abi.fs_layup_group * len(groups))(*groups)
+            self.ctx.call("fs_layups_set", len(groups), arr, ptr(eg))
+        self._geom = (id(geom0.values), xyz.shape)
+        self._dof_key = None
+
+    def _sync_inputs(self, geom0, dchi):
+        if self._geom != (id(geom0.values), np.shape(geom0.values)):
+            xyz = np.asfortranarray(geom0.values, dtype=np.float64)
+            self.ctx.call("fs_geometry_set", ptr(xyz))
+            self._geom = (id(geom0.values), xyz.shape)
+        p, tharr = self._params()
+        self.ctx.call("fs_params_set", p, ptr(tharr))
+        if dchi is not None:
+            d = np.asfortranarray(dchi.dofnums, dtype=np.int64)
+            if d.shape != (geom0.values.shape[0], 6):
+                raise ValueError("dchi must have 6 dofs per node")
+            key = (id(dchi.dofnums), d.shape, int(d.sum()))
+            if key != self._dof_key:
+                self.ctx.call("fs_dofs_set", ptr(d))
+                self._dof_key = key
+
+    # -- reference interface --------------------------------------------------
+    def associategeometry(self, geom0):
+        """associategeometry!(femm, geom0): nodal normals and validity."""
+        self._upload_mesh(geom0)
+        self.ctx.call("fs_normals_compute")
+        nn = geom0.values.shape[0]
+        self._normals = np.zeros((nn, 3), order="F")
+        self._normal_valid = np.zeros(nn, dtype=np.uint8)
+        self.ctx.call("fs_normals_get", ptr(self._normals), ptr(self._normal_valid))
+        self._associatedgeometry = True
+        return self
+
+    def set_normals(self, normals, valid):
+        """Normals from a user coordinate system (the reference's `mcsys`)."""
+        self._normals = np.asfortranarray(normals, dtype=np.float64)
+        self._normal_valid = np.ascontiguousarray(valid, dtype=np.uint8)
+        self.ctx.call("fs_normals_set", ptr(self._normals), ptr(self._normal_valid))
+        self._associatedgeometry = True
+
+    def _fetch(self, nrows, nnz, csr):
+        import scipy.sparse as sp
+        colptr = np.empty(nrows + 1, dtype=np.int64)
+        rowval = np.empty(nnz, dtype=np.int64)
+        nzval = np.empty(nnz, dtype=np.float64)
+        self.ctx.call("fs_matrix_copy", ptr(colptr), ptr(rowval), ptr(nzval))
+        if csr:
+            return sp.csr_matrix((nzval, rowval - 1, colptr - 1), shape=(nrows, nrows))
+        return sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=(nrows, nrows))
+
+    def stiffness(self, assembler, geom0, u1=None, Rfield1=None, dchi=None, precision=FS_FP64):
+        """stiffness(femm, assembler, geom0, u1, Rfield1, dchi) -> K."""
+        if not isinstance(assembler, _Assembler):
+            # stiffness(femm, geom0, u1, Rfield1, dchi): default assembler
+            assembler, geom0, u1, Rfield1, dchi = SysmatAssemblerSparseSymm(), assembler, geom0, u1, Rfield1
+        if not self._associatedgeometry:
+            raise AssertionError("self._associatedgeometry == true")
+        self._sync_inputs(geom0, dchi)
+        nrows = assembler.nrows if assembler.nrows is not None else dchi.nalldofs()
+        import ctypes
+        nnz = ctypes.c_int64()
+        self.ctx.call("fs_stiffness", precision, assembler.mode, nrows, ctypes.byref(nnz))
+        return self._fetch(nrows, nnz.value, assembler.csr)
+
+    def mass(self, assembler, geom0, dchi=None):
+        """mass(femm, assembler, geom0, dchi) -> lumped M."""
+        if not isinstance(assembler, _Assembler):
+            assembler, geom0, dchi = SysmatAssemblerSparseSymm(), assembler, geom0
+        if not self._associatedgeometry:
+            raise AssertionError("self._associatedgeometry == true")
+        self._sync_inputs(geom0, dchi)
+        nrows = assembler.nrows if assembler.nrows is not None else dchi.nalldofs()
+        import ctypes
+        nnz = ctypes.c_int64()
+        self.ctx.call("fs_mass", assembler.mode, nrows, ctypes.byref(nnz))
+        return self._fetch(nrows, nnz.value, assembler.csr)
+
+    # -- extras ----------------------------------------------------------------
+    def element_matrices(self, geom0, precision=FS_FP64):
+        """All element stiffness matrices in the global basis (nelem x nd x nd)."""
+        self._sync_inputs(geom0, None)
+        nd = 6 * self.nen
+        out = np.zeros((self.conn.shape[0], nd, nd))
+        self.ctx.call("fs_element_matrices", precision, ptr(out))
+        return out.transpose(0, 2, 1).copy()
+
+    def element_masses(self, geom0):
+        self._sync_inputs(geom0, None)
+        out = np.zeros((self.conn.shape[0], 2))
+        self.ctx.call("fs_element_masses", ptr(out))
+        return out
+
+    def close(self):
+        self.ctx.close()
+
+    @classmethod
+    def make(cls, fes, thickness, material, stab_fun=None, device=0):
+        return cls(fes, thickness, material, stab_fun, device)
+
+
+class FEMMShellT3FF(_FEMMShell):
+    """src/FEMMShellT3FFModule.jl:101-112"""
+    etype = _abi.FS_T3FF
+    nen = 3
+    default_stab = 5 / 12 / 1.5
+
+
+class FEMMShellQ4RS(_FEMMShell):
+    """src/FEMMShellQ4RSModule.jl:69-79"""
+    etype = _abi.FS_Q4RS
+    nen = 4
+    default_stab = 0.1
+
+
+class _FEMMShellComp(_FEMMShell):
+    """Layered FEMM: `layup_groups` is a list of (fs_layup_group, element list
+    1-based), as the reference's layup_groups field
+    (src/FEMMShellT3FFCompModule.jl:63-77)."""
+
+    def __init__(self, conn, layup_groups, stab_fun=None, device=0):
+        if isinstance(layup_groups, _abi.fs_layup_group):
+            layup_groups = [(layup_groups, np.arange(1, np.shape(conn)[0] + 1))]
+        super().__init__(conn, 0.0, None, stab_fun, device, layup_groups)
+
+    @classmethod
+    def make(cls, fes, layup, stab_fun=None, device=0):
+        return cls(fes, layup, stab_fun, device)
+
+
+class FEMMShellT3FFComp(_FEMMShellComp):
+    etype = _abi.FS_T3FFCOMP
+    nen = 3
+    default_stab = 5 / 12 / 1.5
+
+
+class FEMMShellQ4RSComp(_FEMMShellComp):
+    etype = _abi.FS_Q4RSCOMP
+    nen = 4
+    default_stab = 0.1

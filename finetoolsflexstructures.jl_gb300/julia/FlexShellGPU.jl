@@ -1,0 +1,139 @@
+"""
+    FlexShellGPU
+
+Julia-side binding of libflexshell.so (include/flexshell.h).  It adds methods
+with the reference signatures of FinEtoolsFlexStructures.jl 3.6.4 so that
+driver code calls them unchanged:
+
+    stiffness(femm::FEMMShellT3FF, assembler, geom0, u1, Rfield1, dchi)
+    mass(femm::FEMMShellT3FF, assembler, geom0, dchi)
+
+(and the same for FEMMShellQ4RS, FEMMShellT3FFComp, FEMMShellQ4RSComp).
+`associategeometry!` stays the reference's own; its normals are passed in.
+Not exercised in this repository (no Julia toolchain here); it is the
+binding a maintainer adds next to the reference.
+"""
+module FlexShellGPU
+
+using SparseArrays
+using FinEtools
+using FinEtoolsFlexStructures.FEMMShellT3FFModule: FEMMShellT3FF
+using FinEtoolsFlexStructures.FEMMShellQ4RSModule: FEMMShellQ4RS
+import FinEtoolsFlexStructures.FEMMShellT3FFModule: stiffness, mass
+import FinEtoolsFlexStructures.FEMMShellQ4RSModule: stiffness, mass
+
+const libflexshell = get(ENV, "FLEXSHELL_LIB", "libflexshell.so")
+
+const FS_T3FF, FS_T3FFCOMP, FS_Q4RS, FS_Q4RSCOMP = 0, 1, 2, 3
+const FS_FP64, FS_MIXED = 0, 1
+const FS_ASM_SPARSE, FS_ASM_SPARSE_SYMM, FS_ASM_DIAG = 0, 1, 2
+
+# fs_shell_params (include/flexshell.h)
+struct FsShellParams
+    transv_shear_formulation::Int32
+    reserved::Int32
+    drilling_stiffness_scale::Float64
+    threshold_angle::Float64
+    stab_c::Float64
+    Dps::NTuple{9,Float64}
+    Dt::NTuple{4,Float64}
+    rho::Float64
+    thickness::Float64
+end
+
+mutable struct Ctx
+    h::Ptr{Cvoid}
+end
+
+function check(ctx::Ctx, st::Cint)
+    st == 0 && return nothing
+    buf = Vector{UInt8}(undef, 512)
+    ccall((:fs_last_error, libflexshell), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), ctx.h, buf, 512)
+    msg = unsafe_string(pointer(buf))
+    st == 6 && throw(AssertionError(msg))       # FS_ERR_STATE: the reference @assert
+    throw(ErrorException("flexshell error $st: $msg"))
+end
+
+const CONTEXTS = IdDict{Any,Ctx}()
+
+function context(femm)
+    get!(CONTEXTS, femm) do
+        r = Ref{Ptr{Cvoid}}(C_NULL)
+        st = ccall((:fs_ctx_create, libflexshell), Cint, (Cint, Ref{Ptr{Cvoid}}), 0, r)
+        st == 0 || error("flexshell: no CUDA device")
+        ctx = Ctx(r[])
+        finalizer(c -> ccall((:fs_ctx_destroy, libflexshell), Cint, (Ptr{Cvoid},), c.h), ctx)
+        ctx
+    end
+end
+
+# stab_fun restricted to t^2/(t^2 + c h^2): recover c, verify at two points
+function stab_coefficient(f)
+    c = 1 / f(1.0, 1.0) - 1
+    for (t, h) in ((0.3, 2.0), (0.01, 0.05))
+        isapprox(f(t, h), t^2 / (t^2 + c * h^2); rtol = 1e-12) ||
+            throw(ArgumentError("stab_fun is not of the form t^2/(t^2 + c h^2)"))
+    end
+    return c
+end
+
+asm_mode(::SysmatAssemblerSparseSymm) = FS_ASM_SPARSE_SYMM
+asm_mode(::SysmatAssemblerSparseDiag) = FS_ASM_DIAG
+asm_mode(::AbstractSysmatAssembler) = FS_ASM_SPARSE
+
+function upload!(ctx, femm, etype, geom0, dchi)
+    fes = femm.integdomain.fes
+    conn = collect(reinterpret(Int, fes.conn))          # nen per element, 1-based
+    xyz = geom0.values                                  # nnodes x 3, column-major
+    check(ctx, ccall((:fs_mesh_set, libflexshell), Cint,
+        (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
+        ctx.h, etype, size(xyz, 1), xyz, count(fes), conn, C_NULL, dchi.dofnums))
+    Dps, Dt = femm_material_matrices(femm)
+    t = femm.integdomain.otherdimension(zeros(1, 3), fes.conn[1], zeros(1, 1))
+    p = FsShellParams(etype == FS_T3FF ? femm.transv_shear_formulation : 0, 0,
+        femm.drilling_stiffness_scale, femm.threshold_angle, stab_coefficient(femm.stab_fun),
+        Tuple(vec(Dps)), Tuple(vec(Dt)), massdensity(femm.material), t)
+    check(ctx, ccall((:fs_params_set, libflexshell), Cint, (Ptr{Cvoid}, Ref{FsShellParams}, Ptr{Float64}),
+        ctx.h, p, C_NULL))
+    # normals from the reference's associategeometry! (honours a user mcsys)
+    check(ctx, ccall((:fs_normals_set, libflexshell), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{UInt8}),
+        ctx.h, femm._normals, UInt8.(femm._normal_valid)))
+end
+
+femm_material_matrices(femm) =
+    FinEtoolsFlexStructures.FEMMShellT3FFModule._shell_material_stiffness(femm.material)
+
+function fetch_csc(ctx, n, nnz)
+    colptr = Vector{Int64}(undef, n + 1)
+    rowval = Vector{Int64}(undef, nnz)
+    nzval = Vector{Float64}(undef, nnz)
+    check(ctx, ccall((:fs_matrix_copy, libflexshell), Cint,
+        (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}), ctx.h, colptr, rowval, nzval))
+    return SparseMatrixCSC(n, n, colptr, rowval, nzval)
+end
+
+for (T, etype) in ((FEMMShellT3FF, FS_T3FF), (FEMMShellQ4RS, FS_Q4RS))
+    @eval function stiffness(self::$T, assembler::ASS, geom0::NodalField{Float64},
+        u1::NodalField{TI}, Rfield1::NodalField{TI}, dchi::NodalField{TI};
+        precision = FS_FP64) where {ASS<:AbstractSysmatAssembler,TI<:Number}
+        @assert self._associatedgeometry == true
+        ctx = context(self)
+        upload!(ctx, self, $etype, geom0, dchi)
+        nnz = Ref{Int64}(0)
+        check(ctx, ccall((:fs_stiffness, libflexshell), Cint, (Ptr{Cvoid}, Cint, Cint, Int64, Ref{Int64}),
+            ctx.h, precision, asm_mode(assembler), nalldofs(dchi), nnz))
+        return fetch_csc(ctx, nalldofs(dchi), nnz[])
+    end
+    @eval function mass(self::$T, assembler::A, geom0::NodalField{Float64},
+        dchi::NodalField{TI}) where {A<:AbstractSysmatAssembler,TI<:Number}
+        @assert self._associatedgeometry == true
+        ctx = context(self)
+        upload!(ctx, self, $etype, geom0, dchi)
+        nnz = Ref{Int64}(0)
+        check(ctx, ccall((:fs_mass, libflexshell), Cint, (Ptr{Cvoid}, Cint, Int64, Ref{Int64}),
+            ctx.h, asm_mode(assembler), nalldofs(dchi), nnz))
+        return fetch_csc(ctx, nalldofs(dchi), nnz[])
+    end
+end
+
+end # module

@@ -1,0 +1,172 @@
+/*
+ * flexshell: GB300 (sm_103a) shell element assembly -- C ABI.
+ *
+ * Drop-in boundary for the element-assembly hot path of
+ * FinEtoolsFlexStructures.jl 3.6.4.  Every entry point is plain C (pointers
+ * and sizes, no framework types) so that the Julia shim can `ccall` it; the
+ * Julia methods keep the reference signatures and return the same
+ * SparseMatrixCSC{Float64,Int64}.
+ *
+ * Layouts follow Julia: geometry `nnodes x 3` column-major, dof numbers
+ * `nnodes x 6` column-major and 1-based (free dofs first, as numberdofs!),
+ * connectivity one row of `nen` 1-based node numbers per element
+ * (reinterpret(Int, fes.conn)).  Matrices come back as 1-based CSC arrays;
+ * the assembled matrices are symmetric, so they are also the CSR arrays.
+ *
+ * Every function returns FS_OK (0) or an FS_ERR_* code; fs_last_error()
+ * gives the message.  Calls are blocking (the context stream is
+ * synchronised before return) except where noted.  A context is used by
+ * one host thread at a time.
+ */
+#ifndef FLEXSHELL_H
+#define FLEXSHELL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FS_OK 0
+#define FS_ERR_BAD_INPUT 1        /* invalid argument or mesh data            */
+#define FS_ERR_CUDA 2             /* CUDA runtime error                       */
+#define FS_ERR_OOM 3              /* device allocation failed                 */
+#define FS_ERR_SINGULAR_METRIC 4  /* Q4: "Singular metric matrix" (src/FEMMShellQ4RSModule.jl:308-311) */
+#define FS_ERR_UNSUPPORTED 5      /* option outside the supported family      */
+#define FS_ERR_STATE 6            /* call order (e.g. no associategeometry!)  */
+#define FS_ERR_TIMEOUT 7          /* bounded device wait expired              */
+
+/* element families (FEMM types of the reference) */
+#define FS_T3FF 0       /* FEMMShellT3FF,     src/FEMMShellT3FFModule.jl     */
+#define FS_T3FFCOMP 1   /* FEMMShellT3FFComp, src/FEMMShellT3FFCompModule.jl */
+#define FS_Q4RS 2       /* FEMMShellQ4RS,     src/FEMMShellQ4RSModule.jl     */
+#define FS_Q4RSCOMP 3   /* FEMMShellQ4RSComp, src/FEMMShellQ4RSCompModule.jl */
+
+/* arithmetic of the element strain rows and Gram products */
+#define FS_FP64 0       /* everything in double: the drop-in                 */
+#define FS_MIXED 1      /* float element arithmetic; frames, triads, drilling
+                           factor and CSR accumulation in double             */
+
+/* assembler semantics (FinEtools assemblers) */
+#define FS_ASM_SPARSE 0      /* SysmatAssemblerSparse / SysmatAssemblerSparseCSRSymm
+                                (src/AssemblyModule.jl:20-53): union pattern, explicit zeros kept */
+#define FS_ASM_SPARSE_SYMM 1 /* SysmatAssemblerSparseSymm (default of stiffness/mass):
+                                entries whose assembled value is exactly zero are dropped */
+#define FS_ASM_DIAG 2        /* SysmatAssemblerSparseDiag: diagonal only */
+
+typedef struct fs_ctx fs_ctx;
+
+/* Formulation parameters of a homogeneous FEMM (FEMMShellT3FF / FEMMShellQ4RS fields,
+ * src/FEMMShellT3FFModule.jl:101-112, src/FEMMShellQ4RSModule.jl:69-79). */
+typedef struct {
+    int32_t transv_shear_formulation; /* T3FF only: 0 average B (default), 1 average K */
+    int32_t reserved;
+    double drilling_stiffness_scale;  /* default 1.0 */
+    double threshold_angle;           /* degrees, default 30.0 */
+    double stab_c;                    /* stab_fun(t,h) = t^2/(t^2 + stab_c*h^2):
+                                         T3FF default 5/12/1.5, Q4RS default 0.1 */
+    double Dps[9];                    /* plane-stress stiffness, column-major 3x3 */
+    double Dt[4];                     /* transverse-shear stiffness, column-major 2x2
+                                         (the element applies the 5/6 factor)     */
+    double rho;                       /* mass density                              */
+    double thickness;                 /* used when no per-element thickness given  */
+} fs_shell_params;
+
+/* One layup group (CompositeLayup of src/CompositeLayupModule.jl:185-225,
+ * reduced on the host with laminate_stiffnesses!, laminate_transverse_stiffness!
+ * and laminate_inertia!, or with fs_laminate below). */
+typedef struct {
+    double A[9], B[9], D[9]; /* column-major 3x3 */
+    double H[4];             /* column-major 2x2 */
+    double csmat[9];         /* layup coordinate system (columns = basis vectors) */
+    double thickness;        /* thickness(layup) */
+    double mass_density;     /* laminate_inertia! first result  */
+    double moi_density;      /* laminate_inertia! second result */
+} fs_layup_group;
+
+/* --- context ------------------------------------------------------------- */
+int fs_ctx_create(int device, fs_ctx **out);
+int fs_ctx_destroy(fs_ctx *ctx);
+/* Copies the last error message of this context (NUL terminated). */
+int fs_last_error(const fs_ctx *ctx, char *buf, size_t len);
+/* The CUDA stream (cudaStream_t) all work of the context runs on. */
+int fs_stream(const fs_ctx *ctx, void **stream);
+
+/* --- inputs --------------------------------------------------------------- */
+/* Mesh, connectivity and dof numbering (fes.conn, geom0.values, dchi.dofnums).
+ * `order` (may be NULL) is the 1-based sequence in which elements are
+ * assembled; the layered FEMMs assemble layup group by layup group
+ * (src/FEMMShellT3FFCompModule.jl:600-606).  `dofnums` may be NULL and set
+ * later with fs_dofs_set.  Uploads the arrays. */
+int fs_mesh_set(fs_ctx *ctx, int elem_type, int64_t nnodes, const double *xyz, int64_t nelem,
+                const int64_t *conn, const int64_t *order, const int64_t *dofnums);
+/* New geometry for the same connectivity (geom0.values); keeps normals and pattern. */
+int fs_geometry_set(fs_ctx *ctx, const double *xyz);
+/* Dof numbering (dchi.dofnums after numberdofs!), nnodes x 6 column-major, 1-based. */
+int fs_dofs_set(fs_ctx *ctx, const int64_t *dofnums);
+/* Parameters; `thickness` (may be NULL) is per element, in mesh order. */
+int fs_params_set(fs_ctx *ctx, const fs_shell_params *params, const double *thickness);
+/* Layup groups of a layered FEMM; `elem_group` is the 0-based group of each element. */
+int fs_layups_set(fs_ctx *ctx, int32_t ngroups, const fs_layup_group *groups,
+                  const int32_t *elem_group);
+
+/* --- associategeometry! ----------------------------------------------------- */
+/* Nodal normals and validity flags with the default (isoparametric) normals,
+ * or the layup csys third axis for the layered FEMMs
+ * (src/FEMMShellT3FFModule.jl:570-616, src/FEMMShellQ4RSModule.jl:472-525). */
+int fs_normals_compute(fs_ctx *ctx);
+/* Normals computed by the caller (e.g. a user `mcsys`), nnodes x 3 column-major. */
+int fs_normals_set(fs_ctx *ctx, const double *normals, const uint8_t *valid);
+int fs_normals_get(fs_ctx *ctx, double *normals, uint8_t *valid);
+
+/* --- stiffness / mass ------------------------------------------------------- */
+/* stiffness(femm, assembler, geom0, u1, Rfield1, dchi)
+ * (src/FEMMShellT3FFModule.jl:635-736, src/FEMMShellQ4RSModule.jl:877-947 and the
+ * layered variants).  `nrows` is the matrix size (nalldofs(dchi), or nfreedofs for
+ * the free block); dofs above it are left out as FinEtools does.  The sparsity
+ * pattern is built on the first call for a mesh and reused.  The matrix stays
+ * on the device until fs_matrix_copy. */
+int fs_stiffness(fs_ctx *ctx, int precision, int assembler, int64_t nrows, int64_t *nnz_out);
+/* mass(femm, assembler, geom0, dchi): the lumped mass
+ * (src/FEMMShellT3FFModule.jl:757-811, src/FEMMShellQ4RSModule.jl:968-1022). */
+int fs_mass(fs_ctx *ctx, int assembler, int64_t nrows, int64_t *nnz_out);
+/* The matrix of the last fs_stiffness / fs_mass call into caller memory:
+ * colptr[nrows+1], rowval[nnz], nzval[nnz], 1-based CSC.  Any pointer may be NULL. */
+int fs_matrix_copy(fs_ctx *ctx, int64_t *colptr, int64_t *rowval, double *nzval);
+/* Device pointers of the last matrix (0-based CSR; valid until the next call). */
+int fs_matrix_device(fs_ctx *ctx, const int64_t **rowptr, const int32_t **colidx,
+                     const double **vals, int64_t *nrows, int64_t *nnz);
+/* Device times (milliseconds, CUDA events on the context stream) of the last
+ * fs_stiffness call: [0] element kernel, [1] CSR gather, [2] symbolic phase of
+ * the last pattern build, [3] zero compaction.  `n` entries are written. */
+int fs_timings(const fs_ctx *ctx, double *out, int n);
+/* Element matrices in the global basis (nelem x (6 nen)^2, each column-major), in
+ * mesh order; for parity checks. */
+int fs_element_matrices(fs_ctx *ctx, int precision, double *out);
+/* Lumped element masses (tmass, rmass) per element, in mesh order. */
+int fs_element_masses(fs_ctx *ctx, double *out);
+
+/* --- explicit central difference (examples/.../plate_expl_examples.jl:61-94) --- */
+/* Uses the last matrix from fs_stiffness (must be nrows x nrows).  invMC and C are
+ * the per-dof vectors of _cd_loop! (:69-71).  Values are kept in double
+ * (precision FS_FP64) or rounded to float (FS_MIXED); the state update is double
+ * with Kahan compensation. */
+int fs_explicit_setup(fs_ctx *ctx, int precision, const double *invMC, const double *C, double dt);
+int fs_explicit_set_state(fs_ctx *ctx, const double *U, const double *V, const double *A);
+/* Runs nsteps steps; the step loop is captured once into a CUDA graph. */
+int fs_explicit_run(fs_ctx *ctx, int64_t nsteps);
+int fs_explicit_get_state(fs_ctx *ctx, double *U, double *V, double *A);
+
+/* --- layup reduction (src/CompositeLayupModule.jl:246-330) ------------------ */
+/* ply_Dps: nplies x 9, ply_Dts: nplies x 4 (column-major each); angles in degrees;
+ * shear_model 0 = Vinson-Sierakowski, 1 = constant `tcf`. Host only. */
+int fs_laminate(int32_t nplies, const double *ply_Dps, const double *ply_Dts,
+                const double *ply_thickness, const double *ply_angle_deg, const double *ply_rho,
+                double offset, int32_t shear_model, double tcf, fs_layup_group *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

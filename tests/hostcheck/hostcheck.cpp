@@ -1,0 +1,129 @@
+// Test-only host build of the CUDA library's per-element math
+// (csrc/fs_elem_math.cuh), so the restructured Gram-row formulation can be
+// compared with the oracle on a machine without a GPU.  Not part of the
+// product: the library itself has no CPU path.
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "fs_host_prep.h"
+
+using namespace fs;
+
+template <class R>
+static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t nelem,
+                         const int64_t *conn, const double *normals, const uint8_t *valid,
+                         const double *thick, const fs_shell_params *p, const fs_layup_group *groups,
+                         const int32_t *egroup, double *out)
+{
+    MatConst mc;
+    if (prepare_matconst(*p, mc)) return 1;
+    bool comp = (etype == FS_T3FFCOMP || etype == FS_Q4RSCOMP);
+    int ng = 0;
+    if (comp)
+        for (int64_t e = 0; e < nelem; e++) ng = egroup[e] + 1 > ng ? egroup[e] + 1 : ng;
+    std::vector<GroupConst> gcs(ng > 0 ? ng : 1);
+    for (int g = 0; g < ng; g++)
+        if (prepare_group(groups[g], gcs[g])) return 1;
+    int nn = (etype == FS_T3FF || etype == FS_T3FFCOMP) ? 3 : 4;
+    int nd = 6 * nn;
+    for (int64_t e = 0; e < nelem; e++) {
+        const GroupConst *gc = comp ? &gcs[egroup[e]] : nullptr;
+        const int nrows_max = 40;
+        R rows[nrows_max][24];
+        memset(rows, 0, sizeof(rows));
+        int nrows = 0, st = 0;
+        if (nn == 3) {
+            ElemIn<3> in;
+            for (int a = 0; a < 3; a++) {
+                int64_t node = conn[3 * e + a] - 1;
+                for (int c = 0; c < 3; c++) {
+                    in.X[a][c] = xyz[node + c * nnodes];
+                    in.nrm[a][c] = normals[node + c * nnodes];
+                }
+                in.valid[a] = valid[node] != 0;
+            }
+            in.t = thick[e];
+            if (p->transv_shear_formulation == 1) {
+                nrows = T3Rows<true>::N;
+                st = comp ? t3_rows<R, true, true>(in, mc, gc, &rows[0][0], 24)
+                          : t3_rows<R, false, true>(in, mc, gc, &rows[0][0], 24);
+            } else {
+                nrows = T3Rows<false>::N;
+                st = comp ? t3_rows<R, true, false>(in, mc, gc, &rows[0][0], 24)
+                          : t3_rows<R, false, false>(in, mc, gc, &rows[0][0], 24);
+            }
+        } else {
+            ElemIn<4> in;
+            for (int a = 0; a < 4; a++) {
+                int64_t node = conn[4 * e + a] - 1;
+                for (int c = 0; c < 3; c++) {
+                    in.X[a][c] = xyz[node + c * nnodes];
+                    in.nrm[a][c] = normals[node + c * nnodes];
+                }
+                in.valid[a] = valid[node] != 0;
+            }
+            in.t = thick[e];
+            Q4Elem qe;
+            q4_prepare(in, qe);
+            double tr[4] = {0, 0, 0, 0};
+            for (int j = 0; j < 4; j++) {
+                double trj[4];
+                st |= comp ? q4_point_rows<R, true>(in, qe, j, mc, gc, &rows[8 * j][0], 24, trj)
+                           : q4_point_rows<R, false>(in, qe, j, mc, gc, &rows[8 * j][0], 24, trj);
+                for (int k = 0; k < 4; k++) tr[k] += trj[k];
+            }
+            q4_drill_rows<R>(in, tr, mc.drill_scale, &rows[32][0], 24);
+            nrows = 36;
+        }
+        if (st) return 10 + st;
+        double *K = out + (int64_t)nd * nd * e;
+        for (int j = 0; j < nd; j++)
+            for (int i = 0; i < nd; i++) {
+                R s = 0;
+                for (int r = 0; r < nrows; r++) s += rows[r][i] * rows[r][j];
+                K[i + nd * j] = (double)s;
+            }
+    }
+    return 0;
+}
+
+extern "C" int hc_element_matrices(int etype, int precision, int64_t nnodes, const double *xyz,
+                                   int64_t nelem, const int64_t *conn, const double *normals,
+                                   const uint8_t *valid, const double *thick,
+                                   const fs_shell_params *p, const fs_layup_group *groups,
+                                   const int32_t *egroup, double *out)
+{
+    if (precision == FS_FP64)
+        return elem_matrices<double>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
+                                     egroup, out);
+    return elem_matrices<float>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
+                                egroup, out);
+}
+
+extern "C" int hc_lumped(int etype, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                         const double *thick, double rho, const fs_layup_group *groups,
+                         const int32_t *egroup, double *out)
+{
+    bool comp = (etype == FS_T3FFCOMP || etype == FS_Q4RSCOMP);
+    int nn = (etype == FS_T3FF || etype == FS_T3FFCOMP) ? 3 : 4;
+    for (int64_t e = 0; e < nelem; e++) {
+        GroupConst gc;
+        if (comp) prepare_group(groups[egroup[e]], gc);
+        if (nn == 3) {
+            ElemIn<3> in;
+            for (int a = 0; a < 3; a++)
+                for (int c = 0; c < 3; c++) in.X[a][c] = xyz[(conn[3 * e + a] - 1) + c * nnodes];
+            in.t = thick[e];
+            lumped_mass<3>(in, rho, comp, &gc, out[2 * e], out[2 * e + 1]);
+        } else {
+            ElemIn<4> in;
+            for (int a = 0; a < 4; a++)
+                for (int c = 0; c < 3; c++) in.X[a][c] = xyz[(conn[4 * e + a] - 1) + c * nnodes];
+            in.t = thick[e];
+            lumped_mass<4>(in, rho, comp, &gc, out[2 * e], out[2 * e + 1]);
+        }
+    }
+    return 0;
+}

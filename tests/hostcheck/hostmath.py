@@ -1,0 +1,55 @@
+"""Loader of the test-only host build of the CUDA library's element math."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from flexshell import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+CSRC = os.path.join(ROOT, "finetoolsflexstructures.jl_gb300", "csrc")
+LIB = os.path.join(HERE, "_build", "libhostcheck.so")
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        os.makedirs(os.path.dirname(LIB), exist_ok=True)
+        srcs = [os.path.join(HERE, "hostcheck.cpp"), os.path.join(CSRC, "fs_elem_math.cuh"),
+                os.path.join(CSRC, "fs_host_prep.h")]
+        if not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in srcs):
+            tmp = LIB + ".tmp%d" % os.getpid()
+            subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-I", CSRC,
+                            srcs[0], "-o", tmp], check=True)
+            os.replace(tmp, LIB)
+        _lib = ctypes.CDLL(LIB)
+    return _lib
+
+
+def element_matrices(etype, precision, xyz, conn, normals, valid, thickness, params,
+                     groups=None, egroup=None):
+    xyz = np.asfortranarray(xyz, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int64)
+    normals = np.asfortranarray(normals, dtype=np.float64)
+    valid = np.ascontiguousarray(valid, dtype=np.uint8)
+    nelem = conn.shape[0]
+    th = np.ascontiguousarray(np.broadcast_to(np.asarray(thickness, float), (nelem,)))
+    nd = 6 * conn.shape[1]
+    out = np.zeros((nelem, nd, nd))
+    garr = None
+    eg = None
+    if groups is not None:
+        garr = (_abi.fs_layup_group * len(groups))(*groups)
+        eg = np.ascontiguousarray(egroup if egroup is not None else np.zeros(nelem), dtype=np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+    st = lib().hc_element_matrices(
+        ctypes.c_int(etype), ctypes.c_int(precision), ctypes.c_int64(xyz.shape[0]), P(xyz),
+        ctypes.c_int64(nelem), P(conn), P(normals), P(valid), P(th), ctypes.byref(params),
+        garr, P(eg), P(out))
+    if st != 0:
+        raise RuntimeError("host check failed with status %d" % st)
+    return out.transpose(0, 2, 1).copy()

@@ -118,3 +118,14 @@ def jittered_plate(n, quads, side=1.0, jitter=0.2, seed=0, wavy=0.0, clamp_x0=Tr
         fixed[np.abs(xyz[:, 0]) < 1e-12 * side, :] = True
     dof, nfree = mesh.numberdofs(fixed)
     return xyz, conn, dof, nfree
+
+
+def cross_ply_groups(angles=(0, 90, 90, 0), ply_t=0.25e-3, E1=140e9, E2=10e9, G12=5e9, G13=5e9,
+                     G23=3.5e9, nu12=0.3, rho=1600.0, csmat=None):
+    """Plies of one layup (CompositeLayupModule.Ply, src/CompositeLayupModule.jl:71-97):
+    list of dicts with the ply plane-stress Dps, transverse Dts, thickness,
+    angle and density."""
+    from flexshell import materials
+    mat = materials.lamina_material(rho, E1, E2, nu12, G12, G13, G23)
+    Dps, Dts = materials.shell_material_stiffness(mat)
+    return [dict(Dps=Dps, Dts=Dts, thickness=ply_t, angle=a, rho=rho) for a in angles]

@@ -1,0 +1,280 @@
+"""GPU parity of the CUDA library against the oracle, through the C ABI.
+
+Tolerances: the FP64 path must match the oracle within 1e-12 relative
+(max-abs difference over max-abs value, per matrix) with an identical
+sparsity pattern; the mixed path within 1e-6.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+import flexshell as F
+from flexshell import _abi
+from oracle import oracle as O
+import problems as PB
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 1e-6
+
+
+def relmax(A, B):
+    A = A.toarray() if hasattr(A, "toarray") else A
+    B = B.toarray() if hasattr(B, "toarray") else B
+    return np.abs(A - B).max() / np.abs(B).max()
+
+
+def same_pattern(A, B):
+    A = A.tocsc()
+    B = B.tocsc()
+    A.has_sorted_indices and B.has_sorted_indices
+    return (A.shape == B.shape and np.array_equal(A.indptr, B.indptr)
+            and np.array_equal(A.indices, B.indices))
+
+
+def same_pattern_modulo_cancellation(A, B, rel=1e-14):
+    """Patterns of two zero-dropping (SysmatAssemblerSparseSymm) results: an
+    entry may be stored in only one of them when its exact value is zero and
+    one operation order cancels it exactly while the other leaves round-off;
+    such entries must be below `rel` times the largest entry in both."""
+    A = A.tocsc()
+    B = B.tocsc()
+    if A.shape != B.shape:
+        return False
+    PA = (A != 0).astype(np.int8)
+    PB_ = (B != 0).astype(np.int8)
+    D = (PA - PB_).tocoo()
+    scale = max(abs(A).max(), abs(B).max())
+    for r, c in zip(D.row[D.data != 0], D.col[D.data != 0]):
+        if abs(A[r, c]) > rel * scale or abs(B[r, c]) > rel * scale:
+            return False
+    return True
+
+
+def homog_pair(d, quads, tsf=0):
+    et = O.Q4RS if quads else O.T3FF
+    P = O.Problem(et, d["xyz"], d["conn"], d["dofnums"], thickness=d["thickness"],
+                  material=d["material"], stab_c=d["stab_c"], tsf=tsf)
+    P.compute_normals()
+    m = d["material"]
+    mat = _Mat(m)
+    cls = F.FEMMShellQ4RS if quads else F.FEMMShellT3FF
+    femm = cls(d["conn"], d["thickness"], mat, stab_fun=d["stab_c"])
+    femm.transv_shear_formulation = tsf
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    femm.associategeometry(geom0)
+    return P, femm, geom0, dchi
+
+
+class _Mat:
+    """Material given directly by its plane-stress and shear matrices."""
+
+    def __init__(self, m):
+        self.m = m
+
+    def massdensity(self):
+        return self.m.get("rho", 0.0)
+
+
+# materials.shell_material_stiffness needs tangentmoduli; route _Mat through it
+import flexshell.materials as _materials
+
+_orig = _materials.shell_material_stiffness
+
+
+def _sms(material):
+    if isinstance(material, _Mat):
+        return np.asarray(material.m["Dps"]), np.asarray(material.m["Dt"])
+    return _orig(material)
+
+
+_materials.shell_material_stiffness = _sms
+
+
+@pytest.mark.parametrize("orientation", ["a", "b"])
+def test_fv12_gpu_matches_oracle_and_reference(orientation):
+    d = PB.fv12(orientation)
+    P, femm, geom0, dchi = homog_pair(d, False)
+    # normals
+    assert np.allclose(femm._normals, P.normals, rtol=0, atol=1e-14)
+    assert np.array_equal(femm._normal_valid, P.valid)
+    K = femm.stiffness(F.SysmatAssemblerSparseSymm(), geom0, None, None, dchi)
+    M = femm.mass(F.SysmatAssemblerSparseSymm(), geom0, dchi)
+    Ko = P.assemble_scipy("K", O.DROP_ZEROS)
+    Mo = P.assemble_scipy("M", O.DROP_ZEROS)
+    assert same_pattern_modulo_cancellation(K, Ko)
+    assert same_pattern(M, Mo)
+    # the structural pattern (SysmatAssemblerSparse) is bit-exact
+    Kk = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    assert same_pattern(Kk, P.assemble_scipy("K", O.KEEP_ZEROS))
+    assert relmax(K, Ko) <= FP64_TOL
+    assert relmax(M, Mo) <= FP64_TOL
+    w = sl.eigh(K.toarray(), M.toarray(), eigvals_only=True)
+    fs = np.sqrt(np.abs(w[:14])) / (2 * np.pi)
+    np.testing.assert_allclose(fs[6:], np.array(PB.FV12_REF)[6:], rtol=1e-6)
+    femm.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+@pytest.mark.parametrize("n", [4, 8])
+def test_scordelis_lo_gpu(quads, n):
+    d = PB.scordelis_lo(quads, n)
+    P, femm, geom0, dchi = homog_pair(d, quads)
+    K = femm.stiffness(F.SysmatAssemblerSparseSymm(), geom0, None, None, dchi)
+    Ko = P.assemble_scipy("K", O.DROP_ZEROS)
+    assert same_pattern_modulo_cancellation(K, Ko)
+    assert relmax(K, Ko) <= FP64_TOL
+    Kk = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    assert same_pattern(Kk, P.assemble_scipy("K", O.KEEP_ZEROS))
+    v = PB.solve_probe(K, d)
+    ref = (PB.SLO_Q4_REF if quads else PB.SLO_T3_REF)[PB.SLO_N.index(n)]
+    assert abs(v - ref) <= 1e-4 * abs(ref)
+    # element matrices, FP64 and mixed
+    Ke = femm.element_matrices(geom0, F.FS_FP64)
+    Keo = P.element_stiffness()
+    assert max(relmax(Ke[e], Keo[e]) for e in range(len(Ke))) <= FP64_TOL
+    Km = femm.element_matrices(geom0, F.FS_MIXED)
+    assert relmax(Km, Keo) <= MIXED_TOL
+    femm.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+def test_plate_assemblers_and_mixed(quads):
+    xyz, conn, dof, nfree = PB.jittered_plate(12, quads, wavy=0.01, seed=3)
+    from flexshell import materials
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(200e9, 0.3, 7850.0))
+    d = dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=0.005,
+             material=dict(Dps=Dps, Dt=Dt, rho=7850.0), stab_c=0.1 if quads else 5 / 12 / 1.5)
+    P, femm, geom0, dchi = homog_pair(d, quads)
+    for asm, mode in ((F.SysmatAssemblerSparse(), O.KEEP_ZEROS),
+                      (F.SysmatAssemblerSparseSymm(), O.DROP_ZEROS)):
+        K = femm.stiffness(asm, geom0, None, None, dchi)
+        Ko = P.assemble_scipy("K", mode)
+        if mode == O.KEEP_ZEROS:
+            assert same_pattern(K, Ko)
+        else:
+            assert same_pattern_modulo_cancellation(K, Ko)
+        assert relmax(K, Ko) <= FP64_TOL
+        Km = femm.stiffness(asm, geom0, None, None, dchi, precision=F.FS_MIXED)
+        assert relmax(Km, Ko) <= MIXED_TOL
+        M = femm.mass(asm, geom0, dchi)
+        Mo = P.assemble_scipy("M", mode)
+        assert same_pattern(M, Mo)
+        assert relmax(M, Mo) <= FP64_TOL
+    # free-free block and diagonal mass
+    K = femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi)
+    Ko = P.assemble_scipy("K", O.KEEP_ZEROS, n=nfree)
+    assert same_pattern(K, Ko) and relmax(K, Ko) <= FP64_TOL
+    M = femm.mass(F.SysmatAssemblerSparseDiag(), geom0, dchi)
+    Mo = P.assemble_scipy("M", O.DIAG)
+    assert same_pattern(M, Mo) and relmax(M, Mo) <= FP64_TOL
+    # the assembly is deterministic: bitwise identical on a second run
+    K1 = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    K2 = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    assert np.array_equal(K1.data, K2.data)
+    femm.close()
+
+
+def test_t3_average_k_gpu():
+    d = PB.scordelis_lo(False, 4)
+    P, femm, geom0, dchi = homog_pair(d, False, tsf=1)
+    K = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    Ko = P.assemble_scipy("K", O.KEEP_ZEROS)
+    assert same_pattern(K, Ko) and relmax(K, Ko) <= FP64_TOL
+    femm.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+def test_composite_gpu(quads):
+    plies = PB.cross_ply_groups((30, -45, 60, 0))
+    A, B, D, H, md, mi = O.laminate(plies)
+    g = F.laminate(plies)
+    for name, ref in (("A", A), ("B", B), ("D", D)):
+        got = np.array(getattr(g, name)).reshape(3, 3, order="F")
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(A).max()
+    c, s = np.cos(0.4), np.sin(0.4)
+    cs = np.array([[c, -s, 0], [s, c, 0], [0, 0, 1.0]])
+    g.csmat[:] = list(cs.flatten(order="F"))
+    t = sum(p["thickness"] for p in plies)
+    xyz, conn, dof, nfree = PB.jittered_plate(8, quads, wavy=0.02, seed=7)
+    et = O.Q4RSCOMP if quads else O.T3FFCOMP
+    stab_c = 0.1 if quads else 5 / 12 / 1.5
+    P = O.Problem(et, xyz, conn, dof, groups=[dict(A=A, B=B, D=D, H=H, csmat=cs, thickness=t,
+                                                   mass=md, moi=mi)], stab_c=stab_c)
+    P.compute_normals()
+    cls = F.FEMMShellQ4RSComp if quads else F.FEMMShellT3FFComp
+    femm = cls(conn, g, stab_fun=stab_c)
+    geom0 = F.NodalField(xyz)
+    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(dof)
+    femm.associategeometry(geom0)
+    assert np.allclose(femm._normals, P.normals, atol=1e-14)
+    K = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    Ko = P.assemble_scipy("K", O.KEEP_ZEROS)
+    assert same_pattern(K, Ko) and relmax(K, Ko) <= FP64_TOL
+    Km = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi, precision=F.FS_MIXED)
+    assert relmax(Km, Ko) <= MIXED_TOL
+    M = femm.mass(F.SysmatAssemblerSparseSymm(), geom0, dchi)
+    Mo = P.assemble_scipy("M", O.DROP_ZEROS)
+    assert same_pattern(M, Mo) and relmax(M, Mo) <= FP64_TOL
+    femm.close()
+
+
+def test_errors_are_reported_not_trapped():
+    d = PB.scordelis_lo(False, 4)
+    femm = F.FEMMShellT3FF(d["conn"], 0.25, _Mat(d["material"]), stab_fun=0.2)
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    with pytest.raises(AssertionError):
+        femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    bad = d["conn"].copy()
+    bad[0, 0] = d["xyz"].shape[0] + 5
+    femm2 = F.FEMMShellT3FF(bad, 0.25, _Mat(d["material"]), stab_fun=0.2)
+    with pytest.raises(F.FlexShellError) as ei:
+        femm2.associategeometry(geom0)
+    assert ei.value.code == _abi.FS_ERR_BAD_INPUT
+    femm.close()
+    femm2.close()
+
+
+def test_explicit_steps_match_oracle():
+    xyz, conn, dof, nfree = PB.jittered_plate(10, True, seed=2)
+    from flexshell import materials
+    mat = materials.MatDeforElastIso(200e9, 0.3, 7850.0)
+    femm = F.FEMMShellQ4RS(conn, 0.01, mat)
+    geom0 = F.NodalField(xyz)
+    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(dof)
+    femm.associategeometry(geom0)
+    M = femm.mass(F.SysmatAssemblerFFBlock(F.SysmatAssemblerSparseDiag(), nfree), geom0, dchi)
+    K = femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi).tocsr()
+    m = M.diagonal()
+    w2 = sl.eigh(K.toarray(), np.diag(m), eigvals_only=True)[-1]
+    dt = 0.9 * 2 / np.sqrt(w2)
+    C = 0.01 * m
+    invMC = 1.0 / (m + dt / 2 * C)
+    rng = np.random.default_rng(0)
+    V0 = rng.normal(0, 1e-3, nfree)
+    nsteps = 200
+    U, V, A = np.zeros(nfree), V0.copy(), np.zeros(nfree)
+    O.cd_steps(K.indptr, K.indices, K.data, invMC, C, dt, nsteps, U, V, A)
+    for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 1e-5)):
+        ctx = femm.ctx
+        import ctypes
+        from flexshell._lib import ptr
+        invMC_c = np.ascontiguousarray(invMC)
+        C_c = np.ascontiguousarray(C)
+        ctx.call("fs_explicit_setup", prec, ptr(invMC_c), ptr(C_c), ctypes.c_double(dt))
+        z = np.zeros(nfree)
+        v0 = V0.copy()
+        ctx.call("fs_explicit_set_state", ptr(z), ptr(v0), ptr(z))
+        ctx.call("fs_explicit_run", nsteps)
+        Ug, Vg, Ag = np.zeros(nfree), np.zeros(nfree), np.zeros(nfree)
+        ctx.call("fs_explicit_get_state", ptr(Ug), ptr(Vg), ptr(Ag))
+        assert np.abs(Ug - U).max() <= tol * np.abs(U).max()
+        assert np.abs(Vg - V).max() <= tol * np.abs(V).max()
+    femm.close()
