@@ -138,6 +138,8 @@ int build_pattern(fs_ctx *c, int64_t n);
 int launch_normals(fs_ctx *c);
 int launch_elements(fs_ctx *c, int precision);
 int launch_gather(fs_ctx *c, int precision, double *vals);
+int launch_elements_to(fs_ctx *c, int precision, void *ke);
+int launch_gather_from(fs_ctx *c, int precision, const void *ke, double *vals);
 int launch_masses(fs_ctx *c);
 int assemble_mass(fs_ctx *c, int assembler, int64_t n);
 int compact_zeros(fs_ctx *c, int64_t n, const int64_t *rowptr, const int32_t *colidx,

@@ -514,3 +514,47 @@ int assemble_mass(fs_ctx *c, int assembler, int64_t n)
 }
 
 }  // namespace fs
+
+namespace fs {
+
+// Element matrices of every element into a caller-chosen buffer `ke`
+// (same layout as the context's own buffer); allocates nothing.
+int launch_elements_to(fs_ctx *c, int precision, void *ke)
+{
+    MeshDev &m = c->mesh;
+    if (m.nelem == 0) return FS_OK;
+    bool comp = (m.etype == FS_T3FFCOMP || m.etype == FS_Q4RSCOMP);
+    bool avgk = c->params.transv_shear_formulation == 1;
+    if (m.nen == 3) {
+        if (precision == FS_FP64) {
+            double *k = (double *)ke;
+            if (comp) return avgk ? run_t3<double, true, true>(c, k) : run_t3<double, true, false>(c, k);
+            return avgk ? run_t3<double, false, true>(c, k) : run_t3<double, false, false>(c, k);
+        }
+        float *k = (float *)ke;
+        if (comp) return avgk ? run_t3<float, true, true>(c, k) : run_t3<float, true, false>(c, k);
+        return avgk ? run_t3<float, false, true>(c, k) : run_t3<float, false, false>(c, k);
+    }
+    if (precision == FS_FP64) {
+        double *k = (double *)ke;
+        return comp ? run_q4<double, true>(c, k) : run_q4<double, false>(c, k);
+    }
+    float *k = (float *)ke;
+    return comp ? run_q4<float, true>(c, k) : run_q4<float, false>(c, k);
+}
+
+// CSR values from element matrices held in `ke`; allocates nothing.
+int launch_gather_from(fs_ctx *c, int precision, const void *ke, double *vals)
+{
+    MeshDev &m = c->mesh;
+    if (m.nnodes == 0) return FS_OK;
+    unsigned g = nblk2(m.nnodes, GATHER_WARPS);
+    if (precision == FS_FP64)
+        k_gather<double><<<g, GATHER_WARPS * 32, 0, c->stream>>>(m, c->pat, c->pat.n, (const double *)ke, vals);
+    else
+        k_gather<float><<<g, GATHER_WARPS * 32, 0, c->stream>>>(m, c->pat, c->pat.n, (const float *)ke, vals);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+}  // namespace fs

@@ -50,6 +50,7 @@ def lib():
                                        _c_i64_p, _c_i64_p]
         L.fs_element_matrices.argtypes = [vp, ctypes.c_int, vp]
         L.fs_timings.argtypes = [vp, vp, ctypes.c_int]
+        L.fs_stiffness_values_noalloc.argtypes = [vp, ctypes.c_int, ctypes.c_int64, vp, ctypes.c_int64]
         L.fs_geometry_set.argtypes = [vp, vp]
         L.fs_dofs_set.argtypes = [vp, vp]
         L.fs_element_masses.argtypes = [vp, vp]

@@ -142,6 +142,21 @@ int fs_matrix_device(fs_ctx *ctx, const int64_t **rowptr, const int32_t **colidx
  * fs_stiffness call: [0] element kernel, [1] CSR gather, [2] symbolic phase of
  * the last pattern build, [3] zero compaction.  `n` entries are written. */
 int fs_timings(const fs_ctx *ctx, double *out, int n);
+/* Allocation-free stiffness values.  No counterpart in the reference: it is for
+ * callers that cannot let the library allocate device memory at call time (a
+ * host whose own pool allocator owns the device memory, or a solver loop under
+ * a fixed memory budget).  It writes the CSR values of the stiffness, in the
+ * order of the pattern that fs_stiffness with FS_ASM_SPARSE returns, into the
+ * caller's device buffer `vals` (vals_len >= nnz).  The pattern for `nrows`
+ * must exist (one fs_stiffness or fs_mass call at set-up).  Element matrices
+ * are staged in a fixed 32 MiB device array inside the library, so
+ * nelem * (6 nen)^2 * (8 for FS_FP64, 4 for FS_MIXED) bytes must fit in it
+ * (e.g. 12,945 T3FF elements in FP64); larger meshes get FS_ERR_UNSUPPORTED.
+ * It calls no cudaMalloc/cudaFree.  The first call on a device looks up the
+ * array's address (make it before any stream capture); calls that overlap on
+ * the GPU share the array and race. */
+int fs_stiffness_values_noalloc(fs_ctx *ctx, int precision, int64_t nrows, double *vals,
+                                int64_t vals_len);
 /* Element matrices in the global basis (nelem x (6 nen)^2, each column-major), in
  * mesh order; for parity checks. */
 int fs_element_matrices(fs_ctx *ctx, int precision, double *out);
