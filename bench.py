@@ -188,6 +188,77 @@ class Assembler:
         return v
 
 
+def explicit_c5(torch, device=0, n=512, nsteps=10000, iters=200):
+    """Explicit dynamics (the reference's configuration 5): Q4RS 512 x 512 plate,
+    t = 0.01, steel, simply supported (w = 0 on the boundary), lumped mass,
+    V0_z = 1e-3 sin(pi x) sin(pi y) + N(0, 1e-5) (seed 5), no damping,
+    dt = 0.9 * 2 / omega_max (power iteration), 10,000 steps, stiffness values
+    in float (mixed) and double, state in double with Kahan compensation."""
+    from flexshell import _abi, mesh
+    from flexshell._lib import Context, ptr
+    xyz, conn = mesh.jittered_plate_q(n, 1.0, 0.0, 0, None)
+    xyz = np.asfortranarray(xyz)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    x, y = xyz[:, 0], xyz[:, 1]
+    bnd = (x < 1e-12) | (x > 1 - 1e-12) | (y < 1e-12) | (y > 1 - 1e-12)
+    fixed[bnd, 2] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    dof = np.asfortranarray(dof)
+    ctx = Context(device)
+    ctx.call("fs_mesh_set", _abi.FS_Q4RS, xyz.shape[0], ptr(xyz), conn.shape[0], ptr(np.ascontiguousarray(conn)),
+             None, ptr(dof))
+    from flexshell import materials
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, NU, RHO))
+    ctx.call("fs_params_set", _abi.make_params(Dps, Dt, RHO, 0.01, quads=True), None)
+    ctx.call("fs_normals_compute")
+    nnz = ctypes.c_int64()
+    ctx.call("fs_mass", _abi.FS_ASM_DIAG, ctypes.c_int64(nfree), ctypes.byref(nnz))
+    m = np.empty(nfree)
+    ctx.call("fs_matrix_copy", None, None, ptr(m))
+    ctx.call("fs_stiffness", _abi.FS_FP64, _abi.FS_ASM_SPARSE, ctypes.c_int64(nfree), ctypes.byref(nnz))
+    om = ctypes.c_double()
+    ctx.call("fs_power_iteration", ptr(m), ctypes.c_int64(iters), ctypes.c_uint64(1), ctypes.byref(om))
+    dt = 0.9 * 2.0 / om.value
+    rng = np.random.Generator(np.random.PCG64(5))
+    V0 = np.zeros(nfree)
+    wd = dof[:, 2]
+    free_w = wd <= nfree
+    V0[wd[free_w] - 1] = 1e-3 * np.sin(np.pi * x[free_w]) * np.sin(np.pi * y[free_w]) + rng.normal(0, 1e-5, free_w.sum())
+    C = np.zeros(nfree)
+    invMC = 1.0 / m
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    out = {}
+    finals = {}
+    for prec in (_abi.FS_MIXED, _abi.FS_FP64):
+        ctx.call("fs_explicit_setup", prec, ptr(invMC), ptr(C), ctypes.c_double(dt))
+        z = np.zeros(nfree)
+        ctx.call("fs_explicit_set_state", ptr(z), ptr(V0), ptr(z))
+        ctx.call("fs_explicit_run", ctypes.c_int64(64))  # warm-up (graph capture)
+        ctx.call("fs_explicit_set_state", ptr(z), ptr(V0), ptr(z))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ctx.call("fs_explicit_run", ctypes.c_int64(nsteps))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        U = np.empty(nfree)
+        ctx.call("fs_explicit_get_state", ptr(U), None, None)
+        finals[prec] = U
+        name = "mixed" if prec == _abi.FS_MIXED else "fp64"
+        out["steps_per_s_" + name] = nsteps / (ms * 1e-3)
+        out["ms_per_step_" + name] = ms / nsteps
+    U32, U64 = finals[_abi.FS_MIXED], finals[_abi.FS_FP64]
+    out.update({"elements": conn.shape[0], "dofs": nfree, "nnz": nnz.value, "steps": nsteps,
+                "omega_max": om.value, "dt": dt, "power_iterations": iters,
+                "final_u_rel_err_mixed_vs_fp64": float(np.abs(U32 - U64).max() / np.abs(U64).max()),
+                "final_u_max": float(np.abs(U64).max()),
+                "bytes_per_step_mixed": nnz.value * 8 + nfree * 8 * 12,
+                "bytes_per_step_fp64": nnz.value * 12 + nfree * 8 * 12})
+    ctx.close()
+    return out
+
+
 def time_steps(asm, precision, steps, warmup, torch, stream):
     for _ in range(warmup):
         asm.stiffness(precision)
@@ -211,6 +282,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--n", type=int, default=1024, help="quads per side")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-explicit", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -303,6 +375,7 @@ def main():
     asm.ctx.close()
     del asm
 
+    ex = explicit_c5(torch, device=local) if not args.no_explicit else None
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -359,6 +432,7 @@ def main():
                      "rel_err_K_mixed_vs_fp64_max": err_q4, "ms_elements_mixed": ph_q_mixed[0],
                      "ms_gather_mixed": ph_q_mixed[1], "ms_elements_fp64": ph_q_fp64[0],
                      "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4},
+            "explicit_q4rs_512": ex,
         },
     }
     print(json.dumps(line))

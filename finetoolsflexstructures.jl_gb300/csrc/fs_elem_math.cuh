@@ -73,10 +73,19 @@ FS_HD void make_frame(const double a[3], const double b[3], double e[3][3])
 // the rotation by the vector a = e3_e x n_e (angle |a|, FinEtools rotmat3!),
 // in Rodrigues form R = I + s(x) [a]x + c(x) [a]x^2 with x = |a|^2,
 // s = sin(phi)/phi, c = (1 - cos(phi))/phi^2.  Both are evaluated from
-// their Taylor series in x (9 terms: truncation below 1e-17 for x <= 1).
+// their Taylor series in x (up to 9 terms: truncation below 1e-17 for x <= 1,
+// fewer terms for the small angles of smooth meshes).
 FS_HD void sinc_cosc(double x, double &s, double &c)
 {
-    if (x <= 1.0) {
+    if (x < 1.0e-8) {
+        // truncation below x^2/5! < 1e-18
+        s = 1.0 - x * (1.0 / 6.0);
+        c = 0.5 - x * (1.0 / 24.0);
+    } else if (x < 1.0e-4) {
+        // truncation below x^4/9! < 3e-22
+        s = 1.0 - x * (1.0 / 6.0 - x * (1.0 / 120.0 - x * (1.0 / 5040.0)));
+        c = 0.5 - x * (1.0 / 24.0 - x * (1.0 / 720.0 - x * (1.0 / 40320.0)));
+    } else if (x <= 1.0) {
         // s = sum (-x)^k/(2k+1)!,  c = sum (-x)^k/(2k+2)!
         s = 1.0 / 355687428096000.0;              // 1/17!
         s = 1.0 / 1307674368000.0 - x * s;        // 1/15!
@@ -140,7 +149,8 @@ template <class R, int NN> struct GlobalMap {
     R g[NN][2];     // basis function gradients on the element basis
 };
 
-// Build the map from the double-precision frame and triads.
+// Build the map from the double-precision frame and triads (the products
+// below are transformation arithmetic and run in the working precision).
 template <class R, int NN>
 FS_HD void build_map(const double e[3][3], const double A[NN][3][3], const R g[NN][2],
                      GlobalMap<R, NN> &M)
@@ -148,14 +158,17 @@ FS_HD void build_map(const double e[3][3], const double A[NN][3][3], const R g[N
     for (int k = 0; k < 3; k++)
         for (int c = 0; c < 3; c++) M.e[k][c] = (R)e[k][c];
     for (int i = 0; i < NN; i++) {
+        R Ar[3][3];
+        for (int r = 0; r < 3; r++)
+            for (int k = 0; k < 3; k++) Ar[r][k] = (R)A[i][r][k];
         for (int k = 0; k < 3; k++)
             for (int c = 0; c < 3; c++)
-                M.t[i][k][c] = (R)(A[i][0][k] * e[0][c] + A[i][1][k] * e[1][c] + A[i][2][k] * e[2][c]);
-        double inv33 = 1.0 / A[i][2][2];
+                M.t[i][k][c] = Ar[0][k] * M.e[0][c] + Ar[1][k] * M.e[1][c] + Ar[2][k] * M.e[2][c];
+        R inv33 = (R)1 / Ar[2][2];
         for (int r = 0; r < 2; r++) {
-            for (int k = 0; k < 3; k++) M.A01[i][r][k] = (R)A[i][r][k];
-            M.m[i][r] = (R)(A[i][r][2] * inv33);
-            for (int cl = 0; cl < 2; cl++) M.R2[i][r][cl] = (R)(A[i][r][cl] - inv33 * A[i][r][2] * A[i][cl][2]);
+            for (int k = 0; k < 3; k++) M.A01[i][r][k] = Ar[r][k];
+            M.m[i][r] = Ar[r][2] * inv33;
+            for (int cl = 0; cl < 2; cl++) M.R2[i][r][cl] = Ar[r][cl] - inv33 * Ar[r][2] * Ar[cl][2];
         }
         M.g[i][0] = g[i][0];
         M.g[i][1] = g[i][1];
@@ -216,11 +229,11 @@ FS_HD int lp(int r, int c) { return r * (r + 1) / 2 + c; }  // packed lower inde
 
 // rows_out[r] = scale * sum_{c>=r} L[c][r] rows_in[c]   (L^T applied to stacked rows)
 template <class R, int NN, int NR>
-FS_HD void mix_rows(const double *Lpk, double scale, const R in[NR][NN][5], R out[NR][NN][5])
+FS_HD void mix_rows(const double *Lpk, R scale, const R in[NR][NN][5], R out[NR][NN][5])
 {
     for (int r = 0; r < NR; r++) {
         R f[NR];
-        for (int c = 0; c < NR; c++) f[c] = (c >= r) ? (R)(scale * Lpk[lp(c, r)]) : (R)0;
+        for (int c = 0; c < NR; c++) f[c] = (c >= r) ? scale * (R)Lpk[lp(c, r)] : (R)0;
         for (int i = 0; i < NN; i++)
             for (int q = 0; q < 5; q++) {
                 R s = 0;
@@ -372,9 +385,10 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
         for (int r = 0; r < 3; r++)
             for (int i = 0; i < 3; i++)
                 for (int q = 0; q < 5; q++) { inm[r][i][q] = mb[r][i][q]; inb[r][i][q] = mb[3 + r][i][q]; }
-        mix_rows<R, 3, 3>(mc.Lps, sqrt(t * Ae), inm, (R(*)[3][5])mixed[0]);
-        mix_rows<R, 3, 3>(mc.Lps, sqrt(t * t * t / 12 * Ae), inb, (R(*)[3][5])mixed[3]);
-        double ws = t * stab * Ae * (AVGK ? 1.0 / 3 : 1.0);
+        R tr_ = (R)t, Ar_ = (R)Ae;
+        mix_rows<R, 3, 3>(mc.Lps, sqrt(tr_ * Ar_), inm, (R(*)[3][5])mixed[0]);
+        mix_rows<R, 3, 3>(mc.Lps, sqrt(tr_ * tr_ * tr_ / 12 * Ar_), inb, (R(*)[3][5])mixed[3]);
+        R ws = tr_ * (R)stab * Ar_ * (R)(AVGK ? 1.0 / 3 : 1.0);
         for (int o = 0; o < NS / 2; o++)
             mix_rows<R, 3, 2>(mc.Lt, sqrt(ws), (R(*)[3][5])sh[2 * o], (R(*)[3][5])mixed[6 + 2 * o]);
     } else {
@@ -382,8 +396,8 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
         layup_angle(e, gc->csmat, lm, ln);
         rotate3<R, 3>(lm, ln, (R(*)[3][5])mb[0]);
         rotate3<R, 3>(lm, ln, (R(*)[3][5])mb[3]);
-        mix_rows<R, 3, 6>(gc->L6, sqrt(Ae), mb, (R(*)[3][5])mixed[0]);
-        double ws = stab * Ae * (AVGK ? 1.0 / 3 : 1.0);
+        mix_rows<R, 3, 6>(gc->L6, sqrt((R)Ae), mb, (R(*)[3][5])mixed[0]);
+        R ws = (R)stab * (R)Ae * (R)(AVGK ? 1.0 / 3 : 1.0);
         for (int o = 0; o < NS / 2; o++) {
             rotate2<R, 3>(lm, ln, (R(*)[3][5])sh[2 * o]);
             mix_rows<R, 3, 2>(gc->LH, sqrt(ws), (R(*)[3][5])sh[2 * o], (R(*)[3][5])mixed[6 + 2 * o]);
@@ -391,26 +405,22 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
     }
     // --- drilling factor (double): mean of the nodal-basis bending
     //     diagonals, src/FEMMShellT3FFModule.jl:713-727 ---
-    double ksum = 0.0;
+    R ksumr = 0;
     for (int i = 0; i < 3; i++)
-        for (int cl = 0; cl < 2; cl++) {
-            double s2 = 0.0;
+        for (int cl = 0; cl < 2; cl++)
             for (int r = 0; r < 6 + NS; r++) {
-                double v = (double)mixed[r][i][3] * (double)M.R2[i][0][cl] +
-                           (double)mixed[r][i][4] * (double)M.R2[i][1][cl];
-                s2 += v * v;
+                R v = mixed[r][i][3] * M.R2[i][0][cl] + mixed[r][i][4] * M.R2[i][1][cl];
+                ksumr += v * v;
             }
-            ksum += s2;
-        }
-    double kavg = ksum / 6.0 * mc.drill_scale;
+    double kavg = (double)ksumr / 6.0 * mc.drill_scale;
     // --- global rows ---
     for (int r = 0; r < 6 + NS; r++) expand_row<R, 3>(M, (const R(*)[5])mixed[r], rows + r * rs);
-    double sk = kavg > 0.0 ? sqrt(kavg) : 0.0;
+    R sk = kavg > 0.0 ? sqrt((R)kavg) : (R)0;
     for (int i = 0; i < 3; i++) {
         R *o = rows + (6 + NS + i) * rs;
         for (int q = 0; q < 18; q++) o[q] = 0;
         if (in.valid[i])
-            for (int c = 0; c < 3; c++) o[6 * i + 3 + c] = (R)(sk * (double)M.t[i][2][c]);
+            for (int c = 0; c < 3; c++) o[6 * i + 3 + c] = sk * M.t[i][2][c];
     }
     return (kavg < 0.0) ? 2 : 0;
 }
@@ -520,9 +530,13 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     make_frame(J0, J1, e);
     // element coordinates (centroid relative) and basis gradients
     R X[4], Y[4];
-    for (int a = 0; a < 4; a++) {
-        X[a] = (R)dot3(qe.Xr[a], e[0]);
-        Y[a] = (R)dot3(qe.Xr[a], e[1]);
+    {
+        R e0r[3] = {(R)e[0][0], (R)e[0][1], (R)e[0][2]}, e1r[3] = {(R)e[1][0], (R)e[1][1], (R)e[1][2]};
+        for (int a = 0; a < 4; a++) {
+            R xr[3] = {(R)qe.Xr[a][0], (R)qe.Xr[a][1], (R)qe.Xr[a][2]};
+            X[a] = dot3(xr, e0r);
+            Y[a] = dot3(xr, e1r);
+        }
     }
     R J0r[3] = {(R)J0[0], (R)J0[1], (R)J0[2]}, J1r[3] = {(R)J1[0], (R)J1[1], (R)J1[2]};
     R G11 = dot3(J0r, J0r), G12 = dot3(J0r, J1r), G22 = dot3(J1r, J1r);
@@ -565,33 +579,33 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         for (int r = 0; r < 3; r++)
             for (int i = 0; i < 4; i++)
                 for (int q = 0; q < 5; q++) { inm[r][i][q] = mb[r][i][q]; inb[r][i][q] = mb[3 + r][i][q]; }
-        mix_rows<R, 4, 3>(mc.Lps, sqrt(t * Jac), inm, (R(*)[4][5])mixed[0]);
-        mix_rows<R, 4, 3>(mc.Lps, sqrt(t * t * t / 12.0 * Jac), inb, (R(*)[4][5])mixed[3]);
-        mix_rows<R, 4, 2>(mc.Lt, sqrt(t * stab * Jac), sh, (R(*)[4][5])mixed[6]);
+        R tr_ = (R)t, jr = (R)Jac;
+        mix_rows<R, 4, 3>(mc.Lps, sqrt(tr_ * jr), inm, (R(*)[4][5])mixed[0]);
+        mix_rows<R, 4, 3>(mc.Lps, sqrt(tr_ * tr_ * tr_ / 12 * jr), inb, (R(*)[4][5])mixed[3]);
+        mix_rows<R, 4, 2>(mc.Lt, sqrt(tr_ * (R)stab * jr), sh, (R(*)[4][5])mixed[6]);
     } else {
         double lm, ln;
         layup_angle(e, gc->csmat, lm, ln);
         rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[0]);
         rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[3]);
-        mix_rows<R, 4, 6>(gc->L6, sqrt(Jac), mb, (R(*)[4][5])mixed[0]);
+        mix_rows<R, 4, 6>(gc->L6, sqrt((R)Jac), mb, (R(*)[4][5])mixed[0]);
         rotate2<R, 4>(lm, ln, sh);
-        mix_rows<R, 4, 2>(gc->LH, sqrt(stab * Jac), sh, (R(*)[4][5])mixed[6]);
+        mix_rows<R, 4, 2>(gc->LH, sqrt((R)stab * (R)Jac), sh, (R(*)[4][5])mixed[6]);
     }
     for (int r = 0; r < 8; r++) expand_row<R, 4>(M, (const R(*)[5])mixed[r], rows + r * rs);
     // drilling traces: sum over rows of |b|^2 - (b.n)^2 on the rotation block
     for (int k = 0; k < 4; k++) {
-        const double *nv = in.nrm[k];
-        double nn = sqrt(dot3(nv, nv));
-        double u[3] = {0, 0, 0};
-        if (nn > 0.0) { u[0] = nv[0] / nn; u[1] = nv[1] / nn; u[2] = nv[2] / nn; }
-        double tr = 0.0;
+        R nv[3] = {(R)in.nrm[k][0], (R)in.nrm[k][1], (R)in.nrm[k][2]};
+        R nn = sqrt(dot3(nv, nv));
+        R u[3] = {0, 0, 0};
+        if (nn > (R)0) { u[0] = nv[0] / nn; u[1] = nv[1] / nn; u[2] = nv[2] / nn; }
+        R tr = 0;
         for (int r = 0; r < 8; r++) {
             const R *o = rows + r * rs + 6 * k + 3;
-            double b0 = o[0], b1 = o[1], b2 = o[2];
-            double bn = b0 * u[0] + b1 * u[1] + b2 * u[2];
-            tr += b0 * b0 + b1 * b1 + b2 * b2 - bn * bn;
+            R bn = o[0] * u[0] + o[1] * u[1] + o[2] * u[2];
+            tr += o[0] * o[0] + o[1] * o[1] + o[2] * o[2] - bn * bn;
         }
-        trace[k] = tr;
+        trace[k] = (double)tr;
     }
     return 0;
 }

@@ -12,6 +12,7 @@
 // double (FS_FP64) or float (FS_MIXED).  The step loop is captured once into
 // a CUDA graph and replayed.
 #include <algorithm>
+#include <vector>
 
 #include "fs_internal.cuh"
 
@@ -114,11 +115,127 @@ __global__ void k_to_float(int64_t n, const double *src, float *dst)
     if (i < n) dst[i] = (float)src[i];
 }
 
+// ---------------------------------------------------------------------------
+// power iteration for the largest generalized eigenvalue of (K, M), M
+// diagonal: the reference's `pwr` (clamp_cyl_expl_examples.jl:131-142),
+// w = K v / |K v|, v = M^-1 w / |M^-1 w|, omega = sqrt(v'Kv / v'Mv).
+// Reductions are two-pass with a fixed order: bitwise reproducible.
+// ---------------------------------------------------------------------------
+static const int PI_TPB = 256;
+static const int PI_BLOCKS = 1024;
+
+__global__ void k_spmv(int64_t n, const int64_t *rowptr, const int32_t *colidx, const double *vals,
+                       const double *x, double *y)
+{
+    int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / CD_LANES;
+    const int sub = threadIdx.x & (CD_LANES - 1);
+    double s = 0.0;
+    if (row < n)
+        for (int64_t k = rowptr[row] + sub; k < rowptr[row + 1]; k += CD_LANES) s += vals[k] * x[colidx[k]];
+#pragma unroll
+    for (int o = CD_LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (row < n && sub == 0) y[row] = s;
+}
+
+// partial[b] = sum over this block's strided range of a[i] * b[i] (b may be a weight)
+__global__ void k_dot_partial(int64_t n, const double *a, const double *b, double *partial)
+{
+    __shared__ double sh[PI_TPB];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * PI_TPB + threadIdx.x; i < n; i += (int64_t)PI_BLOCKS * PI_TPB)
+        s += a[i] * b[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = PI_TPB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_dot_final(const double *partial, double *out)
+{
+    __shared__ double sh[PI_TPB];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < PI_BLOCKS; i += PI_TPB) s += partial[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = PI_TPB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+// y = x * (1/sqrt(*nrm2)) * (w ? w[i] : 1)
+__global__ void k_scale(int64_t n, const double *x, const double *nrm2, const double *w, double *y)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double f = 1.0 / sqrt(*nrm2);
+    y[i] = x[i] * f * (w ? w[i] : 1.0);
+}
+
+// deterministic start vector in [0, 1) from a 64-bit mix of (seed, i)
+__global__ void k_start(int64_t n, uint64_t seed, double *v)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t z = seed + 0x9e3779b97f4a7c15ull * (uint64_t)(i + 1);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z = z ^ (z >> 31);
+    v[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
 }  // namespace fs
 
 using namespace fs;
 
 extern "C" {
+
+int fs_power_iteration(fs_ctx *c, const double *mdiag, int64_t iters, uint64_t seed, double *omega_max)
+{
+    if (!c || !mdiag || !omega_max || iters < 1) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    if (!c->mat_rowptr) return set_err(c, FS_ERR_STATE, "no stiffness assembled");
+    int64_t n = c->mat_n;
+    if (n == 0) return set_err(c, FS_ERR_BAD_INPUT, "empty matrix");
+    size_t need = sizeof(double) * (size_t)(4 * n + PI_BLOCKS + 4);
+    FS_TRY(ensure_scratch(c, need));
+    double *v = (double *)c->scratch, *w = v + n, *minv = w + n, *md = minv + n;
+    double *partial = md + n, *red = partial + PI_BLOCKS;
+    FS_CUDA(c, cudaMemcpyAsync(md, mdiag, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    unsigned g = (unsigned)((n + 255) / 256), gs = (unsigned)((n * CD_LANES + 255) / 256);
+    std::vector<double> h((size_t)n);
+    for (int64_t i = 0; i < n; i++) h[i] = 1.0 / mdiag[i];
+    FS_CUDA(c, cudaMemcpyAsync(minv, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    k_start<<<g, 256, 0, c->stream>>>(n, seed, v);
+    for (int64_t it = 0; it < iters; it++) {
+        k_spmv<<<gs, 256, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, c->vals, v, w);
+        k_dot_partial<<<PI_BLOCKS, PI_TPB, 0, c->stream>>>(n, w, w, partial);
+        k_dot_final<<<1, PI_TPB, 0, c->stream>>>(partial, red);
+        k_scale<<<g, 256, 0, c->stream>>>(n, w, red, minv, v);       // v = M^-1 w / |w|
+        k_dot_partial<<<PI_BLOCKS, PI_TPB, 0, c->stream>>>(n, v, v, partial);
+        k_dot_final<<<1, PI_TPB, 0, c->stream>>>(partial, red);
+        k_scale<<<g, 256, 0, c->stream>>>(n, v, red, nullptr, v);    // v = v / |v|
+    }
+    // Rayleigh quotient v'Kv / v'Mv
+    double one = 1.0;
+    FS_CUDA(c, cudaMemcpyAsync(red + 3, &one, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    k_spmv<<<gs, 256, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, c->vals, v, w);
+    k_dot_partial<<<PI_BLOCKS, PI_TPB, 0, c->stream>>>(n, v, w, partial);
+    k_dot_final<<<1, PI_TPB, 0, c->stream>>>(partial, red + 1);
+    k_scale<<<g, 256, 0, c->stream>>>(n, v, red + 3, md, w);  // w = m .* v
+    k_dot_partial<<<PI_BLOCKS, PI_TPB, 0, c->stream>>>(n, v, w, partial);
+    k_dot_final<<<1, PI_TPB, 0, c->stream>>>(partial, red + 2);
+    FS_CUDA(c, cudaGetLastError());
+    double hr[2];
+    FS_CUDA(c, cudaMemcpyAsync(hr, red + 1, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    *omega_max = sqrt(hr[0] / hr[1]);
+    return FS_OK;
+}
 
 int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const double *C, double dt)
 {

@@ -31,7 +31,6 @@ enum : int {
 
 static const int MAX_PAIRS_PER_NODE = 64;   // elements meeting at one node
 static const int MAX_NBRS = 255;            // neighbour nodes of one node (slots are 8-bit)
-static const int GATHER_LMAX = 120;         // row length held in shared memory by the gather
 
 struct MeshDev {
     int etype = -1, nen = 0;
@@ -56,10 +55,12 @@ struct MeshDev {
 struct PatternDev {
     int64_t n = -1;              // matrix size the pattern is built for
     int64_t nnz = 0;
+    int maxlen = 0;              // longest row
     int64_t *nbr_off = nullptr;  // nnodes + 1
     int32_t *nbr = nullptr;      // neighbour nodes, sorted
     uint32_t *pair_slots = nullptr;  // per pair: 8-bit slot of each element node
     int16_t *colpos = nullptr;   // per node: 6 x nnbr positions in the row (or -1)
+    uint16_t *colsrc = nullptr;  // per node: for row position j, neighbour slot * 6 + component
     int32_t *rowlen = nullptr;   // per node: row length L
     int64_t *rowptr = nullptr;   // n + 1
     int32_t *colidx = nullptr;   // nnz, 0-based

@@ -39,6 +39,29 @@ __device__ __forceinline__ void load_elem(const MeshDev &m, int64_t r, ElemIn<NN
 // ---------------------------------------------------------------------------
 // element kernels
 // ---------------------------------------------------------------------------
+// 36 contiguous values of a 6x6 block (16-byte aligned) as 16-byte stores;
+// `transpose` writes acc^T.
+template <class R>
+__device__ __forceinline__ void store_block(R *o, const R (&acc)[6][6], bool transpose)
+{
+    constexpr int V = 16 / sizeof(R);
+    R buf[36];
+#pragma unroll
+    for (int i = 0; i < 6; i++)
+#pragma unroll
+        for (int j = 0; j < 6; j++) buf[i * 6 + j] = transpose ? acc[j][i] : acc[i][j];
+    if (V == 4) {
+        float4 *o4 = reinterpret_cast<float4 *>(o);
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+            o4[q] = make_float4((float)buf[4 * q], (float)buf[4 * q + 1], (float)buf[4 * q + 2], (float)buf[4 * q + 3]);
+    } else {
+        double2 *o2 = reinterpret_cast<double2 *>(o);
+#pragma unroll
+        for (int q = 0; q < 18; q++) o2[q] = make_double2((double)buf[2 * q], (double)buf[2 * q + 1]);
+    }
+}
+
 template <class R, int NN>
 __device__ __forceinline__ void write_blocks(const R *rows, int nrows, R *out)
 {
@@ -63,18 +86,8 @@ __device__ __forceinline__ void write_blocks(const R *rows, int nrows, R *out)
 #pragma unroll
                     for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
             }
-            R *oab = out + (a * NN + b) * 36;
-#pragma unroll
-            for (int i = 0; i < 6; i++)
-#pragma unroll
-                for (int j = 0; j < 6; j++) oab[i * 6 + j] = acc[i][j];
-            if (a != b) {
-                R *oba = out + (b * NN + a) * 36;
-#pragma unroll
-                for (int j = 0; j < 6; j++)
-#pragma unroll
-                    for (int i = 0; i < 6; i++) oba[j * 6 + i] = acc[i][j];
-            }
+            store_block<R>(out + (a * NN + b) * 36, acc, false);
+            if (a != b) store_block<R>(out + (b * NN + a) * 36, acc, true);
         }
 }
 
@@ -150,18 +163,8 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
 #pragma unroll
                 for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
         }
-        R *oab = out + (a * 4 + b) * 36;
-#pragma unroll
-        for (int i = 0; i < 6; i++)
-#pragma unroll
-            for (int j = 0; j < 6; j++) oab[i * 6 + j] = acc[i][j];
-        if (a != b) {
-            R *oba = out + (b * 4 + a) * 36;
-#pragma unroll
-            for (int j = 0; j < 6; j++)
-#pragma unroll
-                for (int i = 0; i < 6; i++) oba[j * 6 + i] = acc[i][j];
-        }
+        store_block<R>(out + (a * 4 + b) * 36, acc, false);
+        if (a != b) store_block<R>(out + (b * 4 + a) * 36, acc, true);
     }
 }
 
@@ -230,17 +233,56 @@ int launch_elements(fs_ctx *c, int precision)
 // ---------------------------------------------------------------------------
 // gather into CSR values
 // ---------------------------------------------------------------------------
-static const int GATHER_WARPS = 8;
+// One warp per node.  The node's element slabs are staged into shared memory
+// with independent coalesced loads, a few pairs at a time; each lane then
+// owns whole row positions j (all six rows of the node) and adds the staged
+// contributions of the pairs in ascending assembly rank.  In double
+// (FS_FP64) the sum is a plain double accumulation.  For float element
+// matrices (FS_MIXED) the sum is carried error-free as an unevaluated pair
+// of floats (TwoSum), then rounded once to double: on GB300, where a double
+// add costs as much as 64 float operations, this keeps one double add per
+// stored value instead of a conversion and an add per contribution, with an
+// error below 2^-46 of the largest contribution.  Rows longer than
+// 32 * G_COLS positions fall back to accumulating in place in double.
+static const int G_MAXP = 8;
+template <class R> struct GatherCfg { static const int WARPS = sizeof(R) == 4 ? 8 : 4; };
 
-template <class R>
-__global__ void __launch_bounds__(GATHER_WARPS * 32)
+// 16-byte asynchronous global -> shared copy (bypassing registers and L1)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// exact float -> double through the bit pattern (normal numbers and zeros),
+// leaving the double unit to the rare subnormal / inf / nan
+__device__ __forceinline__ double f2d_exact(float f)
+{
+    uint32_t u = __float_as_uint(f);
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    uint32_t ex = (u >> 23) & 0xffu;
+    if (ex == 0u || ex == 0xffu) return (double)f;
+    uint32_t hi = (u & 0x80000000u) | ((ex + (1023u - 127u)) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+template <class R, int NEN, int G_COLS>
+__global__ void __launch_bounds__(GatherCfg<R>::WARPS * 32)
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
-    __shared__ double acc_all[GATHER_WARPS][6 * GATHER_LMAX];
+    constexpr int WARPS = GatherCfg<R>::WARPS;
+    constexpr int SLAB = NEN * 36, ND2 = 36 * NEN * NEN;
+    constexpr bool SINGLE = sizeof(R) == 4;
+    constexpr int CH = SLAB * (int)sizeof(R) / 16;  // 16-byte chunks per slab
+    __shared__ __align__(16) R stage_all[WARPS][G_MAXP * SLAB];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int64_t r = (int64_t)blockIdx.x * GATHER_WARPS + w;
+    int64_t r = (int64_t)blockIdx.x * WARPS + w;
     if (r >= m.nnodes) return;
-    const int nen = m.nen, nd = 6 * nen, slab = nen * 36;
+    R *stage = stage_all[w];
     int32_t d[6];
     bool any = false;
 #pragma unroll
@@ -252,21 +294,62 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32)
     const int L = P.rowlen[r];
     const int64_t off6 = P.nbr_off[r] * 6;
     const int64_t pb = m.pp[r], pe = m.pp[r + 1];
-    if (L <= GATHER_LMAX) {
-        double *acc = acc_all[w];
-        for (int i = lane; i < 6 * GATHER_LMAX; i += 32) acc[i] = 0.0;
-        __syncwarp();
-        for (int64_t p = pb; p < pe; p++) {
-            int32_t pe_ = m.pair_e[p];
-            int64_t rank = pe_ >> 2;
-            int a = pe_ & 3;
-            uint32_t slots = P.pair_slots[p];
-            const R *src = ke + rank * (int64_t)(nd * nd) + a * slab;
-            for (int idx = lane; idx < slab; idx += 32) {
-                int b = idx / 36, rem = idx - 36 * b, krow = rem / 6, kc = rem - 6 * krow;
-                int s = (slots >> (8 * b)) & 0xff;
-                int cp = P.colpos[off6 + s * 6 + kc];
-                if (cp >= 0 && d[krow] <= n) acc[krow * GATHER_LMAX + cp] += (double)src[idx];
+    if (L <= 32 * G_COLS) {
+        int sc[G_COLS], kcol[G_COLS];
+        R hi[G_COLS][6], lo[G_COLS][6];
+#pragma unroll
+        for (int c = 0; c < G_COLS; c++) {
+            int j = lane + 32 * c;
+            int cs = j < L ? (int)P.colsrc[off6 + j] : -6;
+            sc[c] = cs >= 0 ? cs / 6 : -1;
+            kcol[c] = cs >= 0 ? cs - 6 * sc[c] : 0;
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                hi[c][k] = 0;
+                lo[c][k] = 0;
+            }
+        }
+        for (int64_t p0 = pb; p0 < pe; p0 += G_MAXP) {
+            const int cnt = (int)min((int64_t)G_MAXP, pe - p0);
+            int32_t pel = lane < cnt ? m.pair_e[p0 + lane] : 0;
+            uint32_t sll = lane < cnt ? P.pair_slots[p0 + lane] : 0u;
+            const int total = cnt * CH;
+            for (int base = 0; base < total; base += 32) {
+                int k = base + lane;
+                int q = k / CH;
+                int32_t peq = __shfl_sync(0xffffffffu, pel, q < cnt ? q : 0);
+                if (k < total) {
+                    int ch = k - q * CH;
+                    const R *src = ke + (int64_t)(peq >> 2) * ND2 + (peq & 3) * SLAB;
+                    cp_async16(reinterpret_cast<char *>(stage + q * SLAB) + 16 * ch,
+                               reinterpret_cast<const char *>(src) + 16 * ch);
+                }
+            }
+            cp_async_wait_all();
+            __syncwarp();
+            for (int q = 0; q < cnt; q++) {
+                uint32_t slots = __shfl_sync(0xffffffffu, sll, q);
+#pragma unroll
+                for (int c = 0; c < G_COLS; c++) {
+                    int b = -1;
+#pragma unroll
+                    for (int bb = 0; bb < NEN; bb++)
+                        if ((int)((slots >> (8 * bb)) & 0xffu) == sc[c]) b = bb;
+                    if (b < 0) continue;
+                    const R *src = stage + q * SLAB + b * 36 + kcol[c];
+#pragma unroll
+                    for (int k = 0; k < 6; k++) {
+                        R v = src[6 * k];
+                        if (SINGLE) {
+                            R t = hi[c][k] + v;
+                            R bp = t - hi[c][k];
+                            lo[c][k] += (hi[c][k] - (t - bp)) + (v - bp);
+                            hi[c][k] = t;
+                        } else {
+                            hi[c][k] += v;
+                        }
+                    }
+                }
             }
             __syncwarp();
         }
@@ -274,10 +357,23 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32)
         for (int k = 0; k < 6; k++) {
             if (d[k] > n) continue;
             double *o = vals + P.rowptr[d[k] - 1];
-            for (int j = lane; j < L; j += 32) o[j] = acc[k * GATHER_LMAX + j];
+#pragma unroll
+            for (int c = 0; c < G_COLS; c++) {
+                int j = lane + 32 * c;
+                if (j >= L) continue;
+                double v;
+                if (SINGLE) {
+                    float t = (float)hi[c][k] + (float)lo[c][k];
+                    float e = (float)lo[c][k] - (t - (float)hi[c][k]);
+                    v = f2d_exact(t);
+                    if (__float_as_uint(e) & 0x7fffffffu) v += f2d_exact(e);
+                } else {
+                    v = (double)hi[c][k];
+                }
+                o[j] = v;
+            }
         }
     } else {
-        // long rows: accumulate in place in the rows this warp owns
 #pragma unroll
         for (int k = 0; k < 6; k++) {
             if (d[k] > n) continue;
@@ -290,8 +386,8 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32)
             int64_t rank = pe_ >> 2;
             int a = pe_ & 3;
             uint32_t slots = P.pair_slots[p];
-            const R *src = ke + rank * (int64_t)(nd * nd) + a * slab;
-            for (int idx = lane; idx < slab; idx += 32) {
+            const R *src = ke + rank * (int64_t)ND2 + a * SLAB;
+            for (int idx = lane; idx < SLAB; idx += 32) {
                 int b = idx / 36, rem = idx - 36 * b, krow = rem / 6, kc = rem - 6 * krow;
                 int s = (slots >> (8 * b)) & 0xff;
                 int cp = P.colpos[off6 + s * 6 + kc];
@@ -306,17 +402,35 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32)
     }
 }
 
-int launch_gather(fs_ctx *c, int precision, double *vals)
+template <class R, int NEN>
+static void gather_launch(fs_ctx *c, const R *ke, double *vals)
 {
     MeshDev &m = c->mesh;
-    if (m.nnodes == 0) return FS_OK;
-    unsigned g = nblk2(m.nnodes, GATHER_WARPS);
-    if (precision == FS_FP64)
-        k_gather<double><<<g, GATHER_WARPS * 32, 0, c->stream>>>(m, c->pat, c->pat.n, (const double *)c->ke, vals);
+    constexpr int W = GatherCfg<R>::WARPS;
+    unsigned g = nblk2(m.nnodes, W);
+    // per-lane columns sized to the longest row (rows beyond 128 accumulate in place)
+    if (c->pat.maxlen <= 64)
+        k_gather<R, NEN, 2><<<g, W * 32, 0, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
     else
-        k_gather<float><<<g, GATHER_WARPS * 32, 0, c->stream>>>(m, c->pat, c->pat.n, (const float *)c->ke, vals);
+        k_gather<R, NEN, 4><<<g, W * 32, 0, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
+}
+
+template <class R>
+static int run_gather(fs_ctx *c, const R *ke, double *vals)
+{
+    if (c->mesh.nen == 3)
+        gather_launch<R, 3>(c, ke, vals);
+    else
+        gather_launch<R, 4>(c, ke, vals);
     FS_CUDA(c, cudaGetLastError());
     return FS_OK;
+}
+
+int launch_gather(fs_ctx *c, int precision, double *vals)
+{
+    if (c->mesh.nnodes == 0) return FS_OK;
+    if (precision == FS_FP64) return run_gather<double>(c, (const double *)c->ke, vals);
+    return run_gather<float>(c, (const float *)c->ke, vals);
 }
 
 // ---------------------------------------------------------------------------
@@ -546,15 +660,9 @@ int launch_elements_to(fs_ctx *c, int precision, void *ke)
 // CSR values from element matrices held in `ke`; allocates nothing.
 int launch_gather_from(fs_ctx *c, int precision, const void *ke, double *vals)
 {
-    MeshDev &m = c->mesh;
-    if (m.nnodes == 0) return FS_OK;
-    unsigned g = nblk2(m.nnodes, GATHER_WARPS);
-    if (precision == FS_FP64)
-        k_gather<double><<<g, GATHER_WARPS * 32, 0, c->stream>>>(m, c->pat, c->pat.n, (const double *)ke, vals);
-    else
-        k_gather<float><<<g, GATHER_WARPS * 32, 0, c->stream>>>(m, c->pat, c->pat.n, (const float *)ke, vals);
-    FS_CUDA(c, cudaGetLastError());
-    return FS_OK;
+    if (c->mesh.nnodes == 0) return FS_OK;
+    if (precision == FS_FP64) return run_gather<double>(c, (const double *)ke, vals);
+    return run_gather<float>(c, (const float *)ke, vals);
 }
 
 }  // namespace fs

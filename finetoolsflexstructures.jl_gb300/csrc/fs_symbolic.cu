@@ -8,6 +8,7 @@
 // row d holds every column that shares an element with it, sorted.  Rows are
 // produced per node: all six dofs of a node share one sorted column list.
 #include <algorithm>
+#include <vector>
 
 #include "fs_internal.cuh"
 
@@ -319,7 +320,7 @@ __global__ void k_count_nbrs(int64_t nnodes, int nen, const int64_t *pp, const i
 __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_t *pp,
                             const int32_t *pair_e, const int32_t *conn, const int32_t *dof,
                             const int64_t *nbr_off, int32_t *nbr, uint32_t *pair_slots,
-                            int16_t *colpos, int32_t *rowlen)
+                            int16_t *colpos, uint16_t *colsrc, int32_t *rowlen)
 {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nnodes) return;
@@ -361,6 +362,7 @@ __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_
                 pos = (int16_t)cntless;
             }
             colpos[off * 6 + s * 6 + k] = pos;
+            if (pos >= 0) colsrc[off * 6 + pos] = (uint16_t)(s * 6 + k);
         }
     rowlen[r] = L;
 }
@@ -427,16 +429,26 @@ int build_pattern(fs_ctx *c, int64_t n)
     FS_TRY(dalloc(c, &P.nbr, (size_t)nbr_total));
     FS_TRY(dalloc(c, &P.pair_slots, (size_t)m.npairs));
     FS_TRY(dalloc(c, &P.colpos, (size_t)nbr_total * 6));
+    FS_TRY(dalloc(c, &P.colsrc, (size_t)nbr_total * 6));
     FS_TRY(dalloc(c, &P.rowlen, (size_t)nn));
     if (nn)
         k_fill_nbrs<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, m.nen, n, m.pp, m.pair_e, m.conn, m.dof, P.nbr_off,
-                                                         P.nbr, P.pair_slots, P.colpos, P.rowlen);
+                                                         P.nbr, P.pair_slots, P.colpos, P.colsrc, P.rowlen);
     // row lengths by dof
     int32_t *owner = nullptr;
     FS_TRY(dalloc(c, &owner, (size_t)n));
     FS_CUDA(c, cudaMemsetAsync(owner, 0, sizeof(int32_t) * std::max<int64_t>(n, 1), c->stream));
     FS_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * std::max<int64_t>(n, 1), c->stream));
     if (nn) k_row_lengths<<<nblk(6 * nn, 256), 256, 0, c->stream>>>(nn, n, m.dof, P.rowlen, cnt, owner, c->d_status);
+    // longest row (selects the gather variant)
+    {
+        std::vector<int32_t> rl((size_t)nn);
+        if (nn) FS_CUDA(c, cudaMemcpyAsync(rl.data(), P.rowlen, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost, c->stream));
+        FS_CUDA(c, cudaStreamSynchronize(c->stream));
+        int mx = 0;
+        for (int64_t i = 0; i < nn; i++) mx = rl[i] > mx ? rl[i] : mx;
+        P.maxlen = mx;
+    }
     FS_TRY(dalloc(c, &P.rowptr, (size_t)n + 1));
     int64_t nnz = 0;
     FS_TRY(exclusive_scan_i64(c, cnt, P.rowptr, n, &nnz));

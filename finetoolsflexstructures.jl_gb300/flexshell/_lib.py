@@ -58,6 +58,7 @@ def lib():
         L.fs_explicit_set_state.argtypes = [vp, vp, vp, vp]
         L.fs_explicit_run.argtypes = [vp, ctypes.c_int64]
         L.fs_explicit_get_state.argtypes = [vp, vp, vp, vp]
+        L.fs_power_iteration.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_uint64, vp]
         L.fs_laminate.argtypes = [ctypes.c_int32, vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_int32,
                                   ctypes.c_double, ctypes.POINTER(_abi.fs_layup_group)]
         _lib = L

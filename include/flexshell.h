@@ -173,6 +173,12 @@ int fs_explicit_set_state(fs_ctx *ctx, const double *U, const double *V, const d
 /* Runs nsteps steps; the step loop is captured once into a CUDA graph. */
 int fs_explicit_run(fs_ctx *ctx, int64_t nsteps);
 int fs_explicit_get_state(fs_ctx *ctx, double *U, double *V, double *A);
+/* Largest angular frequency of (K, M) for a diagonal M (mdiag, nrows entries) by
+ * power iteration on the last assembled stiffness: the reference's `pwr`
+ * (examples/shells/dynamics/homogeneous/explicit/clamp_cyl_expl_examples.jl:131-142),
+ * with a deterministic start vector from `seed`; dt_crit = 2 / omega_max. */
+int fs_power_iteration(fs_ctx *ctx, const double *mdiag, int64_t iters, uint64_t seed,
+                       double *omega_max);
 
 /* --- layup reduction (src/CompositeLayupModule.jl:246-330) ------------------ */
 /* ply_Dps: nplies x 9, ply_Dts: nplies x 4 (column-major each); angles in degrees;

@@ -129,3 +129,47 @@ def cross_ply_groups(angles=(0, 90, 90, 0), ply_t=0.25e-3, E1=140e9, E2=10e9, G1
     mat = materials.lamina_material(rho, E1, E2, nu12, G12, G13, G23)
     Dps, Dts = materials.shell_material_stiffness(mat)
     return [dict(Dps=Dps, Dts=Dts, thickness=ply_t, angle=a, rho=rho) for a in angles]
+
+
+def barbero_plate(quads, n=8):
+    """Barbero Example 3.1 [0/90] plate under opposite in-plane edge loads,
+    test/test_composite_shell_statics.jl:14-97 (T3FFComp) and
+    test/test_composite_shell_statics_q4rs.jl (Q4RSComp).  Returns the mesh,
+    dofs, loads and the ply list."""
+    from flexshell import materials
+    ax = ay = 2.0
+    E1, E2, G12, nu12, G23 = 133860e6, 7706e6, 4306e6, 0.301, 2760e6
+    t = 0.010
+    tol = ax / n / 100
+    mat = materials.lamina_material(E1, E2, nu12, G12, G12, G23)
+    Dps, Dts = materials.shell_material_stiffness(mat)
+    plies = [dict(Dps=Dps, Dts=Dts, thickness=t / 2, angle=0.0, rho=0.0),
+             dict(Dps=Dps, Dts=Dts, thickness=t / 2, angle=90.0, rho=0.0)]
+    xy, conn = mesh.Q4block(ax, ay, n, n) if quads else mesh.T3block(ax, ay, n, n)
+    xyz = mesh.xyz3(xy)
+    inf = np.inf
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    l1 = mesh.selectnode(xyz, [ax, ax, 0, 0, -inf, inf], tol) - 1
+    fixed[l1, 0:3] = True
+    l1 = mesh.selectnode(xyz, [0, 0, 0, 0, -inf, inf], tol) - 1
+    fixed[l1, 1] = True
+    x, y = xyz[:, 0], xyz[:, 1]
+    bnd = (np.abs(x) < tol) | (np.abs(x - ax) < tol) | (np.abs(y) < tol) | (np.abs(y - ay) < tol)
+    fixed[bnd, 2] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    # edge loads: q = +-0.1 MPa * t per unit length in y on the edges y = 0 and y = ay
+    F = np.zeros(int(dof.max()))
+    q = 0.1e6 * t
+    xs = np.linspace(0.0, ax, n + 1)
+    for yy, sgn in ((0.0, 1.0), (ay, -1.0)):
+        nodes = [int(np.argmin(np.abs(x - xv) + np.abs(y - yy))) for xv in xs]
+        for k in range(n):
+            Le = xs[k + 1] - xs[k]
+            for nd in (nodes[k], nodes[k + 1]):
+                F[dof[nd, 1] - 1] += sgn * q * Le / 2
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, F=F, thickness=t)
+
+
+# test/test_composite_shell_statics.jl:97, test/test_composite_shell_statics_q4rs.jl:97
+BARBERO_T3_UZMAX_MM = 0.22004349767718365
+BARBERO_Q4_UZMAX_MM = 0.2278585006007462

@@ -277,4 +277,10 @@ def test_explicit_steps_match_oracle():
         ctx.call("fs_explicit_get_state", ptr(Ug), ptr(Vg), ptr(Ag))
         assert np.abs(Ug - U).max() <= tol * np.abs(U).max()
         assert np.abs(Vg - V).max() <= tol * np.abs(V).max()
+    # power iteration for omega_max (the reference's `pwr`) against the dense solution
+    femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi)
+    om = ctypes.c_double()
+    femm.ctx.call("fs_power_iteration", ptr(np.ascontiguousarray(m)), ctypes.c_int64(2000),
+                  ctypes.c_uint64(7), ctypes.byref(om))
+    assert abs(om.value - np.sqrt(w2)) <= 1e-3 * np.sqrt(w2)
     femm.close()

@@ -82,3 +82,32 @@ def test_free_element_rigid_translations_and_symmetry():
             r = np.zeros(6 * nen)
             r[c::6] = 1.0
             assert np.abs(Ke @ r).max() <= 1e-9 * scale
+
+
+@pytest.mark.parametrize("quads", [False, True])
+def test_barbero_composite_plate(quads):
+    # the reference asserts `≈` (rtol = sqrt(eps))
+    import scipy.sparse.linalg as spl
+    d = PB.barbero_plate(quads)
+    A, B, D, H, md, mi = O.laminate(d["plies"])
+    grp = dict(A=A, B=B, D=D, H=H, csmat=np.eye(3), thickness=d["thickness"], mass=md, moi=mi)
+    et = O.Q4RSCOMP if quads else O.T3FFCOMP
+    P = O.Problem(et, d["xyz"], d["conn"], d["dofnums"], groups=[grp])
+    P.compute_normals()
+    K = P.assemble_scipy("K", O.DROP_ZEROS)
+    nf = d["nfree"]
+    u = spl.spsolve(K[:nf, :nf].tocsc(), d["F"][:nf])
+    dz = d["dofnums"][:, 2]
+    uz = np.where(dz <= nf, u[np.minimum(dz, nf) - 1], 0.0)
+    ref = PB.BARBERO_Q4_UZMAX_MM if quads else PB.BARBERO_T3_UZMAX_MM
+    assert abs(uz.max() / 1e-3 - ref) <= 1.5e-8 * ref
+
+
+def test_laminate_barbero_example_5_6():
+    # test/test_composite_layup.jl:359-389: one ply at -55 degrees, given Dps
+    Dps = np.array([[20.874, 3.260, 0], [3.260, 11.898, 0], [0, 0, 3.789]])
+    A, B, D, H, md, mi = O.laminate([dict(Dps=Dps, Dts=np.eye(2), thickness=1.0, angle=-55.0)])
+    Atrue = np.array([[12.401509954148374, 5.709503642606021, -1.217123826408347],
+                      [5.709503642606021, 15.471482760639574, -3.000216655678807],
+                      [-1.2171238264083473, -3.000216655678808, 6.2385036426060205]])
+    assert np.linalg.norm(A - Atrue) < 1e-15 * np.linalg.norm(Atrue)
