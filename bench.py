@@ -259,6 +259,92 @@ def explicit_c5(torch, device=0, n=512, nsteps=10000, iters=200):
     return out
 
 
+def cylinder_panels(npanels=64, seed=3):
+    """The reference's configuration 3: cylindrical panels (R 25, L 50, 80 deg
+    arc, mapped as test/test_shell_statics.jl:28-33), each an n x n quad grid
+    split into 2 n^2 T3FF triangles with n ~ U{16..256}, thickness
+    ~ U[0.1, 0.5]; E = 4.32e8, nu = 0."""
+    from flexshell import mesh
+    rng = np.random.Generator(np.random.PCG64(seed))
+    R, L, arc = 25.0, 50.0, 80.0 / 180.0 * np.pi
+    panels = []
+    for _ in range(npanels):
+        n = int(rng.integers(16, 257))
+        t = float(rng.uniform(0.1, 0.5))
+        xy, conn = mesh.T3block(arc, L, n, n)
+        a, y = xy[:, 0], xy[:, 1]
+        xyz = np.stack([R * np.sin(a), y, R * (np.cos(a) - 1)], 1)
+        panels.append((xyz, conn, t))
+    return panels
+
+
+def batched_c3(torch, device=0, steps=5, warmup=3):
+    from flexshell import _abi, materials
+    from flexshell._lib import Context, ptr
+    panels = cylinder_panels()
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(4.32e8, 0.0))
+    prm = _abi.make_params(Dps, Dt, 0.0, 0.0)
+    # one combined (block-diagonal) mesh: one element launch and one gather launch
+    xs, cs, ts, off = [], [], [], 0
+    for xyz, conn, t in panels:
+        xs.append(xyz)
+        cs.append(conn + off)
+        ts.append(np.full(conn.shape[0], t))
+        off += xyz.shape[0]
+    xyz = np.asfortranarray(np.concatenate(xs))
+    conn = np.ascontiguousarray(np.concatenate(cs))
+    th = np.ascontiguousarray(np.concatenate(ts))
+    dof, _ = __import__("flexshell").mesh.numberdofs(np.zeros((xyz.shape[0], 6), bool))
+    dof = np.asfortranarray(dof)
+    nel = conn.shape[0]
+    ctx = Context(device)
+    ctx.call("fs_mesh_set", _abi.FS_T3FF, xyz.shape[0], ptr(xyz), nel, ptr(conn), None, ptr(dof))
+    ctx.call("fs_params_set", prm, ptr(th))
+    ctx.call("fs_normals_compute")
+    n = 6 * xyz.shape[0]
+    nnz = ctypes.c_int64()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    out = {"panels": len(panels), "elements": nel, "n_range": [int(min(p[1].shape[0] for p in panels)),
+                                                             int(max(p[1].shape[0] for p in panels))]}
+    for prec, name in ((_abi.FS_MIXED, "mixed"), (_abi.FS_FP64, "fp64")):
+        for _ in range(warmup):
+            ctx.call("fs_stiffness", prec, 0, ctypes.c_int64(n), ctypes.byref(nnz))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.call("fs_stiffness", prec, 0, ctypes.c_int64(n), ctypes.byref(nnz))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out["batched_elements_per_s_" + name] = nel / (e0.elapsed_time(e1) / steps * 1e-3)
+    ctx.close()
+    # one context and one call per panel
+    ctxs = []
+    for xyz_p, conn_p, t in panels:
+        c = Context(device)
+        xp = np.asfortranarray(xyz_p)
+        dp = np.asfortranarray(np.arange(1, 6 * xp.shape[0] + 1, dtype=np.int64).reshape(-1, 6))
+        c.call("fs_mesh_set", _abi.FS_T3FF, xp.shape[0], ptr(xp), conn_p.shape[0], ptr(np.ascontiguousarray(conn_p)),
+               None, ptr(dp))
+        p2 = _abi.make_params(Dps, Dt, 0.0, t)
+        c.call("fs_params_set", p2, None)
+        c.call("fs_normals_compute")
+        ctxs.append((c, 6 * xp.shape[0]))
+    for prec, name in ((_abi.FS_MIXED, "mixed"), (_abi.FS_FP64, "fp64")):
+        for c, nn in ctxs:
+            c.call("fs_stiffness", prec, 0, ctypes.c_int64(nn), ctypes.byref(nnz))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            for c, nn in ctxs:
+                c.call("fs_stiffness", prec, 0, ctypes.c_int64(nn), ctypes.byref(nnz))
+        torch.cuda.synchronize()
+        out["per_mesh_elements_per_s_" + name] = nel / ((time.perf_counter() - t0) / steps)
+    for c, _ in ctxs:
+        c.close()
+    return out
+
+
 def time_steps(asm, precision, steps, warmup, torch, stream):
     for _ in range(warmup):
         asm.stiffness(precision)
@@ -376,6 +462,7 @@ def main():
     del asm
 
     ex = explicit_c5(torch, device=local) if not args.no_explicit else None
+    bc3 = batched_c3(torch, device=local) if not args.no_explicit else None
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -433,6 +520,7 @@ def main():
                      "ms_gather_mixed": ph_q_mixed[1], "ms_elements_fp64": ph_q_fp64[0],
                      "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4},
             "explicit_q4rs_512": ex,
+            "batched_64_cylinder_panels": bc3,
         },
     }
     print(json.dumps(line))

@@ -216,7 +216,7 @@ int fs_ctx_destroy(fs_ctx *c)
     if (x.exec) cudaGraphExecDestroy(x.exec);
     if (x.graph) cudaGraphDestroy(x.graph);
     dfree(&x.U); dfree(&x.V); dfree(&x.A); dfree(&x.F); dfree(&x.cU); dfree(&x.cV);
-    dfree(&x.invMC); dfree(&x.C); dfree(&x.vals32);
+    dfree(&x.invMC); dfree(&x.C); dfree(&x.vals32); dfree(&x.U32);
     cudaFree(c->d_status);
     for (int k = 0; k < 4; k++)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);

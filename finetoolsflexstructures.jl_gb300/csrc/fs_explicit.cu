@@ -8,9 +8,13 @@
 // Two kernels per step: the displacement update, then a row-parallel CSR
 // product fused with the force, acceleration and velocity updates of the
 // row.  The displacement and velocity sums carry Kahan compensation terms so
-// that a long run in double does not drift.  Stiffness values are read as
-// double (FS_FP64) or float (FS_MIXED).  The step loop is captured once into
-// a CUDA graph and replayed.
+// that a long run in double does not drift.  With FS_FP64 the restoring force
+// K U is formed in double.  With FS_MIXED it is formed in float: the
+// displacement kernel also writes a float copy of U and the product runs on
+// float values (a double product would spend one double conversion and one
+// double FMA per stored value, the scarcest pipe on GB300); the force,
+// acceleration and velocity updates stay in double.  The step loop is
+// captured once into a CUDA graph and replayed.
 #include <algorithm>
 #include <vector>
 
@@ -23,7 +27,7 @@ static const int CD_LANES = 8;  // lanes per CSR row
 static const int CD_GRAPH_STEPS = 64;
 
 __global__ void k_cd_disp(int64_t n, double dt, double dt2_2, double *U, double *cU, const double *V,
-                          const double *A)
+                          const double *A, float *U32)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -32,6 +36,7 @@ __global__ void k_cd_disp(int64_t n, double dt, double dt2_2, double *U, double 
     double t = u + y;
     cU[i] = (t - u) - y;
     U[i] = t;
+    if (U32) U32[i] = (float)t;
 }
 
 __device__ __forceinline__ void kahan_add(double &s, double &c, double incr)
@@ -42,21 +47,22 @@ __device__ __forceinline__ void kahan_add(double &s, double &c, double incr)
     s = t;
 }
 
+// VT: value type of K and of the displacement copy the product reads
 template <class VT>
 __global__ void __launch_bounds__(CD_TPB) k_cd_rows(int64_t n, const int64_t *rowptr, const int32_t *colidx,
-                                                  const VT *vals, const double *U, double *V, double *cV,
+                                                  const VT *vals, const VT *Uk, double *V, double *cV,
                                                   double *A, const double *C, const double *invMC, double dt_2)
 {
     int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / CD_LANES;
     const int sub = threadIdx.x & (CD_LANES - 1);
     const unsigned mask = 0xffffffffu;
-    double s = 0.0;
+    VT sv = 0;
     if (row < n) {
-        for (int64_t k = rowptr[row] + sub; k < rowptr[row + 1]; k += CD_LANES)
-            s += (double)vals[k] * U[colidx[k]];
+        for (int64_t k = rowptr[row] + sub; k < rowptr[row + 1]; k += CD_LANES) sv += vals[k] * Uk[colidx[k]];
     }
 #pragma unroll
-    for (int o = CD_LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(mask, s, o);
+    for (int o = CD_LANES / 2; o > 0; o >>= 1) sv += __shfl_xor_sync(mask, sv, o);
+    double s = (double)sv;
     if (row < n && sub == 0) {
         double a = A[row], v = V[row], cv = cV[row];
         double f = -(s + C[row] * (v + dt_2 * a));
@@ -77,12 +83,13 @@ static int enqueue_steps(fs_ctx *c, int64_t nsteps)
     unsigned g1 = (unsigned)((n + CD_TPB - 1) / CD_TPB);
     unsigned g2 = (unsigned)((n * CD_LANES + CD_TPB - 1) / CD_TPB);
     for (int64_t s = 0; s < nsteps; s++) {
-        k_cd_disp<<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A);
-        if (x.precision == FS_FP64)
+        bool single = x.precision != FS_FP64;
+        k_cd_disp<<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A, single ? x.U32 : nullptr);
+        if (!single)
             k_cd_rows<double><<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, c->vals, x.U, x.V,
                                                             x.cV, x.A, x.C, x.invMC, dt / 2);
         else
-            k_cd_rows<float><<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, x.vals32, x.U, x.V,
+            k_cd_rows<float><<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, x.vals32, x.U32, x.V,
                                                            x.cV, x.A, x.C, x.invMC, dt / 2);
     }
     return cuda_check(c, cudaGetLastError(), "explicit step launch");
@@ -265,6 +272,7 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
     FS_CUDA(c, cudaMemcpyAsync(x.invMC, invMC, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     FS_CUDA(c, cudaMemcpyAsync(x.C, C, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     if (precision == FS_MIXED) {
+        FS_TRY(dalloc(c, &x.U32, (size_t)n));
         FS_TRY(dalloc(c, &x.vals32, (size_t)c->mat_nnz));
         if (c->mat_nnz)
             k_to_float<<<(unsigned)((c->mat_nnz + 255) / 256), 256, 0, c->stream>>>(c->mat_nnz, c->vals, x.vals32);

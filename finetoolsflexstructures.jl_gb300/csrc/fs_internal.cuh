@@ -121,6 +121,7 @@ struct fs_ctx {
         double *cU = nullptr, *cV = nullptr;  // Kahan compensations
         double *invMC = nullptr, *C = nullptr;
         float *vals32 = nullptr;
+        float *U32 = nullptr;  // float copy of U read by the float restoring force
         bool ready = false;
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
