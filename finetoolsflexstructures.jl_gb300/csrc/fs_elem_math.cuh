@@ -201,6 +201,68 @@ FS_HD void expand_row(const GlobalMap<R, NN> &M, const R c[NN][5], R *out)
     }
 }
 
+FS_HD int lp(int r, int c) { return r * (r + 1) / 2 + c; }  // packed lower index, r >= c
+
+// Sparse forms of expand_row for the homogeneous shells: membrane rows carry
+// only in-plane translations (u, v), bending and shear rows only w and the
+// rotations; materialising the dense rows would cost registers and spills.
+template <class R, int NN>
+FS_HD void expand_uv(const GlobalMap<R, NN> &M, const R u[NN], const R v[NN], R *out)
+{
+    for (int j = 0; j < NN; j++)
+        for (int q = 0; q < 3; q++) {
+            out[6 * j + q] = u[j] * M.e[0][q] + v[j] * M.e[1][q];
+            out[6 * j + 3 + q] = 0;
+        }
+}
+
+template <class R, int NN, bool HAS_W>
+FS_HD void expand_wt(const GlobalMap<R, NN> &M, const R w[NN], const R tx[NN], const R ty[NN], R *out)
+{
+    R P0[3] = {0, 0, 0}, P1[3] = {0, 0, 0};
+    for (int i = 0; i < NN; i++) {
+        R mu = tx[i] * M.m[i][0] + ty[i] * M.m[i][1];
+        for (int k = 0; k < 3; k++) {
+            P0[k] += mu * M.A01[i][0][k];
+            P1[k] += mu * M.A01[i][1][k];
+        }
+    }
+    for (int j = 0; j < NN; j++) {
+        R h[3];
+        for (int k = 0; k < 3; k++) h[k] = (R)0.5 * (M.g[j][0] * P1[k] - M.g[j][1] * P0[k]);
+        R r0 = tx[j] * M.R2[j][0][0] + ty[j] * M.R2[j][1][0];
+        R r1 = tx[j] * M.R2[j][0][1] + ty[j] * M.R2[j][1][1];
+        for (int q = 0; q < 3; q++) {
+            R tv = h[0] * M.t[j][0][q] + h[1] * M.t[j][1][q] + h[2] * M.t[j][2][q];
+            out[6 * j + q] = HAS_W ? w[j] * M.e[2][q] + tv : tv;
+            out[6 * j + 3 + q] = r0 * M.t[j][0][q] + r1 * M.t[j][1][q];
+        }
+    }
+}
+
+// Membrane and bending rows of a homogeneous shell, mixed with the Cholesky
+// factor L of Dps (rows r = 0..2: sm * sum_{c>=r} L[c][r] strain_c), written
+// as global rows; returns the bending rotations for the drilling factor.
+template <class R, int NN>
+FS_HD void homog_mb_rows(const GlobalMap<R, NN> &M, const double *Lps, R sm, R sb, R *rows, int rs,
+                         R btx[3][NN], R bty[3][NN])
+{
+    for (int r = 0; r < 3; r++) {
+        R c0 = r == 0 ? (R)Lps[lp(0, 0)] : (R)0;
+        R c1 = r <= 1 ? (R)Lps[lp(1, r)] : (R)0;
+        R c2 = (R)Lps[lp(2, r)];
+        R u[NN], v[NN];
+        for (int j = 0; j < NN; j++) {
+            u[j] = sm * (c0 * M.g[j][0] + c2 * M.g[j][1]);
+            v[j] = sm * (c1 * M.g[j][1] + c2 * M.g[j][0]);
+            btx[r][j] = sb * (-c1 * M.g[j][1] - c2 * M.g[j][0]);
+            bty[r][j] = sb * (c0 * M.g[j][0] + c2 * M.g[j][1]);
+        }
+        expand_uv<R, NN>(M, u, v, rows + r * rs);
+        expand_wt<R, NN, false>(M, nullptr, btx[r], bty[r], rows + (3 + r) * rs);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Material factors
 // ---------------------------------------------------------------------------
@@ -225,7 +287,6 @@ struct GroupConst {
     double pad;
 };
 
-FS_HD int lp(int r, int c) { return r * (r + 1) / 2 + c; }  // packed lower index, r >= c
 
 // rows_out[r] = scale * sum_{c>=r} L[c][r] rows_in[c]   (L^T applied to stacked rows)
 template <class R, int NN, int NR>
@@ -347,20 +408,8 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
     GlobalMap<R, 3> M;
     build_map<R, 3>(e, A, g, M);
 
-    // --- element-frame rows ---
-    R mb[6][3][5];
-    for (int r = 0; r < 6; r++)
-        for (int i = 0; i < 3; i++)
-            for (int q = 0; q < 5; q++) mb[r][i][q] = 0;
-    for (int i = 0; i < 3; i++) {
-        mb[0][i][0] = g[i][0];
-        mb[1][i][1] = g[i][1];
-        mb[2][i][0] = g[i][1]; mb[2][i][1] = g[i][0];
-        mb[3][i][4] = g[i][0];
-        mb[4][i][3] = -g[i][1];
-        mb[5][i][3] = -g[i][0]; mb[5][i][4] = g[i][1];
-    }
     const int NS = T3Rows<AVGK>::NS;
+    // --- transverse shear rows in the element frame (w, thx, thy per node) ---
     R sh[NS][3][5];
     for (int r = 0; r < NS; r++)
         for (int i = 0; i < 3; i++)
@@ -376,45 +425,83 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
         t3_bs_ordering<R>(x, y, AeR, 1, 2, 0, (R(*)[3][5])sh[0], (R)(1.0 / 3));
         t3_bs_ordering<R>(x, y, AeR, 2, 0, 1, (R(*)[3][5])sh[0], (R)(1.0 / 3));
     }
-    // --- material mixing ---
     double h2 = 2 * Ae;  // h = sqrt(2 Ae)
     double stab = t * t / (t * t + mc.stab_c * h2);
-    R mixed[6 + NS][3][5];
-    if (!COMP) {
-        R inm[3][3][5], inb[3][3][5];
-        for (int r = 0; r < 3; r++)
-            for (int i = 0; i < 3; i++)
-                for (int q = 0; q < 5; q++) { inm[r][i][q] = mb[r][i][q]; inb[r][i][q] = mb[3 + r][i][q]; }
-        R tr_ = (R)t, Ar_ = (R)Ae;
-        mix_rows<R, 3, 3>(mc.Lps, sqrt(tr_ * Ar_), inm, (R(*)[3][5])mixed[0]);
-        mix_rows<R, 3, 3>(mc.Lps, sqrt(tr_ * tr_ * tr_ / 12 * Ar_), inb, (R(*)[3][5])mixed[3]);
-        R ws = tr_ * (R)stab * Ar_ * (R)(AVGK ? 1.0 / 3 : 1.0);
+    // rotations of every bending/shear row, for the drilling factor
+    R rtx[3 + NS][3], rty[3 + NS][3];
+    if constexpr (!COMP) {
+        // --- homogeneous: sparse rows, Dps and (5/6)Dt Cholesky mixing ---
+        R tr_ = (R)t;
+        homog_mb_rows<R, 3>(M, mc.Lps, sqrt(tr_ * AeR), sqrt(tr_ * tr_ * tr_ / 12 * AeR), rows, rs,
+                            (R(*)[3])rtx[0], (R(*)[3])rty[0]);
+        R ws = sqrt(tr_ * (R)stab * AeR * (R)(AVGK ? 1.0 / 3 : 1.0));
+        R l00 = (R)mc.Lt[lp(0, 0)], l10 = (R)mc.Lt[lp(1, 0)], l11 = (R)mc.Lt[lp(1, 1)];
         for (int o = 0; o < NS / 2; o++)
-            mix_rows<R, 3, 2>(mc.Lt, sqrt(ws), (R(*)[3][5])sh[2 * o], (R(*)[3][5])mixed[6 + 2 * o]);
+            for (int r = 0; r < 2; r++) {
+                R f0 = r == 0 ? ws * l00 : (R)0, f1 = ws * (r == 0 ? l10 : l11);
+                R w[3];
+                for (int i = 0; i < 3; i++) {
+                    w[i] = f0 * sh[2 * o][i][2] + f1 * sh[2 * o + 1][i][2];
+                    rtx[3 + 2 * o + r][i] = f0 * sh[2 * o][i][3] + f1 * sh[2 * o + 1][i][3];
+                    rty[3 + 2 * o + r][i] = f0 * sh[2 * o][i][4] + f1 * sh[2 * o + 1][i][4];
+                }
+                expand_wt<R, 3, true>(M, w, rtx[3 + 2 * o + r], rty[3 + 2 * o + r], rows + (6 + 2 * o + r) * rs);
+            }
     } else {
+        // --- layered: membrane and bending rows rotated by the layup angle and
+        //     mixed with the 6x6 [A B; B D] factor, shear with H ---
+        R mb[6][3][5];
+        for (int r = 0; r < 6; r++)
+            for (int i = 0; i < 3; i++)
+                for (int q = 0; q < 5; q++) mb[r][i][q] = 0;
+        for (int i = 0; i < 3; i++) {
+            mb[0][i][0] = g[i][0];
+            mb[1][i][1] = g[i][1];
+            mb[2][i][0] = g[i][1]; mb[2][i][1] = g[i][0];
+            mb[3][i][4] = g[i][0];
+            mb[4][i][3] = -g[i][1];
+            mb[5][i][3] = -g[i][0]; mb[5][i][4] = g[i][1];
+        }
+        R mixed[6 + NS][3][5];
         double lm, ln;
         layup_angle(e, gc->csmat, lm, ln);
         rotate3<R, 3>(lm, ln, (R(*)[3][5])mb[0]);
         rotate3<R, 3>(lm, ln, (R(*)[3][5])mb[3]);
-        mix_rows<R, 3, 6>(gc->L6, sqrt((R)Ae), mb, (R(*)[3][5])mixed[0]);
-        R ws = (R)stab * (R)Ae * (R)(AVGK ? 1.0 / 3 : 1.0);
+        mix_rows<R, 3, 6>(gc->L6, sqrt(AeR), mb, (R(*)[3][5])mixed[0]);
+        R ws = (R)stab * AeR * (R)(AVGK ? 1.0 / 3 : 1.0);
         for (int o = 0; o < NS / 2; o++) {
             rotate2<R, 3>(lm, ln, (R(*)[3][5])sh[2 * o]);
             mix_rows<R, 3, 2>(gc->LH, sqrt(ws), (R(*)[3][5])sh[2 * o], (R(*)[3][5])mixed[6 + 2 * o]);
         }
+        for (int r = 0; r < 6 + NS; r++) expand_row<R, 3>(M, (const R(*)[5])mixed[r], rows + r * rs);
+        // drilling factor: every mixed row may carry rotations here
+        R ksumr = 0;
+        for (int i = 0; i < 3; i++)
+            for (int cl = 0; cl < 2; cl++)
+                for (int r = 0; r < 6 + NS; r++) {
+                    R v = mixed[r][i][3] * M.R2[i][0][cl] + mixed[r][i][4] * M.R2[i][1][cl];
+                    ksumr += v * v;
+                }
+        double kavg = (double)ksumr / 6.0 * mc.drill_scale;
+        R sk = kavg > 0.0 ? sqrt((R)kavg) : (R)0;
+        for (int i = 0; i < 3; i++) {
+            R *o = rows + (6 + NS + i) * rs;
+            for (int q = 0; q < 18; q++) o[q] = 0;
+            if (in.valid[i])
+                for (int c = 0; c < 3; c++) o[6 * i + 3 + c] = sk * M.t[i][2][c];
+        }
+        return (kavg < 0.0) ? 2 : 0;
     }
-    // --- drilling factor (double): mean of the nodal-basis bending
-    //     diagonals, src/FEMMShellT3FFModule.jl:713-727 ---
+    // --- drilling factor: mean of the nodal-basis bending diagonals,
+    //     src/FEMMShellT3FFModule.jl:713-727 (mean and scale in double) ---
     R ksumr = 0;
     for (int i = 0; i < 3; i++)
         for (int cl = 0; cl < 2; cl++)
-            for (int r = 0; r < 6 + NS; r++) {
-                R v = mixed[r][i][3] * M.R2[i][0][cl] + mixed[r][i][4] * M.R2[i][1][cl];
+            for (int r = 0; r < 3 + NS; r++) {
+                R v = rtx[r][i] * M.R2[i][0][cl] + rty[r][i] * M.R2[i][1][cl];
                 ksumr += v * v;
             }
     double kavg = (double)ksumr / 6.0 * mc.drill_scale;
-    // --- global rows ---
-    for (int r = 0; r < 6 + NS; r++) expand_row<R, 3>(M, (const R(*)[5])mixed[r], rows + r * rs);
     R sk = kavg > 0.0 ? sqrt((R)kavg) : (R)0;
     for (int i = 0; i < 3; i++) {
         R *o = rows + (6 + NS + i) * rs;
@@ -557,33 +644,40 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     for (int i = 0; i < 4; i++) nodal_triad(e, in.nrm[i], in.valid[i], A[i]);
     GlobalMap<R, 4> M;
     build_map<R, 4>(e, A, g, M);
-    R mb[6][4][5];
-    for (int r = 0; r < 6; r++)
-        for (int i = 0; i < 4; i++)
-            for (int q = 0; q < 5; q++) mb[r][i][q] = 0;
-    for (int i = 0; i < 4; i++) {
-        mb[0][i][0] = g[i][0];
-        mb[1][i][1] = g[i][1];
-        mb[2][i][0] = g[i][1]; mb[2][i][1] = g[i][0];
-        mb[3][i][4] = g[i][0];
-        mb[4][i][3] = -g[i][1];
-        mb[5][i][3] = -g[i][0]; mb[5][i][4] = g[i][1];
-    }
     R sh[2][4][5];
     q4_bs<R>(X, Y, (R)xi, (R)eta, sh);
     double t = COMP ? gc->thickness : in.t;
     double stab = t * t / (t * t + mc.stab_c * qe.h2);
-    R mixed[8][4][5];
-    if (!COMP) {
-        R inm[3][4][5], inb[3][4][5];
-        for (int r = 0; r < 3; r++)
-            for (int i = 0; i < 4; i++)
-                for (int q = 0; q < 5; q++) { inm[r][i][q] = mb[r][i][q]; inb[r][i][q] = mb[3 + r][i][q]; }
+    if constexpr (!COMP) {
         R tr_ = (R)t, jr = (R)Jac;
-        mix_rows<R, 4, 3>(mc.Lps, sqrt(tr_ * jr), inm, (R(*)[4][5])mixed[0]);
-        mix_rows<R, 4, 3>(mc.Lps, sqrt(tr_ * tr_ * tr_ / 12 * jr), inb, (R(*)[4][5])mixed[3]);
-        mix_rows<R, 4, 2>(mc.Lt, sqrt(tr_ * (R)stab * jr), sh, (R(*)[4][5])mixed[6]);
+        R btx[3][4], bty[3][4];
+        homog_mb_rows<R, 4>(M, mc.Lps, sqrt(tr_ * jr), sqrt(tr_ * tr_ * tr_ / 12 * jr), rows, rs, btx, bty);
+        R ws = sqrt(tr_ * (R)stab * jr);
+        R l00 = (R)mc.Lt[lp(0, 0)], l10 = (R)mc.Lt[lp(1, 0)], l11 = (R)mc.Lt[lp(1, 1)];
+        for (int r = 0; r < 2; r++) {
+            R f0 = r == 0 ? ws * l00 : (R)0, f1 = ws * (r == 0 ? l10 : l11);
+            R w[4], tx[4], ty[4];
+            for (int i = 0; i < 4; i++) {
+                w[i] = f0 * sh[0][i][2] + f1 * sh[1][i][2];
+                tx[i] = f0 * sh[0][i][3] + f1 * sh[1][i][3];
+                ty[i] = f0 * sh[0][i][4] + f1 * sh[1][i][4];
+            }
+            expand_wt<R, 4, true>(M, w, tx, ty, rows + (6 + r) * rs);
+        }
     } else {
+        R mb[6][4][5];
+        for (int r = 0; r < 6; r++)
+            for (int i = 0; i < 4; i++)
+                for (int q = 0; q < 5; q++) mb[r][i][q] = 0;
+        for (int i = 0; i < 4; i++) {
+            mb[0][i][0] = g[i][0];
+            mb[1][i][1] = g[i][1];
+            mb[2][i][0] = g[i][1]; mb[2][i][1] = g[i][0];
+            mb[3][i][4] = g[i][0];
+            mb[4][i][3] = -g[i][1];
+            mb[5][i][3] = -g[i][0]; mb[5][i][4] = g[i][1];
+        }
+        R mixed[8][4][5];
         double lm, ln;
         layup_angle(e, gc->csmat, lm, ln);
         rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[0]);
@@ -591,8 +685,8 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         mix_rows<R, 4, 6>(gc->L6, sqrt((R)Jac), mb, (R(*)[4][5])mixed[0]);
         rotate2<R, 4>(lm, ln, sh);
         mix_rows<R, 4, 2>(gc->LH, sqrt((R)stab * (R)Jac), sh, (R(*)[4][5])mixed[6]);
+        for (int r = 0; r < 8; r++) expand_row<R, 4>(M, (const R(*)[5])mixed[r], rows + r * rs);
     }
-    for (int r = 0; r < 8; r++) expand_row<R, 4>(M, (const R(*)[5])mixed[r], rows + r * rs);
     // drilling traces: sum over rows of |b|^2 - (b.n)^2 on the rotation block
     for (int k = 0; k < 4; k++) {
         R nv[3] = {(R)in.nrm[k][0], (R)in.nrm[k][1], (R)in.nrm[k][2]};

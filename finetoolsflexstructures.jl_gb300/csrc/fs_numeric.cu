@@ -258,16 +258,27 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
-// exact float -> double through the bit pattern (normal numbers and zeros),
-// leaving the double unit to the rare subnormal / inf / nan
+// exact float -> double built from the bit pattern with integer operations
+// only (zeros, subnormals, normals, inf and nan), so that no conversion
+// lands on the double-precision pipe
 __device__ __forceinline__ double f2d_exact(float f)
 {
-    uint32_t u = __float_as_uint(f);
-    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    uint32_t ex = (u >> 23) & 0xffu;
-    if (ex == 0u || ex == 0xffu) return (double)f;
-    uint32_t hi = (u & 0x80000000u) | ((ex + (1023u - 127u)) << 20) | ((u & 0x7fffffu) >> 3);
-    return __hiloint2double((int)hi, (int)(u << 29));
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t sign = u & 0x80000000u, a = u & 0x7fffffffu;
+    uint32_t ex = a >> 23, man = a & 0x7fffffu;
+    uint32_t dexp;
+    if (ex == 0xffu) {
+        dexp = 0x7ffu;                                   // inf / nan
+    } else if (ex != 0u) {
+        dexp = ex + (1023u - 127u);                      // normal
+    } else if (man != 0u) {
+        const uint32_t sh = (uint32_t)__clz((int)man) - 8u;  // subnormal: normalise
+        man = (man << sh) & 0x7fffffu;
+        dexp = 1023u - 126u - sh;
+    } else {
+        dexp = 0u;                                       // signed zero
+    }
+    return __hiloint2double((int)(sign | (dexp << 20) | (man >> 3)), (int)(man << 29));
 }
 
 template <class R, int NEN, int G_COLS>

