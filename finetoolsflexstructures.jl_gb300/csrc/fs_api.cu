@@ -567,16 +567,17 @@ int fs_element_matrices(fs_ctx *c, int precision, double *out)
     MeshDev &m = c->mesh;
     int nen = m.nen, nd = 6 * nen;
     size_t per = (size_t)nd * nd;
+    size_t stored = (size_t)n_upper_blocks(nen) * 36;
     std::vector<int32_t> eor((size_t)m.nelem);
     if (m.nelem)
         FS_CUDA(c, cudaMemcpy(eor.data(), m.elem_of_rank, sizeof(int32_t) * m.nelem, cudaMemcpyDeviceToHost));
     std::vector<double> kd;
     std::vector<float> kf;
     if (precision == FS_FP64) {
-        kd.resize(per * m.nelem);
+        kd.resize(stored * m.nelem);
         if (m.nelem) FS_CUDA(c, cudaMemcpy(kd.data(), c->ke, sizeof(double) * kd.size(), cudaMemcpyDeviceToHost));
     } else {
-        kf.resize(per * m.nelem);
+        kf.resize(stored * m.nelem);
         if (m.nelem) FS_CUDA(c, cudaMemcpy(kf.data(), c->ke, sizeof(float) * kf.size(), cudaMemcpyDeviceToHost));
     }
     for (int64_t r = 0; r < m.nelem; r++) {
@@ -585,7 +586,8 @@ int fs_element_matrices(fs_ctx *c, int precision, double *out)
             for (int b = 0; b < nen; b++)
                 for (int i = 0; i < 6; i++)
                     for (int j = 0; j < 6; j++) {
-                        size_t src = per * r + (size_t)(a * nen + b) * 36 + i * 6 + j;
+                        size_t src = stored * r +
+                                     (a <= b ? (size_t)ub(a, b, nen) * 36 + i * 6 + j : (size_t)ub(b, a, nen) * 36 + j * 6 + i);
                         double v = precision == FS_FP64 ? kd[src] : (double)kf[src];
                         o[(6 * a + i) + (size_t)nd * (6 * b + j)] = v;
                     }

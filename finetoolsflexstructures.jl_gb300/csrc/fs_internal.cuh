@@ -30,6 +30,11 @@ enum : int {
 };
 
 static const int MAX_PAIRS_PER_NODE = 64;   // elements meeting at one node
+
+// Element matrices are stored as their upper 6x6 node blocks (a <= b) only,
+// row-major inside a block; ub(a, b) is the block's position.
+__host__ __device__ __forceinline__ int n_upper_blocks(int nen) { return nen * (nen + 1) / 2; }
+__host__ __device__ __forceinline__ int ub(int a, int b, int nen) { return a * nen - a * (a - 1) / 2 + (b - a); }
 static const int MAX_NBRS = 255;            // neighbour nodes of one node (slots are 8-bit)
 
 struct MeshDev {

@@ -75,7 +75,7 @@ extern "C" int fs_stiffness_values_noalloc(fs_ctx *c, int precision, int64_t nro
     if (vals_len < c->pat.nnz)
         return set_err(c, FS_ERR_BAD_INPUT, "output buffer shorter than the number of stored entries");
     const int nen = c->mesh.nen;
-    const uint64_t per = (uint64_t)(6 * nen) * (6 * nen) * (precision == FS_FP64 ? 8 : 4);
+    const uint64_t per = (uint64_t)n_upper_blocks(nen) * 36 * (precision == FS_FP64 ? 8 : 4);
     const uint64_t need = per * (uint64_t)c->mesh.nelem;
     if (need > FS_NOALLOC_SCRATCH_BYTES) {
         char msg[200];

@@ -4,10 +4,10 @@
 // Element matrices.  One thread owns one T3 element (or one quadrature point
 // of a Q4 element, four lanes per element).  It writes the element's Gram
 // rows (csrc/fs_elem_math.cuh) into its own slice of shared memory and then
-// forms K = Bh^T Bh as 6x6 node blocks, writing each upper block and its
-// transpose.  Element matrices are stored by assembly rank as nen x nen
-// blocks of 6x6 (row-major inside a block), so the six rows a node owns in
-// an element are one contiguous slab of nen*36 values.
+// forms K = Bh^T Bh as 6x6 node blocks.  The matrix is symmetric, so only its
+// upper node blocks (a <= b) are stored, by assembly rank, row-major inside a
+// block (6 of 9 blocks for T3, 10 of 16 for Q4); the gather reads a lower
+// block as the transpose of its mirror.
 //
 // Gather.  One warp owns one node, i.e. the six CSR rows of its dofs.  It
 // walks the node's (element, local node) pairs in ascending assembly rank
@@ -86,8 +86,7 @@ __device__ __forceinline__ void write_blocks(const R *rows, int nrows, R *out)
 #pragma unroll
                     for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
             }
-            store_block<R>(out + (a * NN + b) * 36, acc, false);
-            if (a != b) store_block<R>(out + (b * NN + a) * 36, acc, true);
+            store_block<R>(out + ub(a, b, NN) * 36, acc, false);
         }
 }
 
@@ -106,7 +105,7 @@ __global__ void __launch_bounds__(EPB) k_t3_elements(const MeshDev m, const MatC
     const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
     int st = t3_rows<R, COMP, AVGK>(in, mc, gc, rows, ND);
     if (st) atomicOr(status, DEV_NEG_DRILL);
-    write_blocks<R, 3>(rows, NR, ke + r * (ND * ND));
+    write_blocks<R, 3>(rows, NR, ke + r * (6 * 36));
 }
 
 template <class R, bool COMP, int EPB>
@@ -140,7 +139,7 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
     if (active && qp == 0) q4_drill_rows<R>(in, tr, mc.drill_scale, rows + 32 * ND, ND);
     __syncwarp();
     if (!active) return;
-    R *out = ke + r * (ND * ND);
+    R *out = ke + r * (10 * 36);
     // ten upper node blocks shared by the four lanes of the element
     for (int bi = qp; bi < 10; bi += 4) {
         int a = bi < 4 ? 0 : (bi < 7 ? 1 : (bi < 9 ? 2 : 3));
@@ -163,8 +162,7 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
 #pragma unroll
                 for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
         }
-        store_block<R>(out + (a * 4 + b) * 36, acc, false);
-        if (a != b) store_block<R>(out + (b * 4 + a) * 36, acc, true);
+        store_block<R>(out + ub(a, b, 4) * 36, acc, false);
     }
 }
 
@@ -197,7 +195,8 @@ int launch_elements(fs_ctx *c, int precision)
 {
     MeshDev &m = c->mesh;
     size_t nd = 6 * m.nen;
-    size_t bytes = (size_t)m.nelem * nd * nd * (precision == FS_FP64 ? 8 : 4);
+    (void)nd;
+    size_t bytes = (size_t)m.nelem * n_upper_blocks(m.nen) * 36 * (precision == FS_FP64 ? 8 : 4);
     if (bytes > c->ke_bytes) {
         if (c->ke) cudaFree(c->ke);
         c->ke = nullptr;
@@ -286,7 +285,7 @@ __global__ void __launch_bounds__(GatherCfg<R>::WARPS * 32)
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
     constexpr int WARPS = GatherCfg<R>::WARPS;
-    constexpr int SLAB = NEN * 36, ND2 = 36 * NEN * NEN;
+    constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
     constexpr bool SINGLE = sizeof(R) == 4;
     constexpr int CH = SLAB * (int)sizeof(R) / 16;  // 16-byte chunks per slab
     __shared__ __align__(16) R stage_all[WARPS][G_MAXP * SLAB];
@@ -325,21 +324,26 @@ __global__ void __launch_bounds__(GatherCfg<R>::WARPS * 32)
             int32_t pel = lane < cnt ? m.pair_e[p0 + lane] : 0;
             uint32_t sll = lane < cnt ? P.pair_slots[p0 + lane] : 0u;
             const int total = cnt * CH;
+            constexpr int BCH = 36 * (int)sizeof(R) / 16;  // 16-byte chunks per block
             for (int base = 0; base < total; base += 32) {
                 int k = base + lane;
                 int q = k / CH;
                 int32_t peq = __shfl_sync(0xffffffffu, pel, q < cnt ? q : 0);
                 if (k < total) {
                     int ch = k - q * CH;
-                    const R *src = ke + (int64_t)(peq >> 2) * ND2 + (peq & 3) * SLAB;
-                    cp_async16(reinterpret_cast<char *>(stage + q * SLAB) + 16 * ch,
-                               reinterpret_cast<const char *>(src) + 16 * ch);
+                    int bb = ch / BCH, cw = ch - bb * BCH;
+                    int a = peq & 3;
+                    // block (a, bb) of the element: stored as itself or as its mirror
+                    const R *src = ke + (int64_t)(peq >> 2) * ND2 + ub(min(a, bb), max(a, bb), NEN) * 36;
+                    cp_async16(reinterpret_cast<char *>(stage + q * SLAB + bb * 36) + 16 * cw,
+                               reinterpret_cast<const char *>(src) + 16 * cw);
                 }
             }
             cp_async_wait_all();
             __syncwarp();
             for (int q = 0; q < cnt; q++) {
                 uint32_t slots = __shfl_sync(0xffffffffu, sll, q);
+                const int aq = __shfl_sync(0xffffffffu, pel, q) & 3;
 #pragma unroll
                 for (int c = 0; c < G_COLS; c++) {
                     int b = -1;
@@ -347,10 +351,13 @@ __global__ void __launch_bounds__(GatherCfg<R>::WARPS * 32)
                     for (int bb = 0; bb < NEN; bb++)
                         if ((int)((slots >> (8 * bb)) & 0xffu) == sc[c]) b = bb;
                     if (b < 0) continue;
-                    const R *src = stage + q * SLAB + b * 36 + kcol[c];
+                    // entry (krow, kcol) of block (aq, b); a mirrored block is read transposed
+                    const bool tr = b < aq;
+                    const R *src = stage + q * SLAB + b * 36 + (tr ? 6 * kcol[c] : kcol[c]);
+                    const int st = tr ? 1 : 6;
 #pragma unroll
                     for (int k = 0; k < 6; k++) {
-                        R v = src[6 * k];
+                        R v = src[st * k];
                         if (SINGLE) {
                             R t = hi[c][k] + v;
                             R bp = t - hi[c][k];
@@ -397,14 +404,15 @@ __global__ void __launch_bounds__(GatherCfg<R>::WARPS * 32)
             int64_t rank = pe_ >> 2;
             int a = pe_ & 3;
             uint32_t slots = P.pair_slots[p];
-            const R *src = ke + rank * (int64_t)ND2 + a * SLAB;
             for (int idx = lane; idx < SLAB; idx += 32) {
                 int b = idx / 36, rem = idx - 36 * b, krow = rem / 6, kc = rem - 6 * krow;
+                const R *blk = ke + rank * (int64_t)ND2 + ub(min(a, b), max(a, b), NEN) * 36;
+                const R v = b < a ? blk[kc * 6 + krow] : blk[rem];
                 int s = (slots >> (8 * b)) & 0xff;
                 int cp = P.colpos[off6 + s * 6 + kc];
                 if (cp >= 0 && d[krow] <= n) {
                     double *o = vals + P.rowptr[d[krow] - 1] + cp;
-                    *o += (double)src[idx];
+                    *o += (double)v;
                 }
             }
             __threadfence_block();

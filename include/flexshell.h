@@ -150,8 +150,8 @@ int fs_timings(const fs_ctx *ctx, double *out, int n);
  * caller's device buffer `vals` (vals_len >= nnz).  The pattern for `nrows`
  * must exist (one fs_stiffness or fs_mass call at set-up).  Element matrices
  * are staged in a fixed 32 MiB device array inside the library, so
- * nelem * (6 nen)^2 * (8 for FS_FP64, 4 for FS_MIXED) bytes must fit in it
- * (e.g. 12,945 T3FF elements in FP64); larger meshes get FS_ERR_UNSUPPORTED.
+ * nelem * 36 nen (nen + 1)/2 * (8 for FS_FP64, 4 for FS_MIXED) bytes (the upper
+ * node blocks of its element matrices) must fit in it (19,418 T3FF elements in FP64); larger meshes get FS_ERR_UNSUPPORTED.
  * It calls no cudaMalloc/cudaFree.  The first call on a device looks up the
  * array's address (make it before any stream capture); calls that overlap on
  * the GPU share the array and race. */

@@ -61,9 +61,9 @@ def test_noalloc_matches_regular_entry_point(quads, precision):
 
 def test_noalloc_rejects_meshes_beyond_the_fixed_scratch():
     import torch
-    # 81 x 81 quads -> 13,122 triangles: above the 12,945 FP64 T3FF elements
-    # that the 32 MiB array holds, below the 25,890 of the mixed path
-    femm, geom0, dchi = _femm(81, False)
+    # 100 x 100 quads -> 20,000 triangles: above the 19,418 FP64 T3FF elements
+    # that the 32 MiB array holds, below the 38,836 of the mixed path
+    femm, geom0, dchi = _femm(100, False)
     n = dchi.nalldofs()
     K = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
     out = torch.empty(K.nnz, dtype=torch.float64, device="cuda:0")
