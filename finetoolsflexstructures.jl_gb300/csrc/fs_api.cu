@@ -67,28 +67,6 @@ static void free_mesh(MeshDev &m)
     m = MeshDev();
 }
 
-// per-element host array (mesh order) -> device array by assembly rank
-template <class T>
-__global__ void k_by_rank(int64_t nelem, const int32_t *elem_of_rank, const T *src, T *dst)
-{
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < nelem) dst[r] = src[elem_of_rank[r]];
-}
-
-template <class T>
-static int upload_by_rank(fs_ctx *c, const T *host, int64_t nelem, T **dst)
-{
-    FS_TRY(dalloc(c, dst, (size_t)nelem));
-    if (nelem == 0) return FS_OK;
-    T *tmp = nullptr;
-    FS_TRY(dalloc(c, &tmp, (size_t)nelem));
-    FS_CUDA(c, cudaMemcpyAsync(tmp, host, sizeof(T) * nelem, cudaMemcpyHostToDevice, c->stream));
-    k_by_rank<T><<<(unsigned)((nelem + 255) / 256), 256, 0, c->stream>>>(nelem, c->mesh.elem_of_rank, tmp, *dst);
-    FS_CUDA(c, cudaGetLastError());
-    FS_CUDA(c, cudaStreamSynchronize(c->stream));
-    cudaFree(tmp);
-    return FS_OK;
-}
 
 __global__ void k_fill_d(int64_t n, double v, double *p)
 {
@@ -130,6 +108,8 @@ static bool is_comp(int et) { return et == FS_T3FFCOMP || et == FS_Q4RSCOMP; }
 static int check_ready(fs_ctx *c, bool need_dofs = true)
 {
     if (c->mesh.etype < 0) return set_err(c, FS_ERR_STATE, "no mesh: call fs_mesh_set first");
+    if (c->mesh.etype == FS_COROTBEAM)
+        return set_err(c, FS_ERR_UNSUPPORTED, "beam mesh: use the fs_beam_* entry points");
     if (!c->params_set) return set_err(c, FS_ERR_STATE, "no parameters: call fs_params_set first");
     if (need_dofs && !c->dofs_ready) return set_err(c, FS_ERR_STATE, "no dof numbering: call fs_dofs_set first");
     if (is_comp(c->mesh.etype) && !c->mesh.groups)
@@ -208,6 +188,7 @@ int fs_ctx_destroy(fs_ctx *c)
     cudaStreamSynchronize(c->stream);
     free_mesh(c->mesh);
     free_pattern(c->pat);
+    free_beam(c);
     if (c->ke) cudaFree(c->ke);
     dfree(&c->tmrm); dfree(&c->vals); dfree(&c->cmp_rowptr); dfree(&c->cmp_colidx); dfree(&c->cmp_vals);
     dfree(&c->stage64);
@@ -246,7 +227,7 @@ int fs_mesh_set(fs_ctx *c, int elem_type, int64_t nnodes, const double *xyz, int
 {
     if (!c) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
-    if (elem_type < FS_T3FF || elem_type > FS_Q4RSCOMP) return set_err(c, FS_ERR_BAD_INPUT, "unknown element type");
+    if (elem_type < FS_T3FF || elem_type > FS_COROTBEAM) return set_err(c, FS_ERR_BAD_INPUT, "unknown element type");
     if (nnodes < 0 || nelem < 0) return set_err(c, FS_ERR_BAD_INPUT, "negative size");
     if ((nnodes && !xyz) || (nelem && !conn))
         return set_err(c, FS_ERR_BAD_INPUT, "missing mesh array");
@@ -255,11 +236,12 @@ int fs_mesh_set(fs_ctx *c, int elem_type, int64_t nnodes, const double *xyz, int
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
     free_mesh(c->mesh);
     free_pattern(c->pat);
+    free_beam(c);
     c->normals_ready = false;
     c->ex.ready = false;
     MeshDev &m = c->mesh;
     m.etype = elem_type;
-    m.nen = (elem_type == FS_T3FF || elem_type == FS_T3FFCOMP) ? 3 : 4;
+    m.nen = (elem_type == FS_T3FF || elem_type == FS_T3FFCOMP) ? 3 : (elem_type == FS_COROTBEAM ? 2 : 4);
     m.nnodes = nnodes;
     m.nelem = nelem;
     FS_TRY(dalloc(c, &m.xyz, (size_t)(3 * nnodes)));
@@ -419,16 +401,14 @@ static int status_to_code(fs_ctx *c, int bits)
     return FS_OK;
 }
 
-int fs_stiffness(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t *nnz_out)
+}  // extern "C"
+
+// Pattern (built on the first call for a matrix size), element kernel, CSR
+// gather and the assembler's post-processing.  beam_which < 0: shell
+// stiffness; else the beam matrix FS_BEAM_*.
+int fs::assemble_matrix(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t *nnz_out, int beam_which,
+                        int mass_type)
 {
-    if (!c) return FS_ERR_BAD_INPUT;
-    FS_CUDA(c, cudaSetDevice(c->device));
-    FS_TRY(check_ready(c));
-    if (precision != FS_FP64 && precision != FS_MIXED) return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
-    if (assembler < FS_ASM_SPARSE || assembler > FS_ASM_DIAG) return set_err(c, FS_ERR_BAD_INPUT, "unknown assembler");
-    if (!c->normals_ready)
-        return set_err(c, FS_ERR_STATE, "associategeometry! has not been called (self._associatedgeometry == true)");
-    if (nrows < 0) return set_err(c, FS_ERR_BAD_INPUT, "negative matrix size");
     if (c->pat.n != nrows || !c->pat.rowptr) {
         FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
         FS_TRY(build_pattern(c, nrows));
@@ -441,7 +421,7 @@ int fs_stiffness(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t
     PatternDev &P = c->pat;
     c->timed = false;
     FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-    FS_TRY(launch_elements(c, precision));
+    FS_TRY(beam_which < 0 ? launch_elements(c, precision) : launch_beam_elements(c, beam_which, mass_type));
     FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
     size_t need = (size_t)std::max<int64_t>(P.nnz, nrows);
     if (need > c->vals_cap || !c->vals) {
@@ -480,6 +460,23 @@ int fs_stiffness(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t
     }
     if (nnz_out) *nnz_out = c->mat_nnz;
     return FS_OK;
+}
+
+extern "C" {
+
+int fs_stiffness(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t *nnz_out)
+{
+    if (!c) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    if (c->mesh.etype == FS_COROTBEAM)
+        return set_err(c, FS_ERR_UNSUPPORTED, "beam mesh: use fs_beam_matrix (FS_BEAM_STIFFNESS)");
+    FS_TRY(check_ready(c));
+    if (precision != FS_FP64 && precision != FS_MIXED) return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
+    if (assembler < FS_ASM_SPARSE || assembler > FS_ASM_DIAG) return set_err(c, FS_ERR_BAD_INPUT, "unknown assembler");
+    if (!c->normals_ready)
+        return set_err(c, FS_ERR_STATE, "associategeometry! has not been called (self._associatedgeometry == true)");
+    if (nrows < 0) return set_err(c, FS_ERR_BAD_INPUT, "negative matrix size");
+    return assemble_matrix(c, precision, assembler, nrows, nnz_out, -1, 0);
 }
 
 int fs_mass(fs_ctx *c, int assembler, int64_t nrows, int64_t *nnz_out)

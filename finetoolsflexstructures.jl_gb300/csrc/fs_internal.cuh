@@ -8,6 +8,7 @@
 
 #include "../../include/flexshell.h"
 #include "fs_elem_math.cuh"
+#include "fs_beam_math.cuh"
 
 namespace fs {
 
@@ -132,6 +133,20 @@ struct fs_ctx {
         cudaGraphExec_t exec = nullptr;
         int64_t graph_steps = 0;
     } ex;
+    // co-rotational beams (FEMMCorotBeam)
+    struct Beam {
+        fs::BeamSection *sec = nullptr;  // per rank
+        double E = 0, nu = 0, rho = 0;
+        double *u1 = nullptr;            // 3 x nnodes (SoA)
+        double *R1 = nullptr;            // 9 x nnodes (SoA), R[:] per node
+        double *v1 = nullptr;            // 6 x nnodes (SoA)
+        bool have_u = false, have_R = false, have_v = false;
+        double *q = nullptr;             // distributed load, 3 per rank
+        double *fe = nullptr;            // element vectors, 12 per rank
+        double *F = nullptr;             // assembled vector
+        size_t F_cap = 0;
+        bool ready = false;
+    } beam;
 };
 
 namespace fs {
@@ -156,6 +171,15 @@ int ensure_scratch(fs_ctx *c, size_t bytes);
 int read_status(fs_ctx *c, int *bits);
 
 int explicit_launch_steps(fs_ctx *c, int64_t nsteps);
+
+// co-rotational beams
+int launch_beam_elements(fs_ctx *c, int which, int mass_type);
+int launch_beam_vector(fs_ctx *c, int which, int64_t n, double *F);
+void free_beam(fs_ctx *c);
+// pattern + element kernel + gather + assembler post-processing shared by the
+// shells (beam_which < 0) and the beams
+int assemble_matrix(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t *nnz_out, int beam_which,
+                    int mass_type);
 
 // helpers
 int set_err(fs_ctx *c, int code, const std::string &msg);
@@ -189,3 +213,30 @@ template <class T> void dfree(T **p)
         if (_s != FS_OK) return _s; \
     } while (0)
 #define FS_CUDA(c, call) FS_TRY(fs::cuda_check((c), (call), #call))
+
+namespace fs {
+
+// per-element host array (mesh order) -> device array by assembly rank
+template <class T>
+__global__ void k_by_rank(int64_t nelem, const int32_t *elem_of_rank, const T *src, T *dst)
+{
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nelem) dst[r] = src[elem_of_rank[r]];
+}
+
+template <class T>
+int upload_by_rank(fs_ctx *c, const T *host, int64_t nelem, T **dst)
+{
+    FS_TRY(dalloc(c, dst, (size_t)nelem));
+    if (nelem == 0) return FS_OK;
+    T *tmp = nullptr;
+    FS_TRY(dalloc(c, &tmp, (size_t)nelem));
+    FS_CUDA(c, cudaMemcpyAsync(tmp, host, sizeof(T) * nelem, cudaMemcpyHostToDevice, c->stream));
+    k_by_rank<T><<<(unsigned)((nelem + 255) / 256), 256, 0, c->stream>>>(nelem, c->mesh.elem_of_rank, tmp, *dst);
+    FS_CUDA(c, cudaGetLastError());
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(tmp);
+    return FS_OK;
+}
+
+}  // namespace fs

@@ -439,6 +439,8 @@ static int run_gather(fs_ctx *c, const R *ke, double *vals)
 {
     if (c->mesh.nen == 3)
         gather_launch<R, 3>(c, ke, vals);
+    else if (c->mesh.nen == 2)
+        gather_launch<R, 2>(c, ke, vals);
     else
         gather_launch<R, 4>(c, ke, vals);
     FS_CUDA(c, cudaGetLastError());

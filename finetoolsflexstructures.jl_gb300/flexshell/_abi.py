@@ -10,9 +10,16 @@ FS_ERR_UNSUPPORTED = 5
 FS_ERR_STATE = 6
 FS_ERR_TIMEOUT = 7
 
-FS_T3FF, FS_T3FFCOMP, FS_Q4RS, FS_Q4RSCOMP = 0, 1, 2, 3
+FS_T3FF, FS_T3FFCOMP, FS_Q4RS, FS_Q4RSCOMP, FS_COROTBEAM = 0, 1, 2, 3, 4
 FS_FP64, FS_MIXED = 0, 1
 FS_ASM_SPARSE, FS_ASM_SPARSE_SYMM, FS_ASM_DIAG = 0, 1, 2
+FS_BEAM_STIFFNESS, FS_BEAM_GEOSTIFFNESS, FS_BEAM_MASS, FS_BEAM_GYROSCOPIC = 0, 1, 2, 3
+FS_BEAM_RESTORING, FS_BEAM_DISTRIBLOAD = 4, 5
+
+
+class fs_beam_section(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("A", "I1", "I2", "I3", "J", "A2s", "A3s")] + [
+        ("x1x2_vector", ctypes.c_double * 3)]
 
 
 class fs_shell_params(ctypes.Structure):
@@ -44,8 +51,9 @@ class fs_layup_group(ctypes.Structure):
 
 def _colmajor(a, n):
     import numpy as np
-    return list(np.asarray(a, dtype=np.float64).reshape(n).tolist()) if False else \
-        list(np.asarray(a, dtype=np.float64).flatten(order="F"))
+    v = np.asarray(a, dtype=np.float64).flatten(order="F")
+    assert v.size == n
+    return list(v)
 
 
 def make_params(Dps, Dt, rho=0.0, thickness=0.0, stab_c=None, drilling_stiffness_scale=1.0,

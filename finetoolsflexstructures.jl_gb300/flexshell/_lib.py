@@ -61,6 +61,13 @@ def lib():
         L.fs_power_iteration.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_uint64, vp]
         L.fs_laminate.argtypes = [ctypes.c_int32, vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_int32,
                                   ctypes.c_double, ctypes.POINTER(_abi.fs_layup_group)]
+        L.fs_beam_setup.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.fs_beam_state_set.argtypes = [vp, vp, vp, vp]
+        L.fs_beam_matrix.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64, _c_i64_p]
+        L.fs_beam_restoringforce.argtypes = [vp, ctypes.c_int64, vp]
+        L.fs_beam_distribloads_global.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int64, vp]
+        L.fs_beam_element_matrices.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+        L.fs_beam_element_vectors.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp]
         _lib = L
     return _lib
 

@@ -43,6 +43,7 @@ extern "C" {
 #define FS_T3FFCOMP 1   /* FEMMShellT3FFComp, src/FEMMShellT3FFCompModule.jl */
 #define FS_Q4RS 2       /* FEMMShellQ4RS,     src/FEMMShellQ4RSModule.jl     */
 #define FS_Q4RSCOMP 3   /* FEMMShellQ4RSComp, src/FEMMShellQ4RSCompModule.jl */
+#define FS_COROTBEAM 4  /* FEMMCorotBeam (2-node L2 beams), src/FEMMCorotBeamModule.jl */
 
 /* arithmetic of the element strain rows and Gram products */
 #define FS_FP64 0       /* everything in double: the drop-in                 */
@@ -179,6 +180,56 @@ int fs_explicit_get_state(fs_ctx *ctx, double *U, double *V, double *A);
  * with a deterministic start vector from `seed`; dt_crit = 2 / omega_max. */
 int fs_power_iteration(fs_ctx *ctx, const double *mdiag, int64_t iters, uint64_t seed,
                        double *omega_max);
+
+/* --- co-rotational beams (src/FEMMCorotBeamModule.jl) ---------------------------
+ * Mesh: fs_mesh_set with FS_COROTBEAM, conn nelem x 2.  All beam arithmetic is
+ * double.  The matrices are assembled like the shell matrices (same assemblers,
+ * same CSR/CSC output through fs_matrix_copy); the vectors are summed in element
+ * order (SysvecAssembler). */
+
+/* what fs_beam_matrix assembles */
+#define FS_BEAM_STIFFNESS 0    /* stiffness(femm, assembler, geom0, u1, Rfield1, dchi)  :972-1023  */
+#define FS_BEAM_GEOSTIFFNESS 1 /* geostiffness(femm, assembler, geom0, u1, Rfield1, dchi) :1042-1094 */
+#define FS_BEAM_MASS 2         /* mass(femm, assembler, geom0, u1, Rfield1, dchi; mass_type) :810-862 */
+#define FS_BEAM_GYROSCOPIC 3   /* gyroscopic(femm, assembler, geom0, u1, Rfield1, v1, dchi; mass_type) :883-952 */
+
+/* mass_type (MASS_TYPE_* of src/FEMMCorotBeamModule.jl:144-147) */
+#define FS_BEAM_MASS_CONSISTENT_NO_ROTATION_INERTIA 0
+#define FS_BEAM_MASS_CONSISTENT_WITH_ROTATION_INERTIA 1 /* the reference default */
+#define FS_BEAM_MASS_LUMPED_DIAGONAL_NO_ROTATION_INERTIA 2
+#define FS_BEAM_MASS_LUMPED_DIAGONAL_WITH_ROTATION_INERTIA 3
+
+/* Cross-section of one element: the FESetL2Beam fields A, I1, I2, I3, J, A2s,
+ * A3s (INFINITY for a Bernoulli section) and x1x2_vector
+ * (src/FESetL2BeamModule.jl:20-31). */
+typedef struct {
+    double A, I1, I2, I3, J, A2s, A3s;
+    double x1x2_vector[3];
+} fs_beam_section;
+
+/* Sections (nelem, mesh order) and the MatDeforElastIso constants. */
+int fs_beam_setup(fs_ctx *ctx, const fs_beam_section *sections, double E, double nu, double rho);
+/* Configuration of the next calls: u1 (nnodes x 3), Rfield1 (nnodes x 9, the
+ * column-major rotation matrix R[:] of each node, as Rfield1.values) and the
+ * velocities v1 (nnodes x 6, gyroscopic only), all column-major.  A NULL array
+ * means zero displacement, identity rotations, zero velocity. */
+int fs_beam_state_set(fs_ctx *ctx, const double *u1, const double *Rfield1, const double *v1);
+/* Assemble FS_BEAM_STIFFNESS / GEOSTIFFNESS / MASS / GYROSCOPIC (nrows as for
+ * fs_stiffness; mass_type used by MASS and GYROSCOPIC).  Copy out with
+ * fs_matrix_copy. */
+int fs_beam_matrix(fs_ctx *ctx, int which, int mass_type, int assembler, int64_t nrows, int64_t *nnz_out);
+/* restoringforce(femm, assembler, geom0, u1, Rfield1, dchi) (:1112-1159) into
+ * host F[nrows]; dofs above nrows are left out. */
+int fs_beam_restoringforce(fs_ctx *ctx, int64_t nrows, double *F);
+/* distribloads_global(femm, assembler, geom0, u1, Rfield1, dchi, fi)
+ * (:1186-1247): force per unit length in global components, one 3-vector for
+ * all elements (per_element 0) or one per element (nelem x 3, row per element). */
+int fs_beam_distribloads_global(fs_ctx *ctx, const double *q, int per_element, int64_t nrows, double *F);
+/* Element matrices (nelem x 144, column-major each, mesh order) or element
+ * vectors (which 4 = restoring force, 5 = distributed load with q as above;
+ * nelem x 12), for parity checks. */
+int fs_beam_element_matrices(fs_ctx *ctx, int which, int mass_type, double *out);
+int fs_beam_element_vectors(fs_ctx *ctx, int which, const double *q, int per_element, double *out);
 
 /* --- layup reduction (src/CompositeLayupModule.jl:246-330) ------------------ */
 /* ply_Dps: nplies x 9, ply_Dts: nplies x 4 (column-major each); angles in degrees;

@@ -922,30 +922,13 @@ int orc_all_element_stiffness(int64_t nnodes, const double *xyz, int64_t nelem,
     return status;
 }
 
-int orc_assemble(int what, int mode, int64_t nnodes, const double *xyz, int64_t nelem,
-                 const int64_t *conn, const int64_t *order, const int64_t *dofnums, int64_t n,
-                 const double *normals, const uint8_t *valid, const orc_params *p, int nthreads,
-                 orc_result **out)
+/* Assembly of element matrices Ke (what 0, nelem x (6 nen)^2 column-major)
+ * or of lumped masses tmrm (what 1, nelem x 2) in the given element order. */
+static orc_result *assemble_from(int what, int mode, int nen, int64_t nnodes, int64_t nelem,
+                                 const int64_t *conn, const int64_t *order, const int64_t *dofnums,
+                                 int64_t n, const double *Ke, const double *tmrm)
 {
-    int nen = nen_of(p->etype), nd = 6 * nen;
-    double *Ke = NULL;
-    double *tmrm = NULL;
-    int status = 0;
-    if (what == 0) {
-        Ke = (double *)malloc(sizeof(double) * nd * nd * (nelem > 0 ? nelem : 1));
-        status = orc_all_element_stiffness(nnodes, xyz, nelem, conn, normals, valid, p, nthreads, Ke);
-        if (status) {
-            free(Ke);
-            return status;
-        }
-    } else {
-        tmrm = (double *)malloc(sizeof(double) * 2 * (nelem > 0 ? nelem : 1));
-        for (int64_t e = 0; e < nelem; e++) {
-            double X[12];
-            gather_X(xyz, nnodes, conn + nen * e, nen, X);
-            orc_element_mass(p, e, X, tmrm + 2 * e, tmrm + 2 * e + 1);
-        }
-    }
+    int nd = 6 * nen;
     orc_result *res = (orc_result *)calloc(1, sizeof(orc_result));
     res->n = n;
     if (mode == ORC_DIAG) {
@@ -1011,9 +994,45 @@ int orc_assemble(int what, int mode, int64_t nnodes, const double *xyz, int64_t 
         res->rowval = rv;
         res->nzval = nz;
     }
+    return res;
+}
+
+int orc_assemble(int what, int mode, int64_t nnodes, const double *xyz, int64_t nelem,
+                 const int64_t *conn, const int64_t *order, const int64_t *dofnums, int64_t n,
+                 const double *normals, const uint8_t *valid, const orc_params *p, int nthreads,
+                 orc_result **out)
+{
+    int nen = nen_of(p->etype), nd = 6 * nen;
+    double *Ke = NULL;
+    double *tmrm = NULL;
+    int status = 0;
+    if (what == 0) {
+        Ke = (double *)malloc(sizeof(double) * nd * nd * (nelem > 0 ? nelem : 1));
+        status = orc_all_element_stiffness(nnodes, xyz, nelem, conn, normals, valid, p, nthreads, Ke);
+        if (status) {
+            free(Ke);
+            return status;
+        }
+    } else {
+        tmrm = (double *)malloc(sizeof(double) * 2 * (nelem > 0 ? nelem : 1));
+        for (int64_t e = 0; e < nelem; e++) {
+            double X[12];
+            gather_X(xyz, nnodes, conn + nen * e, nen, X);
+            orc_element_mass(p, e, X, tmrm + 2 * e, tmrm + 2 * e + 1);
+        }
+    }
+    *out = assemble_from(what, mode, nen, nnodes, nelem, conn, order, dofnums, n, Ke, tmrm);
     free(Ke);
     free(tmrm);
-    *out = res;
+    return 0;
+}
+
+int orc_assemble_elmats(int mode, int nen, int64_t nnodes, int64_t nelem, const int64_t *conn,
+                        const int64_t *order, const int64_t *dofnums, int64_t n, const double *Ke,
+                        orc_result **out)
+{
+    if (nen < 1 || nen > 4) return 1;
+    *out = assemble_from(0, mode, nen, nnodes, nelem, conn, order, dofnums, n, Ke, NULL);
     return 0;
 }
 

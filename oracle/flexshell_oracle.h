@@ -71,6 +71,11 @@ int orc_assemble(int what /*0 K, 1 M*/, int mode, int64_t nnodes, const double *
                  const int64_t *dofnums, int64_t n, const double *normals,
                  const uint8_t *valid, const orc_params *p, int nthreads,
                  orc_result **out);
+/* The same assembly of given element matrices (nelem x (6 nen)^2, column-major
+ * each), e.g. those of the beam oracle. */
+int orc_assemble_elmats(int mode, int nen, int64_t nnodes, int64_t nelem, const int64_t *conn,
+                        const int64_t *order, const int64_t *dofnums, int64_t n, const double *Ke,
+                        orc_result **out);
 int64_t orc_result_nnz(const orc_result *r);
 int64_t orc_result_n(const orc_result *r);
 void orc_result_copy(const orc_result *r, int64_t *colptr, int64_t *rowval, double *nzval);

@@ -32,18 +32,21 @@ _c_i32_p = ctypes.POINTER(ctypes.c_int32)
 _c_u8_p = ctypes.POINTER(ctypes.c_uint8)
 
 
+SOURCES = ("flexshell_oracle.c", "corotbeam_oracle.c")
+HEADERS = ("flexshell_oracle.h", "corotbeam_oracle.h")
+
+
 def build(force=False):
     """Compile the oracle into oracle/_build/liboracle.so with gcc."""
-    src = os.path.join(HERE, "flexshell_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in SOURCES]
+    deps = srcs + [os.path.join(HERE, f) for f in HEADERS]
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(
-                os.path.join(HERE, "flexshell_oracle.h"))):
+            and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(d) for d in deps)):
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
     cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-           "-std=c11", "-D_DEFAULT_SOURCE", src, "-o", tmp, "-lm"]
+           "-std=c11", "-D_DEFAULT_SOURCE"] + srcs + ["-o", tmp, "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -82,6 +85,10 @@ def lib():
         L.orc_all_element_stiffness.restype = ctypes.c_int
         L.orc_cd_steps.restype = ctypes.c_int
         L.orc_laminate.restype = ctypes.c_int
+        L.orc_assemble_elmats.restype = ctypes.c_int
+        L.orc_beam_all.restype = ctypes.c_int
+        L.orc_beam_element.restype = ctypes.c_int
+        L.orc_beam_frame.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -243,3 +250,105 @@ def laminate(plies, offset=0.0, shear_model=0, tcf=0.0):
                        ctypes.byref(mi))
     f = lambda a, s: a.reshape(s, order="F")
     return f(A, (3, 3)), f(B, (3, 3)), f(D, (3, 3)), f(H, (2, 2)), md.value, mi.value
+
+
+# ---------------------------------------------------------------------------
+# co-rotational beam (corotbeam_oracle.c)
+# ---------------------------------------------------------------------------
+BEAM_STIFFNESS, BEAM_GEOSTIFFNESS, BEAM_MASS, BEAM_GYROSCOPIC, BEAM_RESTORING, BEAM_DISTRIBLOAD = range(6)
+
+
+def _result_arrays(res, n):
+    L = lib()
+    nnz = L.orc_result_nnz(res)
+    colptr = np.zeros(n + 1, dtype=np.int64)
+    rowval = np.zeros(nnz, dtype=np.int64)
+    nzval = np.zeros(nnz, dtype=np.float64)
+    L.orc_result_copy(res, _p(colptr, _c_i64_p), _p(rowval, _c_i64_p), _p(nzval, _c_dbl_p))
+    L.orc_result_free(res)
+    return colptr, rowval, nzval
+
+
+def assemble_elmats(Ke, conn, dofnums, n, mode=KEEP_ZEROS, order=None):
+    """Assemble element matrices Ke (nelem, nd, nd) with the FinEtools
+    assembler semantics; returns a scipy CSC matrix."""
+    import scipy.sparse as sp
+    conn = np.ascontiguousarray(conn, dtype=np.int64)
+    dofnums = np.asfortranarray(dofnums, dtype=np.int64)
+    nelem, nen = conn.shape
+    # column-major per element
+    Kc = np.ascontiguousarray(np.asarray(Ke, dtype=np.float64).transpose(0, 2, 1))
+    order = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    res = ctypes.c_void_p()
+    st = lib().orc_assemble_elmats(ctypes.c_int(mode), ctypes.c_int(nen),
+                                   ctypes.c_int64(dofnums.shape[0]), ctypes.c_int64(nelem),
+                                   _p(conn, _c_i64_p), _p(order, _c_i64_p), _p(dofnums, _c_i64_p),
+                                   ctypes.c_int64(n), _p(Kc, _c_dbl_p), ctypes.byref(res))
+    assert st == 0
+    colptr, rowval, nzval = _result_arrays(res, n)
+    return sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=(n, n))
+
+
+def assemble_vector(Fe, conn, dofnums, n):
+    """SysvecAssembler: element vectors (nelem, 6 nen) summed in element order."""
+    conn = np.ascontiguousarray(conn, dtype=np.int64)
+    dofnums = np.asfortranarray(dofnums, dtype=np.int64)
+    Fe = np.ascontiguousarray(Fe, dtype=np.float64)
+    F = np.zeros(n, dtype=np.float64)
+    lib().orc_assemble_vector(ctypes.c_int64(dofnums.shape[0]), ctypes.c_int64(conn.shape[0]),
+                              ctypes.c_int(conn.shape[1]), _p(conn, _c_i64_p), _p(dofnums, _c_i64_p),
+                              ctypes.c_int64(n), _p(Fe, _c_dbl_p), _p(F, _c_dbl_p))
+    return F
+
+
+class Beam:
+    """Inputs of one FEMMCorotBeam call in the reference's layouts.
+
+    xyz (nnodes,3); conn (nelem,2) 1-based; sections (nelem,10): A, I1, I2, I3,
+    J, A2s, A3s, x1x2_vector; E, nu, rho of MatDeforElastIso.
+    """
+
+    def __init__(self, xyz, conn, sections, E, nu, rho=0.0):
+        self.xyz = np.asfortranarray(xyz, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int64)
+        self.sections = np.ascontiguousarray(sections, dtype=np.float64)
+        assert self.sections.shape == (self.conn.shape[0], 10)
+        self.E, self.nu, self.rho = float(E), float(nu), float(rho)
+
+    @property
+    def nnodes(self):
+        return self.xyz.shape[0]
+
+    @property
+    def nelem(self):
+        return self.conn.shape[0]
+
+    def elements(self, which, u1=None, R1=None, v1=None, mass_type=1, q=None):
+        """Element matrices (nelem,12,12) or vectors (nelem,12) of `which`."""
+        nn = self.nnodes
+        u1 = np.asfortranarray(u1 if u1 is not None else np.zeros((nn, 3)), dtype=np.float64)
+        if R1 is None:
+            R1 = np.tile(np.eye(3).flatten(order="F"), (nn, 1))
+        R1 = np.asfortranarray(R1, dtype=np.float64)
+        v1 = None if v1 is None else np.asfortranarray(v1, dtype=np.float64)
+        vec = which in (BEAM_RESTORING, BEAM_DISTRIBLOAD)
+        if q is not None:
+            q = np.ascontiguousarray(np.broadcast_to(np.asarray(q, dtype=np.float64),
+                                                     (self.nelem, 3)))
+        out = np.zeros((self.nelem, 12 if vec else 144), dtype=np.float64)
+        st = lib().orc_beam_all(ctypes.c_int(which), ctypes.c_int64(nn), _p(self.xyz, _c_dbl_p),
+                                ctypes.c_int64(self.nelem), _p(self.conn, _c_i64_p),
+                                _p(u1, _c_dbl_p), _p(R1, _c_dbl_p), _p(v1, _c_dbl_p),
+                                _p(self.sections, _c_dbl_p), ctypes.c_double(self.E),
+                                ctypes.c_double(self.nu), ctypes.c_double(self.rho),
+                                ctypes.c_int(mass_type), _p(q, _c_dbl_p), _p(out, _c_dbl_p))
+        assert st == 0
+        if vec:
+            return out
+        return np.ascontiguousarray(out.reshape(self.nelem, 12, 12).transpose(0, 2, 1))
+
+    def matrix(self, which, dofnums, n, mode=DROP_ZEROS, **kw):
+        return assemble_elmats(self.elements(which, **kw), self.conn, dofnums, n, mode)
+
+    def vector(self, which, dofnums, n, **kw):
+        return assemble_vector(self.elements(which, **kw), self.conn, dofnums, n)

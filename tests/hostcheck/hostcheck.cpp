@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "fs_host_prep.h"
+#include "fs_beam_math.cuh"
 
 using namespace fs;
 
@@ -124,6 +125,59 @@ extern "C" int hc_lumped(int etype, int64_t nnodes, const double *xyz, int64_t n
             in.t = thick[e];
             lumped_mass<4>(in, rho, comp, &gc, out[2 * e], out[2 * e + 1]);
         }
+    }
+    return 0;
+}
+
+// Beam element matrices (which 0..3, 12x12 column-major each) or vectors
+// (which 4 restoring force, 5 distributed load q[3] per element) from the
+// library's beam math (csrc/fs_beam_math.cuh).  Layouts as the oracle's.
+extern "C" int hc_beam_elements(int which, int64_t nnodes, const double *xyz, int64_t nelem,
+                                const int64_t *conn, const double *u1, const double *R1,
+                                const double *v1, const double *sections, double E, double nu,
+                                double rho, int mass_type, const double *q, double *out)
+{
+    const double G = E / 2 / (1 + nu);
+    for (int64_t e = 0; e < nelem; e++) {
+        double x0[2][3], xt[2][3], R[2][3][3], v[2][6];
+        for (int a = 0; a < 2; a++) {
+            int64_t node = conn[2 * e + a] - 1;
+            for (int c = 0; c < 3; c++) {
+                x0[a][c] = xyz[node + c * nnodes];
+                xt[a][c] = x0[a][c] + (u1 ? u1[node + c * nnodes] : 0.0);
+            }
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    R[a][i][j] = R1 ? R1[node + (i + 3 * j) * nnodes] : (i == j ? 1.0 : 0.0);
+            for (int k = 0; k < 6; k++) v[a][k] = v1 ? v1[node + k * nnodes] : 0.0;
+        }
+        BeamSection s;
+        memcpy(&s, sections + 10 * e, sizeof(s));
+        BeamElem el;
+        beam_prepare(x0, xt, R, v, s, E, G, rho, mass_type, el);
+        if (which >= 4) {
+            if (which == 4)
+                beam_restoring(el, out + 12 * e);
+            else
+                beam_distribload(el, q + 3 * e, out + 12 * e);
+            continue;
+        }
+        double *K = out + 144 * e;
+        for (int a = 0; a < 2; a++)
+            for (int b = a; b < 2; b++) {
+                double acc[6][6];
+                switch (which) {
+                case 0: beam_block<0>(el, a, b, acc); break;
+                case 1: beam_block<1>(el, a, b, acc); break;
+                case 2: beam_block<2>(el, a, b, acc); break;
+                default: beam_block<3>(el, a, b, acc); break;
+                }
+                for (int i = 0; i < 6; i++)
+                    for (int j = 0; j < 6; j++) {
+                        K[(6 * a + i) + 12 * (6 * b + j)] = acc[i][j];
+                        K[(6 * b + j) + 12 * (6 * a + i)] = acc[i][j];
+                    }
+            }
     }
     return 0;
 }

@@ -20,7 +20,7 @@ def lib():
     if _lib is None:
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
         srcs = [os.path.join(HERE, "hostcheck.cpp"), os.path.join(CSRC, "fs_elem_math.cuh"),
-                os.path.join(CSRC, "fs_host_prep.h")]
+                os.path.join(CSRC, "fs_host_prep.h"), os.path.join(CSRC, "fs_beam_math.cuh")]
         if not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in srcs):
             tmp = LIB + ".tmp%d" % os.getpid()
             subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-I", CSRC,
@@ -53,3 +53,25 @@ def element_matrices(etype, precision, xyz, conn, normals, valid, thickness, par
     if st != 0:
         raise RuntimeError("host check failed with status %d" % st)
     return out.transpose(0, 2, 1).copy()
+
+
+def beam_elements(which, xyz, conn, sections, E, nu, rho=0.0, u1=None, R1=None, v1=None,
+                  mass_type=1, q=None):
+    """The library's beam element math on the host: (nelem,12,12) or (nelem,12)."""
+    xyz = np.asfortranarray(xyz, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int64)
+    sec = np.ascontiguousarray(sections, dtype=np.float64)
+    f = lambda a: None if a is None else np.asfortranarray(a, dtype=np.float64)
+    u1, R1, v1 = f(u1), f(R1), f(v1)
+    ne = conn.shape[0]
+    if q is not None:
+        q = np.ascontiguousarray(np.broadcast_to(np.asarray(q, dtype=np.float64), (ne, 3)))
+    vec = which >= 4
+    out = np.zeros((ne, 12 if vec else 144))
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+    st = lib().hc_beam_elements(ctypes.c_int(which), ctypes.c_int64(xyz.shape[0]), P(xyz),
+                                ctypes.c_int64(ne), P(conn), P(u1), P(R1), P(v1), P(sec),
+                                ctypes.c_double(E), ctypes.c_double(nu), ctypes.c_double(rho),
+                                ctypes.c_int(mass_type), P(q), P(out))
+    assert st == 0
+    return out if vec else out.reshape(ne, 12, 12).transpose(0, 2, 1).copy()

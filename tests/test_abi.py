@@ -29,6 +29,7 @@ def test_struct_layouts_match_header():
     # fs_shell_params: 2 int32 + 3 doubles + 9 + 4 + 2 doubles
     assert ctypes.sizeof(_abi.fs_shell_params) == 8 + 8 * (3 + 9 + 4 + 2)
     assert ctypes.sizeof(_abi.fs_layup_group) == 8 * (9 * 3 + 4 + 9 + 3)
+    assert ctypes.sizeof(_abi.fs_beam_section) == 8 * 10
 
 
 def test_stab_fun_family():

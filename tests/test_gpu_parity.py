@@ -12,44 +12,12 @@ import flexshell as F
 from flexshell import _abi
 from oracle import oracle as O
 import problems as PB
+from checks import relmax, same_pattern, same_pattern_modulo_cancellation
 
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
 MIXED_TOL = 1e-6
-
-
-def relmax(A, B):
-    A = A.toarray() if hasattr(A, "toarray") else A
-    B = B.toarray() if hasattr(B, "toarray") else B
-    return np.abs(A - B).max() / np.abs(B).max()
-
-
-def same_pattern(A, B):
-    A = A.tocsc()
-    B = B.tocsc()
-    A.has_sorted_indices and B.has_sorted_indices
-    return (A.shape == B.shape and np.array_equal(A.indptr, B.indptr)
-            and np.array_equal(A.indices, B.indices))
-
-
-def same_pattern_modulo_cancellation(A, B, rel=1e-14):
-    """Patterns of two zero-dropping (SysmatAssemblerSparseSymm) results: an
-    entry may be stored in only one of them when its exact value is zero and
-    one operation order cancels it exactly while the other leaves round-off;
-    such entries must be below `rel` times the largest entry in both."""
-    A = A.tocsc()
-    B = B.tocsc()
-    if A.shape != B.shape:
-        return False
-    PA = (A != 0).astype(np.int8)
-    PB_ = (B != 0).astype(np.int8)
-    D = (PA - PB_).tocoo()
-    scale = max(abs(A).max(), abs(B).max())
-    for r, c in zip(D.row[D.data != 0], D.col[D.data != 0]):
-        if abs(A[r, c]) > rel * scale or abs(B[r, c]) > rel * scale:
-            return False
-    return True
 
 
 def homog_pair(d, quads, tsf=0):

@@ -88,3 +88,23 @@ def test_composite_fp64_matches_oracle(quads, angles):
     Kh = HC.element_matrices(et, _abi.FS_FP64, xyz, conn, P.normals, P.valid, 0.0, prm,
                              groups=[g], egroup=np.zeros(len(conn)))
     assert max(_relmax(Kh[e], Ko[e]) for e in range(len(Ko))) <= 1e-12
+
+
+def _beam_case(seed=0):
+    import beams
+    return beams.lattice_frame(seed=seed)
+
+
+@pytest.mark.parametrize("which,mass_type", [(0, 1), (1, 1), (2, 0), (2, 1), (2, 2), (2, 3),
+                                             (3, 0), (3, 1), (3, 3), (4, 1), (5, 1)])
+def test_beam_math_matches_oracle(which, mass_type):
+    # the beam kernels' per-element math (csrc/fs_beam_math.cuh: Gram form of
+    # aN' DN aN, sub-block rotations) against the oracle's dense Te SM Te'
+    xyz, conn, sec, u1, R1, v1, dof, nf = _beam_case()
+    E, nu, rho = 2.1e3, 0.3, 7.8
+    q = np.random.default_rng(2).normal(size=(conn.shape[0], 3))
+    H = HC.beam_elements(which, xyz, conn, sec, E, nu, rho, u1, R1, v1, mass_type, q)
+    b = O.Beam(xyz, conn, sec, E, nu, rho)
+    R = b.elements(which, u1=u1, R1=R1, v1=v1, mass_type=mass_type, q=q)
+    err = max(np.abs(h - r).max() / max(np.abs(r).max(), 1e-300) for h, r in zip(H, R))
+    assert err <= 1e-12
