@@ -49,6 +49,20 @@ def params(quads):
     return _abi.make_params(Dps, Dt, RHO, THICK, quads=quads)
 
 
+def measured_traffic(kernel, nelem):
+    """DRAM bytes (read + write) of one launch of `kernel`, scaled to `nelem`
+    elements from the per-element figure of the committed ncu summary
+    (profiles/*.md lines "traffic_bytes_per_element <kernel> <value>")."""
+    import glob
+    import re
+    for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        for line in open(f):
+            m = re.match(r"\s*traffic_bytes_per_element\s+(\S+)\s+([0-9.eE+]+)", line)
+            if m and m.group(1) == kernel:
+                return float(m.group(2)) * nelem, os.path.basename(f)
+    return None, None
+
+
 def read_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -474,14 +488,20 @@ def main():
     hbm, peak_kind = read_peaks()
     el_ms, ga_ms = t3["ph_mixed"][0], t3["ph_mixed"][1]
     nodes = (args.n + 1) ** 2
-    # algorithmic bytes per launch (per element / per stored value)
-    el_bytes = ne3 * (3 * 4 + 3 * 24 + 3 * 24 + 3 + 8 + 324 * 4)
-    ga_bytes = ne3 * 324 * 4 + nnz * 8 + ne3 * 3 * 8 + nodes * (6 * 4 + 8 + 4 + 8)
+    # algorithmic bytes per launch.  Element kernel: connectivity, coordinates,
+    # normals, flags, thickness in; the 6 upper 6x6 float node blocks out.
+    # Gather: the 9 node blocks each element contributes (a mirrored block is
+    # read for the lower ones), the double CSR values out, and the pattern
+    # (pair lists and slots, per-node dofs/offsets/row pointers, column map).
+    el_bytes = ne3 * (3 * 4 + 3 * 24 + 3 * 24 + 3 + 8 + 216 * 4)
+    ga_bytes = (ne3 * 324 * 4 + nnz * 8 + ne3 * 3 * 8 + nodes * (6 * 4 + 8 + 4 + 8 + 6 * 8)
+                + 2 * nnz // 6)
     if el_ms >= ga_ms:
         dom, ms_dom, alg = "k_t3_elements<float>", el_ms, el_bytes
     else:
         dom, ms_dom, alg = "k_gather<float>", ga_ms, ga_bytes
     achieved = alg / (ms_dom * 1e-3) / 1e9
+    traffic, traffic_src = measured_traffic(dom, ne3)
     cb = None
     if not args.no_cpu:
         cb, _ = cpu_baseline()
@@ -489,12 +509,12 @@ def main():
         "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32-element/f64-assembly", "data": "synthetic",
-        "config": {"workload": "T3FF stiffness assembly, mixed precision, 1024x1024 jittered wavy plate "
-                               "(2,097,152 triangles, 1,050,625 nodes, 6,303,750 dofs)",
+        "config": {"workload": "T3FF stiffness assembly, mixed precision, %dx%d jittered wavy plate "
+                               "(%d triangles, %d nodes, %d dofs)" % (args.n, args.n, ne3, nodes, 6 * nodes),
                    "elements": ne3, "nnz": nnz, "precision": "FS_MIXED", "assembler": "SysmatAssemblerSparse",
                    "pattern": "built once per mesh (symbolic %.2f ms), not in the timed step" % t3["t_sym"],
                    "l2": "inputs larger than L2 (element matrices %.2f GB, values %.2f GB)" % (
-                       ne3 * 324 * 4 / 1e9, nnz * 8 / 1e9),
+                       ne3 * 216 * 4 / 1e9, nnz * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": world * ne3 / (ms_e2e * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
@@ -502,7 +522,8 @@ def main():
                         "rebuilt) + fs_matrix_copy"},
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": peak_kind, "traffic": None,
+                     "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms_dom},
         "clocks": clocks.summary(),
         "cpu_baseline": cb,
