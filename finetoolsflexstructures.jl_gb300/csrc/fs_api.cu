@@ -237,6 +237,7 @@ int fs_mesh_set(fs_ctx *c, int elem_type, int64_t nnodes, const double *xyz, int
     free_mesh(c->mesh);
     free_pattern(c->pat);
     free_beam(c);
+    c->batch = fs_ctx::Batch();
     c->normals_ready = false;
     c->ex.ready = false;
     MeshDev &m = c->mesh;
@@ -420,14 +421,15 @@ int fs::assemble_matrix(fs_ctx *c, int precision, int assembler, int64_t nrows, 
     }
     PatternDev &P = c->pat;
     c->timed = false;
-    FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-    FS_TRY(beam_which < 0 ? launch_elements(c, precision) : launch_beam_elements(c, beam_which, mass_type));
-    FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
     size_t need = (size_t)std::max<int64_t>(P.nnz, nrows);
     if (need > c->vals_cap || !c->vals) {
         FS_TRY(dalloc(c, &c->vals, need));
         c->vals_cap = need;
     }
+    if (beam_which < 0) FS_TRY(autotune_shell(c, precision));
+    FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+    FS_TRY(beam_which < 0 ? launch_elements(c, precision) : launch_beam_elements(c, beam_which, mass_type));
+    FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
     FS_TRY(launch_gather(c, precision, c->vals));
     FS_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
     int bits = 0;
@@ -492,6 +494,23 @@ int fs_mass(fs_ctx *c, int assembler, int64_t nrows, int64_t *nnz_out)
     FS_TRY(launch_masses(c));
     FS_TRY(assemble_mass(c, assembler, nrows));
     if (nnz_out) *nnz_out = c->mat_nnz;
+    return FS_OK;
+}
+
+int fs_autotune(fs_ctx *c, int mode)
+{
+    if (!c) return FS_ERR_BAD_INPUT;
+    if (mode < 0 || mode > 2) return set_err(c, FS_ERR_BAD_INPUT, "autotune mode must be 0, 1 or 2");
+    c->tune.mode = mode;
+    return FS_OK;
+}
+
+int fs_tuning(const fs_ctx *c, int32_t *out)
+{
+    if (!c || !out) return FS_ERR_BAD_INPUT;
+    out[0] = c->tune.elem_epb;
+    out[1] = c->tune.gather_warps;
+    out[2] = c->tune.from_tuner ? 1 : 0;
     return FS_OK;
 }
 

@@ -131,8 +131,9 @@ __global__ void k_to_float(int64_t n, const double *src, float *dst)
 static const int PI_TPB = 256;
 static const int PI_BLOCKS = 1024;
 
+// y = alpha K x, CD_LANES lanes per row
 __global__ void k_spmv(int64_t n, const int64_t *rowptr, const int32_t *colidx, const double *vals,
-                       const double *x, double *y)
+                       const double *x, double *y, double alpha = 1.0)
 {
     int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / CD_LANES;
     const int sub = threadIdx.x & (CD_LANES - 1);
@@ -141,7 +142,7 @@ __global__ void k_spmv(int64_t n, const int64_t *rowptr, const int32_t *colidx, 
         for (int64_t k = rowptr[row] + sub; k < rowptr[row + 1]; k += CD_LANES) s += vals[k] * x[colidx[k]];
 #pragma unroll
     for (int o = CD_LANES / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (row < n && sub == 0) y[row] = s;
+    if (row < n && sub == 0) y[row] = alpha * s;
 }
 
 // partial[b] = sum over this block's strided range of a[i] * b[i] (b may be a weight)
@@ -321,6 +322,26 @@ int fs_explicit_get_state(fs_ctx *c, double *U, double *V, double *A)
     if (U) FS_CUDA(c, cudaMemcpyAsync(U, x.U, bn, cudaMemcpyDeviceToHost, c->stream));
     if (V) FS_CUDA(c, cudaMemcpyAsync(V, x.V, bn, cudaMemcpyDeviceToHost, c->stream));
     if (A) FS_CUDA(c, cudaMemcpyAsync(A, x.A, bn, cudaMemcpyDeviceToHost, c->stream));
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FS_OK;
+}
+
+// Restoring force of the shells: -K U with the last assembled matrix.
+int fs_restoring_force(fs_ctx *c, const double *U, double *F)
+{
+    if (!c) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    if (!c->mat_rowptr) return set_err(c, FS_ERR_STATE, "no stiffness assembled");
+    const int64_t n = c->mat_n;
+    if (n && (!U || !F)) return set_err(c, FS_ERR_BAD_INPUT, "missing vector");
+    if (n == 0) return FS_OK;
+    FS_TRY(ensure_scratch(c, sizeof(double) * 2 * (size_t)n));
+    double *u = (double *)c->scratch, *f = u + n;
+    FS_CUDA(c, cudaMemcpyAsync(u, U, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    const unsigned gs = (unsigned)((n * CD_LANES + 255) / 256);
+    k_spmv<<<gs, 256, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, c->vals, u, f, -1.0);
+    FS_CUDA(c, cudaGetLastError());
+    FS_CUDA(c, cudaMemcpyAsync(F, f, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
     return FS_OK;
 }

@@ -133,6 +133,18 @@ struct fs_ctx {
         cudaGraphExec_t exec = nullptr;
         int64_t graph_steps = 0;
     } ex;
+    // tile shapes of the shell element kernel and of the gather (0: defaults)
+    struct Tune {
+        int mode = -1;         // -1: not read yet (FLEXSHELL_AUTOTUNE), 0 off, 1 on, 2 re-tune
+        int elem_epb = 0;      // elements per block
+        int gather_warps = 0;  // warps (nodes) per block
+        bool from_tuner = false;
+    } tune;
+    // batched meshes fused into one mesh (fs_batch_*): first matrix row of each
+    struct Batch {
+        bool active = false;
+        std::vector<int64_t> roff;  // nmeshes + 1
+    } batch;
     // co-rotational beams (FEMMCorotBeam)
     struct Beam {
         fs::BeamSection *sec = nullptr;  // per rank
@@ -171,6 +183,11 @@ int ensure_scratch(fs_ctx *c, size_t bytes);
 int read_status(fs_ctx *c, int *bits);
 
 int explicit_launch_steps(fs_ctx *c, int64_t nsteps);
+
+// tile-shape autotuner of the shell assembly
+int autotune_shell(fs_ctx *c, int precision);
+size_t t3_smem(int precision, bool avgk, int epb);
+size_t q4_smem(int precision, int epb);
 
 // co-rotational beams
 int launch_beam_elements(fs_ctx *c, int which, int mass_type);

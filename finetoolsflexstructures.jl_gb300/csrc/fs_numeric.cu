@@ -15,6 +15,11 @@
 // left-to-right sum of its element contributions in assembly order, as
 // Julia's sparse(I, J, V) combines duplicates.  No atomics: the result is
 // bitwise reproducible.
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "fs_internal.cuh"
 
 namespace fs {
@@ -166,12 +171,18 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
     }
 }
 
-template <class R, bool COMP, bool AVGK>
-static int run_t3(fs_ctx *c, R *ke)
+// Shared memory of one block of the element kernels (per-element Gram rows).
+size_t t3_smem(int precision, bool avgk, int epb)
 {
-    constexpr int EPB = (sizeof(R) == 8 && AVGK) ? 64 : 128;
-    constexpr int NR = T3Rows<AVGK>::N;
-    size_t smem = sizeof(R) * (size_t)EPB * (NR * 18 + 1);
+    const int nr = avgk ? T3Rows<true>::N : T3Rows<false>::N;
+    return (precision == FS_FP64 ? 8 : 4) * (size_t)epb * (nr * 18 + 1);
+}
+size_t q4_smem(int precision, int epb) { return (precision == FS_FP64 ? 8 : 4) * (size_t)epb * (36 * 24 + 1); }
+
+template <class R, bool COMP, bool AVGK, int EPB>
+static int run_t3_epb(fs_ctx *c, R *ke)
+{
+    const size_t smem = t3_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, AVGK, EPB);
     auto kern = k_t3_elements<R, COMP, AVGK, EPB>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<nblk2(c->mesh.nelem, EPB), EPB, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
@@ -179,16 +190,35 @@ static int run_t3(fs_ctx *c, R *ke)
     return FS_OK;
 }
 
-template <class R, bool COMP>
-static int run_q4(fs_ctx *c, R *ke)
+template <class R, bool COMP, bool AVGK>
+static int run_t3(fs_ctx *c, R *ke)
 {
-    constexpr int EPB = 32;
-    size_t smem = sizeof(R) * (size_t)EPB * (36 * 24 + 1);
+    int epb = c->tune.elem_epb;
+    if (epb <= 0) epb = (sizeof(R) == 8 && AVGK) ? 64 : 128;
+    if (epb == 32) return run_t3_epb<R, COMP, AVGK, 32>(c, ke);
+    if (epb == 64 || (sizeof(R) == 8 && AVGK)) return run_t3_epb<R, COMP, AVGK, 64>(c, ke);
+    return run_t3_epb<R, COMP, AVGK, 128>(c, ke);
+}
+
+template <class R, bool COMP, int EPB>
+static int run_q4_epb(fs_ctx *c, R *ke)
+{
+    const size_t smem = q4_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, EPB);
     auto kern = k_q4_elements<R, COMP, EPB>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<nblk2(c->mesh.nelem, EPB), EPB * 4, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
     FS_CUDA(c, cudaGetLastError());
     return FS_OK;
+}
+
+template <class R, bool COMP>
+static int run_q4(fs_ctx *c, R *ke)
+{
+    int epb = c->tune.elem_epb;
+    if (epb <= 0) epb = 32;
+    if (epb == 16) return run_q4_epb<R, COMP, 16>(c, ke);
+    if (epb == 64 && sizeof(R) == 4) return run_q4_epb<R, COMP, 64>(c, ke);
+    return run_q4_epb<R, COMP, 32>(c, ke);
 }
 
 int launch_elements(fs_ctx *c, int precision)
@@ -244,7 +274,6 @@ int launch_elements(fs_ctx *c, int precision)
 // error below 2^-46 of the largest contribution.  Rows longer than
 // 32 * G_COLS positions fall back to accumulating in place in double.
 static const int G_MAXP = 8;
-template <class R> struct GatherCfg { static const int WARPS = sizeof(R) == 4 ? 8 : 4; };
 
 // 16-byte asynchronous global -> shared copy (bypassing registers and L1)
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -280,19 +309,18 @@ __device__ __forceinline__ double f2d_exact(float f)
     return __hiloint2double((int)(sign | (dexp << 20) | (man >> 3)), (int)(man << 29));
 }
 
-template <class R, int NEN, int G_COLS>
-__global__ void __launch_bounds__(GatherCfg<R>::WARPS * 32)
+template <class R, int NEN, int G_COLS, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
-    constexpr int WARPS = GatherCfg<R>::WARPS;
     constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
     constexpr bool SINGLE = sizeof(R) == 4;
     constexpr int CH = SLAB * (int)sizeof(R) / 16;  // 16-byte chunks per slab
-    __shared__ __align__(16) R stage_all[WARPS][G_MAXP * SLAB];
+    extern __shared__ __align__(16) unsigned char gather_smem[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t r = (int64_t)blockIdx.x * WARPS + w;
     if (r >= m.nnodes) return;
-    R *stage = stage_all[w];
+    R *stage = reinterpret_cast<R *>(gather_smem) + w * (G_MAXP * SLAB);
     int32_t d[6];
     bool any = false;
 #pragma unroll
@@ -421,28 +449,45 @@ __global__ void __launch_bounds__(GatherCfg<R>::WARPS * 32)
     }
 }
 
-template <class R, int NEN>
-static void gather_launch(fs_ctx *c, const R *ke, double *vals)
+template <class R, int NEN, int G_COLS, int W>
+static int gather_launch_w(fs_ctx *c, const R *ke, double *vals)
 {
-    MeshDev &m = c->mesh;
-    constexpr int W = GatherCfg<R>::WARPS;
-    unsigned g = nblk2(m.nnodes, W);
+    const MeshDev &m = c->mesh;
+    const size_t smem = sizeof(R) * (size_t)W * G_MAXP * NEN * 36;
+    auto kern = k_gather<R, NEN, G_COLS, W>;
+    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
+    return FS_OK;
+}
+
+template <class R, int NEN, int G_COLS>
+static int gather_launch_c(fs_ctx *c, const R *ke, double *vals, int warps)
+{
+    if (warps == 4) return gather_launch_w<R, NEN, G_COLS, 4>(c, ke, vals);
+    if (warps == 16) return gather_launch_w<R, NEN, G_COLS, 16>(c, ke, vals);
+    return gather_launch_w<R, NEN, G_COLS, 8>(c, ke, vals);
+}
+
+template <class R, int NEN>
+static int gather_launch(fs_ctx *c, const R *ke, double *vals, int warps)
+{
     // per-lane columns sized to the longest row (rows beyond 128 accumulate in place)
-    if (c->pat.maxlen <= 64)
-        k_gather<R, NEN, 2><<<g, W * 32, 0, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
-    else
-        k_gather<R, NEN, 4><<<g, W * 32, 0, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
+    if (c->pat.maxlen <= 64) return gather_launch_c<R, NEN, 2>(c, ke, vals, warps);
+    return gather_launch_c<R, NEN, 4>(c, ke, vals, warps);
 }
 
 template <class R>
-static int run_gather(fs_ctx *c, const R *ke, double *vals)
+static int run_gather(fs_ctx *c, const R *ke, double *vals, int warps)
 {
+    if (warps <= 0) warps = sizeof(R) == 4 ? 8 : 4;
+    int st;
     if (c->mesh.nen == 3)
-        gather_launch<R, 3>(c, ke, vals);
+        st = gather_launch<R, 3>(c, ke, vals, warps);
     else if (c->mesh.nen == 2)
-        gather_launch<R, 2>(c, ke, vals);
+        st = gather_launch<R, 2>(c, ke, vals, warps);
     else
-        gather_launch<R, 4>(c, ke, vals);
+        st = gather_launch<R, 4>(c, ke, vals, warps);
+    FS_TRY(st);
     FS_CUDA(c, cudaGetLastError());
     return FS_OK;
 }
@@ -450,8 +495,9 @@ static int run_gather(fs_ctx *c, const R *ke, double *vals)
 int launch_gather(fs_ctx *c, int precision, double *vals)
 {
     if (c->mesh.nnodes == 0) return FS_OK;
-    if (precision == FS_FP64) return run_gather<double>(c, (const double *)c->ke, vals);
-    return run_gather<float>(c, (const float *)c->ke, vals);
+    const int w = c->tune.gather_warps;
+    if (precision == FS_FP64) return run_gather<double>(c, (const double *)c->ke, vals, w);
+    return run_gather<float>(c, (const float *)c->ke, vals, w);
 }
 
 // ---------------------------------------------------------------------------
@@ -682,8 +728,118 @@ int launch_elements_to(fs_ctx *c, int precision, void *ke)
 int launch_gather_from(fs_ctx *c, int precision, const void *ke, double *vals)
 {
     if (c->mesh.nnodes == 0) return FS_OK;
-    if (precision == FS_FP64) return run_gather<double>(c, (const double *)ke, vals);
-    return run_gather<float>(c, (const float *)ke, vals);
+    const int w = c->tune.gather_warps;
+    if (precision == FS_FP64) return run_gather<double>(c, (const double *)ke, vals, w);
+    return run_gather<float>(c, (const float *)ke, vals, w);
+}
+
+// ---------------------------------------------------------------------------
+// tile-shape autotuner
+// ---------------------------------------------------------------------------
+// Candidates: elements per block of the element kernel (T3: 32, 64, 128;
+// Q4: 16, 32, 64, as far as their shared memory fits in 227 KB) and warps
+// per block of the gather (4, 8, 16).  Each candidate is timed on the
+// context's own mesh with CUDA events (best of three launches), the element
+// kernel first, then the gather on its output.  The choice is keyed on
+// element family, precision, the average-K option and log2 of the element
+// count, and kept for the whole process.  Tile shapes change only how
+// elements and nodes are grouped into blocks, never the arithmetic of one
+// element or one stored value, so every candidate gives bitwise the same
+// matrix.
+namespace {
+struct TuneKey {
+    int etype, precision, avgk, bucket;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(etype, precision, avgk, bucket) < std::tie(o.etype, o.precision, o.avgk, o.bucket);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune;
+const size_t SMEM_MAX = 227 * 1024;
+const int64_t TUNE_MIN_ELEMENTS = 4096;
+}  // namespace
+
+static int time_best(fs_ctx *c, int (*run)(fs_ctx *, int), int precision, float *best_ms)
+{
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+        FS_TRY(run(c, precision));
+        FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
+        FS_CUDA(c, cudaEventSynchronize(c->ev[1]));
+        float ms = 0.f;
+        FS_CUDA(c, cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+        best = ms < best ? ms : best;
+    }
+    *best_ms = best;
+    return FS_OK;
+}
+
+static int run_elements_once(fs_ctx *c, int precision) { return launch_elements(c, precision); }
+static int run_gather_once(fs_ctx *c, int precision) { return launch_gather(c, precision, c->vals); }
+
+int autotune_shell(fs_ctx *c, int precision)
+{
+    if (c->tune.mode < 0) {
+        const char *e = getenv("FLEXSHELL_AUTOTUNE");
+        c->tune.mode = (e && e[0] == '0') ? 0 : 1;
+    }
+    const MeshDev &m = c->mesh;
+    c->tune.from_tuner = false;
+    if (c->tune.mode == 0 || m.nelem < TUNE_MIN_ELEMENTS) {
+        c->tune.elem_epb = 0;
+        c->tune.gather_warps = 0;
+        return FS_OK;
+    }
+    const bool avgk = c->params.transv_shear_formulation == 1;
+    int bucket = 0;
+    while ((int64_t(1) << (bucket + 1)) <= m.nelem) bucket++;
+    const TuneKey key{m.etype, precision, avgk ? 1 : 0, bucket};
+    if (c->tune.mode == 1) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            c->tune.elem_epb = it->second.first;
+            c->tune.gather_warps = it->second.second;
+            c->tune.from_tuner = true;
+            return FS_OK;
+        }
+    }
+    const bool t3 = m.nen == 3;
+    const int ecand[3] = {t3 ? 32 : 16, t3 ? 64 : 32, t3 ? 128 : 64};
+    int best_e = 0;
+    float best_ms = 1e30f;
+    for (int epb : ecand) {
+        const size_t smem = t3 ? t3_smem(precision, avgk, epb) : q4_smem(precision, epb);
+        if (smem > SMEM_MAX) continue;
+        c->tune.elem_epb = epb;
+        float ms = 0.f;
+        FS_TRY(time_best(c, run_elements_once, precision, &ms));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_e = epb;
+        }
+    }
+    c->tune.elem_epb = best_e;
+    FS_TRY(launch_elements(c, precision));  // the gather candidates read these element matrices
+    int best_w = 0;
+    best_ms = 1e30f;
+    for (int w : {4, 8, 16}) {
+        c->tune.gather_warps = w;
+        float ms = 0.f;
+        FS_TRY(time_best(c, run_gather_once, precision, &ms));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_w = w;
+        }
+    }
+    c->tune.gather_warps = best_w;
+    c->tune.from_tuner = true;
+    if (c->tune.mode == 2) c->tune.mode = 1;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = {best_e, best_w};
+    return FS_OK;
 }
 
 }  // namespace fs

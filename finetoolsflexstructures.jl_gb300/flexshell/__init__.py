@@ -11,5 +11,6 @@ from ._abi import FS_FP64, FS_MIXED
 from .femm import (FEMMShellQ4RS, FEMMShellQ4RSComp, FEMMShellT3FF, FEMMShellT3FFComp,
                    NodalField, SysmatAssemblerFFBlock, SysmatAssemblerSparse,
                    SysmatAssemblerSparseCSRSymm, SysmatAssemblerSparseDiag,
-                   SysmatAssemblerSparseSymm)
+                   SysmatAssemblerSparseSymm, ShellBatch)
+from .beam import FEMMCorotBeam
 from ._lib import Context, FlexShellError, laminate

@@ -61,6 +61,12 @@ def lib():
         L.fs_power_iteration.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_uint64, vp]
         L.fs_laminate.argtypes = [ctypes.c_int32, vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_int32,
                                   ctypes.c_double, ctypes.POINTER(_abi.fs_layup_group)]
+        L.fs_restoring_force.argtypes = [vp, vp, vp]
+        L.fs_autotune.argtypes = [vp, ctypes.c_int]
+        L.fs_tuning.argtypes = [vp, vp]
+        L.fs_batch_set.argtypes = [vp, ctypes.c_int, ctypes.c_int32, vp, vp, vp, vp, vp, vp, vp]
+        L.fs_batch_stiffness.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+        L.fs_batch_matrix_copy.argtypes = [vp, ctypes.c_int32, vp, vp, vp]
         L.fs_beam_setup.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.fs_beam_state_set.argtypes = [vp, vp, vp, vp]
         L.fs_beam_matrix.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64, _c_i64_p]

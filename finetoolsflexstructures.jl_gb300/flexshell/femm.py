@@ -245,6 +245,21 @@ class _FEMMShell:
         self.ctx.call("fs_mass", assembler.mode, nrows, ctypes.byref(nnz))
         return self._fetch(nrows, nnz.value, assembler.csr)
 
+    def restoringforce(self, geom0, u1, Rfield1, dchi, precision=FS_FP64):
+        """-K U for the generalized displacements held in dchi.values (6 per node),
+        returned as a vector of nalldofs(dchi) entries.  An extension: the
+        reference shells have no restoringforce; its explicit loop subtracts
+        E = K U (plate_expl_examples.jl:85)."""
+        K_n = dchi.nalldofs()
+        self.stiffness(SysmatAssemblerSparse(), geom0, u1, Rfield1, dchi, precision=precision)
+        d = np.asarray(dchi.dofnums, dtype=np.int64)
+        U = np.zeros(K_n)
+        ok = (d >= 1) & (d <= K_n)
+        U[d[ok] - 1] = np.asarray(dchi.values)[ok]
+        F = np.zeros(K_n)
+        self.ctx.call("fs_restoring_force", ptr(U), ptr(F))
+        return F
+
     # -- extras ----------------------------------------------------------------
     def element_matrices(self, geom0, precision=FS_FP64):
         """All element stiffness matrices in the global basis (nelem x nd x nd)."""
@@ -307,3 +322,59 @@ class FEMMShellQ4RSComp(_FEMMShellComp):
     etype = _abi.FS_Q4RSCOMP
     nen = 4
     default_stab = 0.1
+
+
+class ShellBatch:
+    """Uneven homogeneous meshes of one shell family assembled together
+    (fs_batch_*): one element launch over the work-list of all elements and
+    one gather launch.  `meshes` is a list of (geom0, conn, dchi, thickness);
+    each mesh's matrix equals what its own FEMM would return."""
+
+    def __init__(self, femm_cls, meshes, material, stab_fun=None, nrows=None, device=0):
+        import ctypes
+        from .materials import shell_material_stiffness
+        self.ctx = Context(device)
+        Dps, Dt = shell_material_stiffness(material)
+        quads = femm_cls.nen == 4
+        p = _abi.make_params(Dps, Dt, material.massdensity(), 0.0,
+                             stab_c=stab_coefficient(stab_fun, femm_cls.default_stab), quads=quads)
+        self.ctx.call("fs_params_set", p, None)
+        self.n = len(meshes)
+        keep = []
+        arr = lambda vals, t: (t * self.n)(*vals)
+        xyzs = [np.asfortranarray(g.values, dtype=np.float64) for g, _, _, _ in meshes]
+        conns = [np.ascontiguousarray(c, dtype=np.int64) for _, c, _, _ in meshes]
+        dofs = [np.asfortranarray(d.dofnums, dtype=np.int64) for _, _, d, _ in meshes]
+        keep += xyzs + conns + dofs
+        self.nrows = [int(nrows[i]) if nrows is not None else d.nalldofs() for i, (_, _, d, _) in enumerate(meshes)]
+        vp = ctypes.c_void_p
+        self.ctx.call("fs_batch_set", femm_cls.etype, self.n,
+                      arr([x.shape[0] for x in xyzs], ctypes.c_int64), arr([x.ctypes.data for x in xyzs], vp),
+                      arr([c.shape[0] for c in conns], ctypes.c_int64), arr([c.ctypes.data for c in conns], vp),
+                      arr([d.ctypes.data for d in dofs], vp), arr(self.nrows, ctypes.c_int64),
+                      arr([float(t) for _, _, _, t in meshes], ctypes.c_double))
+        self._keep = keep
+
+    def stiffness(self, assembler=None, precision=FS_FP64, fetch=True):
+        """All meshes' stiffness matrices (a list of scipy CSC, or CSR for
+        SysmatAssemblerSparseCSRSymm)."""
+        import ctypes
+        import scipy.sparse as sp
+        assembler = assembler or SysmatAssemblerSparseSymm()
+        nnz = (ctypes.c_int64 * self.n)()
+        self.ctx.call("fs_batch_stiffness", precision, assembler.mode, nnz)
+        if not fetch:
+            return None
+        out = []
+        for i in range(self.n):
+            n, z = self.nrows[i], nnz[i]
+            colptr = np.empty(n + 1, dtype=np.int64)
+            rowval = np.empty(z, dtype=np.int64)
+            nzval = np.empty(z, dtype=np.float64)
+            self.ctx.call("fs_batch_matrix_copy", i, ptr(colptr), ptr(rowval), ptr(nzval))
+            cls = sp.csr_matrix if assembler.csr else sp.csc_matrix
+            out.append(cls((nzval, rowval - 1, colptr - 1), shape=(n, n)))
+        return out
+
+    def close(self):
+        self.ctx.close()

@@ -143,6 +143,17 @@ int fs_matrix_device(fs_ctx *ctx, const int64_t **rowptr, const int32_t **colidx
  * fs_stiffness call: [0] element kernel, [1] CSR gather, [2] symbolic phase of
  * the last pattern build, [3] zero compaction.  `n` entries are written. */
 int fs_timings(const fs_ctx *ctx, double *out, int n);
+/* Tile-shape autotuner of the shell assembly (elements per block of the
+ * element kernel, warps per block of the CSR gather).  Mode 1 (the default;
+ * environment FLEXSHELL_AUTOTUNE=0 makes 0 the default): the first fs_stiffness
+ * call for a new key (element family, precision, average-K option, log2 of the
+ * element count; meshes of at least 4096 elements) times every candidate on the
+ * context's mesh and the choice is reused by the whole process; 0: built-in
+ * shapes; 2: re-tune on the next call.  Tile shapes never change the results. */
+int fs_autotune(fs_ctx *ctx, int mode);
+/* Shapes used by the last fs_stiffness: out[0] elements per block (0 =
+ * default), out[1] gather warps per block (0 = default), out[2] 1 if tuned. */
+int fs_tuning(const fs_ctx *ctx, int32_t *out);
 /* Allocation-free stiffness values.  No counterpart in the reference: it is for
  * callers that cannot let the library allocate device memory at call time (a
  * host whose own pool allocator owns the device memory, or a solver loop under
@@ -230,6 +241,33 @@ int fs_beam_distribloads_global(fs_ctx *ctx, const double *q, int per_element, i
  * nelem x 12), for parity checks. */
 int fs_beam_element_matrices(fs_ctx *ctx, int which, int mass_type, double *out);
 int fs_beam_element_vectors(fs_ctx *ctx, int which, const double *q, int per_element, double *out);
+
+/* --- batched assembly of uneven meshes -------------------------------------
+ * Several homogeneous meshes of one family (FS_T3FF or FS_Q4RS) with the
+ * parameters of the last fs_params_set (whose thickness is replaced by one
+ * thickness per mesh).  Mesh i has nnodes[i] nodes (xyz[i], nnodes x 3
+ * column-major), nelem[i] elements (conn[i], 1-based within the mesh), its dof
+ * numbers (dofnums[i], nnodes x 6, 1-based within the mesh) and matrix size
+ * nrows[i].  The meshes are assembled together: one element-kernel launch over
+ * the work-list of all their elements and one gather launch over all their
+ * nodes; each mesh's matrix is bitwise the one fs_stiffness gives for it
+ * alone.  fs_batch_set computes the default normals. */
+int fs_batch_set(fs_ctx *ctx, int elem_type, int32_t nmeshes, const int64_t *nnodes, const double *const *xyz,
+                 const int64_t *nelem, const int64_t *const *conn, const int64_t *const *dofnums,
+                 const int64_t *nrows, const double *thickness);
+/* Assemble all meshes' stiffness matrices; nnz_out[i] (may be NULL) = stored
+ * entries of mesh i. */
+int fs_batch_stiffness(fs_ctx *ctx, int precision, int assembler, int64_t *nnz_out);
+/* Mesh i's matrix of the last fs_batch_stiffness: 1-based CSC (== CSR)
+ * colptr[nrows[i]+1], rowval[nnz_out[i]], nzval[nnz_out[i]]. */
+int fs_batch_matrix_copy(fs_ctx *ctx, int32_t mesh, int64_t *colptr, int64_t *rowval, double *nzval);
+
+/* Restoring force -K U of the shells for the generalized displacements U
+ * (mat_n entries, system numbering) with the last matrix assembled by
+ * fs_stiffness; F gets mat_n entries.  The reference shells have no such
+ * function: _cd_loop! (plate_expl_examples.jl:85) subtracts E = K U; the sign
+ * here follows FEMMCorotBeam.restoringforce (force on the nodes). */
+int fs_restoring_force(fs_ctx *ctx, const double *U, double *F);
 
 /* --- layup reduction (src/CompositeLayupModule.jl:246-330) ------------------ */
 /* ply_Dps: nplies x 9, ply_Dts: nplies x 4 (column-major each); angles in degrees;

@@ -256,3 +256,82 @@ def test_explicit_steps_match_oracle():
                   ctypes.c_uint64(7), ctypes.byref(om))
     assert abs(om.value - np.sqrt(w2)) <= 1e-3 * np.sqrt(w2)
     femm.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+def test_restoring_force_is_minus_K_U(quads):
+    # extension for the shells: F = -K U with U the generalized displacements
+    d = PB.scordelis_lo(quads, 6)
+    P, femm, geom0, dchi = homog_pair(d, quads)
+    rng = np.random.default_rng(4)
+    dchi.values = np.asfortranarray(rng.normal(size=dchi.values.shape))
+    F = femm.restoringforce(geom0, None, None, dchi)
+    n = dchi.nalldofs()
+    K = P.assemble_scipy("K", O.KEEP_ZEROS, n=n)
+    U = np.zeros(n)
+    U[dchi.dofnums.ravel() - 1] = dchi.values.ravel()
+    ref = -(K @ U)
+    assert np.abs(F - ref).max() <= FP64_TOL * 10 * np.abs(ref).max()
+    femm.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+@pytest.mark.parametrize("asm", [F.SysmatAssemblerSparse, F.SysmatAssemblerSparseSymm])
+def test_batch_equals_single_mesh_bitwise(quads, asm):
+    # uneven meshes fused into one launch: each mesh's matrix is bitwise the
+    # one its own FEMM gives (same element arithmetic, same summation order)
+    mat = F.materials.MatDeforElastIso(2.0e11, 0.3, 7850.0)
+    meshes, singles = [], []
+    for k, n in enumerate([3, 7, 5]):
+        xyz, conn, dof, nfree = PB.jittered_plate(n, quads, wavy=0.02, seed=k)
+        geom0 = F.NodalField(xyz)
+        dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+        dchi.dofnums = np.asfortranarray(dof)
+        t = 0.01 * (k + 1)
+        meshes.append((geom0, conn, dchi, t))
+        cls = F.FEMMShellQ4RS if quads else F.FEMMShellT3FF
+        femm = cls(conn, t, mat)
+        femm.associategeometry(geom0)
+        for prec in (F.FS_FP64, F.FS_MIXED):
+            singles.append(femm.stiffness(asm(), geom0, None, None, dchi, precision=prec))
+        femm.close()
+    b = F.ShellBatch(F.FEMMShellQ4RS if quads else F.FEMMShellT3FF, meshes, mat)
+    for j, prec in enumerate((F.FS_FP64, F.FS_MIXED)):
+        Ks = b.stiffness(asm(), precision=prec)
+        for i, K in enumerate(Ks):
+            S = singles[2 * i + j]
+            assert same_pattern(K, S)
+            assert np.array_equal(K.tocsc().data, S.tocsc().data)
+    b.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+def test_autotuner_choice_never_changes_the_matrix(quads):
+    import ctypes
+    mat = F.materials.MatDeforElastIso(2.0e11, 0.3, 7850.0)
+    xyz, conn, dof, nfree = PB.jittered_plate(72 if quads else 50, quads, wavy=0.02, seed=1)
+    geom0 = F.NodalField(xyz)
+    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(dof)
+    cls = F.FEMMShellQ4RS if quads else F.FEMMShellT3FF
+    femm = cls(conn, 0.01, mat)
+    femm.associategeometry(geom0)
+    assert conn.shape[0] >= 4096
+    out = (ctypes.c_int32 * 3)()
+    for prec in (F.FS_FP64, F.FS_MIXED):
+        femm.ctx.call("fs_autotune", 0)
+        K0 = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi, precision=prec)
+        femm.ctx.call("fs_tuning", out)
+        assert list(out) == [0, 0, 0]
+        femm.ctx.call("fs_autotune", 2)
+        K1 = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi, precision=prec)
+        femm.ctx.call("fs_tuning", out)
+        assert out[2] == 1 and out[0] > 0 and out[1] in (4, 8, 16)
+        assert np.array_equal(K0.data, K1.data) and np.array_equal(K0.indices, K1.indices)
+        # a second call reuses the process-wide choice
+        femm.ctx.call("fs_autotune", 1)
+        femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi, precision=prec)
+        out2 = (ctypes.c_int32 * 3)()
+        femm.ctx.call("fs_tuning", out2)
+        assert list(out2) == list(out)
+    femm.close()
