@@ -191,6 +191,11 @@ class Assembler:
         self.ctx.call("fs_stiffness", precision, 0, self.n, ctypes.byref(nnz))
         return nnz.value
 
+    def tiles(self):
+        t = (ctypes.c_int32 * 3)()
+        self.ctx.call("fs_tuning", t)
+        return {"elements_per_block": t[0], "gather_warps": t[1], "tuned": bool(t[2])}
+
     def timings(self):
         t = np.zeros(4)
         self.ctx.call("fs_timings", self.ptr(t), 4)
@@ -298,39 +303,39 @@ def batched_c3(torch, device=0, steps=5, warmup=3):
     panels = cylinder_panels()
     Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(4.32e8, 0.0))
     prm = _abi.make_params(Dps, Dt, 0.0, 0.0)
-    # one combined (block-diagonal) mesh: one element launch and one gather launch
-    xs, cs, ts, off = [], [], [], 0
-    for xyz, conn, t in panels:
-        xs.append(xyz)
-        cs.append(conn + off)
-        ts.append(np.full(conn.shape[0], t))
-        off += xyz.shape[0]
-    xyz = np.asfortranarray(np.concatenate(xs))
-    conn = np.ascontiguousarray(np.concatenate(cs))
-    th = np.ascontiguousarray(np.concatenate(ts))
-    dof, _ = __import__("flexshell").mesh.numberdofs(np.zeros((xyz.shape[0], 6), bool))
-    dof = np.asfortranarray(dof)
-    nel = conn.shape[0]
+    # the batch API (fs_batch_*): one element launch over the work-list of all
+    # panels' elements and one gather launch, each panel with its own dofs
     ctx = Context(device)
-    ctx.call("fs_mesh_set", _abi.FS_T3FF, xyz.shape[0], ptr(xyz), nel, ptr(conn), None, ptr(dof))
-    ctx.call("fs_params_set", prm, ptr(th))
-    ctx.call("fs_normals_compute")
-    n = 6 * xyz.shape[0]
+    ctx.call("fs_params_set", prm, None)
+    xyzs = [np.asfortranarray(p[0]) for p in panels]
+    conns = [np.ascontiguousarray(p[1]) for p in panels]
+    dofs = [np.asfortranarray(np.arange(1, 6 * x.shape[0] + 1, dtype=np.int64).reshape(-1, 6)) for x in xyzs]
+    k = len(panels)
+    arr = lambda vals, t: (t * k)(*vals)
+    vp = ctypes.c_void_p
+    ctx.call("fs_batch_set", _abi.FS_T3FF, k, arr([x.shape[0] for x in xyzs], ctypes.c_int64),
+             arr([x.ctypes.data for x in xyzs], vp), arr([c.shape[0] for c in conns], ctypes.c_int64),
+             arr([c.ctypes.data for c in conns], vp), arr([d.ctypes.data for d in dofs], vp),
+             arr([6 * x.shape[0] for x in xyzs], ctypes.c_int64), arr([p[2] for p in panels], ctypes.c_double))
+    nel = sum(c.shape[0] for c in conns)
     nnz = ctypes.c_int64()
     stream = torch.cuda.ExternalStream(ctx.stream())
     out = {"panels": len(panels), "elements": nel, "n_range": [int(min(p[1].shape[0] for p in panels)),
                                                              int(max(p[1].shape[0] for p in panels))]}
+    tiles = (ctypes.c_int32 * 3)()
     for prec, name in ((_abi.FS_MIXED, "mixed"), (_abi.FS_FP64, "fp64")):
         for _ in range(warmup):
-            ctx.call("fs_stiffness", prec, 0, ctypes.c_int64(n), ctypes.byref(nnz))
+            ctx.call("fs_batch_stiffness", prec, 0, None)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(steps):
-            ctx.call("fs_stiffness", prec, 0, ctypes.c_int64(n), ctypes.byref(nnz))
+            ctx.call("fs_batch_stiffness", prec, 0, None)
         e1.record(stream)
         torch.cuda.synchronize()
         out["batched_elements_per_s_" + name] = nel / (e0.elapsed_time(e1) / steps * 1e-3)
+        ctx.call("fs_tuning", tiles)
+        out["tiles_" + name] = {"elements_per_block": tiles[0], "gather_warps": tiles[1], "tuned": bool(tiles[2])}
     ctx.close()
     # one context and one call per panel
     ctxs = []
@@ -356,6 +361,142 @@ def batched_c3(torch, device=0, steps=5, warmup=3):
         out["per_mesh_elements_per_s_" + name] = nel / ((time.perf_counter() - t0) / steps)
     for c, _ in ctxs:
         c.close()
+    return out
+
+
+def corotbeam_lattice(torch, device=0, n=100, steps=5, warmup=3):
+    """FEMMCorotBeam throughput: beams along the edges of an n^3 lattice
+    (3 n^2 (n-1) elements) in a deformed state (random displacements and
+    nodal rotations), double precision; device time of the element kernel +
+    CSR gather for each matrix, and of the restoring-force kernels."""
+    from flexshell import _abi
+    from flexshell._lib import Context, ptr
+    rng = np.random.Generator(np.random.PCG64(7))
+    g = np.arange(n, dtype=np.float64)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    xyz = np.asfortranarray(np.column_stack([X.ravel(), Y.ravel(), Z.ravel()]) + rng.uniform(-0.1, 0.1, (n ** 3, 3)))
+    idx = np.arange(1, n ** 3 + 1).reshape(n, n, n)
+    conn = np.ascontiguousarray(np.concatenate(
+        [np.column_stack([np.moveaxis(idx, a, 0)[:-1].ravel(), np.moveaxis(idx, a, 0)[1:].ravel()])
+         for a in range(3)]), dtype=np.int64)
+    ne, nn = conn.shape[0], xyz.shape[0]
+    sec = (_abi.fs_beam_section * ne)()
+    arr = np.frombuffer(sec, dtype=np.float64).reshape(ne, 10)
+    arr[:, 0], arr[:, 2], arr[:, 3] = 0.01, 1e-5, 2e-5
+    arr[:, 1] = arr[:, 2] + arr[:, 3]
+    arr[:, 4], arr[:, 5], arr[:, 6] = 2.5e-5, np.inf, np.inf
+    arr[:, 7:] = rng.normal(size=(ne, 3))
+    dof = np.asfortranarray(np.arange(1, 6 * nn + 1, dtype=np.int64).reshape(nn, 6))
+    u1 = np.asfortranarray(rng.uniform(-0.01, 0.01, (nn, 3)))
+    # nodal rotations (Rodrigues) of small random rotation vectors, R[:] per node
+    a = rng.normal(scale=0.05, size=(nn, 3))
+    th = np.linalg.norm(a, axis=1)[:, None, None]
+    S = np.zeros((nn, 3, 3))
+    S[:, 0, 1], S[:, 0, 2], S[:, 1, 2] = -a[:, 2], a[:, 1], -a[:, 0]
+    S = S - S.transpose(0, 2, 1)
+    R = np.eye(3) + np.sin(th) / th * S + (1 - np.cos(th)) / th ** 2 * (S @ S)
+    R1 = np.asfortranarray(R.transpose(0, 2, 1).reshape(nn, 9))
+    v1 = np.asfortranarray(rng.normal(size=(nn, 6)))
+    ctx = Context(device)
+    ctx.call("fs_mesh_set", _abi.FS_COROTBEAM, nn, ptr(xyz), ne, ptr(conn), None, ptr(dof))
+    ctx.call("fs_beam_setup", sec, 2.1e11, 0.3, 7850.0)
+    ctx.call("fs_beam_state_set", ptr(u1), ptr(R1), ptr(v1))
+    nnz = ctypes.c_int64()
+    t = np.zeros(4)
+    out = {"elements": ne, "nodes": nn, "lattice": n}
+    for which, name in ((_abi.FS_BEAM_STIFFNESS, "stiffness"), (_abi.FS_BEAM_GEOSTIFFNESS, "geostiffness"),
+                        (_abi.FS_BEAM_MASS, "mass"), (_abi.FS_BEAM_GYROSCOPIC, "gyroscopic")):
+        for _ in range(warmup):
+            ctx.call("fs_beam_matrix", which, 1, 0, 6 * nn, ctypes.byref(nnz))
+        el = ga = 0.0
+        for _ in range(steps):
+            ctx.call("fs_beam_matrix", which, 1, 0, 6 * nn, ctypes.byref(nnz))
+            ctx.call("fs_timings", ptr(t), 4)
+            el += t[0]
+            ga += t[1]
+        out[name] = {"elements_per_s": ne / ((el + ga) / steps * 1e-3), "ms_elements": el / steps,
+                     "ms_gather": ga / steps}
+    out["nnz"] = nnz.value
+    F = np.empty(6 * nn)
+    for _ in range(warmup):
+        ctx.call("fs_beam_restoringforce", 6 * nn, ptr(F))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.call("fs_beam_restoringforce", 6 * nn, ptr(F))
+    out["restoringforce_elements_per_s_incl_d2h"] = ne / ((time.perf_counter() - t0) / steps)
+    ctx.close()
+    return out
+
+
+def composite_c4(torch, device=0, n=512, n_eig=64, nev=20, steps=5, warmup=3):
+    """The layered Q4RS plate ([0/90/90/0], 0.25 mm plies, 1 m side, simply
+    supported): mixed and FP64 stiffness + lumped-mass assembly at n x n, and
+    the nev lowest eigenvalues (shift-invert Lanczos, SciPy's ARPACK as the
+    reference's eigs) from the FP64 and mixed matrices of an n_eig x n_eig
+    plate (the direct factorisation of the full-size plate is beyond the bench's
+    time budget)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    from flexshell import _abi, materials, mesh
+    from flexshell.femm import (FEMMShellQ4RSComp, NodalField, SysmatAssemblerFFBlock,
+                                SysmatAssemblerSparse, SysmatAssemblerSparseSymm)
+    from flexshell._lib import laminate, ptr
+    lam = materials.lamina_material(1600.0, 140e9, 10e9, 0.3, 5e9, 5e9, 3.5e9)
+    Dps, Dts = materials.shell_material_stiffness(lam)
+    g = laminate([dict(Dps=Dps, Dts=Dts, thickness=0.25e-3, angle=a, rho=1600.0) for a in (0, 90, 90, 0)])
+
+    def plate_c4(m):
+        xy, conn = mesh.Q4block(1.0, 1.0, m, m)
+        xyz = mesh.xyz3(xy)
+        x, y = xyz[:, 0], xyz[:, 1]
+        tol = 1.0 / m / 100
+        bnd = (np.abs(x) < tol) | (np.abs(x - 1) < tol) | (np.abs(y) < tol) | (np.abs(y - 1) < tol)
+        fixed = np.zeros((xyz.shape[0], 6), bool)
+        fixed[bnd, 2] = True
+        dof, nfree = mesh.numberdofs(fixed)
+        femm = FEMMShellQ4RSComp(conn, g, device=device)
+        geom0 = NodalField(xyz)
+        dchi = NodalField(np.zeros((xyz.shape[0], 6)))
+        dchi.dofnums = np.asfortranarray(dof)
+        femm.associategeometry(geom0)
+        return femm, geom0, dchi, nfree
+
+    out = {"elements": n * n, "eig_elements": n_eig * n_eig, "nev": nev}
+    femm, geom0, dchi, nfree = plate_c4(n)
+    stream = torch.cuda.ExternalStream(femm.ctx.stream())
+    asm = SysmatAssemblerSparse()
+    t = np.zeros(4)
+    for prec, name in ((_abi.FS_MIXED, "mixed"), (_abi.FS_FP64, "fp64")):
+        for _ in range(warmup):
+            femm.stiffness(asm, geom0, None, None, dchi, precision=prec)
+        ms = 0.0
+        for _ in range(steps):
+            nnz = ctypes.c_int64()
+            femm.ctx.call("fs_stiffness", prec, 0, dchi.nalldofs(), ctypes.byref(nnz))
+            femm.ctx.call("fs_timings", ptr(t), 4)
+            ms += t[0] + t[1]
+        out["stiffness_elements_per_s_" + name] = n * n / (ms / steps * 1e-3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    femm.mass(SysmatAssemblerSparseSymm(), geom0, dchi)
+    out["mass_ms_incl_copy"] = 1e3 * (time.perf_counter() - t0)
+    femm.close()
+    femm, geom0, dchi, nfree = plate_c4(n_eig)
+    ff = SysmatAssemblerFFBlock(SysmatAssemblerSparseSymm(), nfree)
+    K64 = femm.stiffness(ff, geom0, None, None, dchi)
+    K32 = femm.stiffness(ff, geom0, None, None, dchi, precision=_abi.FS_MIXED)
+    M = femm.mass(ff, geom0, dchi)
+    femm.close()
+    eig = lambda K: np.sort(spl.eigsh(K.tocsc(), k=nev, M=M.tocsc(), sigma=-1.0, which="LM",
+                                      return_eigenvectors=False, tol=1e-12))
+    w64, w32 = eig(K64), eig(K32)
+    big = np.abs(w64) > 1e-6 * np.abs(w64).max()
+    out["rigid_modes"] = int((~big).sum())
+    out["eig_rel_err_mixed_vs_fp64_max"] = float((np.abs(w32 - w64)[big] / np.abs(w64)[big]).max())
+    out["K_rel_err_mixed_vs_fp64_max"] = float(abs(K32 - K64).max() / abs(K64).max())
+    out["M_rel_err_mixed_vs_fp64_max"] = 0.0  # the lumped mass is double in both paths
+    out["lowest_flexural_hz"] = float(np.sqrt(w64[big][0]) / (2 * np.pi))
     return out
 
 
@@ -414,14 +555,17 @@ def main():
         t = torch.tensor([ms_mixed], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_mixed = float(t.item())
+    tiles_mixed = asm.tiles()
     v_mixed = asm.values(nnz)
     ms_fp64, ph_fp64, _ = time_steps(asm, _abi.FS_FP64, args.steps, args.warmup, torch, stream)
+    tiles_fp64 = asm.tiles()
     v_fp64 = asm.values(nnz)
     err_t3 = float(np.abs(v_mixed - v_fp64).max() / np.abs(v_fp64).max())
     fro_t3 = float(np.linalg.norm(v_mixed - v_fp64) / np.linalg.norm(v_fp64))
     del v_mixed, v_fp64
     res["t3"] = dict(ms_mixed=ms_mixed, ms_fp64=ms_fp64, ph_mixed=ph_mixed, ph_fp64=ph_fp64, nnz=nnz,
-                     err=err_t3, fro=fro_t3, t_sym=t_sym, nelem=conn.shape[0])
+                     err=err_t3, fro=fro_t3, t_sym=t_sym, nelem=conn.shape[0],
+                     tiles={"mixed": tiles_mixed, "fp64": tiles_fp64})
 
     # --- e2e through the C ABI from pinned host buffers (T3FF, mixed) ------------
     nn = xyz.shape[0]
@@ -467,8 +611,10 @@ def main():
     asm.stiffness(_abi.FS_MIXED)
     t_sym_q4 = asm.timings()[2]
     ms_q_mixed, ph_q_mixed, nnz_q = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
+    tiles_q = {"mixed": asm.tiles()}
     vq_m = asm.values(nnz_q)
     ms_q_fp64, ph_q_fp64, _ = time_steps(asm, _abi.FS_FP64, args.steps, args.warmup, torch, stream)
+    tiles_q["fp64"] = asm.tiles()
     vq_d = asm.values(nnz_q)
     err_q4 = float(np.abs(vq_m - vq_d).max() / np.abs(vq_d).max())
     del vq_m, vq_d
@@ -477,6 +623,8 @@ def main():
 
     ex = explicit_c5(torch, device=local) if not args.no_explicit else None
     bc3 = batched_c3(torch, device=local) if not args.no_explicit else None
+    beams = corotbeam_lattice(torch, device=local) if not args.no_explicit else None
+    c4 = composite_c4(torch, device=local) if not args.no_explicit else None
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -534,14 +682,16 @@ def main():
                      "rel_err_K_mixed_vs_fp64_max": t3["err"], "rel_err_K_mixed_vs_fp64_fro": t3["fro"],
                      "ms_elements_mixed": t3["ph_mixed"][0], "ms_gather_mixed": t3["ph_mixed"][1],
                      "ms_elements_fp64": t3["ph_fp64"][0], "ms_gather_fp64": t3["ph_fp64"][1],
-                     "ms_symbolic": t3["t_sym"], "e2e_ms": ms_e2e},
+                     "ms_symbolic": t3["t_sym"], "e2e_ms": ms_e2e, "tiles": t3["tiles"]},
             "q4rs": {"elements": ne4, "nnz": nnz_q, "mixed_elements_per_s": ne4 / (ms_q_mixed * 1e-3),
                      "fp64_elements_per_s": ne4 / (ms_q_fp64 * 1e-3), "mixed_over_fp64": ms_q_fp64 / ms_q_mixed,
                      "rel_err_K_mixed_vs_fp64_max": err_q4, "ms_elements_mixed": ph_q_mixed[0],
                      "ms_gather_mixed": ph_q_mixed[1], "ms_elements_fp64": ph_q_fp64[0],
-                     "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4},
+                     "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4, "tiles": tiles_q},
             "explicit_q4rs_512": ex,
             "batched_64_cylinder_panels": bc3,
+            "corotbeam_lattice_100": beams,
+            "composite_q4rs_512": c4,
         },
     }
     print(json.dumps(line))

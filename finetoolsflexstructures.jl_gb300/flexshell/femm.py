@@ -361,10 +361,11 @@ class ShellBatch:
         import ctypes
         import scipy.sparse as sp
         assembler = assembler or SysmatAssemblerSparseSymm()
+        if not fetch:
+            self.ctx.call("fs_batch_stiffness", precision, assembler.mode, None)
+            return None
         nnz = (ctypes.c_int64 * self.n)()
         self.ctx.call("fs_batch_stiffness", precision, assembler.mode, nnz)
-        if not fetch:
-            return None
         out = []
         for i in range(self.n):
             n, z = self.nrows[i], nnz[i]

@@ -8,7 +8,15 @@ driver code calls them unchanged:
     stiffness(femm::FEMMShellT3FF, assembler, geom0, u1, Rfield1, dchi)
     mass(femm::FEMMShellT3FF, assembler, geom0, dchi)
 
-(and the same for FEMMShellQ4RS, FEMMShellT3FFComp, FEMMShellQ4RSComp).
+(and the same for FEMMShellQ4RS, FEMMShellT3FFComp, FEMMShellQ4RSComp), and
+for FEMMCorotBeam
+
+    stiffness / geostiffness (femm, assembler, geom0, u1, Rfield1, dchi)
+    mass(femm, assembler, geom0, u1, Rfield1, dchi; mass_type)
+    gyroscopic(femm, assembler, geom0, u1, Rfield1, v1, dchi; mass_type)
+    restoringforce(femm, assembler, geom0, u1, Rfield1, dchi)
+    distribloads_global(femm, assembler, geom0, u1, Rfield1, dchi, fi)
+
 `associategeometry!` stays the reference's own; its normals are passed in.
 Not exercised in this repository (no Julia toolchain here); it is the
 binding a maintainer adds next to the reference.
@@ -21,10 +29,14 @@ using FinEtoolsFlexStructures.FEMMShellT3FFModule: FEMMShellT3FF
 using FinEtoolsFlexStructures.FEMMShellQ4RSModule: FEMMShellQ4RS
 import FinEtoolsFlexStructures.FEMMShellT3FFModule: stiffness, mass
 import FinEtoolsFlexStructures.FEMMShellQ4RSModule: stiffness, mass
+using FinEtoolsFlexStructures.FEMMCorotBeamModule: FEMMCorotBeam
+import FinEtoolsFlexStructures.FEMMCorotBeamModule: geostiffness, gyroscopic, restoringforce,
+    distribloads_global
 
 const libflexshell = get(ENV, "FLEXSHELL_LIB", "libflexshell.so")
 
-const FS_T3FF, FS_T3FFCOMP, FS_Q4RS, FS_Q4RSCOMP = 0, 1, 2, 3
+const FS_T3FF, FS_T3FFCOMP, FS_Q4RS, FS_Q4RSCOMP, FS_COROTBEAM = 0, 1, 2, 3, 4
+const FS_BEAM_STIFFNESS, FS_BEAM_GEOSTIFFNESS, FS_BEAM_MASS, FS_BEAM_GYROSCOPIC = 0, 1, 2, 3
 const FS_FP64, FS_MIXED = 0, 1
 const FS_ASM_SPARSE, FS_ASM_SPARSE_SYMM, FS_ASM_DIAG = 0, 1, 2
 
@@ -134,6 +146,88 @@ for (T, etype) in ((FEMMShellT3FF, FS_T3FF), (FEMMShellQ4RS, FS_Q4RS))
             ctx.h, asm_mode(assembler), nalldofs(dchi), nnz))
         return fetch_csc(ctx, nalldofs(dchi), nnz[])
     end
+end
+
+# ---------------------------------------------------------------------------
+# FEMMCorotBeam
+# ---------------------------------------------------------------------------
+# fs_beam_section (include/flexshell.h): the FESetL2Beam fields of one element
+struct FsBeamSection
+    A::Float64
+    I1::Float64
+    I2::Float64
+    I3::Float64
+    J::Float64
+    A2s::Float64
+    A3s::Float64
+    x1x2_vector::NTuple{3,Float64}
+end
+
+function beam_upload!(ctx, femm::FEMMCorotBeam, geom0, u1, Rfield1, dchi, v1 = nothing)
+    fes = femm.integdomain.fes
+    d = delegateof(fes)
+    conn = collect(reinterpret(Int, fes.conn))
+    xyz = geom0.values
+    check(ctx, ccall((:fs_mesh_set, libflexshell), Cint,
+        (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
+        ctx.h, FS_COROTBEAM, size(xyz, 1), xyz, count(fes), conn, C_NULL, dchi.dofnums))
+    secs = [FsBeamSection(d.A[i], d.I1[i], d.I2[i], d.I3[i], d.J[i], d.A2s[i], d.A3s[i],
+        Tuple(d.x1x2_vector[i])) for i in 1:count(fes)]
+    check(ctx, ccall((:fs_beam_setup, libflexshell), Cint,
+        (Ptr{Cvoid}, Ptr{FsBeamSection}, Float64, Float64, Float64),
+        ctx.h, secs, femm.material.E, femm.material.nu, massdensity(femm.material)))
+    check(ctx, ccall((:fs_beam_state_set, libflexshell), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        ctx.h, u1.values, Rfield1.values, v1 === nothing ? C_NULL : v1.values))
+end
+
+function beam_matrix(self, which, assembler, geom0, u1, Rfield1, dchi; mass_type = 1, v1 = nothing)
+    ctx = context(self)
+    beam_upload!(ctx, self, geom0, u1, Rfield1, dchi, v1)
+    nnz = Ref{Int64}(0)
+    check(ctx, ccall((:fs_beam_matrix, libflexshell), Cint, (Ptr{Cvoid}, Cint, Cint, Cint, Int64, Ref{Int64}),
+        ctx.h, which, mass_type, asm_mode(assembler), nalldofs(dchi), nnz))
+    return fetch_csc(ctx, nalldofs(dchi), nnz[])
+end
+
+stiffness(self::FEMMCorotBeam, assembler::AbstractSysmatAssembler, geom0::NodalField{Float64},
+    u1::NodalField{Float64}, Rfield1::NodalField{Float64}, dchi::NodalField{TI}) where {TI} =
+    beam_matrix(self, FS_BEAM_STIFFNESS, assembler, geom0, u1, Rfield1, dchi)
+geostiffness(self::FEMMCorotBeam, assembler::AbstractSysmatAssembler, geom0::NodalField{Float64},
+    u1::NodalField{Float64}, Rfield1::NodalField{Float64}, dchi::NodalField{TI}) where {TI} =
+    beam_matrix(self, FS_BEAM_GEOSTIFFNESS, assembler, geom0, u1, Rfield1, dchi)
+mass(self::FEMMCorotBeam, assembler::AbstractSysmatAssembler, geom0::NodalField{Float64},
+    u1::NodalField{Float64}, Rfield1::NodalField{Float64}, dchi::NodalField{TI};
+    mass_type = 1) where {TI} =
+    beam_matrix(self, FS_BEAM_MASS, assembler, geom0, u1, Rfield1, dchi; mass_type = mass_type)
+gyroscopic(self::FEMMCorotBeam, assembler::AbstractSysmatAssembler, geom0::NodalField{Float64},
+    u1::NodalField{Float64}, Rfield1::NodalField{Float64}, v1::NodalField{Float64},
+    dchi::NodalField{TI}; mass_type = 1) where {TI} =
+    beam_matrix(self, FS_BEAM_GYROSCOPIC, assembler, geom0, u1, Rfield1, dchi;
+        mass_type = mass_type, v1 = v1)
+
+function restoringforce(self::FEMMCorotBeam, assembler::AbstractSysvecAssembler, geom0::NodalField{Float64},
+    u1::NodalField{Float64}, Rfield1::NodalField{Float64}, dchi::NodalField{TI}) where {TI}
+    ctx = context(self)
+    beam_upload!(ctx, self, geom0, u1, Rfield1, dchi)
+    F = zeros(nalldofs(dchi))
+    check(ctx, ccall((:fs_beam_restoringforce, libflexshell), Cint, (Ptr{Cvoid}, Int64, Ptr{Float64}),
+        ctx.h, length(F), F))
+    return F
+end
+
+# uniform force intensity (ForceIntensity of a constant vector); loads varying
+# per element go as a 3 x nelem array with per_element = 1
+function distribloads_global(self::FEMMCorotBeam, assembler::AbstractSysvecAssembler,
+    geom0::NodalField{Float64}, u1::NodalField{Float64}, Rfield1::NodalField{Float64},
+    dchi::NodalField{TI}, fi) where {TI}
+    ctx = context(self)
+    beam_upload!(ctx, self, geom0, u1, Rfield1, dchi)
+    q = Float64.(updateforce!(fi, zeros(0, 0), zeros(0, 0), 1, 0)[1:3])
+    F = zeros(nalldofs(dchi))
+    check(ctx, ccall((:fs_beam_distribloads_global, libflexshell), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Cint, Int64, Ptr{Float64}), ctx.h, q, 0, length(F), F))
+    return F
 end
 
 end # module

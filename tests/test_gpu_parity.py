@@ -335,3 +335,35 @@ def test_autotuner_choice_never_changes_the_matrix(quads):
         femm.ctx.call("fs_tuning", out2)
         assert list(out2) == list(out)
     femm.close()
+
+
+def test_composite_eigenvalues_mixed_vs_fp64():
+    # layered Q4RS plate (scaled-down layered-plate configuration): the 20
+    # lowest eigenvalues from the mixed K agree with those from the FP64 K to
+    # 1e-6, and the FP64 ones with the oracle's to 1e-10
+    xyz, conn, dof, nfree, plies = PB.c4_plate(24)
+    g = F.laminate(plies)
+    femm = F.FEMMShellQ4RSComp(conn, g)
+    geom0 = F.NodalField(xyz)
+    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(dof)
+    femm.associategeometry(geom0)
+    asm = F.SysmatAssemblerFFBlock(F.SysmatAssemblerSparseSymm(), nfree)
+    K64 = femm.stiffness(asm, geom0, None, None, dchi)
+    K32 = femm.stiffness(asm, geom0, None, None, dchi, precision=F.FS_MIXED)
+    M = femm.mass(asm, geom0, dchi)
+    w64 = PB.lowest_eigenvalues(K64, M)
+    w32 = PB.lowest_eigenvalues(K32, M)
+    A, B, D, H, md, mi = O.laminate(plies)
+    t = sum(p["thickness"] for p in plies)
+    P = O.Problem(O.Q4RSCOMP, xyz, conn, dof, groups=[dict(A=A, B=B, D=D, H=H, csmat=np.eye(3), thickness=t,
+                                                            mass=md, moi=mi)])
+    P.compute_normals()
+    Ko = P.assemble_scipy("K", O.DROP_ZEROS, n=nfree)
+    Mo = P.assemble_scipy("M", O.DROP_ZEROS, n=nfree)
+    wo = PB.lowest_eigenvalues(Ko, Mo)
+    big = np.abs(w64) > 1e-6 * np.abs(w64).max()  # the rigid in-plane modes are numerical zeros
+    assert np.abs(w64 - wo)[big].max() <= 1e-10 * np.abs(wo).max()
+    rel = np.abs(w32 - w64)[big] / np.abs(w64)[big]
+    assert rel.max() <= 1e-6, rel.max()
+    femm.close()
