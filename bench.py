@@ -431,7 +431,7 @@ def corotbeam_lattice(torch, device=0, n=100, steps=5, warmup=3):
 
 def composite_c4(torch, device=0, n=512, n_eig=64, nev=20, steps=5, warmup=3):
     """The layered Q4RS plate ([0/90/90/0], 0.25 mm plies, 1 m side, simply
-    supported): mixed and FP64 stiffness + lumped-mass assembly at n x n, and
+    supported, in-plane rigid-body motion restrained): mixed and FP64 stiffness + lumped-mass assembly at n x n, and
     the nev lowest eigenvalues (shift-invert Lanczos, SciPy's ARPACK as the
     reference's eigs) from the FP64 and mixed matrices of an n_eig x n_eig
     plate (the direct factorisation of the full-size plate is beyond the bench's
@@ -454,6 +454,9 @@ def composite_c4(torch, device=0, n=512, n_eig=64, nev=20, steps=5, warmup=3):
         bnd = (np.abs(x) < tol) | (np.abs(x - 1) < tol) | (np.abs(y) < tol) | (np.abs(y - 1) < tol)
         fixed = np.zeros((xyz.shape[0], 6), bool)
         fixed[bnd, 2] = True
+        # in-plane rigid-body motion restrained: u = v = 0 at (0, 0), v = 0 at (1, 0)
+        c0, c1 = int(np.argmin(np.abs(x) + np.abs(y))), int(np.argmin(np.abs(x - 1) + np.abs(y)))
+        fixed[c0, 0] = fixed[c0, 1] = fixed[c1, 1] = True
         dof, nfree = mesh.numberdofs(fixed)
         femm = FEMMShellQ4RSComp(conn, g, device=device)
         geom0 = NodalField(xyz)
@@ -491,12 +494,11 @@ def composite_c4(torch, device=0, n=512, n_eig=64, nev=20, steps=5, warmup=3):
     eig = lambda K: np.sort(spl.eigsh(K.tocsc(), k=nev, M=M.tocsc(), sigma=-1.0, which="LM",
                                       return_eigenvectors=False, tol=1e-12))
     w64, w32 = eig(K64), eig(K32)
-    big = np.abs(w64) > 1e-6 * np.abs(w64).max()
-    out["rigid_modes"] = int((~big).sum())
-    out["eig_rel_err_mixed_vs_fp64_max"] = float((np.abs(w32 - w64)[big] / np.abs(w64)[big]).max())
+    out["eig_rel_err_mixed_vs_fp64_max"] = float((np.abs(w32 - w64) / np.abs(w64)).max())
     out["K_rel_err_mixed_vs_fp64_max"] = float(abs(K32 - K64).max() / abs(K64).max())
     out["M_rel_err_mixed_vs_fp64_max"] = 0.0  # the lumped mass is double in both paths
-    out["lowest_flexural_hz"] = float(np.sqrt(w64[big][0]) / (2 * np.pi))
+    out["lowest_hz"] = float(np.sqrt(w64[0]) / (2 * np.pi))
+    out["boundary"] = "w = 0 on the edges; u = v = 0 at (0,0), v = 0 at (1,0)"
     return out
 
 

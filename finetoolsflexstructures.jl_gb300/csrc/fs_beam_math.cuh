@@ -305,7 +305,7 @@ FS_HD void beam_prepare(const double x0[2][3], const double xt[2][3], const doub
 // Node block (a, b) of the global element matrix WHICH (0 stiffness,
 // 1 geometric stiffness, 2 mass, 3 gyroscopic): acc[i][j] = K[6a+i][6b+j].
 template <int WHICH>
-FS_HD void beam_block(const BeamElem &e, int a, int b, double acc[6][6])
+FS_HD void beam_block_raw(const BeamElem &e, int a, int b, double acc[6][6])
 {
     if (WHICH == 0) {
         // K = sum_k DN_k g_k g_k'
@@ -347,6 +347,18 @@ FS_HD void beam_block(const BeamElem &e, int a, int b, double acc[6][6])
             for (int i = 0; i < 3; i++)
                 for (int j = 0; j < 3; j++) acc[3 * pp + i][3 * qq + j] = K[i][j];
         }
+}
+
+// Node block (a, b); a diagonal block is made exactly symmetric from its
+// upper triangle (as complete_lt! does), so the assembled matrix is symmetric
+// to the bit.
+template <int WHICH>
+FS_HD void beam_block(const BeamElem &e, int a, int b, double acc[6][6])
+{
+    beam_block_raw<WHICH>(e, a, b, acc);
+    if (a == b)
+        for (int i = 0; i < 6; i++)
+            for (int j = i + 1; j < 6; j++) acc[j][i] = acc[i][j];
 }
 
 // Restoring force -Te aN' PN (restoringforce, src/FEMMCorotBeamModule.jl:1112-1159).

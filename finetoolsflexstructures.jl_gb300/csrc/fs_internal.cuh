@@ -67,6 +67,13 @@ struct PatternDev {
     uint32_t *pair_slots = nullptr;  // per pair: 8-bit slot of each element node
     int16_t *colpos = nullptr;   // per node: 6 x nnbr positions in the row (or -1)
     uint16_t *colsrc = nullptr;  // per node: for row position j, neighbour slot * 6 + component
+    // per (node, neighbour slot): the node's contributions to that slot's columns, in
+    // ascending pair order; an entry is q | b << 6 | (b < a_q) << 8 with q the pair
+    // index within the node (< 64), b the element node at that slot, a_q the node's
+    // own element node (the block is the mirror of an upper block when b < a_q).
+    // The entries of node r start at pp[r] * nen; sl_off gives each slot's start.
+    uint16_t *sl_off = nullptr;  // per (node, slot), relative to the node's first entry
+    uint16_t *sl_ent = nullptr;  // npairs * nen
     int32_t *rowlen = nullptr;   // per node: row length L
     int64_t *rowptr = nullptr;   // n + 1
     int32_t *colidx = nullptr;   // nnz, 0-based

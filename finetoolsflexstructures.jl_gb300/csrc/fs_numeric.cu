@@ -224,8 +224,6 @@ static int run_q4(fs_ctx *c, R *ke)
 int launch_elements(fs_ctx *c, int precision)
 {
     MeshDev &m = c->mesh;
-    size_t nd = 6 * m.nen;
-    (void)nd;
     size_t bytes = (size_t)m.nelem * n_upper_blocks(m.nen) * 36 * (precision == FS_FP64 ? 8 : 4);
     if (bytes > c->ke_bytes) {
         if (c->ke) cudaFree(c->ke);
@@ -309,18 +307,38 @@ __device__ __forceinline__ double f2d_exact(float f)
     return __hiloint2double((int)(sign | (dexp << 20) | (man >> 3)), (int)(man << 29));
 }
 
+// exact float -> double for normal numbers and zeros from the bit pattern
+// (rebias the exponent, move the mantissa); other values take f2d_exact
+__device__ __forceinline__ double f2d_fast(float f)
+{
+    const uint32_t u = __float_as_uint(f), a = u & 0x7fffffffu;
+    if (a != 0u && a - 0x00800000u >= 0x7f000000u) return f2d_exact(f);  // subnormal, inf, nan
+    const uint32_t h = (u & 0x80000000u) | (a != 0u ? (a >> 3) + 0x38000000u : 0u);
+    return __hiloint2double((int)h, (int)(u << 29));
+}
+
+// shared memory of one warp: G_MAXP staged slabs, then the node's
+// contribution entries (at most 64 pairs x 4 element nodes)
+template <class R, int NEN> struct GatherSmem {
+    static constexpr int PER_WARP = G_MAXP * NEN * 36 * (int)sizeof(R) + 512;
+};
+
 template <class R, int NEN, int G_COLS, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
     constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
     constexpr bool SINGLE = sizeof(R) == 4;
-    constexpr int CH = SLAB * (int)sizeof(R) / 16;  // 16-byte chunks per slab
+    constexpr int BCH = 36 * (int)sizeof(R) / 16;  // 16-byte chunks per 6x6 block
+    constexpr int CH = NEN * BCH;                   // 16-byte chunks per slab
+    constexpr int CPL = (CH + 31) / 32;             // chunks per lane per pair
     extern __shared__ __align__(16) unsigned char gather_smem[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t r = (int64_t)blockIdx.x * WARPS + w;
     if (r >= m.nnodes) return;
-    R *stage = reinterpret_cast<R *>(gather_smem) + w * (G_MAXP * SLAB);
+    unsigned char *wsm = gather_smem + (size_t)w * GatherSmem<R, NEN>::PER_WARP;
+    R *stage = reinterpret_cast<R *>(wsm);
+    uint16_t *sent = reinterpret_cast<uint16_t *>(wsm + G_MAXP * SLAB * sizeof(R));
     int32_t d[6];
     bool any = false;
 #pragma unroll
@@ -330,71 +348,89 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
     if (!any) return;
     const int L = P.rowlen[r];
-    const int64_t off6 = P.nbr_off[r] * 6;
+    const int64_t off = P.nbr_off[r], off6 = off * 6;
     const int64_t pb = m.pp[r], pe = m.pp[r + 1];
     if (L <= 32 * G_COLS) {
-        int sc[G_COLS], kcol[G_COLS];
+        // the node's contribution entries into shared memory
+        const int ntot = (int)(pe - pb) * NEN;
+        const uint16_t *ent = P.sl_ent + pb * NEN;
+        for (int i = lane; i < ntot; i += 32) sent[i] = ent[i];
+        // the lane's columns and the range of entries of their neighbour slot
+        const int nslots = (int)(P.nbr_off[r + 1] - off);
+        int kcol[G_COLS], cur[G_COLS], last[G_COLS];
         R hi[G_COLS][6], lo[G_COLS][6];
 #pragma unroll
         for (int c = 0; c < G_COLS; c++) {
-            int j = lane + 32 * c;
-            int cs = j < L ? (int)P.colsrc[off6 + j] : -6;
-            sc[c] = cs >= 0 ? cs / 6 : -1;
-            kcol[c] = cs >= 0 ? cs - 6 * sc[c] : 0;
+            const int j = lane + 32 * c;
+            kcol[c] = 0;
+            cur[c] = 0;
+            last[c] = 0;
+            if (j < L) {
+                const int cs = (int)P.colsrc[off6 + j];
+                const int sl = cs / 6;
+                kcol[c] = cs - 6 * sl;
+                cur[c] = (int)P.sl_off[off + sl];
+                last[c] = sl + 1 < nslots ? (int)P.sl_off[off + sl + 1] : ntot;
+            }
 #pragma unroll
             for (int k = 0; k < 6; k++) {
                 hi[c][k] = 0;
                 lo[c][k] = 0;
             }
         }
+        // lane-fixed staging chunks: chunk lane + 32 t of every slab
+        int cb[CPL], cwd[CPL];
+#pragma unroll
+        for (int t = 0; t < CPL; t++) {
+            const int ch = lane + 32 * t;
+            cb[t] = ch / BCH;
+            cwd[t] = ch - cb[t] * BCH;
+        }
         for (int64_t p0 = pb; p0 < pe; p0 += G_MAXP) {
             const int cnt = (int)min((int64_t)G_MAXP, pe - p0);
-            int32_t pel = lane < cnt ? m.pair_e[p0 + lane] : 0;
-            uint32_t sll = lane < cnt ? P.pair_slots[p0 + lane] : 0u;
-            const int total = cnt * CH;
-            constexpr int BCH = 36 * (int)sizeof(R) / 16;  // 16-byte chunks per block
-            for (int base = 0; base < total; base += 32) {
-                int k = base + lane;
-                int q = k / CH;
-                int32_t peq = __shfl_sync(0xffffffffu, pel, q < cnt ? q : 0);
-                if (k < total) {
-                    int ch = k - q * CH;
-                    int bb = ch / BCH, cw = ch - bb * BCH;
-                    int a = peq & 3;
-                    // block (a, bb) of the element: stored as itself or as its mirror
-                    const R *src = ke + (int64_t)(peq >> 2) * ND2 + ub(min(a, bb), max(a, bb), NEN) * 36;
-                    cp_async16(reinterpret_cast<char *>(stage + q * SLAB + bb * 36) + 16 * cw,
-                               reinterpret_cast<const char *>(src) + 16 * cw);
+            const int q0 = (int)(p0 - pb);
+            for (int q = 0; q < cnt; q++) {
+                const int32_t pel = m.pair_e[p0 + q];
+                const int a = pel & 3;
+                const R *base = ke + (int64_t)(pel >> 2) * ND2;
+#pragma unroll
+                for (int t = 0; t < CPL; t++) {
+                    if (lane + 32 * t < CH) {
+                        const int bb = cb[t];
+                        // block (a, bb) of the element: stored as itself or as its mirror
+                        const R *src = base + ub(min(a, bb), max(a, bb), NEN) * 36;
+                        cp_async16(reinterpret_cast<char *>(stage + q * SLAB + bb * 36) + 16 * cwd[t],
+                                   reinterpret_cast<const char *>(src) + 16 * cwd[t]);
+                    }
                 }
             }
             cp_async_wait_all();
             __syncwarp();
-            for (int q = 0; q < cnt; q++) {
-                uint32_t slots = __shfl_sync(0xffffffffu, sll, q);
-                const int aq = __shfl_sync(0xffffffffu, pel, q) & 3;
+            // this batch's contributions to the lane's columns, ascending pair order
 #pragma unroll
-                for (int c = 0; c < G_COLS; c++) {
-                    int b = -1;
-#pragma unroll
-                    for (int bb = 0; bb < NEN; bb++)
-                        if ((int)((slots >> (8 * bb)) & 0xffu) == sc[c]) b = bb;
-                    if (b < 0) continue;
-                    // entry (krow, kcol) of block (aq, b); a mirrored block is read transposed
-                    const bool tr = b < aq;
+            for (int c = 0; c < G_COLS; c++) {
+                while (cur[c] < last[c]) {
+                    const uint32_t e = sent[cur[c]];
+                    const int q = (int)(e & 63u) - q0;
+                    if (q >= cnt) break;
+                    const int b = (int)((e >> 6) & 3u);
+                    // entry (krow, kcol) of block (a_q, b); a mirrored block is read transposed
+                    const bool tr = (e >> 8) & 1u;
                     const R *src = stage + q * SLAB + b * 36 + (tr ? 6 * kcol[c] : kcol[c]);
                     const int st = tr ? 1 : 6;
 #pragma unroll
                     for (int k = 0; k < 6; k++) {
-                        R v = src[st * k];
+                        const R v = src[st * k];
                         if (SINGLE) {
-                            R t = hi[c][k] + v;
-                            R bp = t - hi[c][k];
+                            const R t = hi[c][k] + v;
+                            const R bp = t - hi[c][k];
                             lo[c][k] += (hi[c][k] - (t - bp)) + (v - bp);
                             hi[c][k] = t;
                         } else {
                             hi[c][k] += v;
                         }
                     }
+                    cur[c]++;
                 }
             }
             __syncwarp();
@@ -405,14 +441,14 @@ __global__ void __launch_bounds__(WARPS * 32)
             double *o = vals + P.rowptr[d[k] - 1];
 #pragma unroll
             for (int c = 0; c < G_COLS; c++) {
-                int j = lane + 32 * c;
+                const int j = lane + 32 * c;
                 if (j >= L) continue;
                 double v;
                 if (SINGLE) {
-                    float t = (float)hi[c][k] + (float)lo[c][k];
-                    float e = (float)lo[c][k] - (t - (float)hi[c][k]);
-                    v = f2d_exact(t);
-                    if (__float_as_uint(e) & 0x7fffffffu) v += f2d_exact(e);
+                    // hi + lo: exact in double unless their exponents are more than
+                    // 29 apart, then rounded once
+                    v = f2d_fast((float)hi[c][k]);
+                    if (lo[c][k] != (R)0) v += f2d_fast((float)lo[c][k]);
                 } else {
                     v = (double)hi[c][k];
                 }
@@ -453,7 +489,7 @@ template <class R, int NEN, int G_COLS, int W>
 static int gather_launch_w(fs_ctx *c, const R *ke, double *vals)
 {
     const MeshDev &m = c->mesh;
-    const size_t smem = sizeof(R) * (size_t)W * G_MAXP * NEN * 36;
+    const size_t smem = (size_t)W * GatherSmem<R, NEN>::PER_WARP;
     auto kern = k_gather<R, NEN, G_COLS, W>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals);

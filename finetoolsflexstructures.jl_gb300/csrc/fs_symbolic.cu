@@ -320,7 +320,8 @@ __global__ void k_count_nbrs(int64_t nnodes, int nen, const int64_t *pp, const i
 __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_t *pp,
                             const int32_t *pair_e, const int32_t *conn, const int32_t *dof,
                             const int64_t *nbr_off, int32_t *nbr, uint32_t *pair_slots,
-                            int16_t *colpos, uint16_t *colsrc, int32_t *rowlen)
+                            int16_t *colpos, uint16_t *colsrc, int32_t *rowlen, uint16_t *sl_off,
+                            uint16_t *sl_ent)
 {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nnodes) return;
@@ -343,6 +344,23 @@ __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_
             packed |= (uint32_t)(lo & 0xff) << (8 * k);
         }
         pair_slots[p] = packed;
+    }
+    // contribution lists per neighbour slot (ascending pair order)
+    {
+        const int64_t p0 = pp[r];
+        const int np = (int)min((int64_t)MAX_PAIRS_PER_NODE, pp[r + 1] - p0);
+        uint16_t *ent = sl_ent + p0 * nen;
+        int w = 0;
+        for (int s = 0; s < n; s++) {
+            sl_off[off + s] = (uint16_t)w;
+            for (int q = 0; q < np; q++) {
+                const uint32_t packed = pair_slots[p0 + q];
+                const int aq = pair_e[p0 + q] & 3;
+                for (int b = 0; b < nen; b++)
+                    if ((int)((packed >> (8 * b)) & 0xffu) == s)
+                        ent[w++] = (uint16_t)(q | (b << 6) | ((b < aq ? 1 : 0) << 8));
+            }
+        }
     }
     // column positions: rank of each valid column dof among the node's columns
     int L = 0;
@@ -431,9 +449,12 @@ int build_pattern(fs_ctx *c, int64_t n)
     FS_TRY(dalloc(c, &P.colpos, (size_t)nbr_total * 6));
     FS_TRY(dalloc(c, &P.colsrc, (size_t)nbr_total * 6));
     FS_TRY(dalloc(c, &P.rowlen, (size_t)nn));
+    FS_TRY(dalloc(c, &P.sl_off, (size_t)nbr_total));
+    FS_TRY(dalloc(c, &P.sl_ent, (size_t)(m.npairs * m.nen)));
     if (nn)
         k_fill_nbrs<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, m.nen, n, m.pp, m.pair_e, m.conn, m.dof, P.nbr_off,
-                                                         P.nbr, P.pair_slots, P.colpos, P.colsrc, P.rowlen);
+                                                         P.nbr, P.pair_slots, P.colpos, P.colsrc, P.rowlen,
+                                                         P.sl_off, P.sl_ent);
     // row lengths by dof
     int32_t *owner = nullptr;
     FS_TRY(dalloc(c, &owner, (size_t)n));

@@ -179,7 +179,10 @@ def c4_plate(n, side=1.0):
     """The layered-plate configuration: n x n Q4 on a flat square (side 1 m),
     [0/90/90/0] plies of 0.25 mm (E1 140 GPa, E2 10 GPa, G12 = G13 5 GPa, G23
     3.5 GPa, nu12 0.3, rho 1600), cartesian layup csys, simply supported
-    (w = 0 on the boundary)."""
+    (w = 0 on the boundary) with the in-plane rigid-body motion restrained
+    (u = v = 0 at (0, 0), v = 0 at (side, 0)): left free, those three zero
+    modes would be lifted by any rounding of the membrane stiffness into the
+    range of the lowest bending modes."""
     xy, conn = mesh.Q4block(side, side, n, n)
     xyz = mesh.xyz3(xy)
     x, y = xyz[:, 0], xyz[:, 1]
@@ -187,14 +190,16 @@ def c4_plate(n, side=1.0):
     bnd = (np.abs(x) < tol) | (np.abs(x - side) < tol) | (np.abs(y) < tol) | (np.abs(y - side) < tol)
     fixed = np.zeros((xyz.shape[0], 6), bool)
     fixed[bnd, 2] = True
+    c0 = int(np.argmin(np.abs(x) + np.abs(y)))
+    c1 = int(np.argmin(np.abs(x - side) + np.abs(y)))
+    fixed[c0, 0] = fixed[c0, 1] = fixed[c1, 1] = True
     dof, nfree = mesh.numberdofs(fixed)
     return xyz, conn, dof, nfree, cross_ply_groups((0, 90, 90, 0))
 
 
 def lowest_eigenvalues(K, M, nev=20, sigma=-1.0):
     """The nev lowest eigenvalues of (K, M) by shift-invert Lanczos (ARPACK,
-    as the reference's eigs) about `sigma` (the simply supported plate keeps
-    its three in-plane rigid-body modes)."""
+    as the reference's eigs) about `sigma`."""
     import scipy.sparse.linalg as spl
     w = spl.eigsh(K.tocsc(), k=nev, M=M.tocsc(), sigma=sigma, which="LM", return_eigenvectors=False,
                   tol=1e-12)
