@@ -470,7 +470,7 @@ def composite_c4(torch, device=0, n=512, n_eig=64, nev=20, steps=5, warmup=3):
     stream = torch.cuda.ExternalStream(femm.ctx.stream())
     asm = SysmatAssemblerSparse()
     t = np.zeros(4)
-    for prec, name in ((_abi.FS_MIXED, "mixed"), (_abi.FS_FP64, "fp64")):
+    for prec, name in ((_abi.FS_MIXED, "mixed"), (_abi.FS_MIXED_COMP, "mixed_comp"), (_abi.FS_FP64, "fp64")):
         for _ in range(warmup):
             femm.stiffness(asm, geom0, None, None, dchi, precision=prec)
         ms = 0.0
@@ -489,13 +489,16 @@ def composite_c4(torch, device=0, n=512, n_eig=64, nev=20, steps=5, warmup=3):
     ff = SysmatAssemblerFFBlock(SysmatAssemblerSparseSymm(), nfree)
     K64 = femm.stiffness(ff, geom0, None, None, dchi)
     K32 = femm.stiffness(ff, geom0, None, None, dchi, precision=_abi.FS_MIXED)
+    Kc = femm.stiffness(ff, geom0, None, None, dchi, precision=_abi.FS_MIXED_COMP)
     M = femm.mass(ff, geom0, dchi)
     femm.close()
     eig = lambda K: np.sort(spl.eigsh(K.tocsc(), k=nev, M=M.tocsc(), sigma=-1.0, which="LM",
                                       return_eigenvectors=False, tol=1e-12))
-    w64, w32 = eig(K64), eig(K32)
+    w64, w32, wc = eig(K64), eig(K32), eig(Kc)
     out["eig_rel_err_mixed_vs_fp64_max"] = float((np.abs(w32 - w64) / np.abs(w64)).max())
+    out["eig_rel_err_mixed_comp_vs_fp64_max"] = float((np.abs(wc - w64) / np.abs(w64)).max())
     out["K_rel_err_mixed_vs_fp64_max"] = float(abs(K32 - K64).max() / abs(K64).max())
+    out["K_rel_err_mixed_comp_vs_fp64_max"] = float(abs(Kc - K64).max() / abs(K64).max())
     out["M_rel_err_mixed_vs_fp64_max"] = 0.0  # the lumped mass is double in both paths
     out["lowest_hz"] = float(np.sqrt(w64[0]) / (2 * np.pi))
     out["boundary"] = "w = 0 on the edges; u = v = 0 at (0,0), v = 0 at (1,0)"
@@ -564,9 +567,14 @@ def main():
     v_fp64 = asm.values(nnz)
     err_t3 = float(np.abs(v_mixed - v_fp64).max() / np.abs(v_fp64).max())
     fro_t3 = float(np.linalg.norm(v_mixed - v_fp64) / np.linalg.norm(v_fp64))
-    del v_mixed, v_fp64
+    del v_mixed
+    ms_comp, ph_comp, _ = time_steps(asm, _abi.FS_MIXED_COMP, args.steps, args.warmup, torch, stream)
+    v_comp = asm.values(nnz)
+    err_t3c = float(np.abs(v_comp - v_fp64).max() / np.abs(v_fp64).max())
+    del v_comp, v_fp64
     res["t3"] = dict(ms_mixed=ms_mixed, ms_fp64=ms_fp64, ph_mixed=ph_mixed, ph_fp64=ph_fp64, nnz=nnz,
                      err=err_t3, fro=fro_t3, t_sym=t_sym, nelem=conn.shape[0],
+                     ms_comp=ms_comp, ph_comp=ph_comp, err_comp=err_t3c,
                      tiles={"mixed": tiles_mixed, "fp64": tiles_fp64})
 
     # --- e2e through the C ABI from pinned host buffers (T3FF, mixed) ------------
@@ -619,7 +627,11 @@ def main():
     tiles_q["fp64"] = asm.tiles()
     vq_d = asm.values(nnz_q)
     err_q4 = float(np.abs(vq_m - vq_d).max() / np.abs(vq_d).max())
-    del vq_m, vq_d
+    del vq_m
+    ms_q_comp, ph_q_comp, _ = time_steps(asm, _abi.FS_MIXED_COMP, args.steps, args.warmup, torch, stream)
+    vq_c = asm.values(nnz_q)
+    err_q4c = float(np.abs(vq_c - vq_d).max() / np.abs(vq_d).max())
+    del vq_c, vq_d
     asm.ctx.close()
     del asm
 
@@ -684,12 +696,19 @@ def main():
                      "rel_err_K_mixed_vs_fp64_max": t3["err"], "rel_err_K_mixed_vs_fp64_fro": t3["fro"],
                      "ms_elements_mixed": t3["ph_mixed"][0], "ms_gather_mixed": t3["ph_mixed"][1],
                      "ms_elements_fp64": t3["ph_fp64"][0], "ms_gather_fp64": t3["ph_fp64"][1],
-                     "ms_symbolic": t3["t_sym"], "e2e_ms": ms_e2e, "tiles": t3["tiles"]},
+                     "ms_symbolic": t3["t_sym"], "e2e_ms": ms_e2e, "tiles": t3["tiles"],
+                     "mixed_comp_elements_per_s": ne3 / (t3["ms_comp"] * 1e-3),
+                     "mixed_comp_over_fp64": ms_fp64 / t3["ms_comp"],
+                     "rel_err_K_mixed_comp_vs_fp64_max": t3["err_comp"],
+                     "ms_elements_mixed_comp": t3["ph_comp"][0], "ms_gather_mixed_comp": t3["ph_comp"][1]},
             "q4rs": {"elements": ne4, "nnz": nnz_q, "mixed_elements_per_s": ne4 / (ms_q_mixed * 1e-3),
                      "fp64_elements_per_s": ne4 / (ms_q_fp64 * 1e-3), "mixed_over_fp64": ms_q_fp64 / ms_q_mixed,
                      "rel_err_K_mixed_vs_fp64_max": err_q4, "ms_elements_mixed": ph_q_mixed[0],
                      "ms_gather_mixed": ph_q_mixed[1], "ms_elements_fp64": ph_q_fp64[0],
-                     "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4, "tiles": tiles_q},
+                     "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4, "tiles": tiles_q,
+                     "mixed_comp_elements_per_s": ne4 / (ms_q_comp * 1e-3),
+                     "rel_err_K_mixed_comp_vs_fp64_max": err_q4c,
+                     "ms_elements_mixed_comp": ph_q_comp[0], "ms_gather_mixed_comp": ph_q_comp[1]},
             "explicit_q4rs_512": ex,
             "batched_64_cylinder_panels": bc3,
             "corotbeam_lattice_100": beams,

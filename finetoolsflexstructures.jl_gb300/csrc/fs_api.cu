@@ -474,7 +474,8 @@ int fs_stiffness(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t
     if (c->mesh.etype == FS_COROTBEAM)
         return set_err(c, FS_ERR_UNSUPPORTED, "beam mesh: use fs_beam_matrix (FS_BEAM_STIFFNESS)");
     FS_TRY(check_ready(c));
-    if (precision != FS_FP64 && precision != FS_MIXED) return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
+    if (precision != FS_FP64 && precision != FS_MIXED && precision != FS_MIXED_COMP)
+        return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
     if (assembler < FS_ASM_SPARSE || assembler > FS_ASM_DIAG) return set_err(c, FS_ERR_BAD_INPUT, "unknown assembler");
     if (!c->normals_ready)
         return set_err(c, FS_ERR_STATE, "associategeometry! has not been called (self._associatedgeometry == true)");
@@ -575,6 +576,8 @@ int fs_element_matrices(fs_ctx *c, int precision, double *out)
     if (!c || !out) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
     FS_TRY(check_ready(c, false));
+    if (precision != FS_FP64 && precision != FS_MIXED && precision != FS_MIXED_COMP)
+        return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
     if (!c->normals_ready)
         return set_err(c, FS_ERR_STATE, "associategeometry! has not been called (self._associatedgeometry == true)");
     FS_TRY(launch_elements(c, precision));
@@ -594,7 +597,9 @@ int fs_element_matrices(fs_ctx *c, int precision, double *out)
         kd.resize(stored * m.nelem);
         if (m.nelem) FS_CUDA(c, cudaMemcpy(kd.data(), c->ke, sizeof(double) * kd.size(), cudaMemcpyDeviceToHost));
     } else {
-        kf.resize(stored * m.nelem);
+        // float entries, or float pairs (hi, lo) of the compensated path
+        const size_t w = precision == FS_MIXED_COMP ? 2 : 1;
+        kf.resize(w * stored * m.nelem);
         if (m.nelem) FS_CUDA(c, cudaMemcpy(kf.data(), c->ke, sizeof(float) * kf.size(), cudaMemcpyDeviceToHost));
     }
     for (int64_t r = 0; r < m.nelem; r++) {
@@ -605,7 +610,9 @@ int fs_element_matrices(fs_ctx *c, int precision, double *out)
                     for (int j = 0; j < 6; j++) {
                         size_t src = stored * r +
                                      (a <= b ? (size_t)ub(a, b, nen) * 36 + i * 6 + j : (size_t)ub(b, a, nen) * 36 + j * 6 + i);
-                        double v = precision == FS_FP64 ? kd[src] : (double)kf[src];
+                        double v = precision == FS_FP64         ? kd[src]
+                                   : precision == FS_MIXED_COMP ? (double)kf[2 * src] + (double)kf[2 * src + 1]
+                                                                : (double)kf[src];
                         o[(6 * a + i) + (size_t)nd * (6 * b + j)] = v;
                     }
     }

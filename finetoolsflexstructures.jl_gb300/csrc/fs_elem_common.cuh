@@ -1,0 +1,138 @@
+// Device helpers shared by the element kernels (T3 and Q4 translation units)
+// and the numeric phase: element input loading and the stores of the upper
+// node blocks of an element matrix.
+#pragma once
+
+#include "fs_internal.cuh"
+
+namespace fs {
+
+static inline unsigned nblk2(int64_t n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
+
+template <int NN>
+__device__ __forceinline__ void load_elem(const MeshDev &m, int64_t r, ElemIn<NN> &in)
+{
+    for (int a = 0; a < NN; a++) {
+        int node = m.conn[r * NN + a];
+        for (int c = 0; c < 3; c++) {
+            in.X[a][c] = m.xyz[(int64_t)c * m.nnodes + node];
+            in.nrm[a][c] = m.normals[(int64_t)c * m.nnodes + node];
+        }
+        in.valid[a] = m.valid[node] != 0;
+    }
+    in.t = m.thick ? m.thick[r] : 0.0;
+    in.group = m.group ? m.group[r] : 0;
+}
+
+// 36 contiguous values of a 6x6 block (16-byte aligned) as 16-byte stores;
+// `transpose` writes acc^T.
+template <class R>
+__device__ __forceinline__ void store_block(R *o, const R (&acc)[6][6], bool transpose)
+{
+    constexpr int V = 16 / sizeof(R);
+    R buf[36];
+#pragma unroll
+    for (int i = 0; i < 6; i++)
+#pragma unroll
+        for (int j = 0; j < 6; j++) buf[i * 6 + j] = transpose ? acc[j][i] : acc[i][j];
+    if (V == 4) {
+        float4 *o4 = reinterpret_cast<float4 *>(o);
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+            o4[q] = make_float4((float)buf[4 * q], (float)buf[4 * q + 1], (float)buf[4 * q + 2], (float)buf[4 * q + 3]);
+    } else {
+        double2 *o2 = reinterpret_cast<double2 *>(o);
+#pragma unroll
+        for (int q = 0; q < 18; q++) o2[q] = make_double2((double)buf[2 * q], (double)buf[2 * q + 1]);
+    }
+}
+
+// One step of an error-free dot product (Ogita, Rump and Oishi's Dot2):
+// the product a*b is split exactly with an FMA and added to (s, c) by
+// TwoSum.  The _rn intrinsics are never contracted or reassociated.
+__device__ __forceinline__ void dot2_step(float &s, float &c, float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    const float pl = __fmaf_rn(a, b, -p);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    c = __fadd_rn(c, __fadd_rn(e, pl));
+    s = t;
+}
+
+// 36 entries (s + c) of a compensated block as float pairs (hi, lo), hi the
+// rounded sum and lo its error (Fast2Sum), with 16-byte stores
+__device__ __forceinline__ void store_block_pair(float2 *o, const float (&s)[6][6], const float (&c)[6][6])
+{
+    float4 *o4 = reinterpret_cast<float4 *>(o);
+#pragma unroll
+    for (int q = 0; q < 18; q++) {
+        float h[2], l[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int i = (2 * q + u) / 6, j = (2 * q + u) % 6;
+            h[u] = __fadd_rn(s[i][j], c[i][j]);
+            l[u] = __fsub_rn(c[i][j], __fsub_rn(h[u], s[i][j]));
+        }
+        o4[q] = make_float4(h[0], l[0], h[1], l[1]);
+    }
+}
+
+// Upper node blocks of K = sum_rho row_rho row_rho^T.  Storage S: the row
+// type R itself, or float2 pairs for float rows accumulated error-free
+// (FS_MIXED_COMP).
+template <class R, class S, int NN>
+__device__ __forceinline__ void write_blocks(const R *rows, int nrows, S *out)
+{
+    const int ND = 6 * NN;
+    if constexpr (sizeof(S) == 8 && sizeof(R) == 4) {
+        for (int a = 0; a < NN; a++)
+            for (int b = a; b < NN; b++) {
+                float hs[6][6], cs[6][6];
+#pragma unroll
+                for (int i = 0; i < 6; i++)
+#pragma unroll
+                    for (int j = 0; j < 6; j++) hs[i][j] = cs[i][j] = 0.f;
+                for (int rho = 0; rho < nrows; rho++) {
+                    const R *rr = rows + rho * ND;
+                    float ra[6], rb[6];
+#pragma unroll
+                    for (int i = 0; i < 6; i++) {
+                        ra[i] = rr[6 * a + i];
+                        rb[i] = rr[6 * b + i];
+                    }
+#pragma unroll
+                    for (int i = 0; i < 6; i++)
+#pragma unroll
+                        for (int j = 0; j < 6; j++) dot2_step(hs[i][j], cs[i][j], ra[i], rb[j]);
+                }
+                store_block_pair(reinterpret_cast<float2 *>(out) + ub(a, b, NN) * 36, hs, cs);
+            }
+        return;
+    }
+    for (int a = 0; a < NN; a++)
+        for (int b = a; b < NN; b++) {
+            R acc[6][6];
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+#pragma unroll
+                for (int j = 0; j < 6; j++) acc[i][j] = 0;
+            for (int rho = 0; rho < nrows; rho++) {
+                const R *rr = rows + rho * ND;
+                R ra[6], rb[6];
+#pragma unroll
+                for (int i = 0; i < 6; i++) {
+                    ra[i] = rr[6 * a + i];
+                    rb[i] = rr[6 * b + i];
+                }
+#pragma unroll
+                for (int i = 0; i < 6; i++)
+#pragma unroll
+                    for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
+            }
+            store_block<R>(reinterpret_cast<R *>(out) + ub(a, b, NN) * 36, acc, false);
+        }
+}
+
+}  // namespace fs

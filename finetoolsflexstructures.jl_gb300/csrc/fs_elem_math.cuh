@@ -135,6 +135,39 @@ FS_HD void nodal_triad(const double e[3][3], const double n[3], bool valid, doub
     R[2][0] = -s * a1;           R[2][1] = s * a0;            R[2][2] = 1.0 - c * x;
 }
 
+// The triad in the working precision: the double-precision entries of
+// nodal_triad rounded to R.  The matrix has six distinct values up to sign,
+// so only those are rounded (the result equals rounding all nine).
+template <class R>
+FS_HD void nodal_triad_r(const double e[3][3], const double n[3], bool valid, R Ar[3][3])
+{
+    if constexpr (sizeof(R) == 8) {
+        double A[3][3];
+        nodal_triad(e, n, valid, A);
+        for (int r = 0; r < 3; r++)
+            for (int k = 0; k < 3; k++) Ar[r][k] = A[r][k];
+    } else {
+        double a0 = 0.0, a1 = 0.0;
+        if (valid) {
+            a0 = -dot3(e[1], n);
+            a1 = dot3(e[0], n);
+        }
+        const double x = a0 * a0 + a1 * a1;
+        if (!(x > 1.0e-24)) {
+            for (int r = 0; r < 3; r++)
+                for (int k = 0; k < 3; k++) Ar[r][k] = r == k ? (R)1 : (R)0;
+            return;
+        }
+        double s, c;
+        sinc_cosc(x, s, c);
+        const R d0 = (R)(1.0 - c * a1 * a1), d1 = (R)(1.0 - c * a0 * a0), d2 = (R)(1.0 - c * x);
+        const R o = (R)(c * a0 * a1), s1 = (R)(s * a1), s0 = (R)(s * a0);
+        Ar[0][0] = d0; Ar[0][1] = o;  Ar[0][2] = s1;
+        Ar[1][0] = o;  Ar[1][1] = d1; Ar[1][2] = -s0;
+        Ar[2][0] = -s1; Ar[2][1] = s0; Ar[2][2] = d2;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Mapping of element-frame strain rows to global dofs
 // ---------------------------------------------------------------------------
@@ -149,18 +182,15 @@ template <class R, int NN> struct GlobalMap {
     R g[NN][2];     // basis function gradients on the element basis
 };
 
-// Build the map from the double-precision frame and triads (the products
-// below are transformation arithmetic and run in the working precision).
+// Build the map from the double-precision frame and the triads (rounded to
+// R; the products below are transformation arithmetic in the working precision).
 template <class R, int NN>
-FS_HD void build_map(const double e[3][3], const double A[NN][3][3], const R g[NN][2],
-                     GlobalMap<R, NN> &M)
+FS_HD void build_map(const double e[3][3], const R A[NN][3][3], const R g[NN][2], GlobalMap<R, NN> &M)
 {
     for (int k = 0; k < 3; k++)
         for (int c = 0; c < 3; c++) M.e[k][c] = (R)e[k][c];
     for (int i = 0; i < NN; i++) {
-        R Ar[3][3];
-        for (int r = 0; r < 3; r++)
-            for (int k = 0; k < 3; k++) Ar[r][k] = (R)A[i][r][k];
+        const R(&Ar)[3][3] = A[i];
         for (int k = 0; k < 3; k++)
             for (int c = 0; c < 3; c++)
                 M.t[i][k][c] = Ar[0][k] * M.e[0][c] + Ar[1][k] * M.e[1][c] + Ar[2][k] * M.e[2][c];
@@ -272,8 +302,20 @@ struct MatConst {
     double Lt[3];     // Cholesky factor of (5/6) Dt, lower packed (L00,L10,L11)
     double stab_c;    // stab_fun(t,h) = t^2/(t^2 + stab_c h^2)
     double drill_scale;
+    double drill_scale6;  // drill_scale / 6
     double rho;
 };
+
+// Drilling stiffness from the sum of the six nodal-basis bending diagonals:
+// mean times scale, src/FEMMShellT3FFModule.jl:713-727, in double.  The FP64
+// path keeps the reference's order (sum / 6 * scale); the mixed path, whose
+// sum is a float, multiplies by scale / 6 (no double division).
+template <class R>
+FS_HD double drill_mean(double ksum, const MatConst &mc)
+{
+    if constexpr (sizeof(R) == 8) return ksum / 6.0 * mc.drill_scale;
+    return ksum * mc.drill_scale6;
+}
 
 // Layup group (host precomputed from the laminate A,B,D,H): Cholesky factor
 // of the 6x6 [A B; B D] (lower packed, 21) and of H (lower packed, 3).
@@ -397,14 +439,22 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
     double cc = dot3(J1, e[0]), d = dot3(J1, e[1]);
     double Jd = a * d - b * cc;
     double Ae = Jd / 2;
-    double iJ = 1.0 / Jd;
     R g[3][2];
-    g[0][0] = (R)((b - d) * iJ); g[1][0] = (R)(d * iJ); g[2][0] = (R)(-b * iJ);
-    g[0][1] = (R)((cc - a) * iJ); g[1][1] = (R)(-cc * iJ); g[2][1] = (R)(a * iJ);
+    if constexpr (sizeof(R) == 8) {
+        double iJ = 1.0 / Jd;
+        g[0][0] = (b - d) * iJ; g[1][0] = d * iJ; g[2][0] = -b * iJ;
+        g[0][1] = (cc - a) * iJ; g[1][1] = -cc * iJ; g[2][1] = a * iJ;
+    } else {
+        // basis gradients in the working precision from the double-precision
+        // element coordinates (differences taken in double)
+        const R iJ = (R)1 / (R)Jd;
+        g[0][0] = (R)(b - d) * iJ; g[1][0] = (R)d * iJ; g[2][0] = -(R)b * iJ;
+        g[0][1] = (R)(cc - a) * iJ; g[1][1] = -(R)cc * iJ; g[2][1] = (R)a * iJ;
+    }
     double t = COMP ? gc->thickness : in.t;
-    // --- triads (double) ---
-    double A[3][3][3];
-    for (int i = 0; i < 3; i++) nodal_triad(e, in.nrm[i], in.valid[i], A[i]);
+    // --- triads (rotation in double, rounded to R) ---
+    R A[3][3][3];
+    for (int i = 0; i < 3; i++) nodal_triad_r<R>(e, in.nrm[i], in.valid[i], A[i]);
     GlobalMap<R, 3> M;
     build_map<R, 3>(e, A, g, M);
 
@@ -482,7 +532,7 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
                     R v = mixed[r][i][3] * M.R2[i][0][cl] + mixed[r][i][4] * M.R2[i][1][cl];
                     ksumr += v * v;
                 }
-        double kavg = (double)ksumr / 6.0 * mc.drill_scale;
+        double kavg = drill_mean<R>((double)ksumr, mc);
         R sk = kavg > 0.0 ? sqrt((R)kavg) : (R)0;
         for (int i = 0; i < 3; i++) {
             R *o = rows + (6 + NS + i) * rs;
@@ -501,7 +551,7 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
                 R v = rtx[r][i] * M.R2[i][0][cl] + rty[r][i] * M.R2[i][1][cl];
                 ksumr += v * v;
             }
-    double kavg = (double)ksumr / 6.0 * mc.drill_scale;
+    double kavg = drill_mean<R>((double)ksumr, mc);
     R sk = kavg > 0.0 ? sqrt((R)kavg) : (R)0;
     for (int i = 0; i < 3; i++) {
         R *o = rows + (6 + NS + i) * rs;
@@ -640,8 +690,8 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         g[a][0] = pj0[0] * t1 + pj1[0] * t2;
         g[a][1] = pj0[1] * t1 + pj1[1] * t2;
     }
-    double A[4][3][3];
-    for (int i = 0; i < 4; i++) nodal_triad(e, in.nrm[i], in.valid[i], A[i]);
+    R A[4][3][3];
+    for (int i = 0; i < 4; i++) nodal_triad_r<R>(e, in.nrm[i], in.valid[i], A[i]);
     GlobalMap<R, 4> M;
     build_map<R, 4>(e, A, g, M);
     R sh[2][4][5];

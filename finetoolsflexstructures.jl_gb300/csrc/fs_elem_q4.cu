@@ -1,0 +1,136 @@
+// Q4RS / Q4RSComp element kernel: four lanes per element, one per Gauss
+// point (the element math is csrc/fs_elem_math.cuh).
+#include "fs_elem_common.cuh"
+
+namespace fs {
+
+template <class R, bool COMP, int EPB, class S>
+__global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
+{
+    constexpr int NR = 36, ND = 24, STRIDE = NR * ND + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int el = threadIdx.x >> 2, qp = threadIdx.x & 3;
+    R *rows = reinterpret_cast<R *>(smem_raw) + el * STRIDE;
+    int64_t r = (int64_t)blockIdx.x * EPB + el;
+    const bool active = r < m.nelem;
+    ElemIn<4> in;
+    double tr[4] = {0, 0, 0, 0};
+    // element constants computed once per element (by its first lane) and
+    // shared with the other three lanes
+    Q4Elem qe;
+    if (active) {
+        load_elem<4>(m, r, in);
+        if (qp == 0) q4_prepare(in, qe);
+    }
+    {
+        const int src = (threadIdx.x & 31) & ~3;
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) qe.Xr[a][c] = __shfl_sync(0xffffffffu, qe.Xr[a][c], src);
+        qe.h2 = __shfl_sync(0xffffffffu, qe.h2, src);
+    }
+    if (active) {
+        const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
+        int st = q4_point_rows<R, COMP>(in, qe, qp, mc, gc, rows + qp * 8 * ND, ND, tr);
+        if (st) {
+            atomicOr(status, DEV_SINGULAR);
+            for (int k = 0; k < 4; k++) tr[k] = 0.0;
+        }
+    }
+    // sum the drilling traces of the four quadrature points (lanes 4el..4el+3)
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], 1);
+        tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], 2);
+    }
+    if (active && qp == 0) q4_drill_rows<R>(in, tr, mc.drill_scale, rows + 32 * ND, ND);
+    __syncwarp();
+    if (!active) return;
+    S *out = ke + r * (10 * 36);
+    // ten upper node blocks shared by the four lanes of the element
+    for (int bi = qp; bi < 10; bi += 4) {
+        int a = bi < 4 ? 0 : (bi < 7 ? 1 : (bi < 9 ? 2 : 3));
+        int b = a + (bi - (a == 0 ? 0 : (a == 1 ? 4 : (a == 2 ? 7 : 9))));
+        if constexpr (sizeof(S) == 8 && sizeof(R) == 4) {
+            float hs[6][6], cs[6][6];
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+#pragma unroll
+                for (int j = 0; j < 6; j++) hs[i][j] = cs[i][j] = 0.f;
+            for (int rho = 0; rho < NR; rho++) {
+                const R *rr = rows + rho * ND;
+                float ra[6], rb[6];
+#pragma unroll
+                for (int i = 0; i < 6; i++) {
+                    ra[i] = rr[6 * a + i];
+                    rb[i] = rr[6 * b + i];
+                }
+#pragma unroll
+                for (int i = 0; i < 6; i++)
+#pragma unroll
+                    for (int j = 0; j < 6; j++) dot2_step(hs[i][j], cs[i][j], ra[i], rb[j]);
+            }
+            store_block_pair(reinterpret_cast<float2 *>(out) + ub(a, b, 4) * 36, hs, cs);
+            continue;
+        }
+        R acc[6][6];
+#pragma unroll
+        for (int i = 0; i < 6; i++)
+#pragma unroll
+            for (int j = 0; j < 6; j++) acc[i][j] = 0;
+        for (int rho = 0; rho < NR; rho++) {
+            const R *rr = rows + rho * ND;
+            R ra[6], rb[6];
+#pragma unroll
+            for (int i = 0; i < 6; i++) {
+                ra[i] = rr[6 * a + i];
+                rb[i] = rr[6 * b + i];
+            }
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+#pragma unroll
+                for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
+        }
+        store_block<R>(reinterpret_cast<R *>(out) + ub(a, b, 4) * 36, acc, false);
+    }
+}
+
+template <class R, class S, bool COMP, int EPB>
+static int run_q4_epb(fs_ctx *c, S *ke)
+{
+    const size_t smem = q4_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, EPB);
+    auto kern = k_q4_elements<R, COMP, EPB, S>;
+    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<nblk2(c->mesh.nelem, EPB), EPB * 4, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+template <class R, bool COMP, class S = R>
+static int run_q4(fs_ctx *c, S *ke)
+{
+    int epb = c->tune.elem_epb;
+    if (epb <= 0) epb = 32;
+    if (epb == 16) return run_q4_epb<R, S, COMP, 16>(c, ke);
+    if (epb == 64 && sizeof(R) == 4) return run_q4_epb<R, S, COMP, 64>(c, ke);
+    return run_q4_epb<R, S, COMP, 32>(c, ke);
+}
+
+// every Q4 variant: row precision, storage, layered
+int run_q4_any(fs_ctx *c, int precision, void *ke)
+{
+    const bool comp = c->mesh.etype == FS_Q4RSCOMP;
+    if (precision == FS_FP64) {
+        double *k = (double *)ke;
+        return comp ? run_q4<double, true>(c, k) : run_q4<double, false>(c, k);
+    }
+    if (precision == FS_MIXED_COMP) {
+        float2 *k = (float2 *)ke;
+        return comp ? run_q4<float, true>(c, k) : run_q4<float, false>(c, k);
+    }
+    float *k = (float *)ke;
+    return comp ? run_q4<float, true>(c, k) : run_q4<float, false>(c, k);
+}
+
+}  // namespace fs

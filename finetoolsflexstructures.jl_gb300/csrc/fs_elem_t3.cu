@@ -1,0 +1,66 @@
+// T3FF / T3FFComp element kernel: one thread per element (the element
+// math is csrc/fs_elem_math.cuh, the block stores csrc/fs_elem_common.cuh).
+#include "fs_elem_common.cuh"
+
+namespace fs {
+
+template <class R, bool COMP, bool AVGK, int EPB, class S>
+__global__ void __launch_bounds__(EPB) k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
+{
+    constexpr int NR = T3Rows<AVGK>::N;
+    constexpr int ND = 18;
+    constexpr int STRIDE = NR * ND + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *rows = reinterpret_cast<R *>(smem_raw) + threadIdx.x * STRIDE;
+    int64_t r = (int64_t)blockIdx.x * EPB + threadIdx.x;
+    if (r >= m.nelem) return;
+    ElemIn<3> in;
+    load_elem<3>(m, r, in);
+    const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
+    int st = t3_rows<R, COMP, AVGK>(in, mc, gc, rows, ND);
+    if (st) atomicOr(status, DEV_NEG_DRILL);
+    write_blocks<R, S, 3>(rows, NR, ke + r * (6 * 36));
+}
+
+template <class R, class S, bool COMP, bool AVGK, int EPB>
+static int run_t3_epb(fs_ctx *c, S *ke)
+{
+    const size_t smem = t3_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, AVGK, EPB);
+    auto kern = k_t3_elements<R, COMP, AVGK, EPB, S>;
+    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<nblk2(c->mesh.nelem, EPB), EPB, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+template <class R, bool COMP, bool AVGK, class S = R>
+static int run_t3(fs_ctx *c, S *ke)
+{
+    int epb = c->tune.elem_epb;
+    if (epb <= 0) epb = (sizeof(R) == 8 && AVGK) ? 64 : 128;
+    if (epb == 32) return run_t3_epb<R, S, COMP, AVGK, 32>(c, ke);
+    if (epb == 64 || (sizeof(R) == 8 && AVGK)) return run_t3_epb<R, S, COMP, AVGK, 64>(c, ke);
+    return run_t3_epb<R, S, COMP, AVGK, 128>(c, ke);
+}
+
+// every T3 variant: row precision, storage, layered, average-K
+int run_t3_any(fs_ctx *c, int precision, void *ke)
+{
+    const bool comp = c->mesh.etype == FS_T3FFCOMP;
+    const bool avgk = c->params.transv_shear_formulation == 1;
+    if (precision == FS_FP64) {
+        double *k = (double *)ke;
+        if (comp) return avgk ? run_t3<double, true, true>(c, k) : run_t3<double, true, false>(c, k);
+        return avgk ? run_t3<double, false, true>(c, k) : run_t3<double, false, false>(c, k);
+    }
+    if (precision == FS_MIXED_COMP) {
+        float2 *k = (float2 *)ke;
+        if (comp) return avgk ? run_t3<float, true, true>(c, k) : run_t3<float, true, false>(c, k);
+        return avgk ? run_t3<float, false, true>(c, k) : run_t3<float, false, false>(c, k);
+    }
+    float *k = (float *)ke;
+    if (comp) return avgk ? run_t3<float, true, true>(c, k) : run_t3<float, true, false>(c, k);
+    return avgk ? run_t3<float, false, true>(c, k) : run_t3<float, false, false>(c, k);
+}
+
+}  // namespace fs

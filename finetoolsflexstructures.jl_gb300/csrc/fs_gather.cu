@@ -1,0 +1,311 @@
+// CSR value gather (see the description below).
+#include "fs_elem_common.cuh"
+
+namespace fs {
+
+// ---------------------------------------------------------------------------
+// gather into CSR values
+// ---------------------------------------------------------------------------
+// One warp per node.  The node's element slabs are staged into shared memory
+// with independent coalesced loads, a few pairs at a time; each lane then
+// owns whole row positions j (all six rows of the node) and adds the staged
+// contributions of the pairs in ascending assembly rank.  In double
+// (FS_FP64) the sum is a plain double accumulation.  For float element
+// matrices (FS_MIXED) the sum is carried error-free as an unevaluated pair
+// of floats (TwoSum), then rounded once to double: on GB300, where a double
+// add costs as much as 64 float operations, this keeps one double add per
+// stored value instead of a conversion and an add per contribution, with an
+// error below 2^-46 of the largest contribution.  Rows longer than
+// 32 * G_COLS positions fall back to accumulating in place in double.
+static const int G_MAXP = 8;
+
+// 16-byte asynchronous global -> shared copy (bypassing registers and L1)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// exact float -> double built from the bit pattern with integer operations
+// only (zeros, subnormals, normals, inf and nan), so that no conversion
+// lands on the double-precision pipe
+__device__ __forceinline__ double f2d_exact(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t sign = u & 0x80000000u, a = u & 0x7fffffffu;
+    uint32_t ex = a >> 23, man = a & 0x7fffffu;
+    uint32_t dexp;
+    if (ex == 0xffu) {
+        dexp = 0x7ffu;                                   // inf / nan
+    } else if (ex != 0u) {
+        dexp = ex + (1023u - 127u);                      // normal
+    } else if (man != 0u) {
+        const uint32_t sh = (uint32_t)__clz((int)man) - 8u;  // subnormal: normalise
+        man = (man << sh) & 0x7fffffu;
+        dexp = 1023u - 126u - sh;
+    } else {
+        dexp = 0u;                                       // signed zero
+    }
+    return __hiloint2double((int)(sign | (dexp << 20) | (man >> 3)), (int)(man << 29));
+}
+
+// exact float -> double for normal numbers and zeros from the bit pattern
+// (rebias the exponent, move the mantissa); other values take f2d_exact
+__device__ __forceinline__ double f2d_fast(float f)
+{
+    const uint32_t u = __float_as_uint(f), a = u & 0x7fffffffu;
+    if (a != 0u && a - 0x00800000u >= 0x7f000000u) return f2d_exact(f);  // subnormal, inf, nan
+    const uint32_t h = (u & 0x80000000u) | (a != 0u ? (a >> 3) + 0x38000000u : 0u);
+    return __hiloint2double((int)h, (int)(u << 29));
+}
+
+// Accumulation of one stored contribution into a value's accumulator:
+// double entries by double addition; float entries (and both halves of a
+// float pair) error-free into an unevaluated float pair (TwoSum).
+template <class S> struct GatherAcc { typedef float T; };
+template <> struct GatherAcc<double> { typedef double T; };
+
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float v)
+{
+    const float t = hi + v;
+    const float bp = t - hi;
+    lo += (hi - (t - bp)) + (v - bp);
+    hi = t;
+}
+__device__ __forceinline__ void gather_add(float &hi, float &lo, float v) { two_sum_acc(hi, lo, v); }
+__device__ __forceinline__ void gather_add(float &hi, float &lo, float2 v)
+{
+    two_sum_acc(hi, lo, v.x);
+    two_sum_acc(hi, lo, v.y);
+}
+__device__ __forceinline__ void gather_add(double &hi, double &, double v) { hi += v; }
+__device__ __forceinline__ double entry_value(float v) { return (double)v; }
+__device__ __forceinline__ double entry_value(double v) { return v; }
+__device__ __forceinline__ double entry_value(float2 v) { return (double)v.x + (double)v.y; }
+
+// shared memory of one warp: G_MAXP staged slabs, then the node's
+// contribution entries (at most 64 pairs x 4 element nodes)
+template <class R, int NEN> struct GatherSmem {
+    static constexpr int PER_WARP = G_MAXP * NEN * 36 * (int)sizeof(R) + 512;
+};
+
+template <class R, int NEN, int G_COLS, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
+{
+    typedef typename GatherAcc<R>::T A;
+    constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
+    constexpr bool SINGLE = sizeof(A) == 4;
+    constexpr int BCH = 36 * (int)sizeof(R) / 16;  // 16-byte chunks per 6x6 block
+    constexpr int CH = NEN * BCH;                   // 16-byte chunks per slab
+    constexpr int CPL = (CH + 31) / 32;             // chunks per lane per pair
+    extern __shared__ __align__(16) unsigned char gather_smem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t r = (int64_t)blockIdx.x * WARPS + w;
+    if (r >= m.nnodes) return;
+    unsigned char *wsm = gather_smem + (size_t)w * GatherSmem<R, NEN>::PER_WARP;
+    R *stage = reinterpret_cast<R *>(wsm);
+    uint16_t *sent = reinterpret_cast<uint16_t *>(wsm + G_MAXP * SLAB * sizeof(R));
+    int32_t d[6];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        d[k] = m.dof[(int64_t)k * m.nnodes + r];
+        any |= (d[k] <= n);
+    }
+    if (!any) return;
+    const int L = P.rowlen[r];
+    const int64_t off = P.nbr_off[r], off6 = off * 6;
+    const int64_t pb = m.pp[r], pe = m.pp[r + 1];
+    if (L <= 32 * G_COLS) {
+        // the node's contribution entries into shared memory
+        const int ntot = (int)(pe - pb) * NEN;
+        const uint16_t *ent = P.sl_ent + pb * NEN;
+        for (int i = lane; i < ntot; i += 32) sent[i] = ent[i];
+        // the lane's columns and the range of entries of their neighbour slot
+        const int nslots = (int)(P.nbr_off[r + 1] - off);
+        int kcol[G_COLS], cur[G_COLS], last[G_COLS];
+        A hi[G_COLS][6], lo[G_COLS][6];
+#pragma unroll
+        for (int c = 0; c < G_COLS; c++) {
+            const int j = lane + 32 * c;
+            kcol[c] = 0;
+            cur[c] = 0;
+            last[c] = 0;
+            if (j < L) {
+                const int cs = (int)P.colsrc[off6 + j];
+                const int sl = cs / 6;
+                kcol[c] = cs - 6 * sl;
+                cur[c] = (int)P.sl_off[off + sl];
+                last[c] = sl + 1 < nslots ? (int)P.sl_off[off + sl + 1] : ntot;
+            }
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                hi[c][k] = 0;
+                lo[c][k] = 0;
+            }
+        }
+        // lane-fixed staging chunks: chunk lane + 32 t of every slab
+        int cb[CPL], cwd[CPL];
+#pragma unroll
+        for (int t = 0; t < CPL; t++) {
+            const int ch = lane + 32 * t;
+            cb[t] = ch / BCH;
+            cwd[t] = ch - cb[t] * BCH;
+        }
+        for (int64_t p0 = pb; p0 < pe; p0 += G_MAXP) {
+            const int cnt = (int)min((int64_t)G_MAXP, pe - p0);
+            const int q0 = (int)(p0 - pb);
+            for (int q = 0; q < cnt; q++) {
+                const int32_t pel = m.pair_e[p0 + q];
+                const int a = pel & 3;
+                const R *base = ke + (int64_t)(pel >> 2) * ND2;
+#pragma unroll
+                for (int t = 0; t < CPL; t++) {
+                    if (lane + 32 * t < CH) {
+                        const int bb = cb[t];
+                        // block (a, bb) of the element: stored as itself or as its mirror
+                        const R *src = base + ub(min(a, bb), max(a, bb), NEN) * 36;
+                        cp_async16(reinterpret_cast<char *>(stage + q * SLAB + bb * 36) + 16 * cwd[t],
+                                   reinterpret_cast<const char *>(src) + 16 * cwd[t]);
+                    }
+                }
+            }
+            cp_async_wait_all();
+            __syncwarp();
+            // this batch's contributions to the lane's columns, ascending pair order
+#pragma unroll
+            for (int c = 0; c < G_COLS; c++) {
+                while (cur[c] < last[c]) {
+                    const uint32_t e = sent[cur[c]];
+                    const int q = (int)(e & 63u) - q0;
+                    if (q >= cnt) break;
+                    const int b = (int)((e >> 6) & 3u);
+                    // entry (krow, kcol) of block (a_q, b); a mirrored block is read transposed
+                    const bool tr = (e >> 8) & 1u;
+                    const R *src = stage + q * SLAB + b * 36 + (tr ? 6 * kcol[c] : kcol[c]);
+                    const int st = tr ? 1 : 6;
+#pragma unroll
+                    for (int k = 0; k < 6; k++) gather_add(hi[c][k], lo[c][k], src[st * k]);
+                    cur[c]++;
+                }
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            if (d[k] > n) continue;
+            double *o = vals + P.rowptr[d[k] - 1];
+#pragma unroll
+            for (int c = 0; c < G_COLS; c++) {
+                const int j = lane + 32 * c;
+                if (j >= L) continue;
+                double v;
+                if (SINGLE) {
+                    // hi + lo: exact in double unless their exponents are more than
+                    // 29 apart, then rounded once
+                    v = f2d_fast((float)hi[c][k]);
+                    if (lo[c][k] != (A)0) v += f2d_fast((float)lo[c][k]);
+                } else {
+                    v = (double)hi[c][k];
+                }
+                o[j] = v;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            if (d[k] > n) continue;
+            double *o = vals + P.rowptr[d[k] - 1];
+            for (int j = lane; j < L; j += 32) o[j] = 0.0;
+        }
+        __syncwarp();
+        for (int64_t p = pb; p < pe; p++) {
+            int32_t pe_ = m.pair_e[p];
+            int64_t rank = pe_ >> 2;
+            int a = pe_ & 3;
+            uint32_t slots = P.pair_slots[p];
+            for (int idx = lane; idx < SLAB; idx += 32) {
+                int b = idx / 36, rem = idx - 36 * b, krow = rem / 6, kc = rem - 6 * krow;
+                const R *blk = ke + rank * (int64_t)ND2 + ub(min(a, b), max(a, b), NEN) * 36;
+                const R v = b < a ? blk[kc * 6 + krow] : blk[rem];
+                int s = (slots >> (8 * b)) & 0xff;
+                int cp = P.colpos[off6 + s * 6 + kc];
+                if (cp >= 0 && d[krow] <= n) {
+                    double *o = vals + P.rowptr[d[krow] - 1] + cp;
+                    *o += entry_value(v);
+                }
+            }
+            __threadfence_block();
+            __syncwarp();
+        }
+    }
+}
+
+template <class R, int NEN, int G_COLS, int W>
+static int gather_launch_w(fs_ctx *c, const R *ke, double *vals)
+{
+    const MeshDev &m = c->mesh;
+    const size_t smem = (size_t)W * GatherSmem<R, NEN>::PER_WARP;
+    auto kern = k_gather<R, NEN, G_COLS, W>;
+    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
+    return FS_OK;
+}
+
+template <class R, int NEN, int G_COLS>
+static int gather_launch_c(fs_ctx *c, const R *ke, double *vals, int warps)
+{
+    if (warps == 4) return gather_launch_w<R, NEN, G_COLS, 4>(c, ke, vals);
+    if (warps == 16) return gather_launch_w<R, NEN, G_COLS, 16>(c, ke, vals);
+    return gather_launch_w<R, NEN, G_COLS, 8>(c, ke, vals);
+}
+
+template <class R, int NEN>
+static int gather_launch(fs_ctx *c, const R *ke, double *vals, int warps)
+{
+    // per-lane columns sized to the longest row (rows beyond 128 accumulate in place)
+    if (c->pat.maxlen <= 64) return gather_launch_c<R, NEN, 2>(c, ke, vals, warps);
+    return gather_launch_c<R, NEN, 4>(c, ke, vals, warps);
+}
+
+template <class R>
+static int run_gather(fs_ctx *c, const R *ke, double *vals, int warps)
+{
+    if (warps <= 0) warps = sizeof(R) == 4 ? 8 : 4;  // double and float-pair entries: 4
+    int st;
+    if (c->mesh.nen == 3)
+        st = gather_launch<R, 3>(c, ke, vals, warps);
+    else if (c->mesh.nen == 2)
+        st = gather_launch<R, 2>(c, ke, vals, warps);
+    else
+        st = gather_launch<R, 4>(c, ke, vals, warps);
+    FS_TRY(st);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
+int launch_gather(fs_ctx *c, int precision, double *vals)
+{
+    if (c->mesh.nnodes == 0) return FS_OK;
+    const int w = c->tune.gather_warps;
+    if (precision == FS_FP64) return run_gather<double>(c, (const double *)c->ke, vals, w);
+    if (precision == FS_MIXED_COMP) return run_gather<float2>(c, (const float2 *)c->ke, vals, w);
+    return run_gather<float>(c, (const float *)c->ke, vals, w);
+}
+
+// CSR values from element matrices held in `ke`; allocates nothing.
+int launch_gather_from(fs_ctx *c, int precision, const void *ke, double *vals)
+{
+    if (c->mesh.nnodes == 0) return FS_OK;
+    const int w = c->tune.gather_warps;
+    if (precision == FS_FP64) return run_gather<double>(c, (const double *)ke, vals, w);
+    if (precision == FS_MIXED_COMP) return run_gather<float2>(c, (const float2 *)ke, vals, w);
+    return run_gather<float>(c, (const float *)ke, vals, w);
+}
+
+}  // namespace fs

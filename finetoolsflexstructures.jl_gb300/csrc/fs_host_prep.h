@@ -52,6 +52,7 @@ inline int prepare_matconst(const fs_shell_params &p, MatConst &mc)
     if (chol_packed(Dt, 2, mc.Lt)) return 1;
     mc.stab_c = p.stab_c;
     mc.drill_scale = p.drilling_stiffness_scale;
+    mc.drill_scale6 = p.drilling_stiffness_scale / 6.0;
     mc.rho = p.rho;
     return 0;
 }

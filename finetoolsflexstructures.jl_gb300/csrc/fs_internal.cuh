@@ -194,6 +194,9 @@ int explicit_launch_steps(fs_ctx *c, int64_t nsteps);
 // tile-shape autotuner of the shell assembly
 int autotune_shell(fs_ctx *c, int precision);
 size_t t3_smem(int precision, bool avgk, int epb);
+size_t entry_bytes(int precision);
+int run_t3_any(fs_ctx *c, int precision, void *ke);
+int run_q4_any(fs_ctx *c, int precision, void *ke);
 size_t q4_smem(int precision, int epb);
 
 // co-rotational beams

@@ -61,7 +61,8 @@ extern "C" int fs_stiffness_values_noalloc(fs_ctx *c, int precision, int64_t nro
 {
     if (!c) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
-    if (precision != FS_FP64 && precision != FS_MIXED) return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
+    if (precision != FS_FP64 && precision != FS_MIXED && precision != FS_MIXED_COMP)
+        return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
     if (c->mesh.etype < 0 || !c->params_set || !c->dofs_ready)
         return set_err(c, FS_ERR_STATE, "mesh, parameters and dof numbering must be set first");
     if ((c->mesh.etype == FS_T3FFCOMP || c->mesh.etype == FS_Q4RSCOMP) && !c->mesh.groups)
@@ -75,7 +76,7 @@ extern "C" int fs_stiffness_values_noalloc(fs_ctx *c, int precision, int64_t nro
     if (vals_len < c->pat.nnz)
         return set_err(c, FS_ERR_BAD_INPUT, "output buffer shorter than the number of stored entries");
     const int nen = c->mesh.nen;
-    const uint64_t per = (uint64_t)n_upper_blocks(nen) * 36 * (precision == FS_FP64 ? 8 : 4);
+    const uint64_t per = (uint64_t)n_upper_blocks(nen) * 36 * entry_bytes(precision);
     const uint64_t need = per * (uint64_t)c->mesh.nelem;
     if (need > FS_NOALLOC_SCRATCH_BYTES) {
         char msg[200];

@@ -1,5 +1,6 @@
-// Numeric phase: nodal normals, element matrices, the deterministic CSR
-// value gather and the lumped mass.
+// Numeric phase: element-matrix dispatch, nodal normals, lumped mass and
+// the tile-shape autotuner.  The kernels of the element matrices are in
+// fs_elem_t3.cu and fs_elem_q4.cu, the CSR gather in fs_gather.cu.
 //
 // Element matrices.  One thread owns one T3 element (or one quadrature point
 // of a Q4 element, four lanes per element).  It writes the element's Gram
@@ -20,156 +21,9 @@
 #include <mutex>
 #include <tuple>
 
-#include "fs_internal.cuh"
+#include "fs_elem_common.cuh"
 
 namespace fs {
-
-static unsigned nblk2(int64_t n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
-
-template <int NN>
-__device__ __forceinline__ void load_elem(const MeshDev &m, int64_t r, ElemIn<NN> &in)
-{
-    for (int a = 0; a < NN; a++) {
-        int node = m.conn[r * NN + a];
-        for (int c = 0; c < 3; c++) {
-            in.X[a][c] = m.xyz[(int64_t)c * m.nnodes + node];
-            in.nrm[a][c] = m.normals[(int64_t)c * m.nnodes + node];
-        }
-        in.valid[a] = m.valid[node] != 0;
-    }
-    in.t = m.thick ? m.thick[r] : 0.0;
-    in.group = m.group ? m.group[r] : 0;
-}
-
-// ---------------------------------------------------------------------------
-// element kernels
-// ---------------------------------------------------------------------------
-// 36 contiguous values of a 6x6 block (16-byte aligned) as 16-byte stores;
-// `transpose` writes acc^T.
-template <class R>
-__device__ __forceinline__ void store_block(R *o, const R (&acc)[6][6], bool transpose)
-{
-    constexpr int V = 16 / sizeof(R);
-    R buf[36];
-#pragma unroll
-    for (int i = 0; i < 6; i++)
-#pragma unroll
-        for (int j = 0; j < 6; j++) buf[i * 6 + j] = transpose ? acc[j][i] : acc[i][j];
-    if (V == 4) {
-        float4 *o4 = reinterpret_cast<float4 *>(o);
-#pragma unroll
-        for (int q = 0; q < 9; q++)
-            o4[q] = make_float4((float)buf[4 * q], (float)buf[4 * q + 1], (float)buf[4 * q + 2], (float)buf[4 * q + 3]);
-    } else {
-        double2 *o2 = reinterpret_cast<double2 *>(o);
-#pragma unroll
-        for (int q = 0; q < 18; q++) o2[q] = make_double2((double)buf[2 * q], (double)buf[2 * q + 1]);
-    }
-}
-
-template <class R, int NN>
-__device__ __forceinline__ void write_blocks(const R *rows, int nrows, R *out)
-{
-    const int ND = 6 * NN;
-    for (int a = 0; a < NN; a++)
-        for (int b = a; b < NN; b++) {
-            R acc[6][6];
-#pragma unroll
-            for (int i = 0; i < 6; i++)
-#pragma unroll
-                for (int j = 0; j < 6; j++) acc[i][j] = 0;
-            for (int rho = 0; rho < nrows; rho++) {
-                const R *rr = rows + rho * ND;
-                R ra[6], rb[6];
-#pragma unroll
-                for (int i = 0; i < 6; i++) {
-                    ra[i] = rr[6 * a + i];
-                    rb[i] = rr[6 * b + i];
-                }
-#pragma unroll
-                for (int i = 0; i < 6; i++)
-#pragma unroll
-                    for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
-            }
-            store_block<R>(out + ub(a, b, NN) * 36, acc, false);
-        }
-}
-
-template <class R, bool COMP, bool AVGK, int EPB>
-__global__ void __launch_bounds__(EPB) k_t3_elements(const MeshDev m, const MatConst mc, R *ke, int *status)
-{
-    constexpr int NR = T3Rows<AVGK>::N;
-    constexpr int ND = 18;
-    constexpr int STRIDE = NR * ND + 1;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    R *rows = reinterpret_cast<R *>(smem_raw) + threadIdx.x * STRIDE;
-    int64_t r = (int64_t)blockIdx.x * EPB + threadIdx.x;
-    if (r >= m.nelem) return;
-    ElemIn<3> in;
-    load_elem<3>(m, r, in);
-    const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
-    int st = t3_rows<R, COMP, AVGK>(in, mc, gc, rows, ND);
-    if (st) atomicOr(status, DEV_NEG_DRILL);
-    write_blocks<R, 3>(rows, NR, ke + r * (6 * 36));
-}
-
-template <class R, bool COMP, int EPB>
-__global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const MatConst mc, R *ke, int *status)
-{
-    constexpr int NR = 36, ND = 24, STRIDE = NR * ND + 1;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int el = threadIdx.x >> 2, qp = threadIdx.x & 3;
-    R *rows = reinterpret_cast<R *>(smem_raw) + el * STRIDE;
-    int64_t r = (int64_t)blockIdx.x * EPB + el;
-    const bool active = r < m.nelem;
-    ElemIn<4> in;
-    double tr[4] = {0, 0, 0, 0};
-    if (active) {
-        load_elem<4>(m, r, in);
-        const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
-        Q4Elem qe;
-        q4_prepare(in, qe);
-        int st = q4_point_rows<R, COMP>(in, qe, qp, mc, gc, rows + qp * 8 * ND, ND, tr);
-        if (st) {
-            atomicOr(status, DEV_SINGULAR);
-            for (int k = 0; k < 4; k++) tr[k] = 0.0;
-        }
-    }
-    // sum the drilling traces of the four quadrature points (lanes 4el..4el+3)
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], 1);
-        tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], 2);
-    }
-    if (active && qp == 0) q4_drill_rows<R>(in, tr, mc.drill_scale, rows + 32 * ND, ND);
-    __syncwarp();
-    if (!active) return;
-    R *out = ke + r * (10 * 36);
-    // ten upper node blocks shared by the four lanes of the element
-    for (int bi = qp; bi < 10; bi += 4) {
-        int a = bi < 4 ? 0 : (bi < 7 ? 1 : (bi < 9 ? 2 : 3));
-        int b = a + (bi - (a == 0 ? 0 : (a == 1 ? 4 : (a == 2 ? 7 : 9))));
-        R acc[6][6];
-#pragma unroll
-        for (int i = 0; i < 6; i++)
-#pragma unroll
-            for (int j = 0; j < 6; j++) acc[i][j] = 0;
-        for (int rho = 0; rho < NR; rho++) {
-            const R *rr = rows + rho * ND;
-            R ra[6], rb[6];
-#pragma unroll
-            for (int i = 0; i < 6; i++) {
-                ra[i] = rr[6 * a + i];
-                rb[i] = rr[6 * b + i];
-            }
-#pragma unroll
-            for (int i = 0; i < 6; i++)
-#pragma unroll
-                for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
-        }
-        store_block<R>(out + ub(a, b, 4) * 36, acc, false);
-    }
-}
 
 // Shared memory of one block of the element kernels (per-element Gram rows).
 size_t t3_smem(int precision, bool avgk, int epb)
@@ -179,52 +33,19 @@ size_t t3_smem(int precision, bool avgk, int epb)
 }
 size_t q4_smem(int precision, int epb) { return (precision == FS_FP64 ? 8 : 4) * (size_t)epb * (36 * 24 + 1); }
 
-template <class R, bool COMP, bool AVGK, int EPB>
-static int run_t3_epb(fs_ctx *c, R *ke)
+// element kernels of one precision into `ke` (the layout of the element buffer)
+static int run_elements(fs_ctx *c, int precision, void *ke)
 {
-    const size_t smem = t3_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, AVGK, EPB);
-    auto kern = k_t3_elements<R, COMP, AVGK, EPB>;
-    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<nblk2(c->mesh.nelem, EPB), EPB, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
-    FS_CUDA(c, cudaGetLastError());
-    return FS_OK;
+    return c->mesh.nen == 3 ? run_t3_any(c, precision, ke) : run_q4_any(c, precision, ke);
 }
 
-template <class R, bool COMP, bool AVGK>
-static int run_t3(fs_ctx *c, R *ke)
-{
-    int epb = c->tune.elem_epb;
-    if (epb <= 0) epb = (sizeof(R) == 8 && AVGK) ? 64 : 128;
-    if (epb == 32) return run_t3_epb<R, COMP, AVGK, 32>(c, ke);
-    if (epb == 64 || (sizeof(R) == 8 && AVGK)) return run_t3_epb<R, COMP, AVGK, 64>(c, ke);
-    return run_t3_epb<R, COMP, AVGK, 128>(c, ke);
-}
-
-template <class R, bool COMP, int EPB>
-static int run_q4_epb(fs_ctx *c, R *ke)
-{
-    const size_t smem = q4_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, EPB);
-    auto kern = k_q4_elements<R, COMP, EPB>;
-    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<nblk2(c->mesh.nelem, EPB), EPB * 4, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
-    FS_CUDA(c, cudaGetLastError());
-    return FS_OK;
-}
-
-template <class R, bool COMP>
-static int run_q4(fs_ctx *c, R *ke)
-{
-    int epb = c->tune.elem_epb;
-    if (epb <= 0) epb = 32;
-    if (epb == 16) return run_q4_epb<R, COMP, 16>(c, ke);
-    if (epb == 64 && sizeof(R) == 4) return run_q4_epb<R, COMP, 64>(c, ke);
-    return run_q4_epb<R, COMP, 32>(c, ke);
-}
+// bytes of one stored element-matrix entry
+size_t entry_bytes(int precision) { return precision == FS_MIXED ? 4 : 8; }
 
 int launch_elements(fs_ctx *c, int precision)
 {
     MeshDev &m = c->mesh;
-    size_t bytes = (size_t)m.nelem * n_upper_blocks(m.nen) * 36 * (precision == FS_FP64 ? 8 : 4);
+    size_t bytes = (size_t)m.nelem * n_upper_blocks(m.nen) * 36 * entry_bytes(precision);
     if (bytes > c->ke_bytes) {
         if (c->ke) cudaFree(c->ke);
         c->ke = nullptr;
@@ -237,303 +58,7 @@ int launch_elements(fs_ctx *c, int precision)
         c->ke_bytes = bytes;
     }
     if (m.nelem == 0) return FS_OK;
-    bool comp = (m.etype == FS_T3FFCOMP || m.etype == FS_Q4RSCOMP);
-    bool avgk = c->params.transv_shear_formulation == 1;
-    if (m.nen == 3) {
-        if (precision == FS_FP64) {
-            double *k = (double *)c->ke;
-            if (comp) return avgk ? run_t3<double, true, true>(c, k) : run_t3<double, true, false>(c, k);
-            return avgk ? run_t3<double, false, true>(c, k) : run_t3<double, false, false>(c, k);
-        }
-        float *k = (float *)c->ke;
-        if (comp) return avgk ? run_t3<float, true, true>(c, k) : run_t3<float, true, false>(c, k);
-        return avgk ? run_t3<float, false, true>(c, k) : run_t3<float, false, false>(c, k);
-    }
-    if (precision == FS_FP64) {
-        double *k = (double *)c->ke;
-        return comp ? run_q4<double, true>(c, k) : run_q4<double, false>(c, k);
-    }
-    float *k = (float *)c->ke;
-    return comp ? run_q4<float, true>(c, k) : run_q4<float, false>(c, k);
-}
-
-// ---------------------------------------------------------------------------
-// gather into CSR values
-// ---------------------------------------------------------------------------
-// One warp per node.  The node's element slabs are staged into shared memory
-// with independent coalesced loads, a few pairs at a time; each lane then
-// owns whole row positions j (all six rows of the node) and adds the staged
-// contributions of the pairs in ascending assembly rank.  In double
-// (FS_FP64) the sum is a plain double accumulation.  For float element
-// matrices (FS_MIXED) the sum is carried error-free as an unevaluated pair
-// of floats (TwoSum), then rounded once to double: on GB300, where a double
-// add costs as much as 64 float operations, this keeps one double add per
-// stored value instead of a conversion and an add per contribution, with an
-// error below 2^-46 of the largest contribution.  Rows longer than
-// 32 * G_COLS positions fall back to accumulating in place in double.
-static const int G_MAXP = 8;
-
-// 16-byte asynchronous global -> shared copy (bypassing registers and L1)
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all()
-{
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-}
-
-// exact float -> double built from the bit pattern with integer operations
-// only (zeros, subnormals, normals, inf and nan), so that no conversion
-// lands on the double-precision pipe
-__device__ __forceinline__ double f2d_exact(float f)
-{
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t sign = u & 0x80000000u, a = u & 0x7fffffffu;
-    uint32_t ex = a >> 23, man = a & 0x7fffffu;
-    uint32_t dexp;
-    if (ex == 0xffu) {
-        dexp = 0x7ffu;                                   // inf / nan
-    } else if (ex != 0u) {
-        dexp = ex + (1023u - 127u);                      // normal
-    } else if (man != 0u) {
-        const uint32_t sh = (uint32_t)__clz((int)man) - 8u;  // subnormal: normalise
-        man = (man << sh) & 0x7fffffu;
-        dexp = 1023u - 126u - sh;
-    } else {
-        dexp = 0u;                                       // signed zero
-    }
-    return __hiloint2double((int)(sign | (dexp << 20) | (man >> 3)), (int)(man << 29));
-}
-
-// exact float -> double for normal numbers and zeros from the bit pattern
-// (rebias the exponent, move the mantissa); other values take f2d_exact
-__device__ __forceinline__ double f2d_fast(float f)
-{
-    const uint32_t u = __float_as_uint(f), a = u & 0x7fffffffu;
-    if (a != 0u && a - 0x00800000u >= 0x7f000000u) return f2d_exact(f);  // subnormal, inf, nan
-    const uint32_t h = (u & 0x80000000u) | (a != 0u ? (a >> 3) + 0x38000000u : 0u);
-    return __hiloint2double((int)h, (int)(u << 29));
-}
-
-// shared memory of one warp: G_MAXP staged slabs, then the node's
-// contribution entries (at most 64 pairs x 4 element nodes)
-template <class R, int NEN> struct GatherSmem {
-    static constexpr int PER_WARP = G_MAXP * NEN * 36 * (int)sizeof(R) + 512;
-};
-
-template <class R, int NEN, int G_COLS, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
-{
-    constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
-    constexpr bool SINGLE = sizeof(R) == 4;
-    constexpr int BCH = 36 * (int)sizeof(R) / 16;  // 16-byte chunks per 6x6 block
-    constexpr int CH = NEN * BCH;                   // 16-byte chunks per slab
-    constexpr int CPL = (CH + 31) / 32;             // chunks per lane per pair
-    extern __shared__ __align__(16) unsigned char gather_smem[];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int64_t r = (int64_t)blockIdx.x * WARPS + w;
-    if (r >= m.nnodes) return;
-    unsigned char *wsm = gather_smem + (size_t)w * GatherSmem<R, NEN>::PER_WARP;
-    R *stage = reinterpret_cast<R *>(wsm);
-    uint16_t *sent = reinterpret_cast<uint16_t *>(wsm + G_MAXP * SLAB * sizeof(R));
-    int32_t d[6];
-    bool any = false;
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        d[k] = m.dof[(int64_t)k * m.nnodes + r];
-        any |= (d[k] <= n);
-    }
-    if (!any) return;
-    const int L = P.rowlen[r];
-    const int64_t off = P.nbr_off[r], off6 = off * 6;
-    const int64_t pb = m.pp[r], pe = m.pp[r + 1];
-    if (L <= 32 * G_COLS) {
-        // the node's contribution entries into shared memory
-        const int ntot = (int)(pe - pb) * NEN;
-        const uint16_t *ent = P.sl_ent + pb * NEN;
-        for (int i = lane; i < ntot; i += 32) sent[i] = ent[i];
-        // the lane's columns and the range of entries of their neighbour slot
-        const int nslots = (int)(P.nbr_off[r + 1] - off);
-        int kcol[G_COLS], cur[G_COLS], last[G_COLS];
-        R hi[G_COLS][6], lo[G_COLS][6];
-#pragma unroll
-        for (int c = 0; c < G_COLS; c++) {
-            const int j = lane + 32 * c;
-            kcol[c] = 0;
-            cur[c] = 0;
-            last[c] = 0;
-            if (j < L) {
-                const int cs = (int)P.colsrc[off6 + j];
-                const int sl = cs / 6;
-                kcol[c] = cs - 6 * sl;
-                cur[c] = (int)P.sl_off[off + sl];
-                last[c] = sl + 1 < nslots ? (int)P.sl_off[off + sl + 1] : ntot;
-            }
-#pragma unroll
-            for (int k = 0; k < 6; k++) {
-                hi[c][k] = 0;
-                lo[c][k] = 0;
-            }
-        }
-        // lane-fixed staging chunks: chunk lane + 32 t of every slab
-        int cb[CPL], cwd[CPL];
-#pragma unroll
-        for (int t = 0; t < CPL; t++) {
-            const int ch = lane + 32 * t;
-            cb[t] = ch / BCH;
-            cwd[t] = ch - cb[t] * BCH;
-        }
-        for (int64_t p0 = pb; p0 < pe; p0 += G_MAXP) {
-            const int cnt = (int)min((int64_t)G_MAXP, pe - p0);
-            const int q0 = (int)(p0 - pb);
-            for (int q = 0; q < cnt; q++) {
-                const int32_t pel = m.pair_e[p0 + q];
-                const int a = pel & 3;
-                const R *base = ke + (int64_t)(pel >> 2) * ND2;
-#pragma unroll
-                for (int t = 0; t < CPL; t++) {
-                    if (lane + 32 * t < CH) {
-                        const int bb = cb[t];
-                        // block (a, bb) of the element: stored as itself or as its mirror
-                        const R *src = base + ub(min(a, bb), max(a, bb), NEN) * 36;
-                        cp_async16(reinterpret_cast<char *>(stage + q * SLAB + bb * 36) + 16 * cwd[t],
-                                   reinterpret_cast<const char *>(src) + 16 * cwd[t]);
-                    }
-                }
-            }
-            cp_async_wait_all();
-            __syncwarp();
-            // this batch's contributions to the lane's columns, ascending pair order
-#pragma unroll
-            for (int c = 0; c < G_COLS; c++) {
-                while (cur[c] < last[c]) {
-                    const uint32_t e = sent[cur[c]];
-                    const int q = (int)(e & 63u) - q0;
-                    if (q >= cnt) break;
-                    const int b = (int)((e >> 6) & 3u);
-                    // entry (krow, kcol) of block (a_q, b); a mirrored block is read transposed
-                    const bool tr = (e >> 8) & 1u;
-                    const R *src = stage + q * SLAB + b * 36 + (tr ? 6 * kcol[c] : kcol[c]);
-                    const int st = tr ? 1 : 6;
-#pragma unroll
-                    for (int k = 0; k < 6; k++) {
-                        const R v = src[st * k];
-                        if (SINGLE) {
-                            const R t = hi[c][k] + v;
-                            const R bp = t - hi[c][k];
-                            lo[c][k] += (hi[c][k] - (t - bp)) + (v - bp);
-                            hi[c][k] = t;
-                        } else {
-                            hi[c][k] += v;
-                        }
-                    }
-                    cur[c]++;
-                }
-            }
-            __syncwarp();
-        }
-#pragma unroll
-        for (int k = 0; k < 6; k++) {
-            if (d[k] > n) continue;
-            double *o = vals + P.rowptr[d[k] - 1];
-#pragma unroll
-            for (int c = 0; c < G_COLS; c++) {
-                const int j = lane + 32 * c;
-                if (j >= L) continue;
-                double v;
-                if (SINGLE) {
-                    // hi + lo: exact in double unless their exponents are more than
-                    // 29 apart, then rounded once
-                    v = f2d_fast((float)hi[c][k]);
-                    if (lo[c][k] != (R)0) v += f2d_fast((float)lo[c][k]);
-                } else {
-                    v = (double)hi[c][k];
-                }
-                o[j] = v;
-            }
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < 6; k++) {
-            if (d[k] > n) continue;
-            double *o = vals + P.rowptr[d[k] - 1];
-            for (int j = lane; j < L; j += 32) o[j] = 0.0;
-        }
-        __syncwarp();
-        for (int64_t p = pb; p < pe; p++) {
-            int32_t pe_ = m.pair_e[p];
-            int64_t rank = pe_ >> 2;
-            int a = pe_ & 3;
-            uint32_t slots = P.pair_slots[p];
-            for (int idx = lane; idx < SLAB; idx += 32) {
-                int b = idx / 36, rem = idx - 36 * b, krow = rem / 6, kc = rem - 6 * krow;
-                const R *blk = ke + rank * (int64_t)ND2 + ub(min(a, b), max(a, b), NEN) * 36;
-                const R v = b < a ? blk[kc * 6 + krow] : blk[rem];
-                int s = (slots >> (8 * b)) & 0xff;
-                int cp = P.colpos[off6 + s * 6 + kc];
-                if (cp >= 0 && d[krow] <= n) {
-                    double *o = vals + P.rowptr[d[krow] - 1] + cp;
-                    *o += (double)v;
-                }
-            }
-            __threadfence_block();
-            __syncwarp();
-        }
-    }
-}
-
-template <class R, int NEN, int G_COLS, int W>
-static int gather_launch_w(fs_ctx *c, const R *ke, double *vals)
-{
-    const MeshDev &m = c->mesh;
-    const size_t smem = (size_t)W * GatherSmem<R, NEN>::PER_WARP;
-    auto kern = k_gather<R, NEN, G_COLS, W>;
-    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
-    return FS_OK;
-}
-
-template <class R, int NEN, int G_COLS>
-static int gather_launch_c(fs_ctx *c, const R *ke, double *vals, int warps)
-{
-    if (warps == 4) return gather_launch_w<R, NEN, G_COLS, 4>(c, ke, vals);
-    if (warps == 16) return gather_launch_w<R, NEN, G_COLS, 16>(c, ke, vals);
-    return gather_launch_w<R, NEN, G_COLS, 8>(c, ke, vals);
-}
-
-template <class R, int NEN>
-static int gather_launch(fs_ctx *c, const R *ke, double *vals, int warps)
-{
-    // per-lane columns sized to the longest row (rows beyond 128 accumulate in place)
-    if (c->pat.maxlen <= 64) return gather_launch_c<R, NEN, 2>(c, ke, vals, warps);
-    return gather_launch_c<R, NEN, 4>(c, ke, vals, warps);
-}
-
-template <class R>
-static int run_gather(fs_ctx *c, const R *ke, double *vals, int warps)
-{
-    if (warps <= 0) warps = sizeof(R) == 4 ? 8 : 4;
-    int st;
-    if (c->mesh.nen == 3)
-        st = gather_launch<R, 3>(c, ke, vals, warps);
-    else if (c->mesh.nen == 2)
-        st = gather_launch<R, 2>(c, ke, vals, warps);
-    else
-        st = gather_launch<R, 4>(c, ke, vals, warps);
-    FS_TRY(st);
-    FS_CUDA(c, cudaGetLastError());
-    return FS_OK;
-}
-
-int launch_gather(fs_ctx *c, int precision, double *vals)
-{
-    if (c->mesh.nnodes == 0) return FS_OK;
-    const int w = c->tune.gather_warps;
-    if (precision == FS_FP64) return run_gather<double>(c, (const double *)c->ke, vals, w);
-    return run_gather<float>(c, (const float *)c->ke, vals, w);
+    return run_elements(c, precision, c->ke);
 }
 
 // ---------------------------------------------------------------------------
@@ -738,36 +263,10 @@ namespace fs {
 // (same layout as the context's own buffer); allocates nothing.
 int launch_elements_to(fs_ctx *c, int precision, void *ke)
 {
-    MeshDev &m = c->mesh;
-    if (m.nelem == 0) return FS_OK;
-    bool comp = (m.etype == FS_T3FFCOMP || m.etype == FS_Q4RSCOMP);
-    bool avgk = c->params.transv_shear_formulation == 1;
-    if (m.nen == 3) {
-        if (precision == FS_FP64) {
-            double *k = (double *)ke;
-            if (comp) return avgk ? run_t3<double, true, true>(c, k) : run_t3<double, true, false>(c, k);
-            return avgk ? run_t3<double, false, true>(c, k) : run_t3<double, false, false>(c, k);
-        }
-        float *k = (float *)ke;
-        if (comp) return avgk ? run_t3<float, true, true>(c, k) : run_t3<float, true, false>(c, k);
-        return avgk ? run_t3<float, false, true>(c, k) : run_t3<float, false, false>(c, k);
-    }
-    if (precision == FS_FP64) {
-        double *k = (double *)ke;
-        return comp ? run_q4<double, true>(c, k) : run_q4<double, false>(c, k);
-    }
-    float *k = (float *)ke;
-    return comp ? run_q4<float, true>(c, k) : run_q4<float, false>(c, k);
+    if (c->mesh.nelem == 0) return FS_OK;
+    return run_elements(c, precision, ke);
 }
 
-// CSR values from element matrices held in `ke`; allocates nothing.
-int launch_gather_from(fs_ctx *c, int precision, const void *ke, double *vals)
-{
-    if (c->mesh.nnodes == 0) return FS_OK;
-    const int w = c->tune.gather_warps;
-    if (precision == FS_FP64) return run_gather<double>(c, (const double *)ke, vals, w);
-    return run_gather<float>(c, (const float *)ke, vals, w);
-}
 
 // ---------------------------------------------------------------------------
 // tile-shape autotuner

@@ -7,7 +7,7 @@ include/flexshell.h; this package is its host-side mirror of the reference
 interface.
 """
 from . import _abi, mesh, materials
-from ._abi import FS_FP64, FS_MIXED
+from ._abi import FS_FP64, FS_MIXED, FS_MIXED_COMP
 from .femm import (FEMMShellQ4RS, FEMMShellQ4RSComp, FEMMShellT3FF, FEMMShellT3FFComp,
                    NodalField, SysmatAssemblerFFBlock, SysmatAssemblerSparse,
                    SysmatAssemblerSparseCSRSymm, SysmatAssemblerSparseDiag,

@@ -11,7 +11,7 @@ FS_ERR_STATE = 6
 FS_ERR_TIMEOUT = 7
 
 FS_T3FF, FS_T3FFCOMP, FS_Q4RS, FS_Q4RSCOMP, FS_COROTBEAM = 0, 1, 2, 3, 4
-FS_FP64, FS_MIXED = 0, 1
+FS_FP64, FS_MIXED, FS_MIXED_COMP = 0, 1, 2
 FS_ASM_SPARSE, FS_ASM_SPARSE_SYMM, FS_ASM_DIAG = 0, 1, 2
 FS_BEAM_STIFFNESS, FS_BEAM_GEOSTIFFNESS, FS_BEAM_MASS, FS_BEAM_GYROSCOPIC = 0, 1, 2, 3
 FS_BEAM_RESTORING, FS_BEAM_DISTRIBLOAD = 4, 5

@@ -20,7 +20,7 @@ import numpy as np
 from . import _abi, mesh as _mesh
 from ._lib import Context, FlexShellError, ptr
 
-FS_FP64, FS_MIXED = _abi.FS_FP64, _abi.FS_MIXED
+FS_FP64, FS_MIXED, FS_MIXED_COMP = _abi.FS_FP64, _abi.FS_MIXED, _abi.FS_MIXED_COMP
 
 
 # ---------------------------------------------------------------------------

@@ -49,6 +49,10 @@ extern "C" {
 #define FS_FP64 0       /* everything in double: the drop-in                 */
 #define FS_MIXED 1      /* float element arithmetic; frames, triads, drilling
                            factor and CSR accumulation in double             */
+#define FS_MIXED_COMP 2 /* as FS_MIXED, with the element Gram products
+                           accumulated error-free in float (Dot2) and kept as
+                           float pairs: the stiffness keeps the rigid-body
+                           null space to O(eps^2), for thin-plate eigenvalues */
 
 /* assembler semantics (FinEtools assemblers) */
 #define FS_ASM_SPARSE 0      /* SysmatAssemblerSparse / SysmatAssemblerSparseCSRSymm
@@ -162,7 +166,7 @@ int fs_tuning(const fs_ctx *ctx, int32_t *out);
  * caller's device buffer `vals` (vals_len >= nnz).  The pattern for `nrows`
  * must exist (one fs_stiffness or fs_mass call at set-up).  Element matrices
  * are staged in a fixed 32 MiB device array inside the library, so
- * nelem * 36 nen (nen + 1)/2 * (8 for FS_FP64, 4 for FS_MIXED) bytes (the upper
+ * nelem * 36 nen (nen + 1)/2 * (4 for FS_MIXED, else 8) bytes (the upper
  * node blocks of its element matrices) must fit in it (19,418 T3FF elements in FP64); larger meshes get FS_ERR_UNSUPPORTED.
  * It calls no cudaMalloc/cudaFree.  The first call on a device looks up the
  * array's address (make it before any stream capture); calls that overlap on

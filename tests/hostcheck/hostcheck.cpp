@@ -16,7 +16,7 @@ template <class R>
 static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t nelem,
                          const int64_t *conn, const double *normals, const uint8_t *valid,
                          const double *thick, const fs_shell_params *p, const fs_layup_group *groups,
-                         const int32_t *egroup, double *out)
+                         const int32_t *egroup, double *out, bool exact_gram = false)
 {
     MatConst mc;
     if (prepare_matconst(*p, mc)) return 1;
@@ -82,9 +82,16 @@ static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t n
         double *K = out + (int64_t)nd * nd * e;
         for (int j = 0; j < nd; j++)
             for (int i = 0; i < nd; i++) {
-                R s = 0;
-                for (int r = 0; r < nrows; r++) s += rows[r][i] * rows[r][j];
-                K[i + nd * j] = (double)s;
+                if (exact_gram) {
+                    // products of float rows are exact in double; accumulate in double
+                    double s = 0;
+                    for (int r = 0; r < nrows; r++) s += (double)rows[r][i] * (double)rows[r][j];
+                    K[i + nd * j] = s;
+                } else {
+                    R s = 0;
+                    for (int r = 0; r < nrows; r++) s += rows[r][i] * rows[r][j];
+                    K[i + nd * j] = (double)s;
+                }
             }
     }
     return 0;
@@ -100,7 +107,7 @@ extern "C" int hc_element_matrices(int etype, int precision, int64_t nnodes, con
         return elem_matrices<double>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
                                      egroup, out);
     return elem_matrices<float>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
-                                egroup, out);
+                                egroup, out, precision == 2);
 }
 
 extern "C" int hc_lumped(int etype, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,

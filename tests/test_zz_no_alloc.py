@@ -20,7 +20,7 @@ import problems as PB
 
 pytestmark = pytest.mark.gpu
 
-TOL = {_abi.FS_FP64: 1e-12, _abi.FS_MIXED: 1e-6}
+TOL = {_abi.FS_FP64: 1e-12, _abi.FS_MIXED: 1e-6, _abi.FS_MIXED_COMP: 1e-6}
 
 
 def _femm(n, quads):
@@ -36,7 +36,7 @@ def _femm(n, quads):
 
 
 @pytest.mark.parametrize("quads", [False, True])
-@pytest.mark.parametrize("precision", [_abi.FS_FP64, _abi.FS_MIXED])
+@pytest.mark.parametrize("precision", [_abi.FS_FP64, _abi.FS_MIXED, _abi.FS_MIXED_COMP])
 def test_noalloc_matches_regular_entry_point(quads, precision):
     import torch
     femm, geom0, dchi = _femm(16, quads)
