@@ -79,59 +79,75 @@ __device__ __forceinline__ void store_block_pair(float2 *o, const float (&s)[6][
     }
 }
 
+// Accumulator of one 6x6 node block of K = sum_rho row_rho row_rho^T: plain
+// in the row type, or (float rows into float pairs) error-free by Dot2.
+template <class R, bool PAIR> struct BlockAcc {
+    R v[6][6];
+    __device__ __forceinline__ void zero()
+    {
+#pragma unroll
+        for (int i = 0; i < 6; i++)
+#pragma unroll
+            for (int j = 0; j < 6; j++) v[i][j] = 0;
+    }
+    __device__ __forceinline__ void add(int i, int j, R x, R y) { v[i][j] += x * y; }
+    template <class S> __device__ __forceinline__ void store(S *o) { store_block<R>(reinterpret_cast<R *>(o), v, false); }
+};
+template <> struct BlockAcc<float, true> {
+    float s[6][6], c[6][6];
+    __device__ __forceinline__ void zero()
+    {
+#pragma unroll
+        for (int i = 0; i < 6; i++)
+#pragma unroll
+            for (int j = 0; j < 6; j++) s[i][j] = c[i][j] = 0.f;
+    }
+    __device__ __forceinline__ void add(int i, int j, float x, float y) { dot2_step(s[i][j], c[i][j], x, y); }
+    template <class S> __device__ __forceinline__ void store(S *o) { store_block_pair(reinterpret_cast<float2 *>(o), s, c); }
+};
+
+// acc += sum over rows [r0, r1) of row[6a + i] row[6b + j] for i in
+// [I0, I1), j in [J0, J1): the sub-blocks a row can reach
+template <int I0, int I1, int J0, int J1, class R, class Acc>
+__device__ __forceinline__ void gram_rows(Acc &acc, const R *rows, int ND, int r0, int r1, int a, int b)
+{
+    for (int rho = r0; rho < r1; rho++) {
+        const R *rr = rows + rho * ND;
+        R ra[6], rb[6];
+#pragma unroll
+        for (int i = I0; i < I1; i++) ra[i] = rr[6 * a + i];
+#pragma unroll
+        for (int j = J0; j < J1; j++) rb[j] = rr[6 * b + j];
+#pragma unroll
+        for (int i = I0; i < I1; i++)
+#pragma unroll
+            for (int j = J0; j < J1; j++) acc.add(i, j, ra[i], rb[j]);
+    }
+}
+
 // Upper node blocks of K = sum_rho row_rho row_rho^T.  Storage S: the row
 // type R itself, or float2 pairs for float rows accumulated error-free
-// (FS_MIXED_COMP).
-template <class R, class S, int NN>
+// (FS_MIXED_COMP).  SPARSE (homogeneous shells): rows 0..2 are membrane rows
+// (nodal translations only) and the last NN rows drilling rows (the
+// rotations of one node each); their structurally zero products are
+// skipped, in the same row order, so the sums are those of the dense loop.
+template <class R, class S, int NN, bool SPARSE>
 __device__ __forceinline__ void write_blocks(const R *rows, int nrows, S *out)
 {
+    constexpr bool PAIR = sizeof(S) == 8 && sizeof(R) == 4;
     const int ND = 6 * NN;
-    if constexpr (sizeof(S) == 8 && sizeof(R) == 4) {
-        for (int a = 0; a < NN; a++)
-            for (int b = a; b < NN; b++) {
-                float hs[6][6], cs[6][6];
-#pragma unroll
-                for (int i = 0; i < 6; i++)
-#pragma unroll
-                    for (int j = 0; j < 6; j++) hs[i][j] = cs[i][j] = 0.f;
-                for (int rho = 0; rho < nrows; rho++) {
-                    const R *rr = rows + rho * ND;
-                    float ra[6], rb[6];
-#pragma unroll
-                    for (int i = 0; i < 6; i++) {
-                        ra[i] = rr[6 * a + i];
-                        rb[i] = rr[6 * b + i];
-                    }
-#pragma unroll
-                    for (int i = 0; i < 6; i++)
-#pragma unroll
-                        for (int j = 0; j < 6; j++) dot2_step(hs[i][j], cs[i][j], ra[i], rb[j]);
-                }
-                store_block_pair(reinterpret_cast<float2 *>(out) + ub(a, b, NN) * 36, hs, cs);
-            }
-        return;
-    }
     for (int a = 0; a < NN; a++)
         for (int b = a; b < NN; b++) {
-            R acc[6][6];
-#pragma unroll
-            for (int i = 0; i < 6; i++)
-#pragma unroll
-                for (int j = 0; j < 6; j++) acc[i][j] = 0;
-            for (int rho = 0; rho < nrows; rho++) {
-                const R *rr = rows + rho * ND;
-                R ra[6], rb[6];
-#pragma unroll
-                for (int i = 0; i < 6; i++) {
-                    ra[i] = rr[6 * a + i];
-                    rb[i] = rr[6 * b + i];
-                }
-#pragma unroll
-                for (int i = 0; i < 6; i++)
-#pragma unroll
-                    for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
+            BlockAcc<R, PAIR> acc;
+            acc.zero();
+            if (SPARSE) {
+                gram_rows<0, 3, 0, 3>(acc, rows, ND, 0, 3, a, b);
+                gram_rows<0, 6, 0, 6>(acc, rows, ND, 3, nrows - NN, a, b);
+                if (a == b) gram_rows<3, 6, 3, 6>(acc, rows, ND, nrows - NN + a, nrows - NN + a + 1, a, b);
+            } else {
+                gram_rows<0, 6, 0, 6>(acc, rows, ND, 0, nrows, a, b);
             }
-            store_block<R>(reinterpret_cast<R *>(out) + ub(a, b, NN) * 36, acc, false);
+            acc.store(out + ub(a, b, NN) * 36);
         }
 }
 

@@ -52,47 +52,22 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
     for (int bi = qp; bi < 10; bi += 4) {
         int a = bi < 4 ? 0 : (bi < 7 ? 1 : (bi < 9 ? 2 : 3));
         int b = a + (bi - (a == 0 ? 0 : (a == 1 ? 4 : (a == 2 ? 7 : 9))));
-        if constexpr (sizeof(S) == 8 && sizeof(R) == 4) {
-            float hs[6][6], cs[6][6];
-#pragma unroll
-            for (int i = 0; i < 6; i++)
-#pragma unroll
-                for (int j = 0; j < 6; j++) hs[i][j] = cs[i][j] = 0.f;
-            for (int rho = 0; rho < NR; rho++) {
-                const R *rr = rows + rho * ND;
-                float ra[6], rb[6];
-#pragma unroll
-                for (int i = 0; i < 6; i++) {
-                    ra[i] = rr[6 * a + i];
-                    rb[i] = rr[6 * b + i];
-                }
-#pragma unroll
-                for (int i = 0; i < 6; i++)
-#pragma unroll
-                    for (int j = 0; j < 6; j++) dot2_step(hs[i][j], cs[i][j], ra[i], rb[j]);
+        constexpr bool PAIR = sizeof(S) == 8 && sizeof(R) == 4;
+        BlockAcc<R, PAIR> acc;
+        acc.zero();
+        if constexpr (!COMP) {
+            // homogeneous: per Gauss point 3 membrane rows (translations only)
+            // and 5 bending/shear rows; then one drilling row per node
+#pragma unroll 1
+            for (int j = 0; j < 4; j++) {
+                gram_rows<0, 3, 0, 3>(acc, rows, ND, 8 * j, 8 * j + 3, a, b);
+                gram_rows<0, 6, 0, 6>(acc, rows, ND, 8 * j + 3, 8 * j + 8, a, b);
             }
-            store_block_pair(reinterpret_cast<float2 *>(out) + ub(a, b, 4) * 36, hs, cs);
-            continue;
+            if (a == b) gram_rows<3, 6, 3, 6>(acc, rows, ND, 32 + a, 33 + a, a, b);
+        } else {
+            gram_rows<0, 6, 0, 6>(acc, rows, ND, 0, NR, a, b);
         }
-        R acc[6][6];
-#pragma unroll
-        for (int i = 0; i < 6; i++)
-#pragma unroll
-            for (int j = 0; j < 6; j++) acc[i][j] = 0;
-        for (int rho = 0; rho < NR; rho++) {
-            const R *rr = rows + rho * ND;
-            R ra[6], rb[6];
-#pragma unroll
-            for (int i = 0; i < 6; i++) {
-                ra[i] = rr[6 * a + i];
-                rb[i] = rr[6 * b + i];
-            }
-#pragma unroll
-            for (int i = 0; i < 6; i++)
-#pragma unroll
-                for (int j = 0; j < 6; j++) acc[i][j] += ra[i] * rb[j];
-        }
-        store_block<R>(reinterpret_cast<R *>(out) + ub(a, b, 4) * 36, acc, false);
+        acc.store(out + ub(a, b, 4) * 36);
     }
 }
 

@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(EPB) k_t3_elements(const MeshDev m, const MatC
     const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
     int st = t3_rows<R, COMP, AVGK>(in, mc, gc, rows, ND);
     if (st) atomicOr(status, DEV_NEG_DRILL);
-    write_blocks<R, S, 3>(rows, NR, ke + r * (6 * 36));
+    write_blocks<R, S, 3, !COMP>(rows, NR, ke + r * (6 * 36));
 }
 
 template <class R, class S, bool COMP, bool AVGK, int EPB>

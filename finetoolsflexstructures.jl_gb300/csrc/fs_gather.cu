@@ -94,7 +94,7 @@ template <class R, int NEN> struct GatherSmem {
 };
 
 template <class R, int NEN, int G_COLS, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS)  // at least 32 resident warps per SM
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
     typedef typename GatherAcc<R>::T A;
@@ -110,24 +110,28 @@ __global__ void __launch_bounds__(WARPS * 32)
     unsigned char *wsm = gather_smem + (size_t)w * GatherSmem<R, NEN>::PER_WARP;
     R *stage = reinterpret_cast<R *>(wsm);
     uint16_t *sent = reinterpret_cast<uint16_t *>(wsm + G_MAXP * SLAB * sizeof(R));
+    // the node's scalar data: all independent loads issued together
     int32_t d[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) d[k] = m.dof[(int64_t)k * m.nnodes + r];
+    const int L = P.rowlen[r];
+    const int64_t off = P.nbr_off[r], off_next = P.nbr_off[r + 1], off6 = off * 6;
+    const int64_t pb = m.pp[r], pe = m.pp[r + 1];
     bool any = false;
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
-        d[k] = m.dof[(int64_t)k * m.nnodes + r];
-        any |= (d[k] <= n);
-    }
+    for (int k = 0; k < 6; k++) any |= (d[k] <= n);
     if (!any) return;
-    const int L = P.rowlen[r];
-    const int64_t off = P.nbr_off[r], off6 = off * 6;
-    const int64_t pb = m.pp[r], pe = m.pp[r + 1];
     if (L <= 32 * G_COLS) {
+        // row starts of the node's six rows, loaded before the work that needs them
+        int64_t rs6[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) rs6[k] = d[k] <= n ? P.rowptr[d[k] - 1] : 0;
         // the node's contribution entries into shared memory
         const int ntot = (int)(pe - pb) * NEN;
         const uint16_t *ent = P.sl_ent + pb * NEN;
         for (int i = lane; i < ntot; i += 32) sent[i] = ent[i];
         // the lane's columns and the range of entries of their neighbour slot
-        const int nslots = (int)(P.nbr_off[r + 1] - off);
+        const int nslots = (int)(off_next - off);
         int kcol[G_COLS], cur[G_COLS], last[G_COLS];
         A hi[G_COLS][6], lo[G_COLS][6];
 #pragma unroll
@@ -199,7 +203,7 @@ __global__ void __launch_bounds__(WARPS * 32)
 #pragma unroll
         for (int k = 0; k < 6; k++) {
             if (d[k] > n) continue;
-            double *o = vals + P.rowptr[d[k] - 1];
+            double *o = vals + rs6[k];
 #pragma unroll
             for (int c = 0; c < G_COLS; c++) {
                 const int j = lane + 32 * c;

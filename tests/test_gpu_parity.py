@@ -381,13 +381,21 @@ def test_composite_eigenvalues_mixed_vs_fp64():
 
 @pytest.mark.parametrize("quads", [False, True])
 def test_compensated_mixed_matches_oracle(quads):
-    # FS_MIXED_COMP: same pattern, values within the mixed tolerance, and the
-    # rigid-body translations of a flat plate carry no stiffness beyond O(eps^2)
+    # FS_MIXED_COMP: same pattern, values within the mixed tolerance (curved
+    # roof), and on a flat plate, where the element is exactly free of
+    # rigid-body stiffness, a rigid translation carries O(eps^2) energy
+    # against O(eps) with FS_MIXED
     d = PB.scordelis_lo(quads, 6)
     P, femm, geom0, dchi = homog_pair(d, quads)
     Kc = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi, precision=F.FS_MIXED_COMP)
     Ko = P.assemble_scipy("K", O.KEEP_ZEROS)
     assert same_pattern(Kc, Ko) and relmax(Kc, Ko) <= MIXED_TOL
+    femm.close()
+    xyz, conn, dof, nfree = PB.jittered_plate(6, quads, seed=3)
+    cls = F.FEMMShellQ4RS if quads else F.FEMMShellT3FF
+    femm = cls(conn, 0.001, F.materials.MatDeforElastIso(2.0e11, 0.3, 7850.0))
+    geom0 = F.NodalField(xyz)
+    femm.associategeometry(geom0)
     E64 = femm.element_matrices(geom0, precision=F.FS_FP64)
     Ec = femm.element_matrices(geom0, precision=F.FS_MIXED_COMP)
     Em = femm.element_matrices(geom0, precision=F.FS_MIXED)
@@ -396,5 +404,6 @@ def test_compensated_mixed_matches_oracle(quads):
     ec = np.abs(np.einsum("i,eij,j->e", u, Ec, u)).max()
     em = np.abs(np.einsum("i,eij,j->e", u, Em, u)).max()
     scale = np.abs(E64).max()
+    assert e64 <= 1e-13 * scale
     assert ec <= 1e-12 * scale and ec <= em
     femm.close()
