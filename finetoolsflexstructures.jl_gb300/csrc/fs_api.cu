@@ -202,6 +202,12 @@ int fs_ctx_destroy(fs_ctx *c)
     cudaFree(c->d_status);
     for (int k = 0; k < 4; k++)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    for (int k = 0; k < 2; k++)
+        if (c->copy_ev[k]) cudaEventDestroy(c->copy_ev[k]);
     cudaStreamDestroy(c->stream);
     delete c;
     return FS_OK;
@@ -554,6 +560,70 @@ int fs_matrix_copy(fs_ctx *c, int64_t *colptr, int64_t *rowval, double *nzval)
         FS_CUDA(c, cudaMemcpyAsync(rowval, c->stage64, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, c->stream));
     }
     if (nzval && nnz) FS_CUDA(c, cudaMemcpyAsync(nzval, c->vals, sizeof(double) * nnz, cudaMemcpyDeviceToHost, c->stream));
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FS_OK;
+}
+
+int fs_pattern(fs_ctx *c, int64_t nrows, int64_t *nnz_out)
+{
+    if (!c) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    FS_TRY(check_ready(c));
+    if (nrows < 0) return set_err(c, FS_ERR_BAD_INPUT, "negative matrix size");
+    if (c->pat.n != nrows || !c->pat.rowptr) {
+        FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+        FS_TRY(build_pattern(c, nrows));
+        FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
+        FS_CUDA(c, cudaEventSynchronize(c->ev[1]));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        c->t_symbolic_ms = ms;
+    }
+    if (nnz_out) *nnz_out = c->pat.nnz;
+    return FS_OK;
+}
+
+int fs_stiffness_copy(fs_ctx *c, int precision, int64_t nrows, int64_t *colptr, int64_t *rowval, double *nzval)
+{
+    if (!c) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    FS_TRY(check_ready(c));
+    if (precision != FS_FP64 && precision != FS_MIXED && precision != FS_MIXED_COMP)
+        return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
+    if (!c->normals_ready)
+        return set_err(c, FS_ERR_STATE, "associategeometry! has not been called (self._associatedgeometry == true)");
+    if (c->pat.n != nrows || !c->pat.rowptr) return set_err(c, FS_ERR_STATE, "no pattern of this size: call fs_pattern first");
+    if (!colptr || (c->pat.nnz && (!rowval || !nzval))) return set_err(c, FS_ERR_BAD_INPUT, "missing output array");
+    if (!c->copy_stream) {
+        FS_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) FS_CUDA(c, cudaEventCreateWithFlags(&c->copy_ev[k], cudaEventDisableTiming));
+    }
+    const PatternDev &P = c->pat;
+    const int64_t n = nrows, nnz = P.nnz;
+    const size_t need = (size_t)(n + 1 + nnz);
+    if (need > c->stage_cap || !c->stage64) {
+        FS_TRY(dalloc(c, &c->stage64, need));
+        c->stage_cap = need;
+    }
+    // the pattern (1-based) goes out on the copy stream while the kernels run
+    FS_CUDA(c, cudaEventRecord(c->copy_ev[0], c->stream));
+    FS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->copy_ev[0], 0));
+    int64_t *sp = c->stage64, *sr = c->stage64 + n + 1;
+    k_plus_one_i64<<<(unsigned)((n + 1 + 255) / 256), 256, 0, c->copy_stream>>>(n + 1, P.rowptr, sp);
+    if (nnz) k_plus_one_i32<<<(unsigned)((nnz + 255) / 256), 256, 0, c->copy_stream>>>(nnz, P.colidx, sr);
+    FS_CUDA(c, cudaGetLastError());
+    FS_CUDA(c, cudaMemcpyAsync(colptr, sp, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, c->copy_stream));
+    if (nnz) FS_CUDA(c, cudaMemcpyAsync(rowval, sr, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, c->copy_stream));
+    FS_CUDA(c, cudaEventRecord(c->copy_ev[1], c->copy_stream));
+    // values: element kernel and gather on the context stream, then their copy
+    int64_t got = 0;
+    const int st = assemble_matrix(c, precision, FS_ASM_SPARSE, nrows, &got, -1, 0);
+    if (st != FS_OK) {
+        cudaStreamSynchronize(c->copy_stream);
+        return st;
+    }
+    if (nnz) FS_CUDA(c, cudaMemcpyAsync(nzval, c->vals, sizeof(double) * nnz, cudaMemcpyDeviceToHost, c->stream));
+    FS_CUDA(c, cudaStreamWaitEvent(c->stream, c->copy_ev[1], 0));
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
     return FS_OK;
 }

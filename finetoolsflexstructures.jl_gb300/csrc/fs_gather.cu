@@ -94,7 +94,7 @@ template <class R, int NEN> struct GatherSmem {
 };
 
 template <class R, int NEN, int G_COLS, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS)  // at least 32 resident warps per SM
+__global__ void __launch_bounds__(WARPS * 32)
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
     typedef typename GatherAcc<R>::T A;
@@ -122,10 +122,6 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS)  // at least 32 reside
     for (int k = 0; k < 6; k++) any |= (d[k] <= n);
     if (!any) return;
     if (L <= 32 * G_COLS) {
-        // row starts of the node's six rows, loaded before the work that needs them
-        int64_t rs6[6];
-#pragma unroll
-        for (int k = 0; k < 6; k++) rs6[k] = d[k] <= n ? P.rowptr[d[k] - 1] : 0;
         // the node's contribution entries into shared memory
         const int ntot = (int)(pe - pb) * NEN;
         const uint16_t *ent = P.sl_ent + pb * NEN;
@@ -203,7 +199,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS)  // at least 32 reside
 #pragma unroll
         for (int k = 0; k < 6; k++) {
             if (d[k] > n) continue;
-            double *o = vals + rs6[k];
+            double *o = vals + P.rowptr[d[k] - 1];
 #pragma unroll
             for (int c = 0; c < G_COLS; c++) {
                 const int j = lane + 32 * c;

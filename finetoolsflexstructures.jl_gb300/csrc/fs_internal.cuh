@@ -86,6 +86,8 @@ struct PatternDev {
 struct fs_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host copies overlapping the kernels (fs_stiffness_copy)
+    cudaEvent_t copy_ev[2] = {nullptr, nullptr};
     std::string err;
     int *d_status = nullptr;     // kernel status bits
     fs::MeshDev mesh;

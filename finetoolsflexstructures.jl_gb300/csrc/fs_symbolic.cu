@@ -364,24 +364,50 @@ __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_
     }
     // column positions: rank of each valid column dof among the node's columns
     int L = 0;
-    for (int s = 0; s < n; s++)
-        for (int k = 0; k < 6; k++) L += (dof[(int64_t)k * nnodes + buf[s]] <= n_mat);
-    for (int s = 0; s < n; s++)
-        for (int k = 0; k < 6; k++) {
-            int32_t v = dof[(int64_t)k * nnodes + buf[s]];
+    if (6 * n <= MAX_PAIRS_PER_NODE * 4) {
+        // the neighbours' dofs read once into a local list (it overwrites the
+        // neighbour list, already stored: going backwards, buf[s] is read
+        // before cd[6 s ..] is written), excluded dofs marked 0, then ranked
+        int32_t *cd = buf;
+        for (int s = n - 1; s >= 0; s--) {
+            const int32_t node = buf[s];
+            for (int k = 5; k >= 0; k--) {
+                const int32_t v = dof[(int64_t)k * nnodes + node];
+                cd[6 * s + k] = v <= n_mat ? v : 0;
+            }
+        }
+        for (int q = 0; q < 6 * n; q++) L += cd[q] != 0;
+        for (int q = 0; q < 6 * n; q++) {
+            const int32_t v = cd[q];
             int16_t pos = -1;
-            if (v <= n_mat) {
+            if (v != 0) {
                 int cntless = 0;
-                for (int s2 = 0; s2 < n; s2++)
-                    for (int k2 = 0; k2 < 6; k2++) {
-                        int32_t w = dof[(int64_t)k2 * nnodes + buf[s2]];
-                        cntless += (w <= n_mat) & (w < v);
-                    }
+                for (int q2 = 0; q2 < 6 * n; q2++) cntless += (cd[q2] != 0) & (cd[q2] < v);
                 pos = (int16_t)cntless;
             }
-            colpos[off * 6 + s * 6 + k] = pos;
-            if (pos >= 0) colsrc[off * 6 + pos] = (uint16_t)(s * 6 + k);
+            colpos[off * 6 + q] = pos;
+            if (pos >= 0) colsrc[off * 6 + pos] = (uint16_t)q;
         }
+    } else {
+        for (int s = 0; s < n; s++)
+            for (int k = 0; k < 6; k++) L += (dof[(int64_t)k * nnodes + buf[s]] <= n_mat);
+        for (int s = 0; s < n; s++)
+            for (int k = 0; k < 6; k++) {
+                int32_t v = dof[(int64_t)k * nnodes + buf[s]];
+                int16_t pos = -1;
+                if (v <= n_mat) {
+                    int cntless = 0;
+                    for (int s2 = 0; s2 < n; s2++)
+                        for (int k2 = 0; k2 < 6; k2++) {
+                            int32_t w = dof[(int64_t)k2 * nnodes + buf[s2]];
+                            cntless += (w <= n_mat) & (w < v);
+                        }
+                    pos = (int16_t)cntless;
+                }
+                colpos[off * 6 + s * 6 + k] = pos;
+                if (pos >= 0) colsrc[off * 6 + pos] = (uint16_t)(s * 6 + k);
+            }
+    }
     rowlen[r] = L;
 }
 
@@ -398,23 +424,31 @@ __global__ void k_row_lengths(int64_t nnodes, int64_t n_mat, const int32_t *dof,
     }
 }
 
+// One warp per node: position j of the node's rows holds the column of
+// (neighbour slot, component) colsrc[j]; the six rows share it, so each row
+// is written as one contiguous run.
 __global__ void k_fill_colidx(int64_t nnodes, int64_t n_mat, const int32_t *dof, const int64_t *nbr_off,
-                              const int32_t *nbr, const int16_t *colpos, const int64_t *rowptr,
-                              int32_t *colidx)
+                              const int32_t *nbr, const uint16_t *colsrc, const int32_t *rowlen,
+                              const int64_t *rowptr, int32_t *colidx)
 {
-    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (r >= nnodes) return;
-    int64_t off = nbr_off[r];
-    int n = (int)(nbr_off[r + 1] - off);
+    const int64_t off = nbr_off[r];
+    const int L = rowlen[r];
+    int64_t base[6];
+#pragma unroll
     for (int kr = 0; kr < 6; kr++) {
-        int32_t d = dof[(int64_t)kr * nnodes + r];
-        if (d > n_mat) continue;
-        int64_t base = rowptr[d - 1];
-        for (int s = 0; s < n; s++)
-            for (int k = 0; k < 6; k++) {
-                int16_t pos = colpos[off * 6 + s * 6 + k];
-                if (pos >= 0) colidx[base + pos] = dof[(int64_t)k * nnodes + nbr[off + s]] - 1;
-            }
+        const int32_t d = dof[(int64_t)kr * nnodes + r];
+        base[kr] = d <= n_mat ? rowptr[d - 1] : -1;
+    }
+    for (int j = lane; j < L; j += 32) {
+        const int cs = colsrc[off * 6 + j];
+        const int s = cs / 6, k = cs - 6 * s;
+        const int32_t col = dof[(int64_t)k * nnodes + nbr[off + s]] - 1;
+#pragma unroll
+        for (int kr = 0; kr < 6; kr++)
+            if (base[kr] >= 0) colidx[base[kr] + j] = col;
     }
 }
 
@@ -478,7 +512,9 @@ int build_pattern(fs_ctx *c, int64_t n)
     cudaFree(cnt);
     if (bits & DEV_BAD_DOF) return set_err(c, FS_ERR_BAD_INPUT, "two dofs share one dof number");
     FS_TRY(dalloc(c, &P.colidx, (size_t)nnz));
-    if (nn) k_fill_colidx<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.colpos, P.rowptr, P.colidx);
+    if (nn)
+        k_fill_colidx<<<nblk(nn * 32, 256), 256, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.colsrc,
+                                                                  P.rowlen, P.rowptr, P.colidx);
     FS_TRY(dalloc(c, &P.diag_rowptr, (size_t)n + 1));
     FS_TRY(dalloc(c, &P.diag_colidx, (size_t)n));
     k_diag_pattern<<<nblk(n + 1, 256), 256, 0, c->stream>>>(n, P.diag_rowptr, P.diag_colidx);

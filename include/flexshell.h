@@ -140,6 +140,16 @@ int fs_mass(fs_ctx *ctx, int assembler, int64_t nrows, int64_t *nnz_out);
 /* The matrix of the last fs_stiffness / fs_mass call into caller memory:
  * colptr[nrows+1], rowval[nnz], nzval[nnz], 1-based CSC.  Any pointer may be NULL. */
 int fs_matrix_copy(fs_ctx *ctx, int64_t *colptr, int64_t *rowval, double *nzval);
+/* Two-phase stiffness into host arrays for the pattern-keeping assembler
+ * (FS_ASM_SPARSE, also the FF block with nrows = nfreedofs): fs_pattern builds
+ * (or reuses) the pattern for `nrows` and returns the number of stored entries,
+ * so that the caller can allocate colptr[nrows+1], rowval[nnz], nzval[nnz];
+ * fs_stiffness_copy then assembles the values and fills the three arrays
+ * (1-based CSC == CSR), the pattern copy running on a second stream while the
+ * element and gather kernels run.  Results equal fs_stiffness + fs_matrix_copy. */
+int fs_pattern(fs_ctx *ctx, int64_t nrows, int64_t *nnz_out);
+int fs_stiffness_copy(fs_ctx *ctx, int precision, int64_t nrows, int64_t *colptr, int64_t *rowval,
+                      double *nzval);
 /* Device pointers of the last matrix (0-based CSR; valid until the next call). */
 int fs_matrix_device(fs_ctx *ctx, const int64_t **rowptr, const int32_t **colidx,
                      const double **vals, int64_t *nrows, int64_t *nnz);

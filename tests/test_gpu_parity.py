@@ -407,3 +407,23 @@ def test_compensated_mixed_matches_oracle(quads):
     assert e64 <= 1e-13 * scale
     assert ec <= 1e-12 * scale and ec <= em
     femm.close()
+
+
+@pytest.mark.parametrize("precision", [F.FS_FP64, F.FS_MIXED])
+def test_two_phase_copy_equals_stiffness_and_copy(precision):
+    import ctypes
+    from flexshell._lib import ptr
+    d = PB.scordelis_lo(True, 6)
+    P, femm, geom0, dchi = homog_pair(d, True)
+    K = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi, precision=precision)
+    n = dchi.nalldofs()
+    nnz = ctypes.c_int64()
+    femm.ctx.call("fs_pattern", n, ctypes.byref(nnz))
+    assert nnz.value == K.nnz
+    colptr = np.empty(n + 1, dtype=np.int64)
+    rowval = np.empty(nnz.value, dtype=np.int64)
+    nzval = np.empty(nnz.value)
+    femm.ctx.call("fs_stiffness_copy", precision, n, ptr(colptr), ptr(rowval), ptr(nzval))
+    assert np.array_equal(colptr - 1, K.indptr) and np.array_equal(rowval - 1, K.indices)
+    assert np.array_equal(nzval, K.data)
+    femm.close()
