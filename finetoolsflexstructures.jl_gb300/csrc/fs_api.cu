@@ -56,8 +56,17 @@ static void free_pattern(PatternDev &P)
     dfree(&P.nbr_off); dfree(&P.nbr); dfree(&P.pair_slots); dfree(&P.colpos); dfree(&P.colsrc); dfree(&P.rowlen);
     dfree(&P.sl_off); dfree(&P.sl_ent);
     dfree(&P.rowptr); dfree(&P.colidx); dfree(&P.diag_rowptr); dfree(&P.diag_colidx);
+    dfree(&P.tmp_cnt); dfree(&P.tmp_owner);
+    P = PatternDev();
+}
+
+// invalidate the pattern (new mesh or dof numbering) keeping its buffers for
+// the next build: no device free or allocation between assemblies
+static void reset_pattern(PatternDev &P)
+{
     P.n = -1;
     P.nnz = 0;
+    P.maxlen = 0;
 }
 
 static void free_mesh(MeshDev &m)
@@ -199,6 +208,7 @@ int fs_ctx_destroy(fs_ctx *c)
     if (x.graph) cudaGraphDestroy(x.graph);
     dfree(&x.U); dfree(&x.V); dfree(&x.A); dfree(&x.F); dfree(&x.cU); dfree(&x.cV);
     dfree(&x.invMC); dfree(&x.C); dfree(&x.vals32); dfree(&x.U32);
+    dfree(&x.blk); dfree(&x.xp); dfree(&x.pad_of_dof);
     cudaFree(c->d_status);
     for (int k = 0; k < 4; k++)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
@@ -242,7 +252,8 @@ int fs_mesh_set(fs_ctx *c, int elem_type, int64_t nnodes, const double *xyz, int
         return set_err(c, FS_ERR_UNSUPPORTED, "mesh too large (elements < 2^29, nodes < 2^31)");
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
     free_mesh(c->mesh);
-    free_pattern(c->pat);
+    reset_pattern(c->pat);
+    c->mat_rowptr = nullptr;
     free_beam(c);
     c->batch = fs_ctx::Batch();
     c->normals_ready = false;
@@ -308,7 +319,7 @@ int fs_dofs_set(fs_ctx *c, const int64_t *dofnums)
     if (c->mesh.etype < 0) return set_err(c, FS_ERR_STATE, "no mesh: call fs_mesh_set first");
     MeshDev &m = c->mesh;
     if (m.nnodes && !dofnums) return set_err(c, FS_ERR_BAD_INPUT, "missing dof numbers");
-    free_pattern(c->pat);
+    reset_pattern(c->pat);
     c->ex.ready = false;
     c->mat_rowptr = nullptr;
     size_t ndof = (size_t)(6 * m.nnodes);

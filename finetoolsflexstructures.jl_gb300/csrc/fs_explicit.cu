@@ -39,6 +39,37 @@ __global__ void k_cd_disp(int64_t n, double dt, double dt2_2, double *U, double 
     if (U32) U32[i] = (float)t;
 }
 
+// the same displacement update writing the node-padded copy read by the
+// block product (entries of excluded dofs stay zero)
+template <class VT>
+__global__ void k_cd_disp_pad(int64_t n, double dt, double dt2_2, double *U, double *cU, const double *V,
+                              const double *A, const int32_t *pad_of_dof, VT *xp)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double y = (dt * V[i] + dt2_2 * A[i]) - cU[i];
+    double u = U[i];
+    double t = u + y;
+    cU[i] = (t - u) - y;
+    U[i] = t;
+    const int32_t q = pad_of_dof[i];
+    if (q >= 0) xp[q] = (VT)t;
+}
+
+// six contiguous values (8-byte aligned floats, 16-byte aligned doubles)
+__device__ __forceinline__ void load6(const float *p, float v[6])
+{
+    const float2 *q = reinterpret_cast<const float2 *>(p);
+    const float2 a = q[0], b = q[1], c = q[2];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
+}
+__device__ __forceinline__ void load6(const double *p, double v[6])
+{
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    const double2 a = q[0], b = q[1], c = q[2];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
+}
+
 __device__ __forceinline__ void kahan_add(double &s, double &c, double incr)
 {
     double y = incr - c;
@@ -75,6 +106,87 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_rows(int64_t n, const int64_t *ro
     }
 }
 
+// K U from the 6x6 node blocks, fused with the force, acceleration and
+// velocity updates: six threads per node (one per component row, five nodes
+// per warp); the threads of a node read each block as 144 (float) or 288
+// (double) contiguous bytes.
+template <class VT>
+__global__ void __launch_bounds__(CD_TPB) k_cd_bsr(int64_t nnodes, int64_t n, const int32_t *dof,
+                                                 const int64_t *nbr_off, const int32_t *nbr, const VT *blk,
+                                                 const VT *xp, double *V, double *cV, double *A, const double *C,
+                                                 const double *invMC, double dt_2)
+{
+    const int t = threadIdx.x & 31;
+    if (t >= 30) return;
+    const int64_t r = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 5 + t / 6;
+    const int i = t % 6;
+    if (r >= nnodes) return;
+    const int32_t d = dof[(int64_t)i * nnodes + r];
+    if (d > n) return;
+    VT sv = 0;
+    for (int64_t b = nbr_off[r], be = nbr_off[r + 1]; b < be; b++) {
+        VT kv[6], xv[6];
+        load6(blk + b * 36 + i * 6, kv);
+        load6(xp + (int64_t)nbr[b] * 6, xv);
+#pragma unroll
+        for (int j = 0; j < 6; j++) sv += kv[j] * xv[j];
+    }
+    const int64_t row = d - 1;
+    const double s = (double)sv;
+    double a = A[row], v = V[row], cv = cV[row];
+    const double f = -(s + C[row] * (v + dt_2 * a));
+    kahan_add(v, cv, dt_2 * a);
+    a = invMC[row] * f;
+    kahan_add(v, cv, dt_2 * a);
+    A[row] = a;
+    V[row] = v;
+    cV[row] = cv;
+}
+
+// block (node r, neighbour slot s), entry (i, j) = K[dof(r,i), dof(nbr,j)]
+// (zero where either dof is excluded or the matrix has no entry), found by
+// binary search in the sorted CSR row; one warp per node
+template <class VT>
+__global__ void k_bsr_fill(int64_t nnodes, int64_t n, const int32_t *dof, const int64_t *rowptr,
+                           const int32_t *colidx, const double *vals, const int64_t *nbr_off, const int32_t *nbr,
+                           VT *blk)
+{
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= nnodes) return;
+    const int64_t off = nbr_off[r];
+    const int ns = (int)(nbr_off[r + 1] - off);
+    for (int idx = lane; idx < ns * 36; idx += 32) {
+        const int sl = idx / 36, ij = idx - 36 * sl, i = ij / 6, j = ij - 6 * i;
+        const int32_t d = dof[(int64_t)i * nnodes + r];
+        const int32_t e = dof[(int64_t)j * nnodes + nbr[off + sl]];
+        double v = 0.0;
+        if (d <= n && e <= n) {
+            int64_t lo = rowptr[d - 1], hi = rowptr[d] - 1;
+            while (lo <= hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                const int32_t cc = colidx[mid];
+                if (cc == e - 1) {
+                    v = vals[mid];
+                    break;
+                }
+                if (cc < e - 1) lo = mid + 1; else hi = mid - 1;
+            }
+        }
+        blk[(off + sl) * 36 + ij] = (VT)v;
+    }
+}
+
+__global__ void k_pad_map(int64_t nnodes, int64_t n, const int32_t *dof, int32_t *pad_of_dof)
+{
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 6 * nnodes) return;
+    const int64_t r = q / 6;
+    const int k = (int)(q - 6 * r);
+    const int32_t d = dof[(int64_t)k * nnodes + r];
+    if (d <= n) pad_of_dof[d - 1] = (int32_t)q;
+}
+
 static int enqueue_steps(fs_ctx *c, int64_t nsteps)
 {
     auto &x = c->ex;
@@ -82,6 +194,27 @@ static int enqueue_steps(fs_ctx *c, int64_t nsteps)
     double dt = x.dt;
     unsigned g1 = (unsigned)((n + CD_TPB - 1) / CD_TPB);
     unsigned g2 = (unsigned)((n * CD_LANES + CD_TPB - 1) / CD_TPB);
+    if (x.bsr) {
+        const unsigned gb = (unsigned)((x.nnodes + 39) / 40);  // 5 nodes per warp, 8 warps per block
+        for (int64_t s = 0; s < nsteps; s++) {
+            if (x.precision == FS_FP64) {
+                k_cd_disp_pad<double><<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A,
+                                                                     x.pad_of_dof, (double *)x.xp);
+                k_cd_bsr<double><<<gb, CD_TPB, 0, c->stream>>>(x.nnodes, n, c->mesh.dof, c->pat.nbr_off,
+                                                                c->pat.nbr, (const double *)x.blk,
+                                                                (const double *)x.xp, x.V, x.cV, x.A, x.C,
+                                                                x.invMC, dt / 2);
+            } else {
+                k_cd_disp_pad<float><<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A,
+                                                                    x.pad_of_dof, (float *)x.xp);
+                k_cd_bsr<float><<<gb, CD_TPB, 0, c->stream>>>(x.nnodes, n, c->mesh.dof, c->pat.nbr_off,
+                                                               c->pat.nbr, (const float *)x.blk,
+                                                               (const float *)x.xp, x.V, x.cV, x.A, x.C,
+                                                               x.invMC, dt / 2);
+            }
+        }
+        return cuda_check(c, cudaGetLastError(), "explicit step launch");
+    }
     for (int64_t s = 0; s < nsteps; s++) {
         bool single = x.precision != FS_FP64;
         k_cd_disp<<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A, single ? x.U32 : nullptr);
@@ -272,7 +405,34 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
     FS_CUDA(c, cudaMemsetAsync(x.cV, 0, bn, c->stream));
     FS_CUDA(c, cudaMemcpyAsync(x.invMC, invMC, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     FS_CUDA(c, cudaMemcpyAsync(x.C, C, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    if (precision == FS_MIXED) {
+    // 6x6 node-block form when the pattern of the current mesh is there (its
+    // neighbour lists are the block rows); otherwise the CSR product
+    x.bsr = c->pat.n >= 0 && c->pat.nbr_off && c->mesh.nnodes > 0;
+    if (x.bsr) {
+        const MeshDev &m = c->mesh;
+        const int64_t nn = m.nnodes;
+        int64_t nbr_total = 0;
+        FS_CUDA(c, cudaMemcpyAsync(&nbr_total, c->pat.nbr_off + nn, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+        FS_CUDA(c, cudaStreamSynchronize(c->stream));
+        const size_t es = precision == FS_FP64 ? 8 : 4;
+        dfree(&x.blk);
+        dfree(&x.xp);
+        FS_CUDA(c, cudaMalloc(&x.blk, es * 36 * (size_t)std::max<int64_t>(nbr_total, 1)));
+        FS_CUDA(c, cudaMalloc(&x.xp, es * 6 * (size_t)nn));
+        FS_CUDA(c, cudaMemsetAsync(x.xp, 0, es * 6 * (size_t)nn, c->stream));
+        FS_TRY(dalloc(c, &x.pad_of_dof, (size_t)n));
+        FS_CUDA(c, cudaMemsetAsync(x.pad_of_dof, 0xff, sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1), c->stream));
+        k_pad_map<<<(unsigned)((6 * nn + 255) / 256), 256, 0, c->stream>>>(nn, n, m.dof, x.pad_of_dof);
+        const unsigned gw = (unsigned)((nn * 32 + 255) / 256);
+        if (precision == FS_FP64)
+            k_bsr_fill<double><<<gw, 256, 0, c->stream>>>(nn, n, m.dof, c->mat_rowptr, c->mat_colidx, c->vals,
+                                                           c->pat.nbr_off, c->pat.nbr, (double *)x.blk);
+        else
+            k_bsr_fill<float><<<gw, 256, 0, c->stream>>>(nn, n, m.dof, c->mat_rowptr, c->mat_colidx, c->vals,
+                                                          c->pat.nbr_off, c->pat.nbr, (float *)x.blk);
+        FS_CUDA(c, cudaGetLastError());
+        x.nnodes = nn;
+    } else if (precision == FS_MIXED) {
         FS_TRY(dalloc(c, &x.U32, (size_t)n));
         FS_TRY(dalloc(c, &x.vals32, (size_t)c->mat_nnz));
         if (c->mat_nnz)

@@ -79,6 +79,12 @@ struct PatternDev {
     int32_t *colidx = nullptr;   // nnz, 0-based
     int64_t *diag_rowptr = nullptr;  // diagonal pattern (n + 1)
     int32_t *diag_colidx = nullptr;  // n
+    int64_t *tmp_cnt = nullptr;      // temporaries of the symbolic phase
+    int32_t *tmp_owner = nullptr;
+    // allocated capacities (elements): a rebuild reuses the buffers that fit
+    size_t cap_nbr_off = 0, cap_nbr = 0, cap_pair_slots = 0, cap_colpos = 0, cap_colsrc = 0, cap_rowlen = 0,
+           cap_sl_off = 0, cap_sl_ent = 0, cap_rowptr = 0, cap_colidx = 0, cap_diag_rowptr = 0,
+           cap_diag_colidx = 0, cap_tmp_cnt = 0, cap_tmp_owner = 0;
 };
 
 }  // namespace fs
@@ -137,6 +143,12 @@ struct fs_ctx {
         double *invMC = nullptr, *C = nullptr;
         float *vals32 = nullptr;
         float *U32 = nullptr;  // float copy of U read by the float restoring force
+        // 6x6 node-block form of K (block rows = the pattern's neighbour lists)
+        bool bsr = false;
+        int64_t nnodes = 0;
+        void *blk = nullptr;          // nbr_total x 36 (float or double)
+        void *xp = nullptr;           // displacement copy, 6 per node (float or double)
+        int32_t *pad_of_dof = nullptr;  // dof -> node * 6 + component
         bool ready = false;
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
@@ -232,6 +244,14 @@ template <class T> void dfree(T **p)
 {
     if (*p) cudaFree(*p);
     *p = nullptr;
+}
+// device buffer of at least n elements, reused when its capacity suffices
+template <class T> int grow(fs_ctx *c, T **p, size_t *cap, size_t n)
+{
+    if (*p && *cap >= n && n > 0) return FS_OK;
+    const int st = dalloc(c, p, n);
+    *cap = st == FS_OK ? (n ? n : 1) : 0;
+    return st;
 }
 
 }  // namespace fs

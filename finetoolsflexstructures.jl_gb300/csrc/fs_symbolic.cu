@@ -467,31 +467,32 @@ int build_pattern(fs_ctx *c, int64_t n)
     int64_t nn = m.nnodes;
     if (n > 0x7fffffffLL) return set_err(c, FS_ERR_UNSUPPORTED, "matrix size above 2^31-1");
     int64_t *cnt = nullptr;
-    FS_TRY(dalloc(c, &cnt, (size_t)std::max<int64_t>(nn, n)));
+    FS_TRY(grow(c, &P.tmp_cnt, &P.cap_tmp_cnt, (size_t)std::max<int64_t>(nn, n)));
+    cnt = P.tmp_cnt;
     if (nn) k_count_nbrs<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, m.nen, m.pp, m.pair_e, m.conn, cnt, c->d_status);
-    FS_TRY(dalloc(c, &P.nbr_off, (size_t)nn + 1));
+    FS_TRY(grow(c, &P.nbr_off, &P.cap_nbr_off, (size_t)nn + 1));
     int64_t nbr_total = 0;
     FS_TRY(exclusive_scan_i64(c, cnt, P.nbr_off, nn, &nbr_total));
     int bits = 0;
     FS_TRY(read_status(c, &bits));
     if (bits & DEV_NEIGHBORS) {
-        cudaFree(cnt);
         return set_err(c, FS_ERR_UNSUPPORTED, "more than 255 neighbour nodes at one node");
     }
-    FS_TRY(dalloc(c, &P.nbr, (size_t)nbr_total));
-    FS_TRY(dalloc(c, &P.pair_slots, (size_t)m.npairs));
-    FS_TRY(dalloc(c, &P.colpos, (size_t)nbr_total * 6));
-    FS_TRY(dalloc(c, &P.colsrc, (size_t)nbr_total * 6));
-    FS_TRY(dalloc(c, &P.rowlen, (size_t)nn));
-    FS_TRY(dalloc(c, &P.sl_off, (size_t)nbr_total));
-    FS_TRY(dalloc(c, &P.sl_ent, (size_t)(m.npairs * m.nen)));
+    FS_TRY(grow(c, &P.nbr, &P.cap_nbr, (size_t)nbr_total));
+    FS_TRY(grow(c, &P.pair_slots, &P.cap_pair_slots, (size_t)m.npairs));
+    FS_TRY(grow(c, &P.colpos, &P.cap_colpos, (size_t)nbr_total * 6));
+    FS_TRY(grow(c, &P.colsrc, &P.cap_colsrc, (size_t)nbr_total * 6));
+    FS_TRY(grow(c, &P.rowlen, &P.cap_rowlen, (size_t)nn));
+    FS_TRY(grow(c, &P.sl_off, &P.cap_sl_off, (size_t)nbr_total));
+    FS_TRY(grow(c, &P.sl_ent, &P.cap_sl_ent, (size_t)(m.npairs * m.nen)));
     if (nn)
         k_fill_nbrs<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, m.nen, n, m.pp, m.pair_e, m.conn, m.dof, P.nbr_off,
                                                          P.nbr, P.pair_slots, P.colpos, P.colsrc, P.rowlen,
                                                          P.sl_off, P.sl_ent);
     // row lengths by dof
     int32_t *owner = nullptr;
-    FS_TRY(dalloc(c, &owner, (size_t)n));
+    FS_TRY(grow(c, &P.tmp_owner, &P.cap_tmp_owner, (size_t)n));
+    owner = P.tmp_owner;
     FS_CUDA(c, cudaMemsetAsync(owner, 0, sizeof(int32_t) * std::max<int64_t>(n, 1), c->stream));
     FS_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * std::max<int64_t>(n, 1), c->stream));
     if (nn) k_row_lengths<<<nblk(6 * nn, 256), 256, 0, c->stream>>>(nn, n, m.dof, P.rowlen, cnt, owner, c->d_status);
@@ -504,19 +505,17 @@ int build_pattern(fs_ctx *c, int64_t n)
         for (int64_t i = 0; i < nn; i++) mx = rl[i] > mx ? rl[i] : mx;
         P.maxlen = mx;
     }
-    FS_TRY(dalloc(c, &P.rowptr, (size_t)n + 1));
+    FS_TRY(grow(c, &P.rowptr, &P.cap_rowptr, (size_t)n + 1));
     int64_t nnz = 0;
     FS_TRY(exclusive_scan_i64(c, cnt, P.rowptr, n, &nnz));
     FS_TRY(read_status(c, &bits));
-    cudaFree(owner);
-    cudaFree(cnt);
     if (bits & DEV_BAD_DOF) return set_err(c, FS_ERR_BAD_INPUT, "two dofs share one dof number");
-    FS_TRY(dalloc(c, &P.colidx, (size_t)nnz));
+    FS_TRY(grow(c, &P.colidx, &P.cap_colidx, (size_t)nnz));
     if (nn)
         k_fill_colidx<<<nblk(nn * 32, 256), 256, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.colsrc,
                                                                   P.rowlen, P.rowptr, P.colidx);
-    FS_TRY(dalloc(c, &P.diag_rowptr, (size_t)n + 1));
-    FS_TRY(dalloc(c, &P.diag_colidx, (size_t)n));
+    FS_TRY(grow(c, &P.diag_rowptr, &P.cap_diag_rowptr, (size_t)n + 1));
+    FS_TRY(grow(c, &P.diag_colidx, &P.cap_diag_colidx, (size_t)n));
     k_diag_pattern<<<nblk(n + 1, 256), 256, 0, c->stream>>>(n, P.diag_rowptr, P.diag_colidx);
     FS_CUDA(c, cudaGetLastError());
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
