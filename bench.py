@@ -268,12 +268,24 @@ def explicit_c5(torch, device=0, n=512, nsteps=10000, iters=200):
         out["steps_per_s_" + name] = nsteps / (ms * 1e-3)
         out["ms_per_step_" + name] = ms / nsteps
     U32, U64 = finals[_abi.FS_MIXED], finals[_abi.FS_FP64]
+    # algorithmic bytes of one step on node blocks: the blocks (36 values and a
+    # neighbour index each), per node its block range and dofs, per dof the
+    # double state read and written by the two kernels and the displacement
+    # copy (value size es)
+    import scipy.sparse as sps
+    nn_ = xyz.shape[0]
+    rows_ = np.repeat(np.arange(conn.shape[0]), conn.shape[1])
+    inc = sps.csr_matrix((np.ones(rows_.size), (rows_, conn.ravel() - 1)), shape=(conn.shape[0], nn_))
+    nblocks = int((inc.T @ inc).nnz)
+    bsr_bytes = lambda es: nblocks * (36 * es + 4) + nn_ * (8 + 6 * 4) + nfree * (13 * 8 + 4 + es)
     out.update({"elements": conn.shape[0], "dofs": nfree, "nnz": nnz.value, "steps": nsteps,
                 "omega_max": om.value, "dt": dt, "power_iterations": iters,
                 "final_u_rel_err_mixed_vs_fp64": float(np.abs(U32 - U64).max() / np.abs(U64).max()),
                 "final_u_max": float(np.abs(U64).max()),
-                "bytes_per_step_mixed": nnz.value * 8 + nfree * 8 * 12,
-                "bytes_per_step_fp64": nnz.value * 12 + nfree * 8 * 12})
+                "format": "6x6 node blocks (block rows = node neighbour lists)", "blocks": nblocks,
+                "bytes_per_step_mixed": bsr_bytes(4), "bytes_per_step_fp64": bsr_bytes(8),
+                "hbm_gbs_mixed": bsr_bytes(4) * out["steps_per_s_mixed"] / 1e9,
+                "hbm_gbs_fp64": bsr_bytes(8) * out["steps_per_s_fp64"] / 1e9})
     ctx.close()
     return out
 

@@ -361,6 +361,7 @@ int autotune_shell(fs_ctx *c, int precision)
     int best_w = 0;
     best_ms = 1e30f;
     for (int w : {4, 8, 16}) {
+        if (gather_smem_bytes(precision, m.nen, w) > SMEM_MAX) continue;
         c->tune.gather_warps = w;
         float ms = 0.f;
         FS_TRY(time_best(c, run_gather_once, precision, &ms));
