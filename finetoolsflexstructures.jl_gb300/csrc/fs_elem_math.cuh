@@ -623,10 +623,11 @@ FS_HD void q4_bs(const R X[4], const R Y[4], R r, R s, R Bs[2][4][5])
 // Q4 element-level constants shared by the four quadrature points.
 struct Q4Elem {
     double Xr[4][3];   // node coordinates relative to the centroid
-    double h2;         // squared diameter (max distance from node 1)
+    double stab;       // shear stabilisation t^2 / (t^2 + c h^2), h = max distance from node 1
 };
 
-FS_HD void q4_prepare(const ElemIn<4> &in, Q4Elem &qe)
+// `t` is the element (or layup) thickness, `stab_c` the stabilisation constant.
+FS_HD void q4_prepare(const ElemIn<4> &in, double t, double stab_c, Q4Elem &qe)
 {
     double cen[3] = {0, 0, 0};
     for (int a = 0; a < 4; a++)
@@ -641,7 +642,7 @@ FS_HD void q4_prepare(const ElemIn<4> &in, Q4Elem &qe)
             mx = dd > mx ? dd : mx;
         }
     }
-    qe.h2 = mx;
+    qe.stab = t * t / (t * t + stab_c * mx);
 }
 
 // Rows of quadrature point j (8 rows: membrane+bending 6, shear 2) on the
@@ -660,9 +661,6 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         J0[c] = qe.Xr[0][c] * gp[0][0] + qe.Xr[1][c] * gp[1][0] + qe.Xr[2][c] * gp[2][0] + qe.Xr[3][c] * gp[3][0];
         J1[c] = qe.Xr[0][c] * gp[0][1] + qe.Xr[1][c] * gp[1][1] + qe.Xr[2][c] * gp[2][1] + qe.Xr[3][c] * gp[3][1];
     }
-    double nJ[3];
-    cross3(J0, J1, nJ);
-    double Jac = sqrt(dot3(nJ, nJ));
     double e[3][3];
     make_frame(J0, J1, e);
     // element coordinates (centroid relative) and basis gradients
@@ -676,6 +674,13 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         }
     }
     R J0r[3] = {(R)J0[0], (R)J0[1], (R)J0[2]}, J1r[3] = {(R)J1[0], (R)J1[1], (R)J1[2]};
+    // surface Jacobian |J0 x J1| in the working precision
+    R Jac;
+    {
+        R nJ[3];
+        cross3(J0r, J1r, nJ);
+        Jac = sqrt(dot3(nJ, nJ));
+    }
     R G11 = dot3(J0r, J0r), G12 = dot3(J0r, J1r), G22 = dot3(J1r, J1r);
     R detG = G11 * G22 - G12 * G12;
     if (detG == (R)0) return 4;
@@ -696,13 +701,12 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     build_map<R, 4>(e, A, g, M);
     R sh[2][4][5];
     q4_bs<R>(X, Y, (R)xi, (R)eta, sh);
-    double t = COMP ? gc->thickness : in.t;
-    double stab = t * t / (t * t + mc.stab_c * qe.h2);
+    const R stab = (R)qe.stab;
     if constexpr (!COMP) {
-        R tr_ = (R)t, jr = (R)Jac;
+        R tr_ = (R)in.t, jr = Jac;
         R btx[3][4], bty[3][4];
         homog_mb_rows<R, 4>(M, mc.Lps, sqrt(tr_ * jr), sqrt(tr_ * tr_ * tr_ / 12 * jr), rows, rs, btx, bty);
-        R ws = sqrt(tr_ * (R)stab * jr);
+        R ws = sqrt(tr_ * stab * jr);
         R l00 = (R)mc.Lt[lp(0, 0)], l10 = (R)mc.Lt[lp(1, 0)], l11 = (R)mc.Lt[lp(1, 1)];
         for (int r = 0; r < 2; r++) {
             R f0 = r == 0 ? ws * l00 : (R)0, f1 = ws * (r == 0 ? l10 : l11);
@@ -732,9 +736,9 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         layup_angle(e, gc->csmat, lm, ln);
         rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[0]);
         rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[3]);
-        mix_rows<R, 4, 6>(gc->L6, sqrt((R)Jac), mb, (R(*)[4][5])mixed[0]);
+        mix_rows<R, 4, 6>(gc->L6, sqrt(Jac), mb, (R(*)[4][5])mixed[0]);
         rotate2<R, 4>(lm, ln, sh);
-        mix_rows<R, 4, 2>(gc->LH, sqrt((R)stab * (R)Jac), sh, (R(*)[4][5])mixed[6]);
+        mix_rows<R, 4, 2>(gc->LH, sqrt(stab * Jac), sh, (R(*)[4][5])mixed[6]);
         for (int r = 0; r < 8; r++) expand_row<R, 4>(M, (const R(*)[5])mixed[r], rows + r * rs);
     }
     // drilling traces: sum over rows of |b|^2 - (b.n)^2 on the rotation block

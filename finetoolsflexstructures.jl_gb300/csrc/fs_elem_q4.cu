@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
     Q4Elem qe;
     if (active) {
         load_elem<4>(m, r, in);
-        if (qp == 0) q4_prepare(in, qe);
+        if (qp == 0) q4_prepare(in, COMP ? m.groups[in.group].thickness : in.t, mc.stab_c, qe);
     }
     {
         const int src = (threadIdx.x & 31) & ~3;
@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
         for (int a = 0; a < 4; a++)
 #pragma unroll
             for (int c = 0; c < 3; c++) qe.Xr[a][c] = __shfl_sync(0xffffffffu, qe.Xr[a][c], src);
-        qe.h2 = __shfl_sync(0xffffffffu, qe.h2, src);
+        qe.stab = __shfl_sync(0xffffffffu, qe.stab, src);
     }
     if (active) {
         const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;

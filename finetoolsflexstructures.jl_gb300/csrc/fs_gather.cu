@@ -29,7 +29,6 @@ __device__ __forceinline__ void cp_async_wait_all()
 {
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 
 // exact float -> double built from the bit pattern with integer operations
 // only (zeros, subnormals, normals, inf and nan), so that no conversion
@@ -94,135 +93,9 @@ template <class R, int NEN> struct GatherSmem {
     static constexpr int PER_WARP = G_MAXP * NEN * 36 * (int)sizeof(R) + 512;
 };
 
-// scalar data of one node
-struct GNode {
-    int64_t r;
-    int32_t d[6];
-    int L;
-    int64_t off, off_next, pb, pe;
-    bool any;
-};
-
-__device__ __forceinline__ void gnode_load(GNode &g, const MeshDev &m, const PatternDev &P, int64_t r, int64_t n)
-{
-    g.r = r;
-    g.any = false;
-    if (r >= m.nnodes) return;
-#pragma unroll
-    for (int k = 0; k < 6; k++) g.d[k] = m.dof[(int64_t)k * m.nnodes + r];
-    g.L = P.rowlen[r];
-    g.off = P.nbr_off[r];
-    g.off_next = P.nbr_off[r + 1];
-    g.pb = m.pp[r];
-    g.pe = m.pp[r + 1];
-#pragma unroll
-    for (int k = 0; k < 6; k++) g.any |= (g.d[k] <= n);
-}
-
-// Single-batch node: entries to shared memory, the lane's column data, and
-// the asynchronous copies of all its slabs (completed by the caller's wait).
-template <class R, int NEN, int G_COLS>
-__device__ __forceinline__ void gnode_stage(const GNode &g, const MeshDev &m, const PatternDev &P, const R *ke,
-                                            R *stage, uint16_t *sent, int lane, int (&kcol)[G_COLS],
-                                            int (&cur)[G_COLS], int (&last)[G_COLS])
-{
-    constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
-    constexpr int BCH = 36 * (int)sizeof(R) / 16, CH = NEN * BCH, CPL = (CH + 31) / 32;
-    const int ntot = (int)(g.pe - g.pb) * NEN;
-    const uint16_t *ent = P.sl_ent + g.pb * NEN;
-    for (int i = lane; i < ntot; i += 32) sent[i] = ent[i];
-    const int nslots = (int)(g.off_next - g.off);
-#pragma unroll
-    for (int c = 0; c < G_COLS; c++) {
-        const int j = lane + 32 * c;
-        kcol[c] = 0;
-        cur[c] = 0;
-        last[c] = 0;
-        if (j < g.L) {
-            const int cs = (int)P.colsrc[g.off * 6 + j];
-            const int sl = cs / 6;
-            kcol[c] = cs - 6 * sl;
-            cur[c] = (int)P.sl_off[g.off + sl];
-            last[c] = sl + 1 < nslots ? (int)P.sl_off[g.off + sl + 1] : ntot;
-        }
-    }
-    const int cnt = (int)(g.pe - g.pb);
-    for (int q = 0; q < cnt; q++) {
-        const int32_t pel = m.pair_e[g.pb + q];
-        const int a = pel & 3;
-        const R *base = ke + (int64_t)(pel >> 2) * ND2;
-#pragma unroll
-        for (int t = 0; t < CPL; t++) {
-            const int ch = lane + 32 * t;
-            if (ch < CH) {
-                const int bb = ch / BCH, cw = ch - bb * BCH;
-                // block (a, bb) of the element: stored as itself or as its mirror
-                const R *src = base + ub(min(a, bb), max(a, bb), NEN) * 36;
-                cp_async16(reinterpret_cast<char *>(stage + q * SLAB + bb * 36) + 16 * cw,
-                           reinterpret_cast<const char *>(src) + 16 * cw);
-            }
-        }
-    }
-    cp_async_commit();
-}
-
-// Sums of a staged single-batch node (ascending pair order) and its rows.
-template <class R, int NEN, int G_COLS>
-__device__ __forceinline__ void gnode_finish(const GNode &g, const PatternDev &P, int64_t n, const R *stage,
-                                             const uint16_t *sent, int lane, const int (&kcol)[G_COLS],
-                                             int (&cur)[G_COLS], const int (&last)[G_COLS], double *vals)
-{
-    typedef typename GatherAcc<R>::T A;
-    constexpr int SLAB = NEN * 36;
-    constexpr bool SINGLE = sizeof(A) == 4;
-    A hi[G_COLS][6], lo[G_COLS][6];
-#pragma unroll
-    for (int c = 0; c < G_COLS; c++) {
-#pragma unroll
-        for (int k = 0; k < 6; k++) {
-            hi[c][k] = 0;
-            lo[c][k] = 0;
-        }
-        while (cur[c] < last[c]) {
-            const uint32_t e = sent[cur[c]];
-            const int q = (int)(e & 63u);
-            const int b = (int)((e >> 6) & 3u);
-            // entry (krow, kcol) of block (a_q, b); a mirrored block is read transposed
-            const bool tr = (e >> 8) & 1u;
-            const R *src = stage + q * SLAB + b * 36 + (tr ? 6 * kcol[c] : kcol[c]);
-            const int st = tr ? 1 : 6;
-#pragma unroll
-            for (int k = 0; k < 6; k++) gather_add(hi[c][k], lo[c][k], src[st * k]);
-            cur[c]++;
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        if (g.d[k] > n) continue;
-        double *o = vals + P.rowptr[g.d[k] - 1];
-#pragma unroll
-        for (int c = 0; c < G_COLS; c++) {
-            const int j = lane + 32 * c;
-            if (j >= g.L) continue;
-            double v;
-            if (SINGLE) {
-                // hi + lo: exact in double unless their exponents are more than
-                // 29 apart, then rounded once
-                v = f2d_fast((float)hi[c][k]);
-                if (lo[c][k] != (A)0) v += f2d_fast((float)lo[c][k]);
-            } else {
-                v = (double)hi[c][k];
-            }
-            o[j] = v;
-        }
-    }
-}
-
-// Any node: pairs staged G_MAXP at a time; rows longer than 32 G_COLS
-// positions accumulate in place in double.
-template <class R, int NEN, int G_COLS>
-__device__ void gnode_general(const GNode &gn, const MeshDev &m, const PatternDev &P, int64_t n, const R *ke,
-                              R *stage, uint16_t *sent, int lane, double *vals)
+template <class R, int NEN, int G_COLS, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
     typedef typename GatherAcc<R>::T A;
     constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
@@ -230,10 +103,24 @@ __device__ void gnode_general(const GNode &gn, const MeshDev &m, const PatternDe
     constexpr int BCH = 36 * (int)sizeof(R) / 16;  // 16-byte chunks per 6x6 block
     constexpr int CH = NEN * BCH;                   // 16-byte chunks per slab
     constexpr int CPL = (CH + 31) / 32;             // chunks per lane per pair
-    const int32_t *d = gn.d;
-    const int L = gn.L;
-    const int64_t off = gn.off, off_next = gn.off_next, off6 = off * 6;
-    const int64_t pb = gn.pb, pe = gn.pe;
+    extern __shared__ __align__(16) unsigned char gather_smem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t r = (int64_t)blockIdx.x * WARPS + w;
+    if (r >= m.nnodes) return;
+    unsigned char *wsm = gather_smem + (size_t)w * GatherSmem<R, NEN>::PER_WARP;
+    R *stage = reinterpret_cast<R *>(wsm);
+    uint16_t *sent = reinterpret_cast<uint16_t *>(wsm + G_MAXP * SLAB * sizeof(R));
+    // the node's scalar data: all independent loads issued together
+    int32_t d[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) d[k] = m.dof[(int64_t)k * m.nnodes + r];
+    const int L = P.rowlen[r];
+    const int64_t off = P.nbr_off[r], off_next = P.nbr_off[r + 1], off6 = off * 6;
+    const int64_t pb = m.pp[r], pe = m.pp[r + 1];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 6; k++) any |= (d[k] <= n);
+    if (!any) return;
     if (L <= 32 * G_COLS) {
         // the node's contribution entries into shared memory
         const int ntot = (int)(pe - pb) * NEN;
@@ -359,54 +246,14 @@ __device__ void gnode_general(const GNode &gn, const MeshDev &m, const PatternDe
     }
 }
 
-template <class R, int NEN, int G_COLS, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
-{
-    constexpr int SLAB = NEN * 36;
-    extern __shared__ __align__(16) unsigned char gather_smem[];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    // two nodes per warp: their loads, staging and sums overlap
-    const int64_t r0 = ((int64_t)blockIdx.x * WARPS + w) * 2;
-    if (r0 >= m.nnodes) return;
-    unsigned char *wsm = gather_smem + (size_t)w * 2 * GatherSmem<R, NEN>::PER_WARP;
-    R *stage[2];
-    uint16_t *sent[2];
-#pragma unroll
-    for (int u = 0; u < 2; u++) {
-        unsigned char *b = wsm + (size_t)u * GatherSmem<R, NEN>::PER_WARP;
-        stage[u] = reinterpret_cast<R *>(b);
-        sent[u] = reinterpret_cast<uint16_t *>(b + G_MAXP * SLAB * sizeof(R));
-    }
-    GNode g[2];
-    gnode_load(g[0], m, P, r0, n);
-    gnode_load(g[1], m, P, r0 + 1, n);
-    bool fast[2];
-#pragma unroll
-    for (int u = 0; u < 2; u++) fast[u] = g[u].any && g[u].L <= 32 * G_COLS && g[u].pe - g[u].pb <= G_MAXP;
-    int kcol[2][G_COLS], cur[2][G_COLS], last[2][G_COLS];
-#pragma unroll
-    for (int u = 0; u < 2; u++)
-        if (fast[u]) gnode_stage<R, NEN, G_COLS>(g[u], m, P, ke, stage[u], sent[u], lane, kcol[u], cur[u], last[u]);
-    cp_async_wait_all();
-    __syncwarp();
-#pragma unroll
-    for (int u = 0; u < 2; u++)
-        if (fast[u]) gnode_finish<R, NEN, G_COLS>(g[u], P, n, stage[u], sent[u], lane, kcol[u], cur[u], last[u], vals);
-    __syncwarp();
-#pragma unroll
-    for (int u = 0; u < 2; u++)
-        if (g[u].any && !fast[u]) gnode_general<R, NEN, G_COLS>(g[u], m, P, n, ke, stage[u], sent[u], lane, vals);
-}
-
 template <class R, int NEN, int G_COLS, int W>
 static int gather_launch_w(fs_ctx *c, const R *ke, double *vals)
 {
     const MeshDev &m = c->mesh;
-    const size_t smem = (size_t)W * 2 * GatherSmem<R, NEN>::PER_WARP;
+    const size_t smem = (size_t)W * GatherSmem<R, NEN>::PER_WARP;
     auto kern = k_gather<R, NEN, G_COLS, W>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<nblk2((m.nnodes + 1) / 2, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
+    kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
     return FS_OK;
 }
 
@@ -426,11 +273,9 @@ static int gather_launch(fs_ctx *c, const R *ke, double *vals, int warps)
     return gather_launch_c<R, NEN, 4>(c, ke, vals, warps);
 }
 
-// dynamic shared memory of a gather block of `warps` warps
 size_t gather_smem_bytes(int precision, int nen, int warps)
 {
-    const size_t es = entry_bytes(precision);
-    return (size_t)warps * 2 * ((size_t)G_MAXP * nen * 36 * es + 512);
+    return (size_t)warps * ((size_t)G_MAXP * nen * 36 * entry_bytes(precision) + 512);
 }
 
 template <class R>

@@ -67,7 +67,7 @@ static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t n
             }
             in.t = thick[e];
             Q4Elem qe;
-            q4_prepare(in, qe);
+            q4_prepare(in, comp ? gc->thickness : in.t, mc.stab_c, qe);
             double tr[4] = {0, 0, 0, 0};
             for (int j = 0; j < 4; j++) {
                 double trj[4];
