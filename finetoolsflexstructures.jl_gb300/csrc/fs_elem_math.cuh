@@ -135,9 +135,21 @@ FS_HD void nodal_triad(const double e[3][3], const double n[3], bool valid, doub
     R[2][0] = -s * a1;           R[2][1] = s * a0;            R[2][2] = 1.0 - c * x;
 }
 
-// The triad in the working precision: the double-precision entries of
-// nodal_triad rounded to R.  The matrix has six distinct values up to sign,
-// so only those are rounded (the result equals rounding all nine).
+// sin(phi)/phi and (1 - cos(phi))/phi^2 in float for x = phi^2 <= 1: the
+// Taylor series to x^4 (truncation below x^5/11! < 3e-8, under half an ulp
+// of the results).
+FS_HD void sinc_cosc_f(float x, float &s, float &c)
+{
+    s = 1.0f - x * (1.0f / 6.0f - x * (1.0f / 120.0f - x * (1.0f / 5040.0f - x * (1.0f / 362880.0f))));
+    c = 0.5f - x * (1.0f / 24.0f - x * (1.0f / 720.0f - x * (1.0f / 40320.0f - x * (1.0f / 3628800.0f))));
+}
+
+// The triad in the working precision.  Double: nodal_triad.  Float: the
+// rotation vector a = e3 x n (a difference of nearly parallel unit vectors
+// on a smooth mesh) is formed in double from the double frame and rounded
+// once; the Rodrigues entries are evaluated from it in float, each within
+// about one float ulp of the rounded double entry.  Angles beyond one radian
+// (creases) take the double path.
 template <class R>
 FS_HD void nodal_triad_r(const double e[3][3], const double n[3], bool valid, R Ar[3][3])
 {
@@ -147,24 +159,35 @@ FS_HD void nodal_triad_r(const double e[3][3], const double n[3], bool valid, R 
         for (int r = 0; r < 3; r++)
             for (int k = 0; k < 3; k++) Ar[r][k] = A[r][k];
     } else {
-        double a0 = 0.0, a1 = 0.0;
+        double a0d = 0.0, a1d = 0.0;
         if (valid) {
-            a0 = -dot3(e[1], n);
-            a1 = dot3(e[0], n);
+            a0d = -dot3(e[1], n);
+            a1d = dot3(e[0], n);
         }
-        const double x = a0 * a0 + a1 * a1;
-        if (!(x > 1.0e-24)) {
+        const float a0 = (float)a0d, a1 = (float)a1d;
+        const float x = a0 * a0 + a1 * a1;
+        if (!(x > 1.0e-24f)) {
             for (int r = 0; r < 3; r++)
                 for (int k = 0; k < 3; k++) Ar[r][k] = r == k ? (R)1 : (R)0;
             return;
         }
-        double s, c;
-        sinc_cosc(x, s, c);
-        const R d0 = (R)(1.0 - c * a1 * a1), d1 = (R)(1.0 - c * a0 * a0), d2 = (R)(1.0 - c * x);
-        const R o = (R)(c * a0 * a1), s1 = (R)(s * a1), s0 = (R)(s * a0);
-        Ar[0][0] = d0; Ar[0][1] = o;  Ar[0][2] = s1;
-        Ar[1][0] = o;  Ar[1][1] = d1; Ar[1][2] = -s0;
-        Ar[2][0] = -s1; Ar[2][1] = s0; Ar[2][2] = d2;
+        if (x > 1.0f) {
+            const double xd = a0d * a0d + a1d * a1d;
+            double sd, cd;
+            sinc_cosc(xd, sd, cd);
+            const R d0 = (R)(1.0 - cd * a1d * a1d), d1 = (R)(1.0 - cd * a0d * a0d), d2 = (R)(1.0 - cd * xd);
+            const R o = (R)(cd * a0d * a1d), s1 = (R)(sd * a1d), s0 = (R)(sd * a0d);
+            Ar[0][0] = d0; Ar[0][1] = o;  Ar[0][2] = s1;
+            Ar[1][0] = o;  Ar[1][1] = d1; Ar[1][2] = -s0;
+            Ar[2][0] = -s1; Ar[2][1] = s0; Ar[2][2] = d2;
+            return;
+        }
+        float s, c;
+        sinc_cosc_f(x, s, c);
+        const float ca0 = c * a0, ca1 = c * a1;
+        Ar[0][0] = 1.0f - ca1 * a1; Ar[0][1] = ca0 * a1;       Ar[0][2] = s * a1;
+        Ar[1][0] = ca0 * a1;        Ar[1][1] = 1.0f - ca0 * a0; Ar[1][2] = -(s * a0);
+        Ar[2][0] = -(s * a1);       Ar[2][1] = s * a0;          Ar[2][2] = 1.0f - c * x;
     }
 }
 
@@ -573,6 +596,16 @@ FS_HD void q4_point(int j, double &xi, double &eta)
     eta = ((j & 1) ? Q4_GP : -Q4_GP);
 }
 
+template <class T>
+FS_HD void q4_dbasis_t(T xi, T eta, T gp[4][2])
+{
+    const T q = (T)0.25, one = (T)1;
+    gp[0][0] = -q * (one - eta); gp[0][1] = -q * (one - xi);
+    gp[1][0] = q * (one - eta);  gp[1][1] = -q * (one + xi);
+    gp[2][0] = q * (one + eta);  gp[2][1] = q * (one + xi);
+    gp[3][0] = -q * (one + eta); gp[3][1] = q * (one - xi);
+}
+
 FS_HD void q4_dbasis(double xi, double eta, double gp[4][2])
 {
     gp[0][0] = -0.25 * (1 - eta); gp[0][1] = -0.25 * (1 - xi);
@@ -623,6 +656,7 @@ FS_HD void q4_bs(const R X[4], const R Y[4], R r, R s, R Bs[2][4][5])
 // Q4 element-level constants shared by the four quadrature points.
 struct Q4Elem {
     double Xr[4][3];   // node coordinates relative to the centroid
+    float Xf[4][3];    // the same rounded to float (the float rows' element coordinates)
     double stab;       // shear stabilisation t^2 / (t^2 + c h^2), h = max distance from node 1
 };
 
@@ -635,7 +669,10 @@ FS_HD void q4_prepare(const ElemIn<4> &in, double t, double stab_c, Q4Elem &qe)
     for (int c = 0; c < 3; c++) cen[c] /= 4;
     double mx = 0.0;
     for (int a = 0; a < 4; a++) {
-        for (int c = 0; c < 3; c++) qe.Xr[a][c] = in.X[a][c] - cen[c];
+        for (int c = 0; c < 3; c++) {
+            qe.Xr[a][c] = in.X[a][c] - cen[c];
+            qe.Xf[a][c] = (float)qe.Xr[a][c];
+        }
         if (a > 0) {
             double dx = in.X[a][0] - in.X[0][0], dy = in.X[a][1] - in.X[0][1], dz = in.X[a][2] - in.X[0][2];
             double dd = dx * dx + dy * dy + dz * dz;
@@ -668,12 +705,35 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     {
         R e0r[3] = {(R)e[0][0], (R)e[0][1], (R)e[0][2]}, e1r[3] = {(R)e[1][0], (R)e[1][1], (R)e[1][2]};
         for (int a = 0; a < 4; a++) {
-            R xr[3] = {(R)qe.Xr[a][0], (R)qe.Xr[a][1], (R)qe.Xr[a][2]};
+            R xr[3];
+            for (int c = 0; c < 3; c++) xr[c] = sizeof(R) == 4 ? (R)qe.Xf[a][c] : (R)qe.Xr[a][c];
             X[a] = dot3(xr, e0r);
             Y[a] = dot3(xr, e1r);
         }
     }
-    R J0r[3] = {(R)J0[0], (R)J0[1], (R)J0[2]}, J1r[3] = {(R)J1[0], (R)J1[1], (R)J1[2]};
+    // basis gradients and tangents in the working precision (float: from the
+    // float coordinates; double: the values above)
+    R gq[4][2], J0r[3], J1r[3], xir, etar;
+    if constexpr (sizeof(R) == 4) {
+        xir = j < 2 ? -(float)Q4_GP : (float)Q4_GP;
+        etar = (j & 1) ? (float)Q4_GP : -(float)Q4_GP;
+        q4_dbasis_t<R>(xir, etar, gq);
+        for (int c = 0; c < 3; c++) {
+            J0r[c] = qe.Xf[0][c] * gq[0][0] + qe.Xf[1][c] * gq[1][0] + qe.Xf[2][c] * gq[2][0] + qe.Xf[3][c] * gq[3][0];
+            J1r[c] = qe.Xf[0][c] * gq[0][1] + qe.Xf[1][c] * gq[1][1] + qe.Xf[2][c] * gq[2][1] + qe.Xf[3][c] * gq[3][1];
+        }
+    } else {
+        xir = xi;
+        etar = eta;
+        for (int a = 0; a < 4; a++) {
+            gq[a][0] = gp[a][0];
+            gq[a][1] = gp[a][1];
+        }
+        for (int c = 0; c < 3; c++) {
+            J0r[c] = J0[c];
+            J1r[c] = J1[c];
+        }
+    }
     // surface Jacobian |J0 x J1| in the working precision
     R Jac;
     {
@@ -690,8 +750,8 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     // g_a = J invG gradNparams_a, projected on e1, e2
     R pj0[2] = {dot3(e0, J0r), dot3(e1, J0r)}, pj1[2] = {dot3(e0, J1r), dot3(e1, J1r)};
     for (int a = 0; a < 4; a++) {
-        R t1 = i11 * (R)gp[a][0] + i12 * (R)gp[a][1];
-        R t2 = i12 * (R)gp[a][0] + i22 * (R)gp[a][1];
+        R t1 = i11 * gq[a][0] + i12 * gq[a][1];
+        R t2 = i12 * gq[a][0] + i22 * gq[a][1];
         g[a][0] = pj0[0] * t1 + pj1[0] * t2;
         g[a][1] = pj0[1] * t1 + pj1[1] * t2;
     }
@@ -700,7 +760,7 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     GlobalMap<R, 4> M;
     build_map<R, 4>(e, A, g, M);
     R sh[2][4][5];
-    q4_bs<R>(X, Y, (R)xi, (R)eta, sh);
+    q4_bs<R>(X, Y, xir, etar, sh);
     const R stab = (R)qe.stab;
     if constexpr (!COMP) {
         R tr_ = (R)in.t, jr = Jac;

@@ -29,6 +29,12 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
 #pragma unroll
             for (int c = 0; c < 3; c++) qe.Xr[a][c] = __shfl_sync(0xffffffffu, qe.Xr[a][c], src);
         qe.stab = __shfl_sync(0xffffffffu, qe.stab, src);
+        if constexpr (sizeof(R) == 4) {
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) qe.Xf[a][c] = __shfl_sync(0xffffffffu, qe.Xf[a][c], src);
+        }
     }
     if (active) {
         const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;

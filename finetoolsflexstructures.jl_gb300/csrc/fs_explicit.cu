@@ -5,9 +5,13 @@
 //   U += dt V + dt^2/2 A;  E = K U;  F = -(E + C (V + dt/2 A));
 //   V += dt/2 A;  A = invMC F;  V += dt/2 A
 //
-// Two kernels per step: the displacement update, then a row-parallel CSR
-// product fused with the force, acceleration and velocity updates of the
-// row.  The displacement and velocity sums carry Kahan compensation terms so
+// Two kernels per step: the displacement update, then the product K U fused
+// with the force, acceleration and velocity updates of the row.  The product
+// runs on 6x6 node blocks (block rows = the neighbour lists of the pattern,
+// filled from the CSR matrix once at set-up, read as contiguous 144- or
+// 288-byte blocks against a node-padded copy of U), or row-parallel on the CSR
+// arrays when no pattern of the current mesh is at hand.  The displacement
+// and velocity sums carry Kahan compensation terms so
 // that a long run in double does not drift.  With FS_FP64 the restoring force
 // K U is formed in double.  With FS_MIXED it is formed in float: the
 // displacement kernel also writes a float copy of U and the product runs on

@@ -83,6 +83,11 @@ __device__ __forceinline__ void gather_add(float &hi, float &lo, float2 v)
     two_sum_acc(hi, lo, v.y);
 }
 __device__ __forceinline__ void gather_add(double &hi, double &, double v) { hi += v; }
+// the first contribution of a value: taken as is (a stored float pair is
+// already normalised, |lo| <= ulp(hi)/2)
+__device__ __forceinline__ void gather_set(float &hi, float &lo, float v) { hi = v; lo = 0.f; }
+__device__ __forceinline__ void gather_set(float &hi, float &lo, float2 v) { hi = v.x; lo = v.y; }
+__device__ __forceinline__ void gather_set(double &hi, double &, double v) { hi = v; }
 __device__ __forceinline__ double entry_value(float v) { return (double)v; }
 __device__ __forceinline__ double entry_value(double v) { return v; }
 __device__ __forceinline__ double entry_value(float2 v) { return (double)v.x + (double)v.y; }
@@ -93,8 +98,14 @@ template <class R, int NEN> struct GatherSmem {
     static constexpr int PER_WARP = G_MAXP * NEN * 36 * (int)sizeof(R) + 512;
 };
 
+// resident blocks asked of the compiler: 32 warps per SM where the kernel fits
+// 64 registers without spilling (float entries of three-node elements)
+template <class R, int NEN, int WARPS> struct GatherMinBlocks {
+    static constexpr int value = (sizeof(R) == 4 && NEN == 3) ? 32 / WARPS : 1;
+};
+
 template <class R, int NEN, int G_COLS, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, WARPS>::value))
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
     typedef typename GatherAcc<R>::T A;
@@ -122,27 +133,50 @@ __global__ void __launch_bounds__(WARPS * 32)
     for (int k = 0; k < 6; k++) any |= (d[k] <= n);
     if (!any) return;
     if (L <= 32 * G_COLS) {
-        // the node's contribution entries into shared memory
+        // second round of loads, all depending only on the first: lane k < 6
+        // the row pointer of dof k, lane s the first entry of neighbour slot s,
+        // lane q the pair q of the first batch, every lane its columns
+        int64_t rp_l = 0;
+        {
+            int dl = d[0];
+#pragma unroll
+            for (int k = 1; k < 6; k++) dl = lane == k ? d[k] : dl;
+            if (lane < 6 && dl <= n) rp_l = P.rowptr[dl - 1];
+        }
         const int ntot = (int)(pe - pb) * NEN;
+        const int nslots = (int)(off_next - off);
+        const bool slot_shfl = nslots < 32;  // slot starts exchanged by shuffles
+        int sl_l = 0;
+        if (slot_shfl && lane <= nslots) sl_l = lane < nslots ? (int)P.sl_off[off + lane] : ntot;
+        int32_t pel_l = lane < G_MAXP && pb + lane < pe ? m.pair_e[pb + lane] : 0;
+        int cs_l[G_COLS];
+#pragma unroll
+        for (int c = 0; c < G_COLS; c++) {
+            const int j = lane + 32 * c;
+            cs_l[c] = j < L ? (int)P.colsrc[off6 + j] : 0;
+        }
+        // the node's contribution entries into shared memory
         const uint16_t *ent = P.sl_ent + pb * NEN;
         for (int i = lane; i < ntot; i += 32) sent[i] = ent[i];
         // the lane's columns and the range of entries of their neighbour slot
-        const int nslots = (int)(off_next - off);
-        int kcol[G_COLS], cur[G_COLS], last[G_COLS];
+        int kcol[G_COLS], cur[G_COLS], beg[G_COLS], last[G_COLS];
         A hi[G_COLS][6], lo[G_COLS][6];
 #pragma unroll
         for (int c = 0; c < G_COLS; c++) {
             const int j = lane + 32 * c;
-            kcol[c] = 0;
-            cur[c] = 0;
-            last[c] = 0;
-            if (j < L) {
-                const int cs = (int)P.colsrc[off6 + j];
-                const int sl = cs / 6;
-                kcol[c] = cs - 6 * sl;
-                cur[c] = (int)P.sl_off[off + sl];
-                last[c] = sl + 1 < nslots ? (int)P.sl_off[off + sl + 1] : ntot;
+            const int sl = cs_l[c] / 6;
+            kcol[c] = cs_l[c] - 6 * sl;
+            int b0, b1;
+            if (slot_shfl) {
+                b0 = __shfl_sync(0xffffffffu, sl_l, sl);
+                b1 = __shfl_sync(0xffffffffu, sl_l, sl + 1);
+            } else {
+                b0 = (int)P.sl_off[off + sl];
+                b1 = sl + 1 < nslots ? (int)P.sl_off[off + sl + 1] : ntot;
             }
+            cur[c] = j < L ? b0 : 0;
+            last[c] = j < L ? b1 : 0;
+            beg[c] = cur[c];
 #pragma unroll
             for (int k = 0; k < 6; k++) {
                 hi[c][k] = 0;
@@ -160,8 +194,9 @@ __global__ void __launch_bounds__(WARPS * 32)
         for (int64_t p0 = pb; p0 < pe; p0 += G_MAXP) {
             const int cnt = (int)min((int64_t)G_MAXP, pe - p0);
             const int q0 = (int)(p0 - pb);
+            if (p0 != pb) pel_l = lane < cnt ? m.pair_e[p0 + lane] : 0;
             for (int q = 0; q < cnt; q++) {
-                const int32_t pel = m.pair_e[p0 + q];
+                const int32_t pel = __shfl_sync(0xffffffffu, pel_l, q);
                 const int a = pel & 3;
                 const R *base = ke + (int64_t)(pel >> 2) * ND2;
 #pragma unroll
@@ -180,6 +215,20 @@ __global__ void __launch_bounds__(WARPS * 32)
             // this batch's contributions to the lane's columns, ascending pair order
 #pragma unroll
             for (int c = 0; c < G_COLS; c++) {
+                // the value's first contribution initialises the sum
+                if (cur[c] == beg[c] && cur[c] < last[c]) {
+                    const uint32_t e = sent[cur[c]];
+                    const int q = (int)(e & 63u) - q0;
+                    if (q < cnt) {
+                        const int b = (int)((e >> 6) & 3u);
+                        const bool tr = (e >> 8) & 1u;
+                        const R *src = stage + q * SLAB + b * 36 + (tr ? 6 * kcol[c] : kcol[c]);
+                        const int st = tr ? 1 : 6;
+#pragma unroll
+                        for (int k = 0; k < 6; k++) gather_set(hi[c][k], lo[c][k], src[st * k]);
+                        cur[c]++;
+                    }
+                }
                 while (cur[c] < last[c]) {
                     const uint32_t e = sent[cur[c]];
                     const int q = (int)(e & 63u) - q0;
@@ -198,8 +247,9 @@ __global__ void __launch_bounds__(WARPS * 32)
         }
 #pragma unroll
         for (int k = 0; k < 6; k++) {
+            const int64_t rpk = __shfl_sync(0xffffffffu, rp_l, k);
             if (d[k] > n) continue;
-            double *o = vals + P.rowptr[d[k] - 1];
+            double *o = vals + rpk;
 #pragma unroll
             for (int c = 0; c < G_COLS; c++) {
                 const int j = lane + 32 * c;
