@@ -293,17 +293,38 @@ FS_HD void expand_wt(const GlobalMap<R, NN> &M, const R w[NN], const R tx[NN], c
     }
 }
 
+// Per-call constant material data (host precomputed).
+struct MatConst {
+    double Lps[6];    // Cholesky factor of Dps, lower, packed (L00,L10,L11,L20,L21,L22)
+    double Lt[3];     // Cholesky factor of (5/6) Dt, lower packed (L00,L10,L11)
+    double stab_c;    // stab_fun(t,h) = t^2/(t^2 + stab_c h^2)
+    double drill_scale;
+    double drill_scale6;  // drill_scale / 6
+    double rho;
+    float Lpsf[6], Ltf[3];  // the factors rounded to float (mixed rows)
+    float stab_cf;          // stab_c rounded to float
+};
+
+// entry i of a packed factor in the working precision: the float copy for
+// float rows (rounded once on the host), the double factor otherwise
+template <class R>
+FS_HD R lpk(const double *d, const float *f, int i)
+{
+    if constexpr (sizeof(R) == 4) return f[i];
+    return d[i];
+}
+
 // Membrane and bending rows of a homogeneous shell, mixed with the Cholesky
 // factor L of Dps (rows r = 0..2: sm * sum_{c>=r} L[c][r] strain_c), written
 // as global rows; returns the bending rotations for the drilling factor.
 template <class R, int NN>
-FS_HD void homog_mb_rows(const GlobalMap<R, NN> &M, const double *Lps, R sm, R sb, R *rows, int rs,
+FS_HD void homog_mb_rows(const GlobalMap<R, NN> &M, const MatConst &mc, R sm, R sb, R *rows, int rs,
                          R btx[3][NN], R bty[3][NN])
 {
     for (int r = 0; r < 3; r++) {
-        R c0 = r == 0 ? (R)Lps[lp(0, 0)] : (R)0;
-        R c1 = r <= 1 ? (R)Lps[lp(1, r)] : (R)0;
-        R c2 = (R)Lps[lp(2, r)];
+        R c0 = r == 0 ? lpk<R>(mc.Lps, mc.Lpsf, lp(0, 0)) : (R)0;
+        R c1 = r <= 1 ? lpk<R>(mc.Lps, mc.Lpsf, lp(1, r)) : (R)0;
+        R c2 = lpk<R>(mc.Lps, mc.Lpsf, lp(2, r));
         R u[NN], v[NN];
         for (int j = 0; j < NN; j++) {
             u[j] = sm * (c0 * M.g[j][0] + c2 * M.g[j][1]);
@@ -320,14 +341,6 @@ FS_HD void homog_mb_rows(const GlobalMap<R, NN> &M, const double *Lps, R sm, R s
 // Material factors
 // ---------------------------------------------------------------------------
 // Per-call constant material data (host precomputed).
-struct MatConst {
-    double Lps[6];    // Cholesky factor of Dps, lower, packed (L00,L10,L11,L20,L21,L22)
-    double Lt[3];     // Cholesky factor of (5/6) Dt, lower packed (L00,L10,L11)
-    double stab_c;    // stab_fun(t,h) = t^2/(t^2 + stab_c h^2)
-    double drill_scale;
-    double drill_scale6;  // drill_scale / 6
-    double rho;
-};
 
 // Drilling stiffness from the sum of the six nodal-basis bending diagonals:
 // mean times scale, src/FEMMShellT3FFModule.jl:713-727, in double.  The FP64
@@ -350,16 +363,17 @@ struct GroupConst {
     double mass;      // mass density per unit area (laminate_inertia!)
     double moi;       // rotary inertia density
     double pad;
+    float L6f[21], LHf[3];  // the factors rounded to float (mixed rows)
 };
 
 
 // rows_out[r] = scale * sum_{c>=r} L[c][r] rows_in[c]   (L^T applied to stacked rows)
 template <class R, int NN, int NR>
-FS_HD void mix_rows(const double *Lpk, R scale, const R in[NR][NN][5], R out[NR][NN][5])
+FS_HD void mix_rows(const double *Lpk, const float *Lpkf, R scale, const R in[NR][NN][5], R out[NR][NN][5])
 {
     for (int r = 0; r < NR; r++) {
         R f[NR];
-        for (int c = 0; c < NR; c++) f[c] = (c >= r) ? scale * (R)Lpk[lp(c, r)] : (R)0;
+        for (int c = 0; c < NR; c++) f[c] = (c >= r) ? scale * lpk<R>(Lpk, Lpkf, lp(c, r)) : (R)0;
         for (int i = 0; i < NN; i++)
             for (int q = 0; q < 5; q++) {
                 R s = 0;
@@ -458,24 +472,40 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
         J1[c] = in.X[2][c] - in.X[0][c];
     }
     make_frame(J0, J1, e);
-    double a = dot3(J0, e[0]), b = dot3(J0, e[1]);
-    double cc = dot3(J1, e[0]), d = dot3(J1, e[1]);
-    double Jd = a * d - b * cc;
-    double Ae = Jd / 2;
-    R g[3][2];
+    const double t = COMP ? gc->thickness : in.t;
+    // element coordinates x, y of the nodes, basis gradients, area and the
+    // stabilisation factor t^2 / (t^2 + c h^2), h^2 = 2 Ae
+    R g[3][2], x[3], y[3], AeR, stab;
     if constexpr (sizeof(R) == 8) {
+        double a = dot3(J0, e[0]), b = dot3(J0, e[1]);
+        double cc = dot3(J1, e[0]), d = dot3(J1, e[1]);
+        double Jd = a * d - b * cc;
+        double Ae = Jd / 2;
         double iJ = 1.0 / Jd;
         g[0][0] = (b - d) * iJ; g[1][0] = d * iJ; g[2][0] = -b * iJ;
         g[0][1] = (cc - a) * iJ; g[1][1] = -cc * iJ; g[2][1] = a * iJ;
+        x[0] = 0; x[1] = a; x[2] = cc;
+        y[0] = 0; y[1] = b; y[2] = d;
+        AeR = Ae;
+        double h2 = 2 * Ae;
+        stab = t * t / (t * t + mc.stab_c * h2);
     } else {
-        // basis gradients in the working precision from the double-precision
-        // element coordinates (differences taken in double)
-        const R iJ = (R)1 / (R)Jd;
-        g[0][0] = (R)(b - d) * iJ; g[1][0] = (R)d * iJ; g[2][0] = -(R)b * iJ;
-        g[0][1] = (R)(cc - a) * iJ; g[1][1] = -(R)cc * iJ; g[2][1] = (R)a * iJ;
+        // coordinates and the differences of the gradients in double (the
+        // differences of nearby coordinates lose digits in float), rounded
+        // once; the rest in float
+        const double a = dot3(J0, e[0]), b = dot3(J0, e[1]);
+        const double cc = dot3(J1, e[0]), d = dot3(J1, e[1]);
+        const double Jd = a * d - b * cc;
+        const float iJ = 1.0f / (float)Jd;
+        g[0][0] = (float)(b - d) * iJ; g[1][0] = (float)d * iJ; g[2][0] = -(float)b * iJ;
+        g[0][1] = (float)(cc - a) * iJ; g[1][1] = -(float)cc * iJ; g[2][1] = (float)a * iJ;
+        x[0] = 0; x[1] = (float)a; x[2] = (float)cc;
+        y[0] = 0; y[1] = (float)b; y[2] = (float)d;
+        AeR = (float)(Jd / 2);
+        const float tf = (float)t;
+        stab = tf * tf / (tf * tf + mc.stab_cf * (2 * AeR));
     }
-    double t = COMP ? gc->thickness : in.t;
-    // --- triads (rotation in double, rounded to R) ---
+    // --- triads ---
     R A[3][3][3];
     for (int i = 0; i < 3; i++) nodal_triad_r<R>(e, in.nrm[i], in.valid[i], A[i]);
     GlobalMap<R, 3> M;
@@ -487,8 +517,6 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
     for (int r = 0; r < NS; r++)
         for (int i = 0; i < 3; i++)
             for (int q = 0; q < 5; q++) sh[r][i][q] = 0;
-    R x[3] = {0, (R)a, (R)cc}, y[3] = {0, (R)b, (R)d};
-    R AeR = (R)Ae;
     if (AVGK) {
         t3_bs_ordering<R>(x, y, AeR, 0, 1, 2, (R(*)[3][5])sh[0], (R)1);
         t3_bs_ordering<R>(x, y, AeR, 1, 2, 0, (R(*)[3][5])sh[2], (R)1);
@@ -498,17 +526,15 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
         t3_bs_ordering<R>(x, y, AeR, 1, 2, 0, (R(*)[3][5])sh[0], (R)(1.0 / 3));
         t3_bs_ordering<R>(x, y, AeR, 2, 0, 1, (R(*)[3][5])sh[0], (R)(1.0 / 3));
     }
-    double h2 = 2 * Ae;  // h = sqrt(2 Ae)
-    double stab = t * t / (t * t + mc.stab_c * h2);
     // rotations of every bending/shear row, for the drilling factor
     R rtx[3 + NS][3], rty[3 + NS][3];
     if constexpr (!COMP) {
         // --- homogeneous: sparse rows, Dps and (5/6)Dt Cholesky mixing ---
         R tr_ = (R)t;
-        homog_mb_rows<R, 3>(M, mc.Lps, sqrt(tr_ * AeR), sqrt(tr_ * tr_ * tr_ / 12 * AeR), rows, rs,
+        homog_mb_rows<R, 3>(M, mc, sqrt(tr_ * AeR), sqrt(tr_ * tr_ * tr_ / 12 * AeR), rows, rs,
                             (R(*)[3])rtx[0], (R(*)[3])rty[0]);
-        R ws = sqrt(tr_ * (R)stab * AeR * (R)(AVGK ? 1.0 / 3 : 1.0));
-        R l00 = (R)mc.Lt[lp(0, 0)], l10 = (R)mc.Lt[lp(1, 0)], l11 = (R)mc.Lt[lp(1, 1)];
+        R ws = sqrt(tr_ * stab * AeR * (R)(AVGK ? 1.0 / 3 : 1.0));
+        R l00 = lpk<R>(mc.Lt, mc.Ltf, lp(0, 0)), l10 = lpk<R>(mc.Lt, mc.Ltf, lp(1, 0)), l11 = lpk<R>(mc.Lt, mc.Ltf, lp(1, 1));
         for (int o = 0; o < NS / 2; o++)
             for (int r = 0; r < 2; r++) {
                 R f0 = r == 0 ? ws * l00 : (R)0, f1 = ws * (r == 0 ? l10 : l11);
@@ -540,11 +566,11 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
         layup_angle(e, gc->csmat, lm, ln);
         rotate3<R, 3>(lm, ln, (R(*)[3][5])mb[0]);
         rotate3<R, 3>(lm, ln, (R(*)[3][5])mb[3]);
-        mix_rows<R, 3, 6>(gc->L6, sqrt(AeR), mb, (R(*)[3][5])mixed[0]);
-        R ws = (R)stab * AeR * (R)(AVGK ? 1.0 / 3 : 1.0);
+        mix_rows<R, 3, 6>(gc->L6, gc->L6f, sqrt(AeR), mb, (R(*)[3][5])mixed[0]);
+        R ws = stab * AeR * (R)(AVGK ? 1.0 / 3 : 1.0);
         for (int o = 0; o < NS / 2; o++) {
             rotate2<R, 3>(lm, ln, (R(*)[3][5])sh[2 * o]);
-            mix_rows<R, 3, 2>(gc->LH, sqrt(ws), (R(*)[3][5])sh[2 * o], (R(*)[3][5])mixed[6 + 2 * o]);
+            mix_rows<R, 3, 2>(gc->LH, gc->LHf, sqrt(ws), (R(*)[3][5])sh[2 * o], (R(*)[3][5])mixed[6 + 2 * o]);
         }
         for (int r = 0; r < 6 + NS; r++) expand_row<R, 3>(M, (const R(*)[5])mixed[r], rows + r * rs);
         // drilling factor: every mixed row may carry rotations here
@@ -711,16 +737,18 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
             Y[a] = dot3(xr, e1r);
         }
     }
-    // basis gradients and tangents in the working precision (float: from the
-    // float coordinates; double: the values above)
+    // basis gradients and tangents in the working precision (float: the
+    // gradients evaluated in float, the double tangents rounded once --
+    // tangents summed in float from rounded coordinates lose about one more
+    // digit; double: the values above)
     R gq[4][2], J0r[3], J1r[3], xir, etar;
     if constexpr (sizeof(R) == 4) {
         xir = j < 2 ? -(float)Q4_GP : (float)Q4_GP;
         etar = (j & 1) ? (float)Q4_GP : -(float)Q4_GP;
         q4_dbasis_t<R>(xir, etar, gq);
         for (int c = 0; c < 3; c++) {
-            J0r[c] = qe.Xf[0][c] * gq[0][0] + qe.Xf[1][c] * gq[1][0] + qe.Xf[2][c] * gq[2][0] + qe.Xf[3][c] * gq[3][0];
-            J1r[c] = qe.Xf[0][c] * gq[0][1] + qe.Xf[1][c] * gq[1][1] + qe.Xf[2][c] * gq[2][1] + qe.Xf[3][c] * gq[3][1];
+            J0r[c] = (float)J0[c];
+            J1r[c] = (float)J1[c];
         }
     } else {
         xir = xi;
@@ -765,9 +793,9 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     if constexpr (!COMP) {
         R tr_ = (R)in.t, jr = Jac;
         R btx[3][4], bty[3][4];
-        homog_mb_rows<R, 4>(M, mc.Lps, sqrt(tr_ * jr), sqrt(tr_ * tr_ * tr_ / 12 * jr), rows, rs, btx, bty);
+        homog_mb_rows<R, 4>(M, mc, sqrt(tr_ * jr), sqrt(tr_ * tr_ * tr_ / 12 * jr), rows, rs, btx, bty);
         R ws = sqrt(tr_ * stab * jr);
-        R l00 = (R)mc.Lt[lp(0, 0)], l10 = (R)mc.Lt[lp(1, 0)], l11 = (R)mc.Lt[lp(1, 1)];
+        R l00 = lpk<R>(mc.Lt, mc.Ltf, lp(0, 0)), l10 = lpk<R>(mc.Lt, mc.Ltf, lp(1, 0)), l11 = lpk<R>(mc.Lt, mc.Ltf, lp(1, 1));
         for (int r = 0; r < 2; r++) {
             R f0 = r == 0 ? ws * l00 : (R)0, f1 = ws * (r == 0 ? l10 : l11);
             R w[4], tx[4], ty[4];
@@ -796,9 +824,9 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         layup_angle(e, gc->csmat, lm, ln);
         rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[0]);
         rotate3<R, 4>(lm, ln, (R(*)[4][5])mb[3]);
-        mix_rows<R, 4, 6>(gc->L6, sqrt(Jac), mb, (R(*)[4][5])mixed[0]);
+        mix_rows<R, 4, 6>(gc->L6, gc->L6f, sqrt(Jac), mb, (R(*)[4][5])mixed[0]);
         rotate2<R, 4>(lm, ln, sh);
-        mix_rows<R, 4, 2>(gc->LH, sqrt(stab * Jac), sh, (R(*)[4][5])mixed[6]);
+        mix_rows<R, 4, 2>(gc->LH, gc->LHf, sqrt(stab * Jac), sh, (R(*)[4][5])mixed[6]);
         for (int r = 0; r < 8; r++) expand_row<R, 4>(M, (const R(*)[5])mixed[r], rows + r * rs);
     }
     // drilling traces: sum over rows of |b|^2 - (b.n)^2 on the rotation block

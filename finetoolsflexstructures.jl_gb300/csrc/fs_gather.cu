@@ -99,13 +99,16 @@ template <class R, int NEN> struct GatherSmem {
 };
 
 // resident blocks asked of the compiler: 32 warps per SM where the kernel fits
-// 64 registers without spilling (float entries of three-node elements)
-template <class R, int NEN, int WARPS> struct GatherMinBlocks {
-    static constexpr int value = (sizeof(R) == 4 && NEN == 3) ? 32 / WARPS : 1;
+// 64 registers without spilling (float entries of three-node elements), 28
+// for other float entries, 24 (at most 80 registers) for double and float
+// pairs; no bound for the four-column variant of long rows
+template <class R, int NEN, int G_COLS, int WARPS> struct GatherMinBlocks {
+    static constexpr int warps = G_COLS > 2 ? 1 : (sizeof(R) == 4 ? (NEN == 3 ? 32 : 28) : 24);
+    static constexpr int value = warps / WARPS > 0 ? warps / WARPS : 1;
 };
 
 template <class R, int NEN, int G_COLS, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, WARPS>::value))
+__global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, WARPS>::value))
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
     typedef typename GatherAcc<R>::T A;

@@ -54,6 +54,9 @@ inline int prepare_matconst(const fs_shell_params &p, MatConst &mc)
     mc.drill_scale = p.drilling_stiffness_scale;
     mc.drill_scale6 = p.drilling_stiffness_scale / 6.0;
     mc.rho = p.rho;
+    for (int i = 0; i < 6; i++) mc.Lpsf[i] = (float)mc.Lps[i];
+    for (int i = 0; i < 3; i++) mc.Ltf[i] = (float)mc.Lt[i];
+    mc.stab_cf = (float)mc.stab_c;
     return 0;
 }
 
@@ -80,6 +83,8 @@ inline int prepare_group(const fs_layup_group &g, GroupConst &gc)
     gc.thickness = g.thickness;
     gc.mass = g.mass_density;
     gc.moi = g.moi_density;
+    for (int i = 0; i < 21; i++) gc.L6f[i] = (float)gc.L6[i];
+    for (int i = 0; i < 3; i++) gc.LHf[i] = (float)gc.LH[i];
     return 0;
 }
 
