@@ -1159,3 +1159,233 @@ int orc_laminate(int nplies, const double *ply_Dps, const double *ply_Dts, const
     *moi_density = mi;
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Stress resultants at the integration points of the homogeneous      */
+/* shells: inspectintegpoints, src/FEMMShellT3FFModule.jl:850-962 (one */
+/* point per element, the centroid) and src/FEMMShellQ4RSModule.jl:    */
+/* 1061-1170 (the four Gauss points)                                   */
+/* ------------------------------------------------------------------ */
+
+/* the 2x2 tensor [v0 v2; v2 v1] (or the vector (v0, v1) of the shear
+ * forces) seen in the output csys: o2 = [m n; -n m] from
+ * Layup2ElementAngle(E_G, csmat); mo = o2' m o2, fo = o2' f */
+static void resultant_out(const double *E, const double *cs, int quant, const double *v, double *out)
+{
+    double m, n;
+    layup_angle(E, cs, &m, &n);
+    double o[4];
+    o[IX(0, 0, 2)] = m; o[IX(0, 1, 2)] = n;
+    o[IX(1, 0, 2)] = -n; o[IX(1, 1, 2)] = m;
+    if (quant == ORC_RES_SHEAR) {
+        out[0] = o[IX(0, 0, 2)] * v[0] + o[IX(1, 0, 2)] * v[1];
+        out[1] = o[IX(0, 1, 2)] * v[0] + o[IX(1, 1, 2)] * v[1];
+        out[2] = 0.0;
+        return;
+    }
+    double M[4], t[4], R[4];
+    M[IX(0, 0, 2)] = v[0]; M[IX(0, 1, 2)] = v[2];
+    M[IX(1, 0, 2)] = v[2]; M[IX(1, 1, 2)] = v[1];
+    for (int j = 0; j < 2; j++)
+        for (int i = 0; i < 2; i++) t[IX(i, j, 2)] = o[IX(0, i, 2)] * M[IX(0, j, 2)] + o[IX(1, i, 2)] * M[IX(1, j, 2)];
+    for (int j = 0; j < 2; j++)
+        for (int i = 0; i < 2; i++) R[IX(i, j, 2)] = t[IX(i, 0, 2)] * o[IX(0, j, 2)] + t[IX(i, 1, 2)] * o[IX(1, j, 2)];
+    out[0] = R[IX(0, 0, 2)];
+    out[1] = R[IX(1, 1, 2)];
+    out[2] = R[IX(0, 1, 2)];
+}
+
+static void matvec(const double *A, int r, int c, const double *x, double *y)
+{
+    for (int i = 0; i < r; i++) {
+        double s = 0.0;
+        for (int k = 0; k < c; k++) s += A[IX(i, k, r)] * x[k];
+        y[i] = s;
+    }
+}
+
+/* material times strain: moment t^3/12 Dps kurv, membrane t Dps strn,
+ * shear t stab (5/6 Dt) shr */
+static void resultant_material(const orc_params *p, int quant, double t, double stab, const double *s,
+                               double *v)
+{
+    if (quant == ORC_RES_SHEAR) {
+        double Dt5[4];
+        for (int i = 0; i < 4; i++) Dt5[i] = p->Dt[i] * (5.0 / 6.0);
+        double f = t * stab;
+        for (int i = 0; i < 2; i++) v[i] = f * (Dt5[IX(i, 0, 2)] * s[0] + Dt5[IX(i, 1, 2)] * s[1]);
+        v[2] = 0.0;
+        return;
+    }
+    double f = quant == ORC_RES_MOMENT ? (t * t * t) / 12 : t;
+    for (int i = 0; i < 3; i++)
+        v[i] = f * (p->Dps[IX(i, 0, 3)] * s[0] + p->Dps[IX(i, 1, 3)] * s[1] + p->Dps[IX(i, 2, 3)] * s[2]);
+}
+
+static void t3_resultant(const orc_params *p, int64_t e, const double *X, const double *nrm,
+                         const uint8_t *valid, const double *ed, int quant, const double *cs, double *out)
+{
+    const int n = 18;
+    double J0[6], E[9], ee[6], g[6];
+    for (int j = 0; j < 3; j++) {
+        J0[IX(j, 0, 3)] = X[3 * 1 + j] - X[3 * 0 + j];
+        J0[IX(j, 1, 3)] = X[3 * 2 + j] - X[3 * 0 + j];
+    }
+    e_g(E, J0);
+    ee[IX(0, 0, 3)] = ee[IX(0, 1, 3)] = 0.0;
+    ee[IX(1, 0, 3)] = J0[0] * E[0] + J0[1] * E[1] + J0[2] * E[2];
+    ee[IX(1, 1, 3)] = J0[0] * E[3] + J0[1] * E[4] + J0[2] * E[5];
+    ee[IX(2, 0, 3)] = J0[3] * E[0] + J0[4] * E[1] + J0[5] * E[2];
+    ee[IX(2, 1, 3)] = J0[3] * E[3] + J0[4] * E[4] + J0[5] * E[5];
+    double a = ee[IX(1, 0, 3)] - ee[IX(0, 0, 3)], b = ee[IX(1, 1, 3)] - ee[IX(0, 1, 3)];
+    double c = ee[IX(2, 0, 3)] - ee[IX(0, 0, 3)], d = ee[IX(2, 1, 3)] - ee[IX(0, 1, 3)];
+    double J = a * d - b * c;
+    g[IX(0, 0, 3)] = (b - d) / J; g[IX(1, 0, 3)] = d / J; g[IX(2, 0, 3)] = -b / J;
+    g[IX(0, 1, 3)] = (c - a) / J; g[IX(1, 1, 3)] = -c / J; g[IX(2, 1, 3)] = a / J;
+    double Ae = J / 2;
+    double t;
+    elem_thickness(p, e, &t);
+    /* global -> nodal -> element displacements */
+    double AEs[27], T[18 * 18], edn[18], ede[18];
+    uint8_t nv[3];
+    nodal_triads(AEs, nv, E, nrm, valid, 3);
+    transfmat_g_to_a(T, AEs, E, 3);
+    matvec(T, n, n, ed, edn);
+    transfmat_a_to_e(T, AEs, g, 3);
+    matvec(T, n, n, edn, ede);
+    double s[3] = {0, 0, 0}, v[3];
+    if (quant == ORC_RES_MOMENT || quant == ORC_RES_MEMBRANE) {
+        double B[3 * 18] = {0};
+        for (int i = 0; i < 3; i++) {
+            if (quant == ORC_RES_MEMBRANE) {
+                B[IX(0, 6 * i + 0, 3)] = g[IX(i, 0, 3)];
+                B[IX(1, 6 * i + 1, 3)] = g[IX(i, 1, 3)];
+                B[IX(2, 6 * i + 0, 3)] = g[IX(i, 1, 3)];
+                B[IX(2, 6 * i + 1, 3)] = g[IX(i, 0, 3)];
+            } else {
+                B[IX(0, 6 * i + 4, 3)] = g[IX(i, 0, 3)];
+                B[IX(1, 6 * i + 3, 3)] = -g[IX(i, 1, 3)];
+                B[IX(2, 6 * i + 3, 3)] = -g[IX(i, 0, 3)];
+                B[IX(2, 6 * i + 4, 3)] = g[IX(i, 1, 3)];
+            }
+        }
+        matvec(B, 3, n, ede, s);
+        resultant_material(p, quant, t, 0.0, s, v);
+    } else {
+        /* _Bsmat!: the DSG rows averaged over the three node orderings */
+        double Bs[2 * 18] = {0};
+        add_bsmat_o(Bs, ee, Ae, 0, 1, 2);
+        add_bsmat_o(Bs, ee, Ae, 1, 2, 0);
+        add_bsmat_o(Bs, ee, Ae, 2, 0, 1);
+        for (int i = 0; i < 36; i++) Bs[i] *= (1.0 / 3);
+        matvec(Bs, 2, n, ede, s);
+        resultant_material(p, quant, t, stab_fun(t, sqrt(2 * Ae), p->stab_c), s, v);
+    }
+    resultant_out(E, cs, quant, v, out);
+}
+
+static void q4_resultants(const orc_params *p, int64_t e, const double *X, const double *nrm,
+                          const uint8_t *valid, const double *ed, int quant, const double *cs,
+                          int64_t cs_stride, double *out /* 4 x 3 */)
+{
+    const int n = 24;
+    double t;
+    elem_thickness(p, e, &t);
+    double h = q4_diameter(X);
+    double *T = (double *)malloc(sizeof(double) * 3 * n * n);
+    double *Tae = T + n * n, *Tga = T + 2 * n * n;
+    for (int j = 0; j < 4; j++) {
+        double xi, eta, N[4], gp[8], J[6], E[9], ee[8], g[8];
+        q4_point(j, &xi, &eta);
+        q4_basis(xi, eta, N, gp);
+        q4_jac(X, gp, J);
+        e_g(E, J);
+        double cen[3] = {0, 0, 0};
+        for (int a = 0; a < 4; a++)
+            for (int k = 0; k < 3; k++) cen[k] += X[3 * a + k];
+        for (int k = 0; k < 3; k++) cen[k] /= 4;
+        for (int a = 0; a < 4; a++)
+            for (int k = 0; k < 2; k++) {
+                double dd = 0.0;
+                for (int m = 0; m < 3; m++) dd += (X[3 * a + m] - cen[m]) * E[IX(m, k, 3)];
+                ee[IX(a, k, 4)] = dd;
+            }
+        double G11 = J[0] * J[0] + J[1] * J[1] + J[2] * J[2];
+        double G12 = J[0] * J[3] + J[1] * J[4] + J[2] * J[5];
+        double G22 = J[3] * J[3] + J[4] * J[4] + J[5] * J[5];
+        double detG = G11 * G22 - G12 * G12;
+        double i11 = G22 / detG, i12 = -G12 / detG, i22 = G11 / detG;
+        for (int a = 0; a < 4; a++) {
+            double t1 = i11 * gp[IX(a, 0, 4)] + i12 * gp[IX(a, 1, 4)];
+            double t2 = i12 * gp[IX(a, 0, 4)] + i22 * gp[IX(a, 1, 4)];
+            double vv[3];
+            for (int c = 0; c < 3; c++) vv[c] = J[IX(c, 0, 3)] * t1 + J[IX(c, 1, 3)] * t2;
+            g[IX(a, 0, 4)] = E[0] * vv[0] + E[1] * vv[1] + E[2] * vv[2];
+            g[IX(a, 1, 4)] = E[3] * vv[0] + E[4] * vv[1] + E[5] * vv[2];
+        }
+        double AEs[36];
+        uint8_t nv[4];
+        nodal_triads(AEs, nv, E, nrm, valid, 4);
+        transfmat_g_to_a(Tga, AEs, E, 4);
+        transfmat_a_to_e(Tae, AEs, g, 4);
+        matmul_rn(Tae, n, n, Tga, n, T);
+        double ede[24];
+        matvec(T, n, n, ed, ede);
+        double s[3] = {0, 0, 0}, v[3];
+        if (quant == ORC_RES_MOMENT || quant == ORC_RES_MEMBRANE) {
+            double B[3 * 24] = {0};
+            for (int i = 0; i < 4; i++) {
+                int off = 6 * i;
+                if (quant == ORC_RES_MEMBRANE) {
+                    B[IX(0, off + 0, 3)] = g[IX(i, 0, 4)];
+                    B[IX(1, off + 1, 3)] = g[IX(i, 1, 4)];
+                    B[IX(2, off + 0, 3)] = g[IX(i, 1, 4)];
+                    B[IX(2, off + 1, 3)] = g[IX(i, 0, 4)];
+                } else {
+                    B[IX(0, off + 4, 3)] = g[IX(i, 0, 4)];
+                    B[IX(1, off + 3, 3)] = -g[IX(i, 1, 4)];
+                    B[IX(2, off + 3, 3)] = -g[IX(i, 0, 4)];
+                    B[IX(2, off + 4, 3)] = g[IX(i, 1, 4)];
+                }
+            }
+            matvec(B, 3, n, ede, s);
+            resultant_material(p, quant, t, 0.0, s, v);
+        } else {
+            double Bs[2 * 24];
+            q4_bs_elem(Bs, ee, xi, eta);
+            matvec(Bs, 2, n, ede, s);
+            resultant_material(p, quant, t, stab_fun(t, h, p->stab_c), s, v);
+        }
+        resultant_out(E, cs + cs_stride * j, quant, v, out + 3 * j);
+    }
+    free(T);
+}
+
+int orc_resultants(int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                   const double *normals, const uint8_t *valid, const orc_params *p,
+                   const double *u, int quant, const double *cs, int64_t ncs, double *out)
+{
+    if (p->etype != ORC_T3FF && p->etype != ORC_Q4RS) return 1;
+    if (quant < ORC_RES_MOMENT || quant > ORC_RES_MEMBRANE) return 2;
+    const int nen = nen_of(p->etype), npt = nen == 3 ? 1 : 4;
+    if (ncs != 1 && ncs != nelem * npt) return 3;
+    for (int64_t e = 0; e < nelem; e++) {
+        const int64_t *cn = conn + nen * e;
+        double X[12], nrm[12], ed[24];
+        uint8_t vl[4];
+        gather_X(xyz, nnodes, cn, nen, X);
+        for (int k = 0; k < nen; k++) {
+            int64_t nd = cn[k] - 1;
+            for (int c = 0; c < 3; c++) nrm[3 * k + c] = normals[nd + c * nnodes];
+            vl[k] = valid[nd];
+            for (int c = 0; c < 6; c++) ed[6 * k + c] = u[nd + c * nnodes];
+        }
+        const double *c0 = ncs == 1 ? cs : cs + 9 * npt * e;
+        const int64_t cst = ncs == 1 ? 0 : 9;
+        if (nen == 3)
+            t3_resultant(p, e, X, nrm, vl, ed, quant, c0, out + 3 * e);
+        else
+            q4_resultants(p, e, X, nrm, vl, ed, quant, c0, cst, out + 12 * e);
+    }
+    return 0;
+}

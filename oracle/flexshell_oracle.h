@@ -93,6 +93,19 @@ int orc_cd_steps(int64_t n, const int64_t *rowptr, const int64_t *colidx,
                  const double *vals, const double *invMC, const double *C, double dt,
                  int64_t nsteps, double *U, double *V, double *A, int nthreads);
 
+/* Stress resultants at the integration points of the homogeneous shells
+ * (inspectintegpoints, src/FEMMShellT3FFModule.jl:850-962: the centroid of a
+ * T3FF element; src/FEMMShellQ4RSModule.jl:1061-1170: the four Gauss points
+ * of a Q4RS element): quantity ORC_RES_MOMENT (m_xx, m_yy, m_xy),
+ * ORC_RES_SHEAR (q_x, q_y, 0), ORC_RES_MEMBRANE (n_xx, n_yy, n_xy) in the
+ * output csys.  u: nnodes x 6 column-major displacements and rotations;
+ * cs: one 3x3 column-major csys matrix (ncs = 1) or one per point (ncs =
+ * number of points); out: 3 values per point, points in element order. */
+enum { ORC_RES_MOMENT = 1, ORC_RES_SHEAR = 2, ORC_RES_MEMBRANE = 3 };
+int orc_resultants(int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                   const double *normals, const uint8_t *valid, const orc_params *p,
+                   const double *u, int quant, const double *cs, int64_t ncs, double *out);
+
 /* Laminate stiffness of a layup (CompositeLayupModule). */
 int orc_laminate(int nplies, const double *ply_Dps, const double *ply_Dts,
                  const double *ply_t, const double *ply_angle_deg, const double *ply_rho,

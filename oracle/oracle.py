@@ -24,6 +24,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 
 T3FF, T3FFCOMP, Q4RS, Q4RSCOMP = 0, 1, 2, 3
+RES_MOMENT, RES_SHEAR, RES_MEMBRANE = 1, 2, 3
 KEEP_ZEROS, DROP_ZEROS, DIAG = 0, 1, 2
 
 _c_dbl_p = ctypes.POINTER(ctypes.c_double)
@@ -89,6 +90,7 @@ def lib():
         L.orc_beam_all.restype = ctypes.c_int
         L.orc_beam_element.restype = ctypes.c_int
         L.orc_beam_frame.restype = ctypes.c_double
+        L.orc_resultants.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -185,6 +187,28 @@ class Problem:
             raise RuntimeError("oracle element stiffness failed with status %d" % st)
         # stored column-major per element -> transpose to row-major view
         return np.ascontiguousarray(out.transpose(0, 2, 1))
+
+    def resultants(self, u, quantity, cs=None):
+        """Stress resultants at the integration points (inspectintegpoints):
+        quantity RES_MOMENT, RES_SHEAR or RES_MEMBRANE; u (nnodes, 6); cs one
+        3x3 csys matrix or one per point (npoints, 3, 3), identity by default.
+        Returns (npoints, 3), points in element order (Q4: four per element)."""
+        npt = self.nelem * (1 if self.nen == 3 else 4)
+        u = np.asfortranarray(u, dtype=np.float64)
+        if cs is None:
+            cs = np.eye(3)
+        cs = np.asarray(cs, dtype=np.float64)
+        ncs = 1 if cs.ndim == 2 else cs.shape[0]
+        csf = np.ascontiguousarray(cs.reshape(-1, 3, 3).transpose(0, 2, 1))  # column-major each
+        out = np.zeros((npt, 3), dtype=np.float64)
+        st = lib().orc_resultants(
+            ctypes.c_int64(self.nnodes), _p(self.xyz, _c_dbl_p), ctypes.c_int64(self.nelem),
+            _p(self.conn, _c_i64_p), _p(self.normals, _c_dbl_p), _p(self.valid, _c_u8_p),
+            ctypes.byref(self.params), _p(u, _c_dbl_p), ctypes.c_int(quantity), _p(csf, _c_dbl_p),
+            ctypes.c_int64(ncs), _p(out, _c_dbl_p))
+        if st != 0:
+            raise RuntimeError("oracle resultants failed with status %d" % st)
+        return out
 
     def assemble(self, what="K", mode=KEEP_ZEROS, n=None, nthreads=0):
         """Returns (colptr, rowval, nzval) 1-based CSC arrays (== CSR for
