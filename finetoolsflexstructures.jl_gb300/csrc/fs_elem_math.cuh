@@ -303,6 +303,8 @@ struct MatConst {
     double rho;
     float Lpsf[6], Ltf[3];  // the factors rounded to float (mixed rows)
     float stab_cf;          // stab_c rounded to float
+    double Dps[9];          // Dps itself (symmetrised, column-major) and (5/6) Dt:
+    double Dt5[4];          // the stress resultants at the integration points
 };
 
 // entry i of a packed factor in the working precision: the float copy for
@@ -925,6 +927,179 @@ FS_HD void lumped_mass(const ElemIn<NN> &in, double rho, bool comp, const GroupC
         tm = ts / 4;
         rm = rs / 4;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Stress resultants at the integration points of the homogeneous shells
+// (inspectintegpoints, src/FEMMShellT3FFModule.jl:850-962: the centroid of a
+// T3FF element; src/FEMMShellQ4RSModule.jl:1061-1170: the Gauss points of a
+// Q4RS element).  The element-frame strain rows (membrane, curvature or
+// transverse shear) are expanded to the global dofs with the map of the
+// stiffness rows -- the same T_ae T_ga the reference applies to the element
+// displacements -- and applied to them; the resultant (t Dps strain, t^3/12
+// Dps curvature, t stab (5/6) Dt shear) is seen in the output csys by the
+// angle of Layup2ElementAngle(E_G, csmat).  Double precision throughout.
+// ---------------------------------------------------------------------------
+enum { RES_MOMENT = 1, RES_SHEAR = 2, RES_MEMBRANE = 3 };
+
+template <int NN>
+FS_HD void resultant_rows(int quant, const double g[NN][2], double c[3][NN][5])
+{
+    for (int r = 0; r < 3; r++)
+        for (int i = 0; i < NN; i++)
+            for (int q = 0; q < 5; q++) c[r][i][q] = 0.0;
+    for (int i = 0; i < NN; i++) {
+        if (quant == RES_MEMBRANE) {
+            c[0][i][0] = g[i][0];
+            c[1][i][1] = g[i][1];
+            c[2][i][0] = g[i][1]; c[2][i][1] = g[i][0];
+        } else if (quant == RES_MOMENT) {
+            c[0][i][4] = g[i][0];
+            c[1][i][3] = -g[i][1];
+            c[2][i][3] = -g[i][0]; c[2][i][4] = g[i][1];
+        }
+    }
+}
+
+// FinEtools' isoparametric csys (the shells' default mcsys): e1 along the
+// first tangent, e3 along the normal t1 x t2, e2 = e3 x e1; column-major.
+FS_HD void isoparametric_csys(const double t1[3], const double t2[3], double cs[9])
+{
+    double n[3];
+    cross3(t1, t2, n);
+    const double nn = sqrt(dot3(n, n)), l1 = sqrt(dot3(t1, t1));
+    for (int k = 0; k < 3; k++) {
+        cs[k] = t1[k] / l1;
+        cs[6 + k] = n[k] / nn;
+    }
+    double e2[3];
+    cross3(cs + 6, cs, e2);
+    const double l2 = sqrt(dot3(e2, e2));
+    for (int k = 0; k < 3; k++) cs[3 + k] = e2[k] / l2;
+}
+
+// cs: the output csys (column-major), or null for the isoparametric csys of
+// the point's tangents t1, t2
+template <int NN>
+FS_HD void resultant_finish(int quant, const GlobalMap<double, NN> &M, const double e[3][3],
+                            const double c[3][NN][5], const double ue[6 * NN], const MatConst &mc, double t,
+                            double stab, const double *cs, const double t1[3], const double t2[3], double out[3])
+{
+    const int nr = quant == RES_SHEAR ? 2 : 3;
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int r = 0; r < nr; r++) {
+        double row[6 * NN];
+        expand_row<double, NN>(M, c[r], row);
+        double acc = 0.0;
+        for (int k = 0; k < 6 * NN; k++) acc += row[k] * ue[k];
+        s[r] = acc;
+    }
+    double v[3];
+    if (quant == RES_SHEAR) {
+        const double f = t * stab;
+        v[0] = f * (mc.Dt5[0] * s[0] + mc.Dt5[2] * s[1]);
+        v[1] = f * (mc.Dt5[1] * s[0] + mc.Dt5[3] * s[1]);
+        v[2] = 0.0;
+    } else {
+        const double f = quant == RES_MOMENT ? (t * t * t) / 12 : t;
+        for (int i = 0; i < 3; i++) v[i] = f * (mc.Dps[i] * s[0] + mc.Dps[i + 3] * s[1] + mc.Dps[i + 6] * s[2]);
+    }
+    // o2 = [m n; -n m]: moments and membrane forces o2' T o2, shear forces o2' f
+    double csi[9];
+    if (!cs) {
+        isoparametric_csys(t1, t2, csi);
+        cs = csi;
+    }
+    double m, n;
+    layup_angle(e, cs, m, n);
+    if (quant == RES_SHEAR) {
+        out[0] = m * v[0] - n * v[1];
+        out[1] = n * v[0] + m * v[1];
+        out[2] = 0.0;
+    } else {
+        const double t00 = m * v[0] - n * v[2], t01 = m * v[2] - n * v[1];
+        const double t10 = n * v[0] + m * v[2], t11 = n * v[2] + m * v[1];
+        out[0] = t00 * m - t01 * n;
+        out[1] = t10 * n + t11 * m;
+        out[2] = t00 * n + t01 * m;
+    }
+}
+
+// T3FF: one point, the centroid.  ue: the element's 18 global displacements.
+FS_HD void t3_resultant(const ElemIn<3> &in, const MatConst &mc, const double ue[18], int quant,
+                        const double *cs, double out[3])
+{
+    double J0[3], J1[3], e[3][3];
+    for (int c = 0; c < 3; c++) {
+        J0[c] = in.X[1][c] - in.X[0][c];
+        J1[c] = in.X[2][c] - in.X[0][c];
+    }
+    make_frame(J0, J1, e);
+    const double a = dot3(J0, e[0]), b = dot3(J0, e[1]);
+    const double cc = dot3(J1, e[0]), d = dot3(J1, e[1]);
+    const double Jd = a * d - b * cc, Ae = Jd / 2, iJ = 1.0 / Jd;
+    double g[3][2];
+    g[0][0] = (b - d) * iJ; g[1][0] = d * iJ; g[2][0] = -b * iJ;
+    g[0][1] = (cc - a) * iJ; g[1][1] = -cc * iJ; g[2][1] = a * iJ;
+    double A[3][3][3];
+    for (int i = 0; i < 3; i++) nodal_triad(e, in.nrm[i], in.valid[i], A[i]);
+    GlobalMap<double, 3> M;
+    build_map<double, 3>(e, A, g, M);
+    double c[3][3][5];
+    resultant_rows<3>(quant, g, c);
+    if (quant == RES_SHEAR) {
+        // _Bsmat!: the DSG rows averaged over the three node orderings
+        const double x[3] = {0.0, a, cc}, y[3] = {0.0, b, d};
+        t3_bs_ordering<double>(x, y, Ae, 0, 1, 2, (double(*)[3][5])c[0], 1.0 / 3);
+        t3_bs_ordering<double>(x, y, Ae, 1, 2, 0, (double(*)[3][5])c[0], 1.0 / 3);
+        t3_bs_ordering<double>(x, y, Ae, 2, 0, 1, (double(*)[3][5])c[0], 1.0 / 3);
+    }
+    const double t = in.t;
+    const double stab = t * t / (t * t + mc.stab_c * (2 * Ae));
+    resultant_finish<3>(quant, M, e, c, ue, mc, t, stab, cs, J0, J1, out);
+}
+
+// Q4RS: Gauss point j (0..3, the reference's point order).  Returns nonzero
+// on a singular metric (src/FEMMShellQ4RSModule.jl:308-311).
+FS_HD int q4_resultant(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatConst &mc,
+                       const double ue[24], int quant, const double *cs, double out[3])
+{
+    double xi, eta, gp[4][2];
+    q4_point(j, xi, eta);
+    q4_dbasis(xi, eta, gp);
+    double J0[3], J1[3];
+    for (int c = 0; c < 3; c++) {
+        J0[c] = qe.Xr[0][c] * gp[0][0] + qe.Xr[1][c] * gp[1][0] + qe.Xr[2][c] * gp[2][0] + qe.Xr[3][c] * gp[3][0];
+        J1[c] = qe.Xr[0][c] * gp[0][1] + qe.Xr[1][c] * gp[1][1] + qe.Xr[2][c] * gp[2][1] + qe.Xr[3][c] * gp[3][1];
+    }
+    double e[3][3];
+    make_frame(J0, J1, e);
+    double X[4], Y[4];
+    for (int a = 0; a < 4; a++) {
+        X[a] = dot3(qe.Xr[a], e[0]);
+        Y[a] = dot3(qe.Xr[a], e[1]);
+    }
+    const double G11 = dot3(J0, J0), G12 = dot3(J0, J1), G22 = dot3(J1, J1);
+    const double detG = G11 * G22 - G12 * G12;
+    if (detG == 0.0) return 4;
+    const double i11 = G22 / detG, i12 = -G12 / detG, i22 = G11 / detG;
+    const double pj0[2] = {dot3(e[0], J0), dot3(e[1], J0)}, pj1[2] = {dot3(e[0], J1), dot3(e[1], J1)};
+    double g[4][2];
+    for (int a = 0; a < 4; a++) {
+        const double t1 = i11 * gp[a][0] + i12 * gp[a][1];
+        const double t2 = i12 * gp[a][0] + i22 * gp[a][1];
+        g[a][0] = pj0[0] * t1 + pj1[0] * t2;
+        g[a][1] = pj0[1] * t1 + pj1[1] * t2;
+    }
+    double A[4][3][3];
+    for (int i = 0; i < 4; i++) nodal_triad(e, in.nrm[i], in.valid[i], A[i]);
+    GlobalMap<double, 4> M;
+    build_map<double, 4>(e, A, g, M);
+    double c[3][4][5];
+    resultant_rows<4>(quant, g, c);
+    if (quant == RES_SHEAR) q4_bs<double>(X, Y, xi, eta, (double(*)[4][5])c[0]);
+    resultant_finish<4>(quant, M, e, c, ue, mc, in.t, qe.stab, cs, J0, J1, out);
+    return 0;
 }
 
 }  // namespace fs

@@ -57,6 +57,8 @@ inline int prepare_matconst(const fs_shell_params &p, MatConst &mc)
     for (int i = 0; i < 6; i++) mc.Lpsf[i] = (float)mc.Lps[i];
     for (int i = 0; i < 3; i++) mc.Ltf[i] = (float)mc.Lt[i];
     mc.stab_cf = (float)mc.stab_c;
+    for (int i = 0; i < 9; i++) mc.Dps[i] = Dps[i];
+    for (int i = 0; i < 4; i++) mc.Dt5[i] = Dt[i];
     return 0;
 }
 

@@ -15,6 +15,7 @@ FS_FP64, FS_MIXED, FS_MIXED_COMP = 0, 1, 2
 FS_ASM_SPARSE, FS_ASM_SPARSE_SYMM, FS_ASM_DIAG = 0, 1, 2
 FS_BEAM_STIFFNESS, FS_BEAM_GEOSTIFFNESS, FS_BEAM_MASS, FS_BEAM_GYROSCOPIC = 0, 1, 2, 3
 FS_BEAM_RESTORING, FS_BEAM_DISTRIBLOAD = 4, 5
+FS_RES_MOMENT, FS_RES_SHEAR, FS_RES_MEMBRANE = 1, 2, 3
 
 
 class fs_beam_section(ctypes.Structure):

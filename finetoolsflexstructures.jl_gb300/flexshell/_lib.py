@@ -62,6 +62,7 @@ def lib():
         L.fs_laminate.argtypes = [ctypes.c_int32, vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_int32,
                                   ctypes.c_double, ctypes.POINTER(_abi.fs_layup_group)]
         L.fs_restoring_force.argtypes = [vp, vp, vp]
+        L.fs_resultants.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int64, vp]
         L.fs_pattern.argtypes = [vp, ctypes.c_int64, _c_i64_p]
         L.fs_stiffness_copy.argtypes = [vp, ctypes.c_int, ctypes.c_int64, vp, vp, vp]
         L.fs_autotune.argtypes = [vp, ctypes.c_int]

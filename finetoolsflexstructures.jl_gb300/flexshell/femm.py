@@ -260,6 +260,82 @@ class _FEMMShell:
         self.ctx.call("fs_restoring_force", ptr(U), ptr(F))
         return F
 
+    # quantity symbols of inspectintegpoints (src/FEMMShellT3FFModule.jl:893-902);
+    # anything else (the default :Cauchy) reports the bending moments
+    _RES_QUANTITY = {"bending": _abi.FS_RES_MOMENT, "moment": _abi.FS_RES_MOMENT,
+                     "bending_moment": _abi.FS_RES_MOMENT, "transverse_shear": _abi.FS_RES_SHEAR,
+                     "transverse": _abi.FS_RES_SHEAR, "shear": _abi.FS_RES_SHEAR,
+                     "membrane_force": _abi.FS_RES_MEMBRANE, "membrane": _abi.FS_RES_MEMBRANE}
+
+    def _point_locations(self, geom0):
+        """Integration points: per point its element (0-based), its tangents
+        (3x2) and its location, in the reference's point order."""
+        X = np.asarray(geom0.values, dtype=np.float64)[self.conn - 1]  # nelem x nen x 3
+        if self.nen == 3:
+            tang = np.stack([X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]], axis=2)
+            return np.arange(X.shape[0]), np.zeros(X.shape[0], dtype=np.int64), tang, X.mean(axis=1)
+        gp = 0.577350269189626
+        locs, tangs = [], []
+        for j in range(4):
+            xi, eta = (-gp if j < 2 else gp), (gp if j & 1 else -gp)
+            N = np.array([(1 - xi) * (1 - eta), (1 + xi) * (1 - eta), (1 + xi) * (1 + eta), (1 - xi) * (1 + eta)]) / 4
+            dxi = np.array([-(1 - eta), (1 - eta), (1 + eta), -(1 + eta)]) / 4
+            deta = np.array([-(1 - xi), -(1 + xi), (1 + xi), (1 - xi)]) / 4
+            locs.append(np.einsum("a,eac->ec", N, X))
+            tangs.append(np.stack([np.einsum("a,eac->ec", dxi, X), np.einsum("a,eac->ec", deta, X)], axis=2))
+        ne = X.shape[0]
+        el = np.repeat(np.arange(ne), 4)
+        qp = np.tile(np.arange(1, 5), ne)
+        return el, qp, np.stack(tangs, axis=1).reshape(ne * 4, 3, 2), np.stack(locs, axis=1).reshape(ne * 4, 3)
+
+    def resultants(self, geom0, u, quantity="bending", outputcsys=None):
+        """Stress resultants at every integration point (npoints x 3): the
+        values inspectintegpoints hands to its inspector, in double.  outputcsys:
+        None (the isoparametric csys, the reference's default mcsys), a 3x3
+        matrix, an (npoints, 3, 3) array, or a callable (XYZ, tangents, feid,
+        qpid) -> 3x3 evaluated per point like updatecsmat!."""
+        if not self._associatedgeometry:
+            raise AssertionError("self._associatedgeometry == true")
+        self._sync_inputs(geom0, None)
+        q = self._RES_QUANTITY.get(str(quantity).lstrip(":"), _abi.FS_RES_MOMENT)
+        uu = np.asfortranarray(u.values if hasattr(u, "values") else u, dtype=np.float64)
+        if uu.shape != (geom0.values.shape[0], 6):
+            raise ValueError("u must hold 6 values per node")
+        npt = self.conn.shape[0] * (1 if self.nen == 3 else 4)
+        if outputcsys is None:
+            cs, ncs = None, 0
+        elif callable(outputcsys):
+            el, qp, tang, loc = self._point_locations(geom0)
+            cs = np.stack([np.asarray(outputcsys(loc[k].reshape(1, 3), tang[k], el[k] + 1, qp[k]), dtype=np.float64)
+                           for k in range(npt)])
+            ncs = npt
+        else:
+            cs = np.asarray(outputcsys, dtype=np.float64)
+            ncs = 1 if cs.ndim == 2 else cs.shape[0]
+        csf = None if cs is None else np.ascontiguousarray(cs.reshape(-1, 3, 3).transpose(0, 2, 1))
+        out = np.zeros((npt, 3))
+        self.ctx.call("fs_resultants", q, ptr(uu), ptr(csf), ncs, ptr(out))
+        return out
+
+    def inspectintegpoints(self, geom0, u, felist, inspector, idat, quantity="Cauchy", outputcsys=None):
+        """inspectintegpoints(femm, geom0, u, felist, inspector, idat, quantity;
+        outputcsys) (src/FEMMShellT3FFModule.jl:850-962, src/FEMMShellQ4RSModule.jl:
+        1061-1170): all points are evaluated on the GPU in one launch, then
+        inspector(idat, i, conn, ecoords, out, loc) is called for every point of
+        the elements of felist (1-based element numbers) in the reference's
+        order, and the final idat is returned."""
+        out = self.resultants(geom0, u, quantity, outputcsys)
+        X = np.asarray(geom0.values, dtype=np.float64)
+        el, qp, _, loc = self._point_locations(geom0)
+        npe = 1 if self.nen == 3 else 4
+        for i in felist:
+            e = int(i) - 1
+            for j in range(npe):
+                k = e * npe + j
+                idat = inspector(idat, int(i), self.conn[e], X[self.conn[e] - 1], out[k].copy(),
+                                 loc[k].reshape(1, 3))
+        return idat
+
     # -- extras ----------------------------------------------------------------
     def element_matrices(self, geom0, precision=FS_FP64):
         """All element stiffness matrices in the global basis (nelem x nd x nd)."""

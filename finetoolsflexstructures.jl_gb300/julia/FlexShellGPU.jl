@@ -8,8 +8,11 @@ driver code calls them unchanged:
     stiffness(femm::FEMMShellT3FF, assembler, geom0, u1, Rfield1, dchi)
     mass(femm::FEMMShellT3FF, assembler, geom0, dchi)
 
-(and the same for FEMMShellQ4RS, FEMMShellT3FFComp, FEMMShellQ4RSComp), and
-for FEMMCorotBeam
+(and the same for FEMMShellQ4RS, FEMMShellT3FFComp, FEMMShellQ4RSComp),
+
+    inspectintegpoints(femm, geom0, u, dT, felist, inspector, idat, quantity; outputcsys)
+
+for FEMMShellT3FF and FEMMShellQ4RS, and for FEMMCorotBeam
 
     stiffness / geostiffness (femm, assembler, geom0, u1, Rfield1, dchi)
     mass(femm, assembler, geom0, u1, Rfield1, dchi; mass_type)
@@ -29,6 +32,8 @@ using FinEtoolsFlexStructures.FEMMShellT3FFModule: FEMMShellT3FF
 using FinEtoolsFlexStructures.FEMMShellQ4RSModule: FEMMShellQ4RS
 import FinEtoolsFlexStructures.FEMMShellT3FFModule: stiffness, mass
 import FinEtoolsFlexStructures.FEMMShellQ4RSModule: stiffness, mass
+import FinEtoolsFlexStructures.FEMMShellT3FFModule: inspectintegpoints
+import FinEtoolsFlexStructures.FEMMShellQ4RSModule: inspectintegpoints
 using FinEtoolsFlexStructures.FEMMCorotBeamModule: FEMMCorotBeam
 import FinEtoolsFlexStructures.FEMMCorotBeamModule: geostiffness, gyroscopic, restoringforce,
     distribloads_global
@@ -99,7 +104,7 @@ function upload!(ctx, femm, etype, geom0, dchi)
     xyz = geom0.values                                  # nnodes x 3, column-major
     check(ctx, ccall((:fs_mesh_set, libflexshell), Cint,
         (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
-        ctx.h, etype, size(xyz, 1), xyz, count(fes), conn, C_NULL, dchi.dofnums))
+        ctx.h, etype, size(xyz, 1), xyz, count(fes), conn, C_NULL, dchi === nothing ? C_NULL : dchi.dofnums))
     Dps, Dt = femm_material_matrices(femm)
     t = femm.integdomain.otherdimension(zeros(1, 3), fes.conn[1], zeros(1, 1))
     p = FsShellParams(etype == FS_T3FF ? femm.transv_shear_formulation : 0, 0,
@@ -145,6 +150,69 @@ for (T, etype) in ((FEMMShellT3FF, FS_T3FF), (FEMMShellQ4RS, FS_Q4RS))
         check(ctx, ccall((:fs_mass, libflexshell), Cint, (Ptr{Cvoid}, Cint, Int64, Ref{Int64}),
             ctx.h, asm_mode(assembler), nalldofs(dchi), nnz))
         return fetch_csc(ctx, nalldofs(dchi), nnz[])
+    end
+end
+
+# ---------------------------------------------------------------------------
+# inspectintegpoints (src/FEMMShellT3FFModule.jl:850-962,
+# src/FEMMShellQ4RSModule.jl:1061-1170): the resultants of every integration
+# point come from one fs_resultants call; the output csys is evaluated here,
+# per point, with the reference's own updatecsmat!, and the inspector is then
+# called for the points of felist in the reference's order.
+# ---------------------------------------------------------------------------
+const FS_RES_MOMENT, FS_RES_SHEAR, FS_RES_MEMBRANE = 1, 2, 3
+
+function res_quantity(quantity)
+    quantity in (:transverse_shear, :transverse, :shear) && return FS_RES_SHEAR
+    quantity in (:membrane_force, :membrane) && return FS_RES_MEMBRANE
+    return FS_RES_MOMENT    # :bending, :moment, :bending_moment, and the default :Cauchy
+end
+
+# location (1x3) and tangents (3x2) of point j of element i: the centroid and
+# the edge Jacobian of a T3; Gauss point j of GaussRule(2,2) of a Q4
+function point_geometry(geom0, conn, j, nen)
+    X = geom0.values[collect(conn), :]
+    if nen == 3
+        return sum(X, dims = 1) ./ 3, hcat(X[2, :] - X[1, :], X[3, :] - X[1, :])
+    end
+    g = 0.577350269189626
+    xi, eta = (j <= 2 ? -g : g), (iseven(j) ? g : -g)
+    N = [(1 - xi) * (1 - eta), (1 + xi) * (1 - eta), (1 + xi) * (1 + eta), (1 - xi) * (1 + eta)] ./ 4
+    dN = [-(1 - eta) -(1 - xi); (1 - eta) -(1 + xi); (1 + eta) (1 + xi); -(1 + eta) (1 - xi)] ./ 4
+    return reshape(N' * X, 1, 3), X' * dN
+end
+
+for (T, etype, nen) in ((FEMMShellT3FF, FS_T3FF, 3), (FEMMShellQ4RS, FS_Q4RS, 4))
+    @eval function inspectintegpoints(self::$T, geom0::NodalField{FFlt}, u::NodalField{TI},
+        dT::NodalField{FFlt}, felist::FIntVec, inspector::F, idat, quantity = :Cauchy;
+        context...) where {TI<:Number,F<:Function}
+        @assert self._associatedgeometry == true
+        fes = self.integdomain.fes
+        outputcsys = self.mcsys
+        for apair in pairs(context)
+            sy, val = apair
+            sy == :outputcsys && (outputcsys = val)
+        end
+        npe = $nen == 3 ? 1 : 4
+        npt = count(fes) * npe
+        cs = Array{Float64}(undef, 3, 3, npt)
+        for i in 1:count(fes), j in 1:npe
+            loc, J = point_geometry(geom0, fes.conn[i], j, $nen)
+            updatecsmat!(outputcsys, loc, J, i, $nen == 3 ? 0 : j)
+            cs[:, :, (i - 1) * npe + j] .= csmat(outputcsys)
+        end
+        ctx = context(self)
+        upload!(ctx, self, $etype, geom0, nothing)
+        out = Array{Float64}(undef, 3, npt)
+        check(ctx, ccall((:fs_resultants, libflexshell), Cint,
+            (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Float64}),
+            ctx.h, res_quantity(quantity), Matrix{Float64}(u.values), cs, npt, out))
+        for i in felist, j in 1:npe
+            loc, _ = point_geometry(geom0, fes.conn[i], j, $nen)
+            idat = inspector(idat, i, fes.conn[i], geom0.values[collect(fes.conn[i]), :],
+                out[:, (i - 1) * npe + j], loc)
+        end
+        return idat
     end
 end
 

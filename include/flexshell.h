@@ -283,6 +283,27 @@ int fs_batch_matrix_copy(fs_ctx *ctx, int32_t mesh, int64_t *colptr, int64_t *ro
  * here follows FEMMCorotBeam.restoringforce (force on the nodes). */
 int fs_restoring_force(fs_ctx *ctx, const double *U, double *F);
 
+/* Stress resultants at the integration points of a homogeneous shell mesh,
+ * in double: inspectintegpoints(femm, geom0, u, felist, inspector, idat,
+ * quantity; outputcsys) of FEMMShellT3FF (src/FEMMShellT3FFModule.jl:850-962,
+ * one point per element: the centroid) and FEMMShellQ4RS
+ * (src/FEMMShellQ4RSModule.jl:1061-1170, the four Gauss points in the
+ * reference's order), for all elements at once; the host applies the
+ * inspector to the points of felist.  quantity: FS_RES_MOMENT (:bending,
+ * :moment, :bending_moment -> m_xx, m_yy, m_xy), FS_RES_SHEAR (:shear,
+ * :transverse, :transverse_shear -> q_x, q_y, 0), FS_RES_MEMBRANE (:membrane,
+ * :membrane_force -> n_xx, n_yy, n_xy), in the output csys.
+ * u: nnodes x 6 column-major (u.values); csmat: the output csys, ncs = 1 one
+ * 3x3 column-major matrix for every point, or ncs = number of points (nelem
+ * for T3FF, 4 nelem for Q4RS), one per point in element order, or csmat =
+ * NULL with ncs = 0: FinEtools' isoparametric csys of each point (the
+ * default mcsys of the shells); out: 3 doubles per point, element order.
+ * Needs the normals (associategeometry!). */
+#define FS_RES_MOMENT 1
+#define FS_RES_SHEAR 2
+#define FS_RES_MEMBRANE 3
+int fs_resultants(fs_ctx *ctx, int quantity, const double *u, const double *csmat, int64_t ncs, double *out);
+
 /* --- layup reduction (src/CompositeLayupModule.jl:246-330) ------------------ */
 /* ply_Dps: nplies x 9, ply_Dts: nplies x 4 (column-major each); angles in degrees;
  * shear_model 0 = Vinson-Sierakowski, 1 = constant `tcf`. Host only. */

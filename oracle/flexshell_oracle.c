@@ -1195,6 +1195,22 @@ static void resultant_out(const double *E, const double *cs, int quant, const do
     out[2] = R[IX(0, 1, 2)];
 }
 
+/* FinEtools isoparametric! csys (the default mcsys of the shells): e1 along
+ * the first tangent, e3 along the normal t1 x t2, e2 = e3 x e1; column-major */
+static void isoparametric_csys(const double *t1, const double *t2, double *cs)
+{
+    double n[3] = {t1[1] * t2[2] - t1[2] * t2[1], t1[2] * t2[0] - t1[0] * t2[2], t1[0] * t2[1] - t1[1] * t2[0]};
+    double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    double l1 = sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+    for (int k = 0; k < 3; k++) {
+        cs[k] = t1[k] / l1;
+        cs[6 + k] = n[k] / nn;
+    }
+    double e2[3] = {cs[7] * cs[2] - cs[8] * cs[1], cs[8] * cs[0] - cs[6] * cs[2], cs[6] * cs[1] - cs[7] * cs[0]};
+    double l2 = sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
+    for (int k = 0; k < 3; k++) cs[3 + k] = e2[k] / l2;
+}
+
 static void matvec(const double *A, int r, int c, const double *x, double *y)
 {
     for (int i = 0; i < r; i++) {
@@ -1281,6 +1297,11 @@ static void t3_resultant(const orc_params *p, int64_t e, const double *X, const 
         matvec(Bs, 2, n, ede, s);
         resultant_material(p, quant, t, stab_fun(t, sqrt(2 * Ae), p->stab_c), s, v);
     }
+    double csi[9];
+    if (!cs) {
+        isoparametric_csys(J0, J0 + 3, csi);
+        cs = csi;
+    }
     resultant_out(E, cs, quant, v, out);
 }
 
@@ -1356,7 +1377,9 @@ static void q4_resultants(const orc_params *p, int64_t e, const double *X, const
             matvec(Bs, 2, n, ede, s);
             resultant_material(p, quant, t, stab_fun(t, h, p->stab_c), s, v);
         }
-        resultant_out(E, cs + cs_stride * j, quant, v, out + 3 * j);
+        double csi[9];
+        if (!cs) isoparametric_csys(J, J + 3, csi);
+        resultant_out(E, cs ? cs + cs_stride * j : csi, quant, v, out + 3 * j);
     }
     free(T);
 }
@@ -1368,7 +1391,7 @@ int orc_resultants(int64_t nnodes, const double *xyz, int64_t nelem, const int64
     if (p->etype != ORC_T3FF && p->etype != ORC_Q4RS) return 1;
     if (quant < ORC_RES_MOMENT || quant > ORC_RES_MEMBRANE) return 2;
     const int nen = nen_of(p->etype), npt = nen == 3 ? 1 : 4;
-    if (ncs != 1 && ncs != nelem * npt) return 3;
+    if (ncs != 0 && ncs != 1 && ncs != nelem * npt) return 3;
     for (int64_t e = 0; e < nelem; e++) {
         const int64_t *cn = conn + nen * e;
         double X[12], nrm[12], ed[24];
@@ -1380,7 +1403,7 @@ int orc_resultants(int64_t nnodes, const double *xyz, int64_t nelem, const int64
             vl[k] = valid[nd];
             for (int c = 0; c < 6; c++) ed[6 * k + c] = u[nd + c * nnodes];
         }
-        const double *c0 = ncs == 1 ? cs : cs + 9 * npt * e;
+        const double *c0 = ncs == 0 ? NULL : (ncs == 1 ? cs : cs + 9 * npt * e);
         const int64_t cst = ncs == 1 ? 0 : 9;
         if (nen == 3)
             t3_resultant(p, e, X, nrm, vl, ed, quant, c0, out + 3 * e);

@@ -191,15 +191,17 @@ class Problem:
     def resultants(self, u, quantity, cs=None):
         """Stress resultants at the integration points (inspectintegpoints):
         quantity RES_MOMENT, RES_SHEAR or RES_MEMBRANE; u (nnodes, 6); cs one
-        3x3 csys matrix or one per point (npoints, 3, 3), identity by default.
+        3x3 csys matrix or one per point (npoints, 3, 3); None: the
+        isoparametric csys at each point (the shells' default mcsys).
         Returns (npoints, 3), points in element order (Q4: four per element)."""
         npt = self.nelem * (1 if self.nen == 3 else 4)
         u = np.asfortranarray(u, dtype=np.float64)
         if cs is None:
-            cs = np.eye(3)
-        cs = np.asarray(cs, dtype=np.float64)
-        ncs = 1 if cs.ndim == 2 else cs.shape[0]
-        csf = np.ascontiguousarray(cs.reshape(-1, 3, 3).transpose(0, 2, 1))  # column-major each
+            ncs, csf = 0, None
+        else:
+            cs = np.asarray(cs, dtype=np.float64)
+            ncs = 1 if cs.ndim == 2 else cs.shape[0]
+            csf = np.ascontiguousarray(cs.reshape(-1, 3, 3).transpose(0, 2, 1))  # column-major each
         out = np.zeros((npt, 3), dtype=np.float64)
         st = lib().orc_resultants(
             ctypes.c_int64(self.nnodes), _p(self.xyz, _c_dbl_p), ctypes.c_int64(self.nelem),

@@ -110,6 +110,57 @@ extern "C" int hc_element_matrices(int etype, int precision, int64_t nnodes, con
                                 egroup, out, precision == 2);
 }
 
+// Stress resultants at the integration points (the device point math of
+// csrc/fs_elem_math.cuh): quantity 1 moment, 2 shear, 3 membrane; u nnodes x 6
+// column-major; cs one 3x3 column-major matrix (ncs = 1), one per point, or
+// none (ncs = 0: the isoparametric csys).
+extern "C" int hc_resultants(int etype, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                             const double *normals, const uint8_t *valid, const double *thick,
+                             const fs_shell_params *p, const double *u, int quant, const double *cs, int64_t ncs,
+                             double *out)
+{
+    MatConst mc;
+    if (prepare_matconst(*p, mc)) return 1;
+    const int nn = etype == FS_T3FF ? 3 : 4, npt = nn == 3 ? 1 : 4;
+    for (int64_t e = 0; e < nelem; e++) {
+        double ue[24];
+        for (int a = 0; a < nn; a++)
+            for (int k = 0; k < 6; k++) ue[6 * a + k] = u[(conn[nn * e + a] - 1) + k * nnodes];
+        if (nn == 3) {
+            ElemIn<3> in;
+            for (int a = 0; a < 3; a++) {
+                int64_t node = conn[3 * e + a] - 1;
+                for (int c = 0; c < 3; c++) {
+                    in.X[a][c] = xyz[node + c * nnodes];
+                    in.nrm[a][c] = normals[node + c * nnodes];
+                }
+                in.valid[a] = valid[node] != 0;
+            }
+            in.t = thick[e];
+            t3_resultant(in, mc, ue, quant, ncs == 0 ? nullptr : (ncs == 1 ? cs : cs + 9 * e), out + 3 * e);
+        } else {
+            ElemIn<4> in;
+            for (int a = 0; a < 4; a++) {
+                int64_t node = conn[4 * e + a] - 1;
+                for (int c = 0; c < 3; c++) {
+                    in.X[a][c] = xyz[node + c * nnodes];
+                    in.nrm[a][c] = normals[node + c * nnodes];
+                }
+                in.valid[a] = valid[node] != 0;
+            }
+            in.t = thick[e];
+            Q4Elem qe;
+            q4_prepare(in, in.t, mc.stab_c, qe);
+            for (int j = 0; j < 4; j++) {
+                const int64_t q = npt * e + j;
+                if (q4_resultant(in, qe, j, mc, ue, quant, ncs == 0 ? nullptr : (ncs == 1 ? cs : cs + 9 * q), out + 3 * q))
+                    return 4;
+            }
+        }
+    }
+    return 0;
+}
+
 extern "C" int hc_lumped(int etype, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
                          const double *thick, double rho, const fs_layup_group *groups,
                          const int32_t *egroup, double *out)

@@ -55,6 +55,32 @@ def element_matrices(etype, precision, xyz, conn, normals, valid, thickness, par
     return out.transpose(0, 2, 1).copy()
 
 
+def resultants(etype, xyz, conn, normals, valid, thickness, params, u, quantity, cs=None):
+    """The library's integration-point resultant math on the host: (npoints, 3)."""
+    xyz = np.asfortranarray(xyz, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int64)
+    normals = np.asfortranarray(normals, dtype=np.float64)
+    valid = np.ascontiguousarray(valid, dtype=np.uint8)
+    u = np.asfortranarray(u, dtype=np.float64)
+    nelem = conn.shape[0]
+    th = np.ascontiguousarray(np.broadcast_to(np.asarray(thickness, float), (nelem,)))
+    npt = nelem * (1 if conn.shape[1] == 3 else 4)
+    if cs is None:
+        ncs, csf = 0, None
+    else:
+        cs = np.asarray(cs, dtype=np.float64)
+        ncs = 1 if cs.ndim == 2 else cs.shape[0]
+        csf = np.ascontiguousarray(cs.reshape(-1, 3, 3).transpose(0, 2, 1))
+    out = np.zeros((npt, 3))
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+    st = lib().hc_resultants(ctypes.c_int(etype), ctypes.c_int64(xyz.shape[0]), P(xyz), ctypes.c_int64(nelem),
+                             P(conn), P(normals), P(valid), P(th), ctypes.byref(params), P(u),
+                             ctypes.c_int(quantity), P(csf), ctypes.c_int64(ncs), P(out))
+    if st != 0:
+        raise RuntimeError("host check failed with status %d" % st)
+    return out
+
+
 def beam_elements(which, xyz, conn, sections, E, nu, rho=0.0, u1=None, R1=None, v1=None,
                   mass_type=1, q=None):
     """The library's beam element math on the host: (nelem,12,12) or (nelem,12)."""
