@@ -4,14 +4,16 @@
 
 namespace fs {
 
-template <class R, bool COMP, int EPB, class S>
-__global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
+// The elements per block (the tuned tile) is a launch parameter (block size
+// / 4): every tile runs the same compiled kernel and the same arithmetic.
+template <class R, bool COMP, class S>
+__global__ void __launch_bounds__(256) k_q4_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
 {
     constexpr int NR = 36, ND = 24, STRIDE = NR * ND + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int el = threadIdx.x >> 2, qp = threadIdx.x & 3;
     R *rows = reinterpret_cast<R *>(smem_raw) + el * STRIDE;
-    int64_t r = (int64_t)blockIdx.x * EPB + el;
+    int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 2) + el;
     const bool active = r < m.nelem;
     ElemIn<4> in;
     double tr[4] = {0, 0, 0, 0};
@@ -77,25 +79,17 @@ __global__ void __launch_bounds__(EPB * 4) k_q4_elements(const MeshDev m, const 
     }
 }
 
-template <class R, class S, bool COMP, int EPB>
-static int run_q4_epb(fs_ctx *c, S *ke)
-{
-    const size_t smem = q4_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, EPB);
-    auto kern = k_q4_elements<R, COMP, EPB, S>;
-    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<nblk2(c->mesh.nelem, EPB), EPB * 4, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
-    FS_CUDA(c, cudaGetLastError());
-    return FS_OK;
-}
-
 template <class R, bool COMP, class S = R>
 static int run_q4(fs_ctx *c, S *ke)
 {
     int epb = c->tune.elem_epb;
-    if (epb <= 0) epb = 32;
-    if (epb == 16) return run_q4_epb<R, S, COMP, 16>(c, ke);
-    if (epb == 64 && sizeof(R) == 4) return run_q4_epb<R, S, COMP, 64>(c, ke);
-    return run_q4_epb<R, S, COMP, 32>(c, ke);
+    if (epb != 16 && !(epb == 64 && sizeof(R) == 4)) epb = 32;
+    const size_t smem = q4_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, epb);
+    auto kern = k_q4_elements<R, COMP, S>;
+    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<nblk2(c->mesh.nelem, epb), epb * 4, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
 }
 
 // every Q4 variant: row precision, storage, layered

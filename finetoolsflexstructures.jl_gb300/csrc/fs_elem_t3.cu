@@ -4,15 +4,19 @@
 
 namespace fs {
 
-template <class R, bool COMP, bool AVGK, int EPB, class S>
-__global__ void __launch_bounds__(EPB) k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
+// The elements per block (the tuned tile) is the block size, a launch
+// parameter: every tile runs the same compiled kernel, so the tile never
+// changes the arithmetic of an element (compiled variants could contract
+// products and sums into FMAs differently).
+template <class R, bool COMP, bool AVGK, class S>
+__global__ void __launch_bounds__(128) k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
 {
     constexpr int NR = T3Rows<AVGK>::N;
     constexpr int ND = 18;
     constexpr int STRIDE = NR * ND + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R *rows = reinterpret_cast<R *>(smem_raw) + threadIdx.x * STRIDE;
-    int64_t r = (int64_t)blockIdx.x * EPB + threadIdx.x;
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= m.nelem) return;
     ElemIn<3> in;
     load_elem<3>(m, r, in);
@@ -22,25 +26,19 @@ __global__ void __launch_bounds__(EPB) k_t3_elements(const MeshDev m, const MatC
     write_blocks<R, S, 3, !COMP>(rows, NR, ke + r * (6 * 36));
 }
 
-template <class R, class S, bool COMP, bool AVGK, int EPB>
-static int run_t3_epb(fs_ctx *c, S *ke)
-{
-    const size_t smem = t3_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, AVGK, EPB);
-    auto kern = k_t3_elements<R, COMP, AVGK, EPB, S>;
-    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<nblk2(c->mesh.nelem, EPB), EPB, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
-    FS_CUDA(c, cudaGetLastError());
-    return FS_OK;
-}
-
 template <class R, bool COMP, bool AVGK, class S = R>
 static int run_t3(fs_ctx *c, S *ke)
 {
     int epb = c->tune.elem_epb;
     if (epb <= 0) epb = (sizeof(R) == 8 && AVGK) ? 64 : 128;
-    if (epb == 32) return run_t3_epb<R, S, COMP, AVGK, 32>(c, ke);
-    if (epb == 64 || (sizeof(R) == 8 && AVGK)) return run_t3_epb<R, S, COMP, AVGK, 64>(c, ke);
-    return run_t3_epb<R, S, COMP, AVGK, 128>(c, ke);
+    if (epb != 32 && epb != 64) epb = 128;
+    if (sizeof(R) == 8 && AVGK && epb > 64) epb = 64;  // shared memory of the double average-K rows
+    const size_t smem = t3_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, AVGK, epb);
+    auto kern = k_t3_elements<R, COMP, AVGK, S>;
+    FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<nblk2(c->mesh.nelem, epb), epb, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
 }
 
 // every T3 variant: row precision, storage, layered, average-K
