@@ -1,8 +1,10 @@
 // Explicit central-difference time stepping
 // (examples/shells/dynamics/homogeneous/explicit/plate_expl_examples.jl:61-94,
-// _cd_loop!, with mass-proportional damping C and zero external force):
+// _cd_loop!, with mass-proportional damping C and the external force of the
+// example's force!: F(t) = g(t) Fmag, a fixed load vector times a scalar time
+// function, given as its values at the step times):
 //
-//   U += dt V + dt^2/2 A;  E = K U;  F = -(E + C (V + dt/2 A));
+//   U += dt V + dt^2/2 A;  F = g(t) Fmag;  E = K U;  F -= E + C (V + dt/2 A);
 //   V += dt/2 A;  A = invMC F;  V += dt/2 A
 //
 // Two kernels per step: the displacement update, then the product K U fused
@@ -74,6 +76,25 @@ __device__ __forceinline__ void load6(const double *p, double v[6])
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
 }
 
+// External load of step j of the current batch: the state's step index plus
+// j + 1 selects g (zero past the table); null Fmag: no load.
+struct CdLoad {
+    const double *Fmag;
+    const double *mul;
+    int64_t nmul;
+    const int64_t *step;
+    int j;
+    __device__ __forceinline__ double at(int64_t row) const
+    {
+        if (!Fmag) return 0.0;
+        const int64_t s = *step + j + 1;
+        const double g = s < nmul ? mul[s] : 0.0;
+        return g * Fmag[row];
+    }
+};
+
+__global__ void k_step_advance(int64_t *step, int64_t nsteps) { *step += nsteps; }
+
 __device__ __forceinline__ void kahan_add(double &s, double &c, double incr)
 {
     double y = incr - c;
@@ -86,7 +107,8 @@ __device__ __forceinline__ void kahan_add(double &s, double &c, double incr)
 template <class VT>
 __global__ void __launch_bounds__(CD_TPB) k_cd_rows(int64_t n, const int64_t *rowptr, const int32_t *colidx,
                                                   const VT *vals, const VT *Uk, double *V, double *cV,
-                                                  double *A, const double *C, const double *invMC, double dt_2)
+                                                  double *A, const double *C, const double *invMC, double dt_2,
+                                                  CdLoad ld)
 {
     int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / CD_LANES;
     const int sub = threadIdx.x & (CD_LANES - 1);
@@ -100,7 +122,8 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_rows(int64_t n, const int64_t *ro
     double s = (double)sv;
     if (row < n && sub == 0) {
         double a = A[row], v = V[row], cv = cV[row];
-        double f = -(s + C[row] * (v + dt_2 * a));
+        double f = ld.at(row);
+        f -= s + C[row] * (v + dt_2 * a);
         kahan_add(v, cv, dt_2 * a);
         a = invMC[row] * f;
         kahan_add(v, cv, dt_2 * a);
@@ -118,7 +141,7 @@ template <class VT>
 __global__ void __launch_bounds__(CD_TPB) k_cd_bsr(int64_t nnodes, int64_t n, const int32_t *dof,
                                                  const int64_t *nbr_off, const int32_t *nbr, const VT *blk,
                                                  const VT *xp, double *V, double *cV, double *A, const double *C,
-                                                 const double *invMC, double dt_2)
+                                                 const double *invMC, double dt_2, CdLoad ld)
 {
     const int t = threadIdx.x & 31;
     if (t >= 30) return;
@@ -138,7 +161,8 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_bsr(int64_t nnodes, int64_t n, co
     const int64_t row = d - 1;
     const double s = (double)sv;
     double a = A[row], v = V[row], cv = cV[row];
-    const double f = -(s + C[row] * (v + dt_2 * a));
+    double f = ld.at(row);
+    f -= s + C[row] * (v + dt_2 * a);
     kahan_add(v, cv, dt_2 * a);
     a = invMC[row] * f;
     kahan_add(v, cv, dt_2 * a);
@@ -196,39 +220,44 @@ static int enqueue_steps(fs_ctx *c, int64_t nsteps)
     auto &x = c->ex;
     int64_t n = x.n;
     double dt = x.dt;
+    CdLoad ld{x.load ? x.Fmag : nullptr, x.mul, x.nmul, x.step, 0};
     unsigned g1 = (unsigned)((n + CD_TPB - 1) / CD_TPB);
     unsigned g2 = (unsigned)((n * CD_LANES + CD_TPB - 1) / CD_TPB);
     if (x.bsr) {
         const unsigned gb = (unsigned)((x.nnodes + 39) / 40);  // 5 nodes per warp, 8 warps per block
         for (int64_t s = 0; s < nsteps; s++) {
+            ld.j = (int)s;
             if (x.precision == FS_FP64) {
                 k_cd_disp_pad<double><<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A,
                                                                      x.pad_of_dof, (double *)x.xp);
                 k_cd_bsr<double><<<gb, CD_TPB, 0, c->stream>>>(x.nnodes, n, c->mesh.dof, c->pat.nbr_off,
                                                                 c->pat.nbr, (const double *)x.blk,
                                                                 (const double *)x.xp, x.V, x.cV, x.A, x.C,
-                                                                x.invMC, dt / 2);
+                                                                x.invMC, dt / 2, ld);
             } else {
                 k_cd_disp_pad<float><<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A,
                                                                     x.pad_of_dof, (float *)x.xp);
                 k_cd_bsr<float><<<gb, CD_TPB, 0, c->stream>>>(x.nnodes, n, c->mesh.dof, c->pat.nbr_off,
                                                                c->pat.nbr, (const float *)x.blk,
                                                                (const float *)x.xp, x.V, x.cV, x.A, x.C,
-                                                               x.invMC, dt / 2);
+                                                               x.invMC, dt / 2, ld);
             }
         }
+        if (x.load && nsteps > 0) k_step_advance<<<1, 1, 0, c->stream>>>(x.step, nsteps);
         return cuda_check(c, cudaGetLastError(), "explicit step launch");
     }
     for (int64_t s = 0; s < nsteps; s++) {
+        ld.j = (int)s;
         bool single = x.precision != FS_FP64;
         k_cd_disp<<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A, single ? x.U32 : nullptr);
         if (!single)
             k_cd_rows<double><<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, c->vals, x.U, x.V,
-                                                            x.cV, x.A, x.C, x.invMC, dt / 2);
+                                                            x.cV, x.A, x.C, x.invMC, dt / 2, ld);
         else
             k_cd_rows<float><<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, x.vals32, x.U32, x.V,
-                                                           x.cV, x.A, x.C, x.invMC, dt / 2);
+                                                           x.cV, x.A, x.C, x.invMC, dt / 2, ld);
     }
+    if (x.load && nsteps > 0) k_step_advance<<<1, 1, 0, c->stream>>>(x.step, nsteps);
     return cuda_check(c, cudaGetLastError(), "explicit step launch");
 }
 
@@ -394,6 +423,7 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
     if (x.graph) cudaGraphDestroy(x.graph);
     x.exec = nullptr;
     x.graph = nullptr;
+    x.load = false;
     int64_t n = c->mat_n;
     x.n = n;
     x.dt = dt;
@@ -462,6 +492,31 @@ int fs_explicit_set_state(fs_ctx *c, const double *U, const double *V, const dou
         FS_CUDA(c, cudaMemsetAsync(x.cU, 0, bn, c->stream));
         FS_CUDA(c, cudaMemsetAsync(x.cV, 0, bn, c->stream));
     }
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FS_OK;
+}
+
+int fs_explicit_set_load(fs_ctx *c, const double *Fmag, const double *mul, int64_t nmul, int64_t step0)
+{
+    if (!c || nmul < 0 || step0 < 0) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    auto &x = c->ex;
+    if (!x.ready) return set_err(c, FS_ERR_STATE, "call fs_explicit_setup first");
+    if (Fmag && nmul > 0 && !mul) return set_err(c, FS_ERR_BAD_INPUT, "missing time function values");
+    // the captured steps hold the load pointers: capture again on the next run
+    if (x.exec) cudaGraphExecDestroy(x.exec);
+    if (x.graph) cudaGraphDestroy(x.graph);
+    x.exec = nullptr;
+    x.graph = nullptr;
+    x.load = Fmag != nullptr;
+    if (!x.load) return FS_OK;
+    FS_TRY(grow(c, &x.Fmag, &x.cap_Fmag, (size_t)std::max<int64_t>(x.n, 1)));
+    FS_TRY(grow(c, &x.mul, &x.cap_mul, (size_t)std::max<int64_t>(nmul, 1)));
+    if (!x.step) FS_TRY(dalloc(c, &x.step, 1));
+    x.nmul = nmul;
+    FS_CUDA(c, cudaMemcpyAsync(x.Fmag, Fmag, sizeof(double) * (size_t)x.n, cudaMemcpyHostToDevice, c->stream));
+    if (nmul) FS_CUDA(c, cudaMemcpyAsync(x.mul, mul, sizeof(double) * (size_t)nmul, cudaMemcpyHostToDevice, c->stream));
+    FS_CUDA(c, cudaMemcpyAsync(x.step, &step0, sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
     return FS_OK;
 }

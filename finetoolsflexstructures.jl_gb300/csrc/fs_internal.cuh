@@ -153,6 +153,14 @@ struct fs_ctx {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         int64_t graph_steps = 0;
+        // external load g(t) Fmag: Fmag (n), g at the step indices (nmul), and
+        // the step index of the current state on the device (advanced after
+        // every batch of steps)
+        double *Fmag = nullptr, *mul = nullptr;
+        size_t cap_Fmag = 0, cap_mul = 0;
+        int64_t nmul = 0;
+        int64_t *step = nullptr;
+        bool load = false;
     } ex;
     // tile shapes of the shell element kernel and of the gather (0: defaults)
     struct Tune {

@@ -13,4 +13,5 @@ from .femm import (FEMMShellQ4RS, FEMMShellQ4RSComp, FEMMShellT3FF, FEMMShellT3F
                    SysmatAssemblerSparseCSRSymm, SysmatAssemblerSparseDiag,
                    SysmatAssemblerSparseSymm, ShellBatch)
 from .beam import FEMMCorotBeam
+from .explicit import CentralDifference, cd_loop
 from ._lib import Context, FlexShellError, laminate

@@ -57,6 +57,7 @@ def lib():
         L.fs_explicit_setup.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_double]
         L.fs_explicit_set_state.argtypes = [vp, vp, vp, vp]
         L.fs_explicit_run.argtypes = [vp, ctypes.c_int64]
+        L.fs_explicit_set_load.argtypes = [vp, vp, vp, ctypes.c_int64, ctypes.c_int64]
         L.fs_explicit_get_state.argtypes = [vp, vp, vp, vp]
         L.fs_power_iteration.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_uint64, vp]
         L.fs_laminate.argtypes = [ctypes.c_int32, vp, vp, vp, vp, vp, ctypes.c_double, ctypes.c_int32,

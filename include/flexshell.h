@@ -196,6 +196,14 @@ int fs_element_masses(fs_ctx *ctx, double *out);
  * with Kahan compensation. */
 int fs_explicit_setup(fs_ctx *ctx, int precision, const double *invMC, const double *C, double dt);
 int fs_explicit_set_state(fs_ctx *ctx, const double *U, const double *V, const double *A);
+/* External force of the reference example's force!(F, t): F = g(t) Fmag
+ * (plate_expl_examples.jl:202-209 with Fmag from distribloads or a point
+ * load), applied in every step as F = g Fmag - (K U + C (V + dt/2 A)).
+ * Fmag: n values (system numbering); mul[k] = g(k dt), k = 0..nmul-1 (zero
+ * beyond); step0: the step index k of the current state (t = k dt).  The step
+ * index advances with every step run.  Fmag = NULL removes the load.  The
+ * initial acceleration A = invMC F(0) is the caller's (fs_explicit_set_state). */
+int fs_explicit_set_load(fs_ctx *ctx, const double *Fmag, const double *mul, int64_t nmul, int64_t step0);
 /* Runs nsteps steps; the step loop is captured once into a CUDA graph. */
 int fs_explicit_run(fs_ctx *ctx, int64_t nsteps);
 int fs_explicit_get_state(fs_ctx *ctx, double *U, double *V, double *A);

@@ -1063,6 +1063,18 @@ int orc_cd_steps(int64_t n, const int64_t *rowptr, const int64_t *colidx, const 
                  const double *invMC, const double *C, double dt, int64_t nsteps, double *U,
                  double *V, double *A, int nthreads)
 {
+    return orc_cd_steps_load(n, rowptr, colidx, vals, invMC, C, dt, nsteps, U, V, A, NULL, NULL, 0, 0,
+                             nthreads);
+}
+
+/* the same loop with the external force of the example's force!(F, t) =
+ * g(t) Fmag (plate_expl_examples.jl:202-209): mul[k] = g(k dt), the state at
+ * step index step0 */
+int orc_cd_steps_load(int64_t n, const int64_t *rowptr, const int64_t *colidx, const double *vals,
+                      const double *invMC, const double *C, double dt, int64_t nsteps, double *U,
+                      double *V, double *A, const double *Fmag, const double *mul, int64_t nmul,
+                      int64_t step0, int nthreads)
+{
     double dt2_2 = (dt * dt) / 2, dt_2 = dt / 2;
     double *F = (double *)malloc(sizeof(double) * (n > 0 ? n : 1));
 #ifdef _OPENMP
@@ -1070,6 +1082,8 @@ int orc_cd_steps(int64_t n, const int64_t *rowptr, const int64_t *colidx, const 
 #endif
     (void)nthreads;
     for (int64_t step = 0; step < nsteps; step++) {
+        const int64_t k = step0 + step + 1;
+        const double g = (Fmag && k < nmul) ? mul[k] : 0.0;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -1080,7 +1094,7 @@ int orc_cd_steps(int64_t n, const int64_t *rowptr, const int64_t *colidx, const 
         for (int64_t i = 0; i < n; i++) {
             double s = 0.0;
             for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++) s += vals[k] * U[colidx[k]];
-            double f = 0.0; /* external force */
+            double f = Fmag ? g * Fmag[i] : 0.0; /* external force F .= mul .* Fmag */
             f -= s + C[i] * (V[i] + dt_2 * A[i]);
             F[i] = f;
         }

@@ -108,6 +108,14 @@ int orc_resultants(int64_t nnodes, const double *xyz, int64_t nelem, const int64
                    const double *normals, const uint8_t *valid, const orc_params *p,
                    const double *u, int quant, const double *cs, int64_t ncs, double *out);
 
+/* The same loop with the external force F(t) = g(t) Fmag of the example's
+ * force!: mul[k] = g(k dt) (zero from k = nmul), the state at step index
+ * step0 (t = step0 dt). */
+int orc_cd_steps_load(int64_t n, const int64_t *rowptr, const int64_t *colidx,
+                      const double *vals, const double *invMC, const double *C, double dt,
+                      int64_t nsteps, double *U, double *V, double *A, const double *Fmag,
+                      const double *mul, int64_t nmul, int64_t step0, int nthreads);
+
 /* Laminate stiffness of a layup (CompositeLayupModule). */
 int orc_laminate(int nplies, const double *ply_Dps, const double *ply_Dts,
                  const double *ply_t, const double *ply_angle_deg, const double *ply_rho,

@@ -85,6 +85,7 @@ def lib():
         L.orc_result_n.restype = ctypes.c_int64
         L.orc_all_element_stiffness.restype = ctypes.c_int
         L.orc_cd_steps.restype = ctypes.c_int
+        L.orc_cd_steps_load.restype = ctypes.c_int
         L.orc_laminate.restype = ctypes.c_int
         L.orc_assemble_elmats.restype = ctypes.c_int
         L.orc_beam_all.restype = ctypes.c_int
@@ -241,19 +242,25 @@ class Problem:
         return sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=(n, n))
 
 
-def cd_steps(rowptr, colidx, vals, invMC, C, dt, nsteps, U, V, A, nthreads=0):
-    """Central-difference steps on a CSR stiffness (0-based rowptr/colidx)."""
+def cd_steps(rowptr, colidx, vals, invMC, C, dt, nsteps, U, V, A, nthreads=0, Fmag=None, mul=None, step0=0):
+    """Central-difference steps on a CSR stiffness (0-based rowptr/colidx);
+    optional external force g(t) Fmag with mul[k] = g(k dt), the state at step
+    index step0."""
     n = U.shape[0]
     rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
     colidx = np.ascontiguousarray(colidx, dtype=np.int64)
     vals = np.ascontiguousarray(vals, dtype=np.float64)
     for a in (U, V, A):
         assert a.dtype == np.float64 and a.flags.c_contiguous
-    st = lib().orc_cd_steps(ctypes.c_int64(n), _p(rowptr, _c_i64_p), _p(colidx, _c_i64_p),
-                            _p(vals, _c_dbl_p), _p(np.ascontiguousarray(invMC), _c_dbl_p),
-                            _p(np.ascontiguousarray(C), _c_dbl_p), ctypes.c_double(dt),
-                            ctypes.c_int64(nsteps), _p(U, _c_dbl_p), _p(V, _c_dbl_p),
-                            _p(A, _c_dbl_p), ctypes.c_int(nthreads))
+    Fm = None if Fmag is None else np.ascontiguousarray(Fmag, dtype=np.float64)
+    mu = None if mul is None else np.ascontiguousarray(mul, dtype=np.float64)
+    st = lib().orc_cd_steps_load(ctypes.c_int64(n), _p(rowptr, _c_i64_p), _p(colidx, _c_i64_p),
+                                 _p(vals, _c_dbl_p), _p(np.ascontiguousarray(invMC), _c_dbl_p),
+                                 _p(np.ascontiguousarray(C), _c_dbl_p), ctypes.c_double(dt),
+                                 ctypes.c_int64(nsteps), _p(U, _c_dbl_p), _p(V, _c_dbl_p),
+                                 _p(A, _c_dbl_p), _p(Fm, _c_dbl_p), _p(mu, _c_dbl_p),
+                                 ctypes.c_int64(0 if mu is None else mu.shape[0]), ctypes.c_int64(step0),
+                                 ctypes.c_int(nthreads))
     assert st == 0
 
 

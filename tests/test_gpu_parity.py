@@ -258,6 +258,79 @@ def test_explicit_steps_match_oracle():
     femm.close()
 
 
+def test_explicit_load_matches_oracle():
+    # the example's force!(F, t) = g(t) Fmag with the modulated burst of
+    # plate_expl_examples.jl:202-209; 150 steps = two captured 64-step graphs
+    # plus 22 single steps, then a restart from step 150 with step0
+    import ctypes
+    from flexshell._lib import ptr
+    from flexshell import materials
+    xyz, conn, dof, nfree = PB.jittered_plate(10, False, seed=4)
+    mat = materials.MatDeforElastIso(200e9, 0.3, 7850.0)
+    femm = F.FEMMShellT3FF(conn, 0.01, mat)
+    geom0 = F.NodalField(xyz)
+    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(dof)
+    femm.associategeometry(geom0)
+    M = femm.mass(F.SysmatAssemblerFFBlock(F.SysmatAssemblerSparseDiag(), nfree), geom0, dchi)
+    K = femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi).tocsr()
+    m = M.diagonal()
+    w2 = sl.eigh(K.toarray(), np.diag(m), eigvals_only=True)[-1]
+    dt = 0.9 * 2 / np.sqrt(w2)
+    C = 0.02 * m
+    invMC = 1.0 / (m + dt / 2 * C)
+    rng = np.random.default_rng(5)
+    Fmag = rng.normal(0, 1.0, nfree)
+    fm, fc = 1 / (120 * dt), 1 / (15 * dt)
+    t = np.arange(400) * dt
+    mul = np.where(t <= 1 / fm, 0.5 * (1 - np.cos(2 * np.pi * fm * t)) * np.sin(2 * np.pi * fc * t), 0.0)
+    nsteps = 150
+    U, V = np.zeros(nfree), np.zeros(nfree)
+    A = invMC * (mul[0] * Fmag)
+    A0 = A.copy()
+    O.cd_steps(K.indptr, K.indices, K.data, invMC, C, dt, nsteps, U, V, A, Fmag=Fmag, mul=mul)
+    U2, V2, A2 = U.copy(), V.copy(), A.copy()
+    O.cd_steps(K.indptr, K.indices, K.data, invMC, C, dt, 50, U2, V2, A2, Fmag=Fmag, mul=mul, step0=nsteps)
+    ctx = femm.ctx
+    for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 2e-4)):
+        ctx.call("fs_explicit_setup", prec, ptr(np.ascontiguousarray(invMC)), ptr(np.ascontiguousarray(C)),
+                 ctypes.c_double(dt))
+        z = np.zeros(nfree)
+        ctx.call("fs_explicit_set_state", ptr(z), ptr(z), ptr(np.ascontiguousarray(A0)))
+        ctx.call("fs_explicit_set_load", ptr(Fmag), ptr(mul), mul.shape[0], 0)
+        ctx.call("fs_explicit_run", nsteps)
+        Ug, Vg, Ag = np.zeros(nfree), np.zeros(nfree), np.zeros(nfree)
+        ctx.call("fs_explicit_get_state", ptr(Ug), ptr(Vg), ptr(Ag))
+        assert np.abs(Ug - U).max() <= tol * np.abs(U).max()
+        assert np.abs(Vg - V).max() <= tol * np.abs(V).max()
+        # restart: state and step index given again, then 50 more steps
+        ctx.call("fs_explicit_set_state", ptr(Ug), ptr(Vg), ptr(Ag))
+        ctx.call("fs_explicit_set_load", ptr(Fmag), ptr(mul), mul.shape[0], nsteps)
+        ctx.call("fs_explicit_run", 50)
+        ctx.call("fs_explicit_get_state", ptr(Ug), ptr(Vg), ptr(Ag))
+        assert np.abs(Ug - U2).max() <= tol * np.abs(U2).max()
+        # removing the load: free vibration from the same state
+        ctx.call("fs_explicit_set_load", None, None, 0, 0)
+        ctx.call("fs_explicit_run", 10)
+        U3, V3, A3 = U2.copy(), V2.copy(), A2.copy()
+        O.cd_steps(K.indptr, K.indices, K.data, invMC, C, dt, 10, U3, V3, A3)
+        ctx.call("fs_explicit_get_state", ptr(Ug), ptr(Vg), ptr(Ag))
+        assert np.abs(Ug - U3).max() <= tol * np.abs(U3).max()
+    # the Python mirror of _cd_loop! (undamped here: ksi = 0), peeking every 50 steps
+    femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi)
+    seen = []
+    Uf, Vf, Af = F.cd_loop(femm, m, 0.0, 1.0, np.zeros(nfree), np.zeros(nfree), nsteps * dt, dt, Fmag=Fmag,
+                           g=lambda tt: np.interp(tt, t, mul), peek=lambda k, u, v, tt: seen.append(k),
+                           peek_every=50)
+    U4, V4, A4 = np.zeros(nfree), np.zeros(nfree), invMC * 0.0
+    mul4 = np.interp(np.arange(nsteps + 1) * dt, t, mul)
+    A4 = (1.0 / m) * (mul4[0] * Fmag)
+    O.cd_steps(K.indptr, K.indices, K.data, 1.0 / m, np.zeros(nfree), dt, nsteps, U4, V4, A4, Fmag=Fmag, mul=mul4)
+    assert seen == [0, 50, 100, 150]
+    assert np.abs(Uf - U4).max() <= 1e-10 * np.abs(U4).max()
+    femm.close()
+
+
 @pytest.mark.parametrize("quads", [False, True])
 def test_restoring_force_is_minus_K_U(quads):
     # extension for the shells: F = -K U with U the generalized displacements

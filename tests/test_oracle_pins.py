@@ -111,3 +111,31 @@ def test_laminate_barbero_example_5_6():
                       [5.709503642606021, 15.471482760639574, -3.000216655678807],
                       [-1.2171238264083473, -3.000216655678808, 6.2385036426060205]])
     assert np.linalg.norm(A - Atrue) < 1e-15 * np.linalg.norm(Atrue)
+
+
+def test_cd_loop_with_external_force_follows_the_reference_loop():
+    # the oracle's loaded central-difference loop against a direct statement of
+    # _cd_loop! (plate_expl_examples.jl:61-94) with force!(F, t) = g(t) Fmag
+    import scipy.sparse as sp
+    rng = np.random.default_rng(2)
+    n = 12
+    B = rng.normal(size=(n, n))
+    K = sp.csr_matrix(B @ B.T + n * np.eye(n))
+    m = rng.uniform(1.0, 2.0, n)
+    dt, ksi = 0.05, 0.01
+    C = ksi * m
+    invMC = 1.0 / (m + dt / 2 * C)
+    Fmag = rng.normal(size=n)
+    mul = np.sin(0.3 * np.arange(60))
+    U, V, A, F = np.zeros(n), np.zeros(n), invMC * (mul[0] * Fmag), np.zeros(n)
+    Uo, Vo, Ao = U.copy(), V.copy(), A.copy()
+    for step in range(1, 41):
+        U += dt * V + dt ** 2 / 2 * A
+        F[:] = mul[step] * Fmag
+        F -= K @ U + C * (V + dt / 2 * A)
+        V += dt / 2 * A
+        A = invMC * F
+        V += dt / 2 * A
+    O.cd_steps(K.indptr, K.indices, K.data, invMC, C, dt, 40, Uo, Vo, Ao, Fmag=Fmag, mul=mul)
+    assert np.abs(Uo - U).max() <= 1e-12 * np.abs(U).max()
+    assert np.abs(Vo - V).max() <= 1e-12 * np.abs(V).max()
