@@ -65,7 +65,7 @@ def cd_loop(femm, M, ksi, omegad, U0, V0, tend, dt, Fmag=None, g=None, peek=None
     (nsteps = round(tend/dt); if nsteps dt < tend, dt = tend/(nsteps + 1)).
     peek(step, U, V, t) is called at step 0 and after every peek_every steps
     (the state is copied to the host for it).  Returns the final U, V, A."""
-    m = np.asarray(M.diagonal() if hasattr(M, "diagonal") else M, dtype=np.float64)
+    m = np.asarray(M if np.ndim(M) == 1 else M.diagonal(), dtype=np.float64)
     C = (ksi * 2 * omegad) * m
     nsteps = int(round(tend / dt))
     if nsteps * dt < tend:
