@@ -961,29 +961,14 @@ FS_HD void resultant_rows(int quant, const double g[NN][2], double c[3][NN][5])
     }
 }
 
-// FinEtools' isoparametric csys (the shells' default mcsys): e1 along the
-// first tangent, e3 along the normal t1 x t2, e2 = e3 x e1; column-major.
-FS_HD void isoparametric_csys(const double t1[3], const double t2[3], double cs[9])
-{
-    double n[3];
-    cross3(t1, t2, n);
-    const double nn = sqrt(dot3(n, n)), l1 = sqrt(dot3(t1, t1));
-    for (int k = 0; k < 3; k++) {
-        cs[k] = t1[k] / l1;
-        cs[6 + k] = n[k] / nn;
-    }
-    double e2[3];
-    cross3(cs + 6, cs, e2);
-    const double l2 = sqrt(dot3(e2, e2));
-    for (int k = 0; k < 3; k++) cs[3 + k] = e2[k] / l2;
-}
-
-// cs: the output csys (column-major), or null for the isoparametric csys of
-// the point's tangents t1, t2
+// cs: the output csys (column-major), or null for the element frame at the
+// point -- the shells' default mcsys, whose updater (isoparametric!,
+// src/FEMMShellT3FFModule.jl:222-224; _isoparametric!, src/FEMMShellQ4RSModule.jl:
+// 201-203) is _e_g! of the point's tangents
 template <int NN>
 FS_HD void resultant_finish(int quant, const GlobalMap<double, NN> &M, const double e[3][3],
                             const double c[3][NN][5], const double ue[6 * NN], const MatConst &mc, double t,
-                            double stab, const double *cs, const double t1[3], const double t2[3], double out[3])
+                            double stab, const double *cs, double out[3])
 {
     const int nr = quant == RES_SHEAR ? 2 : 3;
     double s[3] = {0.0, 0.0, 0.0};
@@ -1007,7 +992,11 @@ FS_HD void resultant_finish(int quant, const GlobalMap<double, NN> &M, const dou
     // o2 = [m n; -n m]: moments and membrane forces o2' T o2, shear forces o2' f
     double csi[9];
     if (!cs) {
-        isoparametric_csys(t1, t2, csi);
+        for (int k = 0; k < 3; k++) {
+            csi[k] = e[0][k];
+            csi[3 + k] = e[1][k];
+            csi[6 + k] = e[2][k];
+        }
         cs = csi;
     }
     double m, n;
@@ -1056,7 +1045,7 @@ FS_HD void t3_resultant(const ElemIn<3> &in, const MatConst &mc, const double ue
     }
     const double t = in.t;
     const double stab = t * t / (t * t + mc.stab_c * (2 * Ae));
-    resultant_finish<3>(quant, M, e, c, ue, mc, t, stab, cs, J0, J1, out);
+    resultant_finish<3>(quant, M, e, c, ue, mc, t, stab, cs, out);
 }
 
 // Q4RS: Gauss point j (0..3, the reference's point order).  Returns nonzero
@@ -1098,7 +1087,7 @@ FS_HD int q4_resultant(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatCo
     double c[3][4][5];
     resultant_rows<4>(quant, g, c);
     if (quant == RES_SHEAR) q4_bs<double>(X, Y, xi, eta, (double(*)[4][5])c[0]);
-    resultant_finish<4>(quant, M, e, c, ue, mc, in.t, qe.stab, cs, J0, J1, out);
+    resultant_finish<4>(quant, M, e, c, ue, mc, in.t, qe.stab, cs, out);
     return 0;
 }
 

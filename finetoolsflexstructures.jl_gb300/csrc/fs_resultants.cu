@@ -65,7 +65,7 @@ int fs_resultants(fs_ctx *c, int quantity, const double *U, const double *csmat,
     const int npt = m.etype == FS_T3FF ? 1 : 4;
     const int64_t npoints = m.nelem * npt;
     if (ncs != 0 && ncs != 1 && ncs != npoints)
-        return set_err(c, FS_ERR_BAD_INPUT, "csmat: none (ncs = 0, the isoparametric csys), one 3x3 matrix "
+        return set_err(c, FS_ERR_BAD_INPUT, "csmat: none (ncs = 0, the element frame), one 3x3 matrix "
                                             "(ncs = 1) or one per integration point");
     if (npoints == 0) return FS_OK;
     if (!U || (ncs && !csmat) || !out) return set_err(c, FS_ERR_BAD_INPUT, "missing array");

@@ -291,7 +291,7 @@ class _FEMMShell:
     def resultants(self, geom0, u, quantity="bending", outputcsys=None):
         """Stress resultants at every integration point (npoints x 3): the
         values inspectintegpoints hands to its inspector, in double.  outputcsys:
-        None (the isoparametric csys, the reference's default mcsys), a 3x3
+        None (the element frame at the point: the default mcsys), a 3x3
         matrix, an (npoints, 3, 3) array, or a callable (XYZ, tangents, feid,
         qpid) -> 3x3 evaluated per point like updatecsmat!."""
         if not self._associatedgeometry:

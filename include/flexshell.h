@@ -304,8 +304,8 @@ int fs_restoring_force(fs_ctx *ctx, const double *U, double *F);
  * u: nnodes x 6 column-major (u.values); csmat: the output csys, ncs = 1 one
  * 3x3 column-major matrix for every point, or ncs = number of points (nelem
  * for T3FF, 4 nelem for Q4RS), one per point in element order, or csmat =
- * NULL with ncs = 0: FinEtools' isoparametric csys of each point (the
- * default mcsys of the shells); out: 3 doubles per point, element order.
+ * NULL with ncs = 0: the element frame at each point (the shells' default
+ * mcsys, isoparametric! = _e_g!); out: 3 doubles per point, element order.
  * Needs the normals (associategeometry!). */
 #define FS_RES_MOMENT 1
 #define FS_RES_SHEAR 2

@@ -1209,22 +1209,6 @@ static void resultant_out(const double *E, const double *cs, int quant, const do
     out[2] = R[IX(0, 1, 2)];
 }
 
-/* FinEtools isoparametric! csys (the default mcsys of the shells): e1 along
- * the first tangent, e3 along the normal t1 x t2, e2 = e3 x e1; column-major */
-static void isoparametric_csys(const double *t1, const double *t2, double *cs)
-{
-    double n[3] = {t1[1] * t2[2] - t1[2] * t2[1], t1[2] * t2[0] - t1[0] * t2[2], t1[0] * t2[1] - t1[1] * t2[0]};
-    double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    double l1 = sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
-    for (int k = 0; k < 3; k++) {
-        cs[k] = t1[k] / l1;
-        cs[6 + k] = n[k] / nn;
-    }
-    double e2[3] = {cs[7] * cs[2] - cs[8] * cs[1], cs[8] * cs[0] - cs[6] * cs[2], cs[6] * cs[1] - cs[7] * cs[0]};
-    double l2 = sqrt(e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2]);
-    for (int k = 0; k < 3; k++) cs[3 + k] = e2[k] / l2;
-}
-
 static void matvec(const double *A, int r, int c, const double *x, double *y)
 {
     for (int i = 0; i < r; i++) {
@@ -1311,12 +1295,8 @@ static void t3_resultant(const orc_params *p, int64_t e, const double *X, const 
         matvec(Bs, 2, n, ede, s);
         resultant_material(p, quant, t, stab_fun(t, sqrt(2 * Ae), p->stab_c), s, v);
     }
-    double csi[9];
-    if (!cs) {
-        isoparametric_csys(J0, J0 + 3, csi);
-        cs = csi;
-    }
-    resultant_out(E, cs, quant, v, out);
+    /* default mcsys: isoparametric! = _e_g!(J0), the element frame */
+    resultant_out(E, cs ? cs : E, quant, v, out);
 }
 
 static void q4_resultants(const orc_params *p, int64_t e, const double *X, const double *nrm,
@@ -1391,9 +1371,8 @@ static void q4_resultants(const orc_params *p, int64_t e, const double *X, const
             matvec(Bs, 2, n, ede, s);
             resultant_material(p, quant, t, stab_fun(t, h, p->stab_c), s, v);
         }
-        double csi[9];
-        if (!cs) isoparametric_csys(J, J + 3, csi);
-        resultant_out(E, cs ? cs + cs_stride * j : csi, quant, v, out + 3 * j);
+        /* default mcsys: _isoparametric! = _e_g!(J), the frame at the point */
+        resultant_out(E, cs ? cs + cs_stride * j : E, quant, v, out + 3 * j);
     }
     free(T);
 }

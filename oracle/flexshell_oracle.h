@@ -100,9 +100,9 @@ int orc_cd_steps(int64_t n, const int64_t *rowptr, const int64_t *colidx,
  * ORC_RES_SHEAR (q_x, q_y, 0), ORC_RES_MEMBRANE (n_xx, n_yy, n_xy) in the
  * output csys.  u: nnodes x 6 column-major displacements and rotations;
  * cs: one 3x3 column-major csys matrix (ncs = 1), one per point (ncs =
- * number of points), or NULL with ncs = 0 for FinEtools' isoparametric csys
- * (the shells' default mcsys) at each point; out: 3 values per point, points
- * in element order. */
+ * number of points), or NULL with ncs = 0 for the element frame at each
+ * point (the shells' default mcsys, whose updater is _e_g!); out: 3 values
+ * per point, points in element order. */
 enum { ORC_RES_MOMENT = 1, ORC_RES_SHEAR = 2, ORC_RES_MEMBRANE = 3 };
 int orc_resultants(int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
                    const double *normals, const uint8_t *valid, const orc_params *p,

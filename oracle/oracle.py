@@ -192,8 +192,8 @@ class Problem:
     def resultants(self, u, quantity, cs=None):
         """Stress resultants at the integration points (inspectintegpoints):
         quantity RES_MOMENT, RES_SHEAR or RES_MEMBRANE; u (nnodes, 6); cs one
-        3x3 csys matrix or one per point (npoints, 3, 3); None: the
-        isoparametric csys at each point (the shells' default mcsys).
+        3x3 csys matrix or one per point (npoints, 3, 3); None: the element
+        frame at each point (the shells' default mcsys).
         Returns (npoints, 3), points in element order (Q4: four per element)."""
         npt = self.nelem * (1 if self.nen == 3 else 4)
         u = np.asfortranarray(u, dtype=np.float64)

@@ -113,7 +113,7 @@ extern "C" int hc_element_matrices(int etype, int precision, int64_t nnodes, con
 // Stress resultants at the integration points (the device point math of
 // csrc/fs_elem_math.cuh): quantity 1 moment, 2 shear, 3 membrane; u nnodes x 6
 // column-major; cs one 3x3 column-major matrix (ncs = 1), one per point, or
-// none (ncs = 0: the isoparametric csys).
+// none (ncs = 0: the element frame at the point).
 extern "C" int hc_resultants(int etype, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
                              const double *normals, const uint8_t *valid, const double *thick,
                              const fs_shell_params *p, const double *u, int quant, const double *cs, int64_t ncs,

@@ -2,10 +2,10 @@
 inspectintegpoints of FEMMShellT3FF and FEMMShellQ4RS) against the oracle,
 through the C ABI and the Python mirror.  Tolerance 1e-12 relative (max-abs
 difference over max-abs value) with given output frames.  With the default
-isoparametric frame the output angle comes from Layup2ElementAngle of two
-nearly equal frames, whose n = sqrt(1 - m^2) turns one rounding of m into
-about 1e-8 (the reference carries the same noise), so that case is held to
-1e-7."""
+frame (the element frame: the shells' mcsys updater is _e_g!) the output
+angle comes from Layup2ElementAngle of a frame and itself, whose
+n = sqrt(1 - m^2) turns a last-bit difference of m = 1 into about 1e-8 (the
+reference carries the same noise), so that case is held to 1e-7."""
 import ctypes
 
 import numpy as np

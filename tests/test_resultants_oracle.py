@@ -73,13 +73,13 @@ def test_oracle_transverse_shear_closed_form(quads):
 
 @pytest.mark.parametrize("quads", [False, True])
 @pytest.mark.parametrize("quantity", [_abi.FS_RES_MOMENT, _abi.FS_RES_SHEAR, _abi.FS_RES_MEMBRANE])
-@pytest.mark.parametrize("frame", ["isoparametric", "one", "per_point"])
+@pytest.mark.parametrize("frame", ["element", "one", "per_point"])
 def test_host_point_math_matches_oracle(quads, quantity, frame):
     et, d, P, prm = _homog(quads, n=6)
     rng = np.random.default_rng(7)
     u = rng.normal(size=(d["xyz"].shape[0], 6)) * 1e-3
     npt = P.nelem * (4 if quads else 1)
-    cs = {"isoparametric": None, "one": np.linalg.qr(rng.normal(size=(3, 3)))[0],
+    cs = {"element": None, "one": np.linalg.qr(rng.normal(size=(3, 3)))[0],
           "per_point": np.linalg.qr(rng.normal(size=(npt, 3, 3)))[0]}[frame]
     ro = P.resultants(u, quantity, cs)
     rh = HC.resultants(et, d["xyz"], d["conn"], P.normals, P.valid, d["thickness"], prm, u, quantity, cs)
