@@ -621,9 +621,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_e2e = float(t.item())
     h2d = (3 * nn) * 8 + (6 * nn) * 8
-    # over the host link: colptr (int64), the row indices as int32 (widened
-    # into the caller's int64 rowval by host threads as they land), the values
-    d2h = (asm.n + 1) * 8 + nnz * 4 + nnz * 8
+    d2h = (asm.n + 1) * 8 + nnz * 8 + nnz * 8
     del h_colptr, h_rowval, h_nzval
     asm.ctx.close()
     del asm
@@ -695,9 +693,7 @@ def main():
         "e2e": {"value": world * ne3 / (ms_e2e * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
                 "path": "C ABI from pinned host: fs_geometry_set + fs_dofs_set + fs_pattern (pattern "
-                        "rebuilt) + fs_stiffness_copy (CSC copied back into int64 colptr/rowval and double "
-                        "nzval host arrays; row indices sent as int32 and widened by host threads chunk by "
-                        "chunk, overlapping the kernels and the value copy)"},
+                        "rebuilt) + fs_stiffness_copy (CSC copied back, pattern copy overlapping the kernels)"},
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,

@@ -2,7 +2,6 @@
 #include <string.h>
 
 #include <algorithm>
-#include <thread>
 #include <vector>
 
 #include "fs_host_prep.h"
@@ -95,12 +94,6 @@ __global__ void k_plus_one_i32(int64_t n, const int32_t *src, int64_t *dst)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[i] = (int64_t)src[i] + 1;
-}
-
-__global__ void k_plus_one_i32_i32(int64_t n, const int32_t *src, int32_t *dst)
-{
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = src[i] + 1;
 }
 
 // diagonal of a CSR matrix (sorted columns)
@@ -220,9 +213,6 @@ int fs_ctx_destroy(fs_ctx *c)
     cudaFree(c->d_status);
     for (int k = 0; k < 4; k++)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
-    if (c->h_stage32) cudaFreeHost(c->h_stage32);
-    for (int k = 0; k < fs_ctx::COPY_CHUNKS; k++)
-        if (c->chunk_ev[k]) cudaEventDestroy(c->chunk_ev[k]);
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
         cudaStreamDestroy(c->copy_stream);
@@ -619,82 +609,34 @@ int fs_stiffness_copy(fs_ctx *c, int precision, int64_t nrows, int64_t *colptr, 
     if (!c->copy_stream) {
         FS_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
         for (int k = 0; k < 2; k++) FS_CUDA(c, cudaEventCreateWithFlags(&c->copy_ev[k], cudaEventDisableTiming));
-        for (int k = 0; k < fs_ctx::COPY_CHUNKS; k++)
-            FS_CUDA(c, cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming | cudaEventBlockingSync));
     }
     const PatternDev &P = c->pat;
     const int64_t n = nrows, nnz = P.nnz;
-    // device staging: colptr (int64), then the row indices (int32)
-    const size_t need = (size_t)(n + 1) + (size_t)(nnz + 1) / 2;
+    const size_t need = (size_t)(n + 1 + nnz);
     if (need > c->stage_cap || !c->stage64) {
         FS_TRY(dalloc(c, &c->stage64, need));
         c->stage_cap = need;
     }
-    if ((size_t)nnz > c->h_stage32_cap || !c->h_stage32) {
-        if (c->h_stage32) cudaFreeHost(c->h_stage32);
-        c->h_stage32 = nullptr;
-        c->h_stage32_cap = 0;
-        FS_CUDA(c, cudaHostAlloc((void **)&c->h_stage32, sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1),
-                                 cudaHostAllocDefault));
-        c->h_stage32_cap = (size_t)nnz;
-    }
-    // The pattern (1-based) goes out on the copy stream while the kernels
-    // run.  The row indices travel as 32-bit values (half the bytes over the
-    // host link, the slowest part of the call) in chunks; host threads widen
-    // each chunk into the caller's 64-bit rowval as it lands, while the link
-    // carries the next chunk and then the values.
+    // the pattern (1-based) goes out on the copy stream while the kernels run
     FS_CUDA(c, cudaEventRecord(c->copy_ev[0], c->stream));
     FS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->copy_ev[0], 0));
-    int64_t *sp = c->stage64;
-    int32_t *sr = reinterpret_cast<int32_t *>(c->stage64 + n + 1);
+    int64_t *sp = c->stage64, *sr = c->stage64 + n + 1;
     k_plus_one_i64<<<(unsigned)((n + 1 + 255) / 256), 256, 0, c->copy_stream>>>(n + 1, P.rowptr, sp);
-    if (nnz) k_plus_one_i32_i32<<<(unsigned)((nnz + 255) / 256), 256, 0, c->copy_stream>>>(nnz, P.colidx, sr);
+    if (nnz) k_plus_one_i32<<<(unsigned)((nnz + 255) / 256), 256, 0, c->copy_stream>>>(nnz, P.colidx, sr);
     FS_CUDA(c, cudaGetLastError());
     FS_CUDA(c, cudaMemcpyAsync(colptr, sp, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, c->copy_stream));
-    const int nch = fs_ctx::COPY_CHUNKS;
-    int64_t cb[fs_ctx::COPY_CHUNKS + 1];
-    for (int k = 0; k <= nch; k++) cb[k] = nnz * k / nch;
-    for (int k = 0; k < nch; k++) {
-        if (cb[k + 1] > cb[k])
-            FS_CUDA(c, cudaMemcpyAsync(c->h_stage32 + cb[k], sr + cb[k], sizeof(int32_t) * (size_t)(cb[k + 1] - cb[k]),
-                                       cudaMemcpyDeviceToHost, c->copy_stream));
-        FS_CUDA(c, cudaEventRecord(c->chunk_ev[k], c->copy_stream));
-    }
+    if (nnz) FS_CUDA(c, cudaMemcpyAsync(rowval, sr, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, c->copy_stream));
     FS_CUDA(c, cudaEventRecord(c->copy_ev[1], c->copy_stream));
     // values: element kernel and gather on the context stream, then their copy
     int64_t got = 0;
-    int st = assemble_matrix(c, precision, FS_ASM_SPARSE, nrows, &got, -1, 0);
-    if (st == FS_OK && nnz)
-        st = cuda_check(c, cudaMemcpyAsync(nzval, c->vals, sizeof(double) * nnz, cudaMemcpyDeviceToHost, c->stream),
-                        "value copy");
-    // widen the row indices: thread w takes its share of every chunk in turn
-    const int nthr = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    std::vector<std::thread> pool;
-    std::vector<int> tst((size_t)nthr, 0);
-    const int32_t *h32 = c->h_stage32;
-    const int dev = c->device;
-    cudaEvent_t *evs = c->chunk_ev;
-    for (int w = 0; w < nthr && nnz; w++)
-        pool.emplace_back([=, &tst]() {
-            cudaSetDevice(dev);
-            for (int k = 0; k < nch; k++) {
-                if (cudaEventSynchronize(evs[k]) != cudaSuccess) {
-                    tst[w] = 1;
-                    return;
-                }
-                const int64_t len = cb[k + 1] - cb[k];
-                const int64_t lo = cb[k] + len * w / nthr, hi = cb[k] + len * (w + 1) / nthr;
-                for (int64_t i = lo; i < hi; i++) rowval[i] = (int64_t)h32[i];
-            }
-        });
-    for (auto &t : pool) t.join();
-    const cudaError_t e1 = cudaStreamWaitEvent(c->stream, c->copy_ev[1], 0);
-    const cudaError_t e2 = cudaStreamSynchronize(c->stream);
-    FS_TRY(st);
-    FS_CUDA(c, e1);
-    FS_CUDA(c, e2);
-    for (int w = 0; w < nthr; w++)
-        if (tst[w]) return set_err(c, FS_ERR_CUDA, "row index copy failed");
+    const int st = assemble_matrix(c, precision, FS_ASM_SPARSE, nrows, &got, -1, 0);
+    if (st != FS_OK) {
+        cudaStreamSynchronize(c->copy_stream);
+        return st;
+    }
+    if (nnz) FS_CUDA(c, cudaMemcpyAsync(nzval, c->vals, sizeof(double) * nnz, cudaMemcpyDeviceToHost, c->stream));
+    FS_CUDA(c, cudaStreamWaitEvent(c->stream, c->copy_ev[1], 0));
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
     return FS_OK;
 }
 

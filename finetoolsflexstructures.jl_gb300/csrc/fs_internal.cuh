@@ -129,12 +129,6 @@ struct fs_ctx {
     // staging for host copies
     int64_t *stage64 = nullptr;
     size_t stage_cap = 0;
-    // page-locked host staging of the 32-bit row indices (fs_stiffness_copy)
-    // and the events of its chunks
-    int32_t *h_stage32 = nullptr;
-    size_t h_stage32_cap = 0;
-    static const int COPY_CHUNKS = 16;
-    cudaEvent_t chunk_ev[COPY_CHUNKS] = {};
     // host copies re-applied when the mesh changes
     std::vector<double> h_thickness;
     std::vector<fs_layup_group> h_groups;

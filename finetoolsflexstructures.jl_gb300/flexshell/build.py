@@ -58,7 +58,7 @@ def build(force=False, verbose=False, extra=()):
         if r.returncode != 0:
             raise RuntimeError("nvcc failed on %s" % cmd[2])
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)
