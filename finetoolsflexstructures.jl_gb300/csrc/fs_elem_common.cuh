@@ -125,6 +125,45 @@ __device__ __forceinline__ void gram_rows(Acc &acc, const R *rows, int ND, int r
     }
 }
 
+// acc += sum over rows [r0, r1) (stride RS from base) of row[NSTR a + i - IOFF]
+// row[NSTR b + j - IOFF] for i in [I0, I1), j in [J0, J1): the same products
+// as gram_rows on a compact row layout (rows holding a subset of the dofs)
+template <int I0, int I1, int J0, int J1, int RS, int NSTR, int IOFF, class R, class Acc>
+__device__ __forceinline__ void gram_rows_c(Acc &acc, const R *base, int r0, int r1, int a, int b)
+{
+    for (int rho = r0; rho < r1; rho++) {
+        const R *rr = base + rho * RS;
+        R ra[6], rb[6];
+#pragma unroll
+        for (int i = I0; i < I1; i++) ra[i] = rr[NSTR * a + i - IOFF];
+#pragma unroll
+        for (int j = J0; j < J1; j++) rb[j] = rr[NSTR * b + j - IOFF];
+#pragma unroll
+        for (int i = I0; i < I1; i++)
+#pragma unroll
+            for (int j = J0; j < J1; j++) acc.add(i, j, ra[i], rb[j]);
+    }
+}
+
+// Upper node blocks of a homogeneous element from its rows in the
+// CompactRows<NN, NS> layout: the products and their order are those of the
+// SPARSE path of write_blocks, so the blocks are bitwise the same.
+template <class R, class S, int NN, int NS>
+__device__ __forceinline__ void write_blocks_compact(const R *rows, S *out)
+{
+    typedef CompactRows<NN, NS> L;
+    constexpr bool PAIR = sizeof(S) == 8 && sizeof(R) == 4;
+    for (int a = 0; a < NN; a++)
+        for (int b = a; b < NN; b++) {
+            BlockAcc<R, PAIR> acc;
+            acc.zero();
+            gram_rows_c<0, 3, 0, 3, L::MS, 3, 0>(acc, rows, 0, 3, a, b);
+            gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0>(acc, rows + L::BS, 0, 3 + NS, a, b);
+            if (a == b) gram_rows_c<3, 6, 3, 6, 3, 0, 3>(acc, rows + L::DR + 3 * a, 0, 1, a, b);
+            acc.store(out + ub(a, b, NN) * 36);
+        }
+}
+
 // Upper node blocks of K = sum_rho row_rho row_rho^T.  Storage S: the row
 // type R itself, or float2 pairs for float rows accumulated error-free
 // (FS_MIXED_COMP).  SPARSE (homogeneous shells): rows 0..2 are membrane rows

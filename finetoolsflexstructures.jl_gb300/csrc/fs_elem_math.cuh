@@ -269,6 +269,25 @@ FS_HD void expand_uv(const GlobalMap<R, NN> &M, const R u[NN], const R v[NN], R 
         }
 }
 
+// the translations alone (3 per node): a membrane row of the compact layout
+template <class R, int NN>
+FS_HD void expand_uv_c(const GlobalMap<R, NN> &M, const R u[NN], const R v[NN], R *out)
+{
+    for (int j = 0; j < NN; j++)
+        for (int q = 0; q < 3; q++) out[3 * j + q] = u[j] * M.e[0][q] + v[j] * M.e[1][q];
+}
+
+// Compact row layout of a homogeneous element (shared memory of the element
+// kernel): the membrane rows keep only the translations (3 per node), the
+// bending and shear rows all 6 dofs per node, the drilling row of node i only
+// its 3 rotations.  Offsets in R units.
+template <int NN, int NS> struct CompactRows {
+    static constexpr int MS = 3 * NN;                  // membrane row length
+    static constexpr int BS = 3 * MS, BSS = 6 * NN;    // bending + shear rows: start, length
+    static constexpr int DR = BS + (3 + NS) * BSS;     // drilling rows: start (3 each)
+    static constexpr int SIZE = DR + 3 * NN;
+};
+
 template <class R, int NN, bool HAS_W>
 FS_HD void expand_wt(const GlobalMap<R, NN> &M, const R w[NN], const R tx[NN], const R ty[NN], R *out)
 {
@@ -319,7 +338,10 @@ FS_HD R lpk(const double *d, const float *f, int i)
 // Membrane and bending rows of a homogeneous shell, mixed with the Cholesky
 // factor L of Dps (rows r = 0..2: sm * sum_{c>=r} L[c][r] strain_c), written
 // as global rows; returns the bending rotations for the drilling factor.
-template <class R, int NN>
+// COMPACT: membrane row r at rows + 3 NN r (translations only), bending row r
+// at rows + 9 NN + 6 NN r (the CompactRows layout); otherwise rows r and 3 + r
+// of stride rs.
+template <class R, int NN, bool COMPACT = false>
 FS_HD void homog_mb_rows(const GlobalMap<R, NN> &M, const MatConst &mc, R sm, R sb, R *rows, int rs,
                          R btx[3][NN], R bty[3][NN])
 {
@@ -334,8 +356,13 @@ FS_HD void homog_mb_rows(const GlobalMap<R, NN> &M, const MatConst &mc, R sm, R 
             btx[r][j] = sb * (-c1 * M.g[j][1] - c2 * M.g[j][0]);
             bty[r][j] = sb * (c0 * M.g[j][0] + c2 * M.g[j][1]);
         }
-        expand_uv<R, NN>(M, u, v, rows + r * rs);
-        expand_wt<R, NN, false>(M, nullptr, btx[r], bty[r], rows + (3 + r) * rs);
+        if constexpr (COMPACT) {
+            expand_uv_c<R, NN>(M, u, v, rows + 3 * NN * r);
+            expand_wt<R, NN, false>(M, nullptr, btx[r], bty[r], rows + 9 * NN + 6 * NN * r);
+        } else {
+            expand_uv<R, NN>(M, u, v, rows + r * rs);
+            expand_wt<R, NN, false>(M, nullptr, btx[r], bty[r], rows + (3 + r) * rs);
+        }
     }
 }
 
@@ -463,10 +490,12 @@ FS_HD void t3_bs_ordering(const R x[3], const R y[3], R Ae, int s, int p, int q,
 }
 
 // Computes the Gram rows (global dofs, 18 wide) of one T3FF / T3FFComp
-// element.  Returns 0 on success.  `rows` is written with row stride `rs`.
-template <class R, bool COMP, bool AVGK>
+// element.  Returns 0 on success.  `rows` is written with row stride `rs`,
+// or (COMPACT, homogeneous elements) in the CompactRows<3, NS> layout.
+template <class R, bool COMP, bool AVGK, bool COMPACT = false>
 FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc, R *rows, int rs)
 {
+    static_assert(!(COMP && COMPACT), "the compact layout is for homogeneous elements");
     // --- frame and element coordinates (double) ---
     double J0[3], J1[3], e[3][3];
     for (int c = 0; c < 3; c++) {
@@ -513,7 +542,7 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
     GlobalMap<R, 3> M;
     build_map<R, 3>(e, A, g, M);
 
-    const int NS = T3Rows<AVGK>::NS;
+    constexpr int NS = T3Rows<AVGK>::NS;
     // --- transverse shear rows in the element frame (w, thx, thy per node) ---
     R sh[NS][3][5];
     for (int r = 0; r < NS; r++)
@@ -533,8 +562,8 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
     if constexpr (!COMP) {
         // --- homogeneous: sparse rows, Dps and (5/6)Dt Cholesky mixing ---
         R tr_ = (R)t;
-        homog_mb_rows<R, 3>(M, mc, sqrt(tr_ * AeR), sqrt(tr_ * tr_ * tr_ / 12 * AeR), rows, rs,
-                            (R(*)[3])rtx[0], (R(*)[3])rty[0]);
+        homog_mb_rows<R, 3, COMPACT>(M, mc, sqrt(tr_ * AeR), sqrt(tr_ * tr_ * tr_ / 12 * AeR), rows, rs,
+                                     (R(*)[3])rtx[0], (R(*)[3])rty[0]);
         R ws = sqrt(tr_ * stab * AeR * (R)(AVGK ? 1.0 / 3 : 1.0));
         R l00 = lpk<R>(mc.Lt, mc.Ltf, lp(0, 0)), l10 = lpk<R>(mc.Lt, mc.Ltf, lp(1, 0)), l11 = lpk<R>(mc.Lt, mc.Ltf, lp(1, 1));
         for (int o = 0; o < NS / 2; o++)
@@ -546,7 +575,9 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
                     rtx[3 + 2 * o + r][i] = f0 * sh[2 * o][i][3] + f1 * sh[2 * o + 1][i][3];
                     rty[3 + 2 * o + r][i] = f0 * sh[2 * o][i][4] + f1 * sh[2 * o + 1][i][4];
                 }
-                expand_wt<R, 3, true>(M, w, rtx[3 + 2 * o + r], rty[3 + 2 * o + r], rows + (6 + 2 * o + r) * rs);
+                R *row = COMPACT ? rows + CompactRows<3, NS>::BS + CompactRows<3, NS>::BSS * (3 + 2 * o + r)
+                                 : rows + (6 + 2 * o + r) * rs;
+                expand_wt<R, 3, true>(M, w, rtx[3 + 2 * o + r], rty[3 + 2 * o + r], row);
             }
     } else {
         // --- layered: membrane and bending rows rotated by the layup angle and
@@ -605,10 +636,15 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
     double kavg = drill_mean<R>((double)ksumr, mc);
     R sk = kavg > 0.0 ? sqrt((R)kavg) : (R)0;
     for (int i = 0; i < 3; i++) {
-        R *o = rows + (6 + NS + i) * rs;
-        for (int q = 0; q < 18; q++) o[q] = 0;
-        if (in.valid[i])
-            for (int c = 0; c < 3; c++) o[6 * i + 3 + c] = sk * M.t[i][2][c];
+        if constexpr (COMPACT) {
+            R *o = rows + CompactRows<3, NS>::DR + 3 * i;
+            for (int c = 0; c < 3; c++) o[c] = in.valid[i] ? sk * M.t[i][2][c] : (R)0;
+        } else {
+            R *o = rows + (6 + NS + i) * rs;
+            for (int q = 0; q < 18; q++) o[q] = 0;
+            if (in.valid[i])
+                for (int c = 0; c < 3; c++) o[6 * i + 3 + c] = sk * M.t[i][2][c];
+        }
     }
     return (kavg < 0.0) ? 2 : 0;
 }

@@ -11,9 +11,12 @@ namespace fs {
 template <class R, bool COMP, bool AVGK, class S>
 __global__ void __launch_bounds__(128) k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
 {
-    constexpr int NR = T3Rows<AVGK>::N;
+    constexpr int NR = T3Rows<AVGK>::N, NS = T3Rows<AVGK>::NS;
     constexpr int ND = 18;
-    constexpr int STRIDE = NR * ND + 1;
+    // homogeneous elements: the compact rows (126 values instead of 198);
+    // layered ones: dense rows.  An odd stride keeps the threads' rows in
+    // distinct shared-memory banks.
+    constexpr int STRIDE = COMP ? NR * ND + 1 : CompactRows<3, NS>::SIZE + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R *rows = reinterpret_cast<R *>(smem_raw) + threadIdx.x * STRIDE;
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -21,9 +24,12 @@ __global__ void __launch_bounds__(128) k_t3_elements(const MeshDev m, const MatC
     ElemIn<3> in;
     load_elem<3>(m, r, in);
     const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
-    int st = t3_rows<R, COMP, AVGK>(in, mc, gc, rows, ND);
+    int st = t3_rows<R, COMP, AVGK, !COMP>(in, mc, gc, rows, ND);
     if (st) atomicOr(status, DEV_NEG_DRILL);
-    write_blocks<R, S, 3, !COMP>(rows, NR, ke + r * (6 * 36));
+    if constexpr (COMP)
+        write_blocks<R, S, 3, false>(rows, NR, ke + r * (6 * 36));
+    else
+        write_blocks_compact<R, S, 3, NS>(rows, ke + r * (6 * 36));
 }
 
 template <class R, bool COMP, bool AVGK, class S = R>
@@ -33,7 +39,7 @@ static int run_t3(fs_ctx *c, S *ke)
     if (epb <= 0) epb = (sizeof(R) == 8 && AVGK) ? 64 : 128;
     if (epb != 32 && epb != 64) epb = 128;
     if (sizeof(R) == 8 && AVGK && epb > 64) epb = 64;  // shared memory of the double average-K rows
-    const size_t smem = t3_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, AVGK, epb);
+    const size_t smem = t3_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, AVGK, COMP, epb);
     auto kern = k_t3_elements<R, COMP, AVGK, S>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<nblk2(c->mesh.nelem, epb), epb, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);

@@ -215,7 +215,7 @@ int explicit_launch_steps(fs_ctx *c, int64_t nsteps);
 
 // tile-shape autotuner of the shell assembly
 int autotune_shell(fs_ctx *c, int precision);
-size_t t3_smem(int precision, bool avgk, int epb);
+size_t t3_smem(int precision, bool avgk, bool layered, int epb);
 size_t entry_bytes(int precision);
 size_t gather_smem_bytes(int precision, int nen, int warps);
 int run_t3_any(fs_ctx *c, int precision, void *ke);

@@ -26,10 +26,12 @@
 namespace fs {
 
 // Shared memory of one block of the element kernels (per-element Gram rows).
-size_t t3_smem(int precision, bool avgk, int epb)
+size_t t3_smem(int precision, bool avgk, bool layered, int epb)
 {
     const int nr = avgk ? T3Rows<true>::N : T3Rows<false>::N;
-    return (precision == FS_FP64 ? 8 : 4) * (size_t)epb * (nr * 18 + 1);
+    const int per = layered ? nr * 18 + 1
+                            : (avgk ? CompactRows<3, T3Rows<true>::NS>::SIZE : CompactRows<3, T3Rows<false>::NS>::SIZE) + 1;
+    return (precision == FS_FP64 ? 8 : 4) * (size_t)epb * per;
 }
 size_t q4_smem(int precision, int epb) { return (precision == FS_FP64 ? 8 : 4) * (size_t)epb * (36 * 24 + 1); }
 
@@ -346,7 +348,7 @@ int autotune_shell(fs_ctx *c, int precision)
     int best_e = 0;
     float best_ms = 1e30f;
     for (int epb : ecand) {
-        const size_t smem = t3 ? t3_smem(precision, avgk, epb) : q4_smem(precision, epb);
+        const size_t smem = t3 ? t3_smem(precision, avgk, m.etype == FS_T3FFCOMP, epb) : q4_smem(precision, epb);
         if (smem > SMEM_MAX) continue;
         c->tune.elem_epb = epb;
         float ms = 0.f;
