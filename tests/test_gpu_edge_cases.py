@@ -1,0 +1,150 @@
+"""Edge cases of the assembly on the GPU, against the oracle: one element,
+nodes that no element uses, an empty mesh, every dof fixed, a node whose row
+is longer than the gather keeps in registers (the in-place path), and an
+element order that is not the mesh order.  FP64 within 1e-12 of the oracle
+with the identical pattern; mixed within 1e-6."""
+import numpy as np
+import pytest
+
+import flexshell as F
+from flexshell import _abi
+from oracle import oracle as O
+from checks import relmax, same_pattern
+from test_gpu_parity import _Mat
+
+pytestmark = pytest.mark.gpu
+
+E, NU, T = 2.0e11, 0.3, 0.01
+DPS = E / (1 - NU ** 2) * np.array([[1, NU, 0], [NU, 1, 0], [0, 0, (1 - NU) / 2]])
+MAT = dict(Dps=DPS, Dt=E / 2 / (1 + NU) * np.eye(2), rho=7850.0)
+
+
+def _pair(xyz, conn, fixed_nodes=()):
+    quads = conn.shape[1] == 4
+    f = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    for c in range(1, 7):
+        if len(fixed_nodes):
+            f.setebc(fixed_nodes, c)
+    f.numberdofs()
+    et = O.Q4RS if quads else O.T3FF
+    stab = 0.1 if quads else 5 / 12 / 1.5
+    P = O.Problem(et, xyz, conn, f.dofnums, thickness=T, material=MAT, stab_c=stab)
+    P.compute_normals()
+    cls = F.FEMMShellQ4RS if quads else F.FEMMShellT3FF
+    femm = cls(conn, T, _Mat(MAT), stab_fun=stab)
+    geom0 = F.NodalField(xyz)
+    femm.associategeometry(geom0)
+    return P, femm, geom0, f
+
+
+def _check(P, femm, geom0, dchi, n=None):
+    n = dchi.nalldofs() if n is None else n
+    asm = F.SysmatAssemblerSparse() if n == dchi.nalldofs() else F.SysmatAssemblerFFBlock(n)
+    K = femm.stiffness(asm, geom0, None, None, dchi)
+    Ko = P.assemble_scipy("K", O.KEEP_ZEROS, n=n)
+    assert K.shape == Ko.shape and same_pattern(K, Ko)
+    if Ko.nnz:
+        assert relmax(K, Ko) <= 1e-12
+        Km = femm.stiffness(asm, geom0, None, None, dchi, precision=F.FS_MIXED)
+        assert same_pattern(Km, Ko) and relmax(Km, Ko) <= 1e-6
+    return K
+
+
+@pytest.mark.parametrize("quads", [False, True])
+def test_single_element(quads):
+    xyz = np.array([[0.0, 0.0, 0.0], [1.0, 0.1, 0.05], [0.9, 1.2, -0.02], [-0.1, 0.8, 0.03]])
+    conn = np.array([[1, 2, 3, 4]] if quads else [[1, 2, 3]])
+    if not quads:
+        xyz = xyz[:3]
+    P, femm, geom0, dchi = _pair(xyz, conn)
+    K = _check(P, femm, geom0, dchi)
+    assert K.nnz == (6 * conn.shape[1]) ** 2
+    femm.close()
+
+
+def test_unused_nodes_keep_empty_rows():
+    # a 4 x 4 quad patch split into triangles, plus three nodes no element uses
+    n = 4
+    xs, ys = np.meshgrid(np.linspace(0, 1, n + 1), np.linspace(0, 1, n + 1), indexing="ij")
+    xyz = np.c_[xs.ravel(), ys.ravel(), 0.02 * np.sin(3 * xs.ravel())]
+    idx = lambda i, j: i * (n + 1) + j + 1
+    conn = []
+    for i in range(n):
+        for j in range(n):
+            conn += [[idx(i, j), idx(i + 1, j), idx(i + 1, j + 1)], [idx(i, j), idx(i + 1, j + 1), idx(i, j + 1)]]
+    conn = np.array(conn)
+    xyz = np.r_[xyz, [[2.0, 2.0, 0.0], [3.0, 2.0, 0.0], [2.0, 3.0, 0.0]]]
+    P, femm, geom0, dchi = _pair(xyz, conn)
+    K = _check(P, femm, geom0, dchi)
+    orphan = dchi.dofnums[-3:].ravel() - 1
+    Kc = K.tocsc()
+    assert all(Kc.indptr[d + 1] == Kc.indptr[d] for d in orphan)
+    femm.close()
+
+
+def test_empty_mesh_and_all_dofs_fixed():
+    xyz = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]])
+    # every dof fixed: the free-free block is empty
+    P, femm, geom0, dchi = _pair(xyz, np.array([[1, 2, 3]]), fixed_nodes=[1, 2, 3])
+    assert dchi.nfreedofs == 0
+    K = femm.stiffness(F.SysmatAssemblerFFBlock(0), geom0, None, None, dchi)
+    assert K.shape == (0, 0) and K.nnz == 0
+    femm.close()
+    # no elements at all: an all-zero matrix of the requested size
+    import ctypes
+    from flexshell._lib import ptr
+    ctx = F.Context(0)
+    conn = np.zeros((0, 3), dtype=np.int64)
+    xyzf = np.asfortranarray(xyz)
+    dof = np.asfortranarray(np.arange(1, 19, dtype=np.int64).reshape(3, 6))
+    ctx.call("fs_mesh_set", _abi.FS_T3FF, 3, ptr(xyzf), 0, ptr(conn), None, ptr(dof))
+    prm = _abi.make_params(DPS, MAT["Dt"], MAT["rho"], T, stab_c=5 / 12 / 1.5)
+    ctx.call("fs_params_set", prm, None)
+    ctx.call("fs_normals_compute")
+    nnz = ctypes.c_int64(-1)
+    ctx.call("fs_stiffness", _abi.FS_FP64, _abi.FS_ASM_SPARSE, 18, ctypes.byref(nnz))
+    assert nnz.value == 0
+    colptr = np.zeros(19, dtype=np.int64)
+    ctx.call("fs_matrix_copy", ptr(colptr), None, None)
+    assert np.all(colptr == 1)
+    ctx.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+def test_long_rows_take_the_in_place_path(quads):
+    # a fan of 48 triangles (or 24 quads) around one centre node: the centre's
+    # row holds 49 (or 49) nodes x 6 = 294 columns, above the 128 a warp keeps
+    # in registers
+    m = 48
+    ang = np.linspace(0, 2 * np.pi, m, endpoint=False)
+    if quads:
+        ring1 = np.c_[0.5 * np.cos(ang), 0.5 * np.sin(ang), 0.02 * np.cos(2 * ang)]
+        xyz = np.r_[[[0.0, 0.0, 0.0]], ring1]
+        # quads (centre, k, k+1, k+2) for even k: every ring node touches the centre
+        conn = np.array([[1, 2 + k, 2 + (k + 1) % m, 2 + (k + 2) % m] for k in range(0, m, 2)])
+    else:
+        ring = np.c_[np.cos(ang), np.sin(ang), 0.05 * np.sin(3 * ang)]
+        xyz = np.r_[[[0.0, 0.0, 0.0]], ring]
+        conn = np.array([[1, 2 + k, 2 + (k + 1) % m] for k in range(m)])
+    P, femm, geom0, dchi = _pair(xyz, conn)
+    K = _check(P, femm, geom0, dchi)
+    d0 = dchi.dofnums[0, 0] - 1
+    assert K.tocsr()[d0].nnz > 128
+    femm.close()
+
+
+def test_element_order_not_the_mesh_order():
+    # elements listed in a shuffled order: the assembly follows the given order
+    n = 6
+    xs, ys = np.meshgrid(np.linspace(0, 1, n + 1), np.linspace(0, 1, n + 1), indexing="ij")
+    rng = np.random.default_rng(9)
+    xyz = np.c_[xs.ravel(), ys.ravel(), 0.01 * rng.normal(size=xs.size)]
+    idx = lambda i, j: i * (n + 1) + j + 1
+    conn = np.array([[idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)]
+                     for i in range(n) for j in range(n)])
+    conn = conn[rng.permutation(conn.shape[0])]
+    conn = np.array([np.roll(c, rng.integers(4)) for c in conn])  # varied local numbering
+    P, femm, geom0, dchi = _pair(xyz, conn, fixed_nodes=[1, 2, 3])
+    _check(P, femm, geom0, dchi)
+    _check(P, femm, geom0, dchi, n=dchi.nfreedofs)
+    femm.close()
