@@ -112,10 +112,10 @@ def test_empty_mesh_and_all_dofs_fixed():
 
 @pytest.mark.parametrize("quads", [False, True])
 def test_long_rows_take_the_in_place_path(quads):
-    # a fan of 48 triangles (or 24 quads) around one centre node: the centre's
-    # row holds 49 (or 49) nodes x 6 = 294 columns, above the 128 a warp keeps
-    # in registers
-    m = 48
+    # a fan of 48 triangles (or 12 quads with 30 degree corners) around one
+    # centre node: the centre's row holds 49 (or 25) nodes x 6 = 294 (or 150)
+    # columns, above the 128 a warp keeps in registers
+    m = 24 if quads else 48
     ang = np.linspace(0, 2 * np.pi, m, endpoint=False)
     if quads:
         ring1 = np.c_[0.5 * np.cos(ang), 0.5 * np.sin(ang), 0.02 * np.cos(2 * ang)]
