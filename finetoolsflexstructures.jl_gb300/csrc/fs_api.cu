@@ -388,6 +388,22 @@ int fs_normals_compute(fs_ctx *c)
     return FS_OK;
 }
 
+int fs_normals_compute_csys(fs_ctx *c, int kind, const double *params)
+{
+    if (!c) return FS_ERR_BAD_INPUT;
+    FS_CUDA(c, cudaSetDevice(c->device));
+    FS_TRY(check_ready(c, false));
+    if (kind < FS_CSYS_ISOPARAMETRIC || kind > FS_CSYS_SPHERICAL)
+        return set_err(c, FS_ERR_BAD_INPUT, "unknown csys kind");
+    if (kind != FS_CSYS_ISOPARAMETRIC && !params) return set_err(c, FS_ERR_BAD_INPUT, "missing csys parameters");
+    if (kind != FS_CSYS_ISOPARAMETRIC && is_comp(c->mesh.etype))
+        return set_err(c, FS_ERR_UNSUPPORTED, "layered FEMMs take their normals from the layup csys");
+    FS_TRY(launch_normals(c, kind, params));
+    FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->normals_ready = true;
+    return FS_OK;
+}
+
 int fs_normals_set(fs_ctx *c, const double *normals, const uint8_t *valid)
 {
     if (!c || !normals || !valid) return FS_ERR_BAD_INPUT;

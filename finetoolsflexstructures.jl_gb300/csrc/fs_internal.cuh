@@ -198,7 +198,7 @@ int launch_prepare_mesh(fs_ctx *c, const int64_t *d_conn_raw, const int64_t *d_o
 int launch_prepare_dofs(fs_ctx *c, const int64_t *d_dof_raw);
 int build_adjacency(fs_ctx *c);
 int build_pattern(fs_ctx *c, int64_t n);
-int launch_normals(fs_ctx *c);
+int launch_normals(fs_ctx *c, int kind = FS_CSYS_ISOPARAMETRIC, const double *prm = nullptr);
 int launch_elements(fs_ctx *c, int precision);
 int launch_gather(fs_ctx *c, int precision, double *vals);
 int launch_elements_to(fs_ctx *c, int precision, void *ke);

@@ -66,8 +66,37 @@ int launch_elements(fs_ctx *c, int precision)
 // ---------------------------------------------------------------------------
 // nodal normals (associategeometry!)
 // ---------------------------------------------------------------------------
+// A built-in material csys (the mcsys of associategeometry!): its kind and
+// parameters (the FS_CSYS_* values of fs_normals_compute_csys).
+struct CsysSpec {
+    int kind;
+    double prm[9];
+};
+
+// third axis of the csys at the point XYZ (cartesian: fixed; cylindrical:
+// radial from the axis through prm[0..2] along the unit prm[3..5];
+// spherical: radial from the centre prm[0..2])
+__device__ void csys_normal(const CsysSpec &cs, const double XYZ[3], double nn[3])
+{
+    if (cs.kind == FS_CSYS_CARTESIAN) {
+        for (int c = 0; c < 3; c++) nn[c] = cs.prm[6 + c];
+        return;
+    }
+    double r[3];
+    for (int c = 0; c < 3; c++) r[c] = XYZ[c] - cs.prm[c];
+    if (cs.kind == FS_CSYS_CYLINDRICAL) {
+        const double d = r[0] * cs.prm[3] + r[1] * cs.prm[4] + r[2] * cs.prm[5];
+        for (int c = 0; c < 3; c++) r[c] -= d * cs.prm[3 + c];
+    }
+    const double l = sqrt(dot3(r, r));
+    for (int c = 0; c < 3; c++) nn[c] = r[c] / l;
+}
+
+// normal of element `rank` at its node a (times the surface Jacobian for Q4):
+// the layup csys axis (layered), the csys normal at the node (a built-in
+// mcsys), or the element frame normal (isoparametric)
 template <int NN>
-__device__ void elem_node_normal(const MeshDev &m, int64_t rank, int a, bool comp, double nn[3])
+__device__ void elem_node_normal(const MeshDev &m, int64_t rank, int a, bool comp, const CsysSpec &cs, double nn[3])
 {
     double X[NN][3];
     for (int q = 0; q < NN; q++) {
@@ -97,8 +126,12 @@ __device__ void elem_node_normal(const MeshDev &m, int64_t rank, int a, bool com
         jac = sqrt(dot3(cr, cr));
     }
     if (comp) {
-        const double *cs = m.groups[m.group[rank]].csmat;
-        for (int c = 0; c < 3; c++) nn[c] = jac * cs[6 + c];
+        const double *lc = m.groups[m.group[rank]].csmat;
+        for (int c = 0; c < 3; c++) nn[c] = jac * lc[6 + c];
+    } else if (cs.kind != FS_CSYS_ISOPARAMETRIC) {
+        double v[3];
+        csys_normal(cs, X[a], v);
+        for (int c = 0; c < 3; c++) nn[c] = jac * v[c];
     } else {
         double e[3][3];
         make_frame(J0, J1, e);
@@ -106,16 +139,21 @@ __device__ void elem_node_normal(const MeshDev &m, int64_t rank, int a, bool com
     }
 }
 
+// Node sums in assembly order, then the validity test: against the element
+// frame normal for T3 (src/FEMMShellT3FFModule.jl:598-611), against the
+// mcsys normal at the node for Q4 (src/FEMMShellQ4RSModule.jl:505-519).
 template <int NN>
-__global__ void k_normals(const MeshDev m, bool comp, double cos_thr, double *normals, uint8_t *valid)
+__global__ void k_normals(const MeshDev m, bool comp, double cos_thr, const CsysSpec cs, double *normals,
+                          uint8_t *valid)
 {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= m.nnodes) return;
+    const CsysSpec iso{FS_CSYS_ISOPARAMETRIC, {0, 0, 0, 0, 0, 0, 0, 0, 0}};
     double s[3] = {0, 0, 0};
     for (int64_t p = m.pp[r]; p < m.pp[r + 1]; p++) {
         int32_t v = m.pair_e[p];
         double nn[3];
-        elem_node_normal<NN>(m, v >> 2, v & 3, comp, nn);
+        elem_node_normal<NN>(m, v >> 2, v & 3, comp, cs, nn);
         for (int c = 0; c < 3; c++) s[c] += nn[c];
     }
     double len = sqrt(dot3(s, s));
@@ -125,7 +163,7 @@ __global__ void k_normals(const MeshDev m, bool comp, double cos_thr, double *no
     for (int64_t p = m.pp[r]; p < m.pp[r + 1]; p++) {
         int32_t v = m.pair_e[p];
         double nn[3];
-        elem_node_normal<NN>(m, v >> 2, v & 3, comp, nn);
+        elem_node_normal<NN>(m, v >> 2, v & 3, comp, NN == 3 ? iso : cs, nn);
         if (NN == 4) {  // the validity test uses the unit normal at the node
             double l = sqrt(dot3(nn, nn));
             if (l > 0.0)
@@ -137,9 +175,12 @@ __global__ void k_normals(const MeshDev m, bool comp, double cos_thr, double *no
     valid[r] = ok ? 1 : 0;
 }
 
-int launch_normals(fs_ctx *c)
+int launch_normals(fs_ctx *c, int kind, const double *prm)
 {
     MeshDev &m = c->mesh;
+    CsysSpec cs{kind, {0, 0, 0, 0, 0, 0, 0, 0, 0}};
+    const int np = kind == FS_CSYS_CARTESIAN ? 9 : (kind == FS_CSYS_CYLINDRICAL ? 6 : (kind == FS_CSYS_SPHERICAL ? 3 : 0));
+    for (int k = 0; k < np; k++) cs.prm[k] = prm[k];
     if (m.nnodes == 0) return FS_OK;
     double th = c->params.threshold_angle;
     double sn = sin(th / 180.0 * M_PI);
@@ -147,9 +188,9 @@ int launch_normals(fs_ctx *c)
     double cos_thr = 1 - ntol;
     bool comp = (m.etype == FS_T3FFCOMP || m.etype == FS_Q4RSCOMP);
     if (m.nen == 3)
-        k_normals<3><<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, comp, cos_thr, m.normals, m.valid);
+        k_normals<3><<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, comp, cos_thr, cs, m.normals, m.valid);
     else
-        k_normals<4><<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, comp, cos_thr, m.normals, m.valid);
+        k_normals<4><<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, comp, cos_thr, cs, m.normals, m.valid);
     FS_CUDA(c, cudaGetLastError());
     return FS_OK;
 }

@@ -8,7 +8,8 @@ interface.
 """
 from . import _abi, mesh, materials
 from ._abi import FS_FP64, FS_MIXED, FS_MIXED_COMP
-from .femm import (FEMMShellQ4RS, FEMMShellQ4RSComp, FEMMShellT3FF, FEMMShellT3FFComp,
+from .femm import (CSysCartesian, CSysCylindrical, CSysSpherical,
+                   FEMMShellQ4RS, FEMMShellQ4RSComp, FEMMShellT3FF, FEMMShellT3FFComp,
                    NodalField, SysmatAssemblerFFBlock, SysmatAssemblerSparse,
                    SysmatAssemblerSparseCSRSymm, SysmatAssemblerSparseDiag,
                    SysmatAssemblerSparseSymm, ShellBatch)

@@ -16,6 +16,7 @@ FS_ASM_SPARSE, FS_ASM_SPARSE_SYMM, FS_ASM_DIAG = 0, 1, 2
 FS_BEAM_STIFFNESS, FS_BEAM_GEOSTIFFNESS, FS_BEAM_MASS, FS_BEAM_GYROSCOPIC = 0, 1, 2, 3
 FS_BEAM_RESTORING, FS_BEAM_DISTRIBLOAD = 4, 5
 FS_RES_MOMENT, FS_RES_SHEAR, FS_RES_MEMBRANE = 1, 2, 3
+FS_CSYS_ISOPARAMETRIC, FS_CSYS_CARTESIAN, FS_CSYS_CYLINDRICAL, FS_CSYS_SPHERICAL = 0, 1, 2, 3
 
 
 class fs_beam_section(ctypes.Structure):

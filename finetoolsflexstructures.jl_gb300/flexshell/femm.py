@@ -110,12 +110,39 @@ def stab_coefficient(stab_fun, default):
 # ---------------------------------------------------------------------------
 # FEMMs
 # ---------------------------------------------------------------------------
+class CSysCartesian:
+    """A fixed material csys (the reference examples' cartesian!): its third
+    column is every node's normal."""
+    kind = _abi.FS_CSYS_CARTESIAN
+
+    def __init__(self, csmat=np.eye(3)):
+        self.params = np.asarray(csmat, dtype=np.float64).flatten(order="F")
+
+
+class CSysCylindrical:
+    """Radial normals from an axis (the reference examples' cylindrical!,
+    there the y axis through the origin)."""
+    kind = _abi.FS_CSYS_CYLINDRICAL
+
+    def __init__(self, point=(0.0, 0.0, 0.0), axis=(0.0, 1.0, 0.0)):
+        a = np.asarray(axis, dtype=np.float64)
+        self.params = np.r_[np.asarray(point, dtype=np.float64), a / np.linalg.norm(a)]
+
+
+class CSysSpherical:
+    """Radial normals from a centre (the reference examples' spherical!)."""
+    kind = _abi.FS_CSYS_SPHERICAL
+
+    def __init__(self, center=(0.0, 0.0, 0.0)):
+        self.params = np.asarray(center, dtype=np.float64)
+
+
 class _FEMMShell:
     etype = None
     nen = None
     default_stab = None
 
-    def __init__(self, conn, thickness, material=None, stab_fun=None, device=0, layup_groups=None):
+    def __init__(self, conn, thickness, material=None, stab_fun=None, device=0, layup_groups=None, mcsys=None):
         self.conn = np.ascontiguousarray(conn, dtype=np.int64)
         if self.conn.ndim != 2 or self.conn.shape[1] != self.nen:
             raise ValueError("connectivity must be nelem x %d" % self.nen)
@@ -126,6 +153,7 @@ class _FEMMShell:
         self.drilling_stiffness_scale = 1.0
         self.threshold_angle = 30.0
         self.layup_groups = layup_groups
+        self.mcsys = mcsys  # None: isoparametric (the reference default); or a CSys* above
         self.ctx = Context(device)
         self._geom = None
         self._dof_key = None
@@ -193,7 +221,11 @@ class _FEMMShell:
     def associategeometry(self, geom0):
         """associategeometry!(femm, geom0): nodal normals and validity."""
         self._upload_mesh(geom0)
-        self.ctx.call("fs_normals_compute")
+        if self.mcsys is None:
+            self.ctx.call("fs_normals_compute")
+        else:
+            prm = np.ascontiguousarray(self.mcsys.params, dtype=np.float64)
+            self.ctx.call("fs_normals_compute_csys", self.mcsys.kind, ptr(prm))
         nn = geom0.values.shape[0]
         self._normals = np.zeros((nn, 3), order="F")
         self._normal_valid = np.zeros(nn, dtype=np.uint8)

@@ -122,6 +122,23 @@ int fs_layups_set(fs_ctx *ctx, int32_t ngroups, const fs_layup_group *groups,
  * or the layup csys third axis for the layered FEMMs
  * (src/FEMMShellT3FFModule.jl:570-616, src/FEMMShellQ4RSModule.jl:472-525). */
 int fs_normals_compute(fs_ctx *ctx);
+/* The same with a built-in material csys (the FEMM's mcsys) in place of the
+ * isoparametric one (_compute_nodal_normal!, src/FEMMShellT3FFModule.jl:226-230,
+ * in associategeometry! :570-616 / src/FEMMShellQ4RSModule.jl:472-525): the
+ * kinds the reference examples define as closures, generalised.
+ *   FS_CSYS_CARTESIAN   params[9]: the 3x3 column-major csys matrix (its third
+ *                       column is the normal; bent_strip_examples.jl:15-20)
+ *   FS_CSYS_CYLINDRICAL params[6]: a point on the axis and the unit axis
+ *                       direction (radial normal; cylindrical! of
+ *                       clamp_cyl_expl_examples.jl:61-67 is point 0, axis y)
+ *   FS_CSYS_SPHERICAL   params[3]: the centre (radial normal; spherical! of
+ *                       hemisphere_examples.jl:31-39 is the origin)
+ * Homogeneous shells only (layered ones use their layup csys). */
+#define FS_CSYS_ISOPARAMETRIC 0
+#define FS_CSYS_CARTESIAN 1
+#define FS_CSYS_CYLINDRICAL 2
+#define FS_CSYS_SPHERICAL 3
+int fs_normals_compute_csys(fs_ctx *ctx, int kind, const double *params);
 /* Normals computed by the caller (e.g. a user `mcsys`), nnodes x 3 column-major. */
 int fs_normals_set(fs_ctx *ctx, const double *normals, const uint8_t *valid);
 int fs_normals_get(fs_ctx *ctx, double *normals, uint8_t *valid);

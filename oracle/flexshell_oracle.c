@@ -714,8 +714,31 @@ static void gather_X(const double *xyz, int64_t nnodes, const int64_t *cn, int n
         for (int c = 0; c < 3; c++) X[3 * a + c] = xyz[(cn[a] - 1) + c * nnodes];
 }
 
+/* The third axis of the built-in material csys kinds at the point XYZ: the
+ * csys updaters of the reference examples, generalised (cartesian! of
+ * bent_strip_examples.jl:15-20: a fixed matrix; cylindrical! of
+ * clamp_cyl_expl_examples.jl:61-67: radial from an axis, there the y axis;
+ * spherical! of hemisphere_examples.jl:31-39: radial from a centre, there the
+ * origin).  params: CARTESIAN the 3x3 column-major matrix; CYLINDRICAL a
+ * point on the axis and the unit axis direction; SPHERICAL the centre. */
+static void csys_normal(int kind, const double *prm, const double *XYZ, double *nn)
+{
+    double r[3];
+    if (kind == ORC_CSYS_CARTESIAN) {
+        nn[0] = prm[6]; nn[1] = prm[7]; nn[2] = prm[8];
+        return;
+    }
+    for (int c = 0; c < 3; c++) r[c] = XYZ[c] - prm[c];
+    if (kind == ORC_CSYS_CYLINDRICAL) {
+        double d = r[0] * prm[3] + r[1] * prm[4] + r[2] * prm[5];
+        for (int c = 0; c < 3; c++) r[c] -= d * prm[3 + c];
+    }
+    double l = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    for (int c = 0; c < 3; c++) nn[c] = r[c] / l;
+}
+
 static void point_normal(const orc_params *p, int64_t e, const double *X, int j, double *nn,
-                         double *Jac)
+                         double *Jac, int kind, const double *prm)
 {
     int nen = nen_of(p->etype);
     double J[6], E[9];
@@ -735,6 +758,8 @@ static void point_normal(const orc_params *p, int64_t e, const double *X, int j,
     if (is_comp(p->etype)) {
         const double *cs = p->gcsmat + 9 * p->group[e];
         nn[0] = cs[6]; nn[1] = cs[7]; nn[2] = cs[8];
+    } else if (kind != ORC_CSYS_ISOPARAMETRIC) {
+        csys_normal(kind, prm, X + 3 * j, nn);  /* at the node: loc of the nodal rule */
     } else {
         e_g(E, J);
         nn[0] = E[6]; nn[1] = E[7]; nn[2] = E[8];
@@ -744,6 +769,19 @@ static void point_normal(const orc_params *p, int64_t e, const double *X, int j,
 int orc_normals(int etype, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
                 const int64_t *order, double threshold_deg, const orc_params *p, double *normals,
                 uint8_t *valid)
+{
+    return orc_normals_csys(etype, nnodes, xyz, nelem, conn, order, threshold_deg, p, ORC_CSYS_ISOPARAMETRIC,
+                            NULL, normals, valid);
+}
+
+/* The same with the material csys of one of the built-in kinds: the node sums
+ * use the csys normal at the node (weighted by the Jacobian for Q4); the
+ * validity test compares with the element frame normal for T3
+ * (src/FEMMShellT3FFModule.jl:598-611) and with the csys normal for Q4
+ * (src/FEMMShellQ4RSModule.jl:505-519). */
+int orc_normals_csys(int etype, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                     const int64_t *order, double threshold_deg, const orc_params *p, int kind,
+                     const double *prm, double *normals, uint8_t *valid)
 {
     (void)etype;
     int nen = nen_of(p->etype);
@@ -756,7 +794,7 @@ int orc_normals(int etype, int64_t nnodes, const double *xyz, int64_t nelem, con
         gather_X(xyz, nnodes, cn, nen, X);
         for (int j = 0; j < nen; j++) {
             double nn[3], Jac;
-            point_normal(p, e, X, j, nn, &Jac);
+            point_normal(p, e, X, j, nn, &Jac, kind, prm);
             int64_t node = cn[j] - 1;
             for (int c = 0; c < 3; c++) normals[node + c * nnodes] += (nen == 3 ? nn[c] : Jac * nn[c]);
         }
@@ -779,7 +817,7 @@ int orc_normals(int etype, int64_t nnodes, const double *xyz, int64_t nelem, con
         gather_X(xyz, nnodes, cn, nen, X);
         for (int j = 0; j < nen; j++) {
             double nn[3], Jac;
-            point_normal(p, e, X, j, nn, &Jac);
+            point_normal(p, e, X, j, nn, &Jac, nen == 3 ? ORC_CSYS_ISOPARAMETRIC : kind, prm);
             int64_t node = cn[j] - 1;
             double nd = normals[node] * nn[0] + normals[node + nnodes] * nn[1] +
                         normals[node + 2 * nnodes] * nn[2];

@@ -55,6 +55,15 @@ int orc_normals(int etype, int64_t nnodes, const double *xyz, int64_t nelem,
                 const int64_t *conn, const int64_t *order, double threshold_deg,
                 const orc_params *p, double *normals, uint8_t *valid);
 
+/* Normals with a built-in material csys kind instead of the isoparametric
+ * one: ORC_CSYS_CARTESIAN (params: 3x3 column-major matrix), _CYLINDRICAL
+ * (a point on the axis, the unit axis direction), _SPHERICAL (the centre). */
+enum { ORC_CSYS_ISOPARAMETRIC = 0, ORC_CSYS_CARTESIAN = 1, ORC_CSYS_CYLINDRICAL = 2, ORC_CSYS_SPHERICAL = 3 };
+int orc_normals_csys(int etype, int64_t nnodes, const double *xyz, int64_t nelem,
+                     const int64_t *conn, const int64_t *order, double threshold_deg,
+                     const orc_params *p, int kind, const double *params, double *normals,
+                     uint8_t *valid);
+
 int orc_element_stiffness(const orc_params *p, int64_t e, const double *X,
                           const double *nrm, const uint8_t *nvalid, double *Ke);
 

@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 
 T3FF, T3FFCOMP, Q4RS, Q4RSCOMP = 0, 1, 2, 3
 RES_MOMENT, RES_SHEAR, RES_MEMBRANE = 1, 2, 3
+CSYS_ISOPARAMETRIC, CSYS_CARTESIAN, CSYS_CYLINDRICAL, CSYS_SPHERICAL = 0, 1, 2, 3
 KEEP_ZEROS, DROP_ZEROS, DIAG = 0, 1, 2
 
 _c_dbl_p = ctypes.POINTER(ctypes.c_double)
@@ -80,6 +81,7 @@ def lib():
         build()
         L = ctypes.CDLL(LIB_PATH)
         L.orc_normals.restype = ctypes.c_int
+        L.orc_normals_csys.restype = ctypes.c_int
         L.orc_assemble.restype = ctypes.c_int
         L.orc_result_nnz.restype = ctypes.c_int64
         L.orc_result_n.restype = ctypes.c_int64
@@ -162,13 +164,19 @@ class Problem:
     def nen(self):
         return self.conn.shape[1]
 
-    def compute_normals(self, threshold_deg=30.0):
+    def compute_normals(self, threshold_deg=30.0, csys_kind=0, csys_params=None):
+        """associategeometry!: csys_kind 0 the isoparametric normals, 1
+        cartesian (params: 3x3 matrix), 2 cylindrical (point on the axis, unit
+        axis direction), 3 spherical (centre)."""
         nrm = np.zeros((self.nnodes, 3), dtype=np.float64, order="F")
         val = np.zeros(self.nnodes, dtype=np.uint8)
-        st = lib().orc_normals(self.etype, ctypes.c_int64(self.nnodes), _p(self.xyz, _c_dbl_p),
-                               ctypes.c_int64(self.nelem), _p(self.conn, _c_i64_p),
-                               _p(self.order, _c_i64_p), ctypes.c_double(threshold_deg),
-                               ctypes.byref(self.params), _p(nrm, _c_dbl_p), _p(val, _c_u8_p))
+        prm = None if csys_params is None else np.ascontiguousarray(
+            np.asarray(csys_params, dtype=np.float64).flatten(order="F"))
+        st = lib().orc_normals_csys(self.etype, ctypes.c_int64(self.nnodes), _p(self.xyz, _c_dbl_p),
+                                    ctypes.c_int64(self.nelem), _p(self.conn, _c_i64_p),
+                                    _p(self.order, _c_i64_p), ctypes.c_double(threshold_deg),
+                                    ctypes.byref(self.params), ctypes.c_int(csys_kind), _p(prm, _c_dbl_p),
+                                    _p(nrm, _c_dbl_p), _p(val, _c_u8_p))
         assert st == 0
         self.normals, self.valid = nrm, val
         return nrm, val
