@@ -541,10 +541,17 @@ def main():
     ap.add_argument("--n", type=int, default=1024, help="quads per side")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-explicit", action="store_true")
+    ap.add_argument("--explicit-only", action="store_true",
+                    help="only the explicit-dynamics section, on an n x n Q4RS plate for 64 x steps steps "
+                         "(a small case for profiling the step kernels)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.explicit_only:
+        import torch
+        print(json.dumps(explicit_c5(torch, device=0, n=args.n, nsteps=64 * args.steps, iters=50)))
+        return 0
 
     import torch
     import torch.distributed as dist
