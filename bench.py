@@ -147,6 +147,24 @@ def cpu_baseline(steps=None, budget_s=10.0, n=96):
                       "assembly, %d repetitions" % (n, n, el, reps)}, times
 
 
+def max_over_ranks(x, world, dist):
+    """The largest value over the ranks (the slowest replica's time); x itself
+    on one rank.  NCCL reduces a device tensor, gloo a host one."""
+    if world <= 1:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload_text(n):
+    nodes = (n + 1) ** 2
+    return "T3FF stiffness assembly, %dx%d jittered wavy plate (%d triangles, %d nodes, %d dofs)" % (
+        n, n, 2 * n * n, nodes, 6 * nodes)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -161,8 +179,8 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "T3FF stiffness assembly, jittered wavy plate (bounded CPU sample of the "
-                                   "1024x1024 configuration)", "sample": cb["sample"]},
+            "config": {"workload": workload_text(args.n), "precision": "FP64 (the reference's arithmetic)",
+                       "sample": "bounded CPU sample of the workload: " + cb["sample"]},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "elements/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -575,10 +593,7 @@ def main():
     clocks = Clocks(local)
     with clocks:
         ms_mixed, ph_mixed, nnz = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
-    if world > 1:
-        t = torch.tensor([ms_mixed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_mixed = float(t.item())
+    ms_mixed = max_over_ranks(ms_mixed, world, dist)
     tiles_mixed = asm.tiles()
     v_mixed = asm.values(nnz)
     ms_fp64, ph_fp64, _ = time_steps(asm, _abi.FS_FP64, args.steps, args.warmup, torch, stream)
@@ -618,15 +633,14 @@ def main():
     for _ in range(args.warmup):
         e2e_step()
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
     torch.cuda.synchronize()
     ms_e2e = 1e3 * (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(ms_e2e, world, dist)
     h2d = (3 * nn) * 8 + (6 * nn) * 8
     d2h = (asm.n + 1) * 8 + nnz * 8 + nnz * 8
     del h_colptr, h_rowval, h_nzval
@@ -690,8 +704,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32-element/f64-assembly", "data": "synthetic",
-        "config": {"workload": "T3FF stiffness assembly, mixed precision, %dx%d jittered wavy plate "
-                               "(%d triangles, %d nodes, %d dofs)" % (args.n, args.n, ne3, nodes, 6 * nodes),
+        "config": {"workload": workload_text(args.n),
                    "elements": ne3, "nnz": nnz, "precision": "FS_MIXED", "assembler": "SysmatAssemblerSparse",
                    "pattern": "built once per mesh (symbolic %.2f ms), not in the timed step" % t3["t_sym"],
                    "l2": "inputs larger than L2 (element matrices %.2f GB, values %.2f GB)" % (
