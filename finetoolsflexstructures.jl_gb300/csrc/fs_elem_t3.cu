@@ -8,8 +8,17 @@ namespace fs {
 // parameter: every tile runs the same compiled kernel, so the tile never
 // changes the arithmetic of an element (compiled variants could contract
 // products and sums into FMAs differently).
+// Resident blocks of 128 threads asked of the compiler (the register budget
+// per thread): 4 (128 registers) for float rows of homogeneous elements, whose
+// occupancy is otherwise held by registers; 3 (170) for the other float rows;
+// 2 (255) for double rows.
+template <class R, bool COMP, bool AVGK> struct T3MinBlocks {
+    static constexpr int value = sizeof(R) == 8 ? 2 : ((!COMP && !AVGK) ? 4 : 3);
+};
+
 template <class R, bool COMP, bool AVGK, class S>
-__global__ void __launch_bounds__(128) k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
+__global__ void __launch_bounds__(128, (T3MinBlocks<R, COMP, AVGK>::value))
+    k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
 {
     constexpr int NR = T3Rows<AVGK>::N, NS = T3Rows<AVGK>::NS;
     constexpr int ND = 18;

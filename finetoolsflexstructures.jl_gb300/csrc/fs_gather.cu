@@ -180,11 +180,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             cur[c] = j < L ? b0 : 0;
             last[c] = j < L ? b1 : 0;
             beg[c] = cur[c];
-#pragma unroll
-            for (int k = 0; k < 6; k++) {
-                hi[c][k] = 0;
-                lo[c][k] = 0;
-            }
+            // hi, lo: set by the first contribution (every row position has one)
         }
         // lane-fixed staging chunks: chunk lane + 32 t of every slab
         int cb[CPL], cwd[CPL];
