@@ -376,14 +376,31 @@ __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_
                 cd[6 * s + k] = v <= n_mat ? v : 0;
             }
         }
-        for (int q = 0; q < 6 * n; q++) L += cd[q] != 0;
+        // the usual numbering (node-major, the neighbours sorted) lists the
+        // kept dofs in increasing order: their rank is their running count;
+        // any other numbering is ranked by counting
+        bool sorted = true;
+        int32_t prev = 0;
+        for (int q = 0; q < 6 * n; q++) {
+            const int32_t v = cd[q];
+            if (v != 0) {
+                sorted &= v > prev;
+                prev = v;
+                L++;
+            }
+        }
+        int run = 0;
         for (int q = 0; q < 6 * n; q++) {
             const int32_t v = cd[q];
             int16_t pos = -1;
             if (v != 0) {
-                int cntless = 0;
-                for (int q2 = 0; q2 < 6 * n; q2++) cntless += (cd[q2] != 0) & (cd[q2] < v);
-                pos = (int16_t)cntless;
+                if (sorted) {
+                    pos = (int16_t)run++;
+                } else {
+                    int cntless = 0;
+                    for (int q2 = 0; q2 < 6 * n; q2++) cntless += (cd[q2] != 0) & (cd[q2] < v);
+                    pos = (int16_t)cntless;
+                }
             }
             colpos[off * 6 + q] = pos;
             if (pos >= 0) colsrc[off * 6 + pos] = (uint16_t)q;
@@ -409,6 +426,16 @@ __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_
             }
     }
     rowlen[r] = L;
+}
+
+// *out = max(v[0..n)) (out zeroed before; values are non-negative)
+__global__ void k_max_i32(int64_t n, const int32_t *v, int32_t *out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t x = i < n ? v[i] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if ((threadIdx.x & 31) == 0 && x > 0) atomicMax(out, x);
 }
 
 __global__ void k_row_lengths(int64_t nnodes, int64_t n_mat, const int32_t *dof, const int32_t *rowlen,
@@ -496,18 +523,17 @@ int build_pattern(fs_ctx *c, int64_t n)
     FS_CUDA(c, cudaMemsetAsync(owner, 0, sizeof(int32_t) * std::max<int64_t>(n, 1), c->stream));
     FS_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * std::max<int64_t>(n, 1), c->stream));
     if (nn) k_row_lengths<<<nblk(6 * nn, 256), 256, 0, c->stream>>>(nn, n, m.dof, P.rowlen, cnt, owner, c->d_status);
-    // longest row (selects the gather variant)
-    {
-        std::vector<int32_t> rl((size_t)nn);
-        if (nn) FS_CUDA(c, cudaMemcpyAsync(rl.data(), P.rowlen, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost, c->stream));
-        FS_CUDA(c, cudaStreamSynchronize(c->stream));
-        int mx = 0;
-        for (int64_t i = 0; i < nn; i++) mx = rl[i] > mx ? rl[i] : mx;
-        P.maxlen = mx;
-    }
+    // longest row (selects the gather variant): reduced on the device, read
+    // back with the scan total
+    int32_t *d_max = reinterpret_cast<int32_t *>(owner);  // owner counts are consumed by k_row_lengths
+    FS_CUDA(c, cudaMemsetAsync(d_max, 0, sizeof(int32_t), c->stream));
+    if (nn) k_max_i32<<<nblk(nn, 256), 256, 0, c->stream>>>(nn, P.rowlen, d_max);
+    int32_t mx = 0;
+    FS_CUDA(c, cudaMemcpyAsync(&mx, d_max, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
     FS_TRY(grow(c, &P.rowptr, &P.cap_rowptr, (size_t)n + 1));
     int64_t nnz = 0;
     FS_TRY(exclusive_scan_i64(c, cnt, P.rowptr, n, &nnz));
+    P.maxlen = mx;  // the scan's read-back synchronised the stream
     FS_TRY(read_status(c, &bits));
     if (bits & DEV_BAD_DOF) return set_err(c, FS_ERR_BAD_INPUT, "two dofs share one dof number");
     FS_TRY(grow(c, &P.colidx, &P.cap_colidx, (size_t)nnz));
