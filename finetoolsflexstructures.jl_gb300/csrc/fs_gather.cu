@@ -190,6 +190,52 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             cb[t] = ch / BCH;
             cwd[t] = ch - cb[t] * BCH;
         }
+        // entry (krow = 0, kcol) of block (a_q, b) of staged pair q; a mirrored
+        // block is read transposed: the six rows are st apart
+        auto slab_entry = [&](uint32_t e, int kc, int q0, int &st) -> const R * {
+            const int q = (int)(e & 63u) - q0;
+            const int b = (int)((e >> 6) & 3u);
+            const bool tr = (e >> 8) & 1u;
+            st = tr ? 1 : 6;
+            return stage + q * SLAB + b * 36 + (tr ? 6 * kc : kc);
+        };
+        if (pe - pb <= G_MAXP) {
+            // all pairs of the node in one batch (the usual case): every
+            // contribution is staged, each sum runs over its whole list
+            const int cnt = (int)(pe - pb);
+            for (int q = 0; q < cnt; q++) {
+                const int32_t pel = __shfl_sync(0xffffffffu, pel_l, q);
+                const int a = pel & 3;
+                const R *base = ke + (int64_t)(pel >> 2) * ND2;
+#pragma unroll
+                for (int t = 0; t < CPL; t++) {
+                    if (lane + 32 * t < CH) {
+                        const int bb = cb[t];
+                        const R *src = base + ub(min(a, bb), max(a, bb), NEN) * 36;
+                        cp_async16(reinterpret_cast<char *>(stage + q * SLAB + bb * 36) + 16 * cwd[t],
+                                   reinterpret_cast<const char *>(src) + 16 * cwd[t]);
+                    }
+                }
+            }
+            cp_async_wait_all();
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c < G_COLS; c++) {
+                int e = cur[c];
+                const int e1 = last[c];
+                if (e < e1) {
+                    int st;
+                    const R *src = slab_entry(sent[e], kcol[c], 0, st);
+#pragma unroll
+                    for (int k = 0; k < 6; k++) gather_set(hi[c][k], lo[c][k], src[st * k]);
+                    for (e++; e < e1; e++) {
+                        src = slab_entry(sent[e], kcol[c], 0, st);
+#pragma unroll
+                        for (int k = 0; k < 6; k++) gather_add(hi[c][k], lo[c][k], src[st * k]);
+                    }
+                }
+            }
+        } else
         for (int64_t p0 = pb; p0 < pe; p0 += G_MAXP) {
             const int cnt = (int)min((int64_t)G_MAXP, pe - p0);
             const int q0 = (int)(p0 - pb);

@@ -110,6 +110,19 @@ def test_empty_mesh_and_all_dofs_fixed():
     ctx.close()
 
 
+def test_node_with_more_pairs_than_one_staging_batch():
+    # a fan of 10 triangles: the centre node has 10 element pairs, more than the
+    # 8 the gather stages at once, and a row of 66 columns kept in registers
+    m = 10
+    ang = np.linspace(0, 2 * np.pi, m, endpoint=False)
+    xyz = np.r_[[[0.0, 0.0, 0.0]], np.c_[np.cos(ang), np.sin(ang), 0.05 * np.sin(2 * ang)]]
+    conn = np.array([[1, 2 + k, 2 + (k + 1) % m] for k in range(m)])
+    P, femm, geom0, dchi = _pair(xyz, conn)
+    K = _check(P, femm, geom0, dchi)
+    assert K.tocsr()[dchi.dofnums[0, 0] - 1].nnz == 66
+    femm.close()
+
+
 @pytest.mark.parametrize("quads", [False, True])
 def test_long_rows_take_the_in_place_path(quads):
     # a fan of 48 triangles (or 12 quads with 30 degree corners) around one
