@@ -535,35 +535,19 @@ def composite_c4(torch, device=0, n=512, n_eig=64, nev=20, steps=5, warmup=3):
     return out
 
 
-def time_steps(asm, precision, steps, warmup, torch, stream, sep=None):
-    """ms per assembly step with the library's default overlap of the element
-    kernel and the gather; then (into `sep`, when given) the same steps with
-    the overlap off, whose per-step phases time each kernel alone (element
-    kernel, gather, symbolic, compaction: the roofline's launch durations)."""
+def time_steps(asm, precision, steps, warmup, torch, stream):
     for _ in range(warmup):
         asm.stiffness(precision)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phases = np.zeros(4)
     torch.cuda.synchronize()
     ev0.record(stream)
     for _ in range(steps):
         nnz = asm.stiffness(precision)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / steps
-    phases = np.zeros(4)
-    asm.ctx.call("fs_overlap", 0)
-    asm.stiffness(precision)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(steps):
-        asm.stiffness(precision)
         phases += asm.timings()
     ev1.record(stream)
     torch.cuda.synchronize()
-    asm.ctx.call("fs_overlap", 1)
-    if sep is not None:
-        sep.append(ev0.elapsed_time(ev1) / steps)
-    return ms, phases / steps, nnz
+    return ev0.elapsed_time(ev1) / steps, phases / steps, nnz
 
 
 def main():
@@ -608,8 +592,7 @@ def main():
         dist.barrier()
     clocks = Clocks(local)
     with clocks:
-        sep_t3 = []
-        ms_mixed, ph_mixed, nnz = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream, sep_t3)
+        ms_mixed, ph_mixed, nnz = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
     ms_mixed = max_over_ranks(ms_mixed, world, dist)
     tiles_mixed = asm.tiles()
     v_mixed = asm.values(nnz)
@@ -670,8 +653,7 @@ def main():
     stream = torch.cuda.ExternalStream(asm.ctx.stream())
     asm.stiffness(_abi.FS_MIXED)
     t_sym_q4 = asm.timings()[2]
-    sep_q4 = []
-    ms_q_mixed, ph_q_mixed, nnz_q = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream, sep_q4)
+    ms_q_mixed, ph_q_mixed, nnz_q = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
     tiles_q = {"mixed": asm.tiles()}
     vq_m = asm.values(nnz_q)
     ms_q_fp64, ph_q_fp64, _ = time_steps(asm, _abi.FS_FP64, args.steps, args.warmup, torch, stream)
@@ -744,7 +726,6 @@ def main():
                      "fp64_elements_per_s": ne3 / (ms_fp64 * 1e-3),
                      "mixed_over_fp64": ms_fp64 / ms_mixed, "nnz_per_s_mixed": nnz / (ms_mixed * 1e-3),
                      "rel_err_K_mixed_vs_fp64_max": t3["err"], "rel_err_K_mixed_vs_fp64_fro": t3["fro"],
-                     "ms_step_mixed": ms_mixed, "ms_step_mixed_kernels_one_after_the_other": sep_t3[0],
                      "ms_elements_mixed": t3["ph_mixed"][0], "ms_gather_mixed": t3["ph_mixed"][1],
                      "ms_elements_fp64": t3["ph_fp64"][0], "ms_gather_fp64": t3["ph_fp64"][1],
                      "ms_symbolic": t3["t_sym"], "e2e_ms": ms_e2e, "tiles": t3["tiles"],
@@ -754,8 +735,7 @@ def main():
                      "ms_elements_mixed_comp": t3["ph_comp"][0], "ms_gather_mixed_comp": t3["ph_comp"][1]},
             "q4rs": {"elements": ne4, "nnz": nnz_q, "mixed_elements_per_s": ne4 / (ms_q_mixed * 1e-3),
                      "fp64_elements_per_s": ne4 / (ms_q_fp64 * 1e-3), "mixed_over_fp64": ms_q_fp64 / ms_q_mixed,
-                     "rel_err_K_mixed_vs_fp64_max": err_q4, "ms_step_mixed": ms_q_mixed,
-                     "ms_step_mixed_kernels_one_after_the_other": sep_q4[0], "ms_elements_mixed": ph_q_mixed[0],
+                     "rel_err_K_mixed_vs_fp64_max": err_q4, "ms_elements_mixed": ph_q_mixed[0],
                      "ms_gather_mixed": ph_q_mixed[1], "ms_elements_fp64": ph_q_fp64[0],
                      "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4, "tiles": tiles_q,
                      "mixed_comp_elements_per_s": ne4 / (ms_q_comp * 1e-3),

@@ -56,7 +56,7 @@ static void free_pattern(PatternDev &P)
     dfree(&P.nbr_off); dfree(&P.nbr); dfree(&P.pair_slots); dfree(&P.colpos); dfree(&P.colsrc); dfree(&P.rowlen);
     dfree(&P.sl_off); dfree(&P.sl_ent);
     dfree(&P.rowptr); dfree(&P.colidx); dfree(&P.diag_rowptr); dfree(&P.diag_colidx);
-    dfree(&P.tmp_cnt); dfree(&P.tmp_owner); dfree(&P.node_perm);
+    dfree(&P.tmp_cnt); dfree(&P.tmp_owner);
     P = PatternDev();
 }
 
@@ -210,13 +210,6 @@ int fs_ctx_destroy(fs_ctx *c)
     dfree(&x.invMC); dfree(&x.C); dfree(&x.vals32); dfree(&x.U32);
     dfree(&x.blk); dfree(&x.xp); dfree(&x.pad_of_dof);
     dfree(&x.Fmag); dfree(&x.mul); dfree(&x.step);
-    dfree(&c->ov_cnt);
-    for (int k = 0; k <= fs_ctx::OV_CHUNKS; k++)
-        if (c->ov_ev[k]) cudaEventDestroy(c->ov_ev[k]);
-    if (c->gstream) {
-        cudaStreamSynchronize(c->gstream);
-        cudaStreamDestroy(c->gstream);
-    }
     cudaFree(c->d_status);
     for (int k = 0; k < 4; k++)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
@@ -395,13 +388,6 @@ int fs_normals_compute(fs_ctx *c)
     return FS_OK;
 }
 
-int fs_overlap(fs_ctx *c, int on)
-{
-    if (!c || (on != 0 && on != 1)) return FS_ERR_BAD_INPUT;
-    c->overlap = on;
-    return FS_OK;
-}
-
 int fs_normals_compute_csys(fs_ctx *c, int kind, const double *params)
 {
     if (!c) return FS_ERR_BAD_INPUT;
@@ -456,48 +442,6 @@ static int status_to_code(fs_ctx *c, int bits)
 // Pattern (built on the first call for a matrix size), element kernel, CSR
 // gather and the assembler's post-processing.  beam_which < 0: shell
 // stiffness; else the beam matrix FS_BEAM_*.
-// The element kernel in rank chunks on the context stream; after each chunk
-// the nodes it completes are gathered on a second stream, so the gather of
-// the early nodes runs while the later elements are computed.  Every value
-// is still the same sum of the same element matrices: only the order in which
-// nodes are processed changes.  Events: ev[0] start, ev[1] elements done,
-// ev[2] everything done.
-static int assemble_overlapped(fs_ctx *c, int precision)
-{
-    if (!c->gstream) {
-        FS_CUDA(c, cudaStreamCreateWithFlags(&c->gstream, cudaStreamNonBlocking));
-        for (int k = 0; k <= fs_ctx::OV_CHUNKS; k++)
-            FS_CUDA(c, cudaEventCreateWithFlags(&c->ov_ev[k], cudaEventDisableTiming));
-    }
-    FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-    FS_TRY(launch_elements(c, precision, true));  // sizes the element buffer only
-    const int k = c->ov_chunks;
-    int st = FS_OK;
-    for (int i = 0; i < k && st == FS_OK; i++) {
-        c->scope = fs_ctx::Scope();
-        c->scope.r0 = c->ov_rank_bound[i];
-        c->scope.r1 = c->ov_rank_bound[i + 1];
-        st = launch_elements(c, precision);
-        if (st != FS_OK) break;
-        st = cuda_check(c, cudaEventRecord(c->ov_ev[i], c->stream), "event");
-        if (st != FS_OK) break;
-        st = cuda_check(c, cudaStreamWaitEvent(c->gstream, c->ov_ev[i], 0), "stream wait");
-        if (st != FS_OK) break;
-        c->scope = fs_ctx::Scope();
-        c->scope.nodes = c->pat.node_perm + c->ov_node_off[i];
-        c->scope.nlist = c->ov_node_off[i + 1] - c->ov_node_off[i];
-        c->scope.stream = c->gstream;
-        st = launch_gather(c, precision, c->vals);
-    }
-    c->scope = fs_ctx::Scope();
-    FS_TRY(st);
-    FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
-    FS_CUDA(c, cudaEventRecord(c->ov_ev[fs_ctx::OV_CHUNKS], c->gstream));
-    FS_CUDA(c, cudaStreamWaitEvent(c->stream, c->ov_ev[fs_ctx::OV_CHUNKS], 0));
-    FS_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
-    return FS_OK;
-}
-
 int fs::assemble_matrix(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t *nnz_out, int beam_which,
                         int mass_type)
 {
@@ -518,15 +462,11 @@ int fs::assemble_matrix(fs_ctx *c, int precision, int assembler, int64_t nrows, 
         c->vals_cap = need;
     }
     if (beam_which < 0) FS_TRY(autotune_shell(c, precision));
-    if (beam_which < 0 && c->overlap && c->ov_chunks > 1) {
-        FS_TRY(assemble_overlapped(c, precision));
-    } else {
-        FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-        FS_TRY(beam_which < 0 ? launch_elements(c, precision) : launch_beam_elements(c, beam_which, mass_type));
-        FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
-        FS_TRY(launch_gather(c, precision, c->vals));
-        FS_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
-    }
+    FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+    FS_TRY(beam_which < 0 ? launch_elements(c, precision) : launch_beam_elements(c, beam_which, mass_type));
+    FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
+    FS_TRY(launch_gather(c, precision, c->vals));
+    FS_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
     int bits = 0;
     FS_TRY(read_status(c, &bits));
     FS_TRY(status_to_code(c, bits));

@@ -7,15 +7,14 @@ namespace fs {
 // The elements per block (the tuned tile) is a launch parameter (block size
 // / 4): every tile runs the same compiled kernel and the same arithmetic.
 template <class R, bool COMP, class S>
-__global__ void __launch_bounds__(256) k_q4_elements(const MeshDev m, const MatConst mc, S *ke, int *status,
-                                                     int64_t r0, int64_t r1)
+__global__ void __launch_bounds__(256) k_q4_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
 {
     constexpr int NR = 36, ND = 24, STRIDE = NR * ND + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int el = threadIdx.x >> 2, qp = threadIdx.x & 3;
     R *rows = reinterpret_cast<R *>(smem_raw) + el * STRIDE;
-    int64_t r = r0 + (int64_t)blockIdx.x * (blockDim.x >> 2) + el;
-    const bool active = r < r1;
+    int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 2) + el;
+    const bool active = r < m.nelem;
     ElemIn<4> in;
     double tr[4] = {0, 0, 0, 0};
     // element constants computed once per element (by its first lane) and
@@ -88,10 +87,7 @@ static int run_q4(fs_ctx *c, S *ke)
     const size_t smem = q4_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, epb);
     auto kern = k_q4_elements<R, COMP, S>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t r0 = c->scope.r0, r1 = c->scope.r1 < 0 ? c->mesh.nelem : c->scope.r1;
-    if (r1 <= r0) return FS_OK;
-    cudaStream_t st = c->scope.stream ? c->scope.stream : c->stream;
-    kern<<<nblk2(r1 - r0, epb), epb * 4, smem, st>>>(c->mesh, c->mc, ke, c->d_status, r0, r1);
+    kern<<<nblk2(c->mesh.nelem, epb), epb * 4, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
     FS_CUDA(c, cudaGetLastError());
     return FS_OK;
 }

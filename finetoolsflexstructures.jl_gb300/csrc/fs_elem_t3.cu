@@ -18,7 +18,7 @@ template <class R, bool COMP, bool AVGK> struct T3MinBlocks {
 
 template <class R, bool COMP, bool AVGK, class S>
 __global__ void __launch_bounds__(128, (T3MinBlocks<R, COMP, AVGK>::value))
-    k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status, int64_t r0, int64_t r1)
+    k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
 {
     constexpr int NR = T3Rows<AVGK>::N, NS = T3Rows<AVGK>::NS;
     constexpr int ND = 18;
@@ -28,8 +28,8 @@ __global__ void __launch_bounds__(128, (T3MinBlocks<R, COMP, AVGK>::value))
     constexpr int STRIDE = COMP ? NR * ND + 1 : CompactRows<3, NS>::SIZE + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R *rows = reinterpret_cast<R *>(smem_raw) + threadIdx.x * STRIDE;
-    int64_t r = r0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= r1) return;
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m.nelem) return;
     ElemIn<3> in;
     load_elem<3>(m, r, in);
     const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
@@ -51,10 +51,7 @@ static int run_t3(fs_ctx *c, S *ke)
     const size_t smem = t3_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, AVGK, COMP, epb);
     auto kern = k_t3_elements<R, COMP, AVGK, S>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t r0 = c->scope.r0, r1 = c->scope.r1 < 0 ? c->mesh.nelem : c->scope.r1;
-    if (r1 <= r0) return FS_OK;
-    cudaStream_t st = c->scope.stream ? c->scope.stream : c->stream;
-    kern<<<nblk2(r1 - r0, epb), epb, smem, st>>>(c->mesh, c->mc, ke, c->d_status, r0, r1);
+    kern<<<nblk2(c->mesh.nelem, epb), epb, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);
     FS_CUDA(c, cudaGetLastError());
     return FS_OK;
 }

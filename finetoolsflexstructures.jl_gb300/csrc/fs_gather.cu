@@ -109,8 +109,7 @@ template <class R, int NEN, int G_COLS, int WARPS> struct GatherMinBlocks {
 
 template <class R, int NEN, int G_COLS, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, WARPS>::value))
-    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals, const int32_t *nodes,
-             int64_t nlist)
+    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
 {
     typedef typename GatherAcc<R>::T A;
     constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
@@ -120,9 +119,8 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
     constexpr int CPL = (CH + 31) / 32;             // chunks per lane per pair
     extern __shared__ __align__(16) unsigned char gather_smem[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t i = (int64_t)blockIdx.x * WARPS + w;
-    if (i >= nlist) return;
-    const int64_t r = nodes ? nodes[i] : i;
+    int64_t r = (int64_t)blockIdx.x * WARPS + w;
+    if (r >= m.nnodes) return;
     unsigned char *wsm = gather_smem + (size_t)w * GatherSmem<R, NEN>::PER_WARP;
     R *stage = reinterpret_cast<R *>(wsm);
     uint16_t *sent = reinterpret_cast<uint16_t *>(wsm + G_MAXP * SLAB * sizeof(R));
@@ -350,10 +348,7 @@ static int gather_launch_w(fs_ctx *c, const R *ke, double *vals)
     const size_t smem = (size_t)W * GatherSmem<R, NEN>::PER_WARP;
     auto kern = k_gather<R, NEN, G_COLS, W>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t nlist = c->scope.nodes ? c->scope.nlist : m.nnodes;
-    if (nlist <= 0) return FS_OK;
-    cudaStream_t st = c->scope.stream ? c->scope.stream : c->stream;
-    kern<<<nblk2(nlist, W), W * 32, smem, st>>>(m, c->pat, c->pat.n, ke, vals, c->scope.nodes, nlist);
+    kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
     return FS_OK;
 }
 

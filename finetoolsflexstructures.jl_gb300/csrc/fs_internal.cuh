@@ -81,11 +81,10 @@ struct PatternDev {
     int32_t *diag_colidx = nullptr;  // n
     int64_t *tmp_cnt = nullptr;      // temporaries of the symbolic phase
     int32_t *tmp_owner = nullptr;
-    int32_t *node_perm = nullptr;    // nodes ordered by the element chunk that completes them
     // allocated capacities (elements): a rebuild reuses the buffers that fit
     size_t cap_nbr_off = 0, cap_nbr = 0, cap_pair_slots = 0, cap_colpos = 0, cap_colsrc = 0, cap_rowlen = 0,
            cap_sl_off = 0, cap_sl_ent = 0, cap_rowptr = 0, cap_colidx = 0, cap_diag_rowptr = 0,
-           cap_diag_colidx = 0, cap_tmp_cnt = 0, cap_tmp_owner = 0, cap_node_perm = 0;
+           cap_diag_colidx = 0, cap_tmp_cnt = 0, cap_tmp_owner = 0;
 };
 
 }  // namespace fs
@@ -163,25 +162,6 @@ struct fs_ctx {
         int64_t *step = nullptr;
         bool load = false;
     } ex;
-    // launch scope of the element and gather launchers: a range of element
-    // ranks, a list of nodes, the stream (defaults: everything, c->stream)
-    struct Scope {
-        int64_t r0 = 0, r1 = -1;          // element ranks [r0, r1); r1 < 0: all
-        const int32_t *nodes = nullptr;   // nodes to gather (null: all)
-        int64_t nlist = -1;
-        cudaStream_t stream = nullptr;    // null: the context stream
-    } scope;
-    // overlap of the element kernel with the gather: the elements in rank
-    // chunks, the nodes whose elements all lie in the chunks done so far
-    // gathered on a second stream meanwhile (0 off, 1 on)
-    int overlap = 1;
-    static const int OV_CHUNKS = 8;
-    cudaStream_t gstream = nullptr;
-    cudaEvent_t ov_ev[OV_CHUNKS + 1] = {};
-    int64_t ov_node_off[OV_CHUNKS + 1] = {};  // chunk c's nodes: node_perm[off[c], off[c+1])
-    int64_t ov_rank_bound[OV_CHUNKS + 1] = {};
-    int ov_chunks = 0;                        // 0: no chunking for the current pattern
-    int64_t *ov_cnt = nullptr;                // device counts / cursors (2 x (OV_CHUNKS + 1))
     // tile shapes of the shell element kernel and of the gather (0: defaults)
     struct Tune {
         int mode = -1;         // -1: not read yet (FLEXSHELL_AUTOTUNE), 0 off, 1 on, 2 re-tune
@@ -219,7 +199,7 @@ int launch_prepare_dofs(fs_ctx *c, const int64_t *d_dof_raw);
 int build_adjacency(fs_ctx *c);
 int build_pattern(fs_ctx *c, int64_t n);
 int launch_normals(fs_ctx *c, int kind = FS_CSYS_ISOPARAMETRIC, const double *prm = nullptr);
-int launch_elements(fs_ctx *c, int precision, bool size_only = false);
+int launch_elements(fs_ctx *c, int precision);
 int launch_gather(fs_ctx *c, int precision, double *vals);
 int launch_elements_to(fs_ctx *c, int precision, void *ke);
 int launch_gather_from(fs_ctx *c, int precision, const void *ke, double *vals);

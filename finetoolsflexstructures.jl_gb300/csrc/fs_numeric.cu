@@ -44,7 +44,7 @@ static int run_elements(fs_ctx *c, int precision, void *ke)
 // bytes of one stored element-matrix entry
 size_t entry_bytes(int precision) { return precision == FS_MIXED ? 4 : 8; }
 
-int launch_elements(fs_ctx *c, int precision, bool size_only)
+int launch_elements(fs_ctx *c, int precision)
 {
     MeshDev &m = c->mesh;
     size_t bytes = (size_t)m.nelem * n_upper_blocks(m.nen) * 36 * entry_bytes(precision);
@@ -59,7 +59,7 @@ int launch_elements(fs_ctx *c, int precision, bool size_only)
         }
         c->ke_bytes = bytes;
     }
-    if (m.nelem == 0 || size_only) return FS_OK;
+    if (m.nelem == 0) return FS_OK;
     return run_elements(c, precision, c->ke);
 }
 

@@ -486,67 +486,6 @@ __global__ void k_diag_pattern(int64_t n, int64_t *rowptr, int32_t *colidx)
     if (i < n) colidx[i] = (int32_t)i;
 }
 
-// Element-rank chunks of the overlapped assembly: the chunk that completes a
-// node is the chunk of its last element (its pairs are sorted by rank);
-// nodes without elements go with chunk 0.
-struct ChunkBounds {
-    int64_t b[fs_ctx::OV_CHUNKS + 1];
-    int k;
-};
-
-__global__ void k_node_chunk(int64_t nnodes, const int64_t *pp, const int32_t *pair_e, const ChunkBounds cb,
-                             int32_t *chunk_of, int64_t *cnt)
-{
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nnodes) return;
-    int ch = 0;
-    if (pp[r + 1] > pp[r]) {
-        const int64_t last = pair_e[pp[r + 1] - 1] >> 2;
-        while (ch + 1 < cb.k && cb.b[ch + 1] <= last) ch++;
-    }
-    chunk_of[r] = ch;
-    atomicAdd(reinterpret_cast<unsigned long long *>(&cnt[ch]), 1ull);
-}
-
-__global__ void k_node_place(int64_t nnodes, const int32_t *chunk_of, int64_t *cursor, int32_t *node_perm)
-{
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nnodes) return;
-    const unsigned long long pos = atomicAdd(reinterpret_cast<unsigned long long *>(&cursor[chunk_of[r]]), 1ull);
-    node_perm[pos] = (int32_t)r;
-}
-
-// chunks for meshes of at least 2 x 32768 elements (at most OV_CHUNKS)
-static int build_chunks(fs_ctx *c)
-{
-    const MeshDev &m = c->mesh;
-    PatternDev &P = c->pat;
-    const int64_t nn = m.nnodes;
-    int k = (int)std::min<int64_t>(fs_ctx::OV_CHUNKS, m.nelem / 32768);
-    c->ov_chunks = 0;
-    if (k < 2 || nn == 0) return FS_OK;
-    ChunkBounds cb{};
-    cb.k = k;
-    for (int i = 0; i <= k; i++) cb.b[i] = m.nelem * i / k;
-    if (!c->ov_cnt) FS_TRY(dalloc(c, &c->ov_cnt, 2 * (fs_ctx::OV_CHUNKS + 1)));
-    FS_TRY(grow(c, &P.node_perm, &P.cap_node_perm, (size_t)nn));
-    int32_t *chunk_of = reinterpret_cast<int32_t *>(P.tmp_cnt);  // free after the row-pointer scan
-    FS_CUDA(c, cudaMemsetAsync(c->ov_cnt, 0, sizeof(int64_t) * (fs_ctx::OV_CHUNKS + 1), c->stream));
-    k_node_chunk<<<nblk(nn, 256), 256, 0, c->stream>>>(nn, m.pp, m.pair_e, cb, chunk_of, c->ov_cnt);
-    int64_t h[fs_ctx::OV_CHUNKS + 1];
-    FS_CUDA(c, cudaMemcpyAsync(h, c->ov_cnt, sizeof(int64_t) * k, cudaMemcpyDeviceToHost, c->stream));
-    FS_CUDA(c, cudaStreamSynchronize(c->stream));
-    c->ov_node_off[0] = 0;
-    for (int i = 0; i < k; i++) c->ov_node_off[i + 1] = c->ov_node_off[i] + h[i];
-    int64_t *cursor = c->ov_cnt + fs_ctx::OV_CHUNKS + 1;
-    FS_CUDA(c, cudaMemcpyAsync(cursor, c->ov_node_off, sizeof(int64_t) * k, cudaMemcpyHostToDevice, c->stream));
-    k_node_place<<<nblk(nn, 256), 256, 0, c->stream>>>(nn, chunk_of, cursor, P.node_perm);
-    FS_CUDA(c, cudaGetLastError());
-    for (int i = 0; i <= k; i++) c->ov_rank_bound[i] = cb.b[i];
-    c->ov_chunks = k;
-    return FS_OK;
-}
-
 int build_pattern(fs_ctx *c, int64_t n)
 {
     MeshDev &m = c->mesh;
@@ -605,7 +544,6 @@ int build_pattern(fs_ctx *c, int64_t n)
     FS_TRY(grow(c, &P.diag_colidx, &P.cap_diag_colidx, (size_t)n));
     k_diag_pattern<<<nblk(n + 1, 256), 256, 0, c->stream>>>(n, P.diag_rowptr, P.diag_colidx);
     FS_CUDA(c, cudaGetLastError());
-    FS_TRY(build_chunks(c));
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
     P.n = n;
     P.nnz = nnz;

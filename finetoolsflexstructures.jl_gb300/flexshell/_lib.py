@@ -68,7 +68,6 @@ def lib():
         L.fs_pattern.argtypes = [vp, ctypes.c_int64, _c_i64_p]
         L.fs_stiffness_copy.argtypes = [vp, ctypes.c_int, ctypes.c_int64, vp, vp, vp]
         L.fs_autotune.argtypes = [vp, ctypes.c_int]
-        L.fs_overlap.argtypes = [vp, ctypes.c_int]
         L.fs_tuning.argtypes = [vp, vp]
         L.fs_batch_set.argtypes = [vp, ctypes.c_int, ctypes.c_int32, vp, vp, vp, vp, vp, vp, vp]
         L.fs_batch_stiffness.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]

@@ -182,13 +182,6 @@ int fs_timings(const fs_ctx *ctx, double *out, int n);
  * context's mesh and the choice is reused by the whole process; 0: built-in
  * shapes; 2: re-tune on the next call.  Tile shapes never change the results. */
 int fs_autotune(fs_ctx *ctx, int mode);
-/* Overlap of the element kernel with the gather (on = 1, the default): the
- * elements run in rank chunks and the nodes each chunk completes are
- * gathered on a second stream while the next chunks run (meshes of at least
- * 65,536 elements).  Off (0): one element launch, then one gather launch, so
- * that fs_timings reports each kernel alone.  The matrix is the same either
- * way (every value is the same sum in the same order). */
-int fs_overlap(fs_ctx *ctx, int on);
 /* Shapes used by the last fs_stiffness: out[0] elements per block (0 =
  * default), out[1] gather warps per block (0 = default), out[2] 1 if tuned. */
 int fs_tuning(const fs_ctx *ctx, int32_t *out);

@@ -410,31 +410,6 @@ def test_autotuner_choice_never_changes_the_matrix(quads):
     femm.close()
 
 
-@pytest.mark.parametrize("quads", [False, True])
-def test_overlap_never_changes_the_matrix(quads):
-    # meshes above 65,536 elements assemble with the element kernel in rank
-    # chunks and the completed nodes gathered meanwhile on a second stream:
-    # bitwise the same matrix as one element launch followed by one gather
-    mat = F.materials.MatDeforElastIso(2.0e11, 0.3, 7850.0)
-    xyz, conn, dof, nfree = PB.jittered_plate(300, quads, wavy=0.02, seed=3)
-    assert conn.shape[0] >= 2 * 32768
-    geom0 = F.NodalField(xyz)
-    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
-    dchi.dofnums = np.asfortranarray(dof)
-    cls = F.FEMMShellQ4RS if quads else F.FEMMShellT3FF
-    femm = cls(conn, 0.01, mat)
-    femm.associategeometry(geom0)
-    for prec in (F.FS_MIXED, F.FS_FP64, F.FS_MIXED_COMP):
-        femm.ctx.call("fs_overlap", 1)
-        K1 = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi, precision=prec)
-        femm.ctx.call("fs_overlap", 0)
-        K0 = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi, precision=prec)
-        assert np.array_equal(K0.indptr, K1.indptr) and np.array_equal(K0.indices, K1.indices)
-        assert np.array_equal(K0.data, K1.data)
-    femm.ctx.call("fs_overlap", 1)
-    femm.close()
-
-
 def test_composite_eigenvalues_mixed_vs_fp64():
     # layered Q4RS plate (scaled-down layered-plate configuration): the 20
     # lowest eigenvalues from the FP64 K match the oracle's to 1e-10, those of
