@@ -158,9 +158,16 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             const int j = lane + 32 * c;
             cs_l[c] = j < L ? (int)P.colsrc[off6 + j] : 0;
         }
-        // the node's contribution entries into shared memory
+        // the node's contribution entries into shared memory; when all the
+        // node's pairs fit one staging batch (the usual case) each entry is
+        // stored decoded: its slab offset q SLAB + b 36, mirrored flag in bit 15
+        const bool one_batch = pe - pb <= G_MAXP;
         const uint16_t *ent = P.sl_ent + pb * NEN;
-        for (int i = lane; i < ntot; i += 32) sent[i] = ent[i];
+        for (int i = lane; i < ntot; i += 32) {
+            const uint32_t e = ent[i];
+            sent[i] = one_batch ? (uint16_t)((e & 63u) * SLAB + ((e >> 6) & 3u) * 36 | ((e >> 8) & 1u) << 15)
+                                : (uint16_t)e;
+        }
         // the lane's columns and the range of entries of their neighbour slot
         int kcol[G_COLS], cur[G_COLS], beg[G_COLS], last[G_COLS];
         A hi[G_COLS][6], lo[G_COLS][6];
@@ -190,16 +197,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             cb[t] = ch / BCH;
             cwd[t] = ch - cb[t] * BCH;
         }
-        // entry (krow = 0, kcol) of block (a_q, b) of staged pair q; a mirrored
-        // block is read transposed: the six rows are st apart
-        auto slab_entry = [&](uint32_t e, int kc, int q0, int &st) -> const R * {
-            const int q = (int)(e & 63u) - q0;
-            const int b = (int)((e >> 6) & 3u);
-            const bool tr = (e >> 8) & 1u;
-            st = tr ? 1 : 6;
-            return stage + q * SLAB + b * 36 + (tr ? 6 * kc : kc);
-        };
-        if (pe - pb <= G_MAXP) {
+        if (one_batch) {
             // all pairs of the node in one batch (the usual case): every
             // contribution is staged, each sum runs over its whole list
             const int cnt = (int)(pe - pb);
@@ -224,12 +222,19 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
                 int e = cur[c];
                 const int e1 = last[c];
                 if (e < e1) {
-                    int st;
-                    const R *src = slab_entry(sent[e], kcol[c], 0, st);
+                    // decoded entry: slab offset, mirrored blocks read transposed
+                    const int kc = kcol[c], kc6 = 6 * kcol[c];
+                    uint32_t d = sent[e];
+                    bool tr = d >> 15;
+                    const R *src = stage + (d & 0x7fffu) + (tr ? kc6 : kc);
+                    int st = tr ? 1 : 6;
 #pragma unroll
                     for (int k = 0; k < 6; k++) gather_set(hi[c][k], lo[c][k], src[st * k]);
                     for (e++; e < e1; e++) {
-                        src = slab_entry(sent[e], kcol[c], 0, st);
+                        d = sent[e];
+                        tr = d >> 15;
+                        src = stage + (d & 0x7fffu) + (tr ? kc6 : kc);
+                        st = tr ? 1 : 6;
 #pragma unroll
                         for (int k = 0; k < 6; k++) gather_add(hi[c][k], lo[c][k], src[st * k]);
                     }
