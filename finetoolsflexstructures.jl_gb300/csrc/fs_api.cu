@@ -72,7 +72,7 @@ static void reset_pattern(PatternDev &P)
 static void free_mesh(MeshDev &m)
 {
     dfree(&m.xyz); dfree(&m.conn); dfree(&m.elem_of_rank); dfree(&m.dof); dfree(&m.thick);
-    dfree(&m.group); dfree(&m.groups); dfree(&m.normals); dfree(&m.valid); dfree(&m.pp);
+    dfree(&m.group); dfree(&m.groups); dfree(&m.normals); dfree(&m.normals_f); dfree(&m.valid); dfree(&m.pp);
     dfree(&m.pair_e); dfree(&m.elem_pair);
     m = MeshDev();
 }
@@ -269,6 +269,7 @@ int fs_mesh_set(fs_ctx *c, int elem_type, int64_t nnodes, const double *xyz, int
     FS_TRY(dalloc(c, &m.elem_of_rank, (size_t)nelem));
     FS_TRY(dalloc(c, &m.dof, (size_t)(6 * nnodes)));
     FS_TRY(dalloc(c, &m.normals, (size_t)(3 * nnodes)));
+    FS_TRY(dalloc(c, &m.normals_f, (size_t)(3 * nnodes)));
     FS_TRY(dalloc(c, &m.valid, (size_t)nnodes));
     // raw uploads share one staging allocation
     size_t nconn = (size_t)(nelem * m.nen), nord = order ? (size_t)nelem : 0;
@@ -411,6 +412,7 @@ int fs_normals_set(fs_ctx *c, const double *normals, const uint8_t *valid)
     if (c->mesh.etype < 0) return set_err(c, FS_ERR_STATE, "no mesh: call fs_mesh_set first");
     int64_t nn = c->mesh.nnodes;
     FS_CUDA(c, cudaMemcpyAsync(c->mesh.normals, normals, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, c->stream));
+    FS_TRY(round_normals(c));
     FS_CUDA(c, cudaMemcpyAsync(c->mesh.valid, valid, nn, cudaMemcpyHostToDevice, c->stream));
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
     c->normals_ready = true;

@@ -17,6 +17,7 @@ __device__ __forceinline__ void load_elem(const MeshDev &m, int64_t r, ElemIn<NN
         for (int c = 0; c < 3; c++) {
             in.X[a][c] = m.xyz[(int64_t)c * m.nnodes + node];
             in.nrm[a][c] = m.normals[(int64_t)c * m.nnodes + node];
+            in.nrmf[a][c] = m.normals_f[(int64_t)c * m.nnodes + node];
         }
         in.valid[a] = m.valid[node] != 0;
     }

@@ -150,6 +150,39 @@ FS_HD void sinc_cosc_f(float x, float &s, float &c)
 // once; the Rodrigues entries are evaluated from it in float, each within
 // about one float ulp of the rounded double entry.  Angles beyond one radian
 // (creases) take the double path.
+// The triad of the float rows from the element frame and the nodal normal,
+// both rounded to float: the rotation vector, the Rodrigues entries in float
+// (angles beyond one radian evaluate sin and cos in double).  The rounding of
+// the frame and the normal perturbs the rows like the rounding of the rows
+// themselves (it keeps K a Gram matrix).
+FS_HD void nodal_triad_f(const float e[3][3], const float n[3], bool valid, float Ar[3][3])
+{
+    float a0 = 0.0f, a1 = 0.0f;
+    if (valid) {
+        a0 = -dot3(e[1], n);
+        a1 = dot3(e[0], n);
+    }
+    const float x = a0 * a0 + a1 * a1;
+    if (!(x > 1.0e-24f)) {
+        for (int r = 0; r < 3; r++)
+            for (int k = 0; k < 3; k++) Ar[r][k] = r == k ? 1.0f : 0.0f;
+        return;
+    }
+    float s, c;
+    if (x > 1.0f) {
+        double sd, cd;
+        sinc_cosc((double)x, sd, cd);
+        s = (float)sd;
+        c = (float)cd;
+    } else {
+        sinc_cosc_f(x, s, c);
+    }
+    const float ca0 = c * a0, ca1 = c * a1;
+    Ar[0][0] = 1.0f - ca1 * a1; Ar[0][1] = ca0 * a1;       Ar[0][2] = s * a1;
+    Ar[1][0] = ca0 * a1;        Ar[1][1] = 1.0f - ca0 * a0; Ar[1][2] = -(s * a0);
+    Ar[2][0] = -(s * a1);       Ar[2][1] = s * a0;          Ar[2][2] = 1.0f - c * x;
+}
+
 template <class R>
 FS_HD void nodal_triad_r(const double e[3][3], const double n[3], bool valid, R Ar[3][3])
 {
@@ -207,8 +240,8 @@ template <class R, int NN> struct GlobalMap {
 
 // Build the map from the double-precision frame and the triads (rounded to
 // R; the products below are transformation arithmetic in the working precision).
-template <class R, int NN>
-FS_HD void build_map(const double e[3][3], const R A[NN][3][3], const R g[NN][2], GlobalMap<R, NN> &M)
+template <class R, int NN, class E>
+FS_HD void build_map(const E e[3][3], const R A[NN][3][3], const R g[NN][2], GlobalMap<R, NN> &M)
 {
     for (int k = 0; k < 3; k++)
         for (int c = 0; c < 3; c++) M.e[k][c] = (R)e[k][c];
@@ -460,6 +493,7 @@ FS_HD void rotate2(double m, double n, R rows[2][NN][5])
 template <int NN> struct ElemIn {
     double X[NN][3];     // node coordinates
     double nrm[NN][3];   // nodal normals
+    float nrmf[NN][3];   // the same rounded to float (the float rows' triads)
     bool valid[NN];      // normal valid flags
     double t;            // thickness
     int group;           // layup group (composite)
@@ -538,9 +572,17 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
     }
     // --- triads ---
     R A[3][3][3];
-    for (int i = 0; i < 3; i++) nodal_triad_r<R>(e, in.nrm[i], in.valid[i], A[i]);
     GlobalMap<R, 3> M;
-    build_map<R, 3>(e, A, g, M);
+    if constexpr (sizeof(R) == 4) {
+        float ef[3][3];
+        for (int k = 0; k < 3; k++)
+            for (int c = 0; c < 3; c++) ef[k][c] = (float)e[k][c];
+        for (int i = 0; i < 3; i++) nodal_triad_f(ef, in.nrmf[i], in.valid[i], A[i]);
+        build_map<R, 3>(ef, A, g, M);
+    } else {
+        for (int i = 0; i < 3; i++) nodal_triad_r<R>(e, in.nrm[i], in.valid[i], A[i]);
+        build_map<R, 3>(e, A, g, M);
+    }
 
     constexpr int NS = T3Rows<AVGK>::NS;
     // --- transverse shear rows in the element frame (w, thx, thy per node) ---
@@ -822,9 +864,17 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         g[a][1] = pj0[1] * t1 + pj1[1] * t2;
     }
     R A[4][3][3];
-    for (int i = 0; i < 4; i++) nodal_triad_r<R>(e, in.nrm[i], in.valid[i], A[i]);
     GlobalMap<R, 4> M;
-    build_map<R, 4>(e, A, g, M);
+    if constexpr (sizeof(R) == 4) {
+        float ef[3][3];
+        for (int k = 0; k < 3; k++)
+            for (int c = 0; c < 3; c++) ef[k][c] = (float)e[k][c];
+        for (int i = 0; i < 4; i++) nodal_triad_f(ef, in.nrmf[i], in.valid[i], A[i]);
+        build_map<R, 4>(ef, A, g, M);
+    } else {
+        for (int i = 0; i < 4; i++) nodal_triad_r<R>(e, in.nrm[i], in.valid[i], A[i]);
+        build_map<R, 4>(e, A, g, M);
+    }
     R sh[2][4][5];
     q4_bs<R>(X, Y, xir, etar, sh);
     const R stab = (R)qe.stab;

@@ -50,6 +50,7 @@ struct MeshDev {
     GroupConst *groups = nullptr;
     int ngroups = 0;
     double *normals = nullptr;   // 3 x nnodes
+    float *normals_f = nullptr;  // the same rounded to float (the float rows' triads)
     uint8_t *valid = nullptr;
     // node -> (element rank, local node) adjacency, ascending rank
     int64_t npairs = 0;
@@ -199,6 +200,7 @@ int launch_prepare_dofs(fs_ctx *c, const int64_t *d_dof_raw);
 int build_adjacency(fs_ctx *c);
 int build_pattern(fs_ctx *c, int64_t n);
 int launch_normals(fs_ctx *c, int kind = FS_CSYS_ISOPARAMETRIC, const double *prm = nullptr);
+int round_normals(fs_ctx *c);
 int launch_elements(fs_ctx *c, int precision);
 int launch_gather(fs_ctx *c, int precision, double *vals);
 int launch_elements_to(fs_ctx *c, int precision, void *ke);

@@ -175,6 +175,22 @@ __global__ void k_normals(const MeshDev m, bool comp, double cos_thr, const Csys
     valid[r] = ok ? 1 : 0;
 }
 
+__global__ void k_round_normals(int64_t n, const double *src, float *dst)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
+}
+
+// the float copy of the normals read by the float rows' triads
+int round_normals(fs_ctx *c)
+{
+    const MeshDev &m = c->mesh;
+    if (m.nnodes == 0) return FS_OK;
+    k_round_normals<<<nblk2(3 * m.nnodes, 256), 256, 0, c->stream>>>(3 * m.nnodes, m.normals, m.normals_f);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
 int launch_normals(fs_ctx *c, int kind, const double *prm)
 {
     MeshDev &m = c->mesh;
@@ -192,7 +208,7 @@ int launch_normals(fs_ctx *c, int kind, const double *prm)
     else
         k_normals<4><<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, comp, cos_thr, cs, m.normals, m.valid);
     FS_CUDA(c, cudaGetLastError());
-    return FS_OK;
+    return round_normals(c);
 }
 
 // ---------------------------------------------------------------------------

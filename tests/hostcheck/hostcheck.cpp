@@ -42,6 +42,7 @@ static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t n
                 for (int c = 0; c < 3; c++) {
                     in.X[a][c] = xyz[node + c * nnodes];
                     in.nrm[a][c] = normals[node + c * nnodes];
+                    in.nrmf[a][c] = (float)in.nrm[a][c];
                 }
                 in.valid[a] = valid[node] != 0;
             }
@@ -62,6 +63,7 @@ static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t n
                 for (int c = 0; c < 3; c++) {
                     in.X[a][c] = xyz[node + c * nnodes];
                     in.nrm[a][c] = normals[node + c * nnodes];
+                    in.nrmf[a][c] = (float)in.nrm[a][c];
                 }
                 in.valid[a] = valid[node] != 0;
             }
@@ -133,6 +135,7 @@ extern "C" int hc_resultants(int etype, int64_t nnodes, const double *xyz, int64
                 for (int c = 0; c < 3; c++) {
                     in.X[a][c] = xyz[node + c * nnodes];
                     in.nrm[a][c] = normals[node + c * nnodes];
+                    in.nrmf[a][c] = (float)in.nrm[a][c];
                 }
                 in.valid[a] = valid[node] != 0;
             }
@@ -145,6 +148,7 @@ extern "C" int hc_resultants(int etype, int64_t nnodes, const double *xyz, int64
                 for (int c = 0; c < 3; c++) {
                     in.X[a][c] = xyz[node + c * nnodes];
                     in.nrm[a][c] = normals[node + c * nnodes];
+                    in.nrmf[a][c] = (float)in.nrm[a][c];
                 }
                 in.valid[a] = valid[node] != 0;
             }
