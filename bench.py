@@ -586,8 +586,20 @@ def main():
     xyz, conn, dof = plate(args.n, False)
     asm = Assembler(xyz, conn, dof, False, device=local)
     stream = torch.cuda.ExternalStream(asm.ctx.stream())
-    asm.stiffness(_abi.FS_MIXED)  # builds the pattern
+    nnz0 = asm.stiffness(_abi.FS_MIXED)  # builds the pattern
     t_sym = asm.timings()[2]
+    # page-locked host arrays of the end-to-end leg, allocated before the large
+    # host copies of the precision checks below: freshly allocated, while the
+    # host is still returning those pages, they copied 20 % slower
+    nn = xyz.shape[0]
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    h_xyz = pin((3 * nn,), torch.float64)
+    h_xyz[:] = xyz.flatten(order="F")
+    h_dof = pin((6 * nn,), torch.int64)
+    h_dof[:] = dof.flatten(order="F")
+    h_colptr = pin((asm.n + 1,), torch.int64)
+    h_rowval = pin((nnz0,), torch.int64)
+    h_nzval = pin((nnz0,), torch.float64)
     if world > 1:
         dist.barrier()
     clocks = Clocks(local)
@@ -612,15 +624,6 @@ def main():
                      tiles={"mixed": tiles_mixed, "fp64": tiles_fp64})
 
     # --- e2e through the C ABI from pinned host buffers (T3FF, mixed) ------------
-    nn = xyz.shape[0]
-    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
-    h_xyz = pin((3 * nn,), torch.float64)
-    h_xyz[:] = xyz.flatten(order="F")
-    h_dof = pin((6 * nn,), torch.int64)
-    h_dof[:] = dof.flatten(order="F")
-    h_colptr = pin((asm.n + 1,), torch.int64)
-    h_rowval = pin((nnz,), torch.int64)
-    h_nzval = pin((nnz,), torch.float64)
     P = asm.ptr
 
     def e2e_step():
