@@ -124,6 +124,14 @@ __global__ void k_vec_gather(const MeshDev m, int64_t n, const double *fe, doubl
     }
 }
 
+int launch_vec_gather(fs_ctx *c, int64_t n, const double *fe, double *F)
+{
+    const MeshDev &m = c->mesh;
+    if (m.nnodes) k_vec_gather<<<nblk_b(m.nnodes, 128), 128, 0, c->stream>>>(m, n, fe, F);
+    FS_CUDA(c, cudaGetLastError());
+    return FS_OK;
+}
+
 static BeamDev beam_dev(fs_ctx *c)
 {
     BeamDev b;
@@ -183,8 +191,7 @@ int launch_beam_vector(fs_ctx *c, int which, int64_t n, double *F)
     }
     if (F) {
         if (n > 0) FS_CUDA(c, cudaMemsetAsync(F, 0, sizeof(double) * n, c->stream));
-        if (m.nnodes) k_vec_gather<<<nblk_b(m.nnodes, 128), 128, 0, c->stream>>>(m, n, c->beam.fe, F);
-        FS_CUDA(c, cudaGetLastError());
+        FS_TRY(launch_vec_gather(c, n, c->beam.fe, F));
     }
     return FS_OK;
 }

@@ -227,6 +227,8 @@ size_t q4_smem(int precision, int epb);
 // co-rotational beams
 int launch_beam_elements(fs_ctx *c, int which, int mass_type);
 int launch_beam_vector(fs_ctx *c, int which, int64_t n, double *F);
+// per-node sums (ascending assembly rank) of element vectors fe (6 nen per rank) into F[0, n)
+int launch_vec_gather(fs_ctx *c, int64_t n, const double *fe, double *F);
 void free_beam(fs_ctx *c);
 // pattern + element kernel + gather + assembler post-processing shared by the
 // shells (beam_which < 0) and the beams

@@ -15,4 +15,6 @@ from .femm import (CSysCartesian, CSysCylindrical, CSysSpherical,
                    SysmatAssemblerSparseSymm, ShellBatch)
 from .beam import FEMMCorotBeam
 from .explicit import CentralDifference, cd_loop
+from .loads import (FEMMBase, ForceIntensity, GaussRule, IntegDomain, SysvecAssembler,
+                    SysvecAssemblerFBlock, TriRule, distribloads)
 from ._lib import Context, FlexShellError, laminate

@@ -64,6 +64,8 @@ def lib():
                                   ctypes.c_double, ctypes.POINTER(_abi.fs_layup_group)]
         L.fs_restoring_force.argtypes = [vp, vp, vp]
         L.fs_resultants.argtypes = [vp, ctypes.c_int, vp, vp, ctypes.c_int64, vp]
+        L.fs_distribloads.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int64, ctypes.c_int64, vp]
+        L.fs_integration_points.argtypes = [vp, ctypes.c_int, vp]
         L.fs_normals_compute_csys.argtypes = [vp, ctypes.c_int, vp]
         L.fs_pattern.argtypes = [vp, ctypes.c_int64, _c_i64_p]
         L.fs_stiffness_copy.argtypes = [vp, ctypes.c_int, ctypes.c_int64, vp, vp, vp]

@@ -20,6 +20,10 @@ for FEMMShellT3FF and FEMMShellQ4RS, and for FEMMCorotBeam
     restoringforce(femm, assembler, geom0, u1, Rfield1, dchi)
     distribloads_global(femm, assembler, geom0, u1, Rfield1, dchi, fi)
 
+and, for the distributed loads on a shell element set,
+
+    gpu_distribloads(femm::FEMMBase, assembler, geom, P, fi, m)
+
 `associategeometry!` stays the reference's own; its normals are passed in.
 Not exercised in this repository (no Julia toolchain here); it is the
 binding a maintainer adds next to the reference.
@@ -295,6 +299,42 @@ function distribloads_global(self::FEMMCorotBeam, assembler::AbstractSysvecAssem
     F = zeros(nalldofs(dchi))
     check(ctx, ccall((:fs_beam_distribloads_global, libflexshell), Cint,
         (Ptr{Cvoid}, Ptr{Float64}, Cint, Int64, Ptr{Float64}), ctx.h, q, 0, length(F), F))
+    return F
+end
+
+# distributed surface loads of a shell element set: distribloads(femm::FEMMBase,
+# assembler, geom, P, fi, m) of FinEtools on a T3 or Q4 set with TriRule(1, 3,
+# 6) or GaussRule(2, 1..3); fi is evaluated on the host at the points
+# fs_integration_points returns (updateforce!, as FinEtools does point by
+# point), the element loop and the node sums run on the GPU.  A separate name:
+# FEMMBase is FinEtools' own type.
+function gpu_distribloads(self::FEMMBase, assembler::AbstractSysvecAssembler, geom::NodalField{Float64},
+    P::NodalField{TI}, fi::ForceIntensity, m::Int) where {TI}
+    ctx = context(self)
+    fes = self.integdomain.fes
+    nen = nodesperelem(fes)
+    ir = self.integdomain.integration_rule
+    rule = nen == 3 ? ir.npts : ir.order
+    conn = collect(reinterpret(Int, fes.conn))
+    xyz = geom.values
+    check(ctx, ccall((:fs_mesh_set, libflexshell), Cint,
+        (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
+        ctx.h, nen == 3 ? FS_T3FF : FS_Q4RS, size(xyz, 1), xyz, count(fes), conn, C_NULL, P.dofnums))
+    npts = nen == 3 ? rule : rule^2
+    pts = zeros(9, count(fes) * npts)
+    check(ctx, ccall((:fs_integration_points, libflexshell), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}),
+        ctx.h, rule, pts))
+    force = zeros(6, size(pts, 2))
+    for k in 1:size(pts, 2)
+        e, j = divrem(k - 1, npts)
+        force[:, k] .= updateforce!(fi, reshape(pts[1:3, k], 1, 3), reshape(pts[4:9, k], 3, 2),
+            fes.label[e + 1], j + 1)[1:6]
+    end
+    n = assembler isa SysvecAssemblerFBlock ? nfreedofs(P) : nalldofs(P)
+    F = zeros(n)
+    check(ctx, ccall((:fs_distribloads, libflexshell), Cint,
+        (Ptr{Cvoid}, Cint, Cint, Ptr{Float64}, Int64, Int64, Ptr{Float64}),
+        ctx.h, rule, m, force, size(force, 2), n, F))
     return F
 end
 

@@ -329,6 +329,25 @@ int fs_restoring_force(fs_ctx *ctx, const double *U, double *F);
 #define FS_RES_MEMBRANE 3
 int fs_resultants(fs_ctx *ctx, int quantity, const double *u, const double *csmat, int64_t ncs, double *out);
 
+/* Distributed surface loads on the shell mesh: distribloads(FEMMBase(
+ * IntegDomain(fes, rule)), geom0, dchi, fi, m) of FinEtools 8.2.5, as the
+ * reference calls it on its shell element sets
+ * (examples/shells/dynamics/homogeneous/explicit/plate_expl_examples.jl:196-199,
+ * test/test_shell_statics.jl:84-86).  rule: T3 meshes TriRule(npts), npts 1,
+ * 3 or 6; Q4 meshes GaussRule(2, order), order 1, 2 or 3.  m: 2 or 3 (the
+ * element's other dimension is 1).  force: the ForceIntensity's six
+ * components, nforce = 1 (uniform), nelem (one per element, element order) or
+ * nelem x npoints (one per integration point, the points of
+ * fs_integration_points).  F: nrows entries (nalldofs, or nfreedofs for
+ * SysvecAssemblerFBlock), dofs above nrows dropped.  No parameters needed. */
+int fs_distribloads(fs_ctx *ctx, int rule, int m, const double *force, int64_t nforce, int64_t nrows, double *F);
+
+/* The integration points of the same rules, element order, nine doubles per
+ * point: the location and the two parent tangents x,xi and x,eta (the
+ * arguments the reference's ForceIntensity callback receives as XYZ and
+ * tangents). */
+int fs_integration_points(fs_ctx *ctx, int rule, double *out);
+
 /* --- layup reduction (src/CompositeLayupModule.jl:246-330) ------------------ */
 /* ply_Dps: nplies x 9, ply_Dts: nplies x 4 (column-major each); angles in degrees;
  * shear_model 0 = Vinson-Sierakowski, 1 = constant `tcf`. Host only. */

@@ -1443,3 +1443,167 @@ int orc_resultants(int64_t nnodes, const double *xyz, int64_t nelem, const int64
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* distributed surface loads: FinEtools 8.2.5 distribloads(FEMMBase,   */
+/* geom, P, fi::ForceIntensity, m) on the shell element sets           */
+/* (plate_expl_examples.jl:196-199, test/test_shell_statics.jl:84-86)  */
+/* ------------------------------------------------------------------ */
+
+/* integration rule on the parent element: TriRule(npts) for triangles
+ * (1: centroid; 3: the degree-2 interior points; 6: Dunavant's degree-4
+ * rule, orbits (1-2a, a) and permutations), GaussRule(2, order) for
+ * quadrilaterals (xi the outer index); param (npts x 2), weights */
+static int surface_rule(int nen, int rule, double *pc, double *w)
+{
+    if (nen == 3) {
+        if (rule == 1) {
+            pc[0] = pc[1] = 1.0 / 3.0;
+            w[0] = 0.5;
+            return 1;
+        }
+        if (rule == 3) {
+            const double P[3][2] = {{2.0 / 3.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}, {1.0 / 6.0, 1.0 / 6.0}};
+            for (int j = 0; j < 3; j++) {
+                pc[2 * j] = P[j][0];
+                pc[2 * j + 1] = P[j][1];
+                w[j] = 1.0 / 6.0;
+            }
+            return 3;
+        }
+        if (rule == 6) {
+            const double a[2] = {0.445948490915965, 0.091576213509771};
+            const double wt[2] = {0.223381589678011, 0.109951743655322};
+            for (int o = 0; o < 2; o++) {
+                const double b = 1.0 - 2.0 * a[o];
+                const double P[3][2] = {{b, a[o]}, {a[o], b}, {a[o], a[o]}};
+                for (int j = 0; j < 3; j++) {
+                    pc[2 * (3 * o + j)] = P[j][0];
+                    pc[2 * (3 * o + j) + 1] = P[j][1];
+                    w[3 * o + j] = wt[o] / 2.0;
+                }
+            }
+            return 6;
+        }
+        return 0;
+    }
+    double g[3], gw[3];
+    if (rule == 1) {
+        g[0] = 0.0;
+        gw[0] = 2.0;
+    } else if (rule == 2) {
+        g[0] = -1.0 / sqrt(3.0);
+        g[1] = 1.0 / sqrt(3.0);
+        gw[0] = gw[1] = 1.0;
+    } else if (rule == 3) {
+        g[0] = -sqrt(0.6);
+        g[1] = 0.0;
+        g[2] = sqrt(0.6);
+        gw[0] = gw[2] = 5.0 / 9.0;
+        gw[1] = 8.0 / 9.0;
+    } else {
+        return 0;
+    }
+    int r = 0;
+    for (int i = 0; i < rule; i++)
+        for (int j = 0; j < rule; j++, r++) {
+            pc[2 * r] = g[i];
+            pc[2 * r + 1] = g[j];
+            w[r] = gw[i] * gw[j];
+        }
+    return r;
+}
+
+/* bfunparam / bfundparams of FESetT3 and FESetQ4: N (nen), gradN (nen x 2, column-major) */
+static void surface_basis(int nen, double xi, double eta, double *N, double *gN)
+{
+    if (nen == 3) {
+        N[0] = 1.0 - xi - eta;
+        N[1] = xi;
+        N[2] = eta;
+        const double g[6] = {-1.0, 1.0, 0.0, -1.0, 0.0, 1.0};
+        memcpy(gN, g, sizeof g);
+        return;
+    }
+    const double s[4] = {-1.0, 1.0, 1.0, -1.0}, t[4] = {-1.0, -1.0, 1.0, 1.0};
+    for (int a = 0; a < 4; a++) {
+        N[a] = 0.25 * (1.0 + s[a] * xi) * (1.0 + t[a] * eta);
+        gN[a] = 0.25 * s[a] * (1.0 + t[a] * eta);
+        gN[4 + a] = 0.25 * t[a] * (1.0 + s[a] * xi);
+    }
+}
+
+/* locjac!: loc = N' X, J = X' gradN (3 x 2, column-major), X nen x 3 row per node */
+static void surface_locjac(int nen, const double *X, const double *N, const double *gN, double *loc, double *J)
+{
+    for (int i = 0; i < 3; i++) {
+        double l = 0.0, j1 = 0.0, j2 = 0.0;
+        for (int a = 0; a < nen; a++) {
+            l += N[a] * X[3 * a + i];
+            j1 += X[3 * a + i] * gN[a];
+            j2 += X[3 * a + i] * gN[nen + a];
+        }
+        loc[i] = l;
+        J[i] = j1;
+        J[3 + i] = j2;
+    }
+}
+
+int orc_integration_points(int nen, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                           int rule, double *out)
+{
+    double pc[18], w[9], N[4], gN[8];
+    const int np = surface_rule(nen, rule, pc, w);
+    if (!np) return 1;
+    for (int64_t e = 0; e < nelem; e++) {
+        double X[12];
+        gather_X(xyz, nnodes, conn + nen * e, nen, X);
+        for (int j = 0; j < np; j++) {
+            double *o = out + 9 * (e * np + j);
+            surface_basis(nen, pc[2 * j], pc[2 * j + 1], N, gN);
+            surface_locjac(nen, X, N, gN, o, o + 3);
+        }
+    }
+    return 0;
+}
+
+int orc_distribloads(int nen, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                     const int64_t *dofnums, int rule, int m, const double *force, int64_t nforce, int64_t n,
+                     double *F)
+{
+    double pc[18], w[9], N[4], gN[8];
+    const int np = surface_rule(nen, rule, pc, w);
+    if (!np) return 1;
+    if (m != 2 && m != 3) return 2;
+    if (nforce != 1 && nforce != nelem && nforce != nelem * np) return 3;
+    for (int64_t d = 0; d < n; d++) F[d] = 0.0;
+    for (int64_t e = 0; e < nelem; e++) {
+        double X[12], Fe[24], loc[3], J[6];
+        gather_X(xyz, nnodes, conn + nen * e, nen, X);
+        memset(Fe, 0, sizeof Fe);
+        for (int j = 0; j < np; j++) {
+            surface_basis(nen, pc[2 * j], pc[2 * j + 1], N, gN);
+            surface_locjac(nen, X, N, gN, loc, J);
+            /* Jacobiansurface of a 3 x 2 J; Jacobianvolume multiplies by the other dimension 1 */
+            const double a1 = J[1] * J[5] - J[2] * J[4];
+            const double a2 = J[2] * J[3] - J[0] * J[5];
+            const double a3 = J[0] * J[4] - J[1] * J[3];
+            const double Jac = sqrt(a1 * a1 + a2 * a2 + a3 * a3);
+            const double factor = Jac * w[j];
+            const double *f = nforce == 1 ? force : (nforce == nelem ? force + 6 * e : force + 6 * (e * np + j));
+            for (int a = 0; a < nen; a++) {
+                const double Nf = N[a] * factor;
+                for (int k = 0; k < 6; k++) Fe[6 * a + k] += Nf * f[k];
+            }
+        }
+        /* SysvecAssembler: F[dof] += Fe in element order; dofs above n dropped */
+        for (int a = 0; a < nen; a++) {
+            const int64_t nd = conn[nen * e + a] - 1;
+            for (int k = 0; k < 6; k++) {
+                const int64_t d = dofnums[nd + k * nnodes];
+                if (d >= 1 && d <= n) F[d - 1] += Fe[6 * a + k];
+            }
+        }
+    }
+    return 0;
+}

@@ -94,6 +94,8 @@ def lib():
         L.orc_beam_element.restype = ctypes.c_int
         L.orc_beam_frame.restype = ctypes.c_double
         L.orc_resultants.restype = ctypes.c_int
+        L.orc_distribloads.restype = ctypes.c_int
+        L.orc_integration_points.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -339,6 +341,43 @@ def assemble_vector(Fe, conn, dofnums, n):
     lib().orc_assemble_vector(ctypes.c_int64(dofnums.shape[0]), ctypes.c_int64(conn.shape[0]),
                               ctypes.c_int(conn.shape[1]), _p(conn, _c_i64_p), _p(dofnums, _c_i64_p),
                               ctypes.c_int64(n), _p(Fe, _c_dbl_p), _p(F, _c_dbl_p))
+    return F
+
+
+def _surface_args(xyz, conn):
+    xyz = np.asfortranarray(xyz, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int64)
+    return xyz, conn, ctypes.c_int(conn.shape[1]), ctypes.c_int64(xyz.shape[0]), ctypes.c_int64(conn.shape[0])
+
+
+def npoints_of_rule(nen, rule):
+    """Points per element: TriRule(npts) for triangles, GaussRule(2, order) for quadrilaterals."""
+    return rule if nen == 3 else rule * rule
+
+
+def integration_points(xyz, conn, rule):
+    """(nelem x npts, 9): location, x_xi, x_eta of every point, element order."""
+    xyz, conn, nen, nn, ne = _surface_args(xyz, conn)
+    out = np.zeros((conn.shape[0] * npoints_of_rule(conn.shape[1], rule), 9))
+    st = lib().orc_integration_points(nen, nn, _p(xyz, _c_dbl_p), ne, _p(conn, _c_i64_p), ctypes.c_int(rule),
+                                      _p(out, _c_dbl_p))
+    if st != 0:
+        raise RuntimeError("oracle integration_points failed with status %d" % st)
+    return out
+
+
+def distribloads(xyz, conn, dofnums, rule, m, force, n):
+    """distribloads(FEMMBase(IntegDomain(fes, rule)), geom, P, fi, m) with the
+    force given as one 6-vector, one per element or one per point."""
+    xyz, conn, nen, nn, ne = _surface_args(xyz, conn)
+    dofnums = np.asfortranarray(dofnums, dtype=np.int64)
+    f = np.ascontiguousarray(force, dtype=np.float64).reshape(-1, 6)
+    F = np.zeros(n, dtype=np.float64)
+    st = lib().orc_distribloads(nen, nn, _p(xyz, _c_dbl_p), ne, _p(conn, _c_i64_p), _p(dofnums, _c_i64_p),
+                                ctypes.c_int(rule), ctypes.c_int(m), _p(f, _c_dbl_p), ctypes.c_int64(f.shape[0]),
+                                ctypes.c_int64(n), _p(F, _c_dbl_p))
+    if st != 0:
+        raise RuntimeError("oracle distribloads failed with status %d" % st)
     return F
 
 
