@@ -210,9 +210,9 @@ class Assembler:
         return nnz.value
 
     def tiles(self):
-        t = (ctypes.c_int32 * 3)()
-        self.ctx.call("fs_tuning", t)
-        return {"elements_per_block": t[0], "gather_warps": t[1], "tuned": bool(t[2])}
+        t = (ctypes.c_int32 * 4)()
+        self.ctx.call("fs_tuning_ex", t, 4)
+        return {"elements_per_block": t[0], "gather_warps": t[1], "tuned": bool(t[2]), "pairs_once": bool(t[3])}
 
     def timings(self):
         t = np.zeros(4)

@@ -54,7 +54,7 @@ int read_status(fs_ctx *c, int *bits)
 static void free_pattern(PatternDev &P)
 {
     dfree(&P.nbr_off); dfree(&P.nbr); dfree(&P.pair_slots); dfree(&P.colpos); dfree(&P.colsrc); dfree(&P.rowlen);
-    dfree(&P.sl_off); dfree(&P.sl_ent);
+    dfree(&P.sl_off); dfree(&P.sl_ent); dfree(&P.sl_mir);
     dfree(&P.rowptr); dfree(&P.colidx); dfree(&P.diag_rowptr); dfree(&P.diag_colidx);
     dfree(&P.tmp_cnt); dfree(&P.tmp_owner);
     P = PatternDev();
@@ -538,7 +538,7 @@ int fs_mass(fs_ctx *c, int assembler, int64_t nrows, int64_t *nnz_out)
 int fs_autotune(fs_ctx *c, int mode)
 {
     if (!c) return FS_ERR_BAD_INPUT;
-    if (mode < 0 || mode > 2) return set_err(c, FS_ERR_BAD_INPUT, "autotune mode must be 0, 1 or 2");
+    if (mode < 0 || mode > 3) return set_err(c, FS_ERR_BAD_INPUT, "autotune mode must be 0, 1, 2 or 3");
     c->tune.mode = mode;
     return FS_OK;
 }
@@ -549,6 +549,15 @@ int fs_tuning(const fs_ctx *c, int32_t *out)
     out[0] = c->tune.elem_epb;
     out[1] = c->tune.gather_warps;
     out[2] = c->tune.from_tuner ? 1 : 0;
+    return FS_OK;
+}
+
+int fs_tuning_ex(const fs_ctx *c, int32_t *out, int n)
+{
+    if (!c || (n > 0 && !out)) return FS_ERR_BAD_INPUT;
+    const int32_t v[4] = {c->tune.elem_epb, c->tune.gather_warps, c->tune.from_tuner ? 1 : 0,
+                          c->tune.gather_once != 0 ? 1 : 0};
+    for (int k = 0; k < n && k < 4; k++) out[k] = v[k];
     return FS_OK;
 }
 

@@ -109,7 +109,7 @@ template <class R, int NEN, int G_COLS, int WARPS> struct GatherMinBlocks {
 
 template <class R, int NEN, int G_COLS, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, WARPS>::value))
-    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals)
+    k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals, bool once)
 {
     typedef typename GatherAcc<R>::T A;
     constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
@@ -137,9 +137,10 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
     if (!any) return;
     if (L <= 32 * G_COLS) {
         // second round of loads, all depending only on the first: lane k < 6
-        // the row pointer of dof k, lane s the first entry of neighbour slot s,
-        // lane q the pair q of the first batch, every lane its columns
-        int64_t rp_l = 0;
+        // the row pointer of dof k, lane s the first entry of neighbour slot s
+        // and its pair flags, lane q the pair q of the first batch, every lane
+        // its columns
+        int64_t rp_l = -1;  // -1: the dof has no row
         {
             int dl = d[0];
 #pragma unroll
@@ -149,8 +150,19 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
         const int ntot = (int)(pe - pb) * NEN;
         const int nslots = (int)(off_next - off);
         const bool slot_shfl = nslots < 32;  // slot starts exchanged by shuffles
-        int sl_l = 0;
+        // node-block pairs summed once: this node qualifies (register path,
+        // slot data in lanes); a lower neighbour that qualifies writes the
+        // pair's values into this node's rows, an upper one that qualifies
+        // gets them from this node
+        const bool sym = once && slot_shfl && P.sym;
+        constexpr uint32_t QBIT = G_COLS == 2 ? 4u : 8u;
+        int sl_l = 0, nb_l = 0;
+        uint32_t mf_l = 0;  // the slot's mirror index << 4 | flags
         if (slot_shfl && lane <= nslots) sl_l = lane < nslots ? (int)P.sl_off[off + lane] : ntot;
+        if (sym && lane < nslots) {
+            mf_l = (uint32_t)P.sl_mir[off + lane];
+            nb_l = P.nbr[off + lane];
+        }
         int32_t pel_l = lane < G_MAXP && pb + lane < pe ? m.pair_e[pb + lane] : 0;
         int cs_l[G_COLS];
 #pragma unroll
@@ -168,14 +180,47 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             sent[i] = one_batch ? (uint16_t)((e & 63u) * SLAB + ((e >> 6) & 3u) * 36 | ((e >> 8) & 1u) << 15)
                                 : (uint16_t)e;
         }
+        // the row positions this warp sums (all of them, or all but those of
+        // lower qualifying neighbours), packed densely over the lanes through
+        // the staging area: position | colsrc << 8
+        int jcol[G_COLS], csc[G_COLS];
+        if (sym) {
+            uint32_t *pmap = reinterpret_cast<uint32_t *>(stage);
+            int base = 0;
+#pragma unroll
+            for (int c = 0; c < G_COLS; c++) {
+                const int j = lane + 32 * c;
+                const uint32_t f = __shfl_sync(0xffffffffu, mf_l, cs_l[c] / 6);
+                const bool mine = j < L && !((f & 1u) && (f & QBIT));
+                const uint32_t mask = __ballot_sync(0xffffffffu, mine);
+                if (mine) pmap[base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)j | (uint32_t)cs_l[c] << 8;
+                base += __popc(mask);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c < G_COLS; c++) {
+                const int i = lane + 32 * c;
+                const uint32_t v = i < base ? pmap[i] : 0u;
+                jcol[c] = i < base ? (int)(v & 255u) : -1;
+                csc[c] = (int)(v >> 8);
+            }
+            __syncwarp();
+        } else {
+#pragma unroll
+            for (int c = 0; c < G_COLS; c++) {
+                const int j = lane + 32 * c;
+                jcol[c] = j < L ? j : -1;
+                csc[c] = cs_l[c];
+            }
+        }
         // the lane's columns and the range of entries of their neighbour slot
-        int kcol[G_COLS], cur[G_COLS], beg[G_COLS], last[G_COLS];
+        int kcol[G_COLS], cur[G_COLS], beg[G_COLS], last[G_COLS], slc[G_COLS];
         A hi[G_COLS][6], lo[G_COLS][6];
 #pragma unroll
         for (int c = 0; c < G_COLS; c++) {
-            const int j = lane + 32 * c;
-            const int sl = cs_l[c] / 6;
-            kcol[c] = cs_l[c] - 6 * sl;
+            const int sl = csc[c] / 6;
+            slc[c] = sl;
+            kcol[c] = csc[c] - 6 * sl;
             int b0, b1;
             if (slot_shfl) {
                 b0 = __shfl_sync(0xffffffffu, sl_l, sl);
@@ -184,8 +229,8 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
                 b0 = (int)P.sl_off[off + sl];
                 b1 = sl + 1 < nslots ? (int)P.sl_off[off + sl + 1] : ntot;
             }
-            cur[c] = j < L ? b0 : 0;
-            last[c] = j < L ? b1 : 0;
+            cur[c] = jcol[c] >= 0 ? b0 : 0;
+            last[c] = jcol[c] >= 0 ? b1 : 0;
             beg[c] = cur[c];
             // hi, lo: set by the first contribution (every row position has one)
         }
@@ -295,15 +340,28 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             }
             __syncwarp();
         }
+        // write-out, column by column; a column of an upper qualifying
+        // neighbour s puts its six values also into row (s, kcol), at the
+        // positions of this node's dofs in s's rows
 #pragma unroll
-        for (int k = 0; k < 6; k++) {
-            const int64_t rpk = __shfl_sync(0xffffffffu, rp_l, k);
-            if (d[k] > n) continue;
-            double *o = vals + rpk;
+        for (int c = 0; c < G_COLS; c++) {
+            const uint32_t f = __shfl_sync(0xffffffffu, mf_l, slc[c]);
+            const int snode = __shfl_sync(0xffffffffu, nb_l, slc[c]);
+            const bool tw = jcol[c] >= 0 && (f & 2u) && (f & QBIT);
+            int64_t trow = 0;
+            uint32_t tcp[3] = {0u, 0u, 0u};
+            if (tw) {
+                const int32_t dc = m.dof[(int64_t)kcol[c] * m.nnodes + snode];
+                trow = P.rowptr[dc - 1];
+                const uint32_t *cp = reinterpret_cast<const uint32_t *>(P.colpos + 6 * (int64_t)(f >> 4));
+                tcp[0] = cp[0];
+                tcp[1] = cp[1];
+                tcp[2] = cp[2];
+            }
 #pragma unroll
-            for (int c = 0; c < G_COLS; c++) {
-                const int j = lane + 32 * c;
-                if (j >= L) continue;
+            for (int k = 0; k < 6; k++) {
+                const int64_t rpk = __shfl_sync(0xffffffffu, rp_l, k);
+                if (rpk < 0 || jcol[c] < 0) continue;
                 double v;
                 if (SINGLE) {
                     // hi + lo: exact in double unless their exponents are more than
@@ -313,7 +371,8 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
                 } else {
                     v = (double)hi[c][k];
                 }
-                o[j] = v;
+                vals[rpk + jcol[c]] = v;
+                if (tw) vals[trow + (int16_t)(tcp[k >> 1] >> (16 * (k & 1)))] = v;
             }
         }
     } else {
@@ -335,8 +394,11 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
                 const R v = b < a ? blk[kc * 6 + krow] : blk[rem];
                 int s = (slots >> (8 * b)) & 0xff;
                 int cp = P.colpos[off6 + s * 6 + kc];
-                if (cp >= 0 && d[krow] <= n) {
-                    double *o = vals + P.rowptr[d[krow] - 1] + cp;
+                int dk = d[0];  // d[krow] without a local-memory copy of d
+#pragma unroll
+                for (int k = 1; k < 6; k++) dk = krow == k ? d[k] : dk;
+                if (cp >= 0 && dk <= n) {
+                    double *o = vals + P.rowptr[dk - 1] + cp;
                     *o += entry_value(v);
                 }
             }
@@ -353,7 +415,7 @@ static int gather_launch_w(fs_ctx *c, const R *ke, double *vals)
     const size_t smem = (size_t)W * GatherSmem<R, NEN>::PER_WARP;
     auto kern = k_gather<R, NEN, G_COLS, W>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals);
+    kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals, c->tune.gather_once != 0);
     return FS_OK;
 }
 

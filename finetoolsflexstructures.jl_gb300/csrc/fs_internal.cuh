@@ -76,6 +76,11 @@ struct PatternDev {
     uint16_t *sl_off = nullptr;  // per (node, slot), relative to the node's first entry
     uint16_t *sl_ent = nullptr;  // npairs * nen
     int32_t *rowlen = nullptr;   // per node: row length L
+    // per (node, slot): node-block pairs summed once (k_slot_mirror); sym false
+    // when the neighbour entry indices would not fit 28 bits (every node sums
+    // its own rows)
+    uint32_t *sl_mir = nullptr;
+    bool sym = false;
     int64_t *rowptr = nullptr;   // n + 1
     int32_t *colidx = nullptr;   // nnz, 0-based
     int64_t *diag_rowptr = nullptr;  // diagonal pattern (n + 1)
@@ -85,7 +90,7 @@ struct PatternDev {
     // allocated capacities (elements): a rebuild reuses the buffers that fit
     size_t cap_nbr_off = 0, cap_nbr = 0, cap_pair_slots = 0, cap_colpos = 0, cap_colsrc = 0, cap_rowlen = 0,
            cap_sl_off = 0, cap_sl_ent = 0, cap_rowptr = 0, cap_colidx = 0, cap_diag_rowptr = 0,
-           cap_diag_colidx = 0, cap_tmp_cnt = 0, cap_tmp_owner = 0;
+           cap_diag_colidx = 0, cap_tmp_cnt = 0, cap_tmp_owner = 0, cap_sl_mir = 0;
 };
 
 }  // namespace fs
@@ -168,6 +173,7 @@ struct fs_ctx {
         int mode = -1;         // -1: not read yet (FLEXSHELL_AUTOTUNE), 0 off, 1 on, 2 re-tune
         int elem_epb = 0;      // elements per block
         int gather_warps = 0;  // warps (nodes) per block
+        int gather_once = -1;  // node-block pairs summed once: -1 default (yes), 0 no, 1 yes
         bool from_tuner = false;
     } tune;
     // batched meshes fused into one mesh (fs_batch_*): first matrix row of each

@@ -349,7 +349,10 @@ struct TuneKey {
     }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, std::pair<int, int>> g_tune;
+struct TuneVal {
+    int epb, warps, once;
+};
+std::map<TuneKey, TuneVal> g_tune;
 const size_t SMEM_MAX = 227 * 1024;
 const int64_t TUNE_MIN_ELEMENTS = 4096;
 }  // namespace
@@ -381,9 +384,10 @@ int autotune_shell(fs_ctx *c, int precision)
     }
     const MeshDev &m = c->mesh;
     c->tune.from_tuner = false;
-    if (c->tune.mode == 0 || m.nelem < TUNE_MIN_ELEMENTS) {
+    if (c->tune.mode == 0 || c->tune.mode == 3 || m.nelem < TUNE_MIN_ELEMENTS) {
         c->tune.elem_epb = 0;
         c->tune.gather_warps = 0;
+        c->tune.gather_once = c->tune.mode == 3 ? 0 : -1;
         return FS_OK;
     }
     const bool avgk = c->params.transv_shear_formulation == 1;
@@ -394,8 +398,9 @@ int autotune_shell(fs_ctx *c, int precision)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
-            c->tune.elem_epb = it->second.first;
-            c->tune.gather_warps = it->second.second;
+            c->tune.elem_epb = it->second.epb;
+            c->tune.gather_warps = it->second.warps;
+            c->tune.gather_once = it->second.once;
             c->tune.from_tuner = true;
             return FS_OK;
         }
@@ -417,23 +422,30 @@ int autotune_shell(fs_ctx *c, int precision)
     }
     c->tune.elem_epb = best_e;
     FS_TRY(launch_elements(c, precision));  // the gather candidates read these element matrices
-    int best_w = 0;
+    // gather: warps per block, and whether node-block pairs are summed once
+    // (with transposed copies) or by both nodes; bitwise the same values
+    int best_w = 0, best_o = 1;
     best_ms = 1e30f;
     for (int w : {4, 8, 16}) {
         if (gather_smem_bytes(precision, m.nen, w) > SMEM_MAX) continue;
-        c->tune.gather_warps = w;
-        float ms = 0.f;
-        FS_TRY(time_best(c, run_gather_once, precision, &ms));
-        if (ms < best_ms) {
-            best_ms = ms;
-            best_w = w;
+        for (int once : {1, 0}) {
+            c->tune.gather_warps = w;
+            c->tune.gather_once = once;
+            float ms = 0.f;
+            FS_TRY(time_best(c, run_gather_once, precision, &ms));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_w = w;
+                best_o = once;
+            }
         }
     }
     c->tune.gather_warps = best_w;
+    c->tune.gather_once = best_o;
     c->tune.from_tuner = true;
     if (c->tune.mode == 2) c->tune.mode = 1;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = {best_e, best_w};
+    g_tune[key] = {best_e, best_w, best_o};
     return FS_OK;
 }
 

@@ -428,6 +428,42 @@ __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_
     rowlen[r] = L;
 }
 
+// Per (node r, neighbour slot) the data the gather needs to compute each
+// node-block pair once: a block (r, s) with r < s is summed by r's warp,
+// which also writes it transposed into s's rows, when both nodes take the
+// gather's register path (a row of at most 64 or 128 positions, fewer than 32
+// neighbour slots, some row in the matrix); s's warp then skips it.  Per slot
+// one word: m << 4 | flags, flags bit 0 s < r, bit 1 s > r, bit 2 s qualifies
+// at 64 positions, bit 3 at 128; m, for s > r, the slot of r in s's list as an
+// index into the neighbour entries (6 m indexes colpos: the column positions
+// of r's dofs in s's rows).
+__global__ void k_slot_mirror(int64_t nnodes, int64_t n_mat, const int32_t *dof, const int64_t *nbr_off,
+                              const int32_t *nbr, const int32_t *rowlen, uint32_t *mir)
+{
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nnodes) return;
+    const int64_t off = nbr_off[r], n = nbr_off[r + 1] - off;
+    for (int64_t sl = 0; sl < n; sl++) {
+        const int32_t s = nbr[off + sl];
+        const int64_t so = nbr_off[s], sn = nbr_off[s + 1] - so;
+        bool anyrow = false;
+        for (int k = 0; k < 6; k++) anyrow |= dof[(int64_t)k * nnodes + s] <= n_mat;
+        const int L = rowlen[s];
+        const bool q = anyrow && sn < 32;
+        const uint32_t f = (s < r ? 1u : 0u) | (s > r ? 2u : 0u) | (q && L <= 64 ? 4u : 0u) | (q && L <= 128 ? 8u : 0u);
+        uint32_t mv = 0;
+        if (s > r) {
+            int64_t lo = 0, hi = sn - 1;  // r in s's sorted list
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (nbr[so + mid] < r) lo = mid + 1; else hi = mid;
+            }
+            mv = (uint32_t)(so + lo);
+        }
+        mir[off + sl] = mv << 4 | f;
+    }
+}
+
 // *out = max(v[0..n)) (out zeroed before; values are non-negative)
 __global__ void k_max_i32(int64_t n, const int32_t *v, int32_t *out)
 {
@@ -540,6 +576,15 @@ int build_pattern(fs_ctx *c, int64_t n)
     if (nn)
         k_fill_colidx<<<nblk(nn * 32, 256), 256, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.colsrc,
                                                                   P.rowlen, P.rowptr, P.colidx);
+    // node-block pairs summed once (neighbour entry indices fit 28 bits)
+    if (nbr_total < (1LL << 28)) {
+        FS_TRY(grow(c, &P.sl_mir, &P.cap_sl_mir, (size_t)nbr_total));
+        if (nn)
+            k_slot_mirror<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.rowlen, P.sl_mir);
+        P.sym = true;
+    } else {
+        P.sym = false;
+    }
     FS_TRY(grow(c, &P.diag_rowptr, &P.cap_diag_rowptr, (size_t)n + 1));
     FS_TRY(grow(c, &P.diag_colidx, &P.cap_diag_colidx, (size_t)n));
     k_diag_pattern<<<nblk(n + 1, 256), 256, 0, c->stream>>>(n, P.diag_rowptr, P.diag_colidx);

@@ -71,6 +71,7 @@ def lib():
         L.fs_stiffness_copy.argtypes = [vp, ctypes.c_int, ctypes.c_int64, vp, vp, vp]
         L.fs_autotune.argtypes = [vp, ctypes.c_int]
         L.fs_tuning.argtypes = [vp, vp]
+        L.fs_tuning_ex.argtypes = [vp, vp, ctypes.c_int]
         L.fs_batch_set.argtypes = [vp, ctypes.c_int, ctypes.c_int32, vp, vp, vp, vp, vp, vp, vp]
         L.fs_batch_stiffness.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.fs_batch_matrix_copy.argtypes = [vp, ctypes.c_int32, vp, vp, vp]

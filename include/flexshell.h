@@ -175,16 +175,24 @@ int fs_matrix_device(fs_ctx *ctx, const int64_t **rowptr, const int32_t **colidx
  * the last pattern build, [3] zero compaction.  `n` entries are written. */
 int fs_timings(const fs_ctx *ctx, double *out, int n);
 /* Tile-shape autotuner of the shell assembly (elements per block of the
- * element kernel, warps per block of the CSR gather).  Mode 1 (the default;
+ * element kernel; warps per block of the CSR gather and whether each
+ * node-block pair is summed once, by the lower node, and copied transposed
+ * into the upper node's rows, or by both nodes).  Mode 1 (the default;
  * environment FLEXSHELL_AUTOTUNE=0 makes 0 the default): the first fs_stiffness
  * call for a new key (element family, precision, average-K option, log2 of the
  * element count; meshes of at least 4096 elements) times every candidate on the
  * context's mesh and the choice is reused by the whole process; 0: built-in
- * shapes; 2: re-tune on the next call.  Tile shapes never change the results. */
+ * shapes (pairs summed once); 2: re-tune on the next call; 3: built-in shapes
+ * with every pair summed by both nodes.  No choice changes the results. */
 int fs_autotune(fs_ctx *ctx, int mode);
 /* Shapes used by the last fs_stiffness: out[0] elements per block (0 =
  * default), out[1] gather warps per block (0 = default), out[2] 1 if tuned. */
 int fs_tuning(const fs_ctx *ctx, int32_t *out);
+/* The same and the gather's mode: out[0..min(n, 4)) = elements per block,
+ * gather warps per block, 1 if tuned, 1 if each node-block pair is summed by
+ * one of its two nodes and copied transposed into the other's rows (0: both
+ * nodes sum it).  Either mode gives bitwise the same values. */
+int fs_tuning_ex(const fs_ctx *ctx, int32_t *out, int n);
 /* Allocation-free stiffness values.  No counterpart in the reference: it is for
  * callers that cannot let the library allocate device memory at call time (a
  * host whose own pool allocator owns the device memory, or a solver loop under
