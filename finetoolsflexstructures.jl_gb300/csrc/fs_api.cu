@@ -54,7 +54,7 @@ int read_status(fs_ctx *c, int *bits)
 static void free_pattern(PatternDev &P)
 {
     dfree(&P.nbr_off); dfree(&P.nbr); dfree(&P.pair_slots); dfree(&P.colpos); dfree(&P.colsrc); dfree(&P.rowlen);
-    dfree(&P.sl_off); dfree(&P.sl_ent); dfree(&P.sl_mir);
+    dfree(&P.sl_off); dfree(&P.sl_ent); dfree(&P.sl_mir); dfree(&P.lc);
     dfree(&P.rowptr); dfree(&P.colidx); dfree(&P.diag_rowptr); dfree(&P.diag_colidx);
     dfree(&P.tmp_cnt); dfree(&P.tmp_owner);
     P = PatternDev();

@@ -101,14 +101,21 @@ template <class R, int NEN> struct GatherSmem {
 // resident blocks asked of the compiler: 32 warps per SM where the kernel fits
 // 64 registers without spilling (float entries of three-node elements), 28
 // for other float entries, 24 (at most 80 registers) for double and float
-// pairs; no bound for the four-column variant of long rows
-template <class R, int NEN, int G_COLS, int WARPS> struct GatherMinBlocks {
-    static constexpr int warps = G_COLS > 2 ? 1 : (sizeof(R) == 4 ? (NEN == 3 ? 32 : 28) : 24);
+// pairs; the one-column variant 40 (48 registers) for float entries of
+// three-node elements, 36 (56) for the others; no bound for the four-column
+// variant of long rows
+template <class R, int NEN, int G_COLS, int WARPS, int G_OUT> struct GatherMinBlocks {
+    static constexpr int warps =
+        G_COLS > 2 ? 1
+                   : (G_OUT == 1 ? (sizeof(R) == 4 && NEN == 3 ? 40 : 36) : (sizeof(R) == 4 ? (NEN == 3 ? 32 : 28) : 24));
     static constexpr int value = warps / WARPS > 0 ? warps / WARPS : 1;
 };
 
-template <class R, int NEN, int G_COLS, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, WARPS>::value))
+// G_COLS: row positions per lane (32 G_COLS: the longest row of the register
+// path); G_OUT: positions a lane sums (G_OUT = 1 when every node sums at most
+// 32 positions with the pairs summed once)
+template <class R, int NEN, int G_COLS, int WARPS, int G_OUT>
+__global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, WARPS, G_OUT>::value))
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals, bool once)
 {
     typedef typename GatherAcc<R>::T A;
@@ -183,7 +190,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
         // the row positions this warp sums (all of them, or all but those of
         // lower qualifying neighbours), packed densely over the lanes through
         // the staging area: position | colsrc << 8
-        int jcol[G_COLS], csc[G_COLS];
+        int jcol[G_OUT], csc[G_OUT];
         if (sym) {
             uint32_t *pmap = reinterpret_cast<uint32_t *>(stage);
             int base = 0;
@@ -198,7 +205,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             }
             __syncwarp();
 #pragma unroll
-            for (int c = 0; c < G_COLS; c++) {
+            for (int c = 0; c < G_OUT; c++) {
                 const int i = lane + 32 * c;
                 const uint32_t v = i < base ? pmap[i] : 0u;
                 jcol[c] = i < base ? (int)(v & 255u) : -1;
@@ -207,17 +214,17 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             __syncwarp();
         } else {
 #pragma unroll
-            for (int c = 0; c < G_COLS; c++) {
+            for (int c = 0; c < G_OUT; c++) {
                 const int j = lane + 32 * c;
                 jcol[c] = j < L ? j : -1;
                 csc[c] = cs_l[c];
             }
         }
         // the lane's columns and the range of entries of their neighbour slot
-        int kcol[G_COLS], cur[G_COLS], beg[G_COLS], last[G_COLS], slc[G_COLS];
-        A hi[G_COLS][6], lo[G_COLS][6];
+        int kcol[G_OUT], cur[G_OUT], beg[G_OUT], last[G_OUT], slc[G_OUT];
+        A hi[G_OUT][6], lo[G_OUT][6];
 #pragma unroll
-        for (int c = 0; c < G_COLS; c++) {
+        for (int c = 0; c < G_OUT; c++) {
             const int sl = csc[c] / 6;
             slc[c] = sl;
             kcol[c] = csc[c] - 6 * sl;
@@ -263,7 +270,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             cp_async_wait_all();
             __syncwarp();
 #pragma unroll
-            for (int c = 0; c < G_COLS; c++) {
+            for (int c = 0; c < G_OUT; c++) {
                 int e = cur[c];
                 const int e1 = last[c];
                 if (e < e1) {
@@ -309,7 +316,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             __syncwarp();
             // this batch's contributions to the lane's columns, ascending pair order
 #pragma unroll
-            for (int c = 0; c < G_COLS; c++) {
+            for (int c = 0; c < G_OUT; c++) {
                 // the value's first contribution initialises the sum
                 if (cur[c] == beg[c] && cur[c] < last[c]) {
                     const uint32_t e = sent[cur[c]];
@@ -344,7 +351,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
         // neighbour s puts its six values also into row (s, kcol), at the
         // positions of this node's dofs in s's rows
 #pragma unroll
-        for (int c = 0; c < G_COLS; c++) {
+        for (int c = 0; c < G_OUT; c++) {
             const uint32_t f = __shfl_sync(0xffffffffu, mf_l, slc[c]);
             const int snode = __shfl_sync(0xffffffffu, nb_l, slc[c]);
             const bool tw = jcol[c] >= 0 && (f & 2u) && (f & QBIT);
@@ -408,31 +415,37 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
     }
 }
 
-template <class R, int NEN, int G_COLS, int W>
+template <class R, int NEN, int G_COLS, int W, int G_OUT>
 static int gather_launch_w(fs_ctx *c, const R *ke, double *vals)
 {
     const MeshDev &m = c->mesh;
     const size_t smem = (size_t)W * GatherSmem<R, NEN>::PER_WARP;
-    auto kern = k_gather<R, NEN, G_COLS, W>;
+    auto kern = k_gather<R, NEN, G_COLS, W, G_OUT>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<nblk2(m.nnodes, W), W * 32, smem, c->stream>>>(m, c->pat, c->pat.n, ke, vals, c->tune.gather_once != 0);
     return FS_OK;
 }
 
-template <class R, int NEN, int G_COLS>
+template <class R, int NEN, int G_COLS, int G_OUT>
 static int gather_launch_c(fs_ctx *c, const R *ke, double *vals, int warps)
 {
-    if (warps == 4) return gather_launch_w<R, NEN, G_COLS, 4>(c, ke, vals);
-    if (warps == 16) return gather_launch_w<R, NEN, G_COLS, 16>(c, ke, vals);
-    return gather_launch_w<R, NEN, G_COLS, 8>(c, ke, vals);
+    if (warps == 4) return gather_launch_w<R, NEN, G_COLS, 4, G_OUT>(c, ke, vals);
+    if (warps == 16) return gather_launch_w<R, NEN, G_COLS, 16, G_OUT>(c, ke, vals);
+    return gather_launch_w<R, NEN, G_COLS, 8, G_OUT>(c, ke, vals);
 }
 
 template <class R, int NEN>
 static int gather_launch(fs_ctx *c, const R *ke, double *vals, int warps)
 {
     // per-lane columns sized to the longest row (rows beyond 128 accumulate in place)
-    if (c->pat.maxlen <= 64) return gather_launch_c<R, NEN, 2>(c, ke, vals, warps);
-    return gather_launch_c<R, NEN, 4>(c, ke, vals, warps);
+    if (c->pat.maxlen <= 64) {
+        // one summed position per lane when the pairs are summed once and no
+        // node sums more than 32 positions
+        if (c->tune.gather_once != 0 && c->pat.sym && c->pat.maxlc <= 32)
+            return gather_launch_c<R, NEN, 2, 1>(c, ke, vals, warps);
+        return gather_launch_c<R, NEN, 2, 2>(c, ke, vals, warps);
+    }
+    return gather_launch_c<R, NEN, 4, 4>(c, ke, vals, warps);
 }
 
 size_t gather_smem_bytes(int precision, int nen, int warps)

@@ -80,6 +80,8 @@ struct PatternDev {
     // when the neighbour entry indices would not fit 28 bits (every node sums
     // its own rows)
     uint32_t *sl_mir = nullptr;
+    int32_t *lc = nullptr;       // per node: row positions summed with pairs summed once (rows <= 64)
+    int maxlc = 0;               // longest of those (the longest row without sym)
     bool sym = false;
     int64_t *rowptr = nullptr;   // n + 1
     int32_t *colidx = nullptr;   // nnz, 0-based
@@ -90,7 +92,7 @@ struct PatternDev {
     // allocated capacities (elements): a rebuild reuses the buffers that fit
     size_t cap_nbr_off = 0, cap_nbr = 0, cap_pair_slots = 0, cap_colpos = 0, cap_colsrc = 0, cap_rowlen = 0,
            cap_sl_off = 0, cap_sl_ent = 0, cap_rowptr = 0, cap_colidx = 0, cap_diag_rowptr = 0,
-           cap_diag_colidx = 0, cap_tmp_cnt = 0, cap_tmp_owner = 0, cap_sl_mir = 0;
+           cap_diag_colidx = 0, cap_tmp_cnt = 0, cap_tmp_owner = 0, cap_sl_mir = 0, cap_lc = 0;
 };
 
 }  // namespace fs

@@ -436,20 +436,28 @@ __global__ void k_fill_nbrs(int64_t nnodes, int nen, int64_t n_mat, const int64_
 // one word: m << 4 | flags, flags bit 0 s < r, bit 1 s > r, bit 2 s qualifies
 // at 64 positions, bit 3 at 128; m, for s > r, the slot of r in s's list as an
 // index into the neighbour entries (6 m indexes colpos: the column positions
-// of r's dofs in s's rows).
+// of r's dofs in s's rows).  lc: the row positions r's warp sums in the
+// register path of rows up to 64 positions (its row length less the columns
+// of lower neighbours that qualify there; 0 without rows).
 __global__ void k_slot_mirror(int64_t nnodes, int64_t n_mat, const int32_t *dof, const int64_t *nbr_off,
-                              const int32_t *nbr, const int32_t *rowlen, uint32_t *mir)
+                              const int32_t *nbr, const int32_t *rowlen, uint32_t *mir, int32_t *lc)
 {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nnodes) return;
     const int64_t off = nbr_off[r], n = nbr_off[r + 1] - off;
+    bool rrow = false;
+    for (int k = 0; k < 6; k++) rrow |= dof[(int64_t)k * nnodes + r] <= n_mat;
+    const bool rq = rrow && n < 32 && rowlen[r] <= 64;
+    int cnt = rrow ? rowlen[r] : 0;
     for (int64_t sl = 0; sl < n; sl++) {
         const int32_t s = nbr[off + sl];
         const int64_t so = nbr_off[s], sn = nbr_off[s + 1] - so;
-        bool anyrow = false;
-        for (int k = 0; k < 6; k++) anyrow |= dof[(int64_t)k * nnodes + s] <= n_mat;
+        int nfree = 0;
+        for (int k = 0; k < 6; k++) nfree += dof[(int64_t)k * nnodes + s] <= n_mat;
+        const bool anyrow = nfree > 0;
         const int L = rowlen[s];
         const bool q = anyrow && sn < 32;
+        if (rq && s < r && q && L <= 64) cnt -= nfree;
         const uint32_t f = (s < r ? 1u : 0u) | (s > r ? 2u : 0u) | (q && L <= 64 ? 4u : 0u) | (q && L <= 128 ? 8u : 0u);
         uint32_t mv = 0;
         if (s > r) {
@@ -462,6 +470,7 @@ __global__ void k_slot_mirror(int64_t nnodes, int64_t n_mat, const int32_t *dof,
         }
         mir[off + sl] = mv << 4 | f;
     }
+    lc[r] = cnt;
 }
 
 // *out = max(v[0..n)) (out zeroed before; values are non-negative)
@@ -577,10 +586,18 @@ int build_pattern(fs_ctx *c, int64_t n)
         k_fill_colidx<<<nblk(nn * 32, 256), 256, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.colsrc,
                                                                   P.rowlen, P.rowptr, P.colidx);
     // node-block pairs summed once (neighbour entry indices fit 28 bits)
+    P.maxlc = mx;
     if (nbr_total < (1LL << 28)) {
         FS_TRY(grow(c, &P.sl_mir, &P.cap_sl_mir, (size_t)nbr_total));
-        if (nn)
-            k_slot_mirror<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.rowlen, P.sl_mir);
+        FS_TRY(grow(c, &P.lc, &P.cap_lc, (size_t)nn));
+        if (nn) {
+            k_slot_mirror<<<nblk(nn, 128), 128, 0, c->stream>>>(nn, n, m.dof, P.nbr_off, P.nbr, P.rowlen, P.sl_mir,
+                                                               P.lc);
+            // the longest summed row (selects the one-column variant of the gather)
+            FS_CUDA(c, cudaMemsetAsync(d_max, 0, sizeof(int32_t), c->stream));
+            k_max_i32<<<nblk(nn, 256), 256, 0, c->stream>>>(nn, P.lc, d_max);
+            FS_CUDA(c, cudaMemcpyAsync(&mx, d_max, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+        }
         P.sym = true;
     } else {
         P.sym = false;
@@ -590,6 +607,7 @@ int build_pattern(fs_ctx *c, int64_t n)
     k_diag_pattern<<<nblk(n + 1, 256), 256, 0, c->stream>>>(n, P.diag_rowptr, P.diag_colidx);
     FS_CUDA(c, cudaGetLastError());
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (P.sym && nn) P.maxlc = mx;
     P.n = n;
     P.nnz = nnz;
     return FS_OK;
