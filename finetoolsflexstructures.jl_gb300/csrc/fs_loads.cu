@@ -1,12 +1,16 @@
-// Distributed surface loads on the shell meshes:
+// Distributed loads on the shell meshes and their boundary curves:
 // distribloads(FEMMBase(IntegDomain(fes, rule)), geom0, dchi, fi, m) of
 // FinEtools 8.2.5 (FEMMBaseModule), as the reference calls it on its shell
 // element sets (examples/shells/dynamics/homogeneous/explicit/
 // plate_expl_examples.jl:196-199, test/test_shell_statics.jl:84-86,
-// test/test_shell_resultants.jl:108-110).  Per element and integration point
-// the load intensity f (six components, one per nodal dof) contributes
-// N_a(xi) J(xi) w f to node a, J the surface Jacobian |x,xi x x,eta| (times
-// the other dimension 1 for m = 3, as FEMMBase's default); the element vectors
+// test/test_shell_resultants.jl:108-110) and on the two-node line elements of
+// a shell mesh's boundary (meshboundary, GaussRule(1, 2):
+// test/test_shell_statics.jl:212-215, test/test_composite_shell_statics.jl:
+// 80-88).  Per element and integration point the load intensity f (six
+// components, one per nodal dof) contributes N_a(xi) J(xi) w f to node a, J
+// the surface Jacobian |x,xi x x,eta| or, on a line element, the curve
+// Jacobian |x,xi| (times the other dimension 1 for the higher manifold
+// dimensions m, as FEMMBase's default); the element vectors
 // are summed per node in ascending assembly rank, the element-order sum of
 // FinEtools' vector assembler.  One thread per element, double precision.
 #include "fs_internal.cuh"
@@ -16,7 +20,8 @@ namespace fs {
 // integration points on the parent element; T3: TriRule(npts), npts 1, 3 or 6
 // (the centroid; the degree-2 interior rule; Dunavant's degree-4 rule),
 // weights summing to 1/2; Q4: GaussRule(2, order), order 1, 2 or 3, tensor
-// points with xi the outer index, weights summing to 4
+// points with xi the outer index, weights summing to 4; L2: GaussRule(1,
+// order), order 1, 2 or 3, weights summing to 2 (eta unused)
 struct SurfRule {
     int npts = 0;
     double xi[9], eta[9], w[9];
@@ -76,6 +81,15 @@ static bool make_rule(int nen, int rule, SurfRule &R)
         pw[0] = pw[2] = 5.0 / 9.0;
         pw[1] = 8.0 / 9.0;
     }
+    if (nen == 2) {
+        R.npts = rule;
+        for (int i = 0; i < rule; i++) {
+            R.xi[i] = pc[i];
+            R.eta[i] = 0.0;
+            R.w[i] = pw[i];
+        }
+        return true;
+    }
     R.npts = rule * rule;
     for (int i = 0; i < rule; i++)
         for (int j = 0; j < rule; j++) {
@@ -90,7 +104,12 @@ static bool make_rule(int nen, int rule, SurfRule &R)
 template <int NN>
 __device__ __forceinline__ void surf_basis(double xi, double eta, double N[NN], double dx[NN], double de[NN])
 {
-    if constexpr (NN == 3) {
+    if constexpr (NN == 2) {
+        N[0] = 0.5 * (1.0 - xi);
+        N[1] = 0.5 * (1.0 + xi);
+        dx[0] = -0.5; dx[1] = 0.5;
+        de[0] = 0.0; de[1] = 0.0;
+    } else if constexpr (NN == 3) {
         N[0] = 1.0 - xi - eta;
         N[1] = xi;
         N[2] = eta;
@@ -138,10 +157,16 @@ __global__ void __launch_bounds__(128) k_surface_loads(const MeshDev m, const Su
     for (int j = 0; j < R.npts; j++) {
         double N[NN], loc[3], t1[3], t2[3];
         surf_point<NN>(m, R, r, j, N, loc, t1, t2);
-        const double c1 = t1[1] * t2[2] - t1[2] * t2[1];
-        const double c2 = t1[2] * t2[0] - t1[0] * t2[2];
-        const double c3 = t1[0] * t2[1] - t1[1] * t2[0];
-        const double factor = sqrt(c1 * c1 + c2 * c2 + c3 * c3) * R.w[j];
+        double jac;
+        if constexpr (NN == 2) {
+            jac = sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+        } else {
+            const double c1 = t1[1] * t2[2] - t1[2] * t2[1];
+            const double c2 = t1[2] * t2[0] - t1[0] * t2[2];
+            const double c3 = t1[0] * t2[1] - t1[1] * t2[0];
+            jac = sqrt(c1 * c1 + c2 * c2 + c3 * c3);
+        }
+        const double factor = jac * R.w[j];
         const double *fp = nf == 1 ? f : (nf == m.nelem ? f + 6 * q : f + 6 * (q * R.npts + j));
         for (int a = 0; a < NN; a++) {
             const double nf_a = N[a] * factor;
@@ -153,7 +178,8 @@ __global__ void __launch_bounds__(128) k_surface_loads(const MeshDev m, const Su
     for (int k = 0; k < 3 * NN; k++) o2[k] = make_double2(F[2 * k], F[2 * k + 1]);
 }
 
-// point data in element order: location, then the two parent tangents
+// point data in element order: location, then the two parent tangents (the
+// second zero on a line element)
 template <int NN>
 __global__ void __launch_bounds__(128) k_surface_points(const MeshDev m, const SurfRule R, double *out)
 {
@@ -175,11 +201,12 @@ static int check_surface(fs_ctx *c, int rule, SurfRule &R)
 {
     const MeshDev &m = c->mesh;
     if (m.etype < 0) return set_err(c, FS_ERR_STATE, "no mesh: call fs_mesh_set first");
-    if (m.etype == FS_COROTBEAM)
-        return set_err(c, FS_ERR_UNSUPPORTED, "beam mesh: use fs_beam_distribloads_global");
+    // a two-node mesh (FS_COROTBEAM) is the L2 element set of the load
     if (!make_rule(m.nen, rule, R))
-        return set_err(c, FS_ERR_BAD_INPUT, m.nen == 3 ? "triangle rule: TriRule npts 1, 3 or 6"
-                                                       : "quadrilateral rule: GaussRule(2, order), order 1, 2 or 3");
+        return set_err(c, FS_ERR_BAD_INPUT,
+                       m.nen == 3 ? "triangle rule: TriRule npts 1, 3 or 6"
+                                  : (m.nen == 2 ? "line rule: GaussRule(1, order), order 1, 2 or 3"
+                                                : "quadrilateral rule: GaussRule(2, order), order 1, 2 or 3"));
     return FS_OK;
 }
 
@@ -202,7 +229,9 @@ int fs_integration_points(fs_ctx *c, int rule, double *out)
     FS_TRY(ensure_scratch(c, sizeof(double) * 9 * (size_t)np));
     double *d = (double *)c->scratch;
     const unsigned g = (unsigned)((np + 127) / 128);
-    if (m.nen == 3)
+    if (m.nen == 2)
+        k_surface_points<2><<<g, 128, 0, c->stream>>>(m, R, d);
+    else if (m.nen == 3)
         k_surface_points<3><<<g, 128, 0, c->stream>>>(m, R, d);
     else
         k_surface_points<4><<<g, 128, 0, c->stream>>>(m, R, d);
@@ -219,8 +248,9 @@ int fs_distribloads(fs_ctx *c, int rule, int m_dim, const double *force, int64_t
     SurfRule R;
     FS_TRY(check_surface(c, rule, R));
     const MeshDev &m = c->mesh;
-    if (m_dim != 2 && m_dim != 3)
-        return set_err(c, FS_ERR_BAD_INPUT, "m: 2 (surface) or 3 (surface times the other dimension 1)");
+    if (m_dim < (m.nen == 2 ? 1 : 2) || m_dim > 3)
+        return set_err(c, FS_ERR_BAD_INPUT, m.nen == 2 ? "m: 1 (curve), 2 or 3 (curve times the other dimension 1)"
+                                                       : "m: 2 (surface) or 3 (surface times the other dimension 1)");
     if (!c->dofs_ready) return set_err(c, FS_ERR_STATE, "no dof numbering: call fs_dofs_set first");
     if (nrows < 0) return set_err(c, FS_ERR_BAD_INPUT, "negative vector length");
     const int64_t np = m.nelem * R.npts;
@@ -233,7 +263,9 @@ int fs_distribloads(fs_ctx *c, int rule, int m_dim, const double *force, int64_t
     FS_CUDA(c, cudaMemcpyAsync(df, force, sizeof(double) * nfv, cudaMemcpyHostToDevice, c->stream));
     if (m.nelem) {
         const unsigned g = (unsigned)((m.nelem + 127) / 128);
-        if (m.nen == 3)
+        if (m.nen == 2)
+            k_surface_loads<2><<<g, 128, 0, c->stream>>>(m, R, df, nforce, dfe);
+        else if (m.nen == 3)
             k_surface_loads<3><<<g, 128, 0, c->stream>>>(m, R, df, nforce, dfe);
         else
             k_surface_loads<4><<<g, 128, 0, c->stream>>>(m, R, df, nforce, dfe);

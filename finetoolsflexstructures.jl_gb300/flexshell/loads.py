@@ -5,6 +5,8 @@ reference makes around its shell FEMMs:
     fi = ForceIntensity([0, 0, -q, 0, 0, 0])                       # or a callable
     F = distribloads(lfemm, geom0, dchi, fi, 3)                    # test/test_shell_statics.jl:84-86
     Fmag = distribloads(lfemm, vassem, geom0, dchi, fi, 2)         # plate_expl_examples.jl:196-199
+    bfes = mesh.meshboundary(fes)                                  # edge loads on boundary curves:
+    lfemm = FEMMBase(IntegDomain(bfes[l1], GaussRule(1, 2)))       # test/test_shell_statics.jl:212-215
 
 The element loop and the per-node sums run in libflexshell.so
 (fs_distribloads); a callable ForceIntensity is evaluated on the host at the
@@ -28,25 +30,31 @@ class TriRule:
 
 
 class GaussRule:
-    """GaussRule(2, order): order x order points on the quadrilateral."""
+    """GaussRule(2, order): order x order points on the quadrilateral;
+    GaussRule(1, order): order points on the two-node line element."""
 
     def __init__(self, dim, order):
-        if dim != 2 or order not in (1, 2, 3):
-            raise ValueError("GaussRule: dim 2, order 1, 2 or 3")
-        self.npts = order * order
+        if dim not in (1, 2) or order not in (1, 2, 3):
+            raise ValueError("GaussRule: dim 1 or 2, order 1, 2 or 3")
+        self.dim = dim
+        self.npts = order ** dim
         self.code = order
 
 
 class IntegDomain:
-    """IntegDomain(fes, rule): the element set (connectivity, nelem x 3 or
-    nelem x 4, 1-based) and its integration rule."""
+    """IntegDomain(fes, rule): the element set (connectivity, nelem x 2
+    line elements, nelem x 3 triangles or nelem x 4 quadrilaterals, 1-based)
+    and its integration rule."""
 
     def __init__(self, conn, rule):
         self.conn = np.ascontiguousarray(conn, dtype=np.int64)
-        if self.conn.ndim != 2 or self.conn.shape[1] not in (3, 4):
-            raise ValueError("IntegDomain: triangles (nelem x 3) or quadrilaterals (nelem x 4)")
-        if (self.conn.shape[1] == 3) != isinstance(rule, TriRule):
-            raise ValueError("IntegDomain: TriRule for triangles, GaussRule(2, order) for quadrilaterals")
+        if self.conn.ndim != 2 or self.conn.shape[1] not in (2, 3, 4):
+            raise ValueError("IntegDomain: lines (nelem x 2), triangles (nelem x 3) or quadrilaterals (nelem x 4)")
+        nen = self.conn.shape[1]
+        ok = isinstance(rule, TriRule) if nen == 3 else (isinstance(rule, GaussRule) and rule.dim == nen // 2)
+        if not ok:
+            raise ValueError("IntegDomain: GaussRule(1, order) for lines, TriRule for triangles, "
+                             "GaussRule(2, order) for quadrilaterals")
         self.rule = rule
 
 
@@ -97,7 +105,8 @@ class FEMMBase:
         key = (xyz.shape, xyz.tobytes())
         if key != self._key:
             conn = self.integdomain.conn
-            et = _abi.FS_T3FF if conn.shape[1] == 3 else _abi.FS_Q4RS
+            # a two-node set goes in as the library's two-node (beam) mesh type
+            et = {2: _abi.FS_COROTBEAM, 3: _abi.FS_T3FF, 4: _abi.FS_Q4RS}[conn.shape[1]]
             self.ctx.call("fs_mesh_set", et, xyz.shape[0], ptr(xyz), conn.shape[0], ptr(conn), None, None)
             self._key = key
 
@@ -107,7 +116,8 @@ class FEMMBase:
         self.ctx.call("fs_dofs_set", ptr(d))
 
     def integration_points(self, geom):
-        """(npoints, 9): location, x_xi, x_eta of every point, element order."""
+        """(npoints, 9): location, x_xi, x_eta of every point, element order
+        (x_eta zero on line elements)."""
         self._upload(geom)
         rule = self.integdomain.rule
         out = np.zeros((self.integdomain.conn.shape[0] * rule.npts, 9))
@@ -120,9 +130,9 @@ class FEMMBase:
 
 def distribloads(femm, *args):
     """distribloads(femm, [assembler,] geom, P, fi, m): the load vector of
-    the force intensity fi over the element set (m = 2 or 3: a surface load;
-    the elements' other dimension is 1).  Returns nalldofs(P) entries, or
-    nfreedofs with SysvecAssemblerFBlock."""
+    the force intensity fi over the element set (m = 2 or 3 on surfaces, 1, 2
+    or 3 on lines; the elements' other dimension is 1).  Returns nalldofs(P)
+    entries, or nfreedofs with SysvecAssemblerFBlock."""
     if len(args) == 4:
         assembler, (geom, P, fi, m) = SysvecAssembler(), args
     elif len(args) == 5:
@@ -141,7 +151,8 @@ def distribloads(femm, *args):
         for e in range(conn.shape[0]):
             for j in range(rule.npts):
                 out = np.zeros(6)
-                tang = np.column_stack([pts[k, 3:6], pts[k, 6:9]])
+                tang = (pts[k, 3:6].reshape(3, 1) if conn.shape[1] == 2
+                        else np.column_stack([pts[k, 3:6], pts[k, 6:9]]))
                 r = fi.fun(out, pts[k, 0:3].reshape(1, 3), tang, e + 1, j + 1)
                 force[k] = out if r is None else np.asarray(r, dtype=np.float64).ravel()[:6]
                 k += 1

@@ -116,3 +116,37 @@ def quads_to_triangles(conn_q):
     t[0::2] = conn_q[:, [0, 1, 3]]
     t[1::2] = conn_q[:, [1, 2, 3]]
     return t
+
+
+def Q4toT3(conn_q, orientation="default"):
+    """FinEtools Q4toT3: each quad [a b c d] becomes [a b c] and [a c d]
+    (``"alternate"``: [a b d] and [c d b]), the two triangles of a quad
+    adjacent in the element order."""
+    conn_q = np.asarray(conn_q, dtype=np.int64)
+    l1, l2 = ((0, 1, 2), (0, 2, 3)) if orientation == "default" else ((0, 1, 3), (2, 3, 1))
+    t = np.empty((2 * conn_q.shape[0], 3), dtype=np.int64)
+    t[0::2] = conn_q[:, l1]
+    t[1::2] = conn_q[:, l2]
+    return t
+
+
+def meshboundary(conn):
+    """Boundary of a triangle or quadrilateral mesh: the two-node edges that
+    belong to one element only (nedges x 2, 1-based), each with the
+    orientation it has in its element, in the order of the elements and of
+    their edges (node 1-2, 2-3, ...)."""
+    conn = np.asarray(conn, dtype=np.int64)
+    nen = conn.shape[1]
+    edges = np.stack([conn[:, [k, (k + 1) % nen]] for k in range(nen)], 1).reshape(-1, 2)
+    key = np.sort(edges, 1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    return edges[cnt[inv.ravel()] == 1]
+
+
+def selectelem(xyz, conn, box, inflate=0.0):
+    """0-based indexes of the elements whose nodes all lie inside the box
+    [xmin xmax ymin ymax zmin zmax] grown by ``inflate`` (FinEtools
+    selectelem with ``box`` and ``allin = true``)."""
+    inside = np.zeros(np.asarray(xyz).shape[0] + 1, dtype=bool)
+    inside[selectnode(xyz, box, inflate)] = True
+    return np.nonzero(inside[np.asarray(conn, dtype=np.int64)].all(1))[0]

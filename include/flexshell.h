@@ -337,13 +337,17 @@ int fs_restoring_force(fs_ctx *ctx, const double *U, double *F);
 #define FS_RES_MEMBRANE 3
 int fs_resultants(fs_ctx *ctx, int quantity, const double *u, const double *csmat, int64_t ncs, double *out);
 
-/* Distributed surface loads on the shell mesh: distribloads(FEMMBase(
- * IntegDomain(fes, rule)), geom0, dchi, fi, m) of FinEtools 8.2.5, as the
- * reference calls it on its shell element sets
+/* Distributed loads on a shell mesh or on its boundary curves:
+ * distribloads(FEMMBase(IntegDomain(fes, rule)), geom0, dchi, fi, m) of
+ * FinEtools 8.2.5, as the reference calls it on its shell element sets
  * (examples/shells/dynamics/homogeneous/explicit/plate_expl_examples.jl:196-199,
- * test/test_shell_statics.jl:84-86).  rule: T3 meshes TriRule(npts), npts 1,
- * 3 or 6; Q4 meshes GaussRule(2, order), order 1, 2 or 3.  m: 2 or 3 (the
- * element's other dimension is 1).  force: the ForceIntensity's six
+ * test/test_shell_statics.jl:84-86) and on the L2 edges of meshboundary
+ * (test/test_shell_statics.jl:212-215, test/test_composite_shell_statics.jl:80-88).
+ * The element set is the context's mesh: T3 (FS_T3FF) with TriRule(npts),
+ * npts 1, 3 or 6; Q4 (FS_Q4RS) with GaussRule(2, order), order 1, 2 or 3;
+ * two-node line elements (FS_COROTBEAM) with GaussRule(1, order), order 1, 2
+ * or 3.  m: 2 or 3 on surfaces, 1, 2 or 3 on lines (the element's other
+ * dimension is 1).  force: the ForceIntensity's six
  * components, nforce = 1 (uniform), nelem (one per element, element order) or
  * nelem x npoints (one per integration point, the points of
  * fs_integration_points).  F: nrows entries (nalldofs, or nfreedofs for
@@ -353,7 +357,7 @@ int fs_distribloads(fs_ctx *ctx, int rule, int m, const double *force, int64_t n
 /* The integration points of the same rules, element order, nine doubles per
  * point: the location and the two parent tangents x,xi and x,eta (the
  * arguments the reference's ForceIntensity callback receives as XYZ and
- * tangents). */
+ * tangents; x,eta is zero on a line element, whose callback gets x,xi only). */
 int fs_integration_points(fs_ctx *ctx, int rule, double *out);
 
 /* --- layup reduction (src/CompositeLayupModule.jl:246-330) ------------------ */

@@ -1453,7 +1453,8 @@ int orc_resultants(int64_t nnodes, const double *xyz, int64_t nelem, const int64
 /* integration rule on the parent element: TriRule(npts) for triangles
  * (1: centroid; 3: the degree-2 interior points; 6: Dunavant's degree-4
  * rule, orbits (1-2a, a) and permutations), GaussRule(2, order) for
- * quadrilaterals (xi the outer index); param (npts x 2), weights */
+ * quadrilaterals (xi the outer index), GaussRule(1, order) for the line
+ * element; param (npts x 2), weights */
 static int surface_rule(int nen, int rule, double *pc, double *w)
 {
     if (nen == 3) {
@@ -1488,6 +1489,7 @@ static int surface_rule(int nen, int rule, double *pc, double *w)
         return 0;
     }
     double g[3], gw[3];
+    if (nen != 2 && nen != 4) return 0;
     if (rule == 1) {
         g[0] = 0.0;
         gw[0] = 2.0;
@@ -1504,6 +1506,15 @@ static int surface_rule(int nen, int rule, double *pc, double *w)
     } else {
         return 0;
     }
+    if (nen == 2) {
+        /* GaussRule(1, order) on the line element, eta unused */
+        for (int i = 0; i < rule; i++) {
+            pc[2 * i] = g[i];
+            pc[2 * i + 1] = 0.0;
+            w[i] = gw[i];
+        }
+        return rule;
+    }
     int r = 0;
     for (int i = 0; i < rule; i++)
         for (int j = 0; j < rule; j++, r++) {
@@ -1514,9 +1525,17 @@ static int surface_rule(int nen, int rule, double *pc, double *w)
     return r;
 }
 
-/* bfunparam / bfundparams of FESetT3 and FESetQ4: N (nen), gradN (nen x 2, column-major) */
+/* bfunparam / bfundparams of FESetL2, FESetT3 and FESetQ4: N (nen), gradN
+ * (nen x 2, column-major; the second column zero for the line element) */
 static void surface_basis(int nen, double xi, double eta, double *N, double *gN)
 {
+    if (nen == 2) {
+        N[0] = 0.5 * (1.0 - xi);
+        N[1] = 0.5 * (1.0 + xi);
+        const double g[4] = {-0.5, 0.5, 0.0, 0.0};
+        memcpy(gN, g, sizeof g);
+        return;
+    }
     if (nen == 3) {
         N[0] = 1.0 - xi - eta;
         N[1] = xi;
@@ -1574,7 +1593,7 @@ int orc_distribloads(int nen, int64_t nnodes, const double *xyz, int64_t nelem, 
     double pc[18], w[9], N[4], gN[8];
     const int np = surface_rule(nen, rule, pc, w);
     if (!np) return 1;
-    if (m != 2 && m != 3) return 2;
+    if (m < (nen == 2 ? 1 : 2) || m > 3) return 2;
     if (nforce != 1 && nforce != nelem && nforce != nelem * np) return 3;
     for (int64_t d = 0; d < n; d++) F[d] = 0.0;
     for (int64_t e = 0; e < nelem; e++) {
@@ -1584,11 +1603,18 @@ int orc_distribloads(int nen, int64_t nnodes, const double *xyz, int64_t nelem, 
         for (int j = 0; j < np; j++) {
             surface_basis(nen, pc[2 * j], pc[2 * j + 1], N, gN);
             surface_locjac(nen, X, N, gN, loc, J);
-            /* Jacobiansurface of a 3 x 2 J; Jacobianvolume multiplies by the other dimension 1 */
-            const double a1 = J[1] * J[5] - J[2] * J[4];
-            const double a2 = J[2] * J[3] - J[0] * J[5];
-            const double a3 = J[0] * J[4] - J[1] * J[3];
-            const double Jac = sqrt(a1 * a1 + a2 * a2 + a3 * a3);
+            /* Jacobiancurve |x,xi| of the line element, Jacobiansurface |x,xi x x,eta|
+             * of the surface elements; the higher manifold dimensions multiply by
+             * the other dimension 1 (FEMMBase's default) */
+            double Jac;
+            if (nen == 2) {
+                Jac = sqrt(J[0] * J[0] + J[1] * J[1] + J[2] * J[2]);
+            } else {
+                const double a1 = J[1] * J[5] - J[2] * J[4];
+                const double a2 = J[2] * J[3] - J[0] * J[5];
+                const double a3 = J[0] * J[4] - J[1] * J[3];
+                Jac = sqrt(a1 * a1 + a2 * a2 + a3 * a3);
+            }
             const double factor = Jac * w[j];
             const double *f = nforce == 1 ? force : (nforce == nelem ? force + 6 * e : force + 6 * (e * np + j));
             for (int a = 0; a < nen; a++) {

@@ -125,15 +125,17 @@ int orc_cd_steps_load(int64_t n, const int64_t *rowptr, const int64_t *colidx,
                       int64_t nsteps, double *U, double *V, double *A, const double *Fmag,
                       const double *mul, int64_t nmul, int64_t step0, int nthreads);
 
-/* Distributed surface loads, distribloads(FEMMBase(IntegDomain(fes, rule)),
- * geom, P, ForceIntensity, m) of FinEtools 8.2.5 on a T3 (nen 3, TriRule
- * npts 1, 3, 6) or Q4 (nen 4, GaussRule(2, order 1..3)) element set: force 6
+/* Distributed loads, distribloads(FEMMBase(IntegDomain(fes, rule)), geom, P,
+ * ForceIntensity, m) of FinEtools 8.2.5 on an L2 (nen 2, GaussRule(1, order
+ * 1..3), m 1..3: boundary curves of a shell mesh), T3 (nen 3, TriRule npts
+ * 1, 3, 6) or Q4 (nen 4, GaussRule(2, order 1..3), m 2 or 3) element set: force 6
  * values per entry, nforce 1, nelem or nelem x npoints; F (n) accumulated in
  * element order; dofnums nnodes x 6 column-major, 1-based. */
 int orc_distribloads(int nen, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
                      const int64_t *dofnums, int rule, int m, const double *force, int64_t nforce, int64_t n,
                      double *F);
-/* The rule's points, element order, 9 values each: location, x_xi, x_eta. */
+/* The rule's points, element order, 9 values each: location, x_xi, x_eta
+ * (x_eta zero for the line element). */
 int orc_integration_points(int nen, int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
                            int rule, double *out);
 

@@ -351,8 +351,9 @@ def _surface_args(xyz, conn):
 
 
 def npoints_of_rule(nen, rule):
-    """Points per element: TriRule(npts) for triangles, GaussRule(2, order) for quadrilaterals."""
-    return rule if nen == 3 else rule * rule
+    """Points per element: TriRule(npts) for triangles, GaussRule(2, order) for
+    quadrilaterals, GaussRule(1, order) for two-node line elements."""
+    return rule if nen in (2, 3) else rule * rule
 
 
 def integration_points(xyz, conn, rule):

@@ -1,0 +1,67 @@
+"""Writes raasch_hook.npz: the four Raasch hook meshes of the reference's
+test-suite (test/raasch_s4_1x9.inp, _3x18, _5x36, _10x72; read by
+test/test_shell_statics.jl:143-227 through FinEtools' import_ABAQUS) as plain
+arrays, so that the tests run where the reference is absent.
+
+For each mesh the S4 quadrilaterals and the coordinates of the nodes they use
+are kept, with the nodes renumbered in their file order (findunconnnodes +
+compactnodes of the reference test); the split into triangles (Q4toT3) is
+left to the tests.  Run from the repository root:
+
+    python tests/golden/make_raasch_hook.py /root/reference/test
+"""
+import os
+import sys
+
+import numpy as np
+
+MESHES = ["1x9", "3x18", "5x36", "10x72"]
+
+
+def read_abaqus_s4(path):
+    """Node coordinates and S4 connectivity of the first part of an Abaqus
+    input file (the data lines after *Node and *Element, type=S4)."""
+    nodes, elems, mode = {}, [], None
+    with open(path) as f:
+        for line in f:
+            s = line.strip()
+            if not s or s.startswith("**"):
+                continue
+            if s.startswith("*"):
+                kw = s.lower().replace(" ", "")
+                if kw.startswith("*node") and not kw.startswith("*nodeoutput"):
+                    mode = "node" if not nodes else None
+                elif kw.startswith("*element,") and "type=s4" in kw:
+                    mode = "elem"
+                else:
+                    mode = None
+                continue
+            v = [t for t in s.split(",") if t.strip()]
+            if mode == "node":
+                nodes[int(v[0])] = [float(t) for t in v[1:4]]
+            elif mode == "elem":
+                elems.append([int(t) for t in v[1:5]])
+    ids = np.array(sorted(nodes))
+    xyz = np.array([nodes[i] for i in ids], dtype=np.float64)
+    conn = np.array(elems, dtype=np.int64)
+    # compact: keep the connected nodes in their order, renumber 1-based
+    used = np.zeros(ids.max() + 1, dtype=bool)
+    used[conn.ravel()] = True
+    keep = used[ids]
+    newnum = np.zeros(ids.max() + 1, dtype=np.int64)
+    newnum[ids[keep]] = np.arange(1, keep.sum() + 1)
+    return xyz[keep], newnum[conn]
+
+
+def main(src):
+    out = {}
+    for m in MESHES:
+        xyz, conn = read_abaqus_s4(os.path.join(src, "raasch_s4_%s.inp" % m))
+        out["xyz_" + m] = xyz
+        out["conn_" + m] = conn
+        print(m, xyz.shape[0], "nodes", conn.shape[0], "quads")
+    np.savez_compressed(os.path.join(os.path.dirname(os.path.abspath(__file__)), "raasch_hook.npz"), **out)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test")

@@ -69,6 +69,44 @@ def scordelis_lo(quads, n):
                 material=dict(Dps=Dps, Dt=Dt, rho=0.0), stab_c=0.2, F=F, probe=nl)
 
 
+# test/test_shell_statics.jl:229-236: tip deflection in percent of 5.02
+RAASCH_MESHES = ["1x9", "3x18", "5x36", "10x72"]
+RAASCH_REF = [91.7059961843231, 95.9355786538892, 97.19276899988246, 98.38896641657374]
+
+
+def raasch_hook(k):
+    """Raasch hook, test/test_shell_statics.jl:143-227: the reference's Abaqus
+    meshes (tests/golden/raasch_hook.npz), Q4toT3, clamped at x = 0, a shear
+    traction of 0.05 in z on the tip edge (meshboundary, GaussRule(1, 2),
+    distribloads m = 3).  Returns the problem and the tip edges."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "raasch_hook.npz"))
+    m = RAASCH_MESHES[k]
+    xyz, conn = g["xyz_" + m], mesh.Q4toT3(g["conn_" + m])
+    E, nu, t = 3300.0, 0.35, 2.0
+    tol = t / 2
+    inf = np.inf
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    fixed[mesh.selectnode(xyz, [0, 0, -inf, inf, -inf, inf], tol) - 1, :] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, nu))
+    bfes = mesh.meshboundary(conn)
+    edges = bfes[mesh.selectelem(xyz, bfes, [97.9615, 97.9615, -16, -16, 0, 20], tol)]
+    probe = mesh.selectnode(xyz, [97.9615, 97.9615, -16, -16, 0, 0], tol)[0] - 1
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=t,
+                material=dict(Dps=Dps, Dt=Dt, rho=0.0), stab_c=0.2, probe=probe,
+                edges=edges, traction=np.array([0, 0, 0.05, 0, 0, 0.0]))
+
+
+def tip_deflection_percent(K, F, prob):
+    """K_ff u = F_f; the probe's z deflection in percent of 5.02."""
+    import scipy.sparse.linalg as spl
+    nf = prob["nfree"]
+    u = spl.spsolve(K[:nf, :nf].tocsc(), F[:nf])
+    d = prob["dofnums"][prob["probe"], 2]
+    return u[d - 1] / 5.02 * 100
+
+
 def surface_load(xyz, conn, dof, qz):
     """Consistent nodal loads of a uniform z traction (FinEtools distribloads
     with TriRule(3) on triangles / GaussRule(2,2) on quads)."""

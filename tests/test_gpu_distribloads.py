@@ -1,6 +1,7 @@
-"""GPU parity of the distributed surface loads (fs_distribloads,
+"""GPU parity of the distributed loads (fs_distribloads,
 fs_integration_points: FinEtools distribloads on the shell element sets, as
-test/test_shell_statics.jl:84-86 and plate_expl_examples.jl:196-199 call it)
+test/test_shell_statics.jl:84-86 and plate_expl_examples.jl:196-199 call it,
+and on the L2 edges of their boundary, test/test_shell_statics.jl:212-215)
 against the oracle, through the Python mirror and the C ABI.  Tolerance 1e-12
 relative (max-abs difference over max-abs value)."""
 import numpy as np
@@ -92,4 +93,71 @@ def test_per_element_force_and_errors():
         with pytest.raises(FlexShellError) as ei:
             ctx.call("fs_distribloads", rule, m, ptr(fe), nf, n, ptr(out))
         assert ei.value.code == _abi.FS_ERR_BAD_INPUT
+    lfemm.close()
+
+
+def test_line_loads_match_oracle():
+    # the boundary curves of a T3 and a Q4 mesh: every GaussRule(1, order), m,
+    # uniform, per-element and per-point force, and a callable
+    for quads in (False, True):
+        d, geom0, dchi = _setup(quads)
+        edges = F.mesh.meshboundary(d["conn"])
+        n = dchi.nalldofs()
+        q = np.array([0.5, -0.25, -90.0, 0.01, -0.02, 0.03])
+        for order in (1, 2, 3):
+            lfemm = F.FEMMBase(F.IntegDomain(edges, F.GaussRule(1, order)))
+            for m in (1, 2, 3):
+                Fg = F.distribloads(lfemm, geom0, dchi, F.ForceIntensity(q), m)
+                Fo = O.distribloads(d["xyz"], edges, d["dofnums"], order, m, q, n)
+                assert Fg.shape == (n,) and _rel(Fg, Fo) <= 1e-12
+            pts = lfemm.integration_points(geom0)
+            po = O.integration_points(d["xyz"], edges, order)
+            assert pts.shape == (edges.shape[0] * order, 9)
+            assert np.abs(pts - po).max() <= 1e-12 * np.abs(po).max()
+            assert np.all(pts[:, 6:9] == 0.0)
+            fp = np.random.default_rng(order).normal(size=(pts.shape[0], 6))
+            out = np.zeros(n)
+            lfemm.ctx.call("fs_distribloads", order, 1, ptr(fp), fp.shape[0], n, ptr(out))
+            assert _rel(out, O.distribloads(d["xyz"], edges, d["dofnums"], order, 1, fp, n)) <= 1e-12
+            fe = fp[: edges.shape[0]]
+            lfemm.ctx.call("fs_distribloads", order, 2, ptr(fe), fe.shape[0], n, ptr(out))
+            assert _rel(out, O.distribloads(d["xyz"], edges, d["dofnums"], order, 2, fe, n)) <= 1e-12
+
+            def computetrac(forceout, XYZ, tangents, feid, qpid):
+                assert tangents.shape == (3, 1)
+                forceout[:] = 0.0
+                forceout[1] = XYZ[0, 0] * np.linalg.norm(tangents)
+                return forceout
+
+            Fg = F.distribloads(lfemm, geom0, dchi, F.ForceIntensity(float, 6, computetrac), 1)
+            fpts = np.zeros((po.shape[0], 6))
+            fpts[:, 1] = po[:, 0] * np.linalg.norm(po[:, 3:6], axis=1)
+            assert _rel(Fg, O.distribloads(d["xyz"], edges, d["dofnums"], order, 1, fpts, n)) <= 1e-12
+            with pytest.raises(FlexShellError) as ei:
+                lfemm.ctx.call("fs_distribloads", 4, 1, ptr(q), 1, n, ptr(out))
+            assert ei.value.code == _abi.FS_ERR_BAD_INPUT
+            lfemm.close()
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_raasch_hook_on_gpu(k):
+    # test/test_shell_statics.jl:229-236 (rtol 1e-4): the reference's Abaqus
+    # meshes, stiffness and tip-edge load both from the GPU
+    d = PB.raasch_hook(k)
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    dchi.nfreedofs = d["nfree"]
+    mat = F.materials.MatDeforElastIso(3300.0, 0.35)
+    femm = F.FEMMShellT3FF(d["conn"], d["thickness"], mat, stab_fun=d["stab_c"])
+    femm.associategeometry(geom0)
+    K = femm.stiffness(geom0, None, None, dchi)
+    lfemm = F.FEMMBase(F.IntegDomain(d["edges"], F.GaussRule(1, 2)))
+    Fg = F.distribloads(lfemm, geom0, dchi, F.ForceIntensity(d["traction"]), 3)
+    Fo = O.distribloads(d["xyz"], d["edges"], d["dofnums"], 2, 3, d["traction"], dchi.nalldofs())
+    assert _rel(Fg, Fo) <= 1e-12
+    v = PB.tip_deflection_percent(K, Fg, d)
+    assert abs(v - PB.RAASCH_REF[k]) <= 1e-4 * abs(PB.RAASCH_REF[k])
+    assert abs(v - PB.RAASCH_REF[k]) <= 1e-9 * abs(PB.RAASCH_REF[k])
+    femm.close()
     lfemm.close()

@@ -139,3 +139,20 @@ def test_cd_loop_with_external_force_follows_the_reference_loop():
     O.cd_steps(K.indptr, K.indices, K.data, invMC, C, dt, 40, Uo, Vo, Ao, Fmag=Fmag, mul=mul)
     assert np.abs(Uo - U).max() <= 1e-12 * np.abs(U).max()
     assert np.abs(Vo - V).max() <= 1e-12 * np.abs(V).max()
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_raasch_hook_t3ff_edge_load(k):
+    # test/test_shell_statics.jl:229-236: rtol 1e-4 on the tip deflection of
+    # the Raasch hook (the reference's Abaqus meshes), loaded by a shear
+    # traction on its tip edge (distribloads over L2 boundary elements)
+    d = PB.raasch_hook(k)
+    P = _problem(O.T3FF, d)
+    K = P.assemble_scipy("K", O.DROP_ZEROS)
+    F = O.distribloads(d["xyz"], d["edges"], d["dofnums"], 2, 3, d["traction"], K.shape[0])
+    # the traction integrates to 0.05 times the 20-unit tip edge
+    assert abs(F.sum() - 1.0) <= 1e-12
+    v = PB.tip_deflection_percent(K, F, d)
+    assert abs(v - PB.RAASCH_REF[k]) <= 1e-4 * abs(PB.RAASCH_REF[k])
+    # measured: within 6e-11 (the alternate Q4toT3 split is off by up to 1.4e-5)
+    assert abs(v - PB.RAASCH_REF[k]) <= 1e-9 * abs(PB.RAASCH_REF[k])
