@@ -644,15 +644,29 @@ int fs_stiffness_copy(fs_ctx *c, int precision, int64_t nrows, int64_t *colptr, 
         FS_TRY(dalloc(c, &c->stage64, need));
         c->stage_cap = need;
     }
-    // the pattern (1-based) goes out on the copy stream while the kernels run
+    // the pattern (1-based) goes out on the copy stream while the kernels run;
+    // the row indices are widened in chunks on the context stream, each
+    // chunk's copy starting as soon as it is widened, so the host link is
+    // busy from the first chunk on (a single widening pass ahead of one copy
+    // left the link idle for its whole duration)
+    int64_t *sp = c->stage64, *sr = c->stage64 + n + 1;
+    k_plus_one_i64<<<(unsigned)((n + 1 + 255) / 256), 256, 0, c->stream>>>(n + 1, P.rowptr, sp);
+    FS_CUDA(c, cudaGetLastError());
     FS_CUDA(c, cudaEventRecord(c->copy_ev[0], c->stream));
     FS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->copy_ev[0], 0));
-    int64_t *sp = c->stage64, *sr = c->stage64 + n + 1;
-    k_plus_one_i64<<<(unsigned)((n + 1 + 255) / 256), 256, 0, c->copy_stream>>>(n + 1, P.rowptr, sp);
-    if (nnz) k_plus_one_i32<<<(unsigned)((nnz + 255) / 256), 256, 0, c->copy_stream>>>(nnz, P.colidx, sr);
-    FS_CUDA(c, cudaGetLastError());
     FS_CUDA(c, cudaMemcpyAsync(colptr, sp, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, c->copy_stream));
-    if (nnz) FS_CUDA(c, cudaMemcpyAsync(rowval, sr, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, c->copy_stream));
+    const int64_t CHUNK = (int64_t)1 << 22;  // 32 MB of 64-bit row indices
+    for (int64_t k0 = 0; k0 < nnz; k0 += CHUNK) {
+        const int64_t len = nnz - k0 < CHUNK ? nnz - k0 : CHUNK;
+        k_plus_one_i32<<<(unsigned)((len + 255) / 256), 256, 0, c->stream>>>(len, P.colidx + k0, sr + k0);
+        FS_CUDA(c, cudaGetLastError());
+        // a wait takes the event's latest record at the time of the call, so
+        // one event serves every chunk
+        FS_CUDA(c, cudaEventRecord(c->copy_ev[0], c->stream));
+        FS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->copy_ev[0], 0));
+        FS_CUDA(c, cudaMemcpyAsync(rowval + k0, sr + k0, sizeof(int64_t) * len, cudaMemcpyDeviceToHost,
+                                   c->copy_stream));
+    }
     FS_CUDA(c, cudaEventRecord(c->copy_ev[1], c->copy_stream));
     // values: element kernel and gather on the context stream, then their copy
     int64_t got = 0;
