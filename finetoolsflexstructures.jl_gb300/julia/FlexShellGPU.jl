@@ -317,18 +317,20 @@ function gpu_distribloads(self::FEMMBase, assembler::AbstractSysvecAssembler, ge
     rule = nen == 3 ? ir.npts : ir.order
     conn = collect(reinterpret(Int, fes.conn))
     xyz = geom.values
+    # an L2 set (meshboundary edges) goes in as the library's two-node mesh type
+    etype = nen == 2 ? FS_COROTBEAM : (nen == 3 ? FS_T3FF : FS_Q4RS)
     check(ctx, ccall((:fs_mesh_set, libflexshell), Cint,
         (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
-        ctx.h, nen == 3 ? FS_T3FF : FS_Q4RS, size(xyz, 1), xyz, count(fes), conn, C_NULL, P.dofnums))
-    npts = nen == 3 ? rule : rule^2
+        ctx.h, etype, size(xyz, 1), xyz, count(fes), conn, C_NULL, P.dofnums))
+    npts = nen == 4 ? rule^2 : rule
     pts = zeros(9, count(fes) * npts)
     check(ctx, ccall((:fs_integration_points, libflexshell), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}),
         ctx.h, rule, pts))
     force = zeros(6, size(pts, 2))
     for k in 1:size(pts, 2)
         e, j = divrem(k - 1, npts)
-        force[:, k] .= updateforce!(fi, reshape(pts[1:3, k], 1, 3), reshape(pts[4:9, k], 3, 2),
-            fes.label[e + 1], j + 1)[1:6]
+        tangents = nen == 2 ? reshape(pts[4:6, k], 3, 1) : reshape(pts[4:9, k], 3, 2)
+        force[:, k] .= updateforce!(fi, reshape(pts[1:3, k], 1, 3), tangents, fes.label[e + 1], j + 1)[1:6]
     end
     n = assembler isa SysvecAssemblerFBlock ? nfreedofs(P) : nalldofs(P)
     F = zeros(n)
