@@ -205,12 +205,111 @@ def barbero_plate(quads, n=8):
             Le = xs[k + 1] - xs[k]
             for nd in (nodes[k], nodes[k + 1]):
                 F[dof[nd, 1] - 1] += sgn * q * Le / 2
-    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, F=F, thickness=t)
+    # the same loads as the reference builds them: the L2 edges of meshboundary
+    # on y = 0 and y = ay, GaussRule(1, 2), distribloads with m = 1
+    bfes = mesh.meshboundary(conn)
+    edge_loads = [(bfes[mesh.selectelem(xyz, bfes, [-inf, inf, yy, yy, 0, 0], tol)],
+                   np.array([0, sgn * q, 0, 0, 0, 0.0])) for yy, sgn in ((0.0, 1.0), (ay, -1.0))]
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, F=F, thickness=t,
+                edge_loads=edge_loads)
 
 
 # test/test_composite_shell_statics.jl:97, test/test_composite_shell_statics_q4rs.jl:97
 BARBERO_T3_UZMAX_MM = 0.22004349767718365
 BARBERO_Q4_UZMAX_MM = 0.2278585006007462
+
+
+def barbero_example(quads, example):
+    """The layered plates of test/test_composite_shell_statics.jl and
+    test/test_composite_shell_statics_q4rs.jl solved under edge loads built as
+    the reference builds them (meshboundary, selectelem, GaussRule(1, 2),
+    distribloads with m = 1):
+
+    * "3.1x10": Barbero Example 3.1 with ten [0/90] pairs (:117-200), max w;
+    * "3.3": Barbero Example 3.3, [+45/-45/0/0/-45/+45] plies of 1 mm pulled by
+      +-200 N/mm in x on the edges x = 0 and x = ax (:234-323), max u;
+    * "p0/90", "p-45/45": a 1 m square, 50 x 50, [0/90] or [-45/+45] plies,
+      translations fixed on the boundary, a 1 MPa pressure over the surface
+      (TriRule(1) / GaussRule(2, 2), m = 2; :683-753, :774-844), min w.
+
+    Returns the mesh, dofs, plies, the edge loads (L2 connectivity, force
+    intensity) or the surface load (its rule's code and intensity), the
+    displacement component of the answer and the answer in mm."""
+    from flexshell import materials
+    if example.startswith("p"):
+        return _barbero_pressure(quads, example)
+    ax = ay = 2.0
+    n = 8
+    tol = ax / n / 100
+    inf = np.inf
+    if example == "3.1x10":
+        E1, E2, G12, nu12, G23 = 133860e6, 7706e6, 4306e6, 0.301, 2760e6
+        t = 0.010
+        angles = [0.0, 90.0] * 10
+        ply_t = t / 20
+    else:
+        E1, E2, G12, nu12, G23 = 37880e6, 9407e6, 3405e6, 0.299, 3308e6
+        angles = [45.0, -45.0, 0.0, 0.0, -45.0, 45.0]
+        ply_t = 1e-3
+        t = ply_t * 6
+    mat = materials.lamina_material(E1, E2, nu12, G12, G12, G23)
+    Dps, Dts = materials.shell_material_stiffness(mat)
+    plies = [dict(Dps=Dps, Dts=Dts, thickness=ply_t, angle=a, rho=0.0) for a in angles]
+    xy, conn = mesh.Q4block(ax, ay, n, n) if quads else mesh.T3block(ax, ay, n, n)
+    xyz = mesh.xyz3(xy)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    pin, roller = ([ax, ax, 0, 0, -inf, inf], [0, 0, 0, 0, -inf, inf]) if example == "3.1x10" else \
+        ([0, 0, 0, 0, -inf, inf], [ax, ax, 0, 0, -inf, inf])
+    fixed[mesh.selectnode(xyz, pin, tol) - 1, 0:3] = True
+    fixed[mesh.selectnode(xyz, roller, tol) - 1, 1] = True
+    bfes = mesh.meshboundary(conn)
+    fixed[np.unique(bfes) - 1, 2] = True  # connectednodes(meshboundary(fes))
+    dof, nfree = mesh.numberdofs(fixed)
+    if example == "3.1x10":
+        q = 0.1e6 * t
+        boxes = [([-inf, inf, 0, 0, 0, 0], [0, q]), ([-inf, inf, ay, ay, 0, 0], [0, -q])]
+        comp, ref = 2, (0.010650045488315574 if quads else 0.010276258430770539)
+    else:
+        q = 200e3
+        boxes = [([0, 0, -inf, inf, 0, 0], [-q, 0]), ([ax, ax, -inf, inf, 0, 0], [q, 0])]
+        comp, ref = 0, 3.3161098653904544
+    edge_loads = [(bfes[mesh.selectelem(xyz, bfes, b, tol)], np.array(f + [0, 0, 0, 0.0])) for b, f in boxes]
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, thickness=t,
+                edge_loads=edge_loads, surface_load=None, comp=comp, ref=ref, extreme="max")
+
+
+def _barbero_pressure(quads, example):
+    from flexshell import materials
+    ax = ay = 1.0
+    n = 50
+    tol = ax / n / 100
+    E1, E2, G12, nu12, G23 = 133860e6, 7706e6, 4306e6, 0.301, 2760e6
+    t = 0.010
+    angles = [0.0, 90.0] if example == "p0/90" else [-45.0, 45.0]
+    mat = materials.lamina_material(E1, E2, nu12, G12, G12, G23)
+    Dps, Dts = materials.shell_material_stiffness(mat)
+    plies = [dict(Dps=Dps, Dts=Dts, thickness=t / 2, angle=a, rho=0.0) for a in angles]
+    xy, conn = mesh.Q4block(ax, ay, n, n) if quads else mesh.T3block(ax, ay, n, n)
+    xyz = mesh.xyz3(xy)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    fixed[np.unique(mesh.meshboundary(conn)) - 1, 0:3] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    refs = {("p0/90", False): -1502.0324040447633, ("p0/90", True): -1503.4206439821,
+            ("p-45/45", False): -1176.8346659735575, ("p-45/45", True): -1177.349547131}
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, thickness=t, edge_loads=[],
+                surface_load=(2 if quads else 1, np.array([0, 0, -1.0e6, 0, 0, 0])), comp=2,
+                ref=refs[(example, quads)], extreme="min")
+
+
+def max_displacement_mm(K, F, d):
+    """K_ff u = F_f; the largest (d["extreme"] "max") or smallest ("min")
+    nodal displacement of component d["comp"], in mm."""
+    import scipy.sparse.linalg as spl
+    nf = d["nfree"]
+    u = spl.spsolve(K[:nf, :nf].tocsc(), F[:nf])
+    dc = d["dofnums"][:, d["comp"]]
+    v = np.where(dc <= nf, u[np.minimum(dc, nf) - 1], 0.0)
+    return (v.max() if d["extreme"] == "max" else v.min()) / 1e-3
 
 
 def c4_plate(n, side=1.0):

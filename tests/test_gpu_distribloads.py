@@ -161,3 +161,64 @@ def test_raasch_hook_on_gpu(k):
     assert abs(v - PB.RAASCH_REF[k]) <= 1e-9 * abs(PB.RAASCH_REF[k])
     femm.close()
     lfemm.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+def test_barbero_layered_plate_on_gpu(quads):
+    # test/test_composite_shell_statics.jl:14-97 and
+    # test/test_composite_shell_statics_q4rs.jl:14-97 (`≈`, rtol sqrt(eps)):
+    # [0/90] plate, layered stiffness and the in-plane edge loads over the
+    # boundary's L2 elements, all from the GPU
+    import scipy.sparse.linalg as spl
+    d = PB.barbero_plate(quads)
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    dchi.nfreedofs = d["nfree"]
+    g = F.laminate(d["plies"])
+    femm = (F.FEMMShellQ4RSComp if quads else F.FEMMShellT3FFComp)(d["conn"], g)
+    femm.associategeometry(geom0)
+    K = femm.stiffness(geom0, None, None, dchi)
+    Fg = np.zeros(dchi.nalldofs())
+    for edges, f in d["edge_loads"]:
+        lfemm = F.FEMMBase(F.IntegDomain(edges, F.GaussRule(1, 2)))
+        Fg += F.distribloads(lfemm, geom0, dchi, F.ForceIntensity(f), 1)
+        lfemm.close()
+    assert _rel(Fg, d["F"]) <= 1e-12
+    nf = d["nfree"]
+    u = spl.spsolve(K[:nf, :nf].tocsc(), Fg[:nf])
+    dz = d["dofnums"][:, 2]
+    uz = np.where(dz <= nf, u[np.minimum(dz, nf) - 1], 0.0)
+    ref = PB.BARBERO_Q4_UZMAX_MM if quads else PB.BARBERO_T3_UZMAX_MM
+    assert abs(uz.max() / 1e-3 - ref) <= 1.5e-8 * ref
+    femm.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+@pytest.mark.parametrize("example", ["3.1x10", "3.3", "p0/90", "p-45/45"])
+def test_barbero_examples_on_gpu(quads, example):
+    # test/test_composite_shell_statics.jl:117-200, :234-323, :683-753,
+    # :774-844 and the Q4RS file's same tests (`≈`, rtol sqrt(eps)): twenty
+    # [0/90] plies, the [+45/-45/0/0/-45/+45] layup pulled in x, or [0/90] and
+    # [-45/+45] under pressure; stiffness and loads from the GPU
+    d = PB.barbero_example(quads, example)
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    dchi.nfreedofs = d["nfree"]
+    femm = (F.FEMMShellQ4RSComp if quads else F.FEMMShellT3FFComp)(d["conn"], F.laminate(d["plies"]))
+    femm.associategeometry(geom0)
+    K = femm.stiffness(geom0, None, None, dchi)
+    Fg = np.zeros(dchi.nalldofs())
+    for edges, f in d["edge_loads"]:
+        lfemm = F.FEMMBase(F.IntegDomain(edges, F.GaussRule(1, 2)))
+        Fg += F.distribloads(lfemm, geom0, dchi, F.ForceIntensity(f), 1)
+        lfemm.close()
+    if d["surface_load"] is not None:
+        rule, f = d["surface_load"]
+        lfemm = F.FEMMBase(F.IntegDomain(d["conn"], F.GaussRule(2, rule) if quads else F.TriRule(rule)))
+        Fg = F.distribloads(lfemm, geom0, dchi, F.ForceIntensity(f), 2)
+        lfemm.close()
+    v = PB.max_displacement_mm(K, Fg, d)
+    assert abs(v - d["ref"]) <= 1.5e-8 * abs(d["ref"])
+    femm.close()

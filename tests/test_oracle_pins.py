@@ -101,6 +101,29 @@ def test_barbero_composite_plate(quads):
     uz = np.where(dz <= nf, u[np.minimum(dz, nf) - 1], 0.0)
     ref = PB.BARBERO_Q4_UZMAX_MM if quads else PB.BARBERO_T3_UZMAX_MM
     assert abs(uz.max() / 1e-3 - ref) <= 1.5e-8 * ref
+    # the edge loads as the reference forms them (meshboundary, GaussRule(1, 2), m = 1)
+    Fd = sum(O.distribloads(d["xyz"], e, d["dofnums"], 2, 1, f, K.shape[0]) for e, f in d["edge_loads"])
+    assert np.abs(Fd - d["F"]).max() <= 1e-12 * np.abs(d["F"]).max()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+@pytest.mark.parametrize("example", ["3.1x10", "3.3", "p0/90", "p-45/45"])
+def test_barbero_examples_with_edge_loads(quads, example):
+    # test/test_composite_shell_statics.jl:117-200, :234-323, :683-753,
+    # :774-844 and the Q4RS file's same tests: `≈` (rtol sqrt(eps)) on the
+    # extreme displacement
+    d = PB.barbero_example(quads, example)
+    A, B, D, H, md, mi = O.laminate(d["plies"])
+    grp = dict(A=A, B=B, D=D, H=H, csmat=np.eye(3), thickness=d["thickness"], mass=md, moi=mi)
+    P = O.Problem(O.Q4RSCOMP if quads else O.T3FFCOMP, d["xyz"], d["conn"], d["dofnums"], groups=[grp])
+    P.compute_normals()
+    K = P.assemble_scipy("K", O.DROP_ZEROS)
+    Fd = sum(O.distribloads(d["xyz"], e, d["dofnums"], 2, 1, f, K.shape[0]) for e, f in d["edge_loads"])
+    if d["surface_load"] is not None:
+        rule, f = d["surface_load"]
+        Fd = O.distribloads(d["xyz"], d["conn"], d["dofnums"], rule, 2, f, K.shape[0])
+    v = PB.max_displacement_mm(K, Fd, d)
+    assert abs(v - d["ref"]) <= 1.5e-8 * abs(d["ref"])
 
 
 def test_laminate_barbero_example_5_6():
