@@ -228,6 +228,11 @@ def barbero_example(quads, example):
     * "3.1x10": Barbero Example 3.1 with ten [0/90] pairs (:117-200), max w;
     * "3.3": Barbero Example 3.3, [+45/-45/0/0/-45/+45] plies of 1 mm pulled by
       +-200 N/mm in x on the edges x = 0 and x = ax (:234-323), max u;
+    * "r+", "r-": [90/0] plies pulled (+) or pushed (-) in x on the edges
+      x = 0 and x = ax (:870-954), max or min w;
+    * "rot+", "rot-": the same plate turned into the y-z plane, (x, y, z) ->
+      (z, x, y), with the layup csys columns (0,1,0), (0,0,1), (1,0,0) and the
+      loads in z on the edges z = 0 and z = ax (:978-1075), max or min u;
     * "p0/90", "p-45/45": a 1 m square, 50 x 50, [0/90] or [-45/+45] plies,
       translations fixed on the boundary, a 1 MPa pressure over the surface
       (TriRule(1) / GaussRule(2, 2), m = 2; :683-753, :774-844), min w.
@@ -242,11 +247,19 @@ def barbero_example(quads, example):
     n = 8
     tol = ax / n / 100
     inf = np.inf
+    csmat = np.eye(3)
     if example == "3.1x10":
         E1, E2, G12, nu12, G23 = 133860e6, 7706e6, 4306e6, 0.301, 2760e6
         t = 0.010
         angles = [0.0, 90.0] * 10
         ply_t = t / 20
+    elif example.startswith("r"):
+        E1, E2, G12, nu12, G23 = 133860e6, 7706e6, 4306e6, 0.301, 2760e6
+        t = 0.010
+        angles = [90.0, 0.0]
+        ply_t = t / 2
+        if example.startswith("rot"):
+            csmat = np.array([[0, 0, 1], [1, 0, 0], [0, 1, 0.0]])
     else:
         E1, E2, G12, nu12, G23 = 37880e6, 9407e6, 3405e6, 0.299, 3308e6
         angles = [45.0, -45.0, 0.0, 0.0, -45.0, 45.0]
@@ -257,14 +270,38 @@ def barbero_example(quads, example):
     plies = [dict(Dps=Dps, Dts=Dts, thickness=ply_t, angle=a, rho=0.0) for a in angles]
     xy, conn = mesh.Q4block(ax, ay, n, n) if quads else mesh.T3block(ax, ay, n, n)
     xyz = mesh.xyz3(xy)
+    rot = example.startswith("rot")
+    if rot:
+        xyz = xyz[:, [2, 0, 1]].copy()
     fixed = np.zeros((xyz.shape[0], 6), bool)
-    pin, roller = ([ax, ax, 0, 0, -inf, inf], [0, 0, 0, 0, -inf, inf]) if example == "3.1x10" else \
-        ([0, 0, 0, 0, -inf, inf], [ax, ax, 0, 0, -inf, inf])
+    if rot:
+        pin, roller = [0, 0, 0, 0, 0, 0], [0, 0, 0, 0, ax, ax]
+    elif example == "3.1x10" or example.startswith("r"):
+        pin, roller = [ax, ax, 0, 0, -inf, inf], [0, 0, 0, 0, -inf, inf]
+    else:
+        pin, roller = [0, 0, 0, 0, -inf, inf], [ax, ax, 0, 0, -inf, inf]
     fixed[mesh.selectnode(xyz, pin, tol) - 1, 0:3] = True
     fixed[mesh.selectnode(xyz, roller, tol) - 1, 1] = True
     bfes = mesh.meshboundary(conn)
-    fixed[np.unique(bfes) - 1, 2] = True  # connectednodes(meshboundary(fes))
+    fixed[np.unique(bfes) - 1, 0 if rot else 2] = True  # connectednodes(meshboundary(fes))
     dof, nfree = mesh.numberdofs(fixed)
+    extreme = "max"
+    if example.startswith("r"):
+        lm = 1.0 if example.endswith("+") else -1.0
+        q = 0.1e6 * t * lm
+        extreme = "max" if lm > 0 else "min"
+        # the Q4RS file's values as printed there (:951-953, :1067-1069)
+        ref = lm * ((0.22785850060074 if not rot else (0.22785850060 if lm < 0 else 0.227858500600))
+                    if quads else 0.22004349767718365)
+        if rot:
+            boxes = [([0, 0, -inf, inf, ax, ax], [0, 0, q]), ([0, 0, -inf, inf, 0, 0], [0, 0, -q])]
+            comp = 0
+        else:
+            boxes = [([0, 0, -inf, inf, 0, 0], [q, 0, 0]), ([ax, ax, -inf, inf, 0, 0], [-q, 0, 0])]
+            comp = 2
+        edge_loads = [(bfes[mesh.selectelem(xyz, bfes, b, tol)], np.array(f + [0, 0, 0.0])) for b, f in boxes]
+        return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, thickness=t, csmat=csmat,
+                    edge_loads=edge_loads, surface_load=None, comp=comp, ref=ref, extreme=extreme)
     if example == "3.1x10":
         q = 0.1e6 * t
         boxes = [([-inf, inf, 0, 0, 0, 0], [0, q]), ([-inf, inf, ay, ay, 0, 0], [0, -q])]
@@ -274,8 +311,8 @@ def barbero_example(quads, example):
         boxes = [([0, 0, -inf, inf, 0, 0], [-q, 0]), ([ax, ax, -inf, inf, 0, 0], [q, 0])]
         comp, ref = 0, 3.3161098653904544
     edge_loads = [(bfes[mesh.selectelem(xyz, bfes, b, tol)], np.array(f + [0, 0, 0, 0.0])) for b, f in boxes]
-    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, thickness=t,
-                edge_loads=edge_loads, surface_load=None, comp=comp, ref=ref, extreme="max")
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, thickness=t, csmat=csmat,
+                edge_loads=edge_loads, surface_load=None, comp=comp, ref=ref, extreme=extreme)
 
 
 def _barbero_pressure(quads, example):
@@ -296,7 +333,8 @@ def _barbero_pressure(quads, example):
     dof, nfree = mesh.numberdofs(fixed)
     refs = {("p0/90", False): -1502.0324040447633, ("p0/90", True): -1503.4206439821,
             ("p-45/45", False): -1176.8346659735575, ("p-45/45", True): -1177.349547131}
-    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, thickness=t, edge_loads=[],
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, thickness=t, csmat=np.eye(3),
+                edge_loads=[],
                 surface_load=(2 if quads else 1, np.array([0, 0, -1.0e6, 0, 0, 0])), comp=2,
                 ref=refs[(example, quads)], extreme="min")
 

@@ -195,18 +195,22 @@ def test_barbero_layered_plate_on_gpu(quads):
 
 
 @pytest.mark.parametrize("quads", [False, True])
-@pytest.mark.parametrize("example", ["3.1x10", "3.3", "p0/90", "p-45/45"])
+@pytest.mark.parametrize("example", ["3.1x10", "3.3", "r+", "r-", "rot+", "rot-", "p0/90", "p-45/45"])
 def test_barbero_examples_on_gpu(quads, example):
     # test/test_composite_shell_statics.jl:117-200, :234-323, :683-753,
-    # :774-844 and the Q4RS file's same tests (`≈`, rtol sqrt(eps)): twenty
-    # [0/90] plies, the [+45/-45/0/0/-45/+45] layup pulled in x, or [0/90] and
-    # [-45/+45] under pressure; stiffness and loads from the GPU
+    # :774-844, :870-954, :978-1075 and the Q4RS file's same tests (`≈`, rtol
+    # sqrt(eps)): twenty [0/90] plies, the [+45/-45/0/0/-45/+45] layup pulled in
+    # x, [90/0] pulled and pushed, the same plate turned into the y-z plane
+    # with a rotated layup csys, or [0/90] and [-45/+45] under pressure;
+    # stiffness and loads from the GPU
     d = PB.barbero_example(quads, example)
     geom0 = F.NodalField(d["xyz"])
     dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
     dchi.dofnums = np.asfortranarray(d["dofnums"])
     dchi.nfreedofs = d["nfree"]
-    femm = (F.FEMMShellQ4RSComp if quads else F.FEMMShellT3FFComp)(d["conn"], F.laminate(d["plies"]))
+    g = F.laminate(d["plies"])
+    g.csmat[:] = list(np.asarray(d["csmat"]).flatten(order="F"))
+    femm = (F.FEMMShellQ4RSComp if quads else F.FEMMShellT3FFComp)(d["conn"], g)
     femm.associategeometry(geom0)
     K = femm.stiffness(geom0, None, None, dchi)
     Fg = np.zeros(dchi.nalldofs())

@@ -107,14 +107,14 @@ def test_barbero_composite_plate(quads):
 
 
 @pytest.mark.parametrize("quads", [False, True])
-@pytest.mark.parametrize("example", ["3.1x10", "3.3", "p0/90", "p-45/45"])
+@pytest.mark.parametrize("example", ["3.1x10", "3.3", "r+", "r-", "rot+", "rot-", "p0/90", "p-45/45"])
 def test_barbero_examples_with_edge_loads(quads, example):
     # test/test_composite_shell_statics.jl:117-200, :234-323, :683-753,
-    # :774-844 and the Q4RS file's same tests: `≈` (rtol sqrt(eps)) on the
-    # extreme displacement
+    # :774-844, :870-954, :978-1075 and the Q4RS file's same tests: `≈`
+    # (rtol sqrt(eps)) on the extreme displacement
     d = PB.barbero_example(quads, example)
     A, B, D, H, md, mi = O.laminate(d["plies"])
-    grp = dict(A=A, B=B, D=D, H=H, csmat=np.eye(3), thickness=d["thickness"], mass=md, moi=mi)
+    grp = dict(A=A, B=B, D=D, H=H, csmat=d["csmat"], thickness=d["thickness"], mass=md, moi=mi)
     P = O.Problem(O.Q4RSCOMP if quads else O.T3FFCOMP, d["xyz"], d["conn"], d["dofnums"], groups=[grp])
     P.compute_normals()
     K = P.assemble_scipy("K", O.DROP_ZEROS)
