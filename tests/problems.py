@@ -339,6 +339,75 @@ def _barbero_pressure(quads, example):
                 ref=refs[(example, quads)], extreme="min")
 
 
+def sacco_and_sandwich(quads, example):
+    """Pressure-loaded layered plates of test/test_composite_shell_statics.jl
+    (T3FFComp) and its Q4RS file (Q4RSComp), TriRule(1) / GaussRule(2, 2)
+    surface loads with m = 2:
+
+    * "sacco": [0/90] square, a = 250 mm, t = a/10, E1 = 100 GPa, E2 = E1/25,
+      simple supports by edges (:1099-1183); two answers, max w and max u
+      times 100 E2 / (q t (a/t)^4);
+    * "sandwich": Barbero Example 3.7, faces 0.7112 mm over a 19.05 mm core of
+      another material, translations fixed on the boundary (:1210-1282); max w.
+
+    Returns the problem with its list of answers (component, extreme, scale,
+    reference value)."""
+    from flexshell import materials
+    inf = np.inf
+    if example == "sacco":
+        a, n = 0.25, 8
+        E1 = 100e9
+        E2 = E1 / 25
+        mat = materials.lamina_material(E1, E2, 0.25, E2 * 0.5, E2 * 0.5, E2 * 0.2)
+        Dps, Dts = materials.shell_material_stiffness(mat)
+        t = a / 10
+        plies = [dict(Dps=Dps, Dts=Dts, thickness=t / 2, angle=ang, rho=0.0) for ang in (0.0, 90.0)]
+        q = 10.0e3
+    else:
+        a, n = 2 * 0.127, 18
+        face = materials.lamina_material(68947.57e6, 27579.03e6, 0.3, 12927.67e6, 12927.67e6, 12927.67e6)
+        core = materials.lamina_material(0.068948e6, 0.068948e6, 0.0, 0.068948e6, 209.6e6, 82.737e6)
+        tf, tc = 0.7112e-3, 19.05e-3
+        plies = []
+        for m_, tp in ((face, tf), (core, tc), (face, tf)):
+            Dps, Dts = materials.shell_material_stiffness(m_)
+            plies.append(dict(Dps=Dps, Dts=Dts, thickness=tp, angle=0.0, rho=0.0))
+        t = 2 * tf + tc
+        q = 0.689476e6
+    tol = a / n / 100
+    xy, conn = mesh.Q4block(a, a, n, n) if quads else mesh.T3block(a, a, n, n)
+    xyz = mesh.xyz3(xy)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    bnd = np.unique(mesh.meshboundary(conn)) - 1
+    if example == "sacco":
+        for box, comps in (([0, 0, -inf, inf, 0, 0], [1, 3]), ([a, a, -inf, inf, 0, 0], [1, 3]),
+                           ([-inf, inf, 0, 0, 0, 0], [0, 4]), ([-inf, inf, a, a, 0, 0], [0, 4])):
+            fixed[np.ix_(mesh.selectnode(xyz, box, tol) - 1, comps)] = True
+        fixed[bnd, 2] = True
+        sc = 100 * E2 / (q * t * (a / t) ** 4)
+        answers = [(2, "max", sc, 2.0134037916683 if quads else 1.9529295928169146),
+                   (0, "max", sc, 0.128716225 if quads else 0.12375916912652352)]
+    else:
+        fixed[bnd, 0:3] = True
+        answers = [(2, "max", 1e3, 3.201455454 if quads else 3.2024601774900674)]
+    dof, nfree = mesh.numberdofs(fixed)
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, plies=plies, thickness=t, csmat=np.eye(3),
+                edge_loads=[], surface_load=(2 if quads else 1, np.array([0, 0, q, 0, 0, 0])), answers=answers)
+
+
+def extreme_displacements(K, F, d):
+    """K_ff u = F_f; (value, reference) of every answer of d["answers"]."""
+    import scipy.sparse.linalg as spl
+    nf = d["nfree"]
+    u = spl.spsolve(K[:nf, :nf].tocsc(), F[:nf])
+    out = []
+    for comp, ext, scale, ref in d["answers"]:
+        dc = d["dofnums"][:, comp]
+        v = np.where(dc <= nf, u[np.minimum(dc, nf) - 1], 0.0)
+        out.append(((v.max() if ext == "max" else v.min()) * scale, ref))
+    return out
+
+
 def max_displacement_mm(K, F, d):
     """K_ff u = F_f; the largest (d["extreme"] "max") or smallest ("min")
     nodal displacement of component d["comp"], in mm."""

@@ -226,3 +226,25 @@ def test_barbero_examples_on_gpu(quads, example):
     v = PB.max_displacement_mm(K, Fg, d)
     assert abs(v - d["ref"]) <= 1.5e-8 * abs(d["ref"])
     femm.close()
+
+
+@pytest.mark.parametrize("quads", [False, True])
+@pytest.mark.parametrize("example", ["sacco", "sandwich"])
+def test_sacco_and_sandwich_plates_on_gpu(quads, example):
+    # test/test_composite_shell_statics.jl:1099-1183, :1210-1282 and the Q4RS
+    # file's same tests (`≈`, rtol sqrt(eps)): stiffness and pressure from the GPU
+    d = PB.sacco_and_sandwich(quads, example)
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    dchi.nfreedofs = d["nfree"]
+    femm = (F.FEMMShellQ4RSComp if quads else F.FEMMShellT3FFComp)(d["conn"], F.laminate(d["plies"]))
+    femm.associategeometry(geom0)
+    K = femm.stiffness(geom0, None, None, dchi)
+    rule, f = d["surface_load"]
+    lfemm = F.FEMMBase(F.IntegDomain(d["conn"], F.GaussRule(2, rule) if quads else F.TriRule(rule)))
+    Fg = F.distribloads(lfemm, geom0, dchi, F.ForceIntensity(f), 2)
+    lfemm.close()
+    for v, ref in PB.extreme_displacements(K, Fg, d):
+        assert abs(v - ref) <= 1.5e-8 * abs(ref)
+    femm.close()

@@ -126,6 +126,23 @@ def test_barbero_examples_with_edge_loads(quads, example):
     assert abs(v - d["ref"]) <= 1.5e-8 * abs(d["ref"])
 
 
+@pytest.mark.parametrize("quads", [False, True])
+@pytest.mark.parametrize("example", ["sacco", "sandwich"])
+def test_sacco_and_sandwich_plates(quads, example):
+    # test/test_composite_shell_statics.jl:1099-1183, :1210-1282 and the Q4RS
+    # file's same tests: `≈` (rtol sqrt(eps))
+    d = PB.sacco_and_sandwich(quads, example)
+    A, B, D, H, md, mi = O.laminate(d["plies"])
+    grp = dict(A=A, B=B, D=D, H=H, csmat=d["csmat"], thickness=d["thickness"], mass=md, moi=mi)
+    P = O.Problem(O.Q4RSCOMP if quads else O.T3FFCOMP, d["xyz"], d["conn"], d["dofnums"], groups=[grp])
+    P.compute_normals()
+    K = P.assemble_scipy("K", O.DROP_ZEROS)
+    rule, f = d["surface_load"]
+    Fd = O.distribloads(d["xyz"], d["conn"], d["dofnums"], rule, 2, f, K.shape[0])
+    for v, ref in PB.extreme_displacements(K, Fd, d):
+        assert abs(v - ref) <= 1.5e-8 * abs(ref)
+
+
 def test_laminate_barbero_example_5_6():
     # test/test_composite_layup.jl:359-389: one ply at -55 degrees, given Dps
     Dps = np.array([[20.874, 3.260, 0], [3.260, 11.898, 0], [0, 0, 3.789]])
