@@ -368,6 +368,26 @@ class _FEMMShell:
                                  loc[k].reshape(1, 3))
         return idat
 
+    def fieldfromintegpoints(self, geom0, u, quantity, component, outputcsys=None):
+        """fieldfromintegpoints(femm, geom0, u, quantity, component; outputcsys)
+        of FinEtools with its default node-value method (inverse distance): each
+        node's value is the average of the integration-point values of the
+        elements that hold it, weighted by the inverse squared distance from
+        the point to the node.  component: 1-based.  Returns nnodes values
+        (zero at nodes of no element).  The points' values come from the GPU
+        (fs_resultants), the weighting runs on the host."""
+        vals = self.resultants(geom0, u, quantity, outputcsys)[:, int(component) - 1]
+        X = np.asarray(geom0.values, dtype=np.float64)
+        el, _, _, loc = self._point_locations(geom0)
+        nodes = self.conn[el] - 1                                   # npoints x nen
+        d2 = ((X[nodes] - loc[:, None, :]) ** 2).sum(axis=2)
+        w = 1.0 / d2
+        num = np.zeros(X.shape[0])
+        den = np.zeros(X.shape[0])
+        np.add.at(num, nodes.ravel(), (w * vals[:, None]).ravel())
+        np.add.at(den, nodes.ravel(), w.ravel())
+        return np.divide(num, den, out=np.zeros_like(num), where=den > 0)
+
     # -- extras ----------------------------------------------------------------
     def element_matrices(self, geom0, precision=FS_FP64):
         """All element stiffness matrices in the global basis (nelem x nd x nd)."""

@@ -150,3 +150,17 @@ def selectelem(xyz, conn, box, inflate=0.0):
     inside = np.zeros(np.asarray(xyz).shape[0] + 1, dtype=bool)
     inside[selectnode(xyz, box, inflate)] = True
     return np.nonzero(inside[np.asarray(conn, dtype=np.int64)].all(1))[0]
+
+
+def mergenodes(xyz, conn, tolerance):
+    """FinEtools mergenodes: nodes closer than ``tolerance`` to an earlier
+    node become that node; the remaining nodes keep their order.  Returns the
+    new coordinates and connectivity (1-based)."""
+    from scipy.spatial import cKDTree
+    xyz = np.asarray(xyz, dtype=np.float64)
+    rep = np.arange(xyz.shape[0])
+    for i, j in sorted(cKDTree(xyz).query_pairs(tolerance)):
+        rep[max(i, j)] = min(rep[i], rep[j])
+    keep = rep == np.arange(rep.shape[0])
+    num = np.cumsum(keep)[rep]  # 1-based number of each node's survivor
+    return xyz[keep], num[np.asarray(conn, dtype=np.int64) - 1]

@@ -98,6 +98,106 @@ def raasch_hook(k):
                 edges=edges, traction=np.array([0, 0, 0.05, 0, 0, 0.0]))
 
 
+# test/test_shell_statics.jl:530-531 (`≈`, rtol sqrt(eps)): min and max w
+LE5_REF = (-0.01568028415401719, 0.015401663810490641)
+
+
+def le5_cantilever():
+    """LE5 Z-section cantilever, test/test_shell_statics.jl:441-531: the
+    reference's Abaqus triangles (tests/golden/raasch_hook.npz), translations
+    clamped at x = 0, opposite point forces of 0.6 MN in z at (10, 1, 0) and
+    (10, -1, 0) (FESetP1 with PointRule: the force itself at the node)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "raasch_hook.npz"))
+    xyz, conn = g["xyz_le5"], g["conn_le5"]
+    tol = 0.1 / 1000
+    inf = np.inf
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    fixed[mesh.selectnode(xyz, [0, 0, -inf, inf, -inf, inf], tol) - 1, 0:3] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(210e9, 0.3))
+    F = np.zeros(int(dof.max()))
+    for y, fz in ((1.0, 0.6e6), (-1.0, -0.6e6)):
+        nl = mesh.selectnode(xyz, [10, 10, y, y, 0, 0], tol) - 1
+        assert nl.size == 1
+        F[dof[nl[0], 2] - 1] += fz
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=0.1,
+                material=dict(Dps=Dps, Dt=Dt, rho=0.0), stab_c=0.2, F=F)
+
+
+# test/test_shell_statics.jl:690-727: (min, max) of the nodal fields of the
+# moments, membrane forces and shears (rtol 0.01)
+VAULT_REF = {"moment": [(-1520.6449167366522, 14.067403309095397), (-73.8262145426215, 425.93651541819503),
+                        (-0.005341121492547284, 953.0929383629322)],
+             "membrane": [(-306.83173146926623, 309.5860993742647), (-1011.4832977998705, 2167.0403478574167),
+                          (-687.3500043290137, 69.38703021678862)],
+             "shear": [(-13.784764125688811, 21.165312065421237), (-7.4216963152916255, 25.679801383392967)]}
+
+
+def barrel_vault():
+    """Irregular barrel vault, test/test_shell_statics.jl:578-727: the
+    reference's Abaqus triangles (tests/golden/raasch_hook.npz) with coincident
+    nodes merged (mergenodes, t/10), E = 3e6, nu = 0, t = 3, stab 0.2,
+    drilling scale 0.1, gravity-like load -0.625 in x (TriRule(3), m = 3).
+    Also returns the cylindrical output csys of the resultants."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "raasch_hook.npz"))
+    t, R, L = 3.0, 300.0, 600.0
+    xyz, conn = mesh.mergenodes(g["xyz_vault"], g["conn_vault"], t / 10)
+    tol = t / 20
+    inf = np.inf
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    for box, comps in (([-inf, inf, -inf, inf, 0, 0], [0, 1]), ([-inf, inf, -inf, inf, L / 2, L / 2], [2, 3, 4]),
+                       ([-inf, inf, 0, 0, -inf, inf], [1, 3, 5])):
+        fixed[np.ix_(mesh.selectnode(xyz, box, tol) - 1, comps)] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(3.0e6, 0.0))
+
+    def cylindrical(XYZ, tangents, feid, qpid):
+        r = -np.asarray(XYZ, dtype=np.float64).ravel().copy()
+        r[2] = 0.0
+        e3 = r / np.linalg.norm(r)
+        e2 = np.array([0.0, 0.0, 1.0])
+        return np.column_stack([np.cross(e2, e3), e2, e3])
+
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=t,
+                material=dict(Dps=Dps, Dt=Dt, rho=0.0), stab_c=0.2, drill_scale=0.1,
+                load=np.array([-0.625, 0, 0, 0, 0, 0.0]), ocsys=cylindrical)
+
+
+def nodal_displacements(K, F, d):
+    """K_ff u = F_f scattered back to the (nnodes, 6) nodal values."""
+    import scipy.sparse.linalg as spl
+    nf = d["nfree"]
+    u = spl.spsolve(K[:nf, :nf].tocsc(), F[:nf])
+    dof = d["dofnums"]
+    return np.where(dof <= nf, u[np.minimum(dof, nf) - 1], 0.0)
+
+
+def inverse_distance_field(xyz, conn, vals):
+    """Nodal field of one value per T3 element (its centroid), FinEtools'
+    inverse-distance node values (weights 1/|x_node - x_point|^2)."""
+    loc = xyz[conn - 1].mean(axis=1)
+    num = np.zeros(xyz.shape[0])
+    den = np.zeros(xyz.shape[0])
+    for e in range(conn.shape[0]):
+        for a in conn[e] - 1:
+            w = 1.0 / ((xyz[a] - loc[e]) ** 2).sum()
+            num[a] += w * vals[e]
+            den[a] += w
+    return num / den
+
+
+def w_extremes(K, F, d):
+    """K_ff u = F_f; (min, max) of the nodal z displacements."""
+    import scipy.sparse.linalg as spl
+    nf = d["nfree"]
+    u = spl.spsolve(K[:nf, :nf].tocsc(), F[:nf])
+    dz = d["dofnums"][:, 2]
+    w = np.where(dz <= nf, u[np.minimum(dz, nf) - 1], 0.0)
+    return w.min(), w.max()
+
+
 def tip_deflection_percent(K, F, prob):
     """K_ff u = F_f; the probe's z deflection in percent of 5.02."""
     import scipy.sparse.linalg as spl

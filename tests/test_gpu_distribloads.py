@@ -248,3 +248,44 @@ def test_sacco_and_sandwich_plates_on_gpu(quads, example):
     for v, ref in PB.extreme_displacements(K, Fg, d):
         assert abs(v - ref) <= 1.5e-8 * abs(ref)
     femm.close()
+
+
+def test_le5_z_cantilever_on_gpu():
+    # test/test_shell_statics.jl:525-531 (`≈`, rtol sqrt(eps)): T3FF stiffness
+    # of the reference's Z-section mesh from the GPU
+    d = PB.le5_cantilever()
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    femm = F.FEMMShellT3FF(d["conn"], d["thickness"], F.materials.MatDeforElastIso(210e9, 0.3),
+                           stab_fun=d["stab_c"])
+    femm.associategeometry(geom0)
+    K = femm.stiffness(geom0, None, None, dchi)
+    for v, ref in zip(PB.w_extremes(K, d["F"], d), PB.LE5_REF):
+        assert abs(v - ref) <= 1.5e-8 * abs(ref)
+    femm.close()
+
+
+def test_barrel_vault_resultant_fields_on_gpu():
+    # test/test_shell_statics.jl:578-727 (rtol 0.01): stiffness, load,
+    # resultants at the integration points in the cylindrical output csys from
+    # the GPU; fieldfromintegpoints' inverse-distance node values on the host
+    d = PB.barrel_vault()
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    dchi.nfreedofs = d["nfree"]
+    femm = F.FEMMShellT3FF(d["conn"], d["thickness"], F.materials.MatDeforElastIso(3.0e6, 0.0),
+                           stab_fun=d["stab_c"])
+    femm.drilling_stiffness_scale = d["drill_scale"]
+    femm.associategeometry(geom0)
+    K = femm.stiffness(geom0, None, None, dchi)
+    lfemm = F.FEMMBase(F.IntegDomain(d["conn"], F.TriRule(3)))
+    Fg = F.distribloads(lfemm, geom0, dchi, F.ForceIntensity(d["load"]), 3)
+    lfemm.close()
+    U = PB.nodal_displacements(K, Fg, d)
+    for name, refs in PB.VAULT_REF.items():
+        for nc, (rmin, rmax) in enumerate(refs):
+            f = femm.fieldfromintegpoints(geom0, U, name, nc + 1, outputcsys=d["ocsys"])
+            assert abs(f.min() - rmin) <= 0.01 * abs(rmin) and abs(f.max() - rmax) <= 0.01 * abs(rmax)
+    femm.close()

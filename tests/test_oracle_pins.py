@@ -196,3 +196,34 @@ def test_raasch_hook_t3ff_edge_load(k):
     assert abs(v - PB.RAASCH_REF[k]) <= 1e-4 * abs(PB.RAASCH_REF[k])
     # measured: within 6e-11 (the alternate Q4toT3 split is off by up to 1.4e-5)
     assert abs(v - PB.RAASCH_REF[k]) <= 1e-9 * abs(PB.RAASCH_REF[k])
+
+
+def test_le5_z_cantilever_t3ff():
+    # test/test_shell_statics.jl:525-531: `≈` (rtol sqrt(eps)) on the extreme
+    # transverse displacements of the Z-section cantilever (reference mesh)
+    d = PB.le5_cantilever()
+    P = _problem(O.T3FF, d)
+    K = P.assemble_scipy("K", O.DROP_ZEROS)
+    for v, ref in zip(PB.w_extremes(K, d["F"], d), PB.LE5_REF):
+        assert abs(v - ref) <= 1.5e-8 * abs(ref)
+
+
+def test_barrel_vault_resultant_fields():
+    # test/test_shell_statics.jl:690-727 (rtol 0.01): extremes of the nodal
+    # fields (inverse-distance node values) of the moments, membrane forces
+    # and shears at the integration points, in the cylindrical output csys;
+    # measured within 8.2e-3 (the 1/distance weighting misses by up to 83 %)
+    d = PB.barrel_vault()
+    P = O.Problem(O.T3FF, d["xyz"], d["conn"], d["dofnums"], thickness=d["thickness"],
+                  material=d["material"], stab_c=d["stab_c"], drill_scale=d["drill_scale"])
+    P.compute_normals()
+    K = P.assemble_scipy("K", O.DROP_ZEROS)
+    F = O.distribloads(d["xyz"], d["conn"], d["dofnums"], 3, 3, d["load"], K.shape[0])
+    U = PB.nodal_displacements(K, F, d)
+    loc = d["xyz"][d["conn"] - 1].mean(axis=1)
+    cs = np.stack([d["ocsys"](loc[e].reshape(1, 3), None, e + 1, 1) for e in range(loc.shape[0])])
+    for name, q in (("moment", O.RES_MOMENT), ("membrane", O.RES_MEMBRANE), ("shear", O.RES_SHEAR)):
+        out = P.resultants(U, q, cs)
+        for nc, (rmin, rmax) in enumerate(PB.VAULT_REF[name]):
+            f = PB.inverse_distance_field(d["xyz"], d["conn"], out[:, nc])
+            assert abs(f.min() - rmin) <= 0.01 * abs(rmin) and abs(f.max() - rmax) <= 0.01 * abs(rmax)
