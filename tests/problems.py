@@ -188,6 +188,74 @@ def inverse_distance_field(xyz, conn, vals):
     return num / den
 
 
+# test/test_composite_shell_dynamics.jl:93-104 and :192-203 (norm of the
+# difference below 1e-3 of the norm)
+PETYT_REF = [21.822774909379287, 54.52203720717488, 54.60475772077202, 86.5480437899711,
+             108.65349048567792, 108.78050954575491, 138.29506871044424, 140.89370172063866]
+
+
+def petyt_plate():
+    """Simply supported square plate of Petyt 9.2,
+    test/test_composite_shell_dynamics.jl:19-104 (T3FF) and :108-203 (T3FFComp,
+    four isotropic plies at +-45 degrees): 1 m, 8 x 8 T3, E = 1 GPa,
+    nu = 0.396, rho = 2, t = 1 mm, translations fixed on the boundary."""
+    E, nu, rho, t = 1.0e9, 0.396, 2.0, 1.0e-3
+    xy, conn = mesh.T3block(1.0, 1.0, 8, 8)
+    xyz = mesh.xyz3(xy)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    fixed[np.unique(mesh.meshboundary(conn)) - 1, 0:3] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, nu, rho))
+    plies = [dict(Dps=Dps, Dts=Dt, thickness=t / 4, angle=a, rho=rho) for a in (45.0, -45.0, 45.0, -45.0)]
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=t,
+                material=dict(Dps=Dps, Dt=Dt, rho=rho), plies=plies, E=E, nu=nu, rho=rho)
+
+
+# test/test_composite_shell_dynamics.jl:432-443 (norm of the difference below 1e-13)
+NAYAK_REF = [0.04571652264814249, 0.10096323319412286, 0.11467782865238098, 0.16264669289730896,
+             0.18683613787902217, 0.20655080934826295, 0.23954509827380233, 0.2476225295798577,
+             0.2718218525817157]
+NAYAK_CASES = [(10, (1, 2, 3)), (3, (2, -1, 3)), (5, (-1, -2, 3)), (4, (-2, 1, 3))]
+
+
+def cartesian_csys(axes):
+    """CompositeLayupModule.cartesian_csys: column j is sign(axes[j]) times
+    the unit vector of axis |axes[j]| (src/CompositeLayupModule.jl:26-40)."""
+    cs = np.zeros((3, 3))
+    for j, a in enumerate(axes):
+        cs[abs(a) - 1, j] = np.sign(a)
+    return cs
+
+
+def nayak_plate(nplies, axes):
+    """Nayak 4.3 orthotropic plate, test/test_composite_shell_dynamics.jl:353-443:
+    100 mm, 9 x 9 T3, t = ax/10 in nplies equal 0-degree plies, layup csys
+    cartesian_csys(axes), translations fixed on the boundary."""
+    from flexshell import materials
+    ax = 0.1
+    rho = 1500.0
+    mat = materials.lamina_material(rho, 143.52e9, 75.38e9, 0.44, 42.03e9, 25.56e9, 42.65e9)
+    Dps, Dts = materials.shell_material_stiffness(mat)
+    t = ax / 10
+    plies = [dict(Dps=Dps, Dts=Dts, thickness=t / nplies, angle=0.0, rho=rho) for _ in range(nplies)]
+    xy, conn = mesh.T3block(ax, ax, 9, 9)
+    xyz = mesh.xyz3(xy)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    fixed[np.unique(mesh.meshboundary(conn)) - 1, 0:3] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=t, plies=plies,
+                csmat=cartesian_csys(axes), scale=t * np.sqrt(rho / 159.85e9) * 2 * np.pi)
+
+
+def lowest_frequencies(K, M, nfree, n):
+    """The n lowest natural frequencies (Hz) of the free-free blocks."""
+    import scipy.linalg as sl
+    Kf = K[:nfree, :nfree].toarray()
+    Mf = M[:nfree, :nfree].toarray()
+    w = sl.eigh(Kf, Mf, eigvals_only=True, subset_by_index=[0, n - 1])
+    return np.sqrt(np.abs(w)) / (2 * np.pi)
+
+
 def w_extremes(K, F, d):
     """K_ff u = F_f; (min, max) of the nodal z displacements."""
     import scipy.sparse.linalg as spl

@@ -289,3 +289,46 @@ def test_barrel_vault_resultant_fields_on_gpu():
             f = femm.fieldfromintegpoints(geom0, U, name, nc + 1, outputcsys=d["ocsys"])
             assert abs(f.min() - rmin) <= 0.01 * abs(rmin) and abs(f.max() - rmax) <= 0.01 * abs(rmax)
     femm.close()
+
+
+@pytest.mark.parametrize("layered", [False, True])
+def test_petyt_plate_frequencies_on_gpu(layered):
+    # test/test_composite_shell_dynamics.jl:93-104, :192-203 (|f - f_ref| <
+    # 1e-3 |f|; measured 2e-9 per frequency on the oracle): stiffness and
+    # lumped mass from the GPU
+    d = PB.petyt_plate()
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    if layered:
+        femm = F.FEMMShellT3FFComp(d["conn"], F.laminate(d["plies"]))
+    else:
+        femm = F.FEMMShellT3FF(d["conn"], d["thickness"], F.materials.MatDeforElastIso(d["E"], d["nu"], d["rho"]))
+    femm.associategeometry(geom0)
+    K = femm.stiffness(geom0, None, None, dchi)
+    M = femm.mass(geom0, dchi)
+    fs = PB.lowest_frequencies(K, M, d["nfree"], 8)
+    assert np.linalg.norm(fs - PB.PETYT_REF) < 1e-3 * np.linalg.norm(fs)
+    np.testing.assert_allclose(fs, PB.PETYT_REF, rtol=1e-8)
+    femm.close()
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_nayak_plate_frequencies_on_gpu(case):
+    # test/test_composite_shell_dynamics.jl:432-443, 457-460 (|f - f_ref| <
+    # 1e-13 on the nondimensional frequencies): layered stiffness and lumped
+    # mass from the GPU for the four layups and layup csys axes
+    nplies, axes = PB.NAYAK_CASES[case]
+    d = PB.nayak_plate(nplies, axes)
+    geom0 = F.NodalField(d["xyz"])
+    dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(d["dofnums"])
+    g = F.laminate(d["plies"])
+    g.csmat[:] = list(np.asarray(d["csmat"]).flatten(order="F"))
+    femm = F.FEMMShellT3FFComp(d["conn"], g)
+    femm.associategeometry(geom0)
+    K = femm.stiffness(geom0, None, None, dchi)
+    M = femm.mass(geom0, dchi)
+    fs = PB.lowest_frequencies(K, M, d["nfree"], 9)
+    assert np.linalg.norm(np.array(PB.NAYAK_REF) - d["scale"] * fs) < 1e-13
+    femm.close()

@@ -227,3 +227,43 @@ def test_barrel_vault_resultant_fields():
         for nc, (rmin, rmax) in enumerate(PB.VAULT_REF[name]):
             f = PB.inverse_distance_field(d["xyz"], d["conn"], out[:, nc])
             assert abs(f.min() - rmin) <= 0.01 * abs(rmin) and abs(f.max() - rmax) <= 0.01 * abs(rmax)
+
+
+@pytest.mark.parametrize("layered", [False, True])
+def test_petyt_plate_frequencies(layered):
+    # test/test_composite_shell_dynamics.jl:93-104, :192-203: the eight lowest
+    # frequencies, |f - f_ref| < 1e-3 |f| (T3FF, and T3FFComp with four
+    # isotropic plies at +-45 degrees); stiffness and lumped mass
+    d = PB.petyt_plate()
+    if layered:
+        A, B, D, H, md, mi = O.laminate(d["plies"])
+        grp = dict(A=A, B=B, D=D, H=H, csmat=np.eye(3), thickness=d["thickness"], mass=md, moi=mi)
+        P = O.Problem(O.T3FFCOMP, d["xyz"], d["conn"], d["dofnums"], groups=[grp])
+        P.compute_normals()
+    else:
+        P = O.Problem(O.T3FF, d["xyz"], d["conn"], d["dofnums"], thickness=d["thickness"],
+                      material=d["material"])
+        P.compute_normals()
+    K = P.assemble_scipy("K", O.DROP_ZEROS)
+    M = P.assemble_scipy("M", O.DROP_ZEROS)
+    fs = PB.lowest_frequencies(K, M, d["nfree"], 8)
+    assert np.linalg.norm(fs - PB.PETYT_REF) < 1e-3 * np.linalg.norm(fs)
+    # measured: each frequency within 2.1e-9
+    np.testing.assert_allclose(fs, PB.PETYT_REF, rtol=1e-8)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_nayak_plate_frequencies(case):
+    # test/test_composite_shell_dynamics.jl:432-443, 457-460: nondimensional
+    # frequencies of the orthotropic plate, |f - f_ref| < 1e-13, for the four
+    # layups (ply counts and cartesian layup csys axes) the reference runs
+    nplies, axes = PB.NAYAK_CASES[case]
+    d = PB.nayak_plate(nplies, axes)
+    A, B, D, H, md, mi = O.laminate(d["plies"])
+    grp = dict(A=A, B=B, D=D, H=H, csmat=d["csmat"], thickness=d["thickness"], mass=md, moi=mi)
+    P = O.Problem(O.T3FFCOMP, d["xyz"], d["conn"], d["dofnums"], groups=[grp])
+    P.compute_normals()
+    K = P.assemble_scipy("K", O.DROP_ZEROS)
+    M = P.assemble_scipy("M", O.DROP_ZEROS)
+    fs = PB.lowest_frequencies(K, M, d["nfree"], 9)
+    assert np.linalg.norm(np.array(PB.NAYAK_REF) - d["scale"] * fs) < 1e-13
