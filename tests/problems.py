@@ -256,6 +256,52 @@ def lowest_frequencies(K, M, nfree, n):
     return np.sqrt(np.abs(w)) / (2 * np.pi)
 
 
+# test/test_shell_statics.jl:287-291, 364-381 (rtol 1e-3): tip deflection
+# in percent of uex for n = 2, 4, 8, 16 (2n x n mesh) per parameter set
+TWIST_PARAMS = [(0.32, 1.0, 2, 0.001753248285256), (0.32, 1.0, 3, 0.005424534868469),
+                (0.0032, 1.0e-6, 2, 0.001294), (0.0032, 1.0e-6, 3, 0.005256)]
+TWIST_N = [2, 4, 8, 16]
+TWIST_REF = [39.709921740907355, 68.87306876326497, 86.01944734315117, 95.04101960524827,
+             53.10262177376127, 83.8593790803426, 94.91359387874728, 98.21549248655576,
+             48.16757753755567, 79.43420077873479, 92.54464819755955, 96.85008269135751,
+             50.577029703967334, 80.34160167730624, 92.48675665271801, 96.7096641005938]
+
+
+def twisted_beam(k, j):
+    """Twisted beam, test/test_shell_statics.jl:294-360: parameter set k,
+    mesh 2n x n with n = TWIST_N[j] (T3block 'a', twisted by 90 degrees
+    along its length), clamped at x = 0, a point force at the tip centre."""
+    t, force, direction, uex = TWIST_PARAMS[k]
+    n = TWIST_N[j]
+    E, nu, W, L = 0.29e8, 0.22, 1.1, 12.0
+    tol = W / n / 100
+    xy, conn = mesh.T3block(L, W, 2 * n, n, "a")
+    xyz = mesh.xyz3(xy)
+    a = xyz[:, 0] / L * (np.pi / 2)
+    y = xyz[:, 1] - W / 2
+    z = xyz[:, 2].copy()
+    xyz = np.column_stack([xyz[:, 0], y * np.cos(a) - z * np.sin(a), y * np.sin(a) + z * np.cos(a)])
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    fixed[mesh.selectnode(xyz, [0, 0, -np.inf, np.inf, -np.inf, np.inf], tol) - 1, :] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, nu))
+    nl = mesh.selectnode(xyz, [L, L, 0, 0, 0, 0], tol) - 1
+    assert nl.size == 1
+    F = np.zeros(int(dof.max()))
+    F[dof[nl[0], direction - 1] - 1] = force
+    return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=t,
+                material=dict(Dps=Dps, Dt=Dt, rho=0.0), stab_c=5 / 12 / 1.5, F=F,
+                probe=(nl[0], direction - 1), uex=uex, E=E, nu=nu, ref=TWIST_REF[4 * k + j])
+
+
+def twisted_tip_percent(K, d):
+    import scipy.sparse.linalg as spl
+    nf = d["nfree"]
+    u = spl.spsolve(K[:nf, :nf].tocsc(), d["F"][:nf])
+    node, comp = d["probe"]
+    return u[d["dofnums"][node, comp] - 1] / d["uex"] * 100
+
+
 def w_extremes(K, F, d):
     """K_ff u = F_f; (min, max) of the nodal z displacements."""
     import scipy.sparse.linalg as spl

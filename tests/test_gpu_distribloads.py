@@ -332,3 +332,20 @@ def test_nayak_plate_frequencies_on_gpu(case):
     fs = PB.lowest_frequencies(K, M, d["nfree"], 9)
     assert np.linalg.norm(np.array(PB.NAYAK_REF) - d["scale"] * fs) < 1e-13
     femm.close()
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_twisted_beam_on_gpu(k):
+    # test/test_shell_statics.jl:362-400 (rtol 1e-3; within 9.9e-6 on the
+    # oracle): T3FF stiffness of the twisted beams from the GPU
+    for j in range(4):
+        d = PB.twisted_beam(k, j)
+        geom0 = F.NodalField(d["xyz"])
+        dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
+        dchi.dofnums = np.asfortranarray(d["dofnums"])
+        femm = F.FEMMShellT3FF(d["conn"], d["thickness"], F.materials.MatDeforElastIso(d["E"], d["nu"]))
+        femm.associategeometry(geom0)
+        v = PB.twisted_tip_percent(femm.stiffness(geom0, None, None, dchi), d)
+        assert abs(v - d["ref"]) <= 1e-3 * abs(d["ref"])
+        assert abs(v - d["ref"]) <= 2e-5 * abs(d["ref"])
+        femm.close()
