@@ -267,15 +267,24 @@ TWIST_REF = [39.709921740907355, 68.87306876326497, 86.01944734315117, 95.041019
              50.577029703967334, 80.34160167730624, 92.48675665271801, 96.7096641005938]
 
 
-def twisted_beam(k, j):
-    """Twisted beam, test/test_shell_statics.jl:294-360: parameter set k,
-    mesh 2n x n with n = TWIST_N[j] (T3block 'a', twisted by 90 degrees
-    along its length), clamped at x = 0, a point force at the tip centre."""
+# test/test_q4rs_shell_statics.jl:360-377, the same sets on Q4block meshes
+TWIST_Q4_REF = [57.52004303100694, 82.57318302555431, 94.20131995162048, 98.37454367262973,
+                76.28227868667001, 93.90901921611645, 98.28145099724978, 99.43562910255783,
+                68.51008267652144, 90.66189189880987, 97.4223162100464, 99.27913153086936,
+                76.09971224380796, 93.00031411228612, 97.58071557550575, 99.2319932521005]
+
+
+def twisted_beam(k, j, quads=False):
+    """Twisted beam, test/test_shell_statics.jl:294-360 (T3FF, T3block 'a')
+    and test/test_q4rs_shell_statics.jl:288-355 (Q4RS, Q4block, stab
+    t^2/(t^2 + 0.05 h^2)): parameter set k, mesh 2n x n with n = TWIST_N[j],
+    twisted by 90 degrees along its length, clamped at x = 0, a point force at
+    the tip centre."""
     t, force, direction, uex = TWIST_PARAMS[k]
     n = TWIST_N[j]
     E, nu, W, L = 0.29e8, 0.22, 1.1, 12.0
     tol = W / n / 100
-    xy, conn = mesh.T3block(L, W, 2 * n, n, "a")
+    xy, conn = mesh.Q4block(L, W, 2 * n, n) if quads else mesh.T3block(L, W, 2 * n, n, "a")
     xyz = mesh.xyz3(xy)
     a = xyz[:, 0] / L * (np.pi / 2)
     y = xyz[:, 1] - W / 2
@@ -290,8 +299,9 @@ def twisted_beam(k, j):
     F = np.zeros(int(dof.max()))
     F[dof[nl[0], direction - 1] - 1] = force
     return dict(xyz=xyz, conn=conn, dofnums=dof, nfree=nfree, thickness=t,
-                material=dict(Dps=Dps, Dt=Dt, rho=0.0), stab_c=5 / 12 / 1.5, F=F,
-                probe=(nl[0], direction - 1), uex=uex, E=E, nu=nu, ref=TWIST_REF[4 * k + j])
+                material=dict(Dps=Dps, Dt=Dt, rho=0.0), stab_c=0.05 if quads else 5 / 12 / 1.5, F=F,
+                probe=(nl[0], direction - 1), uex=uex, E=E, nu=nu,
+                ref=(TWIST_Q4_REF if quads else TWIST_REF)[4 * k + j])
 
 
 def twisted_tip_percent(K, d):

@@ -334,16 +334,19 @@ def test_nayak_plate_frequencies_on_gpu(case):
     femm.close()
 
 
+@pytest.mark.parametrize("quads", [False, True])
 @pytest.mark.parametrize("k", range(4))
-def test_twisted_beam_on_gpu(k):
-    # test/test_shell_statics.jl:362-400 (rtol 1e-3; within 9.9e-6 on the
-    # oracle): T3FF stiffness of the twisted beams from the GPU
+def test_twisted_beam_on_gpu(k, quads):
+    # test/test_shell_statics.jl:362-400 and test/test_q4rs_shell_statics.jl:
+    # 358-400 (rtol 1e-3; within 9.9e-6 on the oracle): T3FF and Q4RS
+    # stiffness of the twisted beams from the GPU
     for j in range(4):
-        d = PB.twisted_beam(k, j)
+        d = PB.twisted_beam(k, j, quads)
         geom0 = F.NodalField(d["xyz"])
         dchi = F.NodalField(np.zeros((d["xyz"].shape[0], 6)))
         dchi.dofnums = np.asfortranarray(d["dofnums"])
-        femm = F.FEMMShellT3FF(d["conn"], d["thickness"], F.materials.MatDeforElastIso(d["E"], d["nu"]))
+        femm = (F.FEMMShellQ4RS if quads else F.FEMMShellT3FF)(
+            d["conn"], d["thickness"], F.materials.MatDeforElastIso(d["E"], d["nu"]), stab_fun=d["stab_c"])
         femm.associategeometry(geom0)
         v = PB.twisted_tip_percent(femm.stiffness(geom0, None, None, dchi), d)
         assert abs(v - d["ref"]) <= 1e-3 * abs(d["ref"])

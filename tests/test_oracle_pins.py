@@ -269,15 +269,16 @@ def test_nayak_plate_frequencies(case):
     assert np.linalg.norm(np.array(PB.NAYAK_REF) - d["scale"] * fs) < 1e-13
 
 
+@pytest.mark.parametrize("quads", [False, True])
 @pytest.mark.parametrize("k", range(4))
-def test_twisted_beam_t3ff(k):
-    # test/test_shell_statics.jl:362-400: rtol 1e-3 on the tip deflection of
-    # the twisted beam (thick and thin, in-plane and out-of-plane loads,
-    # four meshes each)
+def test_twisted_beam(k, quads):
+    # test/test_shell_statics.jl:362-400 (T3FF) and test/test_q4rs_shell_statics.jl:
+    # 358-400 (Q4RS): rtol 1e-3 on the tip deflection of the twisted beam
+    # (thick and thin, in-plane and out-of-plane loads, four meshes each)
     for j in range(4):
-        d = PB.twisted_beam(k, j)
-        P = _problem(O.T3FF, d)
+        d = PB.twisted_beam(k, j, quads)
+        P = _problem(O.Q4RS if quads else O.T3FF, d)
         v = PB.twisted_tip_percent(P.assemble_scipy("K", O.DROP_ZEROS), d)
         assert abs(v - d["ref"]) <= 1e-3 * abs(d["ref"])
-        # measured: all sixteen within 9.9e-6
+        # measured: all thirty-two within 9.9e-6
         assert abs(v - d["ref"]) <= 2e-5 * abs(d["ref"])
