@@ -115,7 +115,7 @@ __global__ void k_extract_diag(int64_t n, const int64_t *rowptr, const int32_t *
 
 static bool is_comp(int et) { return et == FS_T3FFCOMP || et == FS_Q4RSCOMP; }
 
-static int check_ready(fs_ctx *c, bool need_dofs = true)
+int check_ready(fs_ctx *c, bool need_dofs)
 {
     if (c->mesh.etype < 0) return set_err(c, FS_ERR_STATE, "no mesh: call fs_mesh_set first");
     if (c->mesh.etype == FS_COROTBEAM)
@@ -124,6 +124,14 @@ static int check_ready(fs_ctx *c, bool need_dofs = true)
     if (need_dofs && !c->dofs_ready) return set_err(c, FS_ERR_STATE, "no dof numbering: call fs_dofs_set first");
     if (is_comp(c->mesh.etype) && !c->mesh.groups)
         return set_err(c, FS_ERR_STATE, "layered FEMM without layups: call fs_layups_set first");
+    return FS_OK;
+}
+
+int status_to_code(fs_ctx *c, int bits)
+{
+    if (bits & DEV_SINGULAR) return set_err(c, FS_ERR_SINGULAR_METRIC, "Singular metric matrix in _gradN_e!");
+    if (bits & DEV_NEG_DRILL) return set_err(c, FS_ERR_UNSUPPORTED, "negative drilling stiffness");
+    if (bits) return set_err(c, FS_ERR_BAD_INPUT, "invalid input detected on the device");
     return FS_OK;
 }
 
@@ -187,6 +195,7 @@ int fs_ctx_create(int device, fs_ctx **out)
         delete c;
         return FS_ERR_CUDA;
     }
+    noalloc_setup(c);
     *out = c;
     return FS_OK;
 }
@@ -410,6 +419,8 @@ int fs_normals_set(fs_ctx *c, const double *normals, const uint8_t *valid)
     if (!c || !normals || !valid) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
     if (c->mesh.etype < 0) return set_err(c, FS_ERR_STATE, "no mesh: call fs_mesh_set first");
+    if (c->mesh.etype == FS_COROTBEAM)
+        return set_err(c, FS_ERR_UNSUPPORTED, "beam mesh: beams have no shell normals");
     int64_t nn = c->mesh.nnodes;
     FS_CUDA(c, cudaMemcpyAsync(c->mesh.normals, normals, sizeof(double) * 3 * nn, cudaMemcpyHostToDevice, c->stream));
     FS_TRY(round_normals(c));
@@ -428,14 +439,6 @@ int fs_normals_get(fs_ctx *c, double *normals, uint8_t *valid)
     if (normals) FS_CUDA(c, cudaMemcpyAsync(normals, c->mesh.normals, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, c->stream));
     if (valid) FS_CUDA(c, cudaMemcpyAsync(valid, c->mesh.valid, nn, cudaMemcpyDeviceToHost, c->stream));
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return FS_OK;
-}
-
-static int status_to_code(fs_ctx *c, int bits)
-{
-    if (bits & DEV_SINGULAR) return set_err(c, FS_ERR_SINGULAR_METRIC, "Singular metric matrix in _gradN_e!");
-    if (bits & DEV_NEG_DRILL) return set_err(c, FS_ERR_UNSUPPORTED, "negative drilling stiffness");
-    if (bits) return set_err(c, FS_ERR_BAD_INPUT, "invalid input detected on the device");
     return FS_OK;
 }
 

@@ -134,6 +134,10 @@ struct fs_ctx {
     // scratch
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    // device address of the allocation-free path's fixed scratch array
+    // (fs_noalloc.cu) and the error of its lookup, if it failed
+    void *noalloc_scratch = nullptr;
+    std::string noalloc_err;
     // staging for host copies
     int64_t *stage64 = nullptr;
     size_t stage_cap = 0;
@@ -220,6 +224,14 @@ int compact_zeros(fs_ctx *c, int64_t n, const int64_t *rowptr, const int32_t *co
 int exclusive_scan_i64(fs_ctx *c, const int64_t *in, int64_t *out, int64_t n, int64_t *total);
 int ensure_scratch(fs_ctx *c, size_t bytes);
 int read_status(fs_ctx *c, int *bits);
+// FS_OK when the context holds a shell mesh with parameters (and, with
+// need_dofs, a dof numbering) and its layups if layered; else the error code
+int check_ready(fs_ctx *c, bool need_dofs = true);
+// the error code and message of a kernel status word (DEV_* bits)
+int status_to_code(fs_ctx *c, int bits);
+// address of the allocation-free path's scratch array in the current CUDA
+// context, looked up when the context is created (fs_noalloc.cu)
+void noalloc_setup(fs_ctx *c);
 
 int explicit_launch_steps(fs_ctx *c, int64_t nsteps);
 

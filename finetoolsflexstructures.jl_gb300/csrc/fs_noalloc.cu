@@ -11,14 +11,14 @@
 //
 // The array is FS_NOALLOC_SCRATCH_BYTES (32 MiB) on every GPU that loads the
 // library and stays there until the process exits.  Its device address is
-// looked up once per device, on the first call made with that device
-// current; make that first call before any stream capture.  Every call
-// shares the one array and it keeps the contents of the last call: nothing
-// in it has to start at zero (each call rewrites every element slot it later
-// reads), but calls whose work overlaps on the GPU (two contexts or streams
-// at once) race on it and must be serialised by the caller.
-#include <mutex>
-
+// looked up when a context is created (fs_ctx_create, with the context's
+// device current), so the library's device code and the array are loaded
+// then, not on the first allocation-free call; that call and every later one
+// only use the stored address.  Every call shares the one array and it keeps
+// the contents of the last call: nothing in it has to start at zero (each
+// call rewrites every element slot it later reads), but calls whose work
+// overlaps on the GPU (two contexts or streams at once) race on it and must
+// be serialised by the caller.
 #include "fs_internal.cuh"
 
 #define FS_NOALLOC_SCRATCH_BYTES (32u << 20)
@@ -27,29 +27,21 @@ namespace fs {
 
 static __device__ __align__(256) unsigned char fs_noalloc_scratch[FS_NOALLOC_SCRATCH_BYTES];
 
-// device address of the array, resolved once per device
-static void *noalloc_scratch_ptr(fs_ctx *c, int *status)
+// The array's address in the CUDA context current at context creation (the
+// context every buffer of `c` lives in).  A failed lookup is recorded, not
+// fatal: only the allocation-free entry point needs the address.
+void noalloc_setup(fs_ctx *c)
 {
-    static std::mutex mu;
-    static void *addr[64] = {nullptr};
-    std::lock_guard<std::mutex> lock(mu);
-    if (c->device < 0 || c->device >= 64) {
-        *status = set_err(c, FS_ERR_UNSUPPORTED, "device index above 63");
-        return nullptr;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, fs_noalloc_scratch);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        c->noalloc_scratch = nullptr;
+        c->noalloc_err = std::string("cudaGetSymbolAddress of the scratch array: ") + cudaGetErrorString(e);
+        return;
     }
-    if (!addr[c->device]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, fs_noalloc_scratch);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            *status = set_err(c, FS_ERR_CUDA, std::string("cudaGetSymbolAddress of the scratch array: ") +
-                                                  cudaGetErrorString(e));
-            return nullptr;
-        }
-        addr[c->device] = p;
-    }
-    *status = FS_OK;
-    return addr[c->device];
+    c->noalloc_scratch = p;
+    c->noalloc_err.clear();
 }
 
 }  // namespace fs
@@ -63,10 +55,8 @@ extern "C" int fs_stiffness_values_noalloc(fs_ctx *c, int precision, int64_t nro
     FS_CUDA(c, cudaSetDevice(c->device));
     if (precision != FS_FP64 && precision != FS_MIXED && precision != FS_MIXED_COMP)
         return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
-    if (c->mesh.etype < 0 || !c->params_set || !c->dofs_ready)
-        return set_err(c, FS_ERR_STATE, "mesh, parameters and dof numbering must be set first");
-    if ((c->mesh.etype == FS_T3FFCOMP || c->mesh.etype == FS_Q4RSCOMP) && !c->mesh.groups)
-        return set_err(c, FS_ERR_STATE, "layered FEMM without layups: call fs_layups_set first");
+    // shell mesh (beams are rejected), parameters, dofs and layups
+    FS_TRY(check_ready(c));
     if (!c->normals_ready)
         return set_err(c, FS_ERR_STATE, "associategeometry! has not been called (self._associatedgeometry == true)");
     if (c->pat.n != nrows || !c->pat.rowptr)
@@ -87,14 +77,10 @@ extern "C" int fs_stiffness_values_noalloc(fs_ctx *c, int precision, int64_t nro
                  (unsigned long long)(FS_NOALLOC_SCRATCH_BYTES / per));
         return set_err(c, FS_ERR_UNSUPPORTED, msg);
     }
-    int st = FS_OK;
-    void *scratch = noalloc_scratch_ptr(c, &st);
-    if (!scratch) return st;
-    FS_TRY(launch_elements_to(c, precision, scratch));
-    FS_TRY(launch_gather_from(c, precision, scratch, vals));
+    if (!c->noalloc_scratch) return set_err(c, FS_ERR_CUDA, c->noalloc_err);
+    FS_TRY(launch_elements_to(c, precision, c->noalloc_scratch));
+    FS_TRY(launch_gather_from(c, precision, c->noalloc_scratch, vals));
     int bits = 0;
     FS_TRY(read_status(c, &bits));
-    if (bits & DEV_SINGULAR) return set_err(c, FS_ERR_SINGULAR_METRIC, "Singular metric matrix in _gradN_e!");
-    if (bits) return set_err(c, FS_ERR_BAD_INPUT, "invalid input detected on the device");
-    return FS_OK;
+    return status_to_code(c, bits);
 }

@@ -5,7 +5,7 @@
  * FinEtoolsFlexStructures.jl 3.6.4.  Every entry point is plain C (pointers
  * and sizes, no framework types) so that the Julia shim can `ccall` it; the
  * Julia methods keep the reference signatures and return the same
- * SparseMatrixCSC{Float64,Int64} (see INTEGRATION.md).
+ * SparseMatrixCSC{Float64,Int64}.
  *
  * Layouts follow Julia: geometry `nnodes x 3` column-major, dof numbers
  * `nnodes x 6` column-major and 1-based (free dofs first, as numberdofs!),
@@ -203,9 +203,11 @@ int fs_tuning_ex(const fs_ctx *ctx, int32_t *out, int n);
  * are staged in a fixed 32 MiB device array inside the library, so
  * nelem * 36 nen (nen + 1)/2 * (4 for FS_MIXED, else 8) bytes (the upper
  * node blocks of its element matrices) must fit in it (19,418 T3FF elements in FP64); larger meshes get FS_ERR_UNSUPPORTED.
- * It calls no cudaMalloc/cudaFree.  The first call on a device looks up the
- * array's address (make it before any stream capture); calls that overlap on
- * the GPU share the array and race. */
+ * It calls no cudaMalloc/cudaFree.  The array's address is looked up by
+ * fs_ctx_create (which therefore loads the library's device code and the
+ * array, with 32 MiB free, at context creation); every call shares the one
+ * array, so calls that overlap on the GPU race and must be serialised by the
+ * caller. */
 int fs_stiffness_values_noalloc(fs_ctx *ctx, int precision, int64_t nrows, double *vals,
                                 int64_t vals_len);
 /* Element matrices in the global basis (nelem x (6 nen)^2, each column-major), in

@@ -9,9 +9,9 @@ For each mesh the S4 quadrilaterals (S3R or STRI3 triangles) and
 the coordinates of the nodes they use are kept, with the nodes renumbered in
 their file order (findunconnnodes + compactnodes of the reference tests); the
 split into triangles (Q4toT3) is left to the tests.  Run from the repository
-root:
+root with the reference's test directory as the one argument:
 
-    python tests/golden/make_raasch_hook.py /root/reference/test
+    python tests/golden/make_raasch_hook.py <reference>/test
 """
 import os
 import sys
@@ -76,4 +76,6 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_raasch_hook.py <reference test directory>")
+    main(sys.argv[1])

@@ -56,7 +56,40 @@ def test_noalloc_matches_regular_entry_point(quads, precision):
         # same CSR order as the regular result (symmetric pattern: CSC == CSR)
         err = np.abs(vals - ref.data).max() / np.abs(ref.data).max()
         assert err <= TOL[precision], err
+        # both entry points run the same element and gather kernels: same bits
+        assert np.array_equal(vals, ref.data)
     femm.close()
+
+
+def test_noalloc_rejects_a_beam_mesh():
+    # a co-rotational beam context with its pattern built and shell parameters
+    # set still has no shell element kernel: rejected before any launch
+    import torch
+    from flexshell._lib import Context
+    xyz = np.asfortranarray([[0.0, 0, 0], [1.0, 0, 0], [2.0, 0, 0]])
+    conn = np.ascontiguousarray([[1, 2], [2, 3]], dtype=np.int64)
+    dof = np.asfortranarray(np.arange(1, 19, dtype=np.int64).reshape(3, 6))
+    ctx = Context(0)
+    ctx.call("fs_mesh_set", _abi.FS_COROTBEAM, 3, ptr(xyz), 2, ptr(conn), None, ptr(dof))
+    sec = (_abi.fs_beam_section * 2)()
+    arr = np.frombuffer(sec, dtype=np.float64).reshape(2, 10)
+    arr[:, 0], arr[:, 1], arr[:, 2], arr[:, 3], arr[:, 4] = 0.01, 2e-5, 1e-5, 1e-5, 2e-5
+    arr[:, 5], arr[:, 6], arr[:, 9] = np.inf, np.inf, 1.0
+    ctx.call("fs_beam_setup", sec, 2.1e11, 0.3, 7850.0)
+    nnz = ctypes.c_int64()
+    ctx.call("fs_beam_matrix", _abi.FS_BEAM_STIFFNESS, 1, 0, ctypes.c_int64(18), ctypes.byref(nnz))
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(200e9, 0.3, 7850.0))
+    ctx.call("fs_params_set", _abi.make_params(Dps, Dt, 7850.0, 0.01), None)
+    with pytest.raises(FlexShellError) as ei:
+        ctx.call("fs_normals_set", ptr(np.zeros((3, 3), order="F")), ptr(np.ones(3, np.uint8)))
+    assert ei.value.code == _abi.FS_ERR_UNSUPPORTED
+    out = torch.empty(max(nnz.value, 1), dtype=torch.float64, device="cuda:0")
+    with pytest.raises(FlexShellError) as ei:
+        ctx.call("fs_stiffness_values_noalloc", _abi.FS_FP64, ctypes.c_int64(18),
+                 ctypes.c_void_p(out.data_ptr()), ctypes.c_int64(out.numel()))
+    assert ei.value.code == _abi.FS_ERR_UNSUPPORTED
+    assert "beam" in str(ei.value)
+    ctx.close()
 
 
 def test_noalloc_rejects_meshes_beyond_the_fixed_scratch():
