@@ -9,10 +9,14 @@ rho 7850).  T3FF uses the 2,097,152 triangles of the split quads, Q4RS the
 A step is one stiffness assembly: element matrices + deterministic CSR value
 gather, on device-resident inputs with the sparsity pattern built (it depends
 only on the mesh and is built once per mesh; its time is reported apart).
-`value` is mixed-precision T3FF elements assembled per second; the FP64 path
-and Q4RS are reported beside it.  `e2e` is the same assembly through the C
-ABI from pinned host buffers: geometry and dof numbering uploaded, pattern
-rebuilt, assembled, CSC arrays (colptr, rowval, nzval) copied back.
+`value` is T3FF elements assembled per second in the compensated mixed mode
+(FS_MIXED_COMP: float element rows, Gram products accumulated error-free and
+kept as float pairs, double CSR values), the mode whose stiffness, mass and
+20 lowest layered-plate eigenvalues are all within 1e-6 of FP64; the plain
+mixed mode (FS_MIXED), the FP64 path and Q4RS are reported beside it.  `e2e`
+is the same assembly through the C ABI from pinned host buffers: geometry and
+dof numbering uploaded, pattern rebuilt, assembled, CSC arrays (colptr,
+rowval, nzval) copied back.
 """
 import argparse
 import ctypes
@@ -49,18 +53,29 @@ def params(quads):
     return _abi.make_params(Dps, Dt, RHO, THICK, quads=quads)
 
 
+# DRAM bytes (read + write) per element of one launch of each kernel of the
+# T3FF step, from ncu captures of the 512 x 512 plate (524,288 triangles; the
+# full-size launch is beyond the capture size rule): dram__bytes_read.sum +
+# dram__bytes_write.sum divided by the elements of the launch.  Source: the
+# capture named beside each figure (its summary and command are committed
+# under profiles/); the figures are scaled to the benchmark's element count,
+# traffic growing in proportion to the elements at a fixed mesh type.
+MEASURED_TRAFFIC_PER_ELEMENT = {
+    "k_t3_elements FS_MIXED": (805.0, "ncu --set full, k_t3_elements, FS_MIXED, T3FF 512^2 "
+                                      "(profiles/k_t3_elements_k_gather_t3ff_mixed_512.md)"),
+    "k_gather FS_MIXED": (1984.5, "ncu --set full, k_gather, FS_MIXED, T3FF 512^2 "
+                                  "(profiles/k_t3_elements_k_gather_t3ff_mixed_512.md)"),
+}
+
+
 def measured_traffic(kernel, nelem):
-    """DRAM bytes (read + write) of one launch of `kernel`, scaled to `nelem`
-    elements from the per-element figure of the committed ncu summary
-    (profiles/*.md lines "traffic_bytes_per_element <kernel> <value>")."""
-    import glob
-    import re
-    for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
-        for line in open(f):
-            m = re.match(r"\s*traffic_bytes_per_element\s+(\S+)\s+([0-9.eE+]+)", line)
-            if m and m.group(1) == kernel:
-                return float(m.group(2)) * nelem, os.path.basename(f)
-    return None, None
+    """DRAM bytes of one launch of `kernel` over `nelem` elements from the
+    per-element ncu figure above, and its source; (None, None) when the
+    kernel has not been captured."""
+    if kernel not in MEASURED_TRAFFIC_PER_ELEMENT:
+        return None, None
+    per, src = MEASURED_TRAFFIC_PER_ELEMENT[kernel]
+    return per * nelem, src
 
 
 def read_peaks():
@@ -119,17 +134,22 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(steps=None, budget_s=10.0, n=96):
-    """The oracle (C restatement of the reference loops, OpenMP over elements)
-    on a bounded sample: an n x n quad plate split in triangles."""
+CPU_SAMPLE_N = 256  # the CPU arms' sample: a 256 x 256 corner of the same plate construction
+
+
+def cpu_baseline(steps=None, budget_s=10.0, n=CPU_SAMPLE_N, nthreads=None):
+    """The oracle (C restatement of the reference's stiffness loop and of
+    FinEtools' COO -> sparse(I, J, V) assembly; the element loop over OpenMP
+    threads, the assembly serial as Julia's sparse) on a bounded sample of
+    the workload: an n x n plate of the same construction (jitter, wave,
+    thickness, steel) split in triangles.  nthreads None: every host core."""
     from oracle import oracle as O
     from flexshell import materials
     xyz, conn, dof = plate(n, False, seed=1)
     Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, NU, RHO))
     P = O.Problem(O.T3FF, xyz, conn, dof, thickness=THICK, material=dict(Dps=Dps, Dt=Dt, rho=RHO))
     P.compute_normals()
-    cores = os.cpu_count() or 1
-    P.assemble("K", O.KEEP_ZEROS, nthreads=cores)  # warm
+    cores = nthreads or os.cpu_count() or 1
     t0 = time.perf_counter()
     reps = 0
     times = []
@@ -144,8 +164,9 @@ def cpu_baseline(steps=None, budget_s=10.0, n=96):
             break
     el = conn.shape[0]
     return {"value": el * reps / sum(times), "unit": "elements/s", "cores": cores, "kind": "port",
-            "sample": "T3FF stiffness, %dx%d quad plate split in %d triangles, element loop + COO->CSC "
-                      "assembly, %d repetitions" % (n, n, el, reps)}, times
+            "sample": "T3FF stiffness, %dx%d corner of the plate construction (%d triangles, 1/%d of the "
+                      "1024x1024 workload), element loop + COO->CSC assembly, %d repetition(s)" % (
+                          n, n, el, (1024 // n) ** 2, reps)}, times
 
 
 def max_over_ranks(x, world, dist):
@@ -172,9 +193,8 @@ def run_reference(args):
         return 0
     from oracle import oracle as O
     O.build()
-    w = max(args.warmup, 0)
-    cpu_baseline(steps=max(w, 1), n=64)
-    cb, times = cpu_baseline(steps=args.steps, n=96)
+    cpu_baseline(steps=max(args.warmup, 1))  # untimed warm-up steps
+    cb, times = cpu_baseline(steps=args.steps)
     ms = 1e3 * float(np.mean(times))
     line = {"metric": METRIC, "value": cb["value"], "unit": "elements/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -187,6 +207,52 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def oracle_check_c2(asm, xyz, conn, dof, quads, nnz):
+    """FP64 stiffness of the full-size plate against the oracle (outside every
+    timed region): the oracle's element matrices (the reference's loop) are
+    summed into the GPU matrix's own pattern, which also checks the pattern
+    (no oracle contribution outside it, every stored entry reached), and
+    compared entrywise; the lumped mass diagonal likewise."""
+    from oracle import oracle as O
+    from flexshell import _abi, materials
+    n = asm.n
+    Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, NU, RHO))
+    P = O.Problem(O.Q4RS if quads else O.T3FF, xyz, conn, dof, thickness=THICK,
+                  material=dict(Dps=Dps, Dt=Dt, rho=RHO))
+    P.compute_normals()
+    t0 = time.perf_counter()
+    asm.stiffness(_abi.FS_FP64)
+    colptr = np.empty(n + 1, dtype=np.int64)
+    rowval = np.empty(nnz, dtype=np.int64)
+    v = np.empty(nnz)
+    asm.ctx.call("fs_matrix_copy", asm.ptr(colptr), asm.ptr(rowval), asm.ptr(v))
+    vo, touched, missing = P.stiffness_into_pattern(colptr, rowval, n=n)
+    # entrywise measures (as tests/checks.entrywise_errors), on the shared pattern
+    d = np.zeros(n)
+    cols = np.repeat(np.arange(n), np.diff(colptr))
+    diag = rowval - 1 == cols
+    d[cols[diag]] = np.abs(vo[diag])
+    dv = np.abs(v - vo)
+    mx = np.abs(vo).max()
+    den = np.sqrt(d[rowval - 1] * d[cols])
+    ok = den > 0
+    big = np.abs(vo) > 1e-12 * mx
+    out = {"elements": int(conn.shape[0]), "pattern_identical": bool(missing == 0 and touched.all()),
+           "rel_err_K_fp64_vs_oracle_max": float(dv.max() / mx),
+           "rel_err_K_fp64_vs_oracle_scaled": float((dv[ok] / den[ok]).max()),
+           "rel_err_K_fp64_vs_oracle_entrywise": float((dv[big] / np.abs(vo[big])).max()),
+           "entrywise_floor": "entries above 1e-12 max|K|; scaled: |dK_ij| / sqrt(|K_ii K_jj|)"}
+    del colptr, rowval, v, vo, touched, cols, diag, dv, den, ok, big
+    nnzd = ctypes.c_int64()
+    asm.ctx.call("fs_mass", _abi.FS_ASM_DIAG, ctypes.c_int64(n), ctypes.byref(nnzd))
+    m = np.empty(n)
+    asm.ctx.call("fs_matrix_copy", None, None, asm.ptr(m))
+    _, _, mo, _ = P.assemble("M", O.DIAG, n=n)
+    out["rel_err_M_fp64_vs_oracle_max"] = float(np.abs(m - mo).max() / np.abs(mo).max())
+    out["seconds"] = time.perf_counter() - t0
+    return out
 
 
 class Assembler:
@@ -551,6 +617,35 @@ def time_steps(asm, precision, steps, warmup, torch, stream):
     return ev0.elapsed_time(ev1) / steps, phases / steps, nnz
 
 
+def t3_bytes(nelem, nnz, nodes, precision, pairs_once):
+    """Algorithmic bytes of one launch of each kernel of the T3FF step.
+
+    Element kernel: connectivity (3 x 4), coordinates (3 x 24), double normals
+    (3 x 24; the mixed modes also their float copy, 3 x 12), validity flags
+    (3) and thickness (8) in; the 6 upper 6x6 node blocks out (4 bytes an
+    entry for FS_MIXED, 8 for a float pair or a double).  Gather: the node
+    blocks it sums (each of the 6 upper blocks once when the node-block pairs
+    are summed once, else the 9 blocks, mirrored ones included), the double
+    CSR values out, the pair lists and slots (3 x 8 per element), per node its
+    dofs, offsets, row length and row pointers, and the column map (2 bytes a
+    row position)."""
+    from flexshell import _abi
+    es = 4 if precision == _abi.FS_MIXED else 8
+    el_in = 3 * 4 + 3 * 24 + 3 * 24 + 3 + 8 + (3 * 12 if precision != _abi.FS_FP64 else 0)
+    elem = nelem * (el_in + 216 * es)
+    blocks = 216 if pairs_once else 324
+    gather = (nelem * blocks * es + nnz * 8 + nelem * 3 * 8 + nodes * (6 * 4 + 8 + 4 + 8 + 6 * 8)
+              + 2 * nnz // 6)
+    return elem, gather
+
+
+def survey_step_bytes(nelem, nnz):
+    """The minimal bytes of one T3FF stiffness assembly (the per-element
+    work model of the hot path): inputs connectivity 3 x 4, coordinates 72,
+    normals 72, flags 3 per element, and the double CSR values out."""
+    return nelem * (3 * 4 + 72 + 72 + 3) + nnz * 8
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -559,6 +654,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--n", type=int, default=1024, help="quads per side")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-oracle", action="store_true", help="skip the full-size FP64 check against the oracle")
     ap.add_argument("--no-explicit", action="store_true")
     ap.add_argument("--explicit-only", action="store_true",
                     help="only the explicit-dynamics section, on an n x n Q4RS plate for 64 x steps steps "
@@ -581,13 +677,14 @@ def main():
     if world > 1:
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
+    HEAD = _abi.FS_MIXED_COMP  # the mode behind `value`
 
     res = {}
     # --- T3FF (headline) -----------------------------------------------------
     xyz, conn, dof = plate(args.n, False)
     asm = Assembler(xyz, conn, dof, False, device=local)
     stream = torch.cuda.ExternalStream(asm.ctx.stream())
-    nnz0 = asm.stiffness(_abi.FS_MIXED)  # builds the pattern
+    nnz0 = asm.stiffness(HEAD)  # builds the pattern
     t_sym = asm.timings()[2]
     # page-locked host arrays of the end-to-end leg, allocated before the large
     # host copies of the precision checks below: freshly allocated, while the
@@ -604,29 +701,26 @@ def main():
     if world > 1:
         dist.barrier()
     # clocks sampled over every timed region of the T3FF section (the headline
-    # step, the FP64 and compensated steps and the end-to-end steps)
+    # step, the other modes' steps and the end-to-end steps)
     clocks = Clocks(local)
     clocks.__enter__()
-    ms_mixed, ph_mixed, nnz = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
-    ms_mixed = max_over_ranks(ms_mixed, world, dist)
-    tiles_mixed = asm.tiles()
-    v_mixed = asm.values(nnz)
+    ms_head, ph_head, nnz = time_steps(asm, HEAD, args.steps, args.warmup, torch, stream)
+    ms_head = max_over_ranks(ms_head, world, dist)
+    tiles_head = asm.tiles()
+    v_head = asm.values(nnz)
     ms_fp64, ph_fp64, _ = time_steps(asm, _abi.FS_FP64, args.steps, args.warmup, torch, stream)
     tiles_fp64 = asm.tiles()
     v_fp64 = asm.values(nnz)
-    err_t3 = float(np.abs(v_mixed - v_fp64).max() / np.abs(v_fp64).max())
-    fro_t3 = float(np.linalg.norm(v_mixed - v_fp64) / np.linalg.norm(v_fp64))
-    del v_mixed
-    ms_comp, ph_comp, _ = time_steps(asm, _abi.FS_MIXED_COMP, args.steps, args.warmup, torch, stream)
-    v_comp = asm.values(nnz)
-    err_t3c = float(np.abs(v_comp - v_fp64).max() / np.abs(v_fp64).max())
-    del v_comp, v_fp64
-    res["t3"] = dict(ms_mixed=ms_mixed, ms_fp64=ms_fp64, ph_mixed=ph_mixed, ph_fp64=ph_fp64, nnz=nnz,
-                     err=err_t3, fro=fro_t3, t_sym=t_sym, nelem=conn.shape[0],
-                     ms_comp=ms_comp, ph_comp=ph_comp, err_comp=err_t3c,
-                     tiles={"mixed": tiles_mixed, "fp64": tiles_fp64})
+    err_head = float(np.abs(v_head - v_fp64).max() / np.abs(v_fp64).max())
+    fro_head = float(np.linalg.norm(v_head - v_fp64) / np.linalg.norm(v_fp64))
+    del v_head
+    ms_mx, ph_mx, _ = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
+    tiles_mx = asm.tiles()
+    v_mx = asm.values(nnz)
+    err_mx = float(np.abs(v_mx - v_fp64).max() / np.abs(v_fp64).max())
+    del v_mx, v_fp64
 
-    # --- e2e through the C ABI from pinned host buffers (T3FF, mixed) ------------
+    # --- e2e through the C ABI from pinned host buffers (T3FF, headline mode) ---
     P = asm.ptr
 
     def e2e_step():
@@ -634,7 +728,7 @@ def main():
         asm.ctx.call("fs_dofs_set", P(h_dof))
         k = ctypes.c_int64()
         asm.ctx.call("fs_pattern", asm.n, ctypes.byref(k))
-        asm.ctx.call("fs_stiffness_copy", _abi.FS_MIXED, asm.n, P(h_colptr), P(h_rowval), P(h_nzval))
+        asm.ctx.call("fs_stiffness_copy", HEAD, asm.n, P(h_colptr), P(h_rowval), P(h_nzval))
 
     for _ in range(args.warmup):
         e2e_step()
@@ -651,6 +745,13 @@ def main():
     h2d = (3 * nn) * 8 + (6 * nn) * 8
     d2h = (asm.n + 1) * 8 + nnz * 8 + nnz * 8
     del h_colptr, h_rowval, h_nzval
+    oracle_t3 = None
+    if not args.no_oracle and rank == 0:
+        oracle_t3 = oracle_check_c2(asm, xyz, conn, dof, False, nnz)
+    res["t3"] = dict(ms_head=ms_head, ms_fp64=ms_fp64, ph_head=ph_head, ph_fp64=ph_fp64, nnz=nnz,
+                     err=err_head, fro=fro_head, t_sym=t_sym, nelem=conn.shape[0],
+                     ms_mx=ms_mx, ph_mx=ph_mx, err_mx=err_mx,
+                     tiles={"mixed_comp": tiles_head, "fp64": tiles_fp64, "mixed": tiles_mx})
     asm.ctx.close()
     del asm
 
@@ -658,20 +759,24 @@ def main():
     xyz, conn, dof = plate(args.n, True)
     asm = Assembler(xyz, conn, dof, True, device=local)
     stream = torch.cuda.ExternalStream(asm.ctx.stream())
-    asm.stiffness(_abi.FS_MIXED)
+    asm.stiffness(HEAD)
     t_sym_q4 = asm.timings()[2]
-    ms_q_mixed, ph_q_mixed, nnz_q = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
-    tiles_q = {"mixed": asm.tiles()}
-    vq_m = asm.values(nnz_q)
+    ms_q_head, ph_q_head, nnz_q = time_steps(asm, HEAD, args.steps, args.warmup, torch, stream)
+    tiles_q = {"mixed_comp": asm.tiles()}
+    vq_h = asm.values(nnz_q)
     ms_q_fp64, ph_q_fp64, _ = time_steps(asm, _abi.FS_FP64, args.steps, args.warmup, torch, stream)
     tiles_q["fp64"] = asm.tiles()
     vq_d = asm.values(nnz_q)
-    err_q4 = float(np.abs(vq_m - vq_d).max() / np.abs(vq_d).max())
-    del vq_m
-    ms_q_comp, ph_q_comp, _ = time_steps(asm, _abi.FS_MIXED_COMP, args.steps, args.warmup, torch, stream)
-    vq_c = asm.values(nnz_q)
-    err_q4c = float(np.abs(vq_c - vq_d).max() / np.abs(vq_d).max())
-    del vq_c, vq_d
+    err_q4 = float(np.abs(vq_h - vq_d).max() / np.abs(vq_d).max())
+    del vq_h
+    ms_q_mx, ph_q_mx, _ = time_steps(asm, _abi.FS_MIXED, args.steps, args.warmup, torch, stream)
+    tiles_q["mixed"] = asm.tiles()
+    vq_m = asm.values(nnz_q)
+    err_q4m = float(np.abs(vq_m - vq_d).max() / np.abs(vq_d).max())
+    del vq_m, vq_d
+    oracle_q4 = None
+    if not args.no_oracle and rank == 0:
+        oracle_q4 = oracle_check_c2(asm, xyz, conn, dof, True, nnz_q)
     asm.ctx.close()
     del asm
 
@@ -685,69 +790,87 @@ def main():
         return 0
     t3 = res["t3"]
     ne3, ne4 = t3["nelem"], conn.shape[0]
-    value = world * ne3 / (ms_mixed * 1e-3)
-    # roofline of the dominant kernel of the headline path
+    value = world * ne3 / (ms_head * 1e-3)
+    # roofline of the dominant kernel of the headline step
     hbm, peak_kind = read_peaks()
-    el_ms, ga_ms = t3["ph_mixed"][0], t3["ph_mixed"][1]
+    el_ms, ga_ms = t3["ph_head"][0], t3["ph_head"][1]
     nodes = (args.n + 1) ** 2
-    # algorithmic bytes per launch.  Element kernel: connectivity, coordinates,
-    # normals, flags, thickness in; the 6 upper 6x6 float node blocks out.
-    # Gather: the 9 node blocks each element contributes (a mirrored block is
-    # read for the lower ones), the double CSR values out, and the pattern
-    # (pair lists and slots, per-node dofs/offsets/row pointers, column map).
-    el_bytes = ne3 * (3 * 4 + 3 * 24 + 3 * 24 + 3 + 8 + 216 * 4)
-    ga_bytes = (ne3 * 324 * 4 + nnz * 8 + ne3 * 3 * 8 + nodes * (6 * 4 + 8 + 4 + 8 + 6 * 8)
-                + 2 * nnz // 6)
+    pairs_once = t3["tiles"]["mixed_comp"]["pairs_once"]
+    el_bytes, ga_bytes = t3_bytes(ne3, nnz, nodes, HEAD, pairs_once)
+    step_bytes = survey_step_bytes(ne3, nnz)
+    mode = {_abi.FS_MIXED: "FS_MIXED", _abi.FS_MIXED_COMP: "FS_MIXED_COMP", _abi.FS_FP64: "FS_FP64"}[HEAD]
     if el_ms >= ga_ms:
-        dom, ms_dom, alg = "k_t3_elements<float>", el_ms, el_bytes
+        dom, ms_dom, own = "k_t3_elements " + mode, el_ms, el_bytes
     else:
-        dom, ms_dom, alg = "k_gather<float>", ga_ms, ga_bytes
-    achieved = alg / (ms_dom * 1e-3) / 1e9
+        dom, ms_dom, own = "k_gather " + mode, ga_ms, ga_bytes
+    achieved = step_bytes / (ms_dom * 1e-3) / 1e9
     traffic, traffic_src = measured_traffic(dom, ne3)
-    cb = None
+    tr_el, _ = measured_traffic("k_t3_elements " + mode, ne3)
+    tr_ga, _ = measured_traffic("k_gather " + mode, ne3)
+    cb = cb1 = None
     if not args.no_cpu:
-        cb, _ = cpu_baseline()
+        cb, _ = cpu_baseline(steps=3)
+        cb1, _ = cpu_baseline(steps=1, nthreads=1)
+        cb["single_thread_value"] = cb1["value"]
+        cb["single_thread_sample"] = cb1["sample"]
     line = {
         "metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32-element/f64-assembly", "data": "synthetic",
+        "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-element (compensated, float pairs)/f64-assembly", "data": "synthetic",
         "config": {"workload": workload_text(args.n),
-                   "elements": ne3, "nnz": nnz, "precision": "FS_MIXED", "assembler": "SysmatAssemblerSparse",
+                   "elements": ne3, "nnz": nnz, "precision": "FS_MIXED_COMP", "assembler": "SysmatAssemblerSparse",
                    "pattern": "built once per mesh (symbolic %.2f ms), not in the timed step" % t3["t_sym"],
                    "l2": "inputs larger than L2 (element matrices %.2f GB, values %.2f GB)" % (
-                       ne3 * 216 * 4 / 1e9, nnz * 8 / 1e9),
+                       ne3 * 216 * 8 / 1e9, nnz * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": world * ne3 / (ms_e2e * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
                 "path": "C ABI from pinned host: fs_geometry_set + fs_dofs_set + fs_pattern (pattern "
-                        "rebuilt) + fs_stiffness_copy (CSC copied back, pattern copy overlapping the kernels)"},
+                        "rebuilt) + fs_stiffness_copy (FS_MIXED_COMP; CSC copied back, pattern copy "
+                        "overlapping the kernels)"},
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": peak_kind, "traffic": traffic,
                      "traffic_source": traffic_src,
-                     "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms_dom},
-        "clocks": dict(clocks.summary(), window="the T3FF timed regions: mixed, FP64 and compensated steps, e2e steps"),
+                     "algorithmic_bytes_per_launch": step_bytes,
+                     "algorithmic_bytes_basis": "minimal bytes of the whole assembly per element (inputs 159 B "
+                                                "+ 8 B per stored value) x elements, over the dominant "
+                                                "kernel's time",
+                     "ms_per_launch": ms_dom,
+                     "frac_step": step_bytes / (ms_head * 1e-3) / 1e9 / hbm,
+                     "frac_kernel_own_bytes": own / (ms_dom * 1e-3) / 1e9 / hbm,
+                     "kernel_own_bytes_per_launch": own,
+                     "traffic_step_over_algorithmic": ((tr_el + tr_ga) / step_bytes
+                                                       if tr_el is not None and tr_ga is not None else None)},
+        "clocks": dict(clocks.summary(), window="the T3FF timed regions: the three modes' steps, e2e steps"),
         "cpu_baseline": cb,
         "results": {
-            "t3ff": {"elements": ne3, "nnz": nnz, "mixed_elements_per_s": ne3 / (ms_mixed * 1e-3),
+            "t3ff": {"elements": ne3, "nnz": nnz,
+                     "mixed_comp_elements_per_s": ne3 / (ms_head * 1e-3),
+                     "mixed_comp_over_fp64": ms_fp64 / ms_head,
+                     "nnz_per_s_mixed_comp": nnz / (ms_head * 1e-3),
+                     "rel_err_K_mixed_comp_vs_fp64_max": t3["err"], "rel_err_K_mixed_comp_vs_fp64_fro": t3["fro"],
+                     "ms_elements_mixed_comp": t3["ph_head"][0], "ms_gather_mixed_comp": t3["ph_head"][1],
                      "fp64_elements_per_s": ne3 / (ms_fp64 * 1e-3),
-                     "mixed_over_fp64": ms_fp64 / ms_mixed, "nnz_per_s_mixed": nnz / (ms_mixed * 1e-3),
-                     "rel_err_K_mixed_vs_fp64_max": t3["err"], "rel_err_K_mixed_vs_fp64_fro": t3["fro"],
-                     "ms_elements_mixed": t3["ph_mixed"][0], "ms_gather_mixed": t3["ph_mixed"][1],
                      "ms_elements_fp64": t3["ph_fp64"][0], "ms_gather_fp64": t3["ph_fp64"][1],
+                     "mixed_elements_per_s": ne3 / (t3["ms_mx"] * 1e-3),
+                     "mixed_over_fp64": ms_fp64 / t3["ms_mx"],
+                     "rel_err_K_mixed_vs_fp64_max": t3["err_mx"],
+                     "ms_elements_mixed": t3["ph_mx"][0], "ms_gather_mixed": t3["ph_mx"][1],
+                     "rel_err_M_mixed_vs_fp64_max": 0.0,
                      "ms_symbolic": t3["t_sym"], "e2e_ms": ms_e2e, "tiles": t3["tiles"],
-                     "mixed_comp_elements_per_s": ne3 / (t3["ms_comp"] * 1e-3),
-                     "mixed_comp_over_fp64": ms_fp64 / t3["ms_comp"],
-                     "rel_err_K_mixed_comp_vs_fp64_max": t3["err_comp"],
-                     "ms_elements_mixed_comp": t3["ph_comp"][0], "ms_gather_mixed_comp": t3["ph_comp"][1]},
-            "q4rs": {"elements": ne4, "nnz": nnz_q, "mixed_elements_per_s": ne4 / (ms_q_mixed * 1e-3),
-                     "fp64_elements_per_s": ne4 / (ms_q_fp64 * 1e-3), "mixed_over_fp64": ms_q_fp64 / ms_q_mixed,
-                     "rel_err_K_mixed_vs_fp64_max": err_q4, "ms_elements_mixed": ph_q_mixed[0],
-                     "ms_gather_mixed": ph_q_mixed[1], "ms_elements_fp64": ph_q_fp64[0],
-                     "ms_gather_fp64": ph_q_fp64[1], "ms_symbolic": t_sym_q4, "tiles": tiles_q,
-                     "mixed_comp_elements_per_s": ne4 / (ms_q_comp * 1e-3),
-                     "rel_err_K_mixed_comp_vs_fp64_max": err_q4c,
-                     "ms_elements_mixed_comp": ph_q_comp[0], "ms_gather_mixed_comp": ph_q_comp[1]},
+                     "fp64_vs_oracle": oracle_t3},
+            "q4rs": {"elements": ne4, "nnz": nnz_q,
+                     "mixed_comp_elements_per_s": ne4 / (ms_q_head * 1e-3),
+                     "mixed_comp_over_fp64": ms_q_fp64 / ms_q_head,
+                     "rel_err_K_mixed_comp_vs_fp64_max": err_q4,
+                     "ms_elements_mixed_comp": ph_q_head[0], "ms_gather_mixed_comp": ph_q_head[1],
+                     "fp64_elements_per_s": ne4 / (ms_q_fp64 * 1e-3),
+                     "ms_elements_fp64": ph_q_fp64[0], "ms_gather_fp64": ph_q_fp64[1],
+                     "mixed_elements_per_s": ne4 / (ms_q_mx * 1e-3), "mixed_over_fp64": ms_q_fp64 / ms_q_mx,
+                     "rel_err_K_mixed_vs_fp64_max": err_q4m,
+                     "ms_elements_mixed": ph_q_mx[0], "ms_gather_mixed": ph_q_mx[1],
+                     "ms_symbolic": t_sym_q4, "tiles": tiles_q, "fp64_vs_oracle": oracle_q4},
             "explicit_q4rs_512": ex,
             "batched_64_cylinder_panels": bc3,
             "corotbeam_lattice_100": beams,

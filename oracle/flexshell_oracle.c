@@ -960,6 +960,66 @@ int orc_all_element_stiffness(int64_t nnodes, const double *xyz, int64_t nelem,
     return status;
 }
 
+/* Check helper for meshes too large for a COO buffer: the oracle's element
+ * stiffness matrices (orc_element_stiffness, the reference loop) of every
+ * element, summed into the values of a given 1-based CSC pattern (colptr,
+ * rowval) of size n; dofs above n are left out, as the assemblers do.
+ * touched[k] is set for every stored entry that receives a contribution and
+ * *missing counts contributions whose (row, column) the pattern lacks, so a
+ * pattern equal to the oracle's union pattern gives missing 0 and every entry
+ * touched.  Sums run in no fixed order (OpenMP over elements, atomic adds):
+ * for comparisons at a relative tolerance, not bitwise. */
+int orc_csc_accumulate_stiffness(int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                                 const double *normals, const uint8_t *valid, const orc_params *p,
+                                 const int64_t *dofnums, int64_t n, const int64_t *colptr,
+                                 const int64_t *rowval, double *vals, uint8_t *touched, int64_t *missing,
+                                 int nthreads)
+{
+    int nen = nen_of(p->etype), nd = 6 * nen;
+    int status = 0;
+    int64_t miss = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : status) reduction(+ : miss)
+#endif
+    for (int64_t e = 0; e < nelem; e++) {
+        const int64_t *cn = conn + nen * e;
+        double X[12], nr[12], Ke[24 * 24];
+        uint8_t vl[4];
+        int64_t dn[24];
+        gather_X(xyz, nnodes, cn, nen, X);
+        for (int a = 0; a < nen; a++) {
+            int64_t node = cn[a] - 1;
+            for (int c = 0; c < 3; c++) nr[3 * a + c] = normals[node + c * nnodes];
+            vl[a] = valid[node];
+            for (int k = 0; k < 6; k++) dn[6 * a + k] = dofnums[node + k * nnodes];
+        }
+        status |= orc_element_stiffness(p, e, X, nr, vl, Ke);
+        for (int j = 0; j < nd; j++) {
+            if (dn[j] < 1 || dn[j] > n) continue;
+            const int64_t c0 = colptr[dn[j] - 1] - 1, c1 = colptr[dn[j]] - 1;
+            for (int i = 0; i < nd; i++) {
+                if (dn[i] < 1 || dn[i] > n) continue;
+                int64_t lo = c0, hi = c1 - 1, at = -1;
+                while (lo <= hi) {
+                    const int64_t mid = (lo + hi) >> 1;
+                    if (rowval[mid] == dn[i]) { at = mid; break; }
+                    if (rowval[mid] < dn[i]) lo = mid + 1; else hi = mid - 1;
+                }
+                if (at < 0) { miss++; continue; }
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+                vals[at] += Ke[IX(i, j, nd)];
+                touched[at] = 1;
+            }
+        }
+    }
+    (void)nthreads;
+    *missing = miss;
+    return status;
+}
+
 /* Assembly of element matrices Ke (what 0, nelem x (6 nen)^2 column-major)
  * or of lumped masses tmrm (what 1, nelem x 2) in the given element order. */
 static orc_result *assemble_from(int what, int mode, int nen, int64_t nnodes, int64_t nelem,

@@ -91,6 +91,13 @@ void orc_result_copy(const orc_result *r, int64_t *colptr, int64_t *rowval, doub
 void orc_result_free(orc_result *r);
 
 /* Dense element matrices for all elements (column-major ndof x ndof each). */
+/* element stiffness matrices summed into the values of a given 1-based CSC
+ * pattern (meshes too large for a COO buffer); see the definition */
+int orc_csc_accumulate_stiffness(int64_t nnodes, const double *xyz, int64_t nelem, const int64_t *conn,
+                                 const double *normals, const uint8_t *valid, const orc_params *p,
+                                 const int64_t *dofnums, int64_t n, const int64_t *colptr,
+                                 const int64_t *rowval, double *vals, uint8_t *touched, int64_t *missing,
+                                 int nthreads);
 int orc_all_element_stiffness(int64_t nnodes, const double *xyz, int64_t nelem,
                               const int64_t *conn, const double *normals,
                               const uint8_t *valid, const orc_params *p, int nthreads,

@@ -86,6 +86,7 @@ def lib():
         L.orc_result_nnz.restype = ctypes.c_int64
         L.orc_result_n.restype = ctypes.c_int64
         L.orc_all_element_stiffness.restype = ctypes.c_int
+        L.orc_csc_accumulate_stiffness.restype = ctypes.c_int
         L.orc_cd_steps.restype = ctypes.c_int
         L.orc_cd_steps_load.restype = ctypes.c_int
         L.orc_laminate.restype = ctypes.c_int
@@ -245,6 +246,29 @@ class Problem:
         L.orc_result_copy(res, _p(colptr, _c_i64_p), _p(rowval, _c_i64_p), _p(nzval, _c_dbl_p))
         L.orc_result_free(res)
         return colptr, rowval, nzval, n
+
+    def stiffness_into_pattern(self, colptr, rowval, n=None, nthreads=0):
+        """The oracle's element stiffness matrices summed into the values of
+        a given 1-based CSC pattern (for meshes too large for the COO buffer
+        of `assemble`).  Returns (vals, touched, missing): touched flags the
+        stored entries that got a contribution, missing counts contributions
+        outside the pattern."""
+        if n is None:
+            n = int(self.dofnums.max())
+        colptr = np.ascontiguousarray(colptr, dtype=np.int64)
+        rowval = np.ascontiguousarray(rowval, dtype=np.int64)
+        vals = np.zeros(rowval.shape[0], dtype=np.float64)
+        touched = np.zeros(rowval.shape[0], dtype=np.uint8)
+        missing = ctypes.c_int64()
+        st = lib().orc_csc_accumulate_stiffness(
+            ctypes.c_int64(self.nnodes), _p(self.xyz, _c_dbl_p), ctypes.c_int64(self.nelem),
+            _p(self.conn, _c_i64_p), _p(self.normals, _c_dbl_p), _p(self.valid, _c_u8_p),
+            ctypes.byref(self.params), _p(self.dofnums, _c_i64_p), ctypes.c_int64(n),
+            _p(colptr, _c_i64_p), _p(rowval, _c_i64_p), _p(vals, _c_dbl_p), _p(touched, _c_u8_p),
+            ctypes.byref(missing), ctypes.c_int(nthreads))
+        if st != 0:
+            raise RuntimeError("oracle element stiffness failed with status %d" % st)
+        return vals, touched, missing.value
 
     def assemble_scipy(self, what="K", mode=KEEP_ZEROS, n=None, nthreads=0):
         import scipy.sparse as sp

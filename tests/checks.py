@@ -33,3 +33,30 @@ def same_pattern_modulo_cancellation(A, B, rel=1e-14):
         if abs(A[r, c]) > rel * scale or abs(B[r, c]) > rel * scale:
             return False
     return True
+
+
+def entrywise_errors(A, B, floor=1e-12):
+    """Entrywise comparisons of A against the reference B on B's pattern:
+    relmax = max |A - B| / max |B|; scaled = max |A_ij - B_ij| / sqrt(|B_ii B_jj|)
+    (the natural scale of an entry of a positive semi-definite matrix, which
+    bounds it); entrywise = max |A_ij - B_ij| / |B_ij| over the entries with
+    |B_ij| > floor max |B| (entries that are small only through cancellation
+    carry the rounding of the large terms they are summed from)."""
+    import scipy.sparse as sp
+    A = sp.csr_matrix(A)
+    B = sp.csr_matrix(B)
+    A.sort_indices()
+    B.sort_indices()
+    Bc = B.tocoo()
+    if (A.shape == B.shape and np.array_equal(A.indptr, B.indptr) and np.array_equal(A.indices, B.indices)):
+        dv = A.data - B.data
+    else:
+        dv = np.asarray((A - B)[Bc.row, Bc.col]).ravel()
+    mx = np.abs(B.data).max()
+    d = np.abs(B.diagonal())
+    den = np.sqrt(d[Bc.row] * d[Bc.col])
+    ok = den > 0
+    big = np.abs(Bc.data) > floor * mx
+    return {"relmax": float(np.abs(dv).max() / mx),
+            "scaled": float((np.abs(dv[ok]) / den[ok]).max()) if ok.any() else 0.0,
+            "entrywise": float((np.abs(dv[big]) / np.abs(Bc.data[big])).max()) if big.any() else 0.0}
