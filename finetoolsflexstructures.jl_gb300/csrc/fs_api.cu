@@ -208,6 +208,7 @@ int fs_ctx_destroy(fs_ctx *c)
     free_mesh(c->mesh);
     free_pattern(c->pat);
     free_beam(c);
+    free_shift(c);
     if (c->ke) cudaFree(c->ke);
     dfree(&c->tmrm); dfree(&c->vals); dfree(&c->cmp_rowptr); dfree(&c->cmp_colidx); dfree(&c->cmp_vals);
     dfree(&c->stage64);
@@ -477,6 +478,7 @@ int fs::assemble_matrix(fs_ctx *c, int precision, int assembler, int64_t nrows, 
     FS_TRY(status_to_code(c, bits));
     c->timed = true;
     c->t_compact_ms = 0.0;
+    c->mat_kind = (beam_which < 0 || beam_which == FS_BEAM_STIFFNESS) ? 0 : 2;
     c->mat_n = nrows;
     c->mat_rowptr = P.rowptr;
     c->mat_colidx = P.colidx;

@@ -115,7 +115,9 @@ struct fs_ctx {
     void *ke = nullptr;
     size_t ke_bytes = 0;
     double *tmrm = nullptr;
-    // current matrix
+    // current matrix; mat_kind 0 a stiffness (shell or beam), 1 a mass, 2
+    // another beam matrix
+    int mat_kind = -1;
     int64_t mat_n = 0, mat_nnz = 0;
     const int64_t *mat_rowptr = nullptr;
     const int32_t *mat_colidx = nullptr;
@@ -138,6 +140,8 @@ struct fs_ctx {
     // (fs_noalloc.cu) and the error of its lookup, if it failed
     void *noalloc_scratch = nullptr;
     std::string noalloc_err;
+    // banded Cholesky factor of K - sigma M (fs_eigen.cu), opaque here
+    void *shift = nullptr;
     // staging for host copies
     int64_t *stage64 = nullptr;
     size_t stage_cap = 0;
@@ -232,6 +236,8 @@ int status_to_code(fs_ctx *c, int bits);
 // address of the allocation-free path's scratch array in the current CUDA
 // context, looked up when the context is created (fs_noalloc.cu)
 void noalloc_setup(fs_ctx *c);
+// releases the shift-invert factor of the context (fs_eigen.cu)
+void free_shift(fs_ctx *c);
 
 int explicit_launch_steps(fs_ctx *c, int64_t nsteps);
 

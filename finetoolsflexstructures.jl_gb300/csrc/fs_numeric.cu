@@ -298,6 +298,7 @@ int assemble_mass(fs_ctx *c, int assembler, int64_t n)
     if (m.nnodes)
         k_mass_assemble<<<nblk2(m.nnodes, 128), 128, 0, c->stream>>>(m, P, n, c->tmrm, full, c->vals);
     FS_CUDA(c, cudaGetLastError());
+    c->mat_kind = 1;
     c->mat_n = n;
     if (full) {
         c->mat_rowptr = P.rowptr;

@@ -14,6 +14,7 @@ from .femm import (CSysCartesian, CSysCylindrical, CSysSpherical,
                    SysmatAssemblerSparseCSRSymm, SysmatAssemblerSparseDiag,
                    SysmatAssemblerSparseSymm, ShellBatch)
 from .beam import FEMMCorotBeam
+from .eigen import ShiftInvert, eigs
 from .explicit import CentralDifference, cd_loop
 from .loads import (FEMMBase, ForceIntensity, GaussRule, IntegDomain, SysvecAssembler,
                     SysvecAssemblerFBlock, TriRule, distribloads)

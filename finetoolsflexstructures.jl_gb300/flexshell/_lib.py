@@ -82,6 +82,8 @@ def lib():
         L.fs_beam_distribloads_global.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int64, vp]
         L.fs_beam_element_matrices.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.fs_beam_element_vectors.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp]
+        L.fs_shift_factor.argtypes = [vp, ctypes.c_double, vp, _c_i64_p]
+        L.fs_shift_solve.argtypes = [vp, ctypes.c_int, vp, vp]
         _lib = L
     return _lib
 

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libflexshell.so")
 SOURCES = ["fs_api.cu", "fs_symbolic.cu", "fs_numeric.cu", "fs_elem_t3.cu", "fs_elem_q4.cu", "fs_gather.cu",
            "fs_explicit.cu", "fs_noalloc.cu", "fs_beam.cu", "fs_batch.cu", "fs_resultants.cu",
-           "fs_loads.cu"]
+           "fs_loads.cu", "fs_eigen.cu"]
 HEADERS = ["fs_internal.cuh", "fs_elem_math.cuh", "fs_elem_common.cuh", "fs_beam_math.cuh", "fs_host_prep.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -59,7 +59,7 @@ def build(force=False, verbose=False, extra=()):
         if r.returncode != 0:
             raise RuntimeError("nvcc failed on %s" % cmd[2])
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)

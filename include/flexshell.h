@@ -241,6 +241,22 @@ int fs_explicit_get_state(fs_ctx *ctx, double *U, double *V, double *A);
 int fs_power_iteration(fs_ctx *ctx, const double *mdiag, int64_t iters, uint64_t seed,
                        double *omega_max);
 
+/* --- shift-invert support for the lowest modes ---------------------------------
+ * The inner step of the reference's modal analyses, eigs(K, M; nev, which = :SM)
+ * with a shift (ARPACK's shift-invert mode; test/test_shell_dynamics.jl:79-80,
+ * test/test_composite_shell_dynamics.jl): fs_shift_factor factorises
+ * K - sigma diag(mdiag) on the device, K the last matrix assembled by
+ * fs_stiffness (or fs_beam_matrix with FS_BEAM_STIFFNESS) and mdiag its nrows
+ * lumped masses (fs_mass with FS_ASM_DIAG, assembled before the stiffness).
+ * The factor is a banded Cholesky factor in double; its half-bandwidth comes
+ * from the dof numbering (returned in *bandwidth_out) and its storage is
+ * nrows x (bandwidth + 256) doubles (more than 160 GiB: FS_ERR_UNSUPPORTED).
+ * A matrix that is not positive definite gives FS_ERR_BAD_INPUT.
+ * fs_shift_solve solves (K - sigma M) X = B for nrhs host right-hand sides
+ * (nrows x nrhs, column-major).  An eigensolver (ARPACK) supplies the rest. */
+int fs_shift_factor(fs_ctx *ctx, double sigma, const double *mdiag, int64_t *bandwidth_out);
+int fs_shift_solve(fs_ctx *ctx, int nrhs, const double *b, double *x);
+
 /* --- co-rotational beams (src/FEMMCorotBeamModule.jl) ---------------------------
  * Mesh: fs_mesh_set with FS_COROTBEAM, conn nelem x 2.  All beam arithmetic is
  * double.  The matrices are assembled like the shell matrices (same assemblers,
