@@ -17,7 +17,9 @@
 // Factorisation (right-looking, blocked, lower): for each block column k,
 // potrf of the diagonal block, trsm of the panel below it, syrk of the
 // trailing triangle -- cuSOLVER and cuBLAS dense routines on those views, in
-// double.  Solves: block forward and backward substitution (trsv/gemv for
+// double.  The strictly upper triangle of a diagonal block's view lies on
+// the padding rows of the panel beside it, so the block is factorised in a
+// separate NB x NB buffer and only its lower triangle is copied back.  Solves: block forward and backward substitution (trsv/gemv for
 // one right-hand side, trsm/gemm for several).
 #include <cublas_v2.h>
 #include <cusolverDn.h>
@@ -112,6 +114,7 @@ struct ShiftFactor {
     size_t info_cap = 0;
     double *x = nullptr;
     size_t x_cap = 0;
+    double *w11 = nullptr;  // the diagonal block being factorised (NB x NB)
     unsigned long long *d_kd = nullptr;
     cublasHandle_t blas = nullptr;
     cusolverDnHandle_t sol = nullptr;
@@ -122,7 +125,7 @@ void free_shift(fs_ctx *c)
 {
     ShiftFactor *s = (ShiftFactor *)c->shift;
     if (!s) return;
-    dfree(&s->ab); dfree(&s->work); dfree(&s->info); dfree(&s->x); dfree(&s->d_kd);
+    dfree(&s->ab); dfree(&s->work); dfree(&s->info); dfree(&s->x); dfree(&s->d_kd); dfree(&s->w11);
     if (s->blas) dense_libs().destroy(s->blas);
     if (s->sol) dense_libs().dn_destroy(s->sol);
     delete s;
@@ -153,6 +156,14 @@ __global__ void k_fill_band(int64_t n, const int64_t *rowptr, const int32_t *col
         if (j == i) v -= sigma * mdiag[i];
         ab[(i - j) + j * ld] = v;
     }
+}
+
+// the lower triangle (with the diagonal) of an nb x nb block between two
+// column-major layouts; the other triangle of dst is left as it is
+__global__ void k_copy_lower(int nb, const double *src, int64_t lds, double *dst, int64_t ldd)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < nb && i >= j) dst[i + j * ldd] = src[i + j * lds];
 }
 
 static int blas_check(fs_ctx *c, cublasStatus_t st, const char *what)
@@ -284,8 +295,10 @@ int fs_shift_factor(fs_ctx *c, double sigma, const double *mdiag, int64_t *bandw
                                                                      dm, s->ld, s->ab);
     FS_CUDA(c, cudaGetLastError());
     const int64_t lda = s->ld - 1, nblk = (n + BAND_NB - 1) / BAND_NB;
+    if (!s->w11) FS_TRY(dalloc(c, &s->w11, (size_t)(BAND_NB * BAND_NB)));
+    FS_CUDA(c, cudaMemsetAsync(s->w11, 0, sizeof(double) * BAND_NB * BAND_NB, c->stream));
     int lw = 0;
-    FS_SOLVER(c, D.potrf_buffer(s->sol, CUBLAS_FILL_MODE_LOWER, (int)BAND_NB, s->ab, (int)lda, &lw));
+    FS_SOLVER(c, D.potrf_buffer(s->sol, CUBLAS_FILL_MODE_LOWER, (int)BAND_NB, s->w11, (int)BAND_NB, &lw));
     if (lw > s->lwork || !s->work) {
         FS_TRY(dalloc(c, &s->work, (size_t)std::max(lw, 1)));
         s->lwork = std::max(lw, 1);
@@ -296,11 +309,16 @@ int fs_shift_factor(fs_ctx *c, double sigma, const double *mdiag, int64_t *bandw
     for (int64_t b = 0; b < nblk; b++) {
         const int64_t k = b * BAND_NB, nb = std::min(BAND_NB, n - k), m = std::min(s->kd, n - k - nb);
         double *A11 = s->ab + k * s->ld, *A21 = A11 + nb, *A22 = s->ab + (k + nb) * s->ld;
-        FS_SOLVER(c, D.potrf(s->sol, CUBLAS_FILL_MODE_LOWER, (int)nb, A11, (int)lda, s->work, s->lwork,
-                                      s->info + b));
+        const dim3 cg((unsigned)((nb + 127) / 128), (unsigned)nb);
+        k_copy_lower<<<cg, 128, 0, c->stream>>>((int)nb, A11, lda, s->w11, BAND_NB);
+        FS_CUDA(c, cudaGetLastError());
+        FS_SOLVER(c, D.potrf(s->sol, CUBLAS_FILL_MODE_LOWER, (int)nb, s->w11, (int)BAND_NB, s->work, s->lwork,
+                             s->info + b));
+        k_copy_lower<<<cg, 128, 0, c->stream>>>((int)nb, s->w11, BAND_NB, A11, lda);
+        FS_CUDA(c, cudaGetLastError());
         if (m > 0) {
             FS_BLAS(c, D.trsm(s->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                                   CUBLAS_DIAG_NON_UNIT, (int)m, (int)nb, &one, A11, (int)lda, A21, (int)lda));
+                                   CUBLAS_DIAG_NON_UNIT, (int)m, (int)nb, &one, s->w11, (int)BAND_NB, A21, (int)lda));
             FS_BLAS(c, D.syrk(s->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, (int)m, (int)nb, &mone, A21,
                                    (int)lda, &one, A22, (int)lda));
         }

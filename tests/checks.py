@@ -3,8 +3,16 @@ import numpy as np
 
 
 def relmax(A, B):
-    A = A.toarray() if hasattr(A, "toarray") else A
-    B = B.toarray() if hasattr(B, "toarray") else B
+    """max |A - B| / max |B|; sparse operands stay sparse."""
+    import scipy.sparse as sp
+    if sp.issparse(A) or sp.issparse(B):
+        A = sp.csr_matrix(A)
+        B = sp.csr_matrix(B)
+        D = A - B
+        num = np.abs(D.data).max() if D.nnz else 0.0
+        return num / np.abs(B.data).max()
+    A = np.asarray(A)
+    B = np.asarray(B)
     return np.abs(A - B).max() / np.abs(B).max()
 
 
