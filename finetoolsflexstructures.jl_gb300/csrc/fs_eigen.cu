@@ -6,18 +6,23 @@
 //
 // Storage.  The matrix is symmetric with half-bandwidth kd (the largest
 // i - j of a stored entry under the dof numbering).  Its lower band is kept
-// column by column with leading dimension ld = kd + NB: entry (i, j),
+// column by column with leading dimension ld = kd + 2 NB: entry (i, j),
 // 0 <= i - j < ld, at ab[(i - j) + j ld] = ab[i + j (ld - 1)].  Read with
 // leading dimension ld - 1 the array is therefore an ordinary column-major
 // matrix, and every block the factorisation touches (the NB x NB diagonal
 // block, the kd x NB panel below it, the kd x kd trailing triangle) is a
-// dense sub-matrix of that view.  The NB extra rows hold the panel's
-// entries beyond the band, which are zero and stay zero.
+// dense sub-matrix of that view.  Rows kd+1 .. kd+NB-1 of a column hold the
+// panel's entries beyond the band, which are zero and stay zero.  In the
+// view, the strictly upper triangle of a diagonal w x w block (w <= NB) lies
+// on rows ld-w+1 .. ld-1 of other columns: the last NB rows are kept free so
+// that a library routine touching those entries changes nothing in use.
 //
 // Factorisation (right-looking, blocked, lower): for each block column k,
-// potrf of the diagonal block, trsm of the panel below it, syrk of the
-// trailing triangle -- cuSOLVER and cuBLAS dense routines on those views, in
-// double.  The strictly upper triangle of a diagonal block's view lies on
+// potrf of the diagonal block, trsm of the panel below it, and the update
+// of the trailing triangle column panel by column panel (syrk of each
+// NB x NB diagonal block, gemm of the rectangle below it) -- cuSOLVER and
+// cuBLAS dense routines on those views, in double (cuBLAS in its pedantic
+// math mode: no reduced-precision or emulated arithmetic).  The strictly upper triangle of a diagonal block's view lies on
 // the padding rows of the panel beside it, so the block is factorised in a
 // separate NB x NB buffer and only its lower triangle is copied back.  Solves: block forward and backward substitution (trsv/gemv for
 // one right-hand side, trsm/gemm for several).
@@ -43,6 +48,7 @@ struct DenseLibs {
     decltype(&cublasDestroy_v2) destroy;
     decltype(&cublasSetStream_v2) set_stream;
     decltype(&cublasSetPointerMode_v2) set_pointer_mode;
+    decltype(&cublasSetMathMode) set_math_mode;
     decltype(&cublasDtrsv_v2) trsv;
     decltype(&cublasDgemv_v2) gemv;
     decltype(&cublasDtrsm_v2) trsm;
@@ -86,7 +92,8 @@ static const DenseLibs &dense_libs()
         }
         bool ok = sym(hb, "cublasCreate_v2", &L.create) && sym(hb, "cublasDestroy_v2", &L.destroy) &&
                   sym(hb, "cublasSetStream_v2", &L.set_stream) &&
-                  sym(hb, "cublasSetPointerMode_v2", &L.set_pointer_mode) && sym(hb, "cublasDtrsv_v2", &L.trsv) &&
+                  sym(hb, "cublasSetPointerMode_v2", &L.set_pointer_mode) &&
+                  sym(hb, "cublasSetMathMode", &L.set_math_mode) && sym(hb, "cublasDtrsv_v2", &L.trsv) &&
                   sym(hb, "cublasDgemv_v2", &L.gemv) && sym(hb, "cublasDtrsm_v2", &L.trsm) &&
                   sym(hb, "cublasDgemm_v2", &L.gemm) && sym(hb, "cublasDsyrk_v2", &L.syrk) &&
                   sym(hs, "cusolverDnCreate", &L.dn_create) && sym(hs, "cusolverDnDestroy", &L.dn_destroy) &&
@@ -189,6 +196,7 @@ static int shift_handles(fs_ctx *c, ShiftFactor **out)
         FS_BLAS(c, D.create(&s->blas));
         FS_BLAS(c, D.set_stream(s->blas, c->stream));
         FS_BLAS(c, D.set_pointer_mode(s->blas, CUBLAS_POINTER_MODE_HOST));
+        FS_BLAS(c, D.set_math_mode(s->blas, CUBLAS_PEDANTIC_MATH));
     }
     if (!s->sol) {
         FS_SOLVER(c, D.dn_create(&s->sol));
@@ -275,7 +283,7 @@ int fs_shift_factor(fs_ctx *c, double sigma, const double *mdiag, int64_t *bandw
     FS_CUDA(c, cudaMemcpyAsync(&kd, s->d_kd, sizeof(kd), cudaMemcpyDeviceToHost, c->stream));
     FS_CUDA(c, cudaStreamSynchronize(c->stream));
     s->kd = (int64_t)kd;
-    s->ld = s->kd + BAND_NB;
+    s->ld = s->kd + 2 * BAND_NB;
     const double gib = (double)n * (double)s->ld * 8.0 / (1024.0 * 1024.0 * 1024.0);
     if (gib > 160.0) {
         char msg[240];
@@ -319,8 +327,15 @@ int fs_shift_factor(fs_ctx *c, double sigma, const double *mdiag, int64_t *bandw
         if (m > 0) {
             FS_BLAS(c, D.trsm(s->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
                                    CUBLAS_DIAG_NON_UNIT, (int)m, (int)nb, &one, s->w11, (int)BAND_NB, A21, (int)lda));
-            FS_BLAS(c, D.syrk(s->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, (int)m, (int)nb, &mone, A21,
-                                   (int)lda, &one, A22, (int)lda));
+            for (int64_t p0 = 0; p0 < m; p0 += BAND_NB) {
+                const int64_t w = std::min(BAND_NB, m - p0);
+                FS_BLAS(c, D.syrk(s->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, (int)w, (int)nb, &mone, A21 + p0,
+                                  (int)lda, &one, A22 + p0 + p0 * lda, (int)lda));
+                if (p0 + w < m)
+                    FS_BLAS(c, D.gemm(s->blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)(m - p0 - w), (int)w, (int)nb, &mone,
+                                      A21 + p0 + w, (int)lda, A21 + p0, (int)lda, &one, A22 + p0 + w + p0 * lda,
+                                      (int)lda));
+            }
         }
     }
     std::vector<int> info((size_t)nblk);

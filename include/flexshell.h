@@ -250,7 +250,7 @@ int fs_power_iteration(fs_ctx *ctx, const double *mdiag, int64_t iters, uint64_t
  * lumped masses (fs_mass with FS_ASM_DIAG, assembled before the stiffness).
  * The factor is a banded Cholesky factor in double; its half-bandwidth comes
  * from the dof numbering (returned in *bandwidth_out) and its storage is
- * nrows x (bandwidth + 256) doubles (more than 160 GiB: FS_ERR_UNSUPPORTED).
+ * nrows x (bandwidth + 512) doubles (more than 160 GiB: FS_ERR_UNSUPPORTED).
  * A matrix that is not positive definite gives FS_ERR_BAD_INPUT.
  * fs_shift_solve solves (K - sigma M) X = B for nrhs host right-hand sides
  * (nrows x nrhs, column-major).  An eigensolver (ARPACK) supplies the rest. */
