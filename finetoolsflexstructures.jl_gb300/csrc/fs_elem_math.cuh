@@ -720,6 +720,21 @@ FS_HD void q4_dbasis(double xi, double eta, double gp[4][2])
     gp[3][0] = -0.25 * (1 + eta); gp[3][1] = 0.25 * (1 - xi);
 }
 
+// q4_dbasis at Gauss point j (q4_point) from the two products it can take,
+// 0.25 (1 -+ 0.5773...) evaluated at compile time: the same values, chosen
+// by the signs of xi and eta instead of computed.
+FS_HD void q4_dbasis_gp(int j, double gp[4][2])
+{
+    constexpr double QA = 0.25 * (1.0 - Q4_GP), QB = 0.25 * (1.0 + Q4_GP);
+    const bool xp = j >= 2, ep = (j & 1) != 0;  // xi > 0, eta > 0
+    const double e1m = ep ? QA : QB, e1p = ep ? QB : QA;  // 0.25 (1 - eta), 0.25 (1 + eta)
+    const double x1m = xp ? QA : QB, x1p = xp ? QB : QA;  // 0.25 (1 - xi), 0.25 (1 + xi)
+    gp[0][0] = -e1m; gp[0][1] = -x1m;
+    gp[1][0] = e1m;  gp[1][1] = -x1p;
+    gp[2][0] = e1p;  gp[2][1] = x1p;
+    gp[3][0] = -e1p; gp[3][1] = x1m;
+}
+
 // MITC transverse shear rows in the element frame
 // (reference _Bsmat, src/FEMMShellQ4RSModule.jl:702-751), regrouped: each
 // entry is p*LA*fa(node) + q*LB*fb(node) with (p,q) = (sa,sb) for gxz and
@@ -788,17 +803,33 @@ FS_HD void q4_prepare(const ElemIn<4> &in, double t, double stab_c, Q4Elem &qe)
     qe.stab = t * t / (t * t + stab_c * mx);
 }
 
+// Compact rows of one quadrature point of a homogeneous Q4 element (shared
+// memory of the element kernel): the 3 membrane rows keep the translations
+// only (12 values), the 3 bending and 2 shear rows all 24 dofs.  Offsets in
+// R units; the element's 4 drilling rows (3 rotations each) follow the four
+// points' blocks.
+struct Q4Compact {
+    static constexpr int MS = 12;          // membrane row length
+    static constexpr int BS = 36, BSS = 24; // bending + shear rows: start, length
+    static constexpr int GP = BS + 5 * BSS; // one point's block (156)
+    static constexpr int DR = 4 * GP;       // drilling rows: start (3 each)
+    static constexpr int SIZE = DR + 12;    // 636
+};
+
 // Rows of quadrature point j (8 rows: membrane+bending 6, shear 2) on the
 // global dofs (24 wide), plus this point's contribution to the drilling
 // traces tr(P K_rr P) of each node (src/FEMMShellQ4RSModule.jl:807-838).
 // Returns nonzero on a singular metric (src/FEMMShellQ4RSModule.jl:308-311).
-template <class R, bool COMP>
+// COMPACT (homogeneous elements): `rows` is the point's Q4Compact block and
+// `rs` is not used.
+template <class R, bool COMP, bool COMPACT = false>
 FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatConst &mc,
                         const GroupConst *gc, R *rows, int rs, double trace[4])
 {
+    static_assert(!(COMP && COMPACT), "the compact layout is for homogeneous elements");
     double xi, eta, gp[4][2];
     q4_point(j, xi, eta);
-    q4_dbasis(xi, eta, gp);
+    q4_dbasis_gp(j, gp);
     double J0[3], J1[3];
     for (int c = 0; c < 3; c++) {
         J0[c] = qe.Xr[0][c] * gp[0][0] + qe.Xr[1][c] * gp[1][0] + qe.Xr[2][c] * gp[2][0] + qe.Xr[3][c] * gp[3][0];
@@ -881,7 +912,7 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     if constexpr (!COMP) {
         R tr_ = (R)in.t, jr = Jac;
         R btx[3][4], bty[3][4];
-        homog_mb_rows<R, 4>(M, mc, sqrt(tr_ * jr), sqrt(tr_ * tr_ * tr_ / 12 * jr), rows, rs, btx, bty);
+        homog_mb_rows<R, 4, COMPACT>(M, mc, sqrt(tr_ * jr), sqrt(tr_ * tr_ * tr_ / 12 * jr), rows, rs, btx, bty);
         R ws = sqrt(tr_ * stab * jr);
         R l00 = lpk<R>(mc.Lt, mc.Ltf, lp(0, 0)), l10 = lpk<R>(mc.Lt, mc.Ltf, lp(1, 0)), l11 = lpk<R>(mc.Lt, mc.Ltf, lp(1, 1));
         for (int r = 0; r < 2; r++) {
@@ -892,7 +923,8 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
                 tx[i] = f0 * sh[0][i][3] + f1 * sh[1][i][3];
                 ty[i] = f0 * sh[0][i][4] + f1 * sh[1][i][4];
             }
-            expand_wt<R, 4, true>(M, w, tx, ty, rows + (6 + r) * rs);
+            expand_wt<R, 4, true>(M, w, tx, ty,
+                                  COMPACT ? rows + Q4Compact::BS + Q4Compact::BSS * (3 + r) : rows + (6 + r) * rs);
         }
     } else {
         R mb[6][4][5];
@@ -918,14 +950,18 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
         for (int r = 0; r < 8; r++) expand_row<R, 4>(M, (const R(*)[5])mixed[r], rows + r * rs);
     }
     // drilling traces: sum over rows of |b|^2 - (b.n)^2 on the rotation block
+    // (float rows: the float copy of the normals, the same values as the
+    // double normals rounded here)
     for (int k = 0; k < 4; k++) {
-        R nv[3] = {(R)in.nrm[k][0], (R)in.nrm[k][1], (R)in.nrm[k][2]};
+        R nv[3];
+        for (int c = 0; c < 3; c++) nv[c] = sizeof(R) == 4 ? (R)in.nrmf[k][c] : (R)in.nrm[k][c];
         R nn = sqrt(dot3(nv, nv));
         R u[3] = {0, 0, 0};
         if (nn > (R)0) { u[0] = nv[0] / nn; u[1] = nv[1] / nn; u[2] = nv[2] / nn; }
         R tr = 0;
-        for (int r = 0; r < 8; r++) {
-            const R *o = rows + r * rs + 6 * k + 3;
+        // compact: the membrane rows have no rotations (their terms are zero)
+        for (int r = COMPACT ? 3 : 0; r < 8; r++) {
+            const R *o = (COMPACT ? rows + Q4Compact::BS + Q4Compact::BSS * (r - 3) : rows + r * rs) + 6 * k + 3;
             R bn = o[0] * u[0] + o[1] * u[1] + o[2] * u[2];
             tr += o[0] * o[0] + o[1] * o[1] + o[2] * o[2] - bn * bn;
         }

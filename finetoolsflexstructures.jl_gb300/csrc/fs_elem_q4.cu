@@ -1,46 +1,109 @@
 // Q4RS / Q4RSComp element kernel: four lanes per element, one per Gauss
 // point (the element math is csrc/fs_elem_math.cuh).
+//
+// Each element's inputs (nodes, normals, flags, thickness) and its
+// centroid-relative coordinates are staged in shared memory, one node per
+// lane, and read from there by the four points: no lane holds the whole
+// element in registers.  The element-level double work (centroid,
+// stabilisation factor, drilling factor) is split over the four lanes by
+// node where it is node-wise.  Homogeneous elements keep their rows in the
+// compact layout (Q4Compact: membrane rows on the translations, drilling rows
+// on one node's rotations), layered ones in the dense 36 x 24 layout.
 #include "fs_elem_common.cuh"
 
 namespace fs {
 
+// per-element staging area (shared memory)
+struct Q4Stage {
+    ElemIn<4> in;
+    Q4Elem qe;
+};
+
+// row values (R units) one element keeps in shared memory, with one of
+// padding (an odd stride spreads the elements over the banks)
+__host__ __device__ constexpr int q4_row_values(bool layered) { return layered ? 36 * 24 + 1 : Q4Compact::SIZE + 1; }
+
+size_t q4_smem(int precision, bool layered, int epb)
+{
+    const size_t rv = (size_t)q4_row_values(layered) * (precision == FS_FP64 ? 8 : 4);
+    return (size_t)epb * (sizeof(Q4Stage) + ((rv + 7) & ~(size_t)7));
+}
+
+// Shared memory (about 3 KB per float homogeneous element, 4-7 KB for the
+// others) bounds the resident elements of an SM to 76 or fewer, 304 threads:
+// the register budget of 255 per thread costs no occupancy.
+
 // The elements per block (the tuned tile) is a launch parameter (block size
 // / 4): every tile runs the same compiled kernel and the same arithmetic.
 template <class R, bool COMP, class S>
-__global__ void __launch_bounds__(256) k_q4_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
+__global__ void __launch_bounds__(128, 2) k_q4_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
 {
-    constexpr int NR = 36, ND = 24, STRIDE = NR * ND + 1;
+    constexpr int ND = 24;
+    constexpr int RV = q4_row_values(COMP);
+    constexpr size_t RB = ((size_t)RV * sizeof(R) + 7) & ~(size_t)7;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int epb = blockDim.x >> 2;
     const int el = threadIdx.x >> 2, qp = threadIdx.x & 3;
-    R *rows = reinterpret_cast<R *>(smem_raw) + el * STRIDE;
-    int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 2) + el;
+    Q4Stage &sg = reinterpret_cast<Q4Stage *>(smem_raw)[el];
+    R *rows = reinterpret_cast<R *>(smem_raw + (size_t)epb * sizeof(Q4Stage) + (size_t)el * RB);
+    const int64_t r = (int64_t)blockIdx.x * epb + el;
     const bool active = r < m.nelem;
-    ElemIn<4> in;
-    double tr[4] = {0, 0, 0, 0};
-    // element constants computed once per element (by its first lane) and
-    // shared with the other three lanes
-    Q4Elem qe;
+    const int src = (threadIdx.x & 31) & ~3;  // the element's first lane
+    // --- stage the element: lane qp loads node qp ---
+    double Xa[3] = {0, 0, 0};
     if (active) {
-        load_elem<4>(m, r, in);
-        if (qp == 0) q4_prepare(in, COMP ? m.groups[in.group].thickness : in.t, mc.stab_c, qe);
-    }
-    {
-        const int src = (threadIdx.x & 31) & ~3;
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int c = 0; c < 3; c++) qe.Xr[a][c] = __shfl_sync(0xffffffffu, qe.Xr[a][c], src);
-        qe.stab = __shfl_sync(0xffffffffu, qe.stab, src);
-        if constexpr (sizeof(R) == 4) {
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) qe.Xf[a][c] = __shfl_sync(0xffffffffu, qe.Xf[a][c], src);
+        const int node = m.conn[r * 4 + qp];
+        for (int c = 0; c < 3; c++) {
+            Xa[c] = m.xyz[(int64_t)c * m.nnodes + node];
+            sg.in.X[qp][c] = Xa[c];
+            sg.in.nrm[qp][c] = m.normals[(int64_t)c * m.nnodes + node];
+            sg.in.nrmf[qp][c] = m.normals_f[(int64_t)c * m.nnodes + node];
+        }
+        sg.in.valid[qp] = m.valid[node] != 0;
+        if (qp == 0) {
+            sg.in.t = m.thick ? m.thick[r] : 0.0;
+            sg.in.group = m.group ? m.group[r] : 0;
         }
     }
+    __syncwarp();
+    // --- centroid-relative coordinates and the stabilisation factor
+    //     (q4_prepare, split by node: the same operations in the same order) ---
+    double mxd = 0.0;
     if (active) {
-        const GroupConst *gc = COMP ? &m.groups[in.group] : nullptr;
-        int st = q4_point_rows<R, COMP>(in, qe, qp, mc, gc, rows + qp * 8 * ND, ND, tr);
+        double cen[3] = {0, 0, 0};
+        for (int a = 0; a < 4; a++)
+            for (int c = 0; c < 3; c++) cen[c] += sg.in.X[a][c];
+        for (int c = 0; c < 3; c++) {
+            cen[c] /= 4;
+            sg.qe.Xr[qp][c] = Xa[c] - cen[c];
+            sg.qe.Xf[qp][c] = (float)sg.qe.Xr[qp][c];
+        }
+        if (qp > 0) {
+            const double dx = Xa[0] - sg.in.X[0][0], dy = Xa[1] - sg.in.X[0][1], dz = Xa[2] - sg.in.X[0][2];
+            mxd = dx * dx + dy * dy + dz * dz;
+        }
+    }
+    // the largest of the element's three distances (exact in any order)
+    {
+        const double o1 = __shfl_xor_sync(0xffffffffu, mxd, 1);
+        mxd = o1 > mxd ? o1 : mxd;
+        const double o2 = __shfl_xor_sync(0xffffffffu, mxd, 2);
+        mxd = o2 > mxd ? o2 : mxd;
+    }
+    if (active && qp == 0) {
+        const double t = COMP ? m.groups[sg.in.group].thickness : sg.in.t;
+        sg.qe.stab = t * t / (t * t + mc.stab_c * mxd);
+    }
+    __syncwarp();
+    // --- rows of this lane's quadrature point ---
+    double tr[4] = {0, 0, 0, 0};
+    if (active) {
+        const GroupConst *gc = COMP ? &m.groups[sg.in.group] : nullptr;
+        int st;
+        if constexpr (COMP)
+            st = q4_point_rows<R, true>(sg.in, sg.qe, qp, mc, gc, rows + qp * 8 * ND, ND, tr);
+        else
+            st = q4_point_rows<R, false, true>(sg.in, sg.qe, qp, mc, gc, rows + qp * Q4Compact::GP, 0, tr);
         if (st) {
             atomicOr(status, DEV_SINGULAR);
             for (int k = 0; k < 4; k++) tr[k] = 0.0;
@@ -52,7 +115,34 @@ __global__ void __launch_bounds__(256) k_q4_elements(const MeshDev m, const MatC
         tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], 1);
         tr[k] += __shfl_xor_sync(0xffffffffu, tr[k], 2);
     }
-    if (active && qp == 0) q4_drill_rows<R>(in, tr, mc.drill_scale, rows + 32 * ND, ND);
+    // --- drilling rows (q4_drill_rows, node qp on lane qp) ---
+    bool use = false;
+    if (active) {
+        const double *nv = sg.in.nrm[qp];
+        use = sg.in.valid[qp] && (dot3(nv, nv) != 0.0);  // sqrt(x) != 0 exactly when x != 0
+    }
+    const unsigned um = __ballot_sync(0xffffffffu, use) >> src;
+    if (active) {
+        double sum = 0.0;
+        int cnt = 0;
+        for (int k = 0; k < 4; k++)
+            if ((um >> k) & 1u) {
+                const double v = tr[k] / 2.0;
+                sum += v > 0.0 ? v : 0.0;
+                cnt++;
+            }
+        const double kavg = (cnt ? sum / cnt : 0.0) * mc.drill_scale;
+        const double sk = kavg > 0.0 ? sqrt(kavg) : 0.0;
+        if constexpr (COMP) {
+            R *o = rows + (32 + qp) * ND;
+            for (int q = 0; q < 24; q++) o[q] = 0;
+            if (use && kavg != 0.0)
+                for (int c = 0; c < 3; c++) o[6 * qp + 3 + c] = (R)(sk * sg.in.nrm[qp][c]);
+        } else {
+            R *o = rows + Q4Compact::DR + 3 * qp;
+            for (int c = 0; c < 3; c++) o[c] = (use && kavg != 0.0) ? (R)(sk * sg.in.nrm[qp][c]) : (R)0;
+        }
+    }
     __syncwarp();
     if (!active) return;
     S *out = ke + r * (10 * 36);
@@ -65,15 +155,17 @@ __global__ void __launch_bounds__(256) k_q4_elements(const MeshDev m, const MatC
         acc.zero();
         if constexpr (!COMP) {
             // homogeneous: per Gauss point 3 membrane rows (translations only)
-            // and 5 bending/shear rows; then one drilling row per node
+            // and 5 bending/shear rows; then one drilling row per node -- the
+            // products and their order of the dense layout
 #pragma unroll 1
             for (int j = 0; j < 4; j++) {
-                gram_rows<0, 3, 0, 3>(acc, rows, ND, 8 * j, 8 * j + 3, a, b);
-                gram_rows<0, 6, 0, 6>(acc, rows, ND, 8 * j + 3, 8 * j + 8, a, b);
+                const R *gpb = rows + j * Q4Compact::GP;
+                gram_rows_c<0, 3, 0, 3, Q4Compact::MS, 3, 0>(acc, gpb, 0, 3, a, b);
+                gram_rows_c<0, 6, 0, 6, Q4Compact::BSS, 6, 0>(acc, gpb + Q4Compact::BS, 0, 5, a, b);
             }
-            if (a == b) gram_rows<3, 6, 3, 6>(acc, rows, ND, 32 + a, 33 + a, a, b);
+            if (a == b) gram_rows_c<3, 6, 3, 6, 3, 0, 3>(acc, rows + Q4Compact::DR + 3 * a, 0, 1, a, b);
         } else {
-            gram_rows<0, 6, 0, 6>(acc, rows, ND, 0, NR, a, b);
+            gram_rows<0, 6, 0, 6>(acc, rows, ND, 0, 36, a, b);
         }
         acc.store(out + ub(a, b, 4) * 36);
     }
@@ -83,8 +175,10 @@ template <class R, bool COMP, class S = R>
 static int run_q4(fs_ctx *c, S *ke)
 {
     int epb = c->tune.elem_epb;
-    if (epb != 16 && !(epb == 64 && sizeof(R) == 4)) epb = 32;
-    const size_t smem = q4_smem(sizeof(R) == 8 ? FS_FP64 : FS_MIXED, epb);
+    if (epb != 8 && epb != 16 && epb != 32) epb = 16;
+    const int prec = sizeof(R) == 8 ? FS_FP64 : FS_MIXED;
+    while (epb > 16 && q4_smem(prec, COMP, epb) > 227 * 1024) epb /= 2;
+    const size_t smem = q4_smem(prec, COMP, epb);
     auto kern = k_q4_elements<R, COMP, S>;
     FS_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<nblk2(c->mesh.nelem, epb), epb * 4, smem, c->stream>>>(c->mesh, c->mc, ke, c->d_status);

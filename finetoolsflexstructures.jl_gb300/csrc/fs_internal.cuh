@@ -248,7 +248,7 @@ size_t entry_bytes(int precision);
 size_t gather_smem_bytes(int precision, int nen, int warps);
 int run_t3_any(fs_ctx *c, int precision, void *ke);
 int run_q4_any(fs_ctx *c, int precision, void *ke);
-size_t q4_smem(int precision, int epb);
+size_t q4_smem(int precision, bool layered, int epb);
 
 // co-rotational beams
 int launch_beam_elements(fs_ctx *c, int which, int mass_type);

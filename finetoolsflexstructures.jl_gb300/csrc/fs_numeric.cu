@@ -33,7 +33,6 @@ size_t t3_smem(int precision, bool avgk, bool layered, int epb)
                             : (avgk ? CompactRows<3, T3Rows<true>::NS>::SIZE : CompactRows<3, T3Rows<false>::NS>::SIZE) + 1;
     return (precision == FS_FP64 ? 8 : 4) * (size_t)epb * per;
 }
-size_t q4_smem(int precision, int epb) { return (precision == FS_FP64 ? 8 : 4) * (size_t)epb * (36 * 24 + 1); }
 
 // element kernels of one precision into `ke` (the layout of the element buffer)
 static int run_elements(fs_ctx *c, int precision, void *ke)
@@ -332,7 +331,7 @@ int launch_elements_to(fs_ctx *c, int precision, void *ke)
 // tile-shape autotuner
 // ---------------------------------------------------------------------------
 // Candidates: elements per block of the element kernel (T3: 32, 64, 128;
-// Q4: 16, 32, 64, as far as their shared memory fits in 227 KB) and warps
+// Q4: 8, 16, 32, as far as their shared memory fits in 227 KB) and warps
 // per block of the gather (4, 8, 16).  Each candidate is timed on the
 // context's own mesh with CUDA events (best of three launches), the element
 // kernel first, then the gather on its output.  The choice is keyed on
@@ -407,11 +406,12 @@ int autotune_shell(fs_ctx *c, int precision)
         }
     }
     const bool t3 = m.nen == 3;
-    const int ecand[3] = {t3 ? 32 : 16, t3 ? 64 : 32, t3 ? 128 : 64};
+    const int ecand[3] = {t3 ? 32 : 8, t3 ? 64 : 16, t3 ? 128 : 32};
     int best_e = 0;
     float best_ms = 1e30f;
     for (int epb : ecand) {
-        const size_t smem = t3 ? t3_smem(precision, avgk, m.etype == FS_T3FFCOMP, epb) : q4_smem(precision, epb);
+        const size_t smem = t3 ? t3_smem(precision, avgk, m.etype == FS_T3FFCOMP, epb)
+                               : q4_smem(precision, m.etype == FS_Q4RSCOMP, epb);
         if (smem > SMEM_MAX) continue;
         c->tune.elem_epb = epb;
         float ms = 0.f;

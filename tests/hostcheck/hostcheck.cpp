@@ -243,3 +243,20 @@ extern "C" int hc_beam_elements(int which, int64_t nnodes, const double *xyz, in
     }
     return 0;
 }
+
+// Q4 basis gradients at the four Gauss points: tabulated (out[0..31]) and
+// computed (out[32..63]), gp[j][a][k]
+extern "C" void hc_q4_basis(double *out)
+{
+    for (int j = 0; j < 4; j++) {
+        double xi, eta, a[4][2], b[4][2];
+        q4_point(j, xi, eta);
+        q4_dbasis_gp(j, a);
+        q4_dbasis(xi, eta, b);
+        for (int n = 0; n < 4; n++)
+            for (int k = 0; k < 2; k++) {
+                out[8 * j + 2 * n + k] = a[n][k];
+                out[32 + 8 * j + 2 * n + k] = b[n][k];
+            }
+    }
+}

@@ -101,3 +101,10 @@ def beam_elements(which, xyz, conn, sections, E, nu, rho=0.0, u1=None, R1=None, 
                                 ctypes.c_int(mass_type), P(q), P(out))
     assert st == 0
     return out if vec else out.reshape(ne, 12, 12).transpose(0, 2, 1).copy()
+
+
+def q4_basis_pair():
+    """(tabulated, computed) Q4 basis gradients at the Gauss points, 4 x 4 x 2 each."""
+    out = np.zeros(64)
+    lib().hc_q4_basis(out.ctypes.data_as(ctypes.c_void_p))
+    return out[:32].reshape(4, 4, 2), out[32:].reshape(4, 4, 2)

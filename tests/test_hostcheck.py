@@ -108,3 +108,10 @@ def test_beam_math_matches_oracle(which, mass_type):
     R = b.elements(which, u1=u1, R1=R1, v1=v1, mass_type=mass_type, q=q)
     err = max(np.abs(h - r).max() / max(np.abs(r).max(), 1e-300) for h, r in zip(H, R))
     assert err <= 1e-12
+
+
+def test_q4_basis_at_gauss_points_is_the_computed_basis():
+    # the tabulated Q4 basis gradients at the four Gauss points are bitwise
+    # the computed ones (q4_dbasis_gp against q4_dbasis)
+    gp = HC.q4_basis_pair()
+    assert np.array_equal(gp[0], gp[1])
