@@ -694,7 +694,7 @@ FS_HD int t3_rows(const ElemIn<3> &in, const MatConst &mc, const GroupConst *gc,
 // ---------------------------------------------------------------------------
 // Q4RS: rows of one quadrature point
 // ---------------------------------------------------------------------------
-static const double Q4_GP = 0.577350269189626;  // FinEtools GaussRule(2,2) abscissa
+static constexpr double Q4_GP = 0.577350269189626;  // FinEtools GaussRule(2,2) abscissa
 
 FS_HD void q4_point(int j, double &xi, double &eta)
 {
