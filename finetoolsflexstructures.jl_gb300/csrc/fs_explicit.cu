@@ -19,18 +19,35 @@
 // displacement kernel also writes a float copy of U and the product runs on
 // float values (a double product would spend one double conversion and one
 // double FMA per stored value, the scarcest pipe on GB300); the force,
-// acceleration and velocity updates stay in double.  The step loop is
-// captured once into a CUDA graph and replayed.
+// acceleration and velocity updates stay in double.  With FS_MIXED_COMP the
+// values are the same float blocks, but the displacement copy is a float
+// pair (hi, lo: U to about 48 bits) and K U is summed error-free in float
+// (Dot2 on the hi parts, the lo parts' products added to the error term), so
+// that only the rounding of K remains: the float sum of a row's products
+// cancels to a small fraction of its terms for a smooth displacement field,
+// and the float U copy and the float sum were measured to carry most of the
+// error of FS_MIXED.  The step loop is captured once into a CUDA graph and
+// replayed.
 #include <algorithm>
 #include <vector>
 
-#include "fs_internal.cuh"
+#include "fs_elem_common.cuh"
 
 namespace fs {
 
 static const int CD_TPB = 256;
 static const int CD_LANES = 8;  // lanes per CSR row
 static const int CD_GRAPH_STEPS = 64;
+
+// one entry of a displacement copy: double, float, or the float pair (hi, lo)
+// with hi = U rounded and lo = the rest rounded
+__device__ __forceinline__ void store_disp(double *p, double t) { *p = t; }
+__device__ __forceinline__ void store_disp(float *p, double t) { *p = (float)t; }
+__device__ __forceinline__ void store_disp(float2 *p, double t)
+{
+    const float h = (float)t;
+    *p = make_float2(h, (float)(t - (double)h));
+}
 
 __global__ void k_cd_disp(int64_t n, double dt, double dt2_2, double *U, double *cU, const double *V,
                           const double *A, float *U32)
@@ -43,6 +60,20 @@ __global__ void k_cd_disp(int64_t n, double dt, double dt2_2, double *U, double 
     cU[i] = (t - u) - y;
     U[i] = t;
     if (U32) U32[i] = (float)t;
+}
+
+// the CSR path's displacement update writing the float-pair copy
+__global__ void k_cd_disp_pair(int64_t n, double dt, double dt2_2, double *U, double *cU, const double *V,
+                               const double *A, float2 *U2)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double y = (dt * V[i] + dt2_2 * A[i]) - cU[i];
+    double u = U[i];
+    double t = u + y;
+    cU[i] = (t - u) - y;
+    U[i] = t;
+    store_disp(U2 + i, t);
 }
 
 // the same displacement update writing the node-padded copy read by the
@@ -59,7 +90,7 @@ __global__ void k_cd_disp_pad(int64_t n, double dt, double dt2_2, double *U, dou
     cU[i] = (t - u) - y;
     U[i] = t;
     const int32_t q = pad_of_dof[i];
-    if (q >= 0) xp[q] = (VT)t;
+    if (q >= 0) store_disp(xp + q, t);
 }
 
 // six contiguous values (8-byte aligned floats, 16-byte aligned doubles)
@@ -171,6 +202,96 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_bsr(int64_t nnodes, int64_t n, co
     cV[row] = cv;
 }
 
+// error-free accumulation of kv * (xh + xl) into (s, c): Dot2 on kv * xh,
+// the small product kv * xl added to the error term
+__device__ __forceinline__ void acc_pair(float &s, float &c, float kv, float2 x)
+{
+    dot2_step(s, c, kv, x.x);
+    c = __fmaf_rn(kv, x.y, c);
+}
+// (s1, c1) += (s2, c2) without losing the rounding of s1 + s2 (TwoSum)
+__device__ __forceinline__ void add_pair(float &s, float &c, float s2, float c2)
+{
+    const float t = __fadd_rn(s, s2);
+    const float z = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(s2, z));
+    c = __fadd_rn(__fadd_rn(c, c2), e);
+    s = t;
+}
+
+// The block product of k_cd_bsr with the float-pair displacement copy and
+// the error-free float sum (FS_MIXED_COMP); the rest of the step as there.
+__global__ void __launch_bounds__(CD_TPB) k_cd_bsr_comp(int64_t nnodes, int64_t n, const int32_t *dof,
+                                                      const int64_t *nbr_off, const int32_t *nbr, const float *blk,
+                                                      const float2 *xp, double *V, double *cV, double *A,
+                                                      const double *C, const double *invMC, double dt_2, CdLoad ld)
+{
+    const int t = threadIdx.x & 31;
+    if (t >= 30) return;
+    const int64_t r = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 5 + t / 6;
+    const int i = t % 6;
+    if (r >= nnodes) return;
+    const int32_t d = dof[(int64_t)i * nnodes + r];
+    if (d > n) return;
+    float s = 0.f, c = 0.f;
+    for (int64_t b = nbr_off[r], be = nbr_off[r + 1]; b < be; b++) {
+        float kv[6];
+        load6(blk + b * 36 + i * 6, kv);
+        const float4 *xq = reinterpret_cast<const float4 *>(xp + (int64_t)nbr[b] * 6);
+        const float4 x01 = xq[0], x23 = xq[1], x45 = xq[2];
+        acc_pair(s, c, kv[0], make_float2(x01.x, x01.y));
+        acc_pair(s, c, kv[1], make_float2(x01.z, x01.w));
+        acc_pair(s, c, kv[2], make_float2(x23.x, x23.y));
+        acc_pair(s, c, kv[3], make_float2(x23.z, x23.w));
+        acc_pair(s, c, kv[4], make_float2(x45.x, x45.y));
+        acc_pair(s, c, kv[5], make_float2(x45.z, x45.w));
+    }
+    const int64_t row = d - 1;
+    const double sv = (double)s + (double)c;
+    double a = A[row], v = V[row], cv = cV[row];
+    double f = ld.at(row);
+    f -= sv + C[row] * (v + dt_2 * a);
+    kahan_add(v, cv, dt_2 * a);
+    a = invMC[row] * f;
+    kahan_add(v, cv, dt_2 * a);
+    A[row] = a;
+    V[row] = v;
+    cV[row] = cv;
+}
+
+// The CSR product of k_cd_rows with the float-pair displacement copy and the
+// error-free float sum (FS_MIXED_COMP).
+__global__ void __launch_bounds__(CD_TPB) k_cd_rows_comp(int64_t n, const int64_t *rowptr, const int32_t *colidx,
+                                                       const float *vals, const float2 *Uk, double *V, double *cV,
+                                                       double *A, const double *C, const double *invMC, double dt_2,
+                                                       CdLoad ld)
+{
+    int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / CD_LANES;
+    const int sub = threadIdx.x & (CD_LANES - 1);
+    const unsigned mask = 0xffffffffu;
+    float s = 0.f, c = 0.f;
+    if (row < n) {
+        for (int64_t k = rowptr[row] + sub; k < rowptr[row + 1]; k += CD_LANES) acc_pair(s, c, vals[k], Uk[colidx[k]]);
+    }
+#pragma unroll
+    for (int o = CD_LANES / 2; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(mask, s, o), c2 = __shfl_xor_sync(mask, c, o);
+        add_pair(s, c, s2, c2);
+    }
+    if (row < n && sub == 0) {
+        const double sv = (double)s + (double)c;
+        double a = A[row], v = V[row], cv = cV[row];
+        double f = ld.at(row);
+        f -= sv + C[row] * (v + dt_2 * a);
+        kahan_add(v, cv, dt_2 * a);
+        a = invMC[row] * f;
+        kahan_add(v, cv, dt_2 * a);
+        A[row] = a;
+        V[row] = v;
+        cV[row] = cv;
+    }
+}
+
 // block (node r, neighbour slot s), entry (i, j) = K[dof(r,i), dof(nbr,j)]
 // (zero where either dof is excluded or the matrix has no entry), found by
 // binary search in the sorted CSR row; one warp per node
@@ -234,6 +355,12 @@ static int enqueue_steps(fs_ctx *c, int64_t nsteps)
                                                                 c->pat.nbr, (const double *)x.blk,
                                                                 (const double *)x.xp, x.V, x.cV, x.A, x.C,
                                                                 x.invMC, dt / 2, ld);
+            } else if (x.precision == FS_MIXED_COMP) {
+                k_cd_disp_pad<float2><<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A,
+                                                                     x.pad_of_dof, (float2 *)x.xp);
+                k_cd_bsr_comp<<<gb, CD_TPB, 0, c->stream>>>(x.nnodes, n, c->mesh.dof, c->pat.nbr_off, c->pat.nbr,
+                                                             (const float *)x.blk, (const float2 *)x.xp, x.V, x.cV,
+                                                             x.A, x.C, x.invMC, dt / 2, ld);
             } else {
                 k_cd_disp_pad<float><<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A,
                                                                     x.pad_of_dof, (float *)x.xp);
@@ -248,6 +375,13 @@ static int enqueue_steps(fs_ctx *c, int64_t nsteps)
     }
     for (int64_t s = 0; s < nsteps; s++) {
         ld.j = (int)s;
+        if (x.precision == FS_MIXED_COMP) {
+            k_cd_disp_pair<<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A, (float2 *)x.U32);
+            k_cd_rows_comp<<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, x.vals32,
+                                                          (const float2 *)x.U32, x.V, x.cV, x.A, x.C, x.invMC,
+                                                          dt / 2, ld);
+            continue;
+        }
         bool single = x.precision != FS_FP64;
         k_cd_disp<<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A, single ? x.U32 : nullptr);
         if (!single)
@@ -416,7 +550,8 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
     if (!c || !invMC || !C) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
     if (!c->mat_rowptr) return set_err(c, FS_ERR_STATE, "no stiffness assembled");
-    if (precision != FS_FP64 && precision != FS_MIXED) return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
+    if (precision != FS_FP64 && precision != FS_MIXED && precision != FS_MIXED_COMP)
+        return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
     if (!(dt > 0.0)) return set_err(c, FS_ERR_BAD_INPUT, "time step must be positive");
     auto &x = c->ex;
     if (x.exec) cudaGraphExecDestroy(x.exec);
@@ -448,12 +583,14 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
         int64_t nbr_total = 0;
         FS_CUDA(c, cudaMemcpyAsync(&nbr_total, c->pat.nbr_off + nn, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
         FS_CUDA(c, cudaStreamSynchronize(c->stream));
-        const size_t es = precision == FS_FP64 ? 8 : 4;
+        // block values: double or float; displacement copy: double, float,
+        // or float pairs (FS_MIXED_COMP)
+        const size_t es = precision == FS_FP64 ? 8 : 4, xs = precision == FS_MIXED ? 4 : 8;
         dfree(&x.blk);
         dfree(&x.xp);
         FS_CUDA(c, cudaMalloc(&x.blk, es * 36 * (size_t)std::max<int64_t>(nbr_total, 1)));
-        FS_CUDA(c, cudaMalloc(&x.xp, es * 6 * (size_t)nn));
-        FS_CUDA(c, cudaMemsetAsync(x.xp, 0, es * 6 * (size_t)nn, c->stream));
+        FS_CUDA(c, cudaMalloc(&x.xp, xs * 6 * (size_t)nn));
+        FS_CUDA(c, cudaMemsetAsync(x.xp, 0, xs * 6 * (size_t)nn, c->stream));
         FS_TRY(dalloc(c, &x.pad_of_dof, (size_t)n));
         FS_CUDA(c, cudaMemsetAsync(x.pad_of_dof, 0xff, sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1), c->stream));
         k_pad_map<<<(unsigned)((6 * nn + 255) / 256), 256, 0, c->stream>>>(nn, n, m.dof, x.pad_of_dof);
@@ -466,8 +603,9 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
                                                           c->pat.nbr_off, c->pat.nbr, (float *)x.blk);
         FS_CUDA(c, cudaGetLastError());
         x.nnodes = nn;
-    } else if (precision == FS_MIXED) {
-        FS_TRY(dalloc(c, &x.U32, (size_t)n));
+    } else if (precision != FS_FP64) {
+        // float copy of U, or float pairs (two floats a dof) for FS_MIXED_COMP
+        FS_TRY(dalloc(c, &x.U32, (size_t)n * (precision == FS_MIXED_COMP ? 2 : 1)));
         FS_TRY(dalloc(c, &x.vals32, (size_t)c->mat_nnz));
         if (c->mat_nnz)
             k_to_float<<<(unsigned)((c->mat_nnz + 255) / 256), 256, 0, c->stream>>>(c->mat_nnz, c->vals, x.vals32);
