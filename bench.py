@@ -372,13 +372,14 @@ def explicit_c5(torch, device=0, n=512, nsteps=10000, iters=200):
                 "omega_max": om.value, "dt": dt, "power_iterations": iters,
                 "final_u_rel_err_mixed_vs_fp64": float(np.abs(U32 - U64).max() / np.abs(U64).max()),
                 "final_u_rel_err_mixed_comp_vs_fp64": float(np.abs(Uc - U64).max() / np.abs(U64).max()),
-                "mixed_comp": "float block values, float-pair displacement copy, error-free float sum of K U",
+                "mixed_comp": "float block values with bf16 residuals, float-pair displacement copy, error-free "
+                              "float sum of K U",
                 "final_u_max": float(np.abs(U64).max()),
                 "format": "6x6 node blocks (block rows = node neighbour lists)", "blocks": nblocks,
                 "bytes_per_step_mixed": bsr_bytes(4), "bytes_per_step_fp64": bsr_bytes(8),
                 "hbm_gbs_mixed": bsr_bytes(4) * out["steps_per_s_mixed"] / 1e9,
-                "bytes_per_step_mixed_comp": bsr_bytes(4) + 6 * nn_ * 4,
-                "hbm_gbs_mixed_comp": (bsr_bytes(4) + 6 * nn_ * 4) * out["steps_per_s_mixed_comp"] / 1e9,
+                "bytes_per_step_mixed_comp": bsr_bytes(6) + 6 * nn_ * 2,
+                "hbm_gbs_mixed_comp": (bsr_bytes(6) + 6 * nn_ * 2) * out["steps_per_s_mixed_comp"] / 1e9,
                 "hbm_gbs_fp64": bsr_bytes(8) * out["steps_per_s_fp64"] / 1e9})
     ctx.close()
     return out

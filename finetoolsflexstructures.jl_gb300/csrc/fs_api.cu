@@ -218,7 +218,7 @@ int fs_ctx_destroy(fs_ctx *c)
     if (x.graph) cudaGraphDestroy(x.graph);
     dfree(&x.U); dfree(&x.V); dfree(&x.A); dfree(&x.F); dfree(&x.cU); dfree(&x.cV);
     dfree(&x.invMC); dfree(&x.C); dfree(&x.vals32); dfree(&x.U32);
-    dfree(&x.blk); dfree(&x.xp); dfree(&x.pad_of_dof);
+    dfree(&x.blk); dfree(&x.res); dfree(&x.xp); dfree(&x.pad_of_dof);
     dfree(&x.Fmag); dfree(&x.mul); dfree(&x.step);
     cudaFree(c->d_status);
     for (int k = 0; k < 4; k++)

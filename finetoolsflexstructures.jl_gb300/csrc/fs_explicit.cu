@@ -19,15 +19,18 @@
 // displacement kernel also writes a float copy of U and the product runs on
 // float values (a double product would spend one double conversion and one
 // double FMA per stored value, the scarcest pipe on GB300); the force,
-// acceleration and velocity updates stay in double.  With FS_MIXED_COMP the
-// values are the same float blocks, but the displacement copy is a float
-// pair (hi, lo: U to about 48 bits) and K U is summed error-free in float
-// (Dot2 on the hi parts, the lo parts' products added to the error term), so
-// that only the rounding of K remains: the float sum of a row's products
-// cancels to a small fraction of its terms for a smooth displacement field,
-// and the float U copy and the float sum were measured to carry most of the
-// error of FS_MIXED.  The step loop is captured once into a CUDA graph and
-// replayed.
+// acceleration and velocity updates stay in double.  With FS_MIXED_COMP each
+// value is kept as its float rounding plus the rounding's residual in bf16
+// (K to about 33 bits, 6 bytes a value), the displacement copy is a float
+// pair (hi, lo: U to about 48 bits), and K U is summed error-free in float
+// (Dot2 on the float value times hi; the products with lo and with the
+// residual added to the error term).  A row of K U is a small remainder of
+// its terms for a smooth displacement field, so the float copy of U, the
+// float sum and the float rounding of K each leave errors far above their
+// own 6e-8 in it (measured in that order of size).  The step loop is
+// captured once into a CUDA graph and replayed.
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <vector>
 
@@ -202,12 +205,25 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_bsr(int64_t nnodes, int64_t n, co
     cV[row] = cv;
 }
 
-// error-free accumulation of kv * (xh + xl) into (s, c): Dot2 on kv * xh,
-// the small product kv * xl added to the error term
-__device__ __forceinline__ void acc_pair(float &s, float &c, float kv, float2 x)
+// error-free accumulation of (kv + kr) * (xh + xl) into (s, c): Dot2 on
+// kv * xh, the small products kv * xl and kr * xh added to the error term
+// (kr * xl is below the error of the result)
+__device__ __forceinline__ void acc_pair(float &s, float &c, float kv, float kr, float2 x)
 {
     dot2_step(s, c, kv, x.x);
     c = __fmaf_rn(kv, x.y, c);
+    c = __fmaf_rn(kr, x.x, c);
+}
+// six bf16 residuals (4-byte aligned) as floats
+__device__ __forceinline__ void load6_bf16(const __nv_bfloat16 *p, float v[6])
+{
+    const __nv_bfloat162 *q = reinterpret_cast<const __nv_bfloat162 *>(p);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float2 f = __bfloat1622float2(q[k]);
+        v[2 * k] = f.x;
+        v[2 * k + 1] = f.y;
+    }
 }
 // (s1, c1) += (s2, c2) without losing the rounding of s1 + s2 (TwoSum)
 __device__ __forceinline__ void add_pair(float &s, float &c, float s2, float c2)
@@ -223,8 +239,9 @@ __device__ __forceinline__ void add_pair(float &s, float &c, float s2, float c2)
 // the error-free float sum (FS_MIXED_COMP); the rest of the step as there.
 __global__ void __launch_bounds__(CD_TPB) k_cd_bsr_comp(int64_t nnodes, int64_t n, const int32_t *dof,
                                                       const int64_t *nbr_off, const int32_t *nbr, const float *blk,
-                                                      const float2 *xp, double *V, double *cV, double *A,
-                                                      const double *C, const double *invMC, double dt_2, CdLoad ld)
+                                                      const __nv_bfloat16 *res, const float2 *xp, double *V,
+                                                      double *cV, double *A, const double *C, const double *invMC,
+                                                      double dt_2, CdLoad ld)
 {
     const int t = threadIdx.x & 31;
     if (t >= 30) return;
@@ -235,16 +252,17 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_bsr_comp(int64_t nnodes, int64_t 
     if (d > n) return;
     float s = 0.f, c = 0.f;
     for (int64_t b = nbr_off[r], be = nbr_off[r + 1]; b < be; b++) {
-        float kv[6];
+        float kv[6], kr[6];
         load6(blk + b * 36 + i * 6, kv);
+        load6_bf16(res + b * 36 + i * 6, kr);
         const float4 *xq = reinterpret_cast<const float4 *>(xp + (int64_t)nbr[b] * 6);
         const float4 x01 = xq[0], x23 = xq[1], x45 = xq[2];
-        acc_pair(s, c, kv[0], make_float2(x01.x, x01.y));
-        acc_pair(s, c, kv[1], make_float2(x01.z, x01.w));
-        acc_pair(s, c, kv[2], make_float2(x23.x, x23.y));
-        acc_pair(s, c, kv[3], make_float2(x23.z, x23.w));
-        acc_pair(s, c, kv[4], make_float2(x45.x, x45.y));
-        acc_pair(s, c, kv[5], make_float2(x45.z, x45.w));
+        acc_pair(s, c, kv[0], kr[0], make_float2(x01.x, x01.y));
+        acc_pair(s, c, kv[1], kr[1], make_float2(x01.z, x01.w));
+        acc_pair(s, c, kv[2], kr[2], make_float2(x23.x, x23.y));
+        acc_pair(s, c, kv[3], kr[3], make_float2(x23.z, x23.w));
+        acc_pair(s, c, kv[4], kr[4], make_float2(x45.x, x45.y));
+        acc_pair(s, c, kv[5], kr[5], make_float2(x45.z, x45.w));
     }
     const int64_t row = d - 1;
     const double sv = (double)s + (double)c;
@@ -262,16 +280,16 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_bsr_comp(int64_t nnodes, int64_t 
 // The CSR product of k_cd_rows with the float-pair displacement copy and the
 // error-free float sum (FS_MIXED_COMP).
 __global__ void __launch_bounds__(CD_TPB) k_cd_rows_comp(int64_t n, const int64_t *rowptr, const int32_t *colidx,
-                                                       const float *vals, const float2 *Uk, double *V, double *cV,
-                                                       double *A, const double *C, const double *invMC, double dt_2,
-                                                       CdLoad ld)
+                                                       const float *vals, const __nv_bfloat16 *res,
+                                                       const float2 *Uk, double *V, double *cV, double *A,
+                                                       const double *C, const double *invMC, double dt_2, CdLoad ld)
 {
     int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / CD_LANES;
     const int sub = threadIdx.x & (CD_LANES - 1);
     const unsigned mask = 0xffffffffu;
     float s = 0.f, c = 0.f;
     if (row < n) {
-        for (int64_t k = rowptr[row] + sub; k < rowptr[row + 1]; k += CD_LANES) acc_pair(s, c, vals[k], Uk[colidx[k]]);
+        for (int64_t k = rowptr[row] + sub; k < rowptr[row + 1]; k += CD_LANES) acc_pair(s, c, vals[k], __bfloat162float(res[k]), Uk[colidx[k]]);
     }
 #pragma unroll
     for (int o = CD_LANES / 2; o > 0; o >>= 1) {
@@ -326,6 +344,50 @@ __global__ void k_bsr_fill(int64_t nnodes, int64_t n, const int32_t *dof, const 
     }
 }
 
+// float values and their bf16 residuals: hi = float(v), res = v - hi
+__device__ __forceinline__ void split_value(double v, float &hi, __nv_bfloat16 &res)
+{
+    hi = (float)v;
+    res = __float2bfloat16_rn((float)(v - (double)hi));
+}
+
+// the block form of k_bsr_fill with float values and bf16 residuals
+__global__ void k_bsr_fill_split(int64_t nnodes, int64_t n, const int32_t *dof, const int64_t *rowptr,
+                                 const int32_t *colidx, const double *vals, const int64_t *nbr_off, const int32_t *nbr,
+                                 float *blk, __nv_bfloat16 *res)
+{
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= nnodes) return;
+    const int64_t off = nbr_off[r];
+    const int ns = (int)(nbr_off[r + 1] - off);
+    for (int idx = lane; idx < ns * 36; idx += 32) {
+        const int sl = idx / 36, ij = idx - 36 * sl, i = ij / 6, j = ij - 6 * i;
+        const int32_t d = dof[(int64_t)i * nnodes + r];
+        const int32_t e = dof[(int64_t)j * nnodes + nbr[off + sl]];
+        double v = 0.0;
+        if (d <= n && e <= n) {
+            int64_t lo = rowptr[d - 1], hi = rowptr[d] - 1;
+            while (lo <= hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                const int32_t cc = colidx[mid];
+                if (cc == e - 1) {
+                    v = vals[mid];
+                    break;
+                }
+                if (cc < e - 1) lo = mid + 1; else hi = mid - 1;
+            }
+        }
+        split_value(v, blk[(off + sl) * 36 + ij], res[(off + sl) * 36 + ij]);
+    }
+}
+
+__global__ void k_split_values(int64_t n, const double *src, float *hi, __nv_bfloat16 *res)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) split_value(src[i], hi[i], res[i]);
+}
+
 __global__ void k_pad_map(int64_t nnodes, int64_t n, const int32_t *dof, int32_t *pad_of_dof)
 {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -359,8 +421,9 @@ static int enqueue_steps(fs_ctx *c, int64_t nsteps)
                 k_cd_disp_pad<float2><<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A,
                                                                      x.pad_of_dof, (float2 *)x.xp);
                 k_cd_bsr_comp<<<gb, CD_TPB, 0, c->stream>>>(x.nnodes, n, c->mesh.dof, c->pat.nbr_off, c->pat.nbr,
-                                                             (const float *)x.blk, (const float2 *)x.xp, x.V, x.cV,
-                                                             x.A, x.C, x.invMC, dt / 2, ld);
+                                                             (const float *)x.blk, (const __nv_bfloat16 *)x.res,
+                                                             (const float2 *)x.xp, x.V, x.cV, x.A, x.C, x.invMC,
+                                                             dt / 2, ld);
             } else {
                 k_cd_disp_pad<float><<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A,
                                                                     x.pad_of_dof, (float *)x.xp);
@@ -378,8 +441,8 @@ static int enqueue_steps(fs_ctx *c, int64_t nsteps)
         if (x.precision == FS_MIXED_COMP) {
             k_cd_disp_pair<<<g1, CD_TPB, 0, c->stream>>>(n, dt, dt * dt / 2, x.U, x.cU, x.V, x.A, (float2 *)x.U32);
             k_cd_rows_comp<<<g2, CD_TPB, 0, c->stream>>>(n, c->mat_rowptr, c->mat_colidx, x.vals32,
-                                                          (const float2 *)x.U32, x.V, x.cV, x.A, x.C, x.invMC,
-                                                          dt / 2, ld);
+                                                          (const __nv_bfloat16 *)x.res, (const float2 *)x.U32, x.V,
+                                                          x.cV, x.A, x.C, x.invMC, dt / 2, ld);
             continue;
         }
         bool single = x.precision != FS_FP64;
@@ -595,10 +658,16 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
         FS_CUDA(c, cudaMemsetAsync(x.pad_of_dof, 0xff, sizeof(int32_t) * (size_t)std::max<int64_t>(n, 1), c->stream));
         k_pad_map<<<(unsigned)((6 * nn + 255) / 256), 256, 0, c->stream>>>(nn, n, m.dof, x.pad_of_dof);
         const unsigned gw = (unsigned)((nn * 32 + 255) / 256);
+        dfree(&x.res);
         if (precision == FS_FP64)
             k_bsr_fill<double><<<gw, 256, 0, c->stream>>>(nn, n, m.dof, c->mat_rowptr, c->mat_colidx, c->vals,
                                                            c->pat.nbr_off, c->pat.nbr, (double *)x.blk);
-        else
+        else if (precision == FS_MIXED_COMP) {
+            FS_CUDA(c, cudaMalloc(&x.res, 2 * 36 * (size_t)std::max<int64_t>(nbr_total, 1)));
+            k_bsr_fill_split<<<gw, 256, 0, c->stream>>>(nn, n, m.dof, c->mat_rowptr, c->mat_colidx, c->vals,
+                                                         c->pat.nbr_off, c->pat.nbr, (float *)x.blk,
+                                                         (__nv_bfloat16 *)x.res);
+        } else
             k_bsr_fill<float><<<gw, 256, 0, c->stream>>>(nn, n, m.dof, c->mat_rowptr, c->mat_colidx, c->vals,
                                                           c->pat.nbr_off, c->pat.nbr, (float *)x.blk);
         FS_CUDA(c, cudaGetLastError());
@@ -607,7 +676,13 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
         // float copy of U, or float pairs (two floats a dof) for FS_MIXED_COMP
         FS_TRY(dalloc(c, &x.U32, (size_t)n * (precision == FS_MIXED_COMP ? 2 : 1)));
         FS_TRY(dalloc(c, &x.vals32, (size_t)c->mat_nnz));
-        if (c->mat_nnz)
+        dfree(&x.res);
+        if (precision == FS_MIXED_COMP) {
+            FS_CUDA(c, cudaMalloc(&x.res, 2 * (size_t)std::max<int64_t>(c->mat_nnz, 1)));
+            if (c->mat_nnz)
+                k_split_values<<<(unsigned)((c->mat_nnz + 255) / 256), 256, 0, c->stream>>>(
+                    c->mat_nnz, c->vals, x.vals32, (__nv_bfloat16 *)x.res);
+        } else if (c->mat_nnz)
             k_to_float<<<(unsigned)((c->mat_nnz + 255) / 256), 256, 0, c->stream>>>(c->mat_nnz, c->vals, x.vals32);
         FS_CUDA(c, cudaGetLastError());
     }

@@ -163,6 +163,9 @@ struct fs_ctx {
         bool bsr = false;
         int64_t nnodes = 0;
         void *blk = nullptr;          // nbr_total x 36 (float or double)
+        void *res = nullptr;          // FS_MIXED_COMP: the rounding residual of the float
+                                      // values (K - float(K)) in bf16, same layout as blk
+                                      // (block form) or vals32 (CSR form)
         void *xp = nullptr;           // displacement copy, 6 per node (float or double)
         int32_t *pad_of_dof = nullptr;  // dof -> node * 6 + component
         bool ready = false;

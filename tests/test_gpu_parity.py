@@ -233,8 +233,9 @@ def test_explicit_steps_match_oracle():
     # FP64: double restoring force, so only rounding differs (Kahan state vs plain).
     # Mixed: the restoring force K U is formed in float from float values; K U is
     # a small residual of large terms, so its float rounding shows at ~1e-5 of the
-    # velocity after 200 steps.
-    for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 2e-4)):
+    # velocity after 200 steps (measured 5.4e-5).  Compensated: float values with
+    # bf16 residuals, a float-pair U and an error-free float sum (measured 3.5e-9).
+    for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 2e-4), (F.FS_MIXED_COMP, 1e-7)):
         ctx = femm.ctx
         import ctypes
         from flexshell._lib import ptr
@@ -292,7 +293,7 @@ def test_explicit_load_matches_oracle():
     U2, V2, A2 = U.copy(), V.copy(), A.copy()
     O.cd_steps(K.indptr, K.indices, K.data, invMC, C, dt, 50, U2, V2, A2, Fmag=Fmag, mul=mul, step0=nsteps)
     ctx = femm.ctx
-    for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 2e-4)):
+    for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 2e-4), (F.FS_MIXED_COMP, 1e-7)):
         ctx.call("fs_explicit_setup", prec, ptr(np.ascontiguousarray(invMC)), ptr(np.ascontiguousarray(C)),
                  ctypes.c_double(dt))
         z = np.zeros(nfree)
@@ -499,4 +500,57 @@ def test_two_phase_copy_equals_stiffness_and_copy(precision):
     femm.ctx.call("fs_stiffness_copy", precision, n, ptr(colptr), ptr(rowval), ptr(nzval))
     assert np.array_equal(colptr - 1, K.indptr) and np.array_equal(rowval - 1, K.indices)
     assert np.array_equal(nzval, K.data)
+    femm.close()
+
+
+def test_explicit_smooth_field_error_by_mode():
+    """The explicit configuration at 48 x 48 (Q4RS, t = 0.01, steel, simply
+    supported, V0 = 1e-3 sin(pi x) sin(pi y) plus seeded noise, 0.9 dt_crit,
+    1,500 steps): final displacements of the mixed and compensated steps
+    against the FP64 step.  A smooth field is where K U cancels most: the
+    plain mixed step is off by 1e-5..1e-4 of max |U| here, the compensated
+    one (float values with bf16 residuals, float-pair U, error-free float
+    sum) by 1e-9..1e-8 (9.9e-9 at 128 x 128 after 2,500 steps, 5.5e-7 at
+    512 x 512 after 10,000)."""
+    import ctypes
+    from flexshell import materials, mesh
+    from flexshell._lib import ptr
+    n, nsteps = 48, 1500
+    xyz, conn = mesh.jittered_plate_q(n, 1.0, 0.0, 0, None)
+    fixed = np.zeros((xyz.shape[0], 6), bool)
+    x, y = xyz[:, 0], xyz[:, 1]
+    fixed[(x < 1e-12) | (x > 1 - 1e-12) | (y < 1e-12) | (y > 1 - 1e-12), 2] = True
+    dof, nfree = mesh.numberdofs(fixed)
+    femm = F.FEMMShellQ4RS(conn, 0.01, materials.MatDeforElastIso(200e9, 0.3, 7850.0))
+    geom0 = F.NodalField(xyz)
+    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(dof)
+    femm.associategeometry(geom0)
+    m = femm.mass(F.SysmatAssemblerFFBlock(F.SysmatAssemblerSparseDiag(), nfree), geom0, dchi).diagonal()
+    femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi)
+    om = ctypes.c_double()
+    femm.ctx.call("fs_power_iteration", ptr(np.ascontiguousarray(m)), ctypes.c_int64(300), ctypes.c_uint64(1),
+                  ctypes.byref(om))
+    dt = 0.9 * 2 / om.value
+    rng = np.random.Generator(np.random.PCG64(5))
+    V0 = np.zeros(nfree)
+    wd = dof[:, 2]
+    fw = wd <= nfree
+    V0[wd[fw] - 1] = 1e-3 * np.sin(np.pi * x[fw]) * np.sin(np.pi * y[fw]) + rng.normal(0, 1e-5, fw.sum())
+    invMC = np.ascontiguousarray(1.0 / m)
+    C = np.zeros(nfree)
+    finals = {}
+    for prec in (F.FS_FP64, F.FS_MIXED, F.FS_MIXED_COMP):
+        femm.ctx.call("fs_explicit_setup", prec, ptr(invMC), ptr(C), ctypes.c_double(dt))
+        z = np.zeros(nfree)
+        femm.ctx.call("fs_explicit_set_state", ptr(z), ptr(np.ascontiguousarray(V0)), ptr(z))
+        femm.ctx.call("fs_explicit_run", ctypes.c_int64(nsteps))
+        U = np.zeros(nfree)
+        femm.ctx.call("fs_explicit_get_state", ptr(U), None, None)
+        finals[prec] = U
+    ref = finals[F.FS_FP64]
+    err = {p: np.abs(finals[p] - ref).max() / np.abs(ref).max() for p in (F.FS_MIXED, F.FS_MIXED_COMP)}
+    assert err[F.FS_MIXED] <= 1e-3, err
+    assert err[F.FS_MIXED_COMP] <= 1e-7, err
+    assert err[F.FS_MIXED_COMP] <= err[F.FS_MIXED] / 100, err
     femm.close()
