@@ -7,8 +7,11 @@ driver code calls them unchanged:
 
     stiffness(femm::FEMMShellT3FF, assembler, geom0, u1, Rfield1, dchi)
     mass(femm::FEMMShellT3FF, assembler, geom0, dchi)
+    restoringforce(femm::FEMMShellT3FF, assembler, geom0, u1, Rfield1, dchi)
 
-(and the same for FEMMShellQ4RS, FEMMShellT3FFComp, FEMMShellQ4RSComp),
+(and the same for FEMMShellQ4RS, FEMMShellT3FFComp, FEMMShellQ4RSComp; a
+SysmatAssemblerSparseCSRSymm assembler gives a SparseMatrixCSR, the others a
+SparseMatrixCSC),
 
     inspectintegpoints(femm, geom0, u, dT, felist, inspector, idat, quantity; outputcsys)
 
@@ -24,18 +27,41 @@ and, for the distributed loads on a shell element set,
 
     gpu_distribloads(femm::FEMMBase, assembler, geom, P, fi, m)
 
+the central-difference loop of the explicit examples on the FEMM's last
+stiffness (plate_expl_examples.jl:61-94),
+
+    gpu_cd_loop!(femm, M, ksi, omegad, U0, V0, tend, dt, force!, peek; ...)
+
+and the shift-invert operator of a modal analysis (K - sigma M factorised on
+the GPU), for an eigensolver that takes a user operator:
+
+    gpu_shift_invert(femm, M_ff, sigma)
+
 `associategeometry!` stays the reference's own; its normals are passed in.
+The thickness is the IntegDomain's `otherdimension` at each element's
+centroid (the T3FF loop evaluates it there, src/FEMMShellT3FFModule.jl:677;
+the Q4RS loop per Gauss point, src/FEMMShellQ4RSModule.jl:924: a thickness
+that varies inside a quadrilateral is taken at its centroid).
 Not exercised in this repository (no Julia toolchain here); it is the
 binding a maintainer adds next to the reference.
 """
 module FlexShellGPU
 
 using SparseArrays
+using SparseMatricesCSR
+using LinearAlgebra
 using FinEtools
 using FinEtoolsFlexStructures.FEMMShellT3FFModule: FEMMShellT3FF
 using FinEtoolsFlexStructures.FEMMShellQ4RSModule: FEMMShellQ4RS
+using FinEtoolsFlexStructures.FEMMShellT3FFCompModule: FEMMShellT3FFComp
+using FinEtoolsFlexStructures.FEMMShellQ4RSCompModule: FEMMShellQ4RSComp
+using FinEtoolsFlexStructures.AssemblyModule: SysmatAssemblerSparseCSRSymm
+using FinEtoolsFlexStructures.CompositeLayupModule: laminate_stiffnesses!, laminate_transverse_stiffness!,
+    laminate_inertia!, thickness
 import FinEtoolsFlexStructures.FEMMShellT3FFModule: stiffness, mass
 import FinEtoolsFlexStructures.FEMMShellQ4RSModule: stiffness, mass
+import FinEtoolsFlexStructures.FEMMShellT3FFCompModule: stiffness, mass
+import FinEtoolsFlexStructures.FEMMShellQ4RSCompModule: stiffness, mass
 import FinEtoolsFlexStructures.FEMMShellT3FFModule: inspectintegpoints
 import FinEtoolsFlexStructures.FEMMShellQ4RSModule: inspectintegpoints
 using FinEtoolsFlexStructures.FEMMCorotBeamModule: FEMMCorotBeam
@@ -46,7 +72,7 @@ const libflexshell = get(ENV, "FLEXSHELL_LIB", "libflexshell.so")
 
 const FS_T3FF, FS_T3FFCOMP, FS_Q4RS, FS_Q4RSCOMP, FS_COROTBEAM = 0, 1, 2, 3, 4
 const FS_BEAM_STIFFNESS, FS_BEAM_GEOSTIFFNESS, FS_BEAM_MASS, FS_BEAM_GYROSCOPIC = 0, 1, 2, 3
-const FS_FP64, FS_MIXED = 0, 1
+const FS_FP64, FS_MIXED, FS_MIXED_COMP = 0, 1, 2
 const FS_ASM_SPARSE, FS_ASM_SPARSE_SYMM, FS_ASM_DIAG = 0, 1, 2
 
 # fs_shell_params (include/flexshell.h)
@@ -60,6 +86,18 @@ struct FsShellParams
     Dt::NTuple{4,Float64}
     rho::Float64
     thickness::Float64
+end
+
+# fs_layup_group (include/flexshell.h)
+struct FsLayupGroup
+    A::NTuple{9,Float64}
+    B::NTuple{9,Float64}
+    D::NTuple{9,Float64}
+    H::NTuple{4,Float64}
+    csmat::NTuple{9,Float64}
+    thickness::Float64
+    mass_density::Float64
+    moi_density::Float64
 end
 
 mutable struct Ctx
@@ -102,20 +140,81 @@ asm_mode(::SysmatAssemblerSparseSymm) = FS_ASM_SPARSE_SYMM
 asm_mode(::SysmatAssemblerSparseDiag) = FS_ASM_DIAG
 asm_mode(::AbstractSysmatAssembler) = FS_ASM_SPARSE
 
+is_layered(femm) = femm isa FEMMShellT3FFComp || femm isa FEMMShellQ4RSComp
+
+# element centroid (1 x 3) and the edge Jacobian J0 = [x2 - x1, x3 - x1] (3 x 2)
+function centroid_and_J0(geom0, c)
+    X = geom0.values[collect(c), :]
+    return sum(X, dims = 1) ./ size(X, 1), hcat(X[2, :] - X[1, :], X[3, :] - X[1, :])
+end
+
+# the assembly order of a layered FEMM (layup group by layup group,
+# src/FEMMShellT3FFCompModule.jl:600-606) and its groups: one per layup whose
+# csys is constant, one per element of a layup whose csys varies (its matrix
+# evaluated at the element's centroid, as the element loop does)
+function layup_tables(femm, geom0)
+    fes = femm.integdomain.fes
+    order = Int64[]
+    groups = FsLayupGroup[]
+    egroup = zeros(Int32, count(fes))
+    A, B, D, H = zeros(3, 3), zeros(3, 3), zeros(3, 3), zeros(2, 2)
+    for (layup, eset) in femm.layup_groups
+        laminate_stiffnesses!(layup, A, B, D)
+        laminate_transverse_stiffness!(layup, H)
+        md, mi = laminate_inertia!(layup)
+        mk(cs) = FsLayupGroup(Tuple(vec(A)), Tuple(vec(B)), Tuple(vec(D)), Tuple(vec(H)), Tuple(vec(cs)),
+            thickness(layup), md, mi)
+        if layup.csys.isconstant
+            push!(groups, mk(csmat(layup.csys)))
+            egroup[eset] .= length(groups) - 1
+        else
+            for i in eset
+                loc, J0 = centroid_and_J0(geom0, fes.conn[i])
+                updatecsmat!(layup.csys, loc, J0, i, 0)
+                push!(groups, mk(copy(csmat(layup.csys))))
+                egroup[i] = length(groups) - 1
+            end
+        end
+        append!(order, eset)
+    end
+    return order, groups, egroup
+end
+
+# per-element thickness: otherdimension at the element centroid
+function element_thickness(femm, geom0)
+    fes = femm.integdomain.fes
+    nen = nodesperelem(fes)
+    Nc = fill(1.0 / nen, nen, 1)
+    t = zeros(count(fes))
+    for i in 1:count(fes)
+        loc, _ = centroid_and_J0(geom0, fes.conn[i])
+        t[i] = femm.integdomain.otherdimension(loc, fes.conn[i], Nc)
+    end
+    return t
+end
+
 function upload!(ctx, femm, etype, geom0, dchi)
     fes = femm.integdomain.fes
     conn = collect(reinterpret(Int, fes.conn))          # nen per element, 1-based
     xyz = geom0.values                                  # nnodes x 3, column-major
+    layered = is_layered(femm)
+    order, groups, egroup = layered ? layup_tables(femm, geom0) : (Int64[], FsLayupGroup[], Int32[])
     check(ctx, ccall((:fs_mesh_set, libflexshell), Cint,
         (Ptr{Cvoid}, Cint, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
-        ctx.h, etype, size(xyz, 1), xyz, count(fes), conn, C_NULL, dchi === nothing ? C_NULL : dchi.dofnums))
-    Dps, Dt = femm_material_matrices(femm)
-    t = femm.integdomain.otherdimension(zeros(1, 3), fes.conn[1], zeros(1, 1))
-    p = FsShellParams(etype == FS_T3FF ? femm.transv_shear_formulation : 0, 0,
-        femm.drilling_stiffness_scale, femm.threshold_angle, stab_coefficient(femm.stab_fun),
-        Tuple(vec(Dps)), Tuple(vec(Dt)), massdensity(femm.material), t)
+        ctx.h, etype, size(xyz, 1), xyz, count(fes), conn, layered ? order : C_NULL,
+        dchi === nothing ? C_NULL : dchi.dofnums))
+    Dps, Dt = layered ? (Matrix(1.0I, 3, 3), Matrix(1.0I, 2, 2)) : femm_material_matrices(femm)
+    rho = layered ? 0.0 : massdensity(femm.material)
+    tsf = (etype == FS_T3FF || etype == FS_T3FFCOMP) ? femm.transv_shear_formulation : 0
+    p = FsShellParams(tsf, 0, femm.drilling_stiffness_scale, femm.threshold_angle,
+        stab_coefficient(femm.stab_fun), Tuple(vec(Dps)), Tuple(vec(Dt)), rho, 0.0)
+    th = layered ? C_NULL : element_thickness(femm, geom0)
     check(ctx, ccall((:fs_params_set, libflexshell), Cint, (Ptr{Cvoid}, Ref{FsShellParams}, Ptr{Float64}),
-        ctx.h, p, C_NULL))
+        ctx.h, p, th))
+    if layered
+        check(ctx, ccall((:fs_layups_set, libflexshell), Cint, (Ptr{Cvoid}, Int32, Ptr{FsLayupGroup}, Ptr{Int32}),
+            ctx.h, length(groups), groups, egroup))
+    end
     # normals from the reference's associategeometry! (honours a user mcsys)
     check(ctx, ccall((:fs_normals_set, libflexshell), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{UInt8}),
         ctx.h, femm._normals, UInt8.(femm._normal_valid)))
@@ -124,16 +223,24 @@ end
 femm_material_matrices(femm) =
     FinEtoolsFlexStructures.FEMMShellT3FFModule._shell_material_stiffness(femm.material)
 
-function fetch_csc(ctx, n, nnz)
+# the last matrix as the assembler's result type: the symmetric matrix's CSC
+# arrays are also its CSR arrays, so SysmatAssemblerSparseCSRSymm
+# (src/AssemblyModule.jl:47-53) gets them as a SparseMatrixCSR
+function fetch_matrix(ctx, n, nnz, assembler)
     colptr = Vector{Int64}(undef, n + 1)
     rowval = Vector{Int64}(undef, nnz)
     nzval = Vector{Float64}(undef, nnz)
     check(ctx, ccall((:fs_matrix_copy, libflexshell), Cint,
         (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}), ctx.h, colptr, rowval, nzval))
+    assembler isa SysmatAssemblerSparseCSRSymm && return SparseMatrixCSR{1}(n, n, colptr, rowval, nzval)
     return SparseMatrixCSC(n, n, colptr, rowval, nzval)
 end
+fetch_csc(ctx, n, nnz) = fetch_matrix(ctx, n, nnz, nothing)
 
-for (T, etype) in ((FEMMShellT3FF, FS_T3FF), (FEMMShellQ4RS, FS_Q4RS))
+const SHELLS = ((FEMMShellT3FF, FS_T3FF), (FEMMShellQ4RS, FS_Q4RS),
+    (FEMMShellT3FFComp, FS_T3FFCOMP), (FEMMShellQ4RSComp, FS_Q4RSCOMP))
+
+for (T, etype) in SHELLS
     @eval function stiffness(self::$T, assembler::ASS, geom0::NodalField{Float64},
         u1::NodalField{TI}, Rfield1::NodalField{TI}, dchi::NodalField{TI};
         precision = FS_FP64) where {ASS<:AbstractSysmatAssembler,TI<:Number}
@@ -143,7 +250,7 @@ for (T, etype) in ((FEMMShellT3FF, FS_T3FF), (FEMMShellQ4RS, FS_Q4RS))
         nnz = Ref{Int64}(0)
         check(ctx, ccall((:fs_stiffness, libflexshell), Cint, (Ptr{Cvoid}, Cint, Cint, Int64, Ref{Int64}),
             ctx.h, precision, asm_mode(assembler), nalldofs(dchi), nnz))
-        return fetch_csc(ctx, nalldofs(dchi), nnz[])
+        return fetch_matrix(ctx, nalldofs(dchi), nnz[], assembler)
     end
     @eval function mass(self::$T, assembler::A, geom0::NodalField{Float64},
         dchi::NodalField{TI}) where {A<:AbstractSysmatAssembler,TI<:Number}
@@ -153,7 +260,101 @@ for (T, etype) in ((FEMMShellT3FF, FS_T3FF), (FEMMShellQ4RS, FS_Q4RS))
         nnz = Ref{Int64}(0)
         check(ctx, ccall((:fs_mass, libflexshell), Cint, (Ptr{Cvoid}, Cint, Int64, Ref{Int64}),
             ctx.h, asm_mode(assembler), nalldofs(dchi), nnz))
-        return fetch_csc(ctx, nalldofs(dchi), nnz[])
+        return fetch_matrix(ctx, nalldofs(dchi), nnz[], assembler)
+    end
+    # -K U for the generalized displacements in dchi.values (translations and
+    # rotations of every node through dchi.dofnums): the shells' restoring
+    # force, which the reference has no method for (its explicit loop forms
+    # E = K U, plate_expl_examples.jl:85); the sign of FEMMCorotBeam's
+    # restoringforce (force on the nodes)
+    @eval function restoringforce(self::$T, assembler::AbstractSysvecAssembler, geom0::NodalField{Float64},
+        u1::NodalField{TI}, Rfield1::NodalField{TI}, dchi::NodalField{TI};
+        precision = FS_FP64) where {TI<:Number}
+        @assert self._associatedgeometry == true
+        ctx = context(self)
+        upload!(ctx, self, $etype, geom0, dchi)
+        n = nalldofs(dchi)
+        nnz = Ref{Int64}(0)
+        check(ctx, ccall((:fs_stiffness, libflexshell), Cint, (Ptr{Cvoid}, Cint, Cint, Int64, Ref{Int64}),
+            ctx.h, precision, FS_ASM_SPARSE, n, nnz))
+        U = zeros(n)
+        for k in eachindex(dchi.dofnums)
+            d = dchi.dofnums[k]
+            1 <= d <= n && (U[d] = dchi.values[k])
+        end
+        F = zeros(n)
+        check(ctx, ccall((:fs_restoring_force, libflexshell), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}),
+            ctx.h, U, F))
+        return F
+    end
+end
+
+# ---------------------------------------------------------------------------
+# _cd_loop!(M, K, ksi, U0, V0, tend, dt, force!, peek)
+# (examples/shells/dynamics/homogeneous/explicit/plate_expl_examples.jl:61-94)
+# on the GPU, K the last stiffness assembled for `femm` (assemble it with
+# stiffness(femm, ...) first): C = ksi 2 omegad diag(M), the same time-step
+# adjustment, and force!(F, t) evaluated on the host at every step time once
+# up front as F = g(t) Fmag (the examples' form): `force!` is called at t = 0
+# to give Fmag, `g(t)` scales it (g = t -> 1: a constant load).  The state is
+# copied back for peek(step, U, V, t) every `peek_every` steps.
+# ---------------------------------------------------------------------------
+function gpu_cd_loop!(femm, M, ksi, omegad, U0, V0, tend, dt, force!, peek;
+    g = t -> 1.0, peek_every = 1, precision = FS_MIXED_COMP)
+    ctx = context(femm)
+    m = Vector{Float64}(vec(diag(M)))
+    n = length(m)
+    C = (ksi * 2 * omegad) .* m
+    nsteps = Int64(round(tend / dt))
+    if nsteps * dt < tend
+        dt = tend / (nsteps + 1)
+    end
+    invMC = 1.0 ./ (m .+ (dt / 2) .* C)
+    check(ctx, ccall((:fs_explicit_setup, libflexshell), Cint,
+        (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Float64), ctx.h, precision, invMC, C, dt))
+    Fmag = zeros(n)
+    force!(Fmag, 0.0)
+    mul = [Float64(g(k * dt)) for k in 0:nsteps]
+    A0 = invMC .* (mul[1] .* Fmag)
+    check(ctx, ccall((:fs_explicit_set_state, libflexshell), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), ctx.h, Vector{Float64}(U0),
+        Vector{Float64}(V0), A0))
+    check(ctx, ccall((:fs_explicit_set_load, libflexshell), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Int64), ctx.h, Fmag, mul, length(mul), 0))
+    U, V, A = zeros(n), zeros(n), zeros(n)
+    peek(0, Vector{Float64}(U0), Vector{Float64}(V0), 0.0)
+    done = 0
+    while done < nsteps
+        k = min(max(peek_every, 1), nsteps - done)
+        check(ctx, ccall((:fs_explicit_run, libflexshell), Cint, (Ptr{Cvoid}, Int64), ctx.h, k))
+        done += k
+        check(ctx, ccall((:fs_explicit_get_state, libflexshell), Cint,
+            (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), ctx.h, U, V, A))
+        peek(done, U, V, done * dt)
+    end
+    return U, V, A
+end
+
+# ---------------------------------------------------------------------------
+# Shift-invert operator of a modal analysis: x = (K - sigma M)^{-1} b with K
+# the last stiffness assembled for `femm` (the free-free block, stiffness with
+# nrows = nfreedofs) and the lumped mass M (its diagonal), factorised once on
+# the GPU (fs_shift_factor); the returned function applies it
+# (fs_shift_solve), for an eigensolver that accepts such an operator in place
+# of eigs' own factorisation (test/test_composite_shell_dynamics.jl:70-76).
+# ---------------------------------------------------------------------------
+function gpu_shift_invert(femm, M, sigma)
+    ctx = context(femm)
+    m = Vector{Float64}(vec(diag(M)))
+    kd = Ref{Int64}(0)
+    check(ctx, ccall((:fs_shift_factor, libflexshell), Cint, (Ptr{Cvoid}, Float64, Ptr{Float64}, Ref{Int64}),
+        ctx.h, sigma, m, kd))
+    return function (b::AbstractVecOrMat)
+        B = Matrix{Float64}(reshape(b, length(m), :))
+        X = similar(B)
+        check(ctx, ccall((:fs_shift_solve, libflexshell), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}),
+            ctx.h, size(B, 2), B, X))
+        return b isa AbstractVector ? vec(X) : X
     end
 end
 
