@@ -670,6 +670,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-oracle", action="store_true", help="skip the full-size FP64 check against the oracle")
     ap.add_argument("--no-explicit", action="store_true")
+    ap.add_argument("--eig-n", type=int, default=256,
+                    help="quads per side of the layered plate of the 20-eigenvalue check (512: the reference's "
+                         "configuration, a 45 GB factor)")
     ap.add_argument("--explicit-only", action="store_true",
                     help="only the explicit-dynamics section, on an n x n Q4RS plate for 64 x steps steps "
                          "(a small case for profiling the step kernels)")
@@ -815,7 +818,7 @@ def main():
     ex = explicit_c5(torch, device=local) if not args.no_explicit else None
     bc3 = batched_c3(torch, device=local) if not args.no_explicit else None
     beams = corotbeam_lattice(torch, device=local) if not args.no_explicit else None
-    c4 = composite_c4(torch, device=local) if not args.no_explicit else None
+    c4 = composite_c4(torch, device=local, n_eig=args.eig_n) if not args.no_explicit else None
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
