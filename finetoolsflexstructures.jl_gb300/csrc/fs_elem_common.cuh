@@ -25,26 +25,29 @@ __device__ __forceinline__ void load_elem(const MeshDev &m, int64_t r, ElemIn<NN
     in.group = m.group ? m.group[r] : 0;
 }
 
-// 36 contiguous values of a 6x6 block (16-byte aligned) as 16-byte stores;
-// `transpose` writes acc^T.
-template <class R>
-__device__ __forceinline__ void store_block(R *o, const R (&acc)[6][6], bool transpose)
+// NI rows of a 6x6 block (6 NI contiguous values from a 16-byte boundary for
+// whole blocks, an 8-byte one for the half-blocks of float values): 16-byte
+// stores, or 8-byte ones for float half-blocks
+template <class R, int NI>
+__device__ __forceinline__ void store_rows(R *o, const R (&acc)[NI][6])
 {
-    constexpr int V = 16 / sizeof(R);
-    R buf[36];
-#pragma unroll
-    for (int i = 0; i < 6; i++)
-#pragma unroll
-        for (int j = 0; j < 6; j++) buf[i * 6 + j] = transpose ? acc[j][i] : acc[i][j];
-    if (V == 4) {
+    if (sizeof(R) == 4 && NI == 6) {
         float4 *o4 = reinterpret_cast<float4 *>(o);
 #pragma unroll
-        for (int q = 0; q < 9; q++)
-            o4[q] = make_float4((float)buf[4 * q], (float)buf[4 * q + 1], (float)buf[4 * q + 2], (float)buf[4 * q + 3]);
+        for (int q = 0; q < 9; q++) {
+            const int e = 4 * q;
+            o4[q] = make_float4((float)acc[e / 6][e % 6], (float)acc[(e + 1) / 6][(e + 1) % 6],
+                                (float)acc[(e + 2) / 6][(e + 2) % 6], (float)acc[(e + 3) / 6][(e + 3) % 6]);
+        }
+    } else if (sizeof(R) == 4) {
+        float2 *o2 = reinterpret_cast<float2 *>(o);
+#pragma unroll
+        for (int q = 0; q < 3 * NI; q++) o2[q] = make_float2((float)acc[q / 3][2 * (q % 3)], (float)acc[q / 3][2 * (q % 3) + 1]);
     } else {
         double2 *o2 = reinterpret_cast<double2 *>(o);
 #pragma unroll
-        for (int q = 0; q < 18; q++) o2[q] = make_double2((double)buf[2 * q], (double)buf[2 * q + 1]);
+        for (int q = 0; q < 3 * NI; q++)
+            o2[q] = make_double2((double)acc[q / 3][2 * (q % 3)], (double)acc[q / 3][2 * (q % 3) + 1]);
     }
 }
 
@@ -62,54 +65,171 @@ __device__ __forceinline__ void dot2_step(float &s, float &c, float a, float b)
     s = t;
 }
 
-// 36 entries (s + c) of a compensated block as float pairs (hi, lo), hi the
-// rounded sum and lo its error (Fast2Sum), with 16-byte stores
-__device__ __forceinline__ void store_block_pair(float2 *o, const float (&s)[6][6], const float (&c)[6][6])
-{
-    float4 *o4 = reinterpret_cast<float4 *>(o);
-#pragma unroll
-    for (int q = 0; q < 18; q++) {
-        float h[2], l[2];
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const int i = (2 * q + u) / 6, j = (2 * q + u) % 6;
-            h[u] = __fadd_rn(s[i][j], c[i][j]);
-            l[u] = __fsub_rn(c[i][j], __fsub_rn(h[u], s[i][j]));
-        }
-        o4[q] = make_float4(h[0], l[0], h[1], l[1]);
-    }
-}
-
-// Accumulator of one 6x6 node block of K = sum_rho row_rho row_rho^T: plain
-// in the row type, or (float rows into float pairs) error-free by Dot2.
-template <class R, bool PAIR> struct BlockAcc {
-    R v[6][6];
+// Accumulator of NI rows (6: a whole 6x6 node block of
+// K = sum_rho row_rho row_rho^T; 3: half of one) in the row type.  row()
+// adds the products ra[i] rb[j] of one row for i in [I0, I1), j in
+// [J0, J1) (i outer, j inner; contracted to FMAs); DIAG (a diagonal block,
+// ra = rb): only j >= i, store() mirroring the rest.  Products commute and
+// fma(x, y, z) = fma(y, x, z), so the mirrored entries are bitwise those the
+// full loop computes.
+template <class R, bool PAIR, int NI = 6> struct BlockAcc {
+    R v[NI][6];
     __device__ __forceinline__ void zero()
     {
 #pragma unroll
-        for (int i = 0; i < 6; i++)
+        for (int i = 0; i < NI; i++)
 #pragma unroll
             for (int j = 0; j < 6; j++) v[i][j] = 0;
     }
-    __device__ __forceinline__ void add(int i, int j, R x, R y) { v[i][j] += x * y; }
-    template <class S> __device__ __forceinline__ void store(S *o) { store_block<R>(reinterpret_cast<R *>(o), v, false); }
+    template <int I0, int I1, int J0, int J1, bool DIAG = false>
+    __device__ __forceinline__ void row(const R (&ra)[6], const R (&rb)[6])
+    {
+#pragma unroll
+        for (int i = I0; i < I1; i++)
+#pragma unroll
+            for (int j = J0; j < J1; j++)
+                if (!DIAG || j >= i) v[i][j] += ra[i] * rb[j];
+    }
+    template <bool DIAG = false, class S> __device__ __forceinline__ void store(S *o)
+    {
+        if (DIAG) {
+#pragma unroll
+            for (int i = 1; i < NI; i++)
+#pragma unroll
+                for (int j = 0; j < i; j++) v[i][j] = v[j][i];
+        }
+        store_rows<R, NI>(reinterpret_cast<R *>(o), v);
+    }
 };
-template <> struct BlockAcc<float, true> {
-    float s[6][6], c[6][6];
+
+// Two floats in one 64-bit register pair and the packed FP32x2 arithmetic of
+// the sm_100 family (add/sub/mul/fma .rn .f32x2): both halves rounded to
+// nearest as the scalar instructions round them, two per instruction.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 x2_pack(float lo, float hi)
+{
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void x2_unpack(f32x2 v, float &lo, float &hi) { asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v)); }
+__device__ __forceinline__ f32x2 x2_add(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 x2_sub(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b)
+{
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 x2_fma(f32x2 a, f32x2 b, f32x2 c)
+{
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// s + v by TwoSum (Knuth): s <- fl(s + v), returns the exact error
+__device__ __forceinline__ f32x2 x2_two_sum(f32x2 &s, f32x2 v)
+{
+    const f32x2 t = x2_add(s, v);
+    const f32x2 z = x2_sub(t, s);
+    const f32x2 e = x2_add(x2_sub(s, x2_sub(t, z)), x2_sub(v, z));
+    s = t;
+    return e;
+}
+
+// One step of a three-level compensated dot product on two entries at once
+// (the error-free transformations of Ogita, Rump and Oishi's Dot2, applied
+// once more to the compensation term): the product a b split exactly into p
+// and pl (m = fma(-a, b, p) = -pl exactly), p added to s by TwoSum (error e),
+// e added to c by TwoSum (error f), and f + pl added to d.  What is lost is
+// the rounding of d's terms, about 2^-24 of |d|, itself of the order of
+// 2^-48 of the sum of |a b|: far below Dot2's 2^-48 of that sum.
+__device__ __forceinline__ void dot3_step_x2(f32x2 &s, f32x2 &c, f32x2 &d, f32x2 a, f32x2 na, f32x2 b)
+{
+    const f32x2 p = x2_mul(a, b);
+    const f32x2 m = x2_fma(na, b, p);
+    const f32x2 e = x2_two_sum(s, p);
+    const f32x2 f = x2_two_sum(c, e);
+    d = x2_add(d, x2_sub(f, m));
+}
+
+// Float rows into float pairs (FS_MIXED_COMP): the three-level compensated
+// sums, entries (i, 2q) and (i, 2q + 1) in one packed register pair.  A row
+// reaching only one entry of a pair adds a zero product to the other, which
+// leaves its sums unchanged; DIAG: only the pairs holding an entry j >= i.
+// store() writes s + (c + d) as (hi, lo) float pairs: c + d rounded (below
+// the pair's last bit), then Fast2Sum; DIAG mirrors the entries j < i.
+template <int NI> struct BlockAcc<float, true, NI> {
+    f32x2 s[NI][3], c[NI][3], d[NI][3];
     __device__ __forceinline__ void zero()
     {
 #pragma unroll
-        for (int i = 0; i < 6; i++)
+        for (int i = 0; i < NI; i++)
 #pragma unroll
-            for (int j = 0; j < 6; j++) s[i][j] = c[i][j] = 0.f;
+            for (int q = 0; q < 3; q++) s[i][q] = c[i][q] = d[i][q] = 0ull;
     }
-    __device__ __forceinline__ void add(int i, int j, float x, float y) { dot2_step(s[i][j], c[i][j], x, y); }
-    template <class S> __device__ __forceinline__ void store(S *o) { store_block_pair(reinterpret_cast<float2 *>(o), s, c); }
+    template <int I0, int I1, int J0, int J1, bool DIAG = false>
+    __device__ __forceinline__ void row(const float (&ra)[6], const float (&rb)[6])
+    {
+        constexpr int Q0 = J0 / 2, Q1 = (J1 + 1) / 2;
+        f32x2 b2[3];
+#pragma unroll
+        for (int q = Q0; q < Q1; q++)
+            b2[q] = x2_pack(2 * q >= J0 ? rb[2 * q] : 0.f, 2 * q + 1 < J1 ? rb[2 * q + 1] : 0.f);
+#pragma unroll
+        for (int i = I0; i < I1; i++) {
+            const f32x2 a2 = x2_pack(ra[i], ra[i]), na2 = x2_pack(-ra[i], -ra[i]);
+#pragma unroll
+            for (int q = Q0; q < Q1; q++)
+                if (!DIAG || 2 * q + 1 >= i) dot3_step_x2(s[i][q], c[i][q], d[i][q], a2, na2, b2[q]);
+        }
+    }
+    template <bool DIAG = false, class S> __device__ __forceinline__ void store(S *o)
+    {
+        float h[NI][6], l[NI][6];
+#pragma unroll
+        for (int i = 0; i < NI; i++)
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                if (DIAG && 2 * q + 1 < i) continue;
+                const f32x2 cd = x2_add(c[i][q], d[i][q]);
+                const f32x2 hh = x2_add(s[i][q], cd);
+                const f32x2 ll = x2_sub(cd, x2_sub(hh, s[i][q]));
+                x2_unpack(hh, h[i][2 * q], h[i][2 * q + 1]);
+                x2_unpack(ll, l[i][2 * q], l[i][2 * q + 1]);
+            }
+        if (DIAG) {
+#pragma unroll
+            for (int i = 1; i < NI; i++)
+#pragma unroll
+                for (int j = 0; j < i; j++) {
+                    h[i][j] = h[j][i];
+                    l[i][j] = l[j][i];
+                }
+        }
+        float4 *o4 = reinterpret_cast<float4 *>(o);
+#pragma unroll
+        for (int i = 0; i < NI; i++)
+#pragma unroll
+            for (int q = 0; q < 3; q++)
+                o4[3 * i + q] = make_float4(h[i][2 * q], l[i][2 * q], h[i][2 * q + 1], l[i][2 * q + 1]);
+    }
 };
 
 // acc += sum over rows [r0, r1) of row[6a + i] row[6b + j] for i in
-// [I0, I1), j in [J0, J1): the sub-blocks a row can reach
-template <int I0, int I1, int J0, int J1, class R, class Acc>
+// [I0, I1), j in [J0, J1): the sub-blocks a row can reach (DIAG: a = b, the
+// upper triangle)
+template <int I0, int I1, int J0, int J1, bool DIAG = false, class R, class Acc>
 __device__ __forceinline__ void gram_rows(Acc &acc, const R *rows, int ND, int r0, int r1, int a, int b)
 {
     for (int rho = r0; rho < r1; rho++) {
@@ -119,17 +239,14 @@ __device__ __forceinline__ void gram_rows(Acc &acc, const R *rows, int ND, int r
         for (int i = I0; i < I1; i++) ra[i] = rr[6 * a + i];
 #pragma unroll
         for (int j = J0; j < J1; j++) rb[j] = rr[6 * b + j];
-#pragma unroll
-        for (int i = I0; i < I1; i++)
-#pragma unroll
-            for (int j = J0; j < J1; j++) acc.add(i, j, ra[i], rb[j]);
+        acc.template row<I0, I1, J0, J1, DIAG>(ra, rb);
     }
 }
 
 // acc += sum over rows [r0, r1) (stride RS from base) of row[NSTR a + i - IOFF]
 // row[NSTR b + j - IOFF] for i in [I0, I1), j in [J0, J1): the same products
 // as gram_rows on a compact row layout (rows holding a subset of the dofs)
-template <int I0, int I1, int J0, int J1, int RS, int NSTR, int IOFF, class R, class Acc>
+template <int I0, int I1, int J0, int J1, int RS, int NSTR, int IOFF, bool DIAG = false, class R, class Acc>
 __device__ __forceinline__ void gram_rows_c(Acc &acc, const R *base, int r0, int r1, int a, int b)
 {
     for (int rho = r0; rho < r1; rho++) {
@@ -139,10 +256,54 @@ __device__ __forceinline__ void gram_rows_c(Acc &acc, const R *base, int r0, int
         for (int i = I0; i < I1; i++) ra[i] = rr[NSTR * a + i - IOFF];
 #pragma unroll
         for (int j = J0; j < J1; j++) rb[j] = rr[NSTR * b + j - IOFF];
+        acc.template row<I0, I1, J0, J1, DIAG>(ra, rb);
+    }
+}
+
+// Half-block forms (a three-row accumulator): rows i0 .. i0 + 2 of block
+// (a, b), i0 = 0 or 3 at run time, in the stride-RS layout whose row holds
+// node c's dofs k at NSTR c + k.  The products of each entry and their order
+// are those of the whole-block forms.
+template <int J0, int J1, int RS, int NSTR, class R, class Acc>
+__device__ __forceinline__ void gram_rows_h(Acc &acc, const R *base, int r0, int r1, int a, int b, int i0)
+{
+    for (int rho = r0; rho < r1; rho++) {
+        const R *rr = base + rho * RS;
+        R ra[6], rb[6];
 #pragma unroll
-        for (int i = I0; i < I1; i++)
+        for (int i = 0; i < 3; i++) ra[i] = rr[NSTR * a + i0 + i];
 #pragma unroll
-            for (int j = J0; j < J1; j++) acc.add(i, j, ra[i], rb[j]);
+        for (int j = J0; j < J1; j++) rb[j] = rr[NSTR * b + j];
+        acc.template row<0, 3, J0, J1>(ra, rb);
+    }
+}
+
+// The upper node blocks of an NN-node element: diag(a) computes block
+// (a, a) (its upper triangle), off(a, b) block (a, b) for b > a.
+// Plain stores (float or double): one loop over the blocks, not unrolled,
+// choosing the diagonal or the off-diagonal form (the shorter code measured
+// 28 % faster for the float T3 kernel).  Float-pair stores: the diagonal
+// blocks, then the off-diagonal ones (4 % faster for those).
+template <int NN, bool PAIR, class D, class O>
+__device__ __forceinline__ void for_upper_blocks(D diag, O off)
+{
+    if constexpr (PAIR) {
+#pragma unroll 1
+        for (int a = 0; a < NN; a++) diag(a);
+#pragma unroll 1
+        for (int a = 0; a < NN; a++)
+#pragma unroll 1
+            for (int b = a + 1; b < NN; b++) off(a, b);
+    } else {
+#pragma unroll 1
+        for (int a = 0; a < NN; a++)
+#pragma unroll 1
+            for (int b = a; b < NN; b++) {
+                if (a == b)
+                    diag(a);
+                else
+                    off(a, b);
+            }
     }
 }
 
@@ -154,15 +315,22 @@ __device__ __forceinline__ void write_blocks_compact(const R *rows, S *out)
 {
     typedef CompactRows<NN, NS> L;
     constexpr bool PAIR = sizeof(S) == 8 && sizeof(R) == 4;
-    for (int a = 0; a < NN; a++)
-        for (int b = a; b < NN; b++) {
+    for_upper_blocks<NN, PAIR>(
+        [&](int a) {
+            BlockAcc<R, PAIR> acc;
+            acc.zero();
+            gram_rows_c<0, 3, 0, 3, L::MS, 3, 0, true>(acc, rows, 0, 3, a, a);
+            gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0, true>(acc, rows + L::BS, 0, 3 + NS, a, a);
+            gram_rows_c<3, 6, 3, 6, 3, 0, 3, true>(acc, rows + L::DR + 3 * a, 0, 1, a, a);
+            acc.template store<true>(out + ub(a, a, NN) * 36);
+        },
+        [&](int a, int b) {
             BlockAcc<R, PAIR> acc;
             acc.zero();
             gram_rows_c<0, 3, 0, 3, L::MS, 3, 0>(acc, rows, 0, 3, a, b);
             gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0>(acc, rows + L::BS, 0, 3 + NS, a, b);
-            if (a == b) gram_rows_c<3, 6, 3, 6, 3, 0, 3>(acc, rows + L::DR + 3 * a, 0, 1, a, b);
             acc.store(out + ub(a, b, NN) * 36);
-        }
+        });
 }
 
 // Upper node blocks of K = sum_rho row_rho row_rho^T.  Storage S: the row
@@ -176,19 +344,30 @@ __device__ __forceinline__ void write_blocks(const R *rows, int nrows, S *out)
 {
     constexpr bool PAIR = sizeof(S) == 8 && sizeof(R) == 4;
     const int ND = 6 * NN;
-    for (int a = 0; a < NN; a++)
-        for (int b = a; b < NN; b++) {
+    for_upper_blocks<NN, PAIR>(
+        [&](int a) {
+            BlockAcc<R, PAIR> acc;
+            acc.zero();
+            if (SPARSE) {
+                gram_rows<0, 3, 0, 3, true>(acc, rows, ND, 0, 3, a, a);
+                gram_rows<0, 6, 0, 6, true>(acc, rows, ND, 3, nrows - NN, a, a);
+                gram_rows<3, 6, 3, 6, true>(acc, rows, ND, nrows - NN + a, nrows - NN + a + 1, a, a);
+            } else {
+                gram_rows<0, 6, 0, 6, true>(acc, rows, ND, 0, nrows, a, a);
+            }
+            acc.template store<true>(out + ub(a, a, NN) * 36);
+        },
+        [&](int a, int b) {
             BlockAcc<R, PAIR> acc;
             acc.zero();
             if (SPARSE) {
                 gram_rows<0, 3, 0, 3>(acc, rows, ND, 0, 3, a, b);
                 gram_rows<0, 6, 0, 6>(acc, rows, ND, 3, nrows - NN, a, b);
-                if (a == b) gram_rows<3, 6, 3, 6>(acc, rows, ND, nrows - NN + a, nrows - NN + a + 1, a, b);
             } else {
                 gram_rows<0, 6, 0, 6>(acc, rows, ND, 0, nrows, a, b);
             }
             acc.store(out + ub(a, b, NN) * 36);
-        }
+        });
 }
 
 }  // namespace fs

@@ -146,28 +146,51 @@ __global__ void __launch_bounds__(128, 2) k_q4_elements(const MeshDev m, const M
     __syncwarp();
     if (!active) return;
     S *out = ke + r * (10 * 36);
-    // ten upper node blocks shared by the four lanes of the element
-    for (int bi = qp; bi < 10; bi += 4) {
-        int a = bi < 4 ? 0 : (bi < 7 ? 1 : (bi < 9 ? 2 : 3));
-        int b = a + (bi - (a == 0 ? 0 : (a == 1 ? 4 : (a == 2 ? 7 : 9))));
-        constexpr bool PAIR = sizeof(S) == 8 && sizeof(R) == 4;
+    constexpr bool PAIR = sizeof(S) == 8 && sizeof(R) == 4;
+    // The element's ten upper node blocks over its four lanes, every lane
+    // running the same code at each step: first the diagonal block (qp, qp)
+    // (its upper triangle), then the six off-diagonal blocks as twelve
+    // half-blocks (rows 0-2 of each, then rows 3-5), three per lane.
+    // Homogeneous elements: per Gauss point 3 membrane rows (translations
+    // only, so rows 0-2 of a block) and 5 bending/shear rows; then one
+    // drilling row per node (diagonal blocks only) -- the products and their
+    // order of the dense layout.
+    {
+        const int a = qp;
         BlockAcc<R, PAIR> acc;
         acc.zero();
         if constexpr (!COMP) {
-            // homogeneous: per Gauss point 3 membrane rows (translations only)
-            // and 5 bending/shear rows; then one drilling row per node -- the
-            // products and their order of the dense layout
 #pragma unroll 1
             for (int j = 0; j < 4; j++) {
                 const R *gpb = rows + j * Q4Compact::GP;
-                gram_rows_c<0, 3, 0, 3, Q4Compact::MS, 3, 0>(acc, gpb, 0, 3, a, b);
-                gram_rows_c<0, 6, 0, 6, Q4Compact::BSS, 6, 0>(acc, gpb + Q4Compact::BS, 0, 5, a, b);
+                gram_rows_c<0, 3, 0, 3, Q4Compact::MS, 3, 0, true>(acc, gpb, 0, 3, a, a);
+                gram_rows_c<0, 6, 0, 6, Q4Compact::BSS, 6, 0, true>(acc, gpb + Q4Compact::BS, 0, 5, a, a);
             }
-            if (a == b) gram_rows_c<3, 6, 3, 6, 3, 0, 3>(acc, rows + Q4Compact::DR + 3 * a, 0, 1, a, b);
+            gram_rows_c<3, 6, 3, 6, 3, 0, 3, true>(acc, rows + Q4Compact::DR + 3 * a, 0, 1, a, a);
         } else {
-            gram_rows<0, 6, 0, 6>(acc, rows, ND, 0, 36, a, b);
+            gram_rows<0, 6, 0, 6, true>(acc, rows, ND, 0, 36, a, a);
         }
-        acc.store(out + ub(a, b, 4) * 36);
+        acc.template store<true>(out + ub(a, a, 4) * 36);
+    }
+#pragma unroll 1
+    for (int t = 0; t < 3; t++) {
+        const int u = qp + 4 * t, ob = u < 6 ? u : u - 6, i0 = u < 6 ? 0 : 3;
+        // off-diagonal block ob: (0,1) (0,2) (0,3) (1,2) (1,3) (2,3)
+        const int a = ob < 3 ? 0 : (ob < 5 ? 1 : 2);
+        const int b = ob < 3 ? ob + 1 : (ob < 5 ? ob - 1 : 3);
+        BlockAcc<R, PAIR, 3> acc;
+        acc.zero();
+        if constexpr (!COMP) {
+#pragma unroll 1
+            for (int j = 0; j < 4; j++) {
+                const R *gpb = rows + j * Q4Compact::GP;
+                if (i0 == 0) gram_rows_c<0, 3, 0, 3, Q4Compact::MS, 3, 0>(acc, gpb, 0, 3, a, b);
+                gram_rows_h<0, 6, Q4Compact::BSS, 6>(acc, gpb + Q4Compact::BS, 0, 5, a, b, i0);
+            }
+        } else {
+            gram_rows_h<0, 6, ND, 6>(acc, rows, 0, 36, a, b, i0);
+        }
+        acc.store(out + ub(a, b, 4) * 36 + 6 * i0);
     }
 }
 

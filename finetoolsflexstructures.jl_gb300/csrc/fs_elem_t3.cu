@@ -9,15 +9,19 @@ namespace fs {
 // changes the arithmetic of an element (compiled variants could contract
 // products and sums into FMAs differently).
 // Resident blocks of 128 threads asked of the compiler (the register budget
-// per thread): 4 (128 registers) for float rows of homogeneous elements, whose
-// occupancy is otherwise held by registers; 3 (170) for the other float rows;
-// 2 (255) for double rows.
-template <class R, bool COMP, bool AVGK> struct T3MinBlocks {
-    static constexpr int value = sizeof(R) == 8 ? 2 : ((!COMP && !AVGK) ? 4 : 3);
+// per thread).  Float rows stored as floats: 4 (128 registers) for
+// homogeneous elements, whose occupancy is otherwise held by registers, 3
+// (170) for the others.  Float rows stored as float pairs, whose three-part
+// accumulators take 108 registers: 3 for homogeneous elements, 2 (255) for
+// the others; shared memory limits the 128-element tiles to the same counts.
+// Double rows: 2.
+template <class R, bool COMP, bool AVGK, class S> struct T3MinBlocks {
+    static constexpr bool dense = COMP || AVGK;
+    static constexpr int value = sizeof(R) == 8 ? 2 : (sizeof(S) == 8 ? (dense ? 2 : 3) : (dense ? 3 : 4));
 };
 
 template <class R, bool COMP, bool AVGK, class S>
-__global__ void __launch_bounds__(128, (T3MinBlocks<R, COMP, AVGK>::value))
+__global__ void __launch_bounds__(128, (T3MinBlocks<R, COMP, AVGK, S>::value))
     k_t3_elements(const MeshDev m, const MatConst mc, S *ke, int *status)
 {
     constexpr int NR = T3Rows<AVGK>::N, NS = T3Rows<AVGK>::NS;

@@ -1,4 +1,6 @@
 // CSR value gather (see the description below).
+#include <type_traits>
+
 #include "fs_elem_common.cuh"
 
 namespace fs {
@@ -15,7 +17,9 @@ namespace fs {
 // of floats (TwoSum), then rounded once to double: on GB300, where a double
 // add costs as much as 64 float operations, this keeps one double add per
 // stored value instead of a conversion and an add per contribution, with an
-// error below 2^-46 of the largest contribution.  Rows longer than
+// error below 2^-46 of the largest contribution.  Float-pair element matrices
+// (FS_MIXED_COMP) are summed into a float triple, error below about 2^-70 of
+// the largest contribution, and rounded to double with two adds.  Rows longer than
 // 32 * G_COLS positions fall back to accumulating in place in double.
 static const int G_MAXP = 8;
 
@@ -63,31 +67,103 @@ __device__ __forceinline__ double f2d_fast(float f)
     return __hiloint2double((int)h, (int)(u << 29));
 }
 
-// Accumulation of one stored contribution into a value's accumulator:
-// double entries by double addition; float entries (and both halves of a
-// float pair) error-free into an unevaluated float pair (TwoSum).
-template <class S> struct GatherAcc { typedef float T; };
-template <> struct GatherAcc<double> { typedef double T; };
-
-__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float v)
+// The six sums (rows k = 0..5 of the node) of one of a lane's row positions.
+// set() takes the first contribution, add() the next ones (src[st k]: the
+// six entries of a stored block's column or, transposed, its row), value(k)
+// the sum rounded to double.  Double entries: double addition.  Float
+// entries: an unevaluated float pair, the high sum's error added to the low
+// part (TwoSum), the low part's rounding left.  Float-pair entries
+// (FS_MIXED_COMP): an unevaluated float triple, the stored high half added
+// to the high part and the stored low half and the high sum's error to the
+// low part by TwoSum, the low part's errors going to the tail, so that what
+// is lost is the tail's rounding (about 2^-72 of the contributions) instead
+// of the low part's (2^-48); rows k and k + 1 in one packed register pair.
+template <class R> struct ColSum;
+template <> struct ColSum<double> {
+    double v[6];
+    __device__ __forceinline__ void set(const double *src, int st)
+    {
+#pragma unroll
+        for (int k = 0; k < 6; k++) v[k] = src[st * k];
+    }
+    __device__ __forceinline__ void add(const double *src, int st)
+    {
+#pragma unroll
+        for (int k = 0; k < 6; k++) v[k] += src[st * k];
+    }
+    __device__ __forceinline__ double value(int k) const { return v[k]; }
+};
+__device__ __forceinline__ float two_sum_err(float &s, float v)
 {
-    const float t = hi + v;
-    const float bp = t - hi;
-    lo += (hi - (t - bp)) + (v - bp);
-    hi = t;
+    const float t = s + v;
+    const float bp = t - s;
+    const float e = (s - (t - bp)) + (v - bp);
+    s = t;
+    return e;
 }
-__device__ __forceinline__ void gather_add(float &hi, float &lo, float v) { two_sum_acc(hi, lo, v); }
-__device__ __forceinline__ void gather_add(float &hi, float &lo, float2 v)
-{
-    two_sum_acc(hi, lo, v.x);
-    two_sum_acc(hi, lo, v.y);
-}
-__device__ __forceinline__ void gather_add(double &hi, double &, double v) { hi += v; }
-// the first contribution of a value: taken as is (a stored float pair is
-// already normalised, |lo| <= ulp(hi)/2)
-__device__ __forceinline__ void gather_set(float &hi, float &lo, float v) { hi = v; lo = 0.f; }
-__device__ __forceinline__ void gather_set(float &hi, float &lo, float2 v) { hi = v.x; lo = v.y; }
-__device__ __forceinline__ void gather_set(double &hi, double &, double v) { hi = v; }
+template <> struct ColSum<float> {
+    float hi[6], lo[6];
+    __device__ __forceinline__ void set(const float *src, int st)
+    {
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            hi[k] = src[st * k];
+            lo[k] = 0.f;
+        }
+    }
+    __device__ __forceinline__ void add(const float *src, int st)
+    {
+#pragma unroll
+        for (int k = 0; k < 6; k++) lo[k] += two_sum_err(hi[k], src[st * k]);
+    }
+    // hi + lo: exact in double unless their exponents are more than 29
+    // apart, then rounded once
+    __device__ __forceinline__ double value(int k) const
+    {
+        double v = f2d_fast(hi[k]);
+        if (lo[k] != 0.f) v += f2d_fast(lo[k]);
+        return v;
+    }
+};
+template <> struct ColSum<float2> {
+    f32x2 hi[3], lo[3], tl[3];
+    // a stored float pair is normalised (|lo| <= ulp(hi)/2): taken as is
+    __device__ __forceinline__ void set(const float2 *src, int st)
+    {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const float2 u = src[st * 2 * q], w = src[st * (2 * q + 1)];
+            hi[q] = x2_pack(u.x, w.x);
+            lo[q] = x2_pack(u.y, w.y);
+            tl[q] = 0ull;
+        }
+    }
+    __device__ __forceinline__ void add(const float2 *src, int st)
+    {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const float2 u = src[st * 2 * q], w = src[st * (2 * q + 1)];
+            // the stored low half into the low part, the high half into the
+            // high part and its error into the low part; both errors of the
+            // low part to the tail
+            const f32x2 f0 = x2_two_sum(lo[q], x2_pack(u.y, w.y));
+            const f32x2 f1 = x2_two_sum(lo[q], x2_two_sum(hi[q], x2_pack(u.x, w.x)));
+            tl[q] = x2_add(tl[q], x2_add(f0, f1));
+        }
+    }
+    // hi + (lo + tl): each part exact in double, the two adds rounded
+    __device__ __forceinline__ double value(int k) const
+    {
+        float h0, h1, l0, l1, t0, t1;
+        x2_unpack(hi[k >> 1], h0, h1);
+        x2_unpack(lo[k >> 1], l0, l1);
+        x2_unpack(tl[k >> 1], t0, t1);
+        const float h = (k & 1) ? h1 : h0, l = (k & 1) ? l1 : l0, t = (k & 1) ? t1 : t0;
+        double v = f2d_fast(h);
+        if (l != 0.f || t != 0.f) v += f2d_fast(l) + f2d_fast(t);
+        return v;
+    }
+};
 __device__ __forceinline__ double entry_value(float v) { return (double)v; }
 __device__ __forceinline__ double entry_value(double v) { return v; }
 __device__ __forceinline__ double entry_value(float2 v) { return (double)v.x + (double)v.y; }
@@ -100,14 +176,18 @@ template <class R, int NEN> struct GatherSmem {
 
 // resident blocks asked of the compiler: 32 warps per SM where the kernel fits
 // 64 registers without spilling (float entries of three-node elements), 28
-// for other float entries, 24 (at most 80 registers) for double and float
-// pairs; the one-column variant 40 (48 registers) for float entries of
-// three-node elements, 36 (56) for the others; no bound for the four-column
-// variant of long rows
+// for other float entries, 24 (at most 80 registers) for double entries and
+// 20 (102) for float pairs; the one-column variant 40 (48 registers) for
+// float entries of three-node elements, 36 (56) for the other float and the
+// double entries, 28 (72) for float pairs (whose float triples take 18
+// registers; shared memory holds the 4-warp blocks to 28 warps anyway); no
+// bound for the four-column variant of long rows
 template <class R, int NEN, int G_COLS, int WARPS, int G_OUT> struct GatherMinBlocks {
+    static constexpr bool pair = sizeof(R) == 8 && !std::is_same<R, double>::value;
     static constexpr int warps =
         G_COLS > 2 ? 1
-                   : (G_OUT == 1 ? (sizeof(R) == 4 && NEN == 3 ? 40 : 36) : (sizeof(R) == 4 ? (NEN == 3 ? 32 : 28) : 24));
+                   : (G_OUT == 1 ? (pair ? 28 : (sizeof(R) == 4 && NEN == 3 ? 40 : 36))
+                                 : (pair ? 20 : (sizeof(R) == 4 ? (NEN == 3 ? 32 : 28) : 24)));
     static constexpr int value = warps / WARPS > 0 ? warps / WARPS : 1;
 };
 
@@ -118,9 +198,7 @@ template <class R, int NEN, int G_COLS, int WARPS, int G_OUT>
 __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, WARPS, G_OUT>::value))
     k_gather(const MeshDev m, const PatternDev P, int64_t n, const R *ke, double *vals, bool once)
 {
-    typedef typename GatherAcc<R>::T A;
     constexpr int SLAB = NEN * 36, ND2 = 36 * (NEN * (NEN + 1) / 2);
-    constexpr bool SINGLE = sizeof(A) == 4;
     constexpr int BCH = 36 * (int)sizeof(R) / 16;  // 16-byte chunks per 6x6 block
     constexpr int CH = NEN * BCH;                   // 16-byte chunks per slab
     constexpr int CPL = (CH + 31) / 32;             // chunks per lane per pair
@@ -222,7 +300,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
         }
         // the lane's columns and the range of entries of their neighbour slot
         int kcol[G_OUT], cur[G_OUT], beg[G_OUT], last[G_OUT], slc[G_OUT];
-        A hi[G_OUT][6], lo[G_OUT][6];
+        ColSum<R> sum[G_OUT];
 #pragma unroll
         for (int c = 0; c < G_OUT; c++) {
             const int sl = csc[c] / 6;
@@ -239,7 +317,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             cur[c] = jcol[c] >= 0 ? b0 : 0;
             last[c] = jcol[c] >= 0 ? b1 : 0;
             beg[c] = cur[c];
-            // hi, lo: set by the first contribution (every row position has one)
+            // sum[c]: set by the first contribution (every row position has one)
         }
         // lane-fixed staging chunks: chunk lane + 32 t of every slab
         int cb[CPL], cwd[CPL];
@@ -280,15 +358,13 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
                     bool tr = d >> 15;
                     const R *src = stage + (d & 0x7fffu) + (tr ? kc6 : kc);
                     int st = tr ? 1 : 6;
-#pragma unroll
-                    for (int k = 0; k < 6; k++) gather_set(hi[c][k], lo[c][k], src[st * k]);
+                    sum[c].set(src, st);
                     for (e++; e < e1; e++) {
                         d = sent[e];
                         tr = d >> 15;
                         src = stage + (d & 0x7fffu) + (tr ? kc6 : kc);
                         st = tr ? 1 : 6;
-#pragma unroll
-                        for (int k = 0; k < 6; k++) gather_add(hi[c][k], lo[c][k], src[st * k]);
+                        sum[c].add(src, st);
                     }
                 }
             }
@@ -326,8 +402,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
                         const bool tr = (e >> 8) & 1u;
                         const R *src = stage + q * SLAB + b * 36 + (tr ? 6 * kcol[c] : kcol[c]);
                         const int st = tr ? 1 : 6;
-#pragma unroll
-                        for (int k = 0; k < 6; k++) gather_set(hi[c][k], lo[c][k], src[st * k]);
+                        sum[c].set(src, st);
                         cur[c]++;
                     }
                 }
@@ -340,8 +415,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
                     const bool tr = (e >> 8) & 1u;
                     const R *src = stage + q * SLAB + b * 36 + (tr ? 6 * kcol[c] : kcol[c]);
                     const int st = tr ? 1 : 6;
-#pragma unroll
-                    for (int k = 0; k < 6; k++) gather_add(hi[c][k], lo[c][k], src[st * k]);
+                    sum[c].add(src, st);
                     cur[c]++;
                 }
             }
@@ -369,15 +443,7 @@ __global__ void __launch_bounds__(WARPS * 32, (GatherMinBlocks<R, NEN, G_COLS, W
             for (int k = 0; k < 6; k++) {
                 const int64_t rpk = __shfl_sync(0xffffffffu, rp_l, k);
                 if (rpk < 0 || jcol[c] < 0) continue;
-                double v;
-                if (SINGLE) {
-                    // hi + lo: exact in double unless their exponents are more than
-                    // 29 apart, then rounded once
-                    v = f2d_fast((float)hi[c][k]);
-                    if (lo[c][k] != (A)0) v += f2d_fast((float)lo[c][k]);
-                } else {
-                    v = (double)hi[c][k];
-                }
+                const double v = sum[c].value(k);
                 vals[rpk + jcol[c]] = v;
                 if (tw) vals[trow + (int16_t)(tcp[k >> 1] >> (16 * (k & 1)))] = v;
             }

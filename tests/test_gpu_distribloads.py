@@ -338,8 +338,13 @@ def test_nayak_plate_frequencies_on_gpu(case):
 @pytest.mark.parametrize("k", range(4))
 def test_twisted_beam_on_gpu(k, quads):
     # test/test_shell_statics.jl:362-400 and test/test_q4rs_shell_statics.jl:
-    # 358-400 (rtol 1e-3; within 9.9e-6 on the oracle): T3FF and Q4RS
-    # stiffness of the twisted beams from the GPU
+    # 358-400 (rtol 1e-3): T3FF and Q4RS stiffness of the twisted beams from
+    # the GPU, and its tip value against the oracle's (same solver).  The
+    # thin beams (k = 2, 3) are ill-conditioned: a relative perturbation of
+    # 2.2e-16 of the oracle's own K moves their tip value by up to 2.1e-5 of
+    # the reference (1.3e-9 for k = 0, 1), so the bound against the oracle
+    # is 6e-5 there and 1e-8 for the thick beams.
+    tol = 6e-5 if k >= 2 else 1e-8
     for j in range(4):
         d = PB.twisted_beam(k, j, quads)
         geom0 = F.NodalField(d["xyz"])
@@ -349,6 +354,10 @@ def test_twisted_beam_on_gpu(k, quads):
             d["conn"], d["thickness"], F.materials.MatDeforElastIso(d["E"], d["nu"]), stab_fun=d["stab_c"])
         femm.associategeometry(geom0)
         v = PB.twisted_tip_percent(femm.stiffness(geom0, None, None, dchi), d)
+        P = O.Problem(O.Q4RS if quads else O.T3FF, d["xyz"], d["conn"], d["dofnums"], thickness=d["thickness"],
+                      material=d["material"], stab_c=d["stab_c"])
+        P.compute_normals()
+        vo = PB.twisted_tip_percent(P.assemble_scipy("K", O.KEEP_ZEROS).tocsr(), d)
         assert abs(v - d["ref"]) <= 1e-3 * abs(d["ref"])
-        assert abs(v - d["ref"]) <= 2e-5 * abs(d["ref"])
+        assert abs(v - vo) <= tol * abs(d["ref"])
         femm.close()
