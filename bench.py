@@ -138,39 +138,45 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-CPU_SAMPLE_N = 256  # the CPU arms' sample: a 256 x 256 corner of the same plate construction
-
-
-def cpu_baseline(steps=None, budget_s=10.0, n=CPU_SAMPLE_N, nthreads=None):
+def cpu_baseline(steps=1, warmup=0, n=1024, nthreads=None):
     """The oracle (C restatement of the reference's stiffness loop and of
     FinEtools' COO -> sparse(I, J, V) assembly; the element loop over OpenMP
-    threads, the assembly serial as Julia's sparse) on a bounded sample of
-    the workload: an n x n plate of the same construction (jitter, wave,
-    thickness, steel) split in triangles.  nthreads None: every host core."""
+    threads, the assembly serial as Julia's sparse) on the n x n plate of the
+    workload's construction (seed 0, jitter, wave, thickness, steel) split in
+    triangles: n = 1024 is the workload itself.  warmup untimed steps, then
+    `steps` timed ones; nthreads None: every host core."""
     from oracle import oracle as O
     from flexshell import materials
-    xyz, conn, dof = plate(n, False, seed=1)
+    xyz, conn, dof = plate(n, False)
     Dps, Dt = materials.shell_material_stiffness(materials.MatDeforElastIso(E, NU, RHO))
     P = O.Problem(O.T3FF, xyz, conn, dof, thickness=THICK, material=dict(Dps=Dps, Dt=Dt, rho=RHO))
     P.compute_normals()
     cores = nthreads or os.cpu_count() or 1
-    t0 = time.perf_counter()
-    reps = 0
+    for _ in range(warmup):
+        P.assemble("K", O.KEEP_ZEROS, nthreads=cores)
     times = []
-    while True:
+    for _ in range(max(steps, 1)):
         t1 = time.perf_counter()
         P.assemble("K", O.KEEP_ZEROS, nthreads=cores)
         times.append(time.perf_counter() - t1)
-        reps += 1
-        if steps is not None and reps >= steps:
-            break
-        if steps is None and time.perf_counter() - t0 > budget_s:
-            break
     el = conn.shape[0]
-    return {"value": el * reps / sum(times), "unit": "elements/s", "cores": cores, "kind": "port",
-            "sample": "T3FF stiffness, %dx%d corner of the plate construction (%d triangles, 1/%d of the "
-                      "1024x1024 workload), element loop + COO->CSC assembly, %d repetition(s)" % (
-                          n, n, el, (1024 // n) ** 2, reps)}, times
+    what = ("the full %dx%d workload (%d triangles)" % (n, n, el) if n == 1024 else
+            "a %dx%d plate of the workload's construction (%d triangles, 1/%d of the 1024x1024 workload)"
+            % (n, n, el, (1024 // n) ** 2))
+    return {"value": el * len(times) / sum(times), "unit": "elements/s", "cores": cores, "kind": "port",
+            "sample": "T3FF stiffness, %s, element loop + COO->CSC assembly, %d timed step(s) after %d "
+                      "untimed" % (what, len(times), warmup)}, times
+
+
+def cpu_sample_side(nsteps, budget_s=200.0, nthreads=None):
+    """The largest plate side (1024, the workload, then 512, 256, 128) whose
+    nsteps oracle steps fit `budget_s` seconds, from one timed 128 x 128 step
+    scaled by the element count (the assembly is close to linear in it)."""
+    _, t = cpu_baseline(steps=1, n=128, nthreads=nthreads)
+    for n in (1024, 512, 256):
+        if nsteps * t[0] * (n / 128) ** 2 * 1.2 <= budget_s:
+            return n
+    return 128
 
 
 def max_over_ranks(x, world, dist):
@@ -197,15 +203,16 @@ def run_reference(args):
         return 0
     from oracle import oracle as O
     O.build()
-    cpu_baseline(steps=max(args.warmup, 1))  # untimed warm-up steps
-    cb, times = cpu_baseline(steps=args.steps)
+    # the workload itself when its warm-up and timed steps fit a few minutes
+    n = cpu_sample_side(args.warmup + args.steps)
+    cb, times = cpu_baseline(steps=args.steps, warmup=max(args.warmup, 1), n=n)
     ms = 1e3 * float(np.mean(times))
     line = {"metric": METRIC, "value": cb["value"], "unit": "elements/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": workload_text(args.n), "precision": "FP64 (the reference's arithmetic)",
-                       "sample": "bounded CPU sample of the workload: " + cb["sample"]},
+                       "sample": cb["sample"], "same_workload": n == args.n},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "elements/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -536,7 +543,7 @@ def corotbeam_lattice(torch, device=0, n=100, steps=5, warmup=3):
     return out
 
 
-def composite_c4(torch, device=0, n=512, n_eig=256, nev=20, steps=5, warmup=3):
+def composite_c4(torch, device=0, n=512, n_eig=512, nev=20, steps=5, warmup=3):
     """The layered Q4RS plate ([0/90/90/0], 0.25 mm plies, 1 m side, simply
     supported, in-plane rigid-body motion restrained): stiffness assembly in
     the three arithmetic modes at n x n, and the nev lowest eigenvalues of an
@@ -670,9 +677,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-oracle", action="store_true", help="skip the full-size FP64 check against the oracle")
     ap.add_argument("--no-explicit", action="store_true")
-    ap.add_argument("--eig-n", type=int, default=256,
-                    help="quads per side of the layered plate of the 20-eigenvalue check (512: the reference's "
-                         "configuration, a 45 GB factor)")
+    ap.add_argument("--eig-n", type=int, default=512,
+                    help="quads per side of the layered plate of the 20-eigenvalue check (512, the default: the "
+                         "reference's configuration, 1.58 M dofs, a 45 GB band factor per mode, about three "
+                         "minutes for the three modes)")
     ap.add_argument("--explicit-only", action="store_true",
                     help="only the explicit-dynamics section, on an n x n Q4RS plate for 64 x steps steps "
                          "(a small case for profiling the step kernels)")
@@ -732,6 +740,19 @@ def main():
     h_colptr = pin((asm.n + 1,), torch.int64)
     h_rowval = pin((nnz0,), torch.int64)
     h_nzval = pin((nnz0,), torch.float64)
+    # the host's device-to-host copy rate at this moment (a 1 GiB copy into
+    # page-locked memory, best of three): the end-to-end step is bound by its
+    # 4.3 GB copy back, and the host's memory is shared with other jobs
+    d_probe = torch.ones(1 << 27, dtype=torch.float64, device="cuda")
+    h_probe = torch.empty(1 << 27, dtype=torch.float64, pin_memory=True)
+    d2h_gbs = 0.0
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h_probe.copy_(d_probe, non_blocking=True)
+        torch.cuda.synchronize()
+        d2h_gbs = max(d2h_gbs, (1 << 30) / (time.perf_counter() - t0) / 1e9)
+    del d_probe, h_probe
     if world > 1:
         dist.barrier()
     # clocks sampled over every timed region of the T3FF section (the headline
@@ -846,8 +867,8 @@ def main():
     tr_ga, _ = measured_traffic("k_gather " + mode, ne3)
     cb = cb1 = None
     if not args.no_cpu:
-        cb, _ = cpu_baseline(steps=3)
-        cb1, _ = cpu_baseline(steps=1, nthreads=1)
+        cb, _ = cpu_baseline(steps=1, n=args.n)
+        cb1, _ = cpu_baseline(steps=1, n=args.n, nthreads=1)
         cb["single_thread_value"] = cb1["value"]
         cb["single_thread_sample"] = cb1["sample"]
     line = {
@@ -862,6 +883,7 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": world * ne3 / (ms_e2e * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
+                "host_d2h_gbs": d2h_gbs, "ms_copy_back_at_host_rate": d2h / (d2h_gbs * 1e9) * 1e3,
                 "path": "C ABI from pinned host: fs_geometry_set + fs_dofs_set + fs_pattern (pattern "
                         "rebuilt) + fs_stiffness_copy (FS_MIXED_COMP; CSC copied back, pattern copy "
                         "overlapping the kernels)"},

@@ -229,10 +229,25 @@ template <int NI> struct BlockAcc<float, true, NI> {
 // acc += sum over rows [r0, r1) of row[6a + i] row[6b + j] for i in
 // [I0, I1), j in [J0, J1): the sub-blocks a row can reach (DIAG: a = b, the
 // upper triangle)
-template <int I0, int I1, int J0, int J1, bool DIAG = false, class R, class Acc>
+// The row loop of the gram helpers: unrolled, or (ROLLED) kept a loop.  The
+// T3 kernel's float-pair sums run rolled: a row's body is 16 packed
+// instructions per entry pair, and the unrolled loops stalled it on
+// instruction fetch (21 % slower); the Q4 kernel's run faster unrolled.
+template <bool ROLLED, class F>
+__device__ __forceinline__ void for_rows(int r0, int r1, F body)
+{
+    if constexpr (ROLLED) {
+#pragma unroll 1
+        for (int rho = r0; rho < r1; rho++) body(rho);
+    } else {
+        for (int rho = r0; rho < r1; rho++) body(rho);
+    }
+}
+
+template <int I0, int I1, int J0, int J1, bool DIAG = false, bool ROLLED = false, class R, class Acc>
 __device__ __forceinline__ void gram_rows(Acc &acc, const R *rows, int ND, int r0, int r1, int a, int b)
 {
-    for (int rho = r0; rho < r1; rho++) {
+    for_rows<ROLLED>(r0, r1, [&](int rho) {
         const R *rr = rows + rho * ND;
         R ra[6], rb[6];
 #pragma unroll
@@ -240,16 +255,17 @@ __device__ __forceinline__ void gram_rows(Acc &acc, const R *rows, int ND, int r
 #pragma unroll
         for (int j = J0; j < J1; j++) rb[j] = rr[6 * b + j];
         acc.template row<I0, I1, J0, J1, DIAG>(ra, rb);
-    }
+    });
 }
 
 // acc += sum over rows [r0, r1) (stride RS from base) of row[NSTR a + i - IOFF]
 // row[NSTR b + j - IOFF] for i in [I0, I1), j in [J0, J1): the same products
 // as gram_rows on a compact row layout (rows holding a subset of the dofs)
-template <int I0, int I1, int J0, int J1, int RS, int NSTR, int IOFF, bool DIAG = false, class R, class Acc>
+template <int I0, int I1, int J0, int J1, int RS, int NSTR, int IOFF, bool DIAG = false, bool ROLLED = false,
+          class R, class Acc>
 __device__ __forceinline__ void gram_rows_c(Acc &acc, const R *base, int r0, int r1, int a, int b)
 {
-    for (int rho = r0; rho < r1; rho++) {
+    for_rows<ROLLED>(r0, r1, [&](int rho) {
         const R *rr = base + rho * RS;
         R ra[6], rb[6];
 #pragma unroll
@@ -257,7 +273,7 @@ __device__ __forceinline__ void gram_rows_c(Acc &acc, const R *base, int r0, int
 #pragma unroll
         for (int j = J0; j < J1; j++) rb[j] = rr[NSTR * b + j - IOFF];
         acc.template row<I0, I1, J0, J1, DIAG>(ra, rb);
-    }
+    });
 }
 
 // Half-block forms (a three-row accumulator): rows i0 .. i0 + 2 of block
@@ -267,7 +283,7 @@ __device__ __forceinline__ void gram_rows_c(Acc &acc, const R *base, int r0, int
 template <int J0, int J1, int RS, int NSTR, class R, class Acc>
 __device__ __forceinline__ void gram_rows_h(Acc &acc, const R *base, int r0, int r1, int a, int b, int i0)
 {
-    for (int rho = r0; rho < r1; rho++) {
+    for_rows<false>(r0, r1, [&](int rho) {
         const R *rr = base + rho * RS;
         R ra[6], rb[6];
 #pragma unroll
@@ -275,7 +291,7 @@ __device__ __forceinline__ void gram_rows_h(Acc &acc, const R *base, int r0, int
 #pragma unroll
         for (int j = J0; j < J1; j++) rb[j] = rr[NSTR * b + j];
         acc.template row<0, 3, J0, J1>(ra, rb);
-    }
+    });
 }
 
 // The upper node blocks of an NN-node element: diag(a) computes block
@@ -319,16 +335,16 @@ __device__ __forceinline__ void write_blocks_compact(const R *rows, S *out)
         [&](int a) {
             BlockAcc<R, PAIR> acc;
             acc.zero();
-            gram_rows_c<0, 3, 0, 3, L::MS, 3, 0, true>(acc, rows, 0, 3, a, a);
-            gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0, true>(acc, rows + L::BS, 0, 3 + NS, a, a);
-            gram_rows_c<3, 6, 3, 6, 3, 0, 3, true>(acc, rows + L::DR + 3 * a, 0, 1, a, a);
+            gram_rows_c<0, 3, 0, 3, L::MS, 3, 0, true, PAIR>(acc, rows, 0, 3, a, a);
+            gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0, true, PAIR>(acc, rows + L::BS, 0, 3 + NS, a, a);
+            gram_rows_c<3, 6, 3, 6, 3, 0, 3, true, PAIR>(acc, rows + L::DR + 3 * a, 0, 1, a, a);
             acc.template store<true>(out + ub(a, a, NN) * 36);
         },
         [&](int a, int b) {
             BlockAcc<R, PAIR> acc;
             acc.zero();
-            gram_rows_c<0, 3, 0, 3, L::MS, 3, 0>(acc, rows, 0, 3, a, b);
-            gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0>(acc, rows + L::BS, 0, 3 + NS, a, b);
+            gram_rows_c<0, 3, 0, 3, L::MS, 3, 0, false, PAIR>(acc, rows, 0, 3, a, b);
+            gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0, false, PAIR>(acc, rows + L::BS, 0, 3 + NS, a, b);
             acc.store(out + ub(a, b, NN) * 36);
         });
 }
@@ -349,11 +365,11 @@ __device__ __forceinline__ void write_blocks(const R *rows, int nrows, S *out)
             BlockAcc<R, PAIR> acc;
             acc.zero();
             if (SPARSE) {
-                gram_rows<0, 3, 0, 3, true>(acc, rows, ND, 0, 3, a, a);
-                gram_rows<0, 6, 0, 6, true>(acc, rows, ND, 3, nrows - NN, a, a);
-                gram_rows<3, 6, 3, 6, true>(acc, rows, ND, nrows - NN + a, nrows - NN + a + 1, a, a);
+                gram_rows<0, 3, 0, 3, true, PAIR>(acc, rows, ND, 0, 3, a, a);
+                gram_rows<0, 6, 0, 6, true, PAIR>(acc, rows, ND, 3, nrows - NN, a, a);
+                gram_rows<3, 6, 3, 6, true, PAIR>(acc, rows, ND, nrows - NN + a, nrows - NN + a + 1, a, a);
             } else {
-                gram_rows<0, 6, 0, 6, true>(acc, rows, ND, 0, nrows, a, a);
+                gram_rows<0, 6, 0, 6, true, PAIR>(acc, rows, ND, 0, nrows, a, a);
             }
             acc.template store<true>(out + ub(a, a, NN) * 36);
         },
@@ -361,10 +377,10 @@ __device__ __forceinline__ void write_blocks(const R *rows, int nrows, S *out)
             BlockAcc<R, PAIR> acc;
             acc.zero();
             if (SPARSE) {
-                gram_rows<0, 3, 0, 3>(acc, rows, ND, 0, 3, a, b);
-                gram_rows<0, 6, 0, 6>(acc, rows, ND, 3, nrows - NN, a, b);
+                gram_rows<0, 3, 0, 3, false, PAIR>(acc, rows, ND, 0, 3, a, b);
+                gram_rows<0, 6, 0, 6, false, PAIR>(acc, rows, ND, 3, nrows - NN, a, b);
             } else {
-                gram_rows<0, 6, 0, 6>(acc, rows, ND, 0, nrows, a, b);
+                gram_rows<0, 6, 0, 6, false, PAIR>(acc, rows, ND, 0, nrows, a, b);
             }
             acc.store(out + ub(a, b, NN) * 36);
         });
