@@ -65,9 +65,9 @@ MEASURED_TRAFFIC_PER_ELEMENT = {
                                       "(profiles/k_t3_elements_k_gather_t3ff_mixed_512.md)"),
     "k_gather FS_MIXED": (1984.5, "ncu --set full, k_gather, FS_MIXED, T3FF 512^2 "
                                   "(profiles/k_t3_elements_k_gather_t3ff_mixed_512.md)"),
-    "k_t3_elements FS_MIXED_COMP": (1667.8, "ncu --set full, k_t3_elements, FS_MIXED_COMP, T3FF 512^2 "
+    "k_t3_elements FS_MIXED_COMP": (1663.5, "ncu --set full, k_t3_elements, FS_MIXED_COMP, T3FF 512^2 "
                                             "(profiles/k_t3_elements_k_gather_t3ff_mixed_comp_512.md)"),
-    "k_gather FS_MIXED_COMP": (2873.8, "ncu --set full, k_gather, FS_MIXED_COMP, T3FF 512^2 "
+    "k_gather FS_MIXED_COMP": (2874.2, "ncu --set full, k_gather, FS_MIXED_COMP, T3FF 512^2 "
                                        "(profiles/k_t3_elements_k_gather_t3ff_mixed_comp_512.md)"),
 }
 
