@@ -390,7 +390,8 @@ class _FEMMShell:
 
     # -- extras ----------------------------------------------------------------
     def element_matrices(self, geom0, precision=FS_FP64):
-        """All element stiffness matrices in the global basis (nelem x nd x nd)."""
+        """All element stiffness matrices in the global basis (nelem x nd x nd);
+        FS_MIXED_COMP's float pairs as the doubles nearest hi + lo."""
         self._sync_inputs(geom0, None)
         nd = 6 * self.nen
         out = np.zeros((self.conn.shape[0], nd, nd))

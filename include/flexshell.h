@@ -211,7 +211,9 @@ int fs_tuning_ex(const fs_ctx *ctx, int32_t *out, int n);
 int fs_stiffness_values_noalloc(fs_ctx *ctx, int precision, int64_t nrows, double *vals,
                                 int64_t vals_len);
 /* Element matrices in the global basis (nelem x (6 nen)^2, each column-major), in
- * mesh order; for parity checks. */
+ * mesh order; for parity checks.  FS_MIXED_COMP entries are float pairs
+ * returned as the double nearest hi + lo (a pair can hold more bits than a
+ * double when its low half is far below its high half's last place). */
 int fs_element_matrices(fs_ctx *ctx, int precision, double *out);
 /* Lumped element masses (tmass, rmass) per element, in mesh order. */
 int fs_element_masses(fs_ctx *ctx, double *out);

@@ -4,10 +4,15 @@ Julia's sparse(I, J, V) combines duplicates) — a left-to-right double sum in
 FP64, and in FS_MIXED the error-free float-pair (TwoSum) accumulation of the
 float contributions rounded once to double.  The expected values are
 recomputed on the host from the library's own element matrices, so the
-comparison is bitwise; the meshes exercise the single-batch path (Scordelis-Lo
+comparison is bitwise; in FS_MIXED_COMP the stored float pairs are summed
+error-free and rounded once, checked against the exact sum of the element
+matrices as reported (each pair rounded to a double, which a pair whose low
+half is far below its high half's last place does not fit exactly).  The
+meshes exercise the single-batch path (Scordelis-Lo
 roof, triangles and quadrilaterals) and the multi-batch path (a fan whose
 centre node has more element pairs than one staging batch)."""
 import ctypes
+from fractions import Fraction
 
 import numpy as np
 import pytest
@@ -59,7 +64,38 @@ def _expected(Ke, conn, dof, n, precision):
     return r[start], c[start], hi.astype(np.float64) + lo.astype(np.float64)
 
 
+def _check_exact_sums(femm, geom0, dchi, conn, n):
+    """FS_MIXED_COMP: every stored value within one unit in the last place of
+    the exact sum of its element contributions as reported, plus the
+    reported contributions' own rounding to double (half a unit in the last
+    place of each; a float pair spans up to 24 + 24 bits and the gap between
+    its halves) and what the float triple of the sum can lose (about 2^-72
+    of the contributions' magnitudes)."""
+    asm = F.SysmatAssemblerSparse() if n == dchi.nalldofs() else F.SysmatAssemblerFFBlock(n)
+    K = femm.stiffness(asm, geom0, None, None, dchi, precision=F.FS_MIXED_COMP).tocoo()
+    Ke = femm.element_matrices(geom0, F.FS_MIXED_COMP)
+    r, c, v = _contributions(Ke, conn, dchi.dofnums, n)
+    order = np.lexsort((np.arange(r.size), c, r))
+    r, c, v = r[order], c[order], v[order]
+    start = np.r_[0, np.nonzero((np.diff(r) != 0) | (np.diff(c) != 0))[0] + 1]
+    stop = np.r_[start[1:], r.size]
+    got = dict(zip(zip(K.row.tolist(), K.col.tolist()), K.data.tolist()))
+    assert len(got) == start.size
+    worst, info = 0.0, None
+    for a, b in zip(start.tolist(), stop.tolist()):
+        exact = sum((Fraction(x) for x in v[a:b].tolist()), Fraction(0))
+        g = got[(int(r[a]), int(c[a]))]
+        bound = Fraction(float(np.abs(v[a:b]).sum())) / 2 ** 52
+        if exact != 0:
+            bound += Fraction(float(np.spacing(abs(float(exact)))))
+        q = float(abs(Fraction(g) - exact) / bound) if bound > 0 else float(g != 0.0)
+        if q > worst:
+            worst, info = q, (int(r[a]), int(c[a]), g, float(exact), v[a:b].tolist())
+    assert worst <= 1.0, (n, worst, info)
+
+
 def _check(femm, geom0, dchi, conn, n):
+    _check_exact_sums(femm, geom0, dchi, conn, n)
     for precision in (F.FS_FP64, F.FS_MIXED):
         asm = F.SysmatAssemblerSparse() if n == dchi.nalldofs() else F.SysmatAssemblerFFBlock(n)
         K = femm.stiffness(asm, geom0, None, None, dchi, precision=precision).tocoo()
