@@ -69,6 +69,27 @@ FS_HD void make_frame(const double a[3], const double b[3], double e[3][3])
     cross3(e[2], e[0], e[1]);
 }
 
+// 1/sqrt(x) rounded to nearest in float (device and host)
+FS_HD float rsqrt_f(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return __frsqrt_rn(x);
+#else
+    return (float)(1.0 / sqrt((double)x));
+#endif
+}
+
+// make_frame in float
+FS_HD void make_frame_f(const float a[3], const float b[3], float e[3][3])
+{
+    float s = rsqrt_f(dot3(a, a));
+    for (int c = 0; c < 3; c++) e[0][c] = a[c] * s;
+    cross3(e[0], b, e[2]);
+    s = rsqrt_f(dot3(e[2], e[2]));
+    for (int c = 0; c < 3; c++) e[2][c] *= s;
+    cross3(e[2], e[0], e[1]);
+}
+
 // Nodal triad (reference _NodalTriadsE, src/FEMMShellT3FFModule.jl:355-388):
 // the rotation by the vector a = e3_e x n_e (angle |a|, FinEtools rotmat3!),
 // in Rodrigues form R = I + s(x) [a]x + c(x) [a]x^2 with x = |a|^2,
@@ -822,45 +843,21 @@ struct Q4Compact {
 // Returns nonzero on a singular metric (src/FEMMShellQ4RSModule.jl:308-311).
 // COMPACT (homogeneous elements): `rows` is the point's Q4Compact block and
 // `rs` is not used.
-template <class R, bool COMP, bool COMPACT = false>
+template <class R, bool COMP, bool COMPACT = false, bool FFRAME = false>
 FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatConst &mc,
                         const GroupConst *gc, R *rows, int rs, double trace[4])
 {
     static_assert(!(COMP && COMPACT), "the compact layout is for homogeneous elements");
+    static_assert(!FFRAME || sizeof(R) == 4, "the float frame is for float rows");
     double xi, eta, gp[4][2];
     q4_point(j, xi, eta);
     q4_dbasis_gp(j, gp);
-    double J0[3], J1[3];
-    for (int c = 0; c < 3; c++) {
-        J0[c] = qe.Xr[0][c] * gp[0][0] + qe.Xr[1][c] * gp[1][0] + qe.Xr[2][c] * gp[2][0] + qe.Xr[3][c] * gp[3][0];
-        J1[c] = qe.Xr[0][c] * gp[0][1] + qe.Xr[1][c] * gp[1][1] + qe.Xr[2][c] * gp[2][1] + qe.Xr[3][c] * gp[3][1];
-    }
-    double e[3][3];
-    make_frame(J0, J1, e);
-    // element coordinates (centroid relative) and basis gradients
-    R X[4], Y[4];
-    {
-        R e0r[3] = {(R)e[0][0], (R)e[0][1], (R)e[0][2]}, e1r[3] = {(R)e[1][0], (R)e[1][1], (R)e[1][2]};
-        for (int a = 0; a < 4; a++) {
-            R xr[3];
-            for (int c = 0; c < 3; c++) xr[c] = sizeof(R) == 4 ? (R)qe.Xf[a][c] : (R)qe.Xr[a][c];
-            X[a] = dot3(xr, e0r);
-            Y[a] = dot3(xr, e1r);
-        }
-    }
-    // basis gradients and tangents in the working precision (float: the
-    // gradients evaluated in float, the double tangents rounded once --
-    // tangents summed in float from rounded coordinates lose about one more
-    // digit; double: the values above)
-    R gq[4][2], J0r[3], J1r[3], xir, etar;
+    // basis gradients in the working precision (float rows: evaluated in float)
+    R gq[4][2], xir, etar;
     if constexpr (sizeof(R) == 4) {
         xir = j < 2 ? -(float)Q4_GP : (float)Q4_GP;
         etar = (j & 1) ? (float)Q4_GP : -(float)Q4_GP;
         q4_dbasis_t<R>(xir, etar, gq);
-        for (int c = 0; c < 3; c++) {
-            J0r[c] = (float)J0[c];
-            J1r[c] = (float)J1[c];
-        }
     } else {
         xir = xi;
         etar = eta;
@@ -868,10 +865,44 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
             gq[a][0] = gp[a][0];
             gq[a][1] = gp[a][1];
         }
+    }
+    // tangents and frame: in double from the centroid-relative coordinates,
+    // rounded once to the working precision (tangents summed in float from
+    // rounded coordinates lose about one more digit); or (FFRAME, FS_MIXED's
+    // cheaper choice) in float from the float coordinates and gradients, off
+    // the FP64 pipe
+    R J0r[3], J1r[3], eR[3][3];
+    double e[3][3];  // the double frame (FFRAME: the float one widened, for the layup angle)
+    if constexpr (FFRAME) {
         for (int c = 0; c < 3; c++) {
-            J0r[c] = J0[c];
-            J1r[c] = J1[c];
+            J0r[c] = qe.Xf[0][c] * gq[0][0] + qe.Xf[1][c] * gq[1][0] + qe.Xf[2][c] * gq[2][0] + qe.Xf[3][c] * gq[3][0];
+            J1r[c] = qe.Xf[0][c] * gq[0][1] + qe.Xf[1][c] * gq[1][1] + qe.Xf[2][c] * gq[2][1] + qe.Xf[3][c] * gq[3][1];
         }
+        make_frame_f(J0r, J1r, eR);
+        if constexpr (COMP)
+            for (int k = 0; k < 3; k++)
+                for (int c = 0; c < 3; c++) e[k][c] = eR[k][c];
+    } else {
+        double J0[3], J1[3];
+        for (int c = 0; c < 3; c++) {
+            J0[c] = qe.Xr[0][c] * gp[0][0] + qe.Xr[1][c] * gp[1][0] + qe.Xr[2][c] * gp[2][0] + qe.Xr[3][c] * gp[3][0];
+            J1[c] = qe.Xr[0][c] * gp[0][1] + qe.Xr[1][c] * gp[1][1] + qe.Xr[2][c] * gp[2][1] + qe.Xr[3][c] * gp[3][1];
+        }
+        make_frame(J0, J1, e);
+        for (int c = 0; c < 3; c++) {
+            J0r[c] = (R)J0[c];
+            J1r[c] = (R)J1[c];
+        }
+        for (int k = 0; k < 3; k++)
+            for (int c = 0; c < 3; c++) eR[k][c] = (R)e[k][c];
+    }
+    // element coordinates (centroid relative)
+    R X[4], Y[4];
+    for (int a = 0; a < 4; a++) {
+        R xr[3];
+        for (int c = 0; c < 3; c++) xr[c] = sizeof(R) == 4 ? (R)qe.Xf[a][c] : (R)qe.Xr[a][c];
+        X[a] = dot3(xr, eR[0]);
+        Y[a] = dot3(xr, eR[1]);
     }
     // surface Jacobian |J0 x J1| in the working precision
     R Jac;
@@ -884,10 +915,9 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     R detG = G11 * G22 - G12 * G12;
     if (detG == (R)0) return 4;
     R i11 = G22 / detG, i12 = -G12 / detG, i22 = G11 / detG;
-    R e0[3] = {(R)e[0][0], (R)e[0][1], (R)e[0][2]}, e1[3] = {(R)e[1][0], (R)e[1][1], (R)e[1][2]};
     R g[4][2];
     // g_a = J invG gradNparams_a, projected on e1, e2
-    R pj0[2] = {dot3(e0, J0r), dot3(e1, J0r)}, pj1[2] = {dot3(e0, J1r), dot3(e1, J1r)};
+    R pj0[2] = {dot3(eR[0], J0r), dot3(eR[1], J0r)}, pj1[2] = {dot3(eR[0], J1r), dot3(eR[1], J1r)};
     for (int a = 0; a < 4; a++) {
         R t1 = i11 * gq[a][0] + i12 * gq[a][1];
         R t2 = i12 * gq[a][0] + i22 * gq[a][1];
@@ -897,11 +927,8 @@ FS_HD int q4_point_rows(const ElemIn<4> &in, const Q4Elem &qe, int j, const MatC
     R A[4][3][3];
     GlobalMap<R, 4> M;
     if constexpr (sizeof(R) == 4) {
-        float ef[3][3];
-        for (int k = 0; k < 3; k++)
-            for (int c = 0; c < 3; c++) ef[k][c] = (float)e[k][c];
-        for (int i = 0; i < 4; i++) nodal_triad_f(ef, in.nrmf[i], in.valid[i], A[i]);
-        build_map<R, 4>(ef, A, g, M);
+        for (int i = 0; i < 4; i++) nodal_triad_f(eR, in.nrmf[i], in.valid[i], A[i]);
+        build_map<R, 4>(eR, A, g, M);
     } else {
         for (int i = 0; i < 4; i++) nodal_triad_r<R>(e, in.nrm[i], in.valid[i], A[i]);
         build_map<R, 4>(e, A, g, M);
@@ -996,6 +1023,31 @@ FS_HD void q4_drill_rows(const ElemIn<4> &in, const double trace[4], double scal
         for (int q = 0; q < 24; q++) o[q] = 0;
         if (use[k] && kavg != 0.0)
             for (int c = 0; c < 3; c++) o[6 * k + 3 + c] = (R)(sk * in.nrm[k][c]);
+    }
+}
+
+// q4_drill_rows in float (FS_MIXED's float frames): float traces and normals
+FS_HD void q4_drill_rows_f(const ElemIn<4> &in, const float trace[4], float scale, float *rows, int rs)
+{
+    float sum = 0.f;
+    int cnt = 0;
+    bool use[4];
+    for (int k = 0; k < 4; k++) {
+        const float *nv = in.nrmf[k];
+        use[k] = in.valid[k] && (dot3(nv, nv) != 0.f);
+        if (use[k]) {
+            const float v = trace[k] * 0.5f;
+            sum += v > 0.f ? v : 0.f;
+            cnt++;
+        }
+    }
+    const float kavg = (cnt ? sum / (float)cnt : 0.f) * scale;
+    const float sk = kavg > 0.f ? sqrtf(kavg) : 0.f;
+    for (int k = 0; k < 4; k++) {
+        float *o = rows + k * rs;
+        for (int q = 0; q < 24; q++) o[q] = 0;
+        if (use[k] && kavg != 0.f)
+            for (int c = 0; c < 3; c++) o[6 * k + 3 + c] = sk * in.nrmf[k][c];
     }
 }
 

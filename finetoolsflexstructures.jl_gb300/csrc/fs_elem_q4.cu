@@ -99,16 +99,55 @@ __global__ void __launch_bounds__(128, 2) k_q4_elements(const MeshDev m, const M
     double tr[4] = {0, 0, 0, 0};
     if (active) {
         const GroupConst *gc = COMP ? &m.groups[sg.in.group] : nullptr;
+        // FS_MIXED (float rows stored as floats): the points' tangents and
+        // frames in float; the compensated mode keeps them double
+        constexpr bool FFRAME = sizeof(R) == 4 && sizeof(S) == 4;
         int st;
         if constexpr (COMP)
-            st = q4_point_rows<R, true>(sg.in, sg.qe, qp, mc, gc, rows + qp * 8 * ND, ND, tr);
+            st = q4_point_rows<R, true, false, FFRAME>(sg.in, sg.qe, qp, mc, gc, rows + qp * 8 * ND, ND, tr);
         else
-            st = q4_point_rows<R, false, true>(sg.in, sg.qe, qp, mc, gc, rows + qp * Q4Compact::GP, 0, tr);
+            st = q4_point_rows<R, false, true, FFRAME>(sg.in, sg.qe, qp, mc, gc, rows + qp * Q4Compact::GP, 0, tr);
         if (st) {
             atomicOr(status, DEV_SINGULAR);
             for (int k = 0; k < 4; k++) tr[k] = 0.0;
         }
     }
+    constexpr bool FFRAME = sizeof(R) == 4 && sizeof(S) == 4;
+    if constexpr (FFRAME) {
+        // FS_MIXED: the drilling factor in float (q4_drill_rows_f), the
+        // traces summed over the four points by shuffles
+        float trf[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            trf[k] = (float)tr[k];
+            trf[k] += __shfl_xor_sync(0xffffffffu, trf[k], 1);
+            trf[k] += __shfl_xor_sync(0xffffffffu, trf[k], 2);
+        }
+        bool use = false;
+        if (active) {
+            const float *nv = sg.in.nrmf[qp];
+            use = sg.in.valid[qp] && (dot3(nv, nv) != 0.f);
+        }
+        const unsigned um = __ballot_sync(0xffffffffu, use) >> src;
+        if (active) {
+            float sum = 0.f;
+            int cnt = 0;
+            for (int k = 0; k < 4; k++)
+                if ((um >> k) & 1u) {
+                    const float v = trf[k] * 0.5f;
+                    sum += v > 0.f ? v : 0.f;
+                    cnt++;
+                }
+            const float kavg = (cnt ? sum / (float)cnt : 0.f) * (float)mc.drill_scale;
+            const float sk = kavg > 0.f ? sqrtf(kavg) : 0.f;
+            R *o = rows + Q4Compact::DR + 3 * qp;
+            if constexpr (COMP) o = rows + (32 + qp) * ND;
+            if constexpr (COMP)
+                for (int q = 0; q < 24; q++) o[q] = 0;
+            R *oc = COMP ? o + 6 * qp + 3 : o;
+            for (int c = 0; c < 3; c++) oc[c] = (use && kavg != 0.f) ? (R)(sk * sg.in.nrmf[qp][c]) : (R)0;
+        }
+    } else {
     // sum the drilling traces of the four quadrature points (lanes 4el..4el+3)
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -142,6 +181,7 @@ __global__ void __launch_bounds__(128, 2) k_q4_elements(const MeshDev m, const M
             R *o = rows + Q4Compact::DR + 3 * qp;
             for (int c = 0; c < 3; c++) o[c] = (use && kavg != 0.0) ? (R)(sk * sg.in.nrm[qp][c]) : (R)0;
         }
+    }
     }
     __syncwarp();
     if (!active) return;

@@ -12,7 +12,7 @@
 
 using namespace fs;
 
-template <class R>
+template <class R, bool FFRAME = false>
 static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t nelem,
                          const int64_t *conn, const double *normals, const uint8_t *valid,
                          const double *thick, const fs_shell_params *p, const fs_layup_group *groups,
@@ -71,13 +71,20 @@ static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t n
             Q4Elem qe;
             q4_prepare(in, comp ? gc->thickness : in.t, mc.stab_c, qe);
             double tr[4] = {0, 0, 0, 0};
+            float trf[4] = {0, 0, 0, 0};
             for (int j = 0; j < 4; j++) {
                 double trj[4];
-                st |= comp ? q4_point_rows<R, true>(in, qe, j, mc, gc, &rows[8 * j][0], 24, trj)
-                           : q4_point_rows<R, false>(in, qe, j, mc, gc, &rows[8 * j][0], 24, trj);
-                for (int k = 0; k < 4; k++) tr[k] += trj[k];
+                st |= comp ? q4_point_rows<R, true, false, FFRAME>(in, qe, j, mc, gc, &rows[8 * j][0], 24, trj)
+                           : q4_point_rows<R, false, false, FFRAME>(in, qe, j, mc, gc, &rows[8 * j][0], 24, trj);
+                for (int k = 0; k < 4; k++) {
+                    tr[k] += trj[k];
+                    trf[k] += (float)trj[k];
+                }
             }
-            q4_drill_rows<R>(in, tr, mc.drill_scale, &rows[32][0], 24);
+            if constexpr (FFRAME)
+                q4_drill_rows_f(in, trf, (float)mc.drill_scale, &rows[32][0], 24);
+            else
+                q4_drill_rows<R>(in, tr, mc.drill_scale, &rows[32][0], 24);
             nrows = 36;
         }
         if (st) return 10 + st;
@@ -108,6 +115,11 @@ extern "C" int hc_element_matrices(int etype, int precision, int64_t nnodes, con
     if (precision == FS_FP64)
         return elem_matrices<double>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
                                      egroup, out);
+    // FS_MIXED: the Q4 points' frames in float, as the library's FS_MIXED
+    // kernel; FS_MIXED_COMP (2): double frames, the Gram summed exactly
+    if (precision == FS_MIXED)
+        return elem_matrices<float, true>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
+                                          egroup, out);
     return elem_matrices<float>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
                                 egroup, out, precision == 2);
 }
