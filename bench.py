@@ -65,7 +65,7 @@ MEASURED_TRAFFIC_PER_ELEMENT = {
                                       "(profiles/k_t3_elements_k_gather_t3ff_mixed_512.md)"),
     "k_gather FS_MIXED": (1984.5, "ncu --set full, k_gather, FS_MIXED, T3FF 512^2 "
                                   "(profiles/k_t3_elements_k_gather_t3ff_mixed_512.md)"),
-    "k_t3_elements FS_MIXED_COMP": (1663.5, "ncu --set full, k_t3_elements, FS_MIXED_COMP, T3FF 512^2 "
+    "k_t3_elements FS_MIXED_COMP": (1668.8, "ncu --set full, k_t3_elements, FS_MIXED_COMP, T3FF 512^2 "
                                             "(profiles/k_t3_elements_k_gather_t3ff_mixed_comp_512.md)"),
     "k_gather FS_MIXED_COMP": (2874.2, "ncu --set full, k_gather, FS_MIXED_COMP, T3FF 512^2 "
                                        "(profiles/k_t3_elements_k_gather_t3ff_mixed_comp_512.md)"),
@@ -543,23 +543,26 @@ def corotbeam_lattice(torch, device=0, n=100, steps=5, warmup=3):
     return out
 
 
-def composite_c4(torch, device=0, n=512, n_eig=512, nev=20, steps=5, warmup=3):
+def composite_c4(torch, device=0, n=512, n_eig=512, nev=20, steps=5, warmup=3, n_eig_t3=256):
     """The layered Q4RS plate ([0/90/90/0], 0.25 mm plies, 1 m side, simply
     supported, in-plane rigid-body motion restrained): stiffness assembly in
     the three arithmetic modes at n x n, and the nev lowest eigenvalues of an
     n_eig x n_eig plate from the FP64, compensated mixed and plain mixed
     stiffness with the lumped mass: ARPACK shift-invert (SciPy's eigsh, the
     library behind the reference's eigs) about -1, with K - sigma M
-    factorised and solved on the GPU (flexshell.eigs)."""
+    factorised and solved on the GPU (flexshell.eigs); and the same 20
+    eigenvalues of an n_eig_t3 x n_eig_t3 plate with its quads split in
+    triangles (T3FFComp), FP64 and compensated."""
     from flexshell import _abi, materials, mesh
     from flexshell.eigen import eigs
-    from flexshell.femm import FEMMShellQ4RSComp, NodalField, SysmatAssemblerSparse, SysmatAssemblerSparseSymm
+    from flexshell.femm import (FEMMShellQ4RSComp, FEMMShellT3FFComp, NodalField, SysmatAssemblerSparse,
+                                SysmatAssemblerSparseSymm)
     from flexshell._lib import laminate, ptr
     lam = materials.lamina_material(1600.0, 140e9, 10e9, 0.3, 5e9, 5e9, 3.5e9)
     Dps, Dts = materials.shell_material_stiffness(lam)
     g = laminate([dict(Dps=Dps, Dts=Dts, thickness=0.25e-3, angle=a, rho=1600.0) for a in (0, 90, 90, 0)])
 
-    def plate_c4(m):
+    def plate_c4(m, triangles=False):
         xy, conn = mesh.Q4block(1.0, 1.0, m, m)
         xyz = mesh.xyz3(xy)
         x, y = xyz[:, 0], xyz[:, 1]
@@ -571,7 +574,8 @@ def composite_c4(torch, device=0, n=512, n_eig=512, nev=20, steps=5, warmup=3):
         c0, c1 = int(np.argmin(np.abs(x) + np.abs(y))), int(np.argmin(np.abs(x - 1) + np.abs(y)))
         fixed[c0, 0] = fixed[c0, 1] = fixed[c1, 1] = True
         dof, nfree = mesh.numberdofs(fixed)
-        femm = FEMMShellQ4RSComp(conn, g, device=device)
+        femm = (FEMMShellT3FFComp(mesh.quads_to_triangles(conn), g, device=device) if triangles
+                else FEMMShellQ4RSComp(conn, g, device=device))
         geom0 = NodalField(xyz)
         dchi = NodalField(np.zeros((xyz.shape[0], 6)))
         dchi.dofnums = np.asfortranarray(dof)
@@ -617,6 +621,18 @@ def composite_c4(torch, device=0, n=512, n_eig=512, nev=20, steps=5, warmup=3):
             float((np.abs(w[name] - w["fp64"]) / np.abs(w["fp64"])).max()) if name in w else None)
     out["M_rel_err_mixed_vs_fp64_max"] = 0.0  # the lumped mass is double in every mode
     out["lowest_hz"] = float(np.sqrt(w["fp64"][0]) / (2 * np.pi))
+    # the same plate with its quads split in triangles (T3FFComp: the element
+    # type of the headline step, whose compensated sums are Dot2): the 20
+    # lowest eigenvalues in FP64 and the compensated mode
+    femm, geom0, dchi, nfree = plate_c4(n_eig_t3, triangles=True)
+    wt = {}
+    for prec, name in ((_abi.FS_FP64, "fp64"), (_abi.FS_MIXED_COMP, "mixed_comp")):
+        wt[name] = eigs(femm, geom0, dchi, nev, sigma=-1.0, precision=prec, nfree=nfree, tol=1e-12,
+                        return_eigenvectors=False)
+    femm.close()
+    out["t3_eig_elements"] = 2 * n_eig_t3 * n_eig_t3
+    out["t3_eig_rel_err_mixed_comp_vs_fp64_max"] = float(
+        (np.abs(wt["mixed_comp"] - wt["fp64"]) / np.abs(wt["fp64"])).max())
     out["eigensolver"] = ("ARPACK shift-invert (scipy eigsh) about -1, K - sigma M factorised on the GPU "
                           "(banded Cholesky, double)")
     out["boundary"] = "w = 0 on the edges; u = v = 0 at (0,0), v = 0 at (1,0)"
@@ -909,7 +925,9 @@ def main():
             "M_rel_err_vs_fp64_max": 0.0,
             "eig20_rel_err_vs_fp64_max": c4["eig_rel_err_mixed_comp_vs_fp64_max"] if c4 else None,
             "eig20_plate": ("layered Q4RS plate, %d x %d quads" % ((int(round(np.sqrt(c4["eig_elements"]))),) * 2))
-                           if c4 else None},
+                           if c4 else None,
+            "eig20_t3_rel_err_vs_fp64_max": c4["t3_eig_rel_err_mixed_comp_vs_fp64_max"] if c4 else None,
+            "eig20_t3_plate": ("the same plate as T3FFComp, %d triangles" % c4["t3_eig_elements"]) if c4 else None},
         "results": {
             "t3ff": {"elements": ne3, "nnz": nnz,
                      "mixed_comp_elements_per_s": ne3 / (ms_head * 1e-3),

@@ -163,13 +163,26 @@ __device__ __forceinline__ void dot3_step_x2(f32x2 &s, f32x2 &c, f32x2 &d, f32x2
     d = x2_add(d, x2_sub(f, m));
 }
 
+// Dot2 on two entries at once: the product split exactly, p added to s by
+// TwoSum, its error and the product's (e + pl = e - m) added to c.
+__device__ __forceinline__ void dot2_step_x2(f32x2 &s, f32x2 &c, f32x2 a, f32x2 na, f32x2 b)
+{
+    const f32x2 p = x2_mul(a, b);
+    const f32x2 m = x2_fma(na, b, p);
+    const f32x2 e = x2_two_sum(s, p);
+    c = x2_add(c, x2_sub(e, m));
+}
+
 // Float rows into float pairs (FS_MIXED_COMP): the three-level compensated
 // sums, entries (i, 2q) and (i, 2q + 1) in one packed register pair.  A row
 // reaching only one entry of a pair adds a zero product to the other, which
 // leaves its sums unchanged; DIAG: only the pairs holding an entry j >= i.
 // store() writes s + (c + d) as (hi, lo) float pairs: c + d rounded (below
 // the pair's last bit), then Fast2Sum; DIAG mirrors the entries j < i.
-template <int NI> struct BlockAcc<float, true, NI> {
+// LEVELS 2: Dot2 on entry pairs (s, c; what is lost is c's rounding, about
+// 2^-48 of the summed terms per term summed), for elements with few rows per
+// entry.
+template <int NI, int LEVELS = 3> struct PairAcc {
     f32x2 s[NI][3], c[NI][3], d[NI][3];
     __device__ __forceinline__ void zero()
     {
@@ -191,7 +204,12 @@ template <int NI> struct BlockAcc<float, true, NI> {
             const f32x2 a2 = x2_pack(ra[i], ra[i]), na2 = x2_pack(-ra[i], -ra[i]);
 #pragma unroll
             for (int q = Q0; q < Q1; q++)
-                if (!DIAG || 2 * q + 1 >= i) dot3_step_x2(s[i][q], c[i][q], d[i][q], a2, na2, b2[q]);
+                if (!DIAG || 2 * q + 1 >= i) {
+                    if constexpr (LEVELS == 3)
+                        dot3_step_x2(s[i][q], c[i][q], d[i][q], a2, na2, b2[q]);
+                    else
+                        dot2_step_x2(s[i][q], c[i][q], a2, na2, b2[q]);
+                }
         }
     }
     template <bool DIAG = false, class S> __device__ __forceinline__ void store(S *o)
@@ -202,7 +220,7 @@ template <int NI> struct BlockAcc<float, true, NI> {
 #pragma unroll
             for (int q = 0; q < 3; q++) {
                 if (DIAG && 2 * q + 1 < i) continue;
-                const f32x2 cd = x2_add(c[i][q], d[i][q]);
+                const f32x2 cd = LEVELS == 3 ? x2_add(c[i][q], d[i][q]) : c[i][q];
                 const f32x2 hh = x2_add(s[i][q], cd);
                 const f32x2 ll = x2_sub(cd, x2_sub(hh, s[i][q]));
                 x2_unpack(hh, h[i][2 * q], h[i][2 * q + 1]);
@@ -225,6 +243,7 @@ template <int NI> struct BlockAcc<float, true, NI> {
                 o4[3 * i + q] = make_float4(h[i][2 * q], l[i][2 * q], h[i][2 * q + 1], l[i][2 * q + 1]);
     }
 };
+template <int NI> struct BlockAcc<float, true, NI> : PairAcc<NI, 3> {};
 
 // acc += sum over rows [r0, r1) of row[6a + i] row[6b + j] for i in
 // [I0, I1), j in [J0, J1): the sub-blocks a row can reach (DIAG: a = b, the
@@ -294,6 +313,13 @@ __device__ __forceinline__ void gram_rows_h(Acc &acc, const R *base, int r0, int
     });
 }
 
+// Accumulation depth of the T3 kernels' float-pair sums (at most 9 rows per
+// entry: Dot2 is enough there; the Q4 kernels' 33 rows per entry take three
+// levels, BlockAcc<float, true>).
+constexpr int T3_PAIR_LEVELS = 2;
+template <class R, bool PAIR> struct T3Acc { typedef BlockAcc<R, PAIR> type; };
+template <> struct T3Acc<float, true> { typedef PairAcc<6, T3_PAIR_LEVELS> type; };
+
 // The upper node blocks of an NN-node element: diag(a) computes block
 // (a, a) (its upper triangle), off(a, b) block (a, b) for b > a.
 // Plain stores (float or double): one loop over the blocks, not unrolled,
@@ -333,7 +359,7 @@ __device__ __forceinline__ void write_blocks_compact(const R *rows, S *out)
     constexpr bool PAIR = sizeof(S) == 8 && sizeof(R) == 4;
     for_upper_blocks<NN, PAIR>(
         [&](int a) {
-            BlockAcc<R, PAIR> acc;
+            typename T3Acc<R, PAIR>::type acc;
             acc.zero();
             gram_rows_c<0, 3, 0, 3, L::MS, 3, 0, true, PAIR>(acc, rows, 0, 3, a, a);
             gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0, true, PAIR>(acc, rows + L::BS, 0, 3 + NS, a, a);
@@ -341,7 +367,7 @@ __device__ __forceinline__ void write_blocks_compact(const R *rows, S *out)
             acc.template store<true>(out + ub(a, a, NN) * 36);
         },
         [&](int a, int b) {
-            BlockAcc<R, PAIR> acc;
+            typename T3Acc<R, PAIR>::type acc;
             acc.zero();
             gram_rows_c<0, 3, 0, 3, L::MS, 3, 0, false, PAIR>(acc, rows, 0, 3, a, b);
             gram_rows_c<0, 6, 0, 6, L::BSS, 6, 0, false, PAIR>(acc, rows + L::BS, 0, 3 + NS, a, b);
@@ -362,7 +388,7 @@ __device__ __forceinline__ void write_blocks(const R *rows, int nrows, S *out)
     const int ND = 6 * NN;
     for_upper_blocks<NN, PAIR>(
         [&](int a) {
-            BlockAcc<R, PAIR> acc;
+            typename T3Acc<R, PAIR>::type acc;
             acc.zero();
             if (SPARSE) {
                 gram_rows<0, 3, 0, 3, true, PAIR>(acc, rows, ND, 0, 3, a, a);
@@ -374,7 +400,7 @@ __device__ __forceinline__ void write_blocks(const R *rows, int nrows, S *out)
             acc.template store<true>(out + ub(a, a, NN) * 36);
         },
         [&](int a, int b) {
-            BlockAcc<R, PAIR> acc;
+            typename T3Acc<R, PAIR>::type acc;
             acc.zero();
             if (SPARSE) {
                 gram_rows<0, 3, 0, 3, false, PAIR>(acc, rows, ND, 0, 3, a, b);

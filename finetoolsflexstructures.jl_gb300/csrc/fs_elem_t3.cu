@@ -11,12 +11,12 @@ namespace fs {
 // Resident blocks of 128 threads asked of the compiler (the register budget
 // per thread).  Float rows stored as floats: 4 (128 registers) for
 // homogeneous elements, whose occupancy is otherwise held by registers, 3
-// (170) for the others.  Float rows stored as float pairs, whose three-part
-// accumulators take 108 registers: 2 (255; 170 spilled, and the kernel ran
-// 13 % slower at 3).  Double rows: 2.
+// (170) for the others.  Float rows stored as float pairs (Dot2 accumulators,
+// 72 registers): 3 for homogeneous elements (shared memory allows 3 of the
+// 128-element tiles), 2 (255) for the others.  Double rows: 2.
 template <class R, bool COMP, bool AVGK, class S> struct T3MinBlocks {
     static constexpr bool dense = COMP || AVGK;
-    static constexpr int value = sizeof(R) == 8 ? 2 : (sizeof(S) == 8 ? 2 : (dense ? 3 : 4));
+    static constexpr int value = sizeof(R) == 8 ? 2 : (sizeof(S) == 8 ? (dense ? 2 : 3) : (dense ? 3 : 4));
 };
 
 template <class R, bool COMP, bool AVGK, class S>

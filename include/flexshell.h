@@ -50,11 +50,11 @@ extern "C" {
 #define FS_MIXED 1      /* float element arithmetic; frames, triads, drilling
                            factor and CSR accumulation in double             */
 #define FS_MIXED_COMP 2 /* as FS_MIXED, with the element Gram products
-                           accumulated in float with three-level compensation
-                           (about 2^-70 of the summed terms lost), kept as
-                           float pairs and summed into float triples: the
-                           stiffness keeps the rigid-body null space to
-                           O(eps^2), for thin-plate eigenvalues */
+                           accumulated in compensated float sums (Dot2 for
+                           T3's at most 9 rows per entry, three levels for
+                           Q4's 33), kept as float pairs and summed into
+                           float triples: the stiffness keeps the rigid-body
+                           null space to O(eps^2), for thin-plate eigenvalues */
 
 /* assembler semantics (FinEtools assemblers) */
 #define FS_ASM_SPARSE 0      /* SysmatAssemblerSparse / SysmatAssemblerSparseCSRSymm

@@ -20,10 +20,11 @@ import problems as PB
 pytestmark = pytest.mark.gpu
 
 
-def _c4(n):
+def _c4(n, triangles=False):
     xyz, conn, dof, nfree, plies = PB.c4_plate(n)
     g = F.laminate(plies)
-    femm = F.FEMMShellQ4RSComp(conn, g)
+    femm = (F.FEMMShellT3FFComp(F.mesh.quads_to_triangles(conn), g) if triangles
+            else F.FEMMShellQ4RSComp(conn, g))
     geom0 = F.NodalField(xyz)
     dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
     dchi.dofnums = np.asfortranarray(dof)
@@ -69,8 +70,11 @@ def test_eigs_matches_arpack_with_scipy_factor():
     femm.close()
 
 
-def test_mixed_comp_lowest_eigenvalues_within_1e6():
-    femm, geom0, dchi, nf = _c4(48)
+@pytest.mark.parametrize("triangles", [False, True])
+def test_mixed_comp_lowest_eigenvalues_within_1e6(triangles):
+    # the layered plate as Q4RSComp (three-level compensated element sums) and
+    # with its quads split as T3FFComp (Dot2)
+    femm, geom0, dchi, nf = _c4(48, triangles)
     d64 = F.eigs(femm, geom0, dchi, 20, sigma=-1.0, nfree=nf, return_eigenvectors=False)
     dc = F.eigs(femm, geom0, dchi, 20, sigma=-1.0, nfree=nf, precision=F.FS_MIXED_COMP,
                 return_eigenvectors=False)
