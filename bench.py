@@ -61,9 +61,9 @@ def params(quads):
 # under profiles/); the figures are scaled to the benchmark's element count,
 # traffic growing in proportion to the elements at a fixed mesh type.
 MEASURED_TRAFFIC_PER_ELEMENT = {
-    "k_t3_elements FS_MIXED": (805.0, "ncu --set full, k_t3_elements, FS_MIXED, T3FF 512^2 "
+    "k_t3_elements FS_MIXED": (802.2, "ncu --set full, k_t3_elements, FS_MIXED, T3FF 512^2 "
                                       "(profiles/k_t3_elements_k_gather_t3ff_mixed_512.md)"),
-    "k_gather FS_MIXED": (1984.5, "ncu --set full, k_gather, FS_MIXED, T3FF 512^2 "
+    "k_gather FS_MIXED": (1983.5, "ncu --set full, k_gather, FS_MIXED, T3FF 512^2 "
                                   "(profiles/k_t3_elements_k_gather_t3ff_mixed_512.md)"),
     "k_t3_elements FS_MIXED_COMP": (1668.8, "ncu --set full, k_t3_elements, FS_MIXED_COMP, T3FF 512^2 "
                                             "(profiles/k_t3_elements_k_gather_t3ff_mixed_comp_512.md)"),
