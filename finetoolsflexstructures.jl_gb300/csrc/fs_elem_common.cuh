@@ -3,6 +3,7 @@
 // node blocks of an element matrix.
 #pragma once
 
+#include "fs_comp_sum.cuh"
 #include "fs_internal.cuh"
 
 namespace fs {
@@ -102,77 +103,6 @@ template <class R, bool PAIR, int NI = 6> struct BlockAcc {
     }
 };
 
-// Two floats in one 64-bit register pair and the packed FP32x2 arithmetic of
-// the sm_100 family (add/sub/mul/fma .rn .f32x2): both halves rounded to
-// nearest as the scalar instructions round them, two per instruction.
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 x2_pack(float lo, float hi)
-{
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void x2_unpack(f32x2 v, float &lo, float &hi) { asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v)); }
-__device__ __forceinline__ f32x2 x2_add(f32x2 a, f32x2 b)
-{
-    f32x2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 x2_sub(f32x2 a, f32x2 b)
-{
-    f32x2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b)
-{
-    f32x2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 x2_fma(f32x2 a, f32x2 b, f32x2 c)
-{
-    f32x2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-// s + v by TwoSum (Knuth): s <- fl(s + v), returns the exact error
-__device__ __forceinline__ f32x2 x2_two_sum(f32x2 &s, f32x2 v)
-{
-    const f32x2 t = x2_add(s, v);
-    const f32x2 z = x2_sub(t, s);
-    const f32x2 e = x2_add(x2_sub(s, x2_sub(t, z)), x2_sub(v, z));
-    s = t;
-    return e;
-}
-
-// One step of a three-level compensated dot product on two entries at once
-// (the error-free transformations of Ogita, Rump and Oishi's Dot2, applied
-// once more to the compensation term): the product a b split exactly into p
-// and pl (m = fma(-a, b, p) = -pl exactly), p added to s by TwoSum (error e),
-// e added to c by TwoSum (error f), and f + pl added to d.  What is lost is
-// the rounding of d's terms, about 2^-24 of |d|, itself of the order of
-// 2^-48 of the sum of |a b|: far below Dot2's 2^-48 of that sum.
-__device__ __forceinline__ void dot3_step_x2(f32x2 &s, f32x2 &c, f32x2 &d, f32x2 a, f32x2 na, f32x2 b)
-{
-    const f32x2 p = x2_mul(a, b);
-    const f32x2 m = x2_fma(na, b, p);
-    const f32x2 e = x2_two_sum(s, p);
-    const f32x2 f = x2_two_sum(c, e);
-    d = x2_add(d, x2_sub(f, m));
-}
-
-// Dot2 on two entries at once: the product split exactly, p added to s by
-// TwoSum, its error and the product's (e + pl = e - m) added to c.
-__device__ __forceinline__ void dot2_step_x2(f32x2 &s, f32x2 &c, f32x2 a, f32x2 na, f32x2 b)
-{
-    const f32x2 p = x2_mul(a, b);
-    const f32x2 m = x2_fma(na, b, p);
-    const f32x2 e = x2_two_sum(s, p);
-    c = x2_add(c, x2_sub(e, m));
-}
-
 // Float rows into float pairs (FS_MIXED_COMP): the three-level compensated
 // sums, entries (i, 2q) and (i, 2q + 1) in one packed register pair.  A row
 // reaching only one entry of a pair adds a zero product to the other, which
@@ -220,9 +150,8 @@ template <int NI, int LEVELS = 3> struct PairAcc {
 #pragma unroll
             for (int q = 0; q < 3; q++) {
                 if (DIAG && 2 * q + 1 < i) continue;
-                const f32x2 cd = LEVELS == 3 ? x2_add(c[i][q], d[i][q]) : c[i][q];
-                const f32x2 hh = x2_add(s[i][q], cd);
-                const f32x2 ll = x2_sub(cd, x2_sub(hh, s[i][q]));
+                f32x2 hh, ll;
+                x2_pair_finish<LEVELS>(s[i][q], c[i][q], d[i][q], hh, ll);
                 x2_unpack(hh, h[i][2 * q], h[i][2 * q + 1]);
                 x2_unpack(ll, l[i][2 * q], l[i][2 * q + 1]);
             }
@@ -243,7 +172,7 @@ template <int NI, int LEVELS = 3> struct PairAcc {
                 o4[3 * i + q] = make_float4(h[i][2 * q], l[i][2 * q], h[i][2 * q + 1], l[i][2 * q + 1]);
     }
 };
-template <int NI> struct BlockAcc<float, true, NI> : PairAcc<NI, 3> {};
+template <int NI> struct BlockAcc<float, true, NI> : PairAcc<NI, Q4_PAIR_LEVELS> {};
 
 // acc += sum over rows [r0, r1) of row[6a + i] row[6b + j] for i in
 // [I0, I1), j in [J0, J1): the sub-blocks a row can reach (DIAG: a = b, the
@@ -313,10 +242,8 @@ __device__ __forceinline__ void gram_rows_h(Acc &acc, const R *base, int r0, int
     });
 }
 
-// Accumulation depth of the T3 kernels' float-pair sums (at most 9 rows per
-// entry: Dot2 is enough there; the Q4 kernels' 33 rows per entry take three
-// levels, BlockAcc<float, true>).
-constexpr int T3_PAIR_LEVELS = 2;
+// The T3 kernels' float-pair sums at T3_PAIR_LEVELS (Dot2), the Q4 kernels'
+// (BlockAcc<float, true>) at Q4_PAIR_LEVELS.
 template <class R, bool PAIR> struct T3Acc { typedef BlockAcc<R, PAIR> type; };
 template <> struct T3Acc<float, true> { typedef PairAcc<6, T3_PAIR_LEVELS> type; };
 

@@ -34,39 +34,6 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
-// exact float -> double built from the bit pattern with integer operations
-// only (zeros, subnormals, normals, inf and nan), so that no conversion
-// lands on the double-precision pipe
-__device__ __forceinline__ double f2d_exact(float f)
-{
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t sign = u & 0x80000000u, a = u & 0x7fffffffu;
-    uint32_t ex = a >> 23, man = a & 0x7fffffu;
-    uint32_t dexp;
-    if (ex == 0xffu) {
-        dexp = 0x7ffu;                                   // inf / nan
-    } else if (ex != 0u) {
-        dexp = ex + (1023u - 127u);                      // normal
-    } else if (man != 0u) {
-        const uint32_t sh = (uint32_t)__clz((int)man) - 8u;  // subnormal: normalise
-        man = (man << sh) & 0x7fffffu;
-        dexp = 1023u - 126u - sh;
-    } else {
-        dexp = 0u;                                       // signed zero
-    }
-    return __hiloint2double((int)(sign | (dexp << 20) | (man >> 3)), (int)(man << 29));
-}
-
-// exact float -> double for normal numbers and zeros from the bit pattern
-// (rebias the exponent, move the mantissa); other values take f2d_exact
-__device__ __forceinline__ double f2d_fast(float f)
-{
-    const uint32_t u = __float_as_uint(f), a = u & 0x7fffffffu;
-    if (a != 0u && a - 0x00800000u >= 0x7f000000u) return f2d_exact(f);  // subnormal, inf, nan
-    const uint32_t h = (u & 0x80000000u) | (a != 0u ? (a >> 3) + 0x38000000u : 0u);
-    return __hiloint2double((int)h, (int)(u << 29));
-}
-
 // The six sums (rows k = 0..5 of the node) of one of a lane's row positions.
 // set() takes the first contribution, add() the next ones (src[st k]: the
 // six entries of a stored block's column or, transposed, its row), value(k)
@@ -143,12 +110,7 @@ template <> struct ColSum<float2> {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             const float2 u = src[st * 2 * q], w = src[st * (2 * q + 1)];
-            // the stored low half into the low part, the high half into the
-            // high part and its error into the low part; both errors of the
-            // low part to the tail
-            const f32x2 f0 = x2_two_sum(lo[q], x2_pack(u.y, w.y));
-            const f32x2 f1 = x2_two_sum(lo[q], x2_two_sum(hi[q], x2_pack(u.x, w.x)));
-            tl[q] = x2_add(tl[q], x2_add(f0, f1));
+            x2_triple_add(hi[q], lo[q], tl[q], x2_pack(u.x, w.x), x2_pack(u.y, w.y));
         }
     }
     // hi + (lo + tl): lo + tl exact in double, then one rounding of the
@@ -162,10 +124,7 @@ template <> struct ColSum<float2> {
         x2_unpack(hi[k >> 1], h0, h1);
         x2_unpack(lo[k >> 1], l0, l1);
         x2_unpack(tl[k >> 1], t0, t1);
-        const float h = (k & 1) ? h1 : h0, l = (k & 1) ? l1 : l0, t = (k & 1) ? t1 : t0;
-        double v = f2d_fast(h);
-        if (l != 0.f || t != 0.f) v += f2d_fast(l) + f2d_fast(t);
-        return v;
+        return triple_value((k & 1) ? h1 : h0, (k & 1) ? l1 : l0, (k & 1) ? t1 : t0);
     }
 };
 __device__ __forceinline__ double entry_value(float v) { return (double)v; }

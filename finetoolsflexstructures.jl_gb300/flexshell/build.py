@@ -18,7 +18,8 @@ LIB = os.path.join(BUILD, "libflexshell.so")
 SOURCES = ["fs_api.cu", "fs_symbolic.cu", "fs_numeric.cu", "fs_elem_t3.cu", "fs_elem_q4.cu", "fs_gather.cu",
            "fs_explicit.cu", "fs_noalloc.cu", "fs_beam.cu", "fs_batch.cu", "fs_resultants.cu",
            "fs_loads.cu", "fs_eigen.cu"]
-HEADERS = ["fs_internal.cuh", "fs_elem_math.cuh", "fs_elem_common.cuh", "fs_beam_math.cuh", "fs_host_prep.h"]
+HEADERS = ["fs_internal.cuh", "fs_elem_math.cuh", "fs_elem_common.cuh", "fs_comp_sum.cuh", "fs_beam_math.cuh",
+           "fs_host_prep.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

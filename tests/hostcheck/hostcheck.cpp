@@ -9,14 +9,53 @@
 
 #include "fs_host_prep.h"
 #include "fs_beam_math.cuh"
+#include "fs_comp_sum.cuh"
 
 using namespace fs;
+
+// How the Gram K = sum_r row_r row_r^T of an element is summed.
+enum GramSum {
+    GRAM_PLAIN,  // in the row type, rows in order (FS_FP64, FS_MIXED)
+    GRAM_COMP,   // FS_MIXED_COMP: the kernels' compensated sums (fs_comp_sum.cuh)
+    GRAM_EXACT,  // float rows: products exact in double, summed in double
+    GRAM_ABS     // float rows: sum of |row_r[i] row_r[j]| (error bounds)
+};
+
+// The element kernels' FS_MIXED_COMP sums: entries (i, 2q) and (i, 2q + 1)
+// packed in one f32x2 and summed over the rows in order at LEVELS levels,
+// the pairs holding an entry j >= i only, then the upper triangle mirrored;
+// each entry the double nearest hi + lo (one rounding).
+template <int LEVELS>
+static void comp_gram(const float (*rows)[24], int nrows, int nd, double *K)
+{
+    for (int i = 0; i < nd; i++)
+        for (int q = 0; 2 * q < nd; q++) {
+            if (2 * q + 1 < i) continue;
+            f32x2 s = x2_pack(0.f, 0.f), c = s, d = s, hh, ll;
+            for (int r = 0; r < nrows; r++) {
+                const f32x2 a2 = x2_pack(rows[r][i], rows[r][i]), na2 = x2_pack(-rows[r][i], -rows[r][i]);
+                const f32x2 b2 = x2_pack(rows[r][2 * q], rows[r][2 * q + 1]);
+                if (LEVELS == 3)
+                    dot3_step_x2(s, c, d, a2, na2, b2);
+                else
+                    dot2_step_x2(s, c, a2, na2, b2);
+            }
+            x2_pair_finish<LEVELS>(s, c, d, hh, ll);
+            float h0, h1, l0, l1;
+            x2_unpack(hh, h0, h1);
+            x2_unpack(ll, l0, l1);
+            K[i + nd * (2 * q)] = (double)h0 + (double)l0;
+            K[i + nd * (2 * q + 1)] = (double)h1 + (double)l1;
+        }
+    for (int j = 0; j < nd; j++)
+        for (int i = j + 1; i < nd; i++) K[i + nd * j] = K[j + nd * i];
+}
 
 template <class R, bool FFRAME = false>
 static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t nelem,
                          const int64_t *conn, const double *normals, const uint8_t *valid,
                          const double *thick, const fs_shell_params *p, const fs_layup_group *groups,
-                         const int32_t *egroup, double *out, bool exact_gram = false)
+                         const int32_t *egroup, double *out, GramSum gram = GRAM_PLAIN)
 {
     MatConst mc;
     if (prepare_matconst(*p, mc)) return 1;
@@ -89,13 +128,28 @@ static int elem_matrices(int etype, int64_t nnodes, const double *xyz, int64_t n
         }
         if (st) return 10 + st;
         double *K = out + (int64_t)nd * nd * e;
+        if constexpr (sizeof(R) == 4) {
+            if (gram == GRAM_COMP) {
+                if (nn == 3)
+                    comp_gram<T3_PAIR_LEVELS>(rows, nrows, nd, K);
+                else
+                    comp_gram<Q4_PAIR_LEVELS>(rows, nrows, nd, K);
+                continue;
+            }
+        }
         for (int j = 0; j < nd; j++)
             for (int i = 0; i < nd; i++) {
-                if (exact_gram) {
-                    // products of float rows are exact in double; accumulate in double
-                    double s = 0;
-                    for (int r = 0; r < nrows; r++) s += (double)rows[r][i] * (double)rows[r][j];
-                    K[i + nd * j] = s;
+                if (gram == GRAM_EXACT || gram == GRAM_ABS) {
+                    // products of float rows are exact in double; summed in
+                    // long double (a significand of 64 bits or more: at most
+                    // 36 terms, within 2^-58 of their magnitudes), rounded
+                    // once to double
+                    long double s = 0;
+                    for (int r = 0; r < nrows; r++) {
+                        const double t = (double)rows[r][i] * (double)rows[r][j];
+                        s += gram == GRAM_ABS ? fabs(t) : t;
+                    }
+                    K[i + nd * j] = (double)s;
                 } else {
                     R s = 0;
                     for (int r = 0; r < nrows; r++) s += rows[r][i] * rows[r][j];
@@ -116,12 +170,57 @@ extern "C" int hc_element_matrices(int etype, int precision, int64_t nnodes, con
         return elem_matrices<double>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
                                      egroup, out);
     // FS_MIXED: the Q4 points' frames in float, as the library's FS_MIXED
-    // kernel; FS_MIXED_COMP (2): double frames, the Gram summed exactly
+    // kernel; FS_MIXED_COMP: double frames, float rows, the kernels'
+    // compensated sums.  Test-only precisions 3 and 4: the FS_MIXED_COMP rows'
+    // exact Gram, and the sums of |row_r[i] row_r[j]| of those rows.
     if (precision == FS_MIXED)
         return elem_matrices<float, true>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
                                           egroup, out);
+    const GramSum g = precision == FS_MIXED_COMP ? GRAM_COMP : precision == 3 ? GRAM_EXACT : GRAM_ABS;
+    if (precision != FS_MIXED_COMP && precision != 3 && precision != 4) return 2;
     return elem_matrices<float>(etype, nnodes, xyz, nelem, conn, normals, valid, thick, p, groups,
-                                egroup, out, precision == 2);
+                                egroup, out, g);
+}
+
+// The compensated dot product of the element kernels on both lanes of an
+// f32x2: (a . b0, a . b1) summed in order at `levels` levels (2: Dot2, 3),
+// out = {hi0, lo0, hi1, lo1}.
+extern "C" int hc_comp_dot(int levels, int n, const float *a, const float *b0, const float *b1, float *out)
+{
+    if (levels != 2 && levels != 3) return 1;
+    f32x2 s = x2_pack(0.f, 0.f), c = s, d = s, hh, ll;
+    for (int r = 0; r < n; r++) {
+        const f32x2 a2 = x2_pack(a[r], a[r]), na2 = x2_pack(-a[r], -a[r]), b2 = x2_pack(b0[r], b1[r]);
+        if (levels == 3)
+            dot3_step_x2(s, c, d, a2, na2, b2);
+        else
+            dot2_step_x2(s, c, a2, na2, b2);
+    }
+    if (levels == 3)
+        x2_pair_finish<3>(s, c, d, hh, ll);
+    else
+        x2_pair_finish<2>(s, c, d, hh, ll);
+    x2_unpack(hh, out[0], out[2]);
+    x2_unpack(ll, out[1], out[3]);
+    return 0;
+}
+
+// The gather's column sum of float-pair entries on both lanes of an f32x2:
+// lane k sums the pairs (hi[k n + r], lo[k n + r]), r < n, as a float triple
+// (the first pair taken as is, the next ones by x2_triple_add) and rounds it
+// to double: out[k].
+extern "C" int hc_triple_sum(int n, const float *hi, const float *lo, double *out)
+{
+    if (n < 1) return 1;
+    f32x2 h = x2_pack(hi[0], hi[n]), l = x2_pack(lo[0], lo[n]), t = x2_pack(0.f, 0.f);
+    for (int r = 1; r < n; r++) x2_triple_add(h, l, t, x2_pack(hi[r], hi[n + r]), x2_pack(lo[r], lo[n + r]));
+    float h0, h1, l0, l1, t0, t1;
+    x2_unpack(h, h0, h1);
+    x2_unpack(l, l0, l1);
+    x2_unpack(t, t0, t1);
+    out[0] = triple_value(h0, l0, t0);
+    out[1] = triple_value(h1, l1, t1);
+    return 0;
 }
 
 // Stress resultants at the integration points (the device point math of

@@ -20,10 +20,13 @@ def lib():
     if _lib is None:
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
         srcs = [os.path.join(HERE, "hostcheck.cpp"), os.path.join(CSRC, "fs_elem_math.cuh"),
-                os.path.join(CSRC, "fs_host_prep.h"), os.path.join(CSRC, "fs_beam_math.cuh")]
+                os.path.join(CSRC, "fs_host_prep.h"), os.path.join(CSRC, "fs_beam_math.cuh"),
+                os.path.join(CSRC, "fs_comp_sum.cuh")]
         if not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in srcs):
             tmp = LIB + ".tmp%d" % os.getpid()
-            subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-I", CSRC,
+            # no contraction of a * b + c into an FMA: the compensated sums'
+            # error-free transformations need every operation rounded alone
+            subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-I", CSRC,
                             srcs[0], "-o", tmp], check=True)
             os.replace(tmp, LIB)
         _lib = ctypes.CDLL(LIB)
@@ -108,3 +111,27 @@ def q4_basis_pair():
     out = np.zeros(64)
     lib().hc_q4_basis(out.ctypes.data_as(ctypes.c_void_p))
     return out[:32].reshape(4, 4, 2), out[32:].reshape(4, 4, 2)
+
+
+def comp_dot(levels, a, b0, b1):
+    """The element kernels' compensated dot products (a . b0, a . b1) of float
+    vectors at 2 (Dot2) or 3 levels: ((hi0, lo0), (hi1, lo1)) as float32."""
+    a, b0, b1 = (np.ascontiguousarray(v, dtype=np.float32) for v in (a, b0, b1))
+    out = np.zeros(4, dtype=np.float32)
+    P = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    st = lib().hc_comp_dot(ctypes.c_int(levels), ctypes.c_int(a.size), P(a), P(b0), P(b1), P(out))
+    assert st == 0
+    return (out[0], out[1]), (out[2], out[3])
+
+
+def triple_sum(hi, lo):
+    """The gather's column sums of float pairs: hi, lo of shape (2, n), one
+    column per f32x2 lane; returns the two sums rounded to double."""
+    hi = np.ascontiguousarray(hi, dtype=np.float32)
+    lo = np.ascontiguousarray(lo, dtype=np.float32)
+    assert hi.shape == lo.shape and hi.shape[0] == 2
+    out = np.zeros(2)
+    P = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    st = lib().hc_triple_sum(ctypes.c_int(hi.shape[1]), P(hi), P(lo), P(out))
+    assert st == 0
+    return out
