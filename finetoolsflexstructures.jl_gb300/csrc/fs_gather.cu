@@ -18,8 +18,10 @@ namespace fs {
 // add costs as much as 64 float operations, this keeps one double add per
 // stored value instead of a conversion and an add per contribution, with an
 // error below 2^-46 of the largest contribution.  Float-pair element matrices
-// (FS_MIXED_COMP) are summed into a float triple, error below about 2^-70 of
-// the largest contribution, and rounded to double with two adds.  Rows longer than
+// (FS_MIXED_COMP) are summed into a float triple, which loses only its tail's
+// float rounding (at most 8 n^2 (n + 1) 2^-72 of the n contributions'
+// magnitudes; on ill-conditioned sums of up to 12 contributions below 2^-73
+// of the largest), and rounded to double with two adds.  Rows longer than
 // 32 * G_COLS positions fall back to accumulating in place in double.
 static const int G_MAXP = 8;
 
