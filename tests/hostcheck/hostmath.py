@@ -135,3 +135,51 @@ def triple_sum(hi, lo):
     st = lib().hc_triple_sum(ctypes.c_int(hi.shape[1]), P(hi), P(lo), P(out))
     assert st == 0
     return out
+
+
+DEVLIB = os.path.join(HERE, "_build", "libdevcheck.so")
+_devlib = None
+
+
+def dev_lib():
+    """The test-only device build of the compensated sums (devcheck.cu), for
+    sm_103a; needs nvcc and a GPU."""
+    global _devlib
+    if _devlib is None:
+        os.makedirs(os.path.dirname(DEVLIB), exist_ok=True)
+        srcs = [os.path.join(HERE, "devcheck.cu"), os.path.join(CSRC, "fs_comp_sum.cuh")]
+        if not os.path.exists(DEVLIB) or any(os.path.getmtime(s) > os.path.getmtime(DEVLIB) for s in srcs):
+            from flexshell import build as B
+            tmp = DEVLIB + ".tmp%d" % os.getpid()
+            subprocess.run([B.nvcc()] + B.ARCH + ["-O3", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
+                                                  "-I", CSRC, srcs[0], "-o", tmp], check=True)
+            os.replace(tmp, DEVLIB)
+        _devlib = ctypes.CDLL(DEVLIB)
+    return _devlib
+
+
+def dev_comp_dot(levels, a, b0, b1):
+    """comp_dot on the GPU for m inputs at once: a, b0, b1 of shape (m, n);
+    returns (m, 4) float32: hi0, lo0, hi1, lo1."""
+    a, b0, b1 = (np.ascontiguousarray(v, dtype=np.float32) for v in (a, b0, b1))
+    m, n = a.shape
+    assert b0.shape == (m, n) and b1.shape == (m, n)
+    out = np.zeros((m, 4), dtype=np.float32)
+    P = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    st = dev_lib().dc_comp_dot(ctypes.c_int(levels), ctypes.c_int(n), ctypes.c_int(m), P(a), P(b0), P(b1), P(out))
+    assert st == 0, st
+    return out
+
+
+def dev_triple_sum(hi, lo):
+    """triple_sum on the GPU for m inputs at once: hi, lo of shape (m, 2, n);
+    returns (m, 2) doubles."""
+    hi = np.ascontiguousarray(hi, dtype=np.float32)
+    lo = np.ascontiguousarray(lo, dtype=np.float32)
+    m, two, n = hi.shape
+    assert two == 2 and lo.shape == hi.shape
+    out = np.zeros((m, 2))
+    P = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    st = dev_lib().dc_triple_sum(ctypes.c_int(n), ctypes.c_int(m), P(hi), P(lo), P(out))
+    assert st == 0, st
+    return out
