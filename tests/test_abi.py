@@ -52,3 +52,44 @@ def test_numberdofs_matches_finetools_rule():
     assert d[0].tolist() == [1, 2, 3, 4, 5, 6]
     assert d[1].tolist() == [17, 7, 18, 8, 9, 10]
     assert d[2].tolist() == [11, 12, 13, 14, 15, 16]
+
+
+def _ctypes_matches(expr, c):
+    """A ctypes argtype expression of flexshell/_lib.py against a C parameter
+    (base type, pointer depth); c_void_p is an address, so it stands for any
+    pointer."""
+    base, depth = c
+    scalars = {"ctypes.c_int": {"int", "int32_t"}, "ctypes.c_int32": {"int", "int32_t"},
+               "ctypes.c_int64": {"int64_t"}, "ctypes.c_uint64": {"uint64_t"}, "ctypes.c_double": {"double"},
+               "ctypes.c_size_t": {"size_t"}}
+    if expr in ("vp", "ctypes.c_void_p"):
+        return depth >= 1
+    if expr == "ctypes.c_char_p":
+        return depth == 1 and base == "char"
+    if expr == "_c_i64_p":
+        return depth == 1 and base == "int64_t"
+    m = re.fullmatch(r"ctypes\.POINTER\((.*)\)", expr)
+    if m:
+        inner = m.group(1)
+        if inner.startswith("_abi."):
+            return depth == 1 and base == inner[5:]
+        return depth >= 1 and _ctypes_matches(inner, (base, depth - 1))
+    return depth == 0 and base in scalars.get(expr, ())
+
+
+def test_ctypes_argtypes_match_the_prototypes():
+    # every declared function has argtypes in the Python mirror (ctypes'
+    # default int conversion would truncate 64-bit arguments), with the
+    # prototype's arity and, argument by argument, its width or pointer depth
+    from test_julia_shim import _prototypes, _split_top
+    protos = _prototypes()
+    src = open(os.path.join(ROOT, "finetoolsflexstructures.jl_gb300", "flexshell", "_lib.py")).read()
+    decl = {m.group(1): _split_top(m.group(2))
+            for m in re.finditer(r"L\.(fs_\w+)\.argtypes\s*=\s*\[(.*?)\]\n", src, flags=re.S)}
+    assert set(decl) == set(protos), sorted(set(decl) ^ set(protos))
+    for name, types in decl.items():
+        cparams = protos[name][1]
+        assert len(types) == len(cparams), (name, len(types), len(cparams))
+        for k, (t, c) in enumerate(zip(types, cparams)):
+            assert _ctypes_matches(t, c), "%s argument %d: ctypes %s against C %s%s" % (
+                name, k + 1, t, c[0], " *" * c[1])

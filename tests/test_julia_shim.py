@@ -11,8 +11,8 @@ parse every ccall of the shim and check it against the header's prototype:
   against the built library);
 * the return type is int and the argument tuple has the prototype's arity;
 * each argument type matches the C parameter (width and signedness of
-  scalars, pointer depth and pointee of pointers; Ptr{Cvoid} stands for any
-  pointer to a single object);
+  scalars, pointer depth and pointee of pointers; Ptr{Cvoid} is an address
+  and stands for any pointer);
 * the three struct mirrors (FsShellParams, FsLayupGroup, FsBeamSection) have
   the C structs' fields in order, with the same names, types and array
   lengths, and the ctypes mirror the GPU tests use has the same size;
@@ -108,7 +108,7 @@ def _matches(jt, c):
         if depth < 1:
             return False
         if inner == "Cvoid":
-            return depth == 1
+            return True
         return _matches(inner, (base, depth - 1))
     return depth == 0 and base in SCALARS.get(jt, ())
 
