@@ -10,8 +10,8 @@ A step is one stiffness assembly: element matrices + deterministic CSR value
 gather, on device-resident inputs with the sparsity pattern built (it depends
 only on the mesh and is built once per mesh; its time is reported apart).
 `value` is T3FF elements assembled per second in the compensated mixed mode
-(FS_MIXED_COMP: float element rows, Gram products accumulated error-free and
-kept as float pairs, double CSR values), the mode whose stiffness, mass and
+(FS_MIXED_COMP: float element rows, Gram products accumulated in compensated
+sums and kept as float pairs, double CSR values), the mode whose stiffness, mass and
 20 lowest layered-plate eigenvalues are all within 1e-6 of FP64; the plain
 mixed mode (FS_MIXED), the FP64 path and Q4RS are reported beside it.  `e2e`
 is the same assembly through the C ABI from pinned host buffers: geometry and
@@ -379,7 +379,7 @@ def explicit_c5(torch, device=0, n=512, nsteps=10000, iters=200):
                 "omega_max": om.value, "dt": dt, "power_iterations": iters,
                 "final_u_rel_err_mixed_vs_fp64": float(np.abs(U32 - U64).max() / np.abs(U64).max()),
                 "final_u_rel_err_mixed_comp_vs_fp64": float(np.abs(Uc - U64).max() / np.abs(U64).max()),
-                "mixed_comp": "float block values with bf16 residuals, float-pair displacement copy, error-free "
+                "mixed_comp": "float block values with bf16 residuals, float-pair displacement copy, compensated "
                               "float sum of K U",
                 "final_u_max": float(np.abs(U64).max()),
                 "format": "6x6 node blocks (block rows = node neighbour lists)", "blocks": nblocks,

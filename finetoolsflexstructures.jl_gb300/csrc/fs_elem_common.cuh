@@ -52,7 +52,7 @@ __device__ __forceinline__ void store_rows(R *o, const R (&acc)[NI][6])
     }
 }
 
-// One step of an error-free dot product (Ogita, Rump and Oishi's Dot2):
+// One step of a compensated dot product (Ogita, Rump and Oishi's Dot2):
 // the product a*b is split exactly with an FMA and added to (s, c) by
 // TwoSum.  The _rn intrinsics are never contracted or reassociated.
 __device__ __forceinline__ void dot2_step(float &s, float &c, float a, float b)
@@ -303,8 +303,8 @@ __device__ __forceinline__ void write_blocks_compact(const R *rows, S *out)
 }
 
 // Upper node blocks of K = sum_rho row_rho row_rho^T.  Storage S: the row
-// type R itself, or float2 pairs for float rows accumulated error-free
-// (FS_MIXED_COMP).  SPARSE (homogeneous shells): rows 0..2 are membrane rows
+// type R itself, or float2 pairs for float rows accumulated in compensated
+// sums (FS_MIXED_COMP).  SPARSE (homogeneous shells): rows 0..2 are membrane rows
 // (nodal translations only) and the last NN rows drilling rows (the
 // rotations of one node each); their structurally zero products are
 // skipped, in the same row order, so the sums are those of the dense loop.

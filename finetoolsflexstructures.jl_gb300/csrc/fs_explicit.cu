@@ -22,8 +22,8 @@
 // acceleration and velocity updates stay in double.  With FS_MIXED_COMP each
 // value is kept as its float rounding plus the rounding's residual in bf16
 // (K to about 33 bits, 6 bytes a value), the displacement copy is a float
-// pair (hi, lo: U to about 48 bits), and K U is summed error-free in float
-// (Dot2 on the float value times hi; the products with lo and with the
+// pair (hi, lo: U to about 48 bits), and K U is summed in compensated float
+// sums (Dot2 on the float value times hi; the products with lo and with the
 // residual added to the error term).  A row of K U is a small remainder of
 // its terms for a smooth displacement field, so the float copy of U, the
 // float sum and the float rounding of K each leave errors far above their
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_bsr(int64_t nnodes, int64_t n, co
     cV[row] = cv;
 }
 
-// error-free accumulation of (kv + kr) * (xh + xl) into (s, c): Dot2 on
+// compensated accumulation of (kv + kr) * (xh + xl) into (s, c): Dot2 on
 // kv * xh, the small products kv * xl and kr * xh added to the error term
 // (kr * xl is below the error of the result)
 __device__ __forceinline__ void acc_pair(float &s, float &c, float kv, float kr, float2 x)
@@ -236,7 +236,7 @@ __device__ __forceinline__ void add_pair(float &s, float &c, float s2, float c2)
 }
 
 // The block product of k_cd_bsr with the float-pair displacement copy and
-// the error-free float sum (FS_MIXED_COMP); the rest of the step as there.
+// the compensated float sum (FS_MIXED_COMP); the rest of the step as there.
 __global__ void __launch_bounds__(CD_TPB) k_cd_bsr_comp(int64_t nnodes, int64_t n, const int32_t *dof,
                                                       const int64_t *nbr_off, const int32_t *nbr, const float *blk,
                                                       const __nv_bfloat16 *res, const float2 *xp, double *V,
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(CD_TPB) k_cd_bsr_comp(int64_t nnodes, int64_t 
 }
 
 // The CSR product of k_cd_rows with the float-pair displacement copy and the
-// error-free float sum (FS_MIXED_COMP).
+// compensated float sum (FS_MIXED_COMP).
 __global__ void __launch_bounds__(CD_TPB) k_cd_rows_comp(int64_t n, const int64_t *rowptr, const int32_t *colidx,
                                                        const float *vals, const __nv_bfloat16 *res,
                                                        const float2 *Uk, double *V, double *cV, double *A,

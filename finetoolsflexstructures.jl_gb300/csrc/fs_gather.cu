@@ -13,11 +13,12 @@ namespace fs {
 // owns whole row positions j (all six rows of the node) and adds the staged
 // contributions of the pairs in ascending assembly rank.  In double
 // (FS_FP64) the sum is a plain double accumulation.  For float element
-// matrices (FS_MIXED) the sum is carried error-free as an unevaluated pair
-// of floats (TwoSum), then rounded once to double: on GB300, where a double
-// add costs as much as 64 float operations, this keeps one double add per
-// stored value instead of a conversion and an add per contribution, with an
-// error below 2^-46 of the largest contribution.  Float-pair element matrices
+// matrices (FS_MIXED) the sum is carried as an unevaluated pair of floats
+// (TwoSum into the high part, its errors summed in the low part), then
+// rounded once to double: on GB300, where a double add costs as much as 64
+// float operations, this keeps one double add per stored value instead of a
+// conversion and an add per contribution, with an error below 2^-46 of the
+// largest contribution.  Float-pair element matrices
 // (FS_MIXED_COMP) are summed into a float triple, which loses only its tail's
 // float rounding (at most 8 n^2 (n + 1) 2^-72 of the n contributions'
 // magnitudes; on ill-conditioned sums of up to 12 contributions below 2^-73

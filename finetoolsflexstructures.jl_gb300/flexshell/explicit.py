@@ -18,7 +18,8 @@ class CentralDifference:
     """The step loop of one stiffness: M the diagonal mass (vector), C the
     damping (vector), dt the time step; precision FS_FP64, FS_MIXED (float
     restoring force, double state) or FS_MIXED_COMP (float values, the
-    restoring force summed error-free from a float-pair copy of U)."""
+    restoring force summed in compensated float sums from a float-pair copy
+    of U)."""
 
     def __init__(self, femm, M, C, dt, precision=_abi.FS_FP64):
         self.ctx = femm.ctx

@@ -225,8 +225,9 @@ int fs_element_masses(fs_ctx *ctx, double *out);
  * the per-dof vectors of _cd_loop! (:69-71).  Values are kept in double
  * (precision FS_FP64), rounded to float (FS_MIXED), or as float plus a bf16
  * residual (FS_MIXED_COMP); K U is formed in double (FS_FP64), in float from a
- * float copy of U (FS_MIXED), or error-free in float from a float-pair copy of
- * U (FS_MIXED_COMP); the state update is double with Kahan compensation. */
+ * float copy of U (FS_MIXED), or in compensated float sums from a float-pair
+ * copy of U (FS_MIXED_COMP); the state update is double with Kahan
+ * compensation. */
 int fs_explicit_setup(fs_ctx *ctx, int precision, const double *invMC, const double *C, double dt);
 int fs_explicit_set_state(fs_ctx *ctx, const double *U, const double *V, const double *A);
 /* External force of the reference example's force!(F, t): F = g(t) Fmag

@@ -1,11 +1,11 @@
 """The gather's summation, value by value: every stored value is the sum of
 its element contributions in ascending assembly rank (the order in which
 Julia's sparse(I, J, V) combines duplicates) — a left-to-right double sum in
-FP64, and in FS_MIXED the error-free float-pair (TwoSum) accumulation of the
-float contributions rounded once to double.  The expected values are
+FP64, and in FS_MIXED the float-pair (TwoSum) accumulation of the float
+contributions rounded once to double.  The expected values are
 recomputed on the host from the library's own element matrices, so the
 comparison is bitwise; in FS_MIXED_COMP the stored float pairs are summed
-error-free and rounded once, checked against the exact sum of the element
+as float triples and rounded once, checked against the exact sum of the element
 matrices as reported (each pair rounded to a double, which a pair whose low
 half is far below its high half's last place does not fit exactly).  The
 meshes exercise the single-batch path (Scordelis-Lo

@@ -234,7 +234,7 @@ def test_explicit_steps_match_oracle():
     # Mixed: the restoring force K U is formed in float from float values; K U is
     # a small residual of large terms, so its float rounding shows at ~1e-5 of the
     # velocity after 200 steps (measured 5.4e-5).  Compensated: float values with
-    # bf16 residuals, a float-pair U and an error-free float sum (measured 3.5e-9).
+    # bf16 residuals, a float-pair U and a compensated float sum (measured 3.5e-9).
     for prec, tol in ((F.FS_FP64, 1e-10), (F.FS_MIXED, 2e-4), (F.FS_MIXED_COMP, 1e-7)):
         ctx = femm.ctx
         import ctypes
@@ -444,7 +444,7 @@ def test_composite_eigenvalues_mixed_vs_fp64():
     # O(eps |K|) errors in the shear-dominated w-w block of this 1 mm plate,
     # a spurious foundation stiffness that shifts every bending eigenvalue
     # (about 0.07 here, 8e-5 of the lowest); FS_MIXED_COMP accumulates them
-    # error-free and keeps the 1e-6 target
+    # in compensated sums and keeps the 1e-6 target
     rel = np.abs(w32 - w64) / np.abs(w64)
     assert rel.max() <= 1e-3, rel.max()
     relc = np.abs(wc - w64) / np.abs(w64)
@@ -509,7 +509,7 @@ def test_explicit_smooth_field_error_by_mode():
     1,500 steps): final displacements of the mixed and compensated steps
     against the FP64 step.  A smooth field is where K U cancels most: the
     plain mixed step is off by 1e-5..1e-4 of max |U| here, the compensated
-    one (float values with bf16 residuals, float-pair U, error-free float
+    one (float values with bf16 residuals, float-pair U, compensated float
     sum) by 1e-9..1e-8 (9.9e-9 at 128 x 128 after 2,500 steps, 5.5e-7 at
     512 x 512 after 10,000)."""
     import ctypes
