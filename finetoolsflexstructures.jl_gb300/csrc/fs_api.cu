@@ -127,6 +127,13 @@ int check_ready(fs_ctx *c, bool need_dofs)
     return FS_OK;
 }
 
+int check_last_stiffness(fs_ctx *c)
+{
+    if (!c->mat_rowptr || c->mat_kind != 0)
+        return set_err(c, FS_ERR_STATE, "no stiffness: fs_stiffness must be the last matrix assembled");
+    return FS_OK;
+}
+
 int status_to_code(fs_ctx *c, int bits)
 {
     if (bits & DEV_SINGULAR) return set_err(c, FS_ERR_SINGULAR_METRIC, "Singular metric matrix in _gradN_e!");

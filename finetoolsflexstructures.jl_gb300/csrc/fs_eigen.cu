@@ -260,8 +260,7 @@ int fs_shift_factor(fs_ctx *c, double sigma, const double *mdiag, int64_t *bandw
 {
     if (!c) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
-    if (!c->mat_rowptr || c->mat_kind != 0)
-        return set_err(c, FS_ERR_STATE, "no stiffness: fs_stiffness must be the last matrix assembled");
+    FS_TRY(check_last_stiffness(c));
     const int64_t n = c->mat_n;
     if (n > 0 && !mdiag) return set_err(c, FS_ERR_BAD_INPUT, "missing mass diagonal");
     ShiftFactor *s = nullptr;

@@ -569,7 +569,7 @@ int fs_power_iteration(fs_ctx *c, const double *mdiag, int64_t iters, uint64_t s
 {
     if (!c || !mdiag || !omega_max || iters < 1) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
-    if (!c->mat_rowptr) return set_err(c, FS_ERR_STATE, "no stiffness assembled");
+    FS_TRY(check_last_stiffness(c));
     int64_t n = c->mat_n;
     if (n == 0) return set_err(c, FS_ERR_BAD_INPUT, "empty matrix");
     size_t need = sizeof(double) * (size_t)(4 * n + PI_BLOCKS + 4);
@@ -612,7 +612,7 @@ int fs_explicit_setup(fs_ctx *c, int precision, const double *invMC, const doubl
 {
     if (!c || !invMC || !C) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
-    if (!c->mat_rowptr) return set_err(c, FS_ERR_STATE, "no stiffness assembled");
+    FS_TRY(check_last_stiffness(c));
     if (precision != FS_FP64 && precision != FS_MIXED && precision != FS_MIXED_COMP)
         return set_err(c, FS_ERR_BAD_INPUT, "unknown precision");
     if (!(dt > 0.0)) return set_err(c, FS_ERR_BAD_INPUT, "time step must be positive");
@@ -763,7 +763,7 @@ int fs_restoring_force(fs_ctx *c, const double *U, double *F)
 {
     if (!c) return FS_ERR_BAD_INPUT;
     FS_CUDA(c, cudaSetDevice(c->device));
-    if (!c->mat_rowptr) return set_err(c, FS_ERR_STATE, "no stiffness assembled");
+    FS_TRY(check_last_stiffness(c));
     const int64_t n = c->mat_n;
     if (n && (!U || !F)) return set_err(c, FS_ERR_BAD_INPUT, "missing vector");
     if (n == 0) return FS_OK;

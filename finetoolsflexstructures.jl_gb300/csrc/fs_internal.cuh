@@ -236,6 +236,10 @@ int read_status(fs_ctx *c, int *bits);
 int check_ready(fs_ctx *c, bool need_dofs = true);
 // the error code and message of a kernel status word (DEV_* bits)
 int status_to_code(fs_ctx *c, int bits);
+// FS_OK when the context's current matrix is a stiffness (the last matrix
+// assembled came from fs_stiffness or fs_beam_matrix with FS_BEAM_STIFFNESS),
+// else FS_ERR_STATE: the entry points that use "the last stiffness"
+int check_last_stiffness(fs_ctx *c);
 // address of the allocation-free path's scratch array in the current CUDA
 // context, looked up when the context is created (fs_noalloc.cu)
 void noalloc_setup(fs_ctx *c);

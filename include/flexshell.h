@@ -47,8 +47,11 @@ extern "C" {
 
 /* arithmetic of the element strain rows and Gram products */
 #define FS_FP64 0       /* everything in double: the drop-in                 */
-#define FS_MIXED 1      /* float element arithmetic; frames, triads, drilling
-                           factor and CSR accumulation in double             */
+#define FS_MIXED 1      /* float element arithmetic on element frames and
+                           coordinates formed in double (the Q4 Gauss-point
+                           frames and drilling factor in float); CSR values
+                           summed from the float blocks as float pairs and
+                           rounded once to double                            */
 #define FS_MIXED_COMP 2 /* as FS_MIXED, with the element Gram products
                            accumulated in compensated float sums (Dot2 for
                            T3's at most 9 rows per entry, three levels for
@@ -221,7 +224,8 @@ int fs_element_matrices(fs_ctx *ctx, int precision, double *out);
 int fs_element_masses(fs_ctx *ctx, double *out);
 
 /* --- explicit central difference (examples/.../plate_expl_examples.jl:61-94) --- */
-/* Uses the last matrix from fs_stiffness (must be nrows x nrows).  invMC and C are
+/* Uses the last matrix from fs_stiffness (must be nrows x nrows; FS_ERR_STATE
+ * when the last matrix assembled is not a stiffness).  invMC and C are
  * the per-dof vectors of _cd_loop! (:69-71).  Values are kept in double
  * (precision FS_FP64), rounded to float (FS_MIXED), or as float plus a bf16
  * residual (FS_MIXED_COMP); K U is formed in double (FS_FP64), in float from a
@@ -242,7 +246,8 @@ int fs_explicit_set_load(fs_ctx *ctx, const double *Fmag, const double *mul, int
 int fs_explicit_run(fs_ctx *ctx, int64_t nsteps);
 int fs_explicit_get_state(fs_ctx *ctx, double *U, double *V, double *A);
 /* Largest angular frequency of (K, M) for a diagonal M (mdiag, nrows entries) by
- * power iteration on the last assembled stiffness: the reference's `pwr`
+ * power iteration on the last assembled stiffness (FS_ERR_STATE when the last
+ * matrix assembled is not a stiffness): the reference's `pwr`
  * (examples/shells/dynamics/homogeneous/explicit/clamp_cyl_expl_examples.jl:131-142),
  * with a deterministic start vector from `seed`; dt_crit = 2 / omega_max. */
 int fs_power_iteration(fs_ctx *ctx, const double *mdiag, int64_t iters, uint64_t seed,
@@ -336,7 +341,8 @@ int fs_batch_matrix_copy(fs_ctx *ctx, int32_t mesh, int64_t *colptr, int64_t *ro
 
 /* Restoring force -K U of the shells for the generalized displacements U
  * (mat_n entries, system numbering) with the last matrix assembled by
- * fs_stiffness; F gets mat_n entries.  The reference shells have no such
+ * fs_stiffness (FS_ERR_STATE when the last matrix is not a stiffness); F gets
+ * mat_n entries.  The reference shells have no such
  * function: _cd_loop! (plate_expl_examples.jl:85) subtracts E = K U; the sign
  * here follows FEMMCorotBeam.restoringforce (force on the nodes). */
 int fs_restoring_force(fs_ctx *ctx, const double *U, double *F);

@@ -1,8 +1,9 @@
 """Edge cases of the assembly on the GPU, against the oracle: one element,
 nodes that no element uses, an empty mesh, every dof fixed, a node whose row
-is longer than the gather keeps in registers (the in-place path), and an
-element order that is not the mesh order.  FP64 within 1e-12 of the oracle
-with the identical pattern; mixed within 1e-6."""
+is longer than the gather keeps in registers (the in-place path), an
+element order that is not the mesh order, and the entry points that need
+the last matrix to be a stiffness.  FP64 within 1e-12 of the oracle with the
+identical pattern; mixed within 1e-6."""
 import numpy as np
 import pytest
 
@@ -160,4 +161,39 @@ def test_element_order_not_the_mesh_order():
     P, femm, geom0, dchi = _pair(xyz, conn, fixed_nodes=[1, 2, 3])
     _check(P, femm, geom0, dchi)
     _check(P, femm, geom0, dchi, n=dchi.nfreedofs)
+    femm.close()
+
+
+def test_last_stiffness_entry_points_refuse_another_matrix():
+    # fs_explicit_setup, fs_power_iteration, fs_restoring_force and
+    # fs_shift_factor use the last matrix assembled, which must be a
+    # stiffness: after fs_mass each returns FS_ERR_STATE (before any launch);
+    # after fs_stiffness again they run
+    import ctypes
+    import problems as PB
+    from flexshell import materials
+    from flexshell._lib import FlexShellError, ptr
+    xyz, conn, dof, nfree = PB.jittered_plate(4, False, seed=1)
+    femm = F.FEMMShellT3FF(conn, 0.01, materials.MatDeforElastIso(200e9, 0.3, 7850.0))
+    geom0 = F.NodalField(xyz)
+    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(dof)
+    femm.associategeometry(geom0)
+    femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi)
+    m = np.ascontiguousarray(
+        femm.mass(F.SysmatAssemblerFFBlock(F.SysmatAssemblerSparseDiag(), nfree), geom0, dchi).diagonal())
+    invm, c, u, f = 1.0 / m, np.zeros(nfree), np.ones(nfree), np.zeros(nfree)
+    om, kd = ctypes.c_double(), ctypes.c_int64()
+    calls = [("fs_explicit_setup", (F.FS_FP64, ptr(invm), ptr(c), ctypes.c_double(1e-6))),
+             ("fs_power_iteration", (ptr(m), ctypes.c_int64(5), ctypes.c_uint64(1), ctypes.byref(om))),
+             ("fs_restoring_force", (ptr(u), ptr(f))),
+             ("fs_shift_factor", (ctypes.c_double(0.0), ptr(m), ctypes.byref(kd)))]
+    for name, args in calls:
+        with pytest.raises(FlexShellError) as e:
+            femm.ctx.call(name, *args)
+        assert e.value.code == _abi.FS_ERR_STATE, name
+    femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi)
+    for name, args in calls[:3]:
+        femm.ctx.call(name, *args)
+    assert om.value > 0 and np.abs(f).max() > 0
     femm.close()
