@@ -272,6 +272,7 @@ int fs_mesh_set(fs_ctx *c, int elem_type, int64_t nnodes, const double *xyz, int
     free_mesh(c->mesh);
     reset_pattern(c->pat);
     c->mat_rowptr = nullptr;
+    free_shift(c);  // a factor of the previous mesh's stiffness
     free_beam(c);
     c->batch = fs_ctx::Batch();
     c->normals_ready = false;
@@ -341,6 +342,7 @@ int fs_dofs_set(fs_ctx *c, const int64_t *dofnums)
     reset_pattern(c->pat);
     c->ex.ready = false;
     c->mat_rowptr = nullptr;
+    free_shift(c);  // its band and size follow the previous numbering
     size_t ndof = (size_t)(6 * m.nnodes);
     FS_TRY(ensure_scratch(c, sizeof(int64_t) * (ndof + 1)));
     int64_t *raw = (int64_t *)c->scratch;

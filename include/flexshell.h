@@ -265,7 +265,10 @@ int fs_power_iteration(fs_ctx *ctx, const double *mdiag, int64_t iters, uint64_t
  * nrows x (bandwidth + 512) doubles (more than 160 GiB: FS_ERR_UNSUPPORTED).
  * A matrix that is not positive definite gives FS_ERR_BAD_INPUT.
  * fs_shift_solve solves (K - sigma M) X = B for nrhs host right-hand sides
- * (nrows x nrhs, column-major).  An eigensolver (ARPACK) supplies the rest. */
+ * (nrows x nrhs, column-major).  A new mesh or dof numbering (fs_mesh_set,
+ * fs_dofs_set) releases the factor: fs_shift_solve then returns FS_ERR_STATE
+ * until fs_shift_factor is called again.  An eigensolver (ARPACK) supplies
+ * the rest. */
 int fs_shift_factor(fs_ctx *ctx, double sigma, const double *mdiag, int64_t *bandwidth_out);
 int fs_shift_solve(fs_ctx *ctx, int nrhs, const double *b, double *x);
 

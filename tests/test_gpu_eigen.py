@@ -99,4 +99,13 @@ def test_shift_errors():
         F.ShiftInvert(femm.ctx, Md, 2.0 * w0)
     assert ei.value.code == _abi.FS_ERR_BAD_INPUT
     assert "positive definite" in str(ei.value)
+    # a new dof numbering releases the factor: the next solve is refused
+    # instead of using a factor whose size and band belong to the old one
+    femm.stiffness(F.SysmatAssemblerFFBlock(F.SysmatAssemblerSparse(), nf), geom0, None, None, dchi)
+    S = F.ShiftInvert(femm.ctx, Md, -1.0)
+    S.solve(np.ones(nf))
+    femm.ctx.call("fs_dofs_set", ptr(np.asfortranarray(dchi.dofnums, dtype=np.int64)))
+    with pytest.raises(FlexShellError) as ei:
+        S.solve(np.ones(nf))
+    assert ei.value.code == _abi.FS_ERR_STATE
     femm.close()
