@@ -276,7 +276,7 @@ int fs_mesh_set(fs_ctx *c, int elem_type, int64_t nnodes, const double *xyz, int
     free_beam(c);
     c->batch = fs_ctx::Batch();
     c->normals_ready = false;
-    c->ex.ready = false;
+    end_explicit(c);
     MeshDev &m = c->mesh;
     m.etype = elem_type;
     m.nen = (elem_type == FS_T3FF || elem_type == FS_T3FFCOMP) ? 3 : (elem_type == FS_COROTBEAM ? 2 : 4);
@@ -340,7 +340,7 @@ int fs_dofs_set(fs_ctx *c, const int64_t *dofnums)
     MeshDev &m = c->mesh;
     if (m.nnodes && !dofnums) return set_err(c, FS_ERR_BAD_INPUT, "missing dof numbers");
     reset_pattern(c->pat);
-    c->ex.ready = false;
+    end_explicit(c);
     c->mat_rowptr = nullptr;
     free_shift(c);  // its band and size follow the previous numbering
     size_t ndof = (size_t)(6 * m.nnodes);
@@ -460,6 +460,7 @@ int fs_normals_get(fs_ctx *c, double *normals, uint8_t *valid)
 int fs::assemble_matrix(fs_ctx *c, int precision, int assembler, int64_t nrows, int64_t *nnz_out, int beam_which,
                         int mass_type)
 {
+    end_explicit(c);  // the current matrix (and maybe the pattern) changes
     if (c->pat.n != nrows || !c->pat.rowptr) {
         FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
         FS_TRY(build_pattern(c, nrows));
@@ -542,6 +543,7 @@ int fs_mass(fs_ctx *c, int assembler, int64_t nrows, int64_t *nnz_out)
     if (!c->normals_ready)
         return set_err(c, FS_ERR_STATE, "associategeometry! has not been called (self._associatedgeometry == true)");
     if (nrows < 0) return set_err(c, FS_ERR_BAD_INPUT, "negative matrix size");
+    end_explicit(c);  // the current matrix (and maybe the pattern) changes
     FS_TRY(build_pattern(c, nrows));
     FS_TRY(launch_masses(c));
     FS_TRY(assemble_mass(c, assembler, nrows));
@@ -624,6 +626,7 @@ int fs_pattern(fs_ctx *c, int64_t nrows, int64_t *nnz_out)
     FS_TRY(check_ready(c));
     if (nrows < 0) return set_err(c, FS_ERR_BAD_INPUT, "negative matrix size");
     if (c->pat.n != nrows || !c->pat.rowptr) {
+        end_explicit(c);  // its captured steps read the pattern
         FS_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
         FS_TRY(build_pattern(c, nrows));
         FS_CUDA(c, cudaEventRecord(c->ev[1], c->stream));

@@ -559,6 +559,16 @@ __global__ void k_start(int64_t n, uint64_t seed, double *v)
     v[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0);
 }
 
+void end_explicit(fs_ctx *c)
+{
+    auto &x = c->ex;
+    if (x.exec) cudaGraphExecDestroy(x.exec);
+    if (x.graph) cudaGraphDestroy(x.graph);
+    x.exec = nullptr;
+    x.graph = nullptr;
+    x.ready = false;
+}
+
 }  // namespace fs
 
 using namespace fs;

@@ -245,6 +245,10 @@ int check_last_stiffness(fs_ctx *c);
 void noalloc_setup(fs_ctx *c);
 // releases the shift-invert factor of the context (fs_eigen.cu)
 void free_shift(fs_ctx *c);
+// ends the explicit step's state and releases its captured steps, which read
+// the pattern's neighbour lists and, in the CSR form, the current matrix:
+// called before either changes (fs_explicit.cu)
+void end_explicit(fs_ctx *c);
 
 int explicit_launch_steps(fs_ctx *c, int64_t nsteps);
 

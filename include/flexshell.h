@@ -225,7 +225,10 @@ int fs_element_masses(fs_ctx *ctx, double *out);
 
 /* --- explicit central difference (examples/.../plate_expl_examples.jl:61-94) --- */
 /* Uses the last matrix from fs_stiffness (must be nrows x nrows; FS_ERR_STATE
- * when the last matrix assembled is not a stiffness).  invMC and C are
+ * when the last matrix assembled is not a stiffness).  A later assembly in the
+ * context (fs_stiffness, fs_mass, fs_beam_matrix, a new fs_pattern) or a new
+ * mesh or dof numbering ends the explicit state: fs_explicit_* then return
+ * FS_ERR_STATE until fs_explicit_setup is called again.  invMC and C are
  * the per-dof vectors of _cd_loop! (:69-71).  Values are kept in double
  * (precision FS_FP64), rounded to float (FS_MIXED), or as float plus a bf16
  * residual (FS_MIXED_COMP); K U is formed in double (FS_FP64), in float from a

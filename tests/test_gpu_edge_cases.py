@@ -1,8 +1,9 @@
 """Edge cases of the assembly on the GPU, against the oracle: one element,
 nodes that no element uses, an empty mesh, every dof fixed, a node whose row
 is longer than the gather keeps in registers (the in-place path), an
-element order that is not the mesh order, and the entry points that need
-the last matrix to be a stiffness.  FP64 within 1e-12 of the oracle with the
+element order that is not the mesh order, the entry points that need the
+last matrix to be a stiffness, and the end of the explicit state at a new
+assembly.  FP64 within 1e-12 of the oracle with the
 identical pattern; mixed within 1e-6."""
 import numpy as np
 import pytest
@@ -196,4 +197,43 @@ def test_last_stiffness_entry_points_refuse_another_matrix():
     for name, args in calls[:3]:
         femm.ctx.call(name, *args)
     assert om.value > 0 and np.abs(f).max() > 0
+    femm.close()
+
+
+def test_explicit_state_ends_with_a_new_assembly():
+    # the captured explicit steps read the pattern and, in the CSR form, the
+    # current matrix: an assembly after fs_explicit_setup ends the state, so
+    # the next run is refused (FS_ERR_STATE) instead of reading buffers that
+    # the assembly may have replaced; a new setup starts it again
+    import ctypes
+    import problems as PB
+    from flexshell import materials
+    from flexshell._lib import FlexShellError, ptr
+    xyz, conn, dof, nfree = PB.jittered_plate(4, True, seed=2)
+    femm = F.FEMMShellQ4RS(conn, 0.01, materials.MatDeforElastIso(200e9, 0.3, 7850.0))
+    geom0 = F.NodalField(xyz)
+    dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    dchi.dofnums = np.asfortranarray(dof)
+    femm.associategeometry(geom0)
+    m = np.ascontiguousarray(
+        femm.mass(F.SysmatAssemblerFFBlock(F.SysmatAssemblerSparseDiag(), nfree), geom0, dchi).diagonal())
+    femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi)
+    invm, c, v0 = 1.0 / m, np.zeros(nfree), np.full(nfree, 1e-3)
+    z, u = np.zeros(nfree), np.zeros(nfree)
+    ctx = femm.ctx
+    ctx.call("fs_explicit_setup", F.FS_FP64, ptr(invm), ptr(c), ctypes.c_double(1e-7))
+    ctx.call("fs_explicit_set_state", ptr(z), ptr(v0), ptr(z))
+    ctx.call("fs_explicit_run", ctypes.c_int64(64))
+    femm.mass(F.SysmatAssemblerFFBlock(F.SysmatAssemblerSparseDiag(), nfree), geom0, dchi)
+    for name, args in (("fs_explicit_run", (ctypes.c_int64(64),)),
+                       ("fs_explicit_get_state", (ptr(u), None, None))):
+        with pytest.raises(FlexShellError) as e:
+            ctx.call(name, *args)
+        assert e.value.code == _abi.FS_ERR_STATE, name
+    femm.stiffness(F.SysmatAssemblerFFBlock(nfree), geom0, None, None, dchi)
+    ctx.call("fs_explicit_setup", F.FS_FP64, ptr(invm), ptr(c), ctypes.c_double(1e-7))
+    ctx.call("fs_explicit_set_state", ptr(z), ptr(v0), ptr(z))
+    ctx.call("fs_explicit_run", ctypes.c_int64(64))
+    ctx.call("fs_explicit_get_state", ptr(u), None, None)
+    assert np.abs(u).max() > 0
     femm.close()
