@@ -120,6 +120,10 @@ int fs_batch_matrix_copy(fs_ctx *c, int32_t mesh, int64_t *colptr, int64_t *rowv
     FS_CUDA(c, cudaSetDevice(c->device));
     if (!c->batch.active || !c->mat_rowptr) return set_err(c, FS_ERR_STATE, "no batch matrix assembled");
     const std::vector<int64_t> &roff = c->batch.roff;
+    // the row slices below index the current matrix: it must be the batch's
+    // stiffness (a mass or another matrix size assembled since: refused)
+    if (c->mat_kind != 0 || c->mat_n != roff.back())
+        return set_err(c, FS_ERR_STATE, "the current matrix is not the batch's: call fs_batch_stiffness again");
     if (mesh < 0 || mesh >= (int32_t)roff.size() - 1) return set_err(c, FS_ERR_BAD_INPUT, "mesh index out of range");
     const int64_t r0 = roff[(size_t)mesh], n = roff[(size_t)mesh + 1] - r0;
     int64_t b[2];

@@ -342,7 +342,8 @@ int fs_batch_set(fs_ctx *ctx, int elem_type, int32_t nmeshes, const int64_t *nno
  * entries of mesh i. */
 int fs_batch_stiffness(fs_ctx *ctx, int precision, int assembler, int64_t *nnz_out);
 /* Mesh i's matrix of the last fs_batch_stiffness: 1-based CSC (== CSR)
- * colptr[nrows[i]+1], rowval[nnz_out[i]], nzval[nnz_out[i]]. */
+ * colptr[nrows[i]+1], rowval[nnz_out[i]], nzval[nnz_out[i]].  FS_ERR_STATE
+ * when another matrix (a mass, another size) has been assembled since. */
 int fs_batch_matrix_copy(fs_ctx *ctx, int32_t mesh, int64_t *colptr, int64_t *rowval, double *nzval);
 
 /* Restoring force -K U of the shells for the generalized displacements U

@@ -2,8 +2,8 @@
 nodes that no element uses, an empty mesh, every dof fixed, a node whose row
 is longer than the gather keeps in registers (the in-place path), an
 element order that is not the mesh order, the entry points that need the
-last matrix to be a stiffness, and the end of the explicit state at a new
-assembly.  FP64 within 1e-12 of the oracle with the
+last matrix to be a stiffness, the end of the explicit state at a new
+assembly, and the batch copy of a current matrix that is not the batch's.  FP64 within 1e-12 of the oracle with the
 identical pattern; mixed within 1e-6."""
 import numpy as np
 import pytest
@@ -237,3 +237,33 @@ def test_explicit_state_ends_with_a_new_assembly():
     ctx.call("fs_explicit_get_state", ptr(u), None, None)
     assert np.abs(u).max() > 0
     femm.close()
+
+
+def test_batch_copy_refuses_another_current_matrix():
+    # the batch copy slices the current matrix at the meshes' row offsets:
+    # after a matrix of another size is assembled in the batch's context it
+    # is refused (FS_ERR_STATE) instead of reading past that matrix's rows
+    import ctypes
+    import problems as PB
+    from flexshell import materials
+    from flexshell._lib import FlexShellError, ptr
+    meshes = []
+    for k, n in enumerate([3, 4]):
+        xyz, conn, dof, nfree = PB.jittered_plate(n, False, seed=k)
+        dchi = F.NodalField(np.zeros((xyz.shape[0], 6)))
+        dchi.dofnums = np.asfortranarray(dof)
+        meshes.append((F.NodalField(xyz), conn, dchi, 0.01))
+    b = F.ShellBatch(F.FEMMShellT3FF, meshes, materials.MatDeforElastIso(2.0e11, 0.3, 7850.0))
+    Ks = b.stiffness(F.SysmatAssemblerSparse())
+    total = sum(b.nrows)
+    nnz = ctypes.c_int64()
+    b.ctx.call("fs_mass", _abi.FS_ASM_DIAG, ctypes.c_int64(total - 6), ctypes.byref(nnz))
+    colptr = np.empty(b.nrows[1] + 1, dtype=np.int64)
+    with pytest.raises(FlexShellError) as e:
+        b.ctx.call("fs_batch_matrix_copy", 1, ptr(colptr), None, None)
+    assert e.value.code == _abi.FS_ERR_STATE
+    # assembled again, the copy gives the same matrices
+    Ks2 = b.stiffness(F.SysmatAssemblerSparse())
+    for K, K2 in zip(Ks, Ks2):
+        assert np.array_equal(K.indptr, K2.indptr) and np.array_equal(K.data, K2.data)
+    b.close()
