@@ -310,12 +310,14 @@ function gpu_cd_loop!(femm, M, ksi, omegad, U0, V0, tend, dt, force!, peek;
         dt = tend / (nsteps + 1)
     end
     invMC = 1.0 ./ (m .+ (dt / 2) .* C)
-    check(ctx, ccall((:fs_explicit_setup, libflexshell), Cint,
-        (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Float64), ctx.h, precision, invMC, C, dt))
+    # the load first: an assembly in this context after fs_explicit_setup
+    # (a force! that assembles) would end the explicit state
     Fmag = zeros(n)
     force!(Fmag, 0.0)
     mul = [Float64(g(k * dt)) for k in 0:nsteps]
     A0 = invMC .* (mul[1] .* Fmag)
+    check(ctx, ccall((:fs_explicit_setup, libflexshell), Cint,
+        (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Float64), ctx.h, precision, invMC, C, dt))
     check(ctx, ccall((:fs_explicit_set_state, libflexshell), Cint,
         (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), ctx.h, Vector{Float64}(U0),
         Vector{Float64}(V0), A0))
