@@ -93,3 +93,23 @@ def test_ctypes_argtypes_match_the_prototypes():
         for k, (t, c) in enumerate(zip(types, cparams)):
             assert _ctypes_matches(t, c), "%s argument %d: ctypes %s against C %s%s" % (
                 name, k + 1, t, c[0], " *" * c[1])
+
+
+def test_without_a_gpu_the_library_fails_loudly():
+    # the library has no CPU path: without a CUDA device no context can be
+    # created, so a FEMM cannot be made and nothing is computed elsewhere
+    # (skipped where a device is present)
+    from flexshell._lib import Context, FlexShellError
+    try:
+        ctx = Context(0)
+    except FlexShellError as e:
+        err = e
+    else:
+        ctx.close()
+        import pytest
+        pytest.skip("a CUDA device is present")
+    assert "cannot create a context" in str(err)
+    import pytest
+    from flexshell import materials
+    with pytest.raises(FlexShellError):
+        femm.FEMMShellT3FF(np.array([[1, 2, 3]]), 0.01, materials.MatDeforElastIso(2e11, 0.3, 7850.0))
