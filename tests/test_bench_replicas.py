@@ -56,3 +56,29 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     assert bench.run_reference(args) == 0
     assert capsys.readouterr().out == ""
     assert bench.max_over_ranks(3.0, 1, None) == 3.0
+
+
+def test_reference_arm_line_keeps_the_contract(monkeypatch, capsys):
+    # the reference arm's JSON line on a 16 x 16 plate (the sample side forced
+    # small): the metric, unit and direction of the GPU arm, "impl":
+    # "reference", a cpu_baseline describing the run and an e2e with no
+    # host-device traffic
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setattr(bench, "cpu_sample_side", lambda nsteps, **kw: 16)
+    args = type("A", (), dict(warmup=1, steps=1, gpus=1, n=16))()
+    assert bench.run_reference(args) == 0
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC
+    assert d["unit"] == "elements/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 1 and d["n_gpus"] == 1
+    assert d["config"]["same_workload"] is True and "512 triangles" in d["config"]["workload"]
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
+    assert cb["unit"] == "elements/s" and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "elements/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
