@@ -88,6 +88,26 @@ def lib():
     return _lib
 
 
+class InputCache:
+    """A host copy of the array last uploaded to a context.  The reference
+    reads geom0 and dchi on every call, so an upload is repeated exactly when
+    the caller's array differs from the copy: replaced or changed in place
+    (an identity key would miss both an in-place change and a new array that
+    reuses a freed one's address)."""
+
+    def __init__(self):
+        self.copy = None
+
+    def stale(self, a):
+        return self.copy is None or self.copy.shape != a.shape or not np.array_equal(self.copy, a)
+
+    def store(self, a):
+        self.copy = np.array(a, copy=True, order="F")
+
+    def clear(self):
+        self.copy = None
+
+
 def ptr(a):
     """Address of a numpy array (or None)."""
     if a is None:

@@ -22,7 +22,7 @@ import ctypes
 import numpy as np
 
 from . import _abi
-from ._lib import Context, ptr
+from ._lib import Context, InputCache, ptr
 from .femm import NodalField, SysmatAssemblerSparseSymm, _Assembler
 
 MASS_TYPE_CONSISTENT_NO_ROTATION_INERTIA = 0
@@ -284,8 +284,8 @@ class FEMMCorotBeam:
             raise ValueError("sections must be nelem x 10")
         self.material = material
         self.ctx = Context(device)
-        self._geom = None
-        self._dof_key = None
+        self._geom = InputCache()
+        self._dofs = InputCache()
 
     @property
     def nelem(self):
@@ -293,25 +293,25 @@ class FEMMCorotBeam:
 
     def _sync(self, geom0, u1, Rfield1, dchi, v1=None):
         xyz = np.asfortranarray(geom0.values, dtype=np.float64)
-        if self._geom is None or self._geom[1] != xyz.shape:
+        if self._geom.copy is None or self._geom.copy.shape != xyz.shape:
             self.ctx.call("fs_mesh_set", _abi.FS_COROTBEAM, xyz.shape[0], ptr(xyz), self.nelem,
                           ptr(self.conn), None, None)
             secs = (_abi.fs_beam_section * self.nelem)()
             ctypes.memmove(secs, self.sections.ctypes.data, self.sections.nbytes)
             m = self.material
             self.ctx.call("fs_beam_setup", secs, float(m.E), float(m.nu), float(m.massdensity()))
-            self._dof_key = None
-        elif self._geom[0] != id(geom0.values):
+            self._geom.store(xyz)
+            self._dofs.clear()
+        elif self._geom.stale(xyz):
             self.ctx.call("fs_geometry_set", ptr(xyz))
-        self._geom = (id(geom0.values), xyz.shape)
+            self._geom.store(xyz)
         if dchi is not None:
             d = np.asfortranarray(dchi.dofnums, dtype=np.int64)
             if d.shape != (xyz.shape[0], 6):
                 raise ValueError("dchi must have 6 dofs per node")
-            key = (id(dchi.dofnums), int(d.sum()), d.tobytes()[:64])
-            if key != self._dof_key:
+            if self._dofs.stale(d):
                 self.ctx.call("fs_dofs_set", ptr(d))
-                self._dof_key = key
+                self._dofs.store(d)
         arr = lambda f, w: None if f is None else np.asfortranarray(
             np.asarray(getattr(f, "values", f), dtype=np.float64).reshape(xyz.shape[0], w, order="F"))
         u, R, v = arr(u1, 3), arr(Rfield1, 9), arr(v1, 6)

@@ -18,7 +18,7 @@ the reference shells.
 import numpy as np
 
 from . import _abi, mesh as _mesh
-from ._lib import Context, FlexShellError, ptr
+from ._lib import Context, FlexShellError, InputCache, ptr
 
 FS_FP64, FS_MIXED, FS_MIXED_COMP = _abi.FS_FP64, _abi.FS_MIXED, _abi.FS_MIXED_COMP
 
@@ -155,8 +155,8 @@ class _FEMMShell:
         self.layup_groups = layup_groups
         self.mcsys = mcsys  # None: isoparametric (the reference default); or a CSys* above
         self.ctx = Context(device)
-        self._geom = None
-        self._dof_key = None
+        self._geom = InputCache()
+        self._dofs = InputCache()
         self._associatedgeometry = False
         self._normals = None
         self._normal_valid = None
@@ -198,24 +198,26 @@ class _FEMMShell:
                 eg[np.asarray(g[1], dtype=np.int64) - 1] = k
             arr = (_abi.fs_layup_group * len(groups))(*groups)
             self.ctx.call("fs_layups_set", len(groups), arr, ptr(eg))
-        self._geom = (id(geom0.values), xyz.shape)
-        self._dof_key = None
+        self._geom.store(xyz)
+        self._dofs.clear()
 
     def _sync_inputs(self, geom0, dchi):
-        if self._geom != (id(geom0.values), np.shape(geom0.values)):
-            xyz = np.asfortranarray(geom0.values, dtype=np.float64)
+        xyz = np.asfortranarray(geom0.values, dtype=np.float64)
+        if self._geom.copy is not None and xyz.shape != self._geom.copy.shape:
+            raise ValueError("geometry with %d nodes for a mesh of %d: call associategeometry with it first"
+                             % (xyz.shape[0], self._geom.copy.shape[0]))
+        if self._geom.stale(xyz):
             self.ctx.call("fs_geometry_set", ptr(xyz))
-            self._geom = (id(geom0.values), xyz.shape)
+            self._geom.store(xyz)
         p, tharr = self._params()
         self.ctx.call("fs_params_set", p, ptr(tharr))
         if dchi is not None:
             d = np.asfortranarray(dchi.dofnums, dtype=np.int64)
             if d.shape != (geom0.values.shape[0], 6):
                 raise ValueError("dchi must have 6 dofs per node")
-            key = (id(dchi.dofnums), d.shape, int(d.sum()))
-            if key != self._dof_key:
+            if self._dofs.stale(d):
                 self.ctx.call("fs_dofs_set", ptr(d))
-                self._dof_key = key
+                self._dofs.store(d)
 
     # -- reference interface --------------------------------------------------
     def associategeometry(self, geom0):

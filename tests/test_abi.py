@@ -113,3 +113,27 @@ def test_without_a_gpu_the_library_fails_loudly():
     from flexshell import materials
     with pytest.raises(FlexShellError):
         femm.FEMMShellT3FF(np.array([[1, 2, 3]]), 0.01, materials.MatDeforElastIso(2e11, 0.3, 7850.0))
+
+
+def test_input_cache_sees_in_place_changes_and_replacements():
+    # the mirror re-uploads geom0 / dchi exactly when their content differs
+    # from what it uploaded last: an in-place move, an in-place renumbering
+    # (which keeps the dof numbers' sum) and a new shape are seen; an equal
+    # copy is not an upload
+    from flexshell._lib import InputCache
+    c = InputCache()
+    a = np.asfortranarray(np.arange(12.0).reshape(4, 3))
+    assert c.stale(a)
+    c.store(a)
+    assert not c.stale(a)
+    a[2, 1] += 1e-9
+    assert c.stale(a)
+    c.store(a)
+    assert not c.stale(a.copy())
+    d = np.asfortranarray(np.arange(1, 13, dtype=np.int64).reshape(4, 3))
+    c.store(d)
+    d[[0, 1]] = d[[1, 0]]
+    assert c.stale(d) and c.copy.sum() == d.sum()
+    assert c.stale(np.zeros((5, 3)))
+    c.clear()
+    assert c.stale(d)

@@ -99,3 +99,26 @@ def test_cd_loop_compensated_follows_fp64():
     err = np.abs(res[F.FS_MIXED_COMP] - res[F.FS_FP64]).max() / np.abs(res[F.FS_FP64]).max()
     assert err <= 1e-7, err
     femm.close()
+
+
+def test_inputs_changed_in_place_are_uploaded():
+    # the reference reads geom0 and dchi on every call: nodes moved in place
+    # and dofs renumbered in place (the same array objects) reach the next
+    # stiffness, which equals a fresh FEMM's on the same inputs (with the
+    # first FEMM's normals: neither recomputes them without associategeometry)
+    femm, geom0, dchi, xyz, conn, dof, nfree = _homog(False, 0.01, n=6)
+    K0 = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    geom0.values[:, 2] += 0.05 * geom0.values[:, 0] ** 2
+    dchi.dofnums[[0, 1]] = dchi.dofnums[[1, 0]]
+    K1 = femm.stiffness(F.SysmatAssemblerSparse(), geom0, None, None, dchi)
+    fresh = F.FEMMShellT3FF(conn, 0.01, STEEL)
+    g2 = F.NodalField(np.array(geom0.values))
+    d2 = F.NodalField(np.zeros((xyz.shape[0], 6)))
+    d2.dofnums = np.asfortranarray(np.array(dchi.dofnums))
+    fresh.associategeometry(g2)
+    fresh.set_normals(femm._normals, femm._normal_valid)
+    Kf = fresh.stiffness(F.SysmatAssemblerSparse(), g2, None, None, d2)
+    assert abs(K1 - K0).max() > 0
+    assert same_pattern(K1, Kf) and np.array_equal(K1.tocsc().data, Kf.tocsc().data)
+    fresh.close()
+    femm.close()
