@@ -185,30 +185,33 @@ def test_gather_triple_sum_error_bound(n):
 
 
 def _comp_cases():
+    """(element type, xyz, conn, oracle problem, thickness, parameters, layup
+    groups, element groups, rows per element)."""
     out = []
     for quads in (False, True):
         et, d, P, prm = _homog(quads)
-        out.append((et, d["xyz"], d["conn"], P, d["thickness"], prm, None, None))
+        out.append((et, d["xyz"], d["conn"], P, d["thickness"], prm, None, None, 36 if quads else 11))
         et, xyz, conn, P, prm, g = _composite(quads)
-        out.append((et, xyz, conn, P, 0.0, prm, [g], np.zeros(len(conn))))
+        out.append((et, xyz, conn, P, 0.0, prm, [g], np.zeros(len(conn)), 36 if quads else 11))
+    et, d, P, prm = _homog(False, tsf=1)  # T3 average K: 15 rows
+    out.append((et, d["xyz"], d["conn"], P, d["thickness"], prm, None, None, 15))
     return out
 
 
-@pytest.mark.parametrize("case", range(4), ids=["t3ff", "t3ffcomp", "q4rs", "q4rscomp"])
+@pytest.mark.parametrize("case", range(5), ids=["t3ff", "t3ffcomp", "q4rs", "q4rscomp", "t3ff_avgk"])
 def test_comp_element_matrices_within_the_sums_bounds(case):
     # every entry of the compensated element matrices against the exact Gram
     # of the same float rows: within the Dot2 bound (T3) or the three-level
     # bound (Q4) plus the final rounding to double (the layered T3 plate has
     # entries near 1e-34, where the underflow term is the one that counts);
     # and against the oracle's FP64 matrices within the float rows' own error
-    et, xyz, conn, P, th, prm, groups, eg = _comp_cases()[case]
+    et, xyz, conn, P, th, prm, groups, eg, nrows = _comp_cases()[case]
     args = (xyz, conn, P.normals, P.valid, th, prm)
     kw = dict(groups=groups, egroup=eg)
     Kc = HC.element_matrices(et, _abi.FS_MIXED_COMP, *args, **kw)
     Kx = HC.element_matrices(et, 3, *args, **kw)
     Ka = HC.element_matrices(et, 4, *args, **kw)
     quads = conn.shape[1] == 4
-    nrows = 36 if quads else 11
     g = _gamma(nrows + 1)
     coef = 2.1 * U * g if quads else g * g
     bound = coef * Ka + 2.0 ** -52 * np.abs(Kx) + 2 * nrows * ETA
