@@ -4,9 +4,11 @@ It serves callers that cannot let the library allocate device memory when
 they ask for a stiffness (their own pool allocator owns the GPU memory, or
 their solver loop runs under a fixed memory budget).  The test calls it
 through the C ABI, twice in a row, into a device buffer the caller owns, and
-checks the values against the regular fs_stiffness entry point with the
-tolerance of the other GPU tests.  This file is collected last so that a run
-stopping at the first failure has run every other test before it.
+checks the values against the regular fs_stiffness entry point bit for bit
+(both run the same element and gather kernels); a beam context and a mesh
+beyond the fixed array are rejected before any launch.  This file is
+collected last so that a run stopping at the first failure has run every
+other test before it.
 """
 import ctypes
 
