@@ -24,7 +24,9 @@ only to half the subnormal spacing eta = 2^-149 (the instructions keep
 subnormals, as IEEE arithmetic does on the host): an absolute 2 n eta is
 added to the dot-product bounds.
 Then the element matrices of the compensated path are checked against the
-exact Gram of the same float rows with the same bounds, entry by entry.
+exact Gram of the same float rows with the same bounds, entry by entry, and
+the thin layered plate's lowest eigenvalues are computed from them: the
+reason the compensated mode exists, reproduced on the host.
 """
 from fractions import Fraction
 
@@ -221,3 +223,38 @@ def test_comp_element_matrices_within_the_sums_bounds(case):
     assert max(_relmax(Kc[e], Kx[e]) for e in range(len(Kc))) <= 1e-12
     Ko = P.element_stiffness()
     assert _relmax(Kc, Ko) <= 1e-6
+
+
+def test_layered_plate_eigenvalues_need_the_compensated_sums():
+    # the layered plate ([0/90/90/0], t/L = 0.001) at 32 x 32 quads: element
+    # matrices from the kernels' own arithmetic on the host, assembled in
+    # double, and the 20 lowest eigenvalues with the oracle's lumped mass,
+    # against FP64.  Plain float Gram sums (FS_MIXED) miss the 1e-6 target by
+    # orders of magnitude (their rounding is not of the Gram form and acts as a
+    # spurious foundation under the bending modes; measured 2.0e-5 at 16 x 16,
+    # 2.5e-3 here); the compensated sums meet it (measured 9.2e-8)
+    import scipy.sparse as sp
+    import problems as PB
+    xyz, conn, dof, nfree, plies = PB.c4_plate(32)
+    A, B, D, H, md, mi = O.laminate(plies)
+    t = sum(p["thickness"] for p in plies)
+    P = O.Problem(O.Q4RSCOMP, xyz, conn, dof, stab_c=0.1,
+                  groups=[dict(A=A, B=B, D=D, H=H, csmat=np.eye(3), thickness=t, mass=md, moi=mi)])
+    P.compute_normals()
+    g = _abi.make_group(A, B, D, H, np.eye(3), t, md, mi)
+    prm = _abi.make_params(np.eye(3), np.eye(2), 0.0, t, stab_c=0.1, quads=True)
+    M = P.assemble_scipy("M", O.KEEP_ZEROS, n=nfree)
+    dd = np.stack([np.concatenate([dof[a - 1] for a in e]) - 1 for e in conn])
+    r, c = np.repeat(dd, 24, axis=1).ravel(), np.tile(dd, (1, 24)).ravel()
+    keep = (r < nfree) & (c < nfree)
+
+    def lowest(precision):
+        Ke = HC.element_matrices(O.Q4RSCOMP, precision, xyz, conn, P.normals, P.valid, 0.0, prm,
+                                 groups=[g], egroup=np.zeros(len(conn)))
+        K = sp.csc_matrix((Ke.ravel()[keep], (r[keep], c[keep])), shape=(nfree, nfree))
+        return PB.lowest_eigenvalues(K, M)
+
+    w64 = lowest(_abi.FS_FP64)
+    err = {p: np.max(np.abs(lowest(p) - w64) / np.abs(w64)) for p in (_abi.FS_MIXED, _abi.FS_MIXED_COMP)}
+    assert err[_abi.FS_MIXED_COMP] <= 1e-6, err
+    assert err[_abi.FS_MIXED] >= 1e-4, err
